@@ -1,0 +1,208 @@
+/*
+ * les_gb300.h -- C ABI of the GB300-native per-timestep spectral core of the
+ * KhaledGhannam/LES large-eddy-simulation code.
+ *
+ * Every entry point replaces one Fortran external subroutine of the reference
+ * (cited as file:line in the reference tree).  The Fortran arrays keep their
+ * shape and column-major layout:
+ *
+ *   real field     double[nz][ny][ld]      ld = nx+2          (ld,ny,nz)
+ *   complex plane  double[ny][lh][2]       lh = nx/2+1        (lh,ny) view
+ *   padded field   double[nz][ny2][ld_big] ny2 = 3ny/2, ld_big = 3nx/2+2
+ *   pressure       double[nz+1][ny][ld]    levels 0..nz-1 valid on exit
+ *   surface plane  double[ny][nx]          (nx,ny)
+ *
+ * nz is the Fortran array extent (number of uvp levels + 1).  All pointers
+ * passed to the per-routine entry points are HOST pointers unless the context
+ * was switched to device-pointer mode with les_ctx_set_pointer_mode().
+ *
+ * Return value: 0 (LES_OK) or a negative les_status.  The reference prints a
+ * message and calls `stop`; the Fortran shim turns a negative status into the
+ * same message plus `stop`.
+ *
+ * Threading: one context per ensemble member; a context is bound to one CUDA
+ * stream and is not thread-safe.  Different contexts may be driven from
+ * different host threads.
+ */
+#ifndef LES_GB300_H
+#define LES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum les_status {
+  LES_OK = 0,
+  LES_ERR_ARG = -1,         /* bad argument, shape or size                     */
+  LES_ERR_CUDA = -2,        /* CUDA runtime error (message: les_last_error)    */
+  LES_ERR_OOM = -3,         /* device allocation failed                        */
+  LES_ERR_PIVOT = -4,       /* zero pivot: tridag_array.f90:34-37,62-67 `stop` */
+  LES_ERR_CFL = -5,         /* CFLu > 0.1 or < 0: main.f90:455-458 `stop`      */
+  LES_ERR_NAN = -6,         /* non-finite value detected in the state          */
+  LES_ERR_TIMEOUT = -7,     /* bounded device wait expired                     */
+  LES_ERR_STATE = -8,       /* call made before the required set-up            */
+  LES_ERR_UNSUPPORTED = -9  /* size or mode not supported                      */
+} les_status;
+
+/* Run configuration.  Mirrors the compile-time parameters of param.f90 and
+ * the run-time namelist param_nml (param.f90:183-190), which the reference
+ * fixes at compile time; here they are per-context run-time values. */
+typedef struct les_config {
+  int nx, ny, nz;       /* param.f90:56   grid; nz = uvp levels + 1             */
+  int model;            /* param.f90:115  5 = Lagrangian scale-dependent,
+                                          3 = plane-averaged scale-dependent    */
+  int s_flag;           /* param.f90:158  1 = active potential temperature      */
+  int initu;            /* param.f90:79   0 = Euler first momentum step         */
+  int initsc;           /* param.f90:79   0 = Euler first scalar step           */
+  int cs_count;         /* param.f90:100  steps between dynamic Cs updates (5)  */
+  int jt_total0;        /* total_time.dat (param.f90:203-214) step offset        */
+  int precision;        /* 0 = FP64 throughout, 1 = FP32-mixed form             */
+  int rmsdiv_every;     /* main.f90:451   rmsdiv/CFL diagnostic period (500)    */
+  int reserved0;
+  double l_x, l_y;      /* param.f90:62   horizontal box (nondimensional)       */
+  double lz_over_zi;    /* param.f90:63   L_z / z_i                             */
+  double z_i;           /* param.f90:63   [m]                                   */
+  double u_star;        /* param.f90:69   [m/s]                                 */
+  double dt;            /* param.f90:219  nondimensional time step              */
+  double vonk;          /* param.f90:98   von Karman constant                   */
+  double t_scale;       /* param.f90:82   [K]                                   */
+  double dtdz_top;      /* param.f90:81   [K/m]                                 */
+  double pr;            /* param.f90:53   SGS Prandtl number                    */
+  double g;             /* param.f90:177  [m/s^2]                               */
+} les_config;
+
+/* State arrays that mirror the reference's module arrays (sim_param.f90:18-38,
+ * sgsmodule.f90:8-34, scalars_module.f90:31-36, bottombc.f90:9-16). */
+typedef enum les_field {
+  LES_U = 0, LES_V, LES_W, LES_THETA,
+  LES_DUDX, LES_DUDY, LES_DUDZ, LES_DVDX, LES_DVDY, LES_DVDZ,
+  LES_DWDX, LES_DWDY, LES_DWDZ,
+  LES_RHSX, LES_RHSY, LES_RHSZ, LES_RHSX_F, LES_RHSY_F, LES_RHSZ_F,
+  LES_DPDX, LES_DPDY, LES_DPDZ,
+  LES_TXX, LES_TXY, LES_TYY, LES_TXZ, LES_TYZ, LES_TZZ,
+  LES_DIVTX, LES_DIVTY, LES_DIVTZ,
+  LES_P,                 /* (ld,ny,0:nz) */
+  LES_F_LM, LES_F_MM, LES_F_QN, LES_F_NN, LES_BETA, LES_CS_OPT2, LES_NU_T,
+  LES_U_LAG, LES_V_LAG, LES_W_LAG,
+  LES_RHS_T, LES_RHS_TF, LES_BETA_SCAL, LES_DTDX, LES_DTDY, LES_DTDZ,
+  LES_S11, LES_S12, LES_S13, LES_S22, LES_S23, LES_S33,   /* calc_Sij output */
+  /* surface planes (nx,ny) */
+  LES_ZO, LES_WT_S, LES_USTAR_AVG, LES_PHI_M, LES_PSI_M, LES_PSI_M0,
+  LES_PHI_H, LES_PSI_H, LES_PSI_H0, LES_SGS_T3_SFC,
+  LES_NUM_FIELDS
+} les_field;
+
+typedef struct les_ctx les_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces init_fft / init_wavenumber (fft.f90:35-81) and the two
+ * test_filter_init calls of main.f90:166-170; allocates the device mirrors of
+ * the module arrays and all scratch.  Fields start at zero, as the reference's
+ * static module storage does. */
+int les_ctx_create(const les_config* cfg, les_ctx** out);
+int les_ctx_destroy(les_ctx* ctx);
+/* 0 = per-routine array arguments are host pointers (default), 1 = device. */
+int les_ctx_set_pointer_mode(les_ctx* ctx, int device_pointers);
+/* Stream the context launches on (a cudaStream_t, passed as void*). */
+void* les_ctx_stream(les_ctx* ctx);
+/* Bytes of device memory this context holds. */
+size_t les_ctx_device_bytes(const les_ctx* ctx);
+/* Estimated device bytes for a configuration (admission control). */
+size_t les_estimate_device_bytes(const les_config* cfg);
+const char* les_last_error(void);
+
+/* ---- state transfer ------------------------------------------------------ */
+/* bottombc.f90:23-59 (patches): zo = roughness / z_i (nondimensional), wt_s =
+ * kinematic surface heat flux [K m/s]; both (nx,ny). */
+int les_set_surface(les_ctx* ctx, const double* zo, const double* wt_s);
+/* Copy one module array host -> device / device -> host.  Real fields are
+ * (ld,ny,nz), LES_P is (ld,ny,nz+1), surface planes are (nx,ny). */
+int les_set_field(les_ctx* ctx, les_field f, const double* host);
+int les_get_field(les_ctx* ctx, les_field f, double* host);
+/* Device address of a module array (for zero-copy use by the caller). */
+double* les_field_device_ptr(les_ctx* ctx, les_field f);
+size_t les_field_elems(const les_ctx* ctx, les_field f);
+/* Bind Fortran module arrays once; les_sync_* then copy all bound arrays. */
+int les_register_field(les_ctx* ctx, les_field f, double* host);
+int les_sync_from_host(les_ctx* ctx);
+int les_sync_to_host(les_ctx* ctx);
+/* Step counters (param.f90:147-148). */
+int les_get_counters(les_ctx* ctx, int* jt, int* jt_total);
+
+/* ---- fused time step ------------------------------------------------------ */
+/* main.f90:202-478: nsteps iterations of the time loop on the device-resident
+ * state (obukhov, filt_da, ddz, wallstress, sgs_stag, theta_all_in_one,
+ * divstress, convec, AB2, press_stag_array, project, rmsdiv). */
+int les_step(les_ctx* ctx, int nsteps);
+/* rmsdiv.f90:1-113 on the start-of-step derivatives of the last step, and
+ * timestep_conditions (scalars_module2.f90:22-70): cfl[0]=CFLu, cfl[1]=visc. */
+int les_rmsdiv(les_ctx* ctx, double* rms);
+int les_timestep_conditions(les_ctx* ctx, double* cflu, double* visc_stab);
+
+/* ---- per-routine entry points (array arguments) --------------------------- */
+/* ddx.f90:1-31 / ddy.f90:1-31 : spectral derivative of nlev planes. */
+int les_ddx(les_ctx* ctx, double* dfdx, const double* f, int nlev);
+int les_ddy(les_ctx* ctx, double* dfdy, const double* f, int nlev);
+/* ddxy.f90:1-29 */
+int les_ddxy(les_ctx* ctx, double* dfdx, double* dfdy, const double* f, int nlev);
+/* filt_da.f90:3-42 : f <- Nyquist-filtered f, plus dfdx, dfdy. */
+int les_filt_da(les_ctx* ctx, double* f, double* dfdx, double* dfdy, int nlev);
+/* ddz_uv.f90:5-57, ddz_w.f90:6-51 (nz levels; untouched levels kept). */
+int les_ddz_uv(les_ctx* ctx, double* dfdz, const double* f);
+int les_ddz_w(les_ctx* ctx, double* dfdz, const double* f);
+/* padd.f90:1-26 / unpadd.f90:1-22 on nplanes complex planes. */
+int les_padd(les_ctx* ctx, double* u_big, const double* u, int nplanes);
+int les_unpadd(les_ctx* ctx, double* cc, const double* cc_big, int nplanes);
+/* dealias1.f90:1-31 / dealias2.f90:1-33 on nlev planes. */
+int les_dealias1(les_ctx* ctx, const double* u, double* u_big, int nlev);
+int les_dealias2(les_ctx* ctx, double* u, double* u_big, int nlev);
+/* test_filtermodule.f90:13-30 : in-place filter of nplanes (ld,ny) planes
+ * with transfer function G (lh,ny) that carries the 1/(nx*ny) normalisation. */
+int les_test_filter(les_ctx* ctx, double* f, const double* G, int nplanes);
+/* test_filtermodule.f90:32-63 : G for filter width alpha*delta. */
+int les_test_filter_init(les_ctx* ctx, double alpha, double* G);
+/* Plain unnormalised in-place 2-D real transforms of nplanes planes
+ * (rfftwnd_f77_one_real_to_complex / complex_to_real with the plans of
+ * fft.f90:40-47); big = 1 selects the 3/2-padded plan. */
+int les_fft_r2c(les_ctx* ctx, double* planes, int nplanes, int big);
+int les_fft_c2r(les_ctx* ctx, double* planes, int nplanes, int big);
+/* tridag_array.f90:1-109 : a,b,c (lh,ny,nz+1) real; r,u (lh,ny,nz+1) complex. */
+int les_tridag_array(les_ctx* ctx, const double* a, const double* b, const double* c,
+                     const double* r, double* u);
+/* Routines that read the module arrays bound to the context. */
+/* convec.f90:1-248 -> cx, cy, cz (ld,ny,nz), valid 1:nz-1. */
+int les_convec(les_ctx* ctx, double* cx, double* cy, double* cz);
+/* divstress_uv.f90:1-63 / divstress_w.f90:4-86 */
+int les_divstress_uv(les_ctx* ctx, double* divt, const double* tx, const double* ty,
+                     const double* tz);
+int les_divstress_w(les_ctx* ctx, double* divt, const double* tx, const double* ty,
+                    const double* tz);
+/* press_stag_array.f90:1-294 on the context's u,v,w (u*) and divtz:
+ * p_hat (ld,ny,0:nz) physical pressure, dfdx/dfdy (ld,ny,nz). */
+int les_press_stag_array(les_ctx* ctx, double* p_hat, double* dfdx, double* dfdy);
+/* sgs_stag.f90:3-364 on the context state (includes calc_Sij, the Lagrangian
+ * accumulation, the dynamic-model dispatch and the tau_ij assembly). */
+int les_sgs_stag(les_ctx* ctx);
+/* lagrange_Sdep.f90:4-478 (calls interpolag_Sdep) with S_ij (ld,ny,nz). */
+int les_lagrange_sdep(les_ctx* ctx, const double* S11, const double* S12, const double* S13,
+                      const double* S22, const double* S23, const double* S33);
+/* interpolag_Sdep.f90:2-380 on the context's F_* and u/v/w_lag. */
+int les_interpolag_sdep(les_ctx* ctx);
+/* scaledep_dynamic.f90:4-255 -> cs_opt2 (nz) with S_ij (ld,ny,nz). */
+int les_scaledep_dynamic(les_ctx* ctx, double* cs_opt2, const double* S11, const double* S12,
+                         const double* S13, const double* S22, const double* S23,
+                         const double* S33);
+/* wallstress.f90:5-69, scalars_module.f90:508-690 (obukhov),
+ * forcing.f90:128-219 (project), scalars_module.f90:57-171 (theta_all_in_one). */
+int les_wallstress(les_ctx* ctx);
+int les_obukhov(les_ctx* ctx);
+int les_project(les_ctx* ctx);
+int les_theta_all_in_one(les_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LES_GB300_H */
