@@ -1,0 +1,166 @@
+"""GB300-native per-timestep spectral core of the KhaledGhannam/LES code.
+
+The compute path is the CUDA library les_gb300/_lib/liblesgb300.so built for
+sm_103a (see build.py); this module is its ctypes binding.  The C ABI is
+declared in include/les_gb300.h and mirrors the reference's Fortran
+subroutine interfaces (ddx, filt_da, convec, press_stag_array, ...), with
+the reference's column-major array layouts.  There is no CPU fallback: if
+the library is missing or no GPU is present the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .config import (LesConfig, FIELDS, FIELD_ID, SURFACE_FIELDS, make_config, dims,
+                     field_shape, initial_state, uniform_surface, striped_surface,
+                     patch_surface, workload)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liblesgb300.so")
+
+STATUS = {0: "LES_OK", -1: "LES_ERR_ARG", -2: "LES_ERR_CUDA", -3: "LES_ERR_OOM",
+          -4: "LES_ERR_PIVOT", -5: "LES_ERR_CFL", -6: "LES_ERR_NAN", -7: "LES_ERR_TIMEOUT",
+          -8: "LES_ERR_STATE", -9: "LES_ERR_UNSUPPORTED"}
+
+
+class LesError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("les_gb300 CUDA library not built: run les_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p
+        L.les_last_error.restype = ctypes.c_char_p
+        L.les_ctx_create.argtypes = [ctypes.POINTER(LesConfig), ctypes.POINTER(vp)]
+        L.les_ctx_stream.restype = vp
+        L.les_ctx_stream.argtypes = [vp]
+        L.les_ctx_device_bytes.restype = ctypes.c_size_t
+        L.les_ctx_device_bytes.argtypes = [vp]
+        L.les_estimate_device_bytes.restype = ctypes.c_size_t
+        L.les_estimate_device_bytes.argtypes = [ctypes.POINTER(LesConfig)]
+        L.les_field_device_ptr.restype = vp
+        L.les_field_device_ptr.argtypes = [vp, ip]
+        L.les_field_elems.restype = ctypes.c_size_t
+        L.les_field_elems.argtypes = [vp, ip]
+        for name in ["les_ctx_destroy", "les_step", "les_set_field", "les_get_field",
+                     "les_set_surface", "les_rmsdiv", "les_ctx_set_pointer_mode"]:
+            getattr(L, name).restype = ip
+        L.les_ctx_destroy.argtypes = [vp]
+        L.les_step.argtypes = [vp, ip]
+        L.les_set_field.argtypes = [vp, ip, dp]
+        L.les_get_field.argtypes = [vp, ip, dp]
+        L.les_set_surface.argtypes = [vp, dp, dp]
+        L.les_rmsdiv.argtypes = [vp, dp]
+        L.les_ctx_set_pointer_mode.argtypes = [vp, ip]
+        _lib = L
+    return _lib
+
+
+def check(code):
+    if code != 0:
+        raise LesError(code, lib().les_last_error().decode(errors="replace"))
+    return code
+
+
+def _ptr(a):
+    if isinstance(a, np.ndarray):
+        assert a.dtype == np.float64 and a.flags.c_contiguous, "float64 C-contiguous array required"
+        return ctypes.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):  # torch tensor on the device
+        return ctypes.c_void_p(a.data_ptr())
+    return ctypes.c_void_p(int(a))
+
+
+class Context:
+    """One ensemble member: device-resident state plus the routines of the
+    reference's time step (main.f90:202-478)."""
+
+    def __init__(self, cfg, surface=None):
+        self.cfg = cfg
+        self.L = lib()
+        h = ctypes.c_void_p()
+        check(self.L.les_ctx_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.d = dims(cfg)
+        if surface is not None:
+            self.set_surface(surface)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.les_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- state --------------------------------------------------------------
+    def set_surface(self, s):
+        zo = np.ascontiguousarray(s.zo, dtype=np.float64)
+        wt = np.ascontiguousarray(s.wt_s, dtype=np.float64)
+        check(self.L.les_set_surface(self.h, _ptr(zo), _ptr(wt)))
+
+    def set(self, name, value):
+        a = np.ascontiguousarray(np.broadcast_to(value, field_shape(self.cfg, name)), dtype=np.float64)
+        check(self.L.les_set_field(self.h, FIELD_ID[name], _ptr(a)))
+
+    def get(self, name):
+        a = np.empty(field_shape(self.cfg, name), dtype=np.float64)
+        check(self.L.les_get_field(self.h, FIELD_ID[name], _ptr(a)))
+        return a
+
+    def device_ptr(self, name):
+        return self.L.les_field_device_ptr(self.h, FIELD_ID[name])
+
+    def stream(self):
+        return self.L.les_ctx_stream(self.h)
+
+    def device_bytes(self):
+        return self.L.les_ctx_device_bytes(self.h)
+
+    def counters(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        check(self.L.les_get_counters(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    # --- time stepping --------------------------------------------------------
+    def step(self, n=1):
+        check(self.L.les_step(self.h, int(n)))
+
+    def rmsdiv(self):
+        r = ctypes.c_double()
+        check(self.L.les_rmsdiv(self.h, ctypes.byref(r)))
+        return r.value
+
+    def timestep_conditions(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(self.L.les_timestep_conditions(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    # --- per-routine entry points (host arrays) --------------------------------
+    def call(self, name, *arrays, ints=(), doubles=()):
+        args = [self.h] + [_ptr(a) for a in arrays] + [ctypes.c_int(i) for i in ints] + \
+            [ctypes.c_double(x) for x in doubles]
+        fn = getattr(self.L, "les_" + name)
+        fn.restype = ctypes.c_int
+        return check(fn(*args))
+
+    def set_pointer_mode(self, device):
+        check(self.L.les_ctx_set_pointer_mode(self.h, 1 if device else 0))
+
+
+def estimate_device_bytes(cfg):
+    return lib().les_estimate_device_bytes(ctypes.byref(cfg))

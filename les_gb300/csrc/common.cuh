@@ -1,0 +1,55 @@
+// Shared device/host helpers for the GB300 LES core.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#define LES_PI 3.1415926535897932384626433   /* param.f90:51 */
+#define LES_BOGUS (-1234567890.0)              /* param.f90:50 */
+
+namespace les {
+
+// Complex type traits for the two arithmetic precisions.
+template <typename T> struct CT;
+template <> struct CT<double> { typedef double2 type; };
+template <> struct CT<float> { typedef float2 type; };
+
+template <typename T> __host__ __device__ __forceinline__ typename CT<T>::type mk(T a, T b) {
+  typename CT<T>::type r; r.x = a; r.y = b; return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { a.x *= s; a.y *= s; return a; }
+// i * a
+template <typename C> __device__ __forceinline__ C cmuli(C a) { C r; r.x = -a.y; r.y = a.x; return r; }
+// -i * a
+template <typename C> __device__ __forceinline__ C cmulmi(C a) { C r; r.x = a.y; r.y = -a.x; return r; }
+template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+
+// eye * k * f = (-k f.im, k f.re), the reference's spectral derivative
+// (ddx.f90:152, filt_da.f90:117-118).
+template <typename C, typename T> __device__ __forceinline__ C ik(C f, T k) {
+  C r; r.x = -(k * f.y); r.y = k * f.x; return r;
+}
+
+// FP32 truncation max(real(a), real(b)) of the reference's default-real MAX.
+__device__ __forceinline__ double fmax32(double a, double b) {
+  float fa = __double2float_rn(a), fb = __double2float_rn(b);
+  return (double)(fa > fb ? fa : fb);
+}
+
+}  // namespace les
+
+#define LES_CUDA_CHECK(expr)                                                           \
+  do {                                                                                 \
+    cudaError_t _e = (expr);                                                           \
+    if (_e != cudaSuccess) {                                                           \
+      les_set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(_e)); \
+      return LES_ERR_CUDA;                                                             \
+    }                                                                                  \
+  } while (0)
+
+void les_set_error(const char* fmt, ...);

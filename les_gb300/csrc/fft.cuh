@@ -1,0 +1,173 @@
+// Batched shared-memory Stockham FFTs for the horizontal planes of the LES
+// fields.  They replace FFTW 2's in-place 2-D real transforms
+// (rfftwnd_f77_one_real_to_complex / complex_to_real with the plans of
+// fft.f90:40-47): unnormalised, forward sign -1, x (the contiguous Fortran
+// dimension) is the halved real dimension, complex output (lh,ny) over an
+// (ld,ny) plane.  A 2-D transform is split into
+//   rows_r2c  : real x-FFT of every row (length nx through an nx/2 complex FFT)
+//   cols      : complex y-FFT of tiles of kx columns, with a spectral operator
+//               between the forward and inverse passes (derivatives, test
+//               filters, 3/2 zero padding / truncation, oddball removal)
+//   rows_c2r  : real inverse x-FFT of every row
+// so that one launch of each kernel processes every level of several fields.
+// Sizes are 2^a 3^b (radix 4, 2, 3 stages).
+#pragma once
+#include "common.cuh"
+
+namespace les {
+
+constexpr int FFT_MAX_STAGES = 12;
+
+struct FftPlanDev {
+  int n;
+  int nst;
+  int radix[FFT_MAX_STAGES];
+  int twoff[FFT_MAX_STAGES];
+  const double2* tw;  // forward twiddles, per stage (R-1)*Ns entries
+};
+
+struct RealPlanDev {
+  FftPlanDev c;       // complex FFT of length m = nx/2
+  int nx;
+  const double2* w;   // exp(-2 pi i k / nx), k = 0..m
+};
+
+// ---- radix butterflies -----------------------------------------------------
+template <typename C> __device__ __forceinline__ void dft2(C* v) {
+  C a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+template <typename C> __device__ __forceinline__ void dft4(C* v, int sign) {
+  C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  C t2 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+  C t3 = sign < 0 ? cmulmi(d) : cmuli(d);
+  v[0] = cadd(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[2] = csub(t0, t2);
+  v[3] = csub(t1, t3);
+}
+template <typename C, typename T> __device__ __forceinline__ void dft3(C* v, int sign) {
+  const T s3 = (T)0.86602540378443864676372317075294;
+  C a0 = v[0];
+  C sum = cadd(v[1], v[2]), dif = csub(v[1], v[2]);
+  C m = csub(a0, cscale(sum, (T)0.5));
+  const T ss = sign < 0 ? -s3 : s3;
+  C rot; rot.x = -ss * dif.y; rot.y = ss * dif.x;
+  v[0] = cadd(a0, sum);
+  v[1] = cadd(m, rot);
+  v[2] = csub(m, rot);
+}
+
+template <typename T> __device__ __forceinline__ typename CT<T>::type twid(const double2* tw, int idx, int sign) {
+  double2 w = __ldg(&tw[idx]);
+  return mk<T>((T)w.x, sign < 0 ? (T)w.y : (T)(-w.y));
+}
+
+// One Stockham pass over all batches.  Element (b, i) lives at
+//   COLS : x[i * nb + b]          (tiles of columns, b fastest)
+//   ROWS : x[b * bstride + i]     (rows, i fastest)
+template <typename T, bool COLS>
+__device__ __forceinline__ void fft_pass(const typename CT<T>::type* __restrict__ x,
+                                         typename CT<T>::type* __restrict__ y, int n, int nb,
+                                         int bstride, int R, int Ns, const double2* tw, int sign) {
+  typedef typename CT<T>::type C;
+  const int m = n / R;
+  const int total = m * nb;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int b, j;
+    if (COLS) { b = t % nb; j = t / nb; }
+    else { j = t % m; b = t / m; }
+    const int k = j % Ns;
+    C v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (r < R) v[r] = COLS ? x[(j + r * m) * nb + b] : x[b * bstride + j + r * m];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < 4; ++r)
+        if (r < R) v[r] = cmul(v[r], twid<T>(tw, (r - 1) * Ns + k, sign));
+    }
+    if (R == 4) dft4(v, sign);
+    else if (R == 2) dft2(v);
+    else dft3<C, T>(v, sign);
+    const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (r < R) {
+        if (COLS) y[(base + r * Ns) * nb + b] = v[r];
+        else y[b * bstride + base + r * Ns] = v[r];
+      }
+  }
+}
+
+// Full transform; returns the buffer holding the result (x or y).
+template <typename T, bool COLS>
+__device__ typename CT<T>::type* fft_smem(typename CT<T>::type* x, typename CT<T>::type* y, int nb,
+                                          int bstride, const FftPlanDev& P, int sign) {
+  int Ns = 1;
+  for (int s = 0; s < P.nst; ++s) {
+    const int R = P.radix[s];
+    fft_pass<T, COLS>(x, y, P.n, nb, bstride, R, Ns, P.tw + P.twoff[s], sign);
+    __syncthreads();
+    typename CT<T>::type* t = x; x = y; y = t;
+    Ns *= R;
+  }
+  return x;
+}
+
+// ---- job descriptors --------------------------------------------------------
+constexpr int JOB_MAXF = 24;
+
+// rows_r2c / rows_c2r: nfield fields x nlev planes.
+struct RowJob {
+  int nfield, nlev;
+  int ny;                 // rows per plane
+  int ld;                 // physical row stride (reals)
+  int wc;                 // work-buffer row stride (complex entries)
+  int ncols;              // complex columns stored (r2c) / read (c2r), <= nx/2+1
+  long pstride_phys;      // reals between consecutive planes of a physical field
+  long pstride_work;      // complex entries between consecutive work planes
+  const void* phys[JOB_MAXF];   // physical field base (plane 0)
+  void* work[JOB_MAXF];         // work buffer base (plane 0)
+  double scale[JOB_MAXF];       // r2c: multiply input by scale before the transform
+  double div[JOB_MAXF];         // r2c: when non-zero, input is (x / div) * scale
+};
+
+// Spectral coefficient codes for the column operator.
+enum ColCoef {
+  CC_NONE = 0,
+  CC_ONE = 1,     // copy
+  CC_G = 2,       // x G_test       (test_filtermodule.f90:247)
+  CC_GG = 3,      // x G_test_test
+  CC_IKX = 4,     // x i kx         (ddx.f90:152)
+  CC_IKY = 5,     // x i ky         (ddy.f90:183)
+  CC_KILL = 6     // copy with the Nyquist row/column zeroed (filt_da.f90:114-115)
+};
+enum ColMap { MAP_SAME = 0, MAP_PAD = 1, MAP_UNPAD = 2 };
+enum ColDir { DIR_FWD = 1, DIR_INV = 2, DIR_BOTH = 3 };
+
+constexpr int COL_MAXI = 4;
+constexpr int COL_MAXO = 6;
+
+struct ColJob {
+  int nin, nout, nlev;
+  int nf;                 // independent field sets (grid z); set f uses
+  long fs_in, fs_out;     // in[i] + f*fs_in and out[o] + f*fs_out
+  int ny_in, ny_out;      // transform lengths
+  int map, dir;
+  int ncols;              // kx columns processed
+  int ny_small;           // ny of the small grid (pad/unpad mapping)
+  int wc_in, wc_out;      // row strides (complex)
+  long ps_in, ps_out;     // plane strides (complex)
+  int coef[COL_MAXO][COL_MAXI];
+  const void* in[COL_MAXI];
+  void* out[COL_MAXO];
+  const double* kx;       // (lh,ny) wavenumber tables of the small grid
+  const double* ky;
+  const double* G;        // G_test (lh,ny)
+  const double* GG;       // G_test_test
+  int lh;                 // row stride of the (lh,ny) tables
+};
+
+}  // namespace les

@@ -1,0 +1,679 @@
+// C ABI of the GB300 LES core: context set-up, state transfer and the
+// per-routine entry points declared in include/les_gb300.h.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include "les_internal.h"
+
+static thread_local char g_err[512] = "";
+void les_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+namespace les {
+
+static bool is_2a3b(int n) {
+  if (n <= 0) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+// Stockham plan for a complex FFT of length n: radix 4, then 2, then 3.
+// Twiddles exp(-2 pi i k r / (Ns R)) are evaluated in long double.
+static int make_plan(les_ctx* c, int n, HostPlan& hp) {
+  FftPlanDev& P = hp.c;
+  P.n = n;
+  P.nst = 0;
+  int m = n;
+  while (m % 4 == 0) { P.radix[P.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { P.radix[P.nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { P.radix[P.nst++] = 3; m /= 3; }
+  if (m != 1 || P.nst > FFT_MAX_STAGES) { les_set_error("FFT size %d is not 2^a 3^b", n); return LES_ERR_UNSUPPORTED; }
+  std::vector<double2> tw;
+  int Ns = 1;
+  for (int s = 0; s < P.nst; ++s) {
+    const int R = P.radix[s];
+    P.twoff[s] = (int)tw.size();
+    for (int r = 1; r < R; ++r)
+      for (int k = 0; k < Ns; ++k) {
+        const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)((long long)k * r) /
+                                (long double)((long long)Ns * R);
+        tw.push_back(make_double2((double)cosl(ang), (double)sinl(ang)));
+      }
+    Ns *= R;
+  }
+  if (tw.empty()) tw.push_back(make_double2(1.0, 0.0));
+  LES_CUDA_CHECK(cudaMalloc(&hp.dev, tw.size() * sizeof(double2)));
+  c->allocs.push_back(hp.dev);
+  LES_CUDA_CHECK(cudaMemcpy(hp.dev, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  P.tw = hp.dev;
+  return 0;
+}
+static int make_real_plan(les_ctx* c, int nx, HostRealPlan& rp) {
+  HostPlan hp;
+  int st = make_plan(c, nx / 2, hp);
+  if (st) return st;
+  rp.r.c = hp.c;
+  rp.r.nx = nx;
+  const int m = nx / 2;
+  std::vector<double2> w(m + 1);
+  for (int k = 0; k <= m; ++k) {
+    const long double ang = -2.0L * 3.14159265358979323846264338327950288L * k / (long double)nx;
+    w[k] = make_double2((double)cosl(ang), (double)sinl(ang));
+  }
+  LES_CUDA_CHECK(cudaMalloc(&rp.dev, w.size() * sizeof(double2)));
+  c->allocs.push_back(rp.dev);
+  LES_CUDA_CHECK(cudaMemcpy(rp.dev, w.data(), w.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  rp.r.w = rp.dev;
+  return 0;
+}
+
+static int dalloc(les_ctx* c, void** p, size_t bytes) {
+  if (bytes == 0) bytes = 256;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    les_set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    return LES_ERR_OOM;
+  }
+  c->allocs.push_back(*p);
+  c->bytes += bytes;
+  LES_CUDA_CHECK(cudaMemset(*p, 0, bytes));
+  return 0;
+}
+
+static void grid_of(const les_config& k, Grid& g) {
+  g.nx = k.nx; g.ny = k.ny; g.nz = k.nz;
+  g.nx2 = 3 * g.nx / 2; g.ny2 = 3 * g.ny / 2;          // param.f90:59
+  g.lh = g.nx / 2 + 1; g.ld = 2 * g.lh;                 // param.f90:60
+  g.lh_big = g.nx2 / 2 + 1; g.ld_big = 2 * g.lh_big;
+  g.dz = (k.lz_over_zi * k.z_i) / k.z_i / (g.nz - 1);   // param.f90:64
+  g.dx = k.l_x / g.nx; g.dy = k.l_y / g.ny;            // param.f90:65
+  g.delta = 1.0 * std::pow(g.dx * g.dy, 1.0 / 2.0);     // sgs_stag.f90:43
+  g.nplane = (size_t)g.ld * g.ny;
+  g.nfield = g.nplane * g.nz;
+  g.nplane_big = (size_t)g.ld_big * g.ny2;
+  g.nfield_big = g.nplane_big * g.nz;
+  g.C = (size_t)g.ny * g.lh;
+  g.CB = (size_t)g.ny2 * (g.nx / 2);
+}
+
+struct Sizes {
+  size_t wsA, wsB, wsP, big, tmp, fields, surf, spare;
+  int lag_chunk, ntmp;
+};
+static Sizes sizes_of(const Grid& g) {
+  Sizes s{};
+  s.lag_chunk = std::min(32, g.nz);
+  const size_t nz = g.nz, C = g.C, CB = g.CB, ch = s.lag_chunk;
+  s.wsA = std::max({6 * nz * C, 21 * ch * C, 3 * nz * CB, (size_t)(g.nx2 / 2 + 1) * g.ny2 * 2}) * sizeof(double2);
+  s.wsB = std::max({9 * nz * C, 6 * nz * CB, 42 * ch * C, (size_t)(g.nx2 / 2 + 1) * g.ny2 * 2}) * sizeof(double2);
+  s.wsP = ((3 * (nz - 1) + 2 + (nz + 1)) * C) * sizeof(double2) + (nz + 1) * C * sizeof(double);
+  s.big = 9 * g.nfield_big * sizeof(double);
+  s.ntmp = (int)std::max<size_t>(63 * ch, 3 * nz + 2);
+  s.tmp = (size_t)s.ntmp * g.nplane * sizeof(double);
+  s.fields = 0;
+  for (int f = 0; f < LES_ZO; ++f) s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
+  s.surf = (size_t)(LES_NUM_FIELDS - LES_ZO + 1) * g.nx * g.ny * sizeof(double);
+  s.spare = 4 * g.nfield * sizeof(double);
+  return s;
+}
+
+static void wavenumbers(const les_config& k, const Grid& g, std::vector<double>& kx, std::vector<double>& ky,
+                        std::vector<double>& k2) {
+  // fft.f90:54-81
+  const int lh = g.lh, ny = g.ny;
+  kx.assign((size_t)lh * ny, 0.0); ky.assign((size_t)lh * ny, 0.0); k2.assign((size_t)lh * ny, 0.0);
+  for (int jy = 0; jy < ny; ++jy)
+    for (int jx = 0; jx < lh - 1; ++jx) kx[(size_t)jy * lh + jx] = (double)jx;
+  for (int jy = 0; jy < ny; ++jy) {
+    const int m = ((jy + ny / 2) % ny) - ny / 2;
+    for (int jx = 0; jx < lh; ++jx) ky[(size_t)jy * lh + jx] = (double)m;
+  }
+  for (int jy = 0; jy < ny; ++jy) { kx[(size_t)jy * lh + lh - 1] = 0.0; ky[(size_t)jy * lh + lh - 1] = 0.0; }
+  for (int jx = 0; jx < lh; ++jx) { kx[(size_t)(ny / 2) * lh + jx] = 0.0; ky[(size_t)(ny / 2) * lh + jx] = 0.0; }
+  const double fx = 2.0 * LES_PI / k.l_x, fy = 2.0 * LES_PI / k.l_y;
+  for (size_t i = 0; i < kx.size(); ++i) {
+    kx[i] = fx * kx[i];
+    ky[i] = fy * ky[i];
+    k2[i] = kx[i] * kx[i] + ky[i] * ky[i];
+  }
+}
+// test_filtermodule.f90:32-63 (ifilter = 1)
+static void filter_G(const Grid& g, const std::vector<double>& k2, double alpha, std::vector<double>& G) {
+  G.assign((size_t)g.lh * g.ny, 1.0 / (double)(g.nx * g.ny));
+  const double delta = alpha * std::sqrt(g.dx * g.dy);
+  const double q = LES_PI / delta;
+  const double kc2 = q * q;
+  for (size_t i = 0; i < G.size(); ++i)
+    if (k2[i] >= kc2) G[i] = 0.0;
+  for (int jy = 0; jy < g.ny; ++jy) G[(size_t)jy * g.lh + g.lh - 1] = 0.0;
+  for (int jx = 0; jx < g.lh; ++jx) G[(size_t)(g.ny / 2) * g.lh + jx] = 0.0;
+}
+
+static size_t felems(const les_ctx* c, int f) {
+  if (f >= LES_ZO) return (size_t)c->g.nx * c->g.ny;
+  if (f == LES_P) return c->g.nplane * (c->g.nz + 1);
+  return c->g.nfield;
+}
+
+}  // namespace les
+
+using namespace les;
+
+extern "C" {
+
+const char* les_last_error(void) { return g_err; }
+
+size_t les_estimate_device_bytes(const les_config* cfg) {
+  if (!cfg) return 0;
+  Grid g;
+  grid_of(*cfg, g);
+  Sizes s = sizes_of(g);
+  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + (1u << 20);
+}
+
+int les_ctx_create(const les_config* cfg, les_ctx** out) {
+  if (!cfg || !out) { les_set_error("null argument"); return LES_ERR_ARG; }
+  *out = nullptr;
+  const les_config& k = *cfg;
+  if (k.nx < 8 || k.ny < 8 || k.nz < 4 || k.nx % 4 || k.ny % 2 || !is_2a3b(k.nx) || !is_2a3b(k.ny)) {
+    les_set_error("unsupported grid %dx%dx%d: nx%%4 == 0, ny%%2 == 0, both 2^a 3^b, nz >= 4", k.nx, k.ny, k.nz);
+    return LES_ERR_ARG;
+  }
+  if (k.cs_count < 1 || k.dt <= 0.0 || k.z_i <= 0.0 || k.u_star <= 0.0 || k.lz_over_zi <= 0.0) {
+    les_set_error("invalid physical parameters");
+    return LES_ERR_ARG;
+  }
+  if (k.precision != 0 && k.precision != 1) { les_set_error("precision must be 0 or 1"); return LES_ERR_ARG; }
+  if (k.model != 5 && k.model != 3) { les_set_error("model must be 5 or 3"); return LES_ERR_UNSUPPORTED; }
+  les_ctx* c = new les_ctx();
+  c->cfg = k;
+  c->jt_total = k.jt_total0;
+  grid_of(k, c->g);
+  const Grid& g = c->g;
+  int st = 0;
+  auto fail = [&](int code) { les_ctx_destroy(c); return code; };
+  if (cudaGetDevice(&c->device) != cudaSuccess) { les_set_error("no CUDA device"); delete c; return LES_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    les_set_error("stream creation failed"); delete c; return LES_ERR_CUDA;
+  }
+  c->own_stream = true;
+  for (int f = 0; f < LES_NUM_FIELDS; ++f) {
+    c->fsize[f] = felems(c, f);
+    if ((st = dalloc(c, (void**)&c->f[f], c->fsize[f] * sizeof(double)))) return fail(st);
+  }
+  if ((st = dalloc(c, (void**)&c->z_os, (size_t)g.nx * g.ny * sizeof(double)))) return fail(st);
+  {  // phi_m = phi_h = 1 (set by obukhov before first use in any case)
+    std::vector<double> one((size_t)g.nx * g.ny, 1.0);
+    cudaMemcpy(c->f[LES_PHI_M], one.data(), one.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->f[LES_PHI_H], one.data(), one.size() * sizeof(double), cudaMemcpyHostToDevice);
+  }
+  std::vector<double> kx, ky, k2, G, GG;
+  wavenumbers(k, g, kx, ky, k2);
+  filter_G(g, k2, 2.0 * 1.0, G);   // main.f90:166 (filter_size = 1)
+  filter_G(g, k2, 4.0 * 1.0, GG);  // main.f90:169
+  const size_t tb = (size_t)g.lh * g.ny * sizeof(double);
+  if ((st = dalloc(c, (void**)&c->kx, tb)) || (st = dalloc(c, (void**)&c->ky, tb)) ||
+      (st = dalloc(c, (void**)&c->G, tb)) || (st = dalloc(c, (void**)&c->GG, tb)))
+    return fail(st);
+  cudaMemcpy(c->kx, kx.data(), tb, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->ky, ky.data(), tb, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->G, G.data(), tb, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->GG, GG.data(), tb, cudaMemcpyHostToDevice);
+  if ((st = make_real_plan(c, g.nx, c->rx)) || (st = make_real_plan(c, g.nx2, c->rxb)) ||
+      (st = make_plan(c, g.ny, c->cy)) || (st = make_plan(c, g.ny2, c->cyb)))
+    return fail(st);
+  Sizes s = sizes_of(g);
+  c->lag_chunk = s.lag_chunk;
+  c->ntmp = s.ntmp;
+  c->nbig = 9;
+  if ((st = dalloc(c, &c->wsA, s.wsA)) || (st = dalloc(c, &c->wsB, s.wsB)) || (st = dalloc(c, &c->wsP, s.wsP)) ||
+      (st = dalloc(c, (void**)&c->big, s.big)) || (st = dalloc(c, (void**)&c->tmp, s.tmp)) ||
+      (st = dalloc(c, (void**)&c->spare, s.spare)) || (st = dalloc(c, (void**)&c->dscal, 64 * sizeof(double))) ||
+      (st = dalloc(c, (void**)&c->dred, 16 * (size_t)(g.nz + 8) * sizeof(double))))
+    return fail(st);
+  c->wsA_bytes = s.wsA; c->wsB_bytes = s.wsB; c->wsP_bytes = s.wsP;
+  if (cudaMallocHost(&c->host_scal, 64 * sizeof(double)) != cudaSuccess) { les_set_error("pinned alloc failed"); return fail(LES_ERR_OOM); }
+  if (cudaDeviceSynchronize() != cudaSuccess) { les_set_error("%s", cudaGetErrorString(cudaGetLastError())); return fail(LES_ERR_CUDA); }
+  *out = c;
+  return LES_OK;
+}
+
+int les_ctx_destroy(les_ctx* c) {
+  if (!c) return LES_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->host_scal) cudaFreeHost(c->host_scal);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return LES_OK;
+}
+
+int les_ctx_set_pointer_mode(les_ctx* c, int device_pointers) {
+  if (!c) return LES_ERR_ARG;
+  c->ptr_mode = device_pointers ? 1 : 0;
+  return LES_OK;
+}
+void* les_ctx_stream(les_ctx* c) { return c ? (void*)c->stream : nullptr; }
+size_t les_ctx_device_bytes(const les_ctx* c) { return c ? c->bytes : 0; }
+
+int les_set_surface(les_ctx* c, const double* zo, const double* wt_s) {
+  if (!c || !zo || !wt_s) return LES_ERR_ARG;
+  const size_t n = (size_t)c->g.nx * c->g.ny;
+  std::vector<double> zos(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (!(zo[i] > 0.0)) { les_set_error("zo must be positive"); return LES_ERR_ARG; }
+    zos[i] = zo[i] / 7.39;  // bottombc.f90:274 with zom/z_i = zo
+  }
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->f[LES_ZO], zo, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->f[LES_WT_S], wt_s, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->z_os, zos.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  c->surface_set = true;
+  return LES_OK;
+}
+
+int les_set_field(les_ctx* c, les_field f, const double* host) {
+  if (!c || !host || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], host, c->fsize[f] * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  return LES_OK;
+}
+int les_get_field(les_ctx* c, les_field f, double* host) {
+  if (!c || !host || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
+  LES_CUDA_CHECK(cudaMemcpyAsync(host, c->f[f], c->fsize[f] * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  return LES_OK;
+}
+double* les_field_device_ptr(les_ctx* c, les_field f) {
+  if (!c || f < 0 || f >= LES_NUM_FIELDS) return nullptr;
+  return c->f[f];
+}
+size_t les_field_elems(const les_ctx* c, les_field f) {
+  if (!c || f < 0 || f >= LES_NUM_FIELDS) return 0;
+  return c->fsize[f];
+}
+int les_register_field(les_ctx* c, les_field f, double* host) {
+  if (!c || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
+  c->reg[f] = host;
+  return LES_OK;
+}
+int les_sync_from_host(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  for (int f = 0; f < LES_NUM_FIELDS; ++f)
+    if (c->reg[f]) LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], c->reg[f], c->fsize[f] * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  return LES_OK;
+}
+int les_sync_to_host(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  for (int f = 0; f < LES_NUM_FIELDS; ++f)
+    if (c->reg[f]) LES_CUDA_CHECK(cudaMemcpyAsync(c->reg[f], c->f[f], c->fsize[f] * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  return LES_OK;
+}
+int les_get_counters(les_ctx* c, int* jt, int* jt_total) {
+  if (!c) return LES_ERR_ARG;
+  if (jt) *jt = c->jt;
+  if (jt_total) *jt_total = c->jt_total;
+  return LES_OK;
+}
+
+int les_step(les_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return LES_ERR_ARG;
+  if (!c->surface_set) { les_set_error("les_set_surface must be called before les_step"); return LES_ERR_STATE; }
+  for (int i = 0; i < nsteps; ++i) {
+    int st = step_fp64(c);
+    if (st) return st;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { les_set_error("%s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
+  return LES_OK;
+}
+
+int les_rmsdiv(les_ctx* c, double* rms) {
+  if (!c || !rms) return LES_ERR_ARG;
+  op_rmsdiv(c, c->dscal + 1);
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 1, c->dscal + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  *rms = c->host_scal[1];
+  return LES_OK;
+}
+int les_timestep_conditions(les_ctx* c, double* cflu, double* visc) {
+  if (!c || !cflu || !visc) return LES_ERR_ARG;
+  return op_tsc(c, cflu, visc);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// per-routine entry points: host or device array arguments
+namespace {
+struct Arg {
+  les_ctx* c;
+  const void* user;
+  double* dev = nullptr;
+  size_t n;
+  bool owned = false;
+  Arg(les_ctx* c_, const void* u, size_t n_) : c(c_), user(u), n(n_) {}
+  int in() {
+    if (c->ptr_mode) { dev = (double*)user; return 0; }
+    if (cudaMalloc(&dev, n * sizeof(double)) != cudaSuccess) { les_set_error("staging alloc failed"); return LES_ERR_OOM; }
+    owned = true;
+    if (cudaMemcpyAsync(dev, user, n * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) return LES_ERR_CUDA;
+    return 0;
+  }
+  int alloc() {
+    if (c->ptr_mode) { dev = (double*)user; return 0; }
+    if (cudaMalloc(&dev, n * sizeof(double)) != cudaSuccess) { les_set_error("staging alloc failed"); return LES_ERR_OOM; }
+    owned = true;
+    cudaMemsetAsync(dev, 0, n * sizeof(double), c->stream);
+    return 0;
+  }
+  int out() {
+    if (c->ptr_mode) return 0;
+    if (cudaMemcpyAsync((void*)user, dev, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return LES_ERR_CUDA;
+    return 0;
+  }
+  ~Arg() {
+    if (owned) { cudaStreamSynchronize(c->stream); cudaFree(dev); }
+  }
+};
+int finish(les_ctx* c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) { les_set_error("%s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
+  return LES_OK;
+}
+}  // namespace
+
+#define CHK(x) do { int _s = (x); if (_s) return _s; } while (0)
+
+extern "C" {
+
+int les_ddx(les_ctx* c, double* dfdx, const double* f, int nlev) {
+  if (!c || !dfdx || !f || nlev < 1 || nlev > c->g.nz + 1) return LES_ERR_ARG;
+  const size_t n = c->g.nplane * nlev;
+  Arg A(c, f, n), B(c, dfdx, n);
+  CHK(A.in()); CHK(B.alloc());
+  op_ddxy(c, B.dev, nullptr, A.dev, nlev);
+  CHK(B.out());
+  return finish(c);
+}
+int les_ddy(les_ctx* c, double* dfdy, const double* f, int nlev) {
+  if (!c || !dfdy || !f || nlev < 1 || nlev > c->g.nz + 1) return LES_ERR_ARG;
+  const size_t n = c->g.nplane * nlev;
+  Arg A(c, f, n), B(c, dfdy, n);
+  CHK(A.in()); CHK(B.alloc());
+  op_ddxy(c, nullptr, B.dev, A.dev, nlev);
+  CHK(B.out());
+  return finish(c);
+}
+int les_ddxy(les_ctx* c, double* dfdx, double* dfdy, const double* f, int nlev) {
+  if (!c || !dfdx || !dfdy || !f || nlev < 1 || nlev > c->g.nz + 1) return LES_ERR_ARG;
+  const size_t n = c->g.nplane * nlev;
+  Arg A(c, f, n), B(c, dfdx, n), D(c, dfdy, n);
+  CHK(A.in()); CHK(B.alloc()); CHK(D.alloc());
+  op_ddxy(c, B.dev, D.dev, A.dev, nlev);
+  CHK(B.out()); CHK(D.out());
+  return finish(c);
+}
+int les_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev) {
+  if (!c || !f || !dfdx || !dfdy || nlev < 1 || nlev > c->g.nz + 1) return LES_ERR_ARG;
+  const size_t n = c->g.nplane * nlev;
+  Arg A(c, f, n), B(c, dfdx, n), D(c, dfdy, n);
+  CHK(A.in()); CHK(B.alloc()); CHK(D.alloc());
+  op_filt_da(c, A.dev, B.dev, D.dev, nlev);
+  CHK(A.out()); CHK(B.out()); CHK(D.out());
+  return finish(c);
+}
+int les_ddz_uv(les_ctx* c, double* dfdz, const double* f) {
+  if (!c || !dfdz || !f) return LES_ERR_ARG;
+  Arg A(c, f, c->g.nfield), B(c, dfdz, c->g.nfield);
+  CHK(A.in()); CHK(B.in());
+  op_ddz(c, B.dev, A.dev, 1);
+  CHK(B.out());
+  return finish(c);
+}
+int les_ddz_w(les_ctx* c, double* dfdz, const double* f) {
+  if (!c || !dfdz || !f) return LES_ERR_ARG;
+  Arg A(c, f, c->g.nfield), B(c, dfdz, c->g.nfield);
+  CHK(A.in()); CHK(B.in());
+  op_ddz(c, B.dev, A.dev, 0);
+  CHK(B.out());
+  return finish(c);
+}
+int les_dealias1(les_ctx* c, const double* u, double* u_big, int nlev) {
+  if (!c || !u || !u_big || nlev < 1 || nlev > c->g.nz) return LES_ERR_ARG;
+  Arg A(c, u, c->g.nplane * nlev), B(c, u_big, c->g.nplane_big * nlev);
+  CHK(A.in()); CHK(B.alloc());
+  const double* in[1] = {A.dev};
+  double* out[1] = {B.dev};
+  op_dealias1(c, in, out, 1, nlev);
+  CHK(B.out());
+  return finish(c);
+}
+int les_dealias2(les_ctx* c, double* u, double* u_big, int nlev) {
+  if (!c || !u || !u_big || nlev < 1 || nlev > c->g.nz) return LES_ERR_ARG;
+  Arg A(c, u, c->g.nplane * nlev), B(c, u_big, c->g.nplane_big * nlev);
+  CHK(A.alloc()); CHK(B.in());
+  const double* in[1] = {B.dev};
+  double* out[1] = {A.dev};
+  op_dealias2(c, out, in, 1, nlev, 1.0 / (double)(c->g.nx2 * c->g.ny2));
+  CHK(A.out());
+  return finish(c);
+}
+int les_fft_r2c(les_ctx* c, double* planes, int nplanes, int big) {
+  if (!c || !planes || nplanes < 1) return LES_ERR_ARG;
+  const size_t np = big ? c->g.nplane_big : c->g.nplane;
+  const size_t per = (big ? (size_t)c->g.lh_big * c->g.ny2 : c->g.C) * sizeof(double2);
+  const int chunk = (int)std::max<size_t>(1, std::min(c->wsA_bytes, c->wsB_bytes) / per);
+  Arg A(c, planes, np * nplanes);
+  CHK(A.in());
+  for (int p0 = 0; p0 < nplanes; p0 += chunk) op_fft(c, A.dev + (size_t)p0 * np, std::min(chunk, nplanes - p0), big, 0);
+  CHK(A.out());
+  return finish(c);
+}
+int les_fft_c2r(les_ctx* c, double* planes, int nplanes, int big) {
+  if (!c || !planes || nplanes < 1) return LES_ERR_ARG;
+  const size_t np = big ? c->g.nplane_big : c->g.nplane;
+  const size_t per = (big ? (size_t)c->g.lh_big * c->g.ny2 : c->g.C) * sizeof(double2);
+  const int chunk = (int)std::max<size_t>(1, std::min(c->wsA_bytes, c->wsB_bytes) / per);
+  Arg A(c, planes, np * nplanes);
+  CHK(A.in());
+  for (int p0 = 0; p0 < nplanes; p0 += chunk) op_fft(c, A.dev + (size_t)p0 * np, std::min(chunk, nplanes - p0), big, 1);
+  CHK(A.out());
+  return finish(c);
+}
+int les_tridag_array(les_ctx* c, const double* a, const double* b, const double* cc, const double* r, double* u) {
+  if (!c || !a || !b || !cc || !r || !u) return LES_ERR_ARG;
+  const size_t nk = (size_t)c->g.lh * c->g.ny * (c->g.nz + 1);
+  Arg A(c, a, nk), B(c, b, nk), Cc(c, cc, nk), R(c, r, 2 * nk), U(c, u, 2 * nk);
+  CHK(A.in()); CHK(B.in()); CHK(Cc.in()); CHK(R.in()); CHK(U.in());
+  int* flag = reinterpret_cast<int*>(c->dscal + 8);
+  cudaMemsetAsync(flag, 0, sizeof(int), c->stream);
+  // zero-pivot check on row 1 (tridag_array.f90:32-39)
+  std::vector<double> b1((size_t)c->g.lh * c->g.ny);
+  if (c->ptr_mode) cudaMemcpy(b1.data(), b, b1.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  else std::memcpy(b1.data(), b, b1.size() * sizeof(double));
+  for (int jy = 0; jy < c->g.ny; ++jy)
+    for (int jx = 0; jx < c->g.lh - 1; ++jx)
+      if (b1[(size_t)jy * c->g.lh + jx] == 0.0) { les_set_error("tridag_array: rewrite eqs, jx, jy= %d %d", jx + 1, jy + 1); return LES_ERR_PIVOT; }
+  op_tridag(c, A.dev, B.dev, Cc.dev, R.dev, U.dev);
+  CHK(U.out());
+  int st = finish(c);
+  if (st) return st;
+  int fl = 0;
+  cudaMemcpy(&fl, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  if (fl) { les_set_error("tridag_array failed: zero pivot"); return LES_ERR_PIVOT; }
+  return LES_OK;
+}
+int les_convec(les_ctx* c, double* cx, double* cy, double* cz) {
+  if (!c || !cx || !cy || !cz) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg X(c, cx, n), Y(c, cy, n), Z(c, cz, n);
+  CHK(X.alloc()); CHK(Y.alloc()); CHK(Z.alloc());
+  op_convec(c, X.dev, Y.dev, Z.dev);
+  CHK(X.out()); CHK(Y.out()); CHK(Z.out());
+  return finish(c);
+}
+int les_divstress_uv(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz) {
+  if (!c || !divt || !tx || !ty || !tz) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg D(c, divt, n), X(c, tx, n), Y(c, ty, n), Z(c, tz, n);
+  CHK(D.alloc()); CHK(X.in()); CHK(Y.in()); CHK(Z.in());
+  op_divstress_one(c, D.dev, X.dev, Y.dev, Z.dev, 0);
+  CHK(D.out());
+  return finish(c);
+}
+int les_divstress_w(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz) {
+  if (!c || !divt || !tx || !ty || !tz) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg D(c, divt, n), X(c, tx, n), Y(c, ty, n), Z(c, tz, n);
+  CHK(D.alloc()); CHK(X.in()); CHK(Y.in()); CHK(Z.in());
+  op_divstress_one(c, D.dev, X.dev, Y.dev, Z.dev, 1);
+  CHK(D.out());
+  return finish(c);
+}
+int les_press_stag_array(les_ctx* c, double* p_hat, double* dfdx, double* dfdy) {
+  if (!c || !p_hat || !dfdx || !dfdy) return LES_ERR_ARG;
+  Arg P(c, p_hat, c->g.nplane * (c->g.nz + 1)), X(c, dfdx, c->g.nfield), Y(c, dfdy, c->g.nfield);
+  CHK(P.alloc()); CHK(X.alloc()); CHK(Y.alloc());
+  int* flag = reinterpret_cast<int*>(c->dscal + 8);
+  cudaMemsetAsync(flag, 0, sizeof(int), c->stream);
+  op_press(c, P.dev, X.dev, Y.dev);
+  CHK(P.out()); CHK(X.out()); CHK(Y.out());
+  int st = finish(c);
+  if (st) return st;
+  int fl = 0;
+  cudaMemcpy(&fl, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  if (fl) { les_set_error("tridag_array failed: zero pivot"); return LES_ERR_PIVOT; }
+  return LES_OK;
+}
+int les_sgs_stag(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  op_sgs_stag(c);
+  return finish(c);
+}
+int les_lagrange_sdep(les_ctx* c, const double* S11, const double* S12, const double* S13, const double* S22,
+                      const double* S23, const double* S33) {
+  if (!c || !S11 || !S12 || !S13 || !S22 || !S23 || !S33) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg a(c, S11, n), b(c, S12, n), d(c, S13, n), e(c, S22, n), f(c, S23, n), h(c, S33, n);
+  CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in());
+  const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
+  op_lagrange(c, S);
+  return finish(c);
+}
+int les_interpolag_sdep(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  op_interpolag(c);
+  return finish(c);
+}
+int les_scaledep_dynamic(les_ctx* c, double* cs_opt2, const double* S11, const double* S12, const double* S13,
+                         const double* S22, const double* S23, const double* S33) {
+  if (!c || !cs_opt2 || !S11 || !S12 || !S13 || !S22 || !S23 || !S33) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg a(c, S11, n), b(c, S12, n), d(c, S13, n), e(c, S22, n), f(c, S23, n), h(c, S33, n), o(c, cs_opt2, c->g.nz);
+  CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in()); CHK(o.alloc());
+  const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
+  op_scaledep(c, o.dev, S);
+  CHK(o.out());
+  return finish(c);
+}
+int les_wallstress(les_ctx* c) { if (!c) return LES_ERR_ARG; op_wallstress(c); return finish(c); }
+int les_obukhov(les_ctx* c) { if (!c) return LES_ERR_ARG; op_obukhov(c); return finish(c); }
+int les_project(les_ctx* c) { if (!c) return LES_ERR_ARG; op_project(c); return finish(c); }
+int les_theta_all_in_one(les_ctx* c) { if (!c) return LES_ERR_ARG; op_theta(c); return finish(c); }
+
+int les_test_filter(les_ctx* c, double* f, const double* G, int nplanes) {
+  if (!c || !f || !G || nplanes < 1) return LES_ERR_ARG;
+  // the transfer function must be one of the context's two filters
+  const size_t nk = (size_t)c->g.lh * c->g.ny;
+  std::vector<double> hg(nk), t0(nk), t1(nk);
+  if (c->ptr_mode) cudaMemcpy(hg.data(), G, nk * sizeof(double), cudaMemcpyDeviceToHost);
+  else std::memcpy(hg.data(), G, nk * sizeof(double));
+  cudaMemcpy(t0.data(), c->G, nk * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaMemcpy(t1.data(), c->GG, nk * sizeof(double), cudaMemcpyDeviceToHost);
+  int which = -1;
+  if (std::memcmp(hg.data(), t0.data(), nk * sizeof(double)) == 0) which = 0;
+  else if (std::memcmp(hg.data(), t1.data(), nk * sizeof(double)) == 0) which = 1;
+  if (which < 0) { les_set_error("les_test_filter: G must be G_test or G_test_test of this context"); return LES_ERR_UNSUPPORTED; }
+  Arg A(c, f, c->g.nplane * nplanes);
+  CHK(A.in());
+  op_test_filter(c, A.dev, A.dev, nplanes, which, (long)c->g.nplane);
+  CHK(A.out());
+  return finish(c);
+}
+int les_test_filter_init(les_ctx* c, double alpha, double* G) {
+  if (!c || !G || !(alpha > 0.0)) return LES_ERR_ARG;
+  std::vector<double> kx, ky, k2, g;
+  wavenumbers(c->cfg, c->g, kx, ky, k2);
+  filter_G(c->g, k2, alpha, g);
+  if (c->ptr_mode) LES_CUDA_CHECK(cudaMemcpy(G, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice));
+  else std::memcpy(G, g.data(), g.size() * sizeof(double));
+  return LES_OK;
+}
+
+// padd.f90 / unpadd.f90 on complex planes
+}  // extern "C"
+
+namespace les {
+__global__ void k_padd(double2* ub, const double2* us, int lh, int ny, int lhb, int ny2, int nx, int np) {
+  const size_t tot = (size_t)lhb * ny2 * np;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i / ((size_t)lhb * ny2));
+    const size_t r = i - (size_t)p * lhb * ny2;
+    const int jy = (int)(r / lhb), jx = (int)(r % lhb);
+    double2 v = make_double2(0.0, 0.0);
+    if (jx < nx / 2) {
+      int js = -1;
+      if (jy < ny / 2) js = jy;
+      else if (jy > ny2 - ny / 2) js = jy - (ny2 - ny);
+      if (js >= 0) v = us[(size_t)p * lh * ny + (size_t)js * lh + jx];
+    }
+    ub[i] = v;
+  }
+}
+__global__ void k_unpadd(double2* cc, const double2* cb, int lh, int ny, int lhb, int ny2, int nx, int np) {
+  const size_t tot = (size_t)lh * ny * np;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i / ((size_t)lh * ny));
+    const size_t r = i - (size_t)p * lh * ny;
+    const int jy = (int)(r / lh), jx = (int)(r % lh);
+    double2 v = make_double2(0.0, 0.0);
+    if (jx < nx / 2 && jy != ny / 2) {
+      const int jb = (jy < ny / 2) ? jy : jy + (ny2 - ny);
+      v = cb[(size_t)p * lhb * ny2 + (size_t)jb * lhb + jx];
+    }
+    cc[i] = v;
+  }
+}
+}  // namespace les
+
+extern "C" {
+int les_padd(les_ctx* c, double* u_big, const double* u, int nplanes) {
+  if (!c || !u_big || !u || nplanes < 1) return LES_ERR_ARG;
+  const Grid& g = c->g;
+  Arg B(c, u_big, g.nplane_big * nplanes), S(c, u, g.nplane * nplanes);
+  CHK(B.alloc()); CHK(S.in());
+  k_padd<<<256, 256, 0, c->stream>>>((double2*)B.dev, (const double2*)S.dev, g.lh, g.ny, g.lh_big, g.ny2, g.nx, nplanes);
+  CHK(B.out());
+  return finish(c);
+}
+int les_unpadd(les_ctx* c, double* cc, const double* cc_big, int nplanes) {
+  if (!c || !cc || !cc_big || nplanes < 1) return LES_ERR_ARG;
+  const Grid& g = c->g;
+  Arg S(c, cc, g.nplane * nplanes), B(c, cc_big, g.nplane_big * nplanes);
+  CHK(S.alloc()); CHK(B.in());
+  k_unpadd<<<256, 256, 0, c->stream>>>((double2*)S.dev, (const double2*)B.dev, g.lh, g.ny, g.lh_big, g.ny2, g.nx, nplanes);
+  CHK(S.out());
+  return finish(c);
+}
+}  // extern "C"

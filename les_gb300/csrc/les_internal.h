@@ -1,0 +1,103 @@
+// Internal context of the GB300 LES core (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <vector>
+#include <string>
+#include "../../include/les_gb300.h"
+#include "fft.cuh"
+
+namespace les {
+
+template <typename T, typename TIn>
+int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s);
+template <typename T, typename TOut>
+int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s);
+template <typename T>
+int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s);
+
+// Host-side FFT plan: owns the device twiddle table.
+struct HostPlan {
+  FftPlanDev c{};
+  double2* dev = nullptr;
+};
+struct HostRealPlan {
+  RealPlanDev r{};
+  double2* dev = nullptr;
+};
+
+// Grid constants computed once on the host in the reference's expression
+// order (param.f90:56-65, fft.f90:54-81, test_filtermodule.f90:32-63).
+struct Grid {
+  int nx, ny, nz, ld, lh, nx2, ny2, ld_big, lh_big;
+  double dx, dy, dz, delta;
+  size_t nplane, nfield, nplane_big, nfield_big;
+  size_t C, CB;  // complex entries of a small x-spectrum plane (ny*lh) and a
+                 // big truncated one (ny2*(nx/2))
+};
+
+}  // namespace les
+
+struct les_ctx {
+  les_config cfg;
+  les::Grid g;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int device = 0;
+  int ptr_mode = 0;  // 0 host pointers, 1 device pointers
+  int jt = 0, jt_total = 0;
+  bool surface_set = false;
+
+  // module arrays (device), indexed by les_field
+  double* f[LES_NUM_FIELDS] = {};
+  size_t fsize[LES_NUM_FIELDS] = {};
+  double* reg[LES_NUM_FIELDS] = {};  // registered host arrays
+
+  // derived surface plane
+  double* z_os = nullptr;
+  // spectral tables (lh,ny)
+  double *kx = nullptr, *ky = nullptr, *G = nullptr, *GG = nullptr;
+  // FFT plans
+  les::HostRealPlan rx, rxb;   // real x-transforms of length nx, nx2
+  les::HostPlan cy, cyb;       // complex y-transforms of length ny, ny2
+  // scratch
+  void* wsA = nullptr;  size_t wsA_bytes = 0;
+  void* wsB = nullptr;  size_t wsB_bytes = 0;
+  void* wsP = nullptr;  size_t wsP_bytes = 0;  // pressure spectra + gam
+  double* big = nullptr;  int nbig = 0;        // big physical fields
+  double* tmp = nullptr;  int ntmp = 0;        // small physical temp planes
+  double* spare = nullptr;                     // 4 fields (interpolated F_*)
+  int lag_chunk = 32;
+  double* dscal = nullptr;                     // device scalars / reductions
+  double* dred = nullptr;                      // per-level reduction results
+  double* host_scal = nullptr;                 // pinned host mirror
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  double rmsdiv_last = 0.0;
+  int status_flags = 0;
+};
+
+namespace les {
+int step_fp64(les_ctx* c);
+int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev);
+int op_ddxy(les_ctx* c, double* dfdx, double* dfdy, const double* f, int nlev);
+int op_test_filter(les_ctx* c, double* out, const double* in, int nplanes, int which, long pstride);
+int op_dealias1(les_ctx* c, const double* const* in, double* const* out, int nf, int nlev);
+int op_dealias2(les_ctx* c, double* const* out, const double* const* in, int nf, int nlev, double scale);
+int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse);
+int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, const double* r, double* u);
+int op_obukhov(les_ctx* c);
+int op_wallstress(les_ctx* c);
+int op_sgs_stag(les_ctx* c);
+int op_lagrange(les_ctx* c, const double* const* S);
+int op_interpolag(les_ctx* c);
+int op_scaledep(les_ctx* c, double* cs_z_dev, const double* const* S);
+int op_theta(les_ctx* c);
+int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz);
+int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz, int w_variant);
+int op_convec(les_ctx* c, double* cx, double* cy, double* cz);
+int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy);
+int op_project(les_ctx* c);
+int op_rmsdiv(les_ctx* c, double* out);
+int op_tsc(les_ctx* c, double* cflu, double* visc);
+int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv);
+}  // namespace les

@@ -1,0 +1,1622 @@
+// Per-routine device operations and the fused FP64 time step.
+// Every kernel cites the reference routine it restates (file:line).
+#include <algorithm>
+#include <cmath>
+#include "les_internal.h"
+
+namespace les {
+
+typedef double2 C2;
+struct Ptr6 { const double* p[6]; };
+
+// ---------------------------------------------------------------------------
+// launch helpers
+static inline dim3 grid1(size_t n, int bs = 256) {
+  size_t b = (n + bs - 1) / bs;
+  if (b > 152 * 64) b = 152 * 64;
+  if (b == 0) b = 1;
+  return dim3((unsigned)b);
+}
+#define GSTRIDE(i, n) for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (n); i += (size_t)gridDim.x * blockDim.x)
+
+__global__ void k_fill(double* p, size_t n, double v) { GSTRIDE(i, n) p[i] = v; }
+static void fill(les_ctx* c, double* p, size_t n, double v) {
+  if (n) k_fill<<<grid1(n), 256, 0, c->stream>>>(p, n, v);
+}
+
+// ---------------------------------------------------------------------------
+// spectral pipeline helpers
+static int r2c(les_ctx* c, int nf, int nlev, const double* const* in, long pstride,
+               const double* scale, const double* div, void* ws, bool big, int ncols) {
+  const Grid& g = c->g;
+  for (int f0 = 0; f0 < nf; f0 += JOB_MAXF) {
+    const int n = std::min(JOB_MAXF, nf - f0);
+    RowJob J{};
+    J.nfield = n; J.nlev = nlev;
+    J.ny = big ? g.ny2 : g.ny;
+    J.ld = big ? g.ld_big : g.ld;
+    J.wc = big ? g.nx / 2 : g.lh;
+    J.ncols = ncols;
+    J.pstride_phys = pstride;
+    J.pstride_work = (long)J.ny * J.wc;
+    for (int f = 0; f < n; ++f) {
+      J.phys[f] = in[f0 + f];
+      J.work[f] = (C2*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
+      J.scale[f] = scale ? scale[f0 + f] : 1.0;
+      J.div[f] = div ? div[f0 + f] : 0.0;
+    }
+    launch_rows_r2c<double, double>(J, big ? c->rxb.r : c->rx.r, c->stream);
+  }
+  return 0;
+}
+static int c2r(les_ctx* c, int nf, int nlev, void* ws, double* const* out, long pstride, bool big,
+               int ncols) {
+  const Grid& g = c->g;
+  for (int f0 = 0; f0 < nf; f0 += JOB_MAXF) {
+    const int n = std::min(JOB_MAXF, nf - f0);
+    RowJob J{};
+    J.nfield = n; J.nlev = nlev;
+    J.ny = big ? g.ny2 : g.ny;
+    J.ld = big ? g.ld_big : g.ld;
+    J.wc = big ? g.nx / 2 : g.lh;
+    J.ncols = ncols;
+    J.pstride_phys = pstride;
+    J.pstride_work = (long)J.ny * J.wc;
+    for (int f = 0; f < n; ++f) {
+      J.phys[f] = out[f0 + f];
+      J.work[f] = (C2*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
+      J.scale[f] = 1.0;
+      J.div[f] = 0.0;
+    }
+    launch_rows_c2r<double, double>(J, big ? c->rxb.r : c->rx.r, c->stream);
+  }
+  return 0;
+}
+static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
+  const Grid& g = c->g;
+  ColJob J{};
+  J.nlev = nlev; J.map = map; J.dir = dir; J.nf = 1;
+  J.ny_small = g.ny;
+  J.kx = c->kx; J.ky = c->ky; J.G = c->G; J.GG = c->GG; J.lh = g.lh;
+  if (map == MAP_SAME) {
+    J.ny_in = J.ny_out = g.ny; J.ncols = g.lh; J.wc_in = J.wc_out = g.lh;
+  } else if (map == MAP_PAD) {
+    J.ny_in = g.ny; J.ny_out = g.ny2; J.ncols = g.nx / 2; J.wc_in = g.lh; J.wc_out = g.nx / 2;
+  } else {
+    J.ny_in = g.ny2; J.ny_out = g.ny; J.ncols = g.nx / 2; J.wc_in = g.nx / 2; J.wc_out = g.lh;
+  }
+  J.ps_in = (long)J.ny_in * J.wc_in;
+  J.ps_out = (long)J.ny_out * J.wc_out;
+  return J;
+}
+static int cols(les_ctx* c, const ColJob& J) {
+  const FftPlanDev& Pin = (J.ny_in == c->g.ny) ? c->cy.c : c->cyb.c;
+  const FftPlanDev& Pout = (J.ny_out == c->g.ny) ? c->cy.c : c->cyb.c;
+  return launch_cols<double>(J, Pin, Pout, c->stream);
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reductions (fixed order: one CTA per plane, fixed tree)
+// mode 0: sum f[plane](1:nx,1:ny)
+__global__ void __launch_bounds__(512) k_plane_sum(const double* f, long pstride, int ld, int nx, int ny,
+                                                   double* out) {
+  __shared__ double sh[512];
+  const double* p = f + (size_t)blockIdx.x * pstride;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+    const int jy = i / nx, jx = i - jy * nx;
+    s += p[(size_t)jy * ld + jx];
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 256; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+// ---------------------------------------------------------------------------
+// ddz_uv.f90:36-55 and ddz_w.f90:81-106 (non-MPI)
+__global__ void k_ddz(double* __restrict__ dfdz, const double* __restrict__ f, int ld, int nx, int ny,
+                      int nz, double cst, int uv) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const size_t r = i - (size_t)(jz - 1) * np;
+    const int jx = (int)(r % ld);
+    if (jz == nz) { dfdz[i] = 0.0; continue; }
+    if (jx >= nx) continue;
+    if (uv) {
+      if (jz >= 2) dfdz[i] = cst * (f[i] - f[i - np]);
+    } else {
+      dfdz[i] = cst * (f[i + np] - f[i]);
+    }
+  }
+}
+int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv) {
+  const Grid& g = c->g;
+  k_ddz<<<grid1(g.nfield), 256, 0, c->stream>>>(dfdz, f, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, uv);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// filt_da.f90:3-42 for nf fields at once
+static int filt_da_multi(les_ctx* c, double* const* f, double* const* dx, double* const* dy, int nf,
+                         int nlev) {
+  const Grid& g = c->g;
+  double sc[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) sc[i] = 1.0 / (double)(g.nx * g.ny);
+  const double* in[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) in[i] = f[i];
+  r2c(c, nf, nlev, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nlev);
+  J.nin = 1; J.nout = 3; J.nf = nf;
+  J.in[0] = c->wsA; J.fs_in = (long)nlev * g.C;
+  J.out[0] = c->wsB;
+  J.out[1] = (C2*)c->wsB + (size_t)nf * nlev * g.C;
+  J.out[2] = (C2*)c->wsB + (size_t)2 * nf * nlev * g.C;
+  J.fs_out = (long)nlev * g.C;
+  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY;
+  cols(c, J);
+  double* out[3 * JOB_MAXF];
+  for (int i = 0; i < nf; ++i) { out[i] = f[i]; out[nf + i] = dx[i]; out[2 * nf + i] = dy[i]; }
+  c2r(c, 3 * nf, nlev, c->wsB, out, (long)g.nplane, false, g.lh);
+  return 0;
+}
+int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev) {
+  double* a[1] = {f}; double* b[1] = {dfdx}; double* d[1] = {dfdy};
+  return filt_da_multi(c, a, b, d, 1, nlev);
+}
+// ddx.f90 / ddy.f90 / ddxy.f90 (dfdx or dfdy may be null)
+int op_ddxy(les_ctx* c, double* dfdx, double* dfdy, const double* f, int nlev) {
+  const Grid& g = c->g;
+  double sc = 1.0 / (double)(g.nx * g.ny);
+  r2c(c, 1, nlev, &f, (long)g.nplane, &sc, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nlev);
+  J.nin = 1; J.nout = 0;
+  J.in[0] = c->wsA;
+  double* out[2]; int no = 0;
+  if (dfdx) { J.out[J.nout] = (C2*)c->wsB + (size_t)J.nout * nlev * g.C; J.coef[J.nout][0] = CC_IKX; out[no++] = dfdx; J.nout++; }
+  if (dfdy) { J.out[J.nout] = (C2*)c->wsB + (size_t)J.nout * nlev * g.C; J.coef[J.nout][0] = CC_IKY; out[no++] = dfdy; J.nout++; }
+  cols(c, J);
+  c2r(c, no, nlev, c->wsB, out, (long)g.nplane, false, g.lh);
+  return 0;
+}
+// test_filtermodule.f90:13-30 on nplanes planes; which = 0 (G_test) / 1 (G_test_test)
+int op_test_filter(les_ctx* c, double* out, const double* in, int nplanes, int which, long pstride) {
+  const Grid& g = c->g;
+  r2c(c, 1, nplanes, &in, pstride, nullptr, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nplanes);
+  J.nin = 1; J.nout = 1; J.in[0] = c->wsA; J.out[0] = c->wsB;
+  J.coef[0][0] = which == 0 ? CC_G : CC_GG;
+  cols(c, J);
+  c2r(c, 1, nplanes, c->wsB, &out, pstride, false, g.lh);
+  return 0;
+}
+// plain transforms (rfftwnd_f77_one_*), in place on (ld,ny) planes
+int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse) {
+  const Grid& g = c->g;
+  const long ps = big ? (long)g.nplane_big : (long)g.nplane;
+  const int lhh = big ? g.lh_big : g.lh;
+  const int nyy = big ? g.ny2 : g.ny;
+  // full-width work planes for these entry points
+  RowJob J{};
+  J.nfield = 1; J.nlev = nplanes; J.ny = nyy; J.ld = big ? g.ld_big : g.ld;
+  J.wc = lhh; J.ncols = lhh; J.pstride_phys = ps; J.pstride_work = (long)nyy * lhh;
+  J.phys[0] = planes; J.work[0] = c->wsA; J.scale[0] = 1.0; J.div[0] = 0.0;
+  ColJob K{};
+  K.nin = 1; K.nout = 1; K.nlev = nplanes; K.nf = 1; K.ny_in = K.ny_out = nyy; K.map = MAP_SAME;
+  K.ncols = lhh; K.ny_small = nyy; K.wc_in = K.wc_out = lhh; K.ps_in = K.ps_out = (long)nyy * lhh;
+  K.coef[0][0] = CC_ONE; K.kx = c->kx; K.ky = c->ky; K.G = c->G; K.GG = c->GG; K.lh = g.lh;
+  const HostRealPlan& rp = big ? c->rxb : c->rx;
+  const HostPlan& cp = big ? c->cyb : c->cy;
+  if (!inverse) {
+    launch_rows_r2c<double, double>(J, rp.r, c->stream);
+    K.dir = DIR_FWD; K.in[0] = c->wsA; K.out[0] = c->wsB;
+    launch_cols<double>(K, cp.c, cp.c, c->stream);
+    // copy spectra back into the planes (complex view of (ld,ny))
+    cudaMemcpy2DAsync(planes, (size_t)J.ld * sizeof(double), c->wsB, (size_t)lhh * sizeof(C2),
+                      (size_t)lhh * sizeof(C2), (size_t)nyy * nplanes, cudaMemcpyDeviceToDevice, c->stream);
+  } else {
+    cudaMemcpy2DAsync(c->wsA, (size_t)lhh * sizeof(C2), planes, (size_t)J.ld * sizeof(double),
+                      (size_t)lhh * sizeof(C2), (size_t)nyy * nplanes, cudaMemcpyDeviceToDevice, c->stream);
+    K.dir = DIR_INV; K.in[0] = c->wsA; K.out[0] = c->wsB;
+    launch_cols<double>(K, cp.c, cp.c, c->stream);
+    J.work[0] = c->wsB;
+    launch_rows_c2r<double, double>(J, rp.r, c->stream);
+  }
+  return 0;
+}
+
+// dealias1.f90:1-31 for nf fields: small (ld,ny,nlev) -> big (ld_big,ny2,nlev)
+int op_dealias1(les_ctx* c, const double* const* in, double* const* out, int nf, int nlev) {
+  const Grid& g = c->g;
+  double sc[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) sc[i] = 1.0 / (double)(g.nx * g.ny);
+  r2c(c, nf, nlev, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_PAD, DIR_BOTH, nlev);
+  J.nin = 1; J.nout = 1; J.nf = nf;
+  J.in[0] = c->wsA; J.fs_in = (long)nlev * g.C;
+  J.out[0] = c->wsB; J.fs_out = (long)nlev * g.CB;
+  J.coef[0][0] = CC_ONE;
+  cols(c, J);
+  c2r(c, nf, nlev, c->wsB, out, (long)g.nplane_big, true, g.nx / 2);
+  return 0;
+}
+// dealias2.f90:1-33 for nf fields: big -> small; the big input is multiplied
+// by `scale` (1/(nx2*ny2) in dealias2, 1 when the caller folded it in)
+int op_dealias2(les_ctx* c, double* const* out, const double* const* in, int nf, int nlev, double scale) {
+  const Grid& g = c->g;
+  double sc[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) sc[i] = scale;
+  r2c(c, nf, nlev, in, (long)g.nplane_big, sc, nullptr, c->wsA, true, g.nx / 2);
+  ColJob J = coljob(c, MAP_UNPAD, DIR_BOTH, nlev);
+  J.nin = 1; J.nout = 1; J.nf = nf;
+  J.in[0] = c->wsA; J.fs_in = (long)nlev * g.CB;
+  J.out[0] = c->wsB; J.fs_out = (long)nlev * g.C;
+  J.coef[0][0] = CC_ONE;
+  cols(c, J);
+  c2r(c, nf, nlev, c->wsB, out, (long)g.nplane, false, g.nx / 2);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// scalars_module.f90:508-690 obukhov (q = 0, patch_flag = 1); u1, v1 are the
+// 4-delta filtered first-level velocities, theta_sum the plane sum of theta(1).
+__global__ void k_obukhov(const double* __restrict__ u1, const double* __restrict__ v1,
+                          const double* __restrict__ theta, const double* __restrict__ zo,
+                          const double* __restrict__ z_os, double* __restrict__ sgs_t3,
+                          double* ustar_avg, double* psi_m, double* psi_m0, double* psi_h,
+                          double* psi_h0, double* phi_m, double* phi_h, const double* theta_sum,
+                          int nx, int ny, int ld, double dz, double vonk, double g_, double nxny_f) {
+  GSTRIDE(s, (size_t)nx * ny) {
+    const int jy = (int)(s / nx), jx = (int)(s - (size_t)jy * nx);
+    const size_t i = (size_t)jy * ld + jx;
+    const double theta_ = theta_sum[0] / nxny_f;
+    const double u_avg = sqrt(u1[i] * u1[i] + v1[i] * v1[i]);
+    const double us = u_avg * vonk / (log(0.5 * dz / zo[s]) - psi_m[s] + psi_m0[s]);
+    ustar_avg[s] = us;
+    const double wt_avg = sgs_t3[s];
+    const double wtv_avg = sgs_t3[s] + 0.61 * theta[i] * (0.001 * 100.0 * 0.0);
+    const double L = -(us * us * us) / (vonk * (g_ / theta_) * wtv_avg);
+    double zeta = 0.5 * dz / L, zeta0 = zo[s] / L, zeta0s = z_os[s] / L;
+    if (zeta < -30.0) zeta = -30.0;
+    if (zeta > 2.0) zeta = 2.0;
+    if (zeta0 < -30.0) zeta0 = -30.0;
+    if (zeta0 > 2.0) zeta0 = 2.0;
+    if (zeta0s < -30.0) zeta0s = -30.0;
+    if (zeta0s > 2.0) zeta0s = 2.0;
+    if (L < 0.0 && wt_avg != 0.0) {
+      const double x = pow(1.0 - 16.0 * zeta, 0.25);
+      psi_m[s] = 2.0 * log((1.0 + x) / 2.0) + log((1.0 + x * x) / 2.0) - 2.0 * atan(x) + LES_PI / 2.0;
+      psi_h[s] = 2.0 * log((1.0 + x * x) / 2.0);
+      phi_m[s] = 1.0 / x;
+      phi_h[s] = 1.0 / (x * x);
+      const double x0 = pow(1.0 - 16.0 * zeta0, 0.25);
+      const double x0s = pow(1.0 - 16.0 * zeta0s, 0.25);
+      psi_m0[s] = 2.0 * log((1.0 + x0) / 2.0) + log((1.0 + x0 * x0) / 2.0) - 2.0 * atan(x0) + LES_PI / 2.0;
+      psi_h0[s] = 2.0 * log((1.0 + x0s * x0s) / 2.0);
+    } else if (L > 0.0 && wt_avg != 0.0) {
+      phi_m[s] = 1.0 + 5.0 * zeta;
+      phi_h[s] = 1.0 + 5.0 * zeta;
+      psi_m[s] = -1.0 * 5.0 * zeta;
+      psi_h[s] = -1.0 * 5.0 * zeta;
+      psi_m0[s] = -1.0 * 5.0 * zeta0;
+      psi_h0[s] = -1.0 * 5.0 * zeta0s;
+    } else {
+      psi_m[s] = 0.0; psi_m0[s] = 0.0; psi_h[s] = 0.0; psi_h0[s] = 0.0;
+      phi_m[s] = 1.0; phi_h[s] = 1.0;
+    }
+  }
+}
+__global__ void k_obukhov_init(double* psi_m, double* psi_m0, double* psi_h, double* psi_h0,
+                               double* sgs_t3, const double* wt_s, size_t n, int initsc, double div) {
+  GSTRIDE(s, n) {
+    psi_m[s] = 0.0; psi_m0[s] = 0.0; psi_h[s] = 0.0; psi_h0[s] = 0.0;
+    if (!initsc) sgs_t3[s] = wt_s[s] / div;
+  }
+}
+int op_obukhov(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  const size_t ns = (size_t)g.nx * g.ny;
+  if (c->jt == 1)  // SCAL_init = 1 (scalars_module.f90:525-542)
+    k_obukhov_init<<<grid1(ns), 256, 0, c->stream>>>(c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PSI_H],
+                                                     c->f[LES_PSI_H0], c->f[LES_SGS_T3_SFC], c->f[LES_WT_S],
+                                                     ns, k.initsc, k.u_star * k.t_scale);
+  k_plane_sum<<<1, 512, 0, c->stream>>>(c->f[LES_THETA], 0, g.ld, g.nx, g.ny, c->dscal + 0);
+  double* u1 = c->tmp;
+  double* v1 = c->tmp + g.nplane;
+  op_test_filter(c, u1, c->f[LES_U], 1, 1, (long)g.nplane);
+  op_test_filter(c, v1, c->f[LES_V], 1, 1, (long)g.nplane);
+  const double g_ = (k.g * k.z_i) / (k.u_star * k.u_star);
+  k_obukhov<<<grid1(ns), 256, 0, c->stream>>>(u1, v1, c->f[LES_THETA], c->f[LES_ZO], c->z_os,
+                                              c->f[LES_SGS_T3_SFC], c->f[LES_USTAR_AVG], c->f[LES_PSI_M],
+                                              c->f[LES_PSI_M0], c->f[LES_PSI_H], c->f[LES_PSI_H0],
+                                              c->f[LES_PHI_M], c->f[LES_PHI_H], c->dscal + 0, g.nx, g.ny,
+                                              g.ld, g.dz, k.vonk, g_, (double)(float)(g.nx * g.ny));
+  return 0;
+}
+
+// wallstress.f90:5-69 ('wall')
+__global__ void k_wallstress(const double* __restrict__ u, const double* __restrict__ v,
+                             const double* __restrict__ u1, const double* __restrict__ v1,
+                             const double* __restrict__ zo, const double* __restrict__ psi_m,
+                             const double* __restrict__ psi_m0, const double* __restrict__ phi_m,
+                             double* ustar_avg, double* txz, double* tyz, double* dudz, double* dvdz,
+                             int nx, int ny, int ld, double dz, double vonk) {
+  GSTRIDE(s, (size_t)nx * ny) {
+    const int jy = (int)(s / nx), jx = (int)(s - (size_t)jy * nx);
+    const size_t i = (size_t)jy * ld + jx;
+    const double denom = log(0.5 * dz / zo[s]) - psi_m[s] + psi_m0[s];
+    const double u_avg = sqrt(u1[i] * u1[i] + v1[i] * v1[i]);
+    const double us = u_avg * vonk / denom;
+    ustar_avg[s] = us;
+    const double cst = -(us * us) / u_avg;
+    txz[i] = cst * u1[i];
+    tyz[i] = cst * v1[i];
+    const double a = us / (0.5 * dz * vonk) * u1[i] / u_avg * phi_m[s];
+    const double b = us / (0.5 * dz * vonk) * v1[i] / u_avg * phi_m[s];
+    dudz[i] = (u[i] == 0.0) ? 0.0 : a;
+    dvdz[i] = (v[i] == 0.0) ? 0.0 : b;
+  }
+}
+int op_wallstress(les_ctx* c) {
+  const Grid& g = c->g;
+  double* u1 = c->tmp;
+  double* v1 = c->tmp + g.nplane;
+  op_test_filter(c, u1, c->f[LES_U], 1, 1, (long)g.nplane);
+  op_test_filter(c, v1, c->f[LES_V], 1, 1, (long)g.nplane);
+  k_wallstress<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(
+      c->f[LES_U], c->f[LES_V], u1, v1, c->f[LES_ZO], c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PHI_M],
+      c->f[LES_USTAR_AVG], c->f[LES_TXZ], c->f[LES_TYZ], c->f[LES_DUDZ], c->f[LES_DVDZ], g.nx, g.ny, g.ld,
+      g.dz, c->cfg.vonk);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// sgs_stag.f90:371-498 calc_Sij ('wall') fused with the Lagrangian velocity
+// accumulation of sgs_stag.f90:59-69
+__global__ void k_calc_sij(const double* __restrict__ dudx, const double* __restrict__ dudy,
+                           const double* __restrict__ dudz, const double* __restrict__ dvdx,
+                           const double* __restrict__ dvdy, const double* __restrict__ dvdz,
+                           const double* __restrict__ dwdx, const double* __restrict__ dwdy,
+                           const double* __restrict__ dwdz, double* S11, double* S12, double* S13,
+                           double* S22, double* S23, double* S33, const double* __restrict__ u,
+                           const double* __restrict__ v, const double* __restrict__ w, double* ul,
+                           double* vl, double* wl, int ld, int nx, int ny, int nz, int lag) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
+    if (lag) { ul[i] += u[i]; vl[i] += v[i]; wl[i] += w[i]; }
+    if (jx >= nx) continue;
+    double ux, uy, uz, vx, vy, vz, wx, wy, wz;
+    if (jz == 1) {
+      ux = dudx[i]; uy = dudy[i]; uz = dudz[i];
+      vx = dvdx[i]; vy = dvdy[i]; vz = dvdz[i];
+      wx = 0.5 * (dwdx[i] + dwdx[i + np]);
+      wy = 0.5 * (dwdy[i] + dwdy[i + np]);
+      wz = dwdz[i];
+    } else {
+      ux = 0.5 * (dudx[i] + dudx[i - np]);
+      uy = 0.5 * (dudy[i] + dudy[i - np]);
+      uz = dudz[i];
+      vx = 0.5 * (dvdx[i] + dvdx[i - np]);
+      vy = 0.5 * (dvdy[i] + dvdy[i - np]);
+      vz = dvdz[i];
+      wx = dwdx[i];
+      wy = dwdy[i];
+      wz = 0.5 * (dwdz[i] + dwdz[i - np]);
+    }
+    S11[i] = ux; S12[i] = 0.5 * (uy + vx); S13[i] = 0.5 * (uz + wx);
+    S22[i] = vy; S23[i] = 0.5 * (vz + wy); S33[i] = wz;
+  }
+}
+
+__device__ __forceinline__ double smag(double a11, double a22, double a33, double a12, double a13, double a23) {
+  return sqrt(2.0 * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0 * (a12 * a12 + a13 * a13 + a23 * a23)));
+}
+
+// sgs_stag.f90:166-211 (Cs override and Nu_t)
+__global__ void k_nut(const double* __restrict__ S11, const double* __restrict__ S12,
+                      const double* __restrict__ S13, const double* __restrict__ S22,
+                      const double* __restrict__ S23, const double* __restrict__ S33, double* Cs,
+                      double* Nu_t, int ld, int nx, int ny, int nz, double l2, int override_cs, double cs_ov) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    if (override_cs) Cs[i] = cs_ov;
+    const int jx = (int)(i % ld);
+    if (jx >= nx) continue;
+    const double S = smag(S11[i], S22[i], S33[i], S12[i], S13[i], S23[i]);
+    Nu_t[i] = S * Cs[i] * l2;
+  }
+}
+// sgs_stag.f90:218-364 (tau_ij, 'wall', molec = .false.)
+__global__ void k_tau(const double* __restrict__ S11, const double* __restrict__ S12,
+                      const double* __restrict__ S13, const double* __restrict__ S22,
+                      const double* __restrict__ S23, const double* __restrict__ S33,
+                      const double* __restrict__ Nu_t, double* txx, double* txy, double* tyy, double* txz,
+                      double* tyz, double* tzz, int ld, int nx, int ny, int nz) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
+    if (jz == nz) {
+      txx[i] = LES_BOGUS; txy[i] = LES_BOGUS; tyy[i] = LES_BOGUS; tzz[i] = LES_BOGUS;
+      txz[i] = 0.0; tyz[i] = 0.0;
+      continue;
+    }
+    if (jx >= nx) continue;
+    if (jz == 1) {
+      const double cst = Nu_t[i], nu = 0.0;
+      txx[i] = -2.0 * (cst + nu) * S11[i];
+      txy[i] = -2.0 * (cst + nu) * S12[i];
+      tyy[i] = -2.0 * (cst + nu) * S22[i];
+      tzz[i] = -2.0 * (cst + nu) * S33[i];
+      // txz, tyz at the wall come from wallstress
+    } else {
+      const size_t ip = i + np;
+      const double cst = 0.5 * (Nu_t[i] + Nu_t[ip]), nu = 0.0;
+      txx[i] = -2.0 * (cst + nu) * 0.5 * (S11[i] + S11[ip]);
+      txy[i] = -2.0 * (cst + nu) * 0.5 * (S12[i] + S12[ip]);
+      tyy[i] = -2.0 * (cst + nu) * 0.5 * (S22[i] + S22[ip]);
+      tzz[i] = -2.0 * (cst + nu) * 0.5 * (S33[i] + S33[ip]);
+      const double c2 = Nu_t[i];
+      txz[i] = -2.0 * (c2 + nu) * S13[i];
+      tyz[i] = -2.0 * (c2 + nu) * S23[i];
+    }
+  }
+}
+
+__global__ void k_bcast_levels(double* dst, const double* lev, size_t np, size_t n) {
+  GSTRIDE(i, n) dst[i] = lev[i / np];
+}
+
+int op_sgs_stag(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  const bool lag = (k.model == 4 || k.model == 5 || k.model == 7);
+  k_calc_sij<<<grid1(g.nfield), 256, 0, c->stream>>>(
+      c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
+      c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
+      c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
+      c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0);
+  const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
+  if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {  // sgs_stag.f90:120-160
+    if (k.model == 3) {
+      double* csz = c->dred;
+      op_scaledep(c, csz, S);
+      // Cs_opt2(:,:,jz) = ziko(jz)
+      k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield);
+    } else if (k.model == 5) {
+      op_lagrange(c, S);
+    }
+  }
+  int ov = 0;
+  double csov = 0.0;
+  if ((k.model == 5 || k.model == 6 || k.model == 7) && c->jt_total < 500) {  // :166-173
+    ov = 1;
+    const float c016 = 0.16f;
+    csov = (double)(c016 * c016);
+  }
+  const double delta = g.delta;
+  k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
+                                               c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, delta * delta, ov, csov);
+  k_tau<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_NU_T],
+                                               c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ],
+                                               c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// interpolag_Sdep.f90:2-380 (non-MPI).  Reads the accumulated u/v/w_lag and
+// the old F_*, writes the interpolated F_* into Fn.
+__device__ __forceinline__ double lag_disp_u(const double* ul, size_t i, size_t np, int jz, double cs,
+                                             double dt, double dxx) {
+  const double a = ul[i] / cs;
+  const double ua = (jz >= 2) ? 0.5 * (a + ul[i - np] / cs) : a;
+  return -ua * dt * cs / dxx;
+}
+__global__ void k_interpolag(const double* __restrict__ ul, const double* __restrict__ vl,
+                             const double* __restrict__ wl, const double* __restrict__ FLM,
+                             const double* __restrict__ FMM, const double* __restrict__ FQN,
+                             const double* __restrict__ FNN, double* oLM, double* oMM, double* oQN,
+                             double* oNN, int ld, int nx, int ny, int nz, double cs, double dt, double dx,
+                             double dy, double dz) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(t, (size_t)nx * ny * nz) {
+    const int jx = (int)(t % nx);
+    const int jy = (int)((t / nx) % ny);
+    const int jz = (int)(t / ((size_t)nx * ny)) + 1;
+    const size_t i = (size_t)jx + (size_t)ld * jy + np * (jz - 1);
+    const double xp = lag_disp_u(ul, i, np, jz, cs, dt, dx);
+    const double yp = lag_disp_u(vl, i, np, jz, cs, dt, dy);
+    double zp;
+    {
+      // level 2 after the near-wall doubling and clipping (:285-293);
+      // level 1 takes level 2's final value
+      const size_t i2 = (size_t)jx + (size_t)ld * jy + np;
+      if (jz <= 2) {
+        double z2 = -(wl[i2] / cs) * dt * cs / dz;
+        z2 = z2 + fmin(z2, 0.0);
+        z2 = fmin(1.0, z2);
+        z2 = fmax(-1.0, z2);
+        zp = z2;
+      } else {
+        zp = -(wl[i] / cs) * dt * cs / dz;
+      }
+    }
+    const int addx = (xp < 0.0) ? -1 : 1;  // int(sign(1,x)), sign(1,-0) = +1
+    const int addy = (yp < 0.0) ? -1 : 1;
+    const int addz = (zp < 0.0) ? -1 : 1;
+    int xa = jx + addx; if (xa < 0) xa = nx - 1; if (xa >= nx) xa = 0;
+    int ya = jy + addy; if (ya < 0) ya = ny - 1; if (ya >= ny) ya = 0;
+    int za = (jz - 1) + addz; if (za < 0) za = 0; if (za >= nz) za = nz - 1;
+    const double cx = fabs(xp), cy = fabs(yp), cz = fabs(zp);
+    const double fx = 1.0 - cx, fy = 1.0 - cy, fz = 1.0 - cz;
+    const size_t z0 = np * (jz - 1), z1 = np * za;
+    const size_t a00 = (size_t)jx + (size_t)ld * jy, a01 = (size_t)jx + (size_t)ld * ya;
+    const size_t a10 = (size_t)xa + (size_t)ld * jy, a11 = (size_t)xa + (size_t)ld * ya;
+#define LAGI(F)                                                                      \
+  (fx * fy * (F[a00 + z0] * fz + F[a00 + z1] * cz) + fx * cy * (F[a01 + z0] * fz + F[a01 + z1] * cz) + \
+   cx * fy * (F[a10 + z0] * fz + F[a10 + z1] * cz) + cx * cy * (F[a11 + z0] * fz + F[a11 + z1] * cz))
+    oLM[i] = LAGI(FLM);
+    oMM[i] = LAGI(FMM);
+    oQN[i] = LAGI(FQN);
+    oNN[i] = LAGI(FNN);
+#undef LAGI
+  }
+}
+int op_interpolag(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  double* Fn[4];
+  for (int q = 0; q < 4; ++q) Fn[q] = c->spare + (size_t)q * g.nfield;
+  k_interpolag<<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
+      c->f[LES_U_LAG], c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN],
+      c->f[LES_F_NN], Fn[0], Fn[1], Fn[2], Fn[3], g.ld, g.nx, g.ny, g.nz, (double)k.cs_count, k.dt, g.dx, g.dy,
+      g.dz);
+  // interior values changed; padding columns are never read
+  for (int q = 0; q < 4; ++q)
+    cudaMemcpyAsync(c->f[LES_F_LM + q], Fn[q], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemsetAsync(c->f[LES_U_LAG], 0, g.nfield * sizeof(double), c->stream);
+  cudaMemsetAsync(c->f[LES_V_LAG], 0, g.nfield * sizeof(double), c->stream);
+  cudaMemsetAsync(c->f[LES_W_LAG], 0, g.nfield * sizeof(double), c->stream);
+  return 0;
+}
+
+// lagrange_Sdep.f90:127-285 inputs: 21 planes per level of the chunk
+__global__ void k_lag_prep(const double* __restrict__ u, const double* __restrict__ v,
+                           const double* __restrict__ w, Ptr6 Sp,
+                           double* out, int ld, int nx, int ny, int jz0, int nlev, size_t np) {
+  const size_t tot = np * nlev;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jz = jz0 + lc;  // 1-based
+    const size_t i = (size_t)(jz - 1) * np + r;
+    double ub, vb, wb;
+    if (jz == 1) { ub = u[i]; vb = v[i]; wb = 0.25 * w[i + np]; }
+    else { ub = 0.5 * (u[i] + u[i - np]); vb = 0.5 * (v[i] + v[i - np]); wb = w[i]; }
+    const size_t stride = np * nlev;
+    double* o = out + t;
+    o[0 * stride] = ub; o[1 * stride] = vb; o[2 * stride] = wb;
+    o[3 * stride] = ub * ub; o[4 * stride] = ub * vb; o[5 * stride] = ub * wb;
+    o[6 * stride] = vb * vb; o[7 * stride] = vb * wb; o[8 * stride] = wb * wb;
+    const double s11 = Sp.p[0][i], s12 = Sp.p[1][i], s13 = Sp.p[2][i], s22 = Sp.p[3][i], s23 = Sp.p[4][i], s33 = Sp.p[5][i];
+    const double S = smag(s11, s22, s33, s12, s13, s23);
+    o[9 * stride] = s11; o[10 * stride] = s12; o[11 * stride] = s13;
+    o[12 * stride] = s22; o[13 * stride] = s23; o[14 * stride] = s33;
+    o[15 * stride] = S * s11; o[16 * stride] = S * s12; o[17 * stride] = S * s13;
+    o[18 * stride] = S * s22; o[19 * stride] = S * s23; o[20 * stride] = S * s33;
+  }
+}
+
+__device__ __forceinline__ double pow_m18(double x) { return 1.0 / sqrt(sqrt(sqrt(x))); }
+
+// lagrange_Sdep.f90:268-421 from the 42 filtered planes (G: q, GG: 21+q)
+__global__ void k_lag_final(const double* __restrict__ flt, double* F_LM, double* F_MM, double* F_QN,
+                            double* F_NN, double* Beta, double* Cs, int ld, int nx, int ny, int nz, int jz0,
+                            int nlev, size_t np, double cst, double opftdelta, double lagran_dt, int bexp_one,
+                            double bexp) {
+  const size_t tot = np * nlev;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jx = (int)(r % ld);
+    const int jz = jz0 + lc;
+    const size_t gi = (size_t)(jz - 1) * np + r;
+    if (jx >= nx) { Cs[gi] = (double)1e-24f; continue; }
+    const size_t st = np * nlev;
+    const double* G = flt + t;
+    const double* H = flt + t + 21 * st;
+    const double ub = G[0], vb = G[st], wb = G[2 * st];
+    const double uh = H[0], vh = H[st], wh = H[2 * st];
+    const double Lq[6] = {G[3 * st] - ub * ub, G[4 * st] - ub * vb, G[5 * st] - ub * wb,
+                          G[6 * st] - vb * vb, G[7 * st] - vb * wb, G[8 * st] - wb * wb};
+    const double Qq[6] = {H[3 * st] - uh * uh, H[4 * st] - uh * vh, H[5 * st] - uh * wh,
+                          H[6 * st] - vh * vh, H[7 * st] - vh * wh, H[8 * st] - wh * wh};
+    double Sb_[6], Sh_[6], SSb[6], SSh[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      Sb_[q] = G[(9 + q) * st]; Sh_[q] = H[(9 + q) * st];
+      SSb[q] = G[(15 + q) * st]; SSh[q] = H[(15 + q) * st];
+    }
+    const double Sb = smag(Sb_[0], Sb_[3], Sb_[5], Sb_[1], Sb_[2], Sb_[4]);
+    const double Sh = smag(Sh_[0], Sh_[3], Sh_[5], Sh_[1], Sh_[2], Sh_[4]);
+    double M[6], N[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      M[q] = cst * (SSb[q] - 4.0 * Sb * Sb_[q]);
+      N[q] = cst * (SSh[q] - 16.0 * Sh * Sh_[q]);
+    }
+    const double LM = Lq[0] * M[0] + Lq[3] * M[3] + Lq[5] * M[5] + 2.0 * (Lq[1] * M[1] + Lq[2] * M[2] + Lq[4] * M[4]);
+    const double MM = M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + 2.0 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+    const double QN = Qq[0] * N[0] + Qq[3] * N[3] + Qq[5] * N[5] + 2.0 * (Qq[1] * N[1] + Qq[2] * N[2] + Qq[4] * N[4]);
+    const double NN = N[0] * N[0] + N[3] * N[3] + N[5] * N[5] + 2.0 * (N[1] * N[1] + N[2] * N[2] + N[4] * N[4]);
+    const double e24 = (double)1e-24f;
+    double flm = F_LM[gi], fmm = F_MM[gi];
+    double Tn = fmax32(flm * fmm, e24);
+    Tn = opftdelta * pow_m18(Tn);
+    Tn = fmax32(e24, Tn);
+    double dumfac = lagran_dt / Tn;
+    double epsi = dumfac / (1.0 + dumfac);
+    flm = (epsi * LM + (1.0 - epsi) * flm);
+    fmm = (epsi * MM + (1.0 - epsi) * fmm);
+    flm = fmax32(e24, flm);
+    double cs2d = fmax32(e24, flm / fmm);
+    F_LM[gi] = flm; F_MM[gi] = fmm;
+    double fqn = F_QN[gi], fnn = F_NN[gi];
+    Tn = fmax32(fqn * fnn, e24);
+    Tn = opftdelta * pow_m18(Tn);
+    Tn = fmax32(e24, Tn);
+    dumfac = lagran_dt / Tn;
+    epsi = dumfac / (1.0 + dumfac);
+    fqn = (epsi * QN + (1.0 - epsi) * fqn);
+    fnn = (epsi * NN + (1.0 - epsi) * fnn);
+    fqn = fmax32(e24, fqn);
+    double cs4d = fmax32(e24, fqn / fnn);
+    F_QN[gi] = fqn; F_NN[gi] = fnn;
+    double beta = bexp_one ? cs4d / cs2d : pow(cs4d / cs2d, bexp);
+    if (jz == nz) beta = 1.0;
+    Beta[gi] = beta;
+    const double betaclip = fmax32(beta, 1.0 / (2.0 * 4.0));
+    Cs[gi] = fmax32(e24, cs2d / betaclip);
+  }
+}
+
+// lagrange_Sdep.f90:4-478 ; S = S11,S12,S13,S22,S23,S33 (device)
+int op_lagrange(les_ctx* c, const double* const* S) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  op_interpolag(c);
+  const double delta = g.delta;
+  const double cst = 2.0 * (delta * delta);
+  const double opftdelta = 1.5 * delta;
+  const double lagran_dt = k.dt * (double)k.cs_count;
+  const double bexp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
+  const int bone = (bexp == 1.0) ? 1 : 0;
+  Ptr6 Sp;
+  for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
+  const int nch = c->lag_chunk;
+  for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
+    const int nl = std::min(nch, g.nz - jz0 + 1);
+    double* prep = c->tmp;                              // 21 * nl planes
+    double* flt = c->tmp + (size_t)21 * nch * g.nplane;  // 42 * nl planes
+    k_lag_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W],
+                                                           Sp, prep, g.ld, g.nx,
+                                                           g.ny, jz0, nl, g.nplane);
+    const double* in[21];
+    for (int q = 0; q < 21; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
+    r2c(c, 21, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nl);
+    J.nin = 1; J.nout = 2; J.nf = 21;
+    J.in[0] = c->wsA; J.fs_in = (long)nl * g.C;
+    J.out[0] = c->wsB; J.out[1] = (C2*)c->wsB + (size_t)21 * nl * g.C; J.fs_out = (long)nl * g.C;
+    J.coef[0][0] = CC_G; J.coef[1][0] = CC_GG;
+    cols(c, J);
+    double* out[42];
+    for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
+    c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    k_lag_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+        flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
+        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp);
+  }
+  // the level loop's pointer table must outlive the launches
+  return 0;
+}
+
+// scaledep_dynamic.f90:4-255 (plane sums over 1:nx) -> cs_z (device, nz)
+__global__ void k_sd_prep(const double* __restrict__ u, const double* __restrict__ v,
+                          const double* __restrict__ w, Ptr6 Sp, double* out,
+                          int ld, int nx, int ny, int jz0, int nlev, size_t np) {
+  const size_t tot = np * nlev;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jz = jz0 + lc;
+    const size_t i = (size_t)(jz - 1) * np + r;
+    double ub, vb, wb, L11, L12, L13, L22, L23, L33;
+    if (jz == 1) {
+      ub = u[i]; vb = v[i]; wb = 0.25 * w[i + np];
+      L11 = u[i] * u[i]; L12 = u[i] * v[i]; L13 = u[i] * 0.25 * w[i + np];
+      L22 = v[i] * v[i]; L23 = v[i] * 0.25 * w[i + np];
+      const double tt = 0.25 * w[i + np]; L33 = tt * tt;
+    } else {
+      ub = 0.5 * (u[i] + u[i - np]); vb = 0.5 * (v[i] + v[i - np]); wb = w[i];
+      L11 = 0.5 * (u[i] + u[i - np]) * 0.5 * (u[i] + u[i - np]);
+      L12 = 0.5 * (u[i] + u[i - np]) * 0.5 * (v[i] + v[i - np]);
+      L13 = 0.5 * (u[i] + u[i - np]) * w[i];
+      L22 = 0.5 * (v[i] + v[i - np]) * 0.5 * (v[i] + v[i - np]);
+      L23 = 0.5 * (v[i] + v[i - np]) * w[i];
+      L33 = w[i] * w[i];
+    }
+    const size_t stride = np * nlev;
+    double* o = out + t;
+    o[0] = ub; o[stride] = vb; o[2 * stride] = wb;
+    o[3 * stride] = L11; o[4 * stride] = L12; o[5 * stride] = L13;
+    o[6 * stride] = L22; o[7 * stride] = L23; o[8 * stride] = L33;
+    const double s11 = Sp.p[0][i], s12 = Sp.p[1][i], s13 = Sp.p[2][i], s22 = Sp.p[3][i], s23 = Sp.p[4][i], s33 = Sp.p[5][i];
+    const double S = smag(s11, s22, s33, s12, s13, s23);
+    o[9 * stride] = s11; o[10 * stride] = s12; o[11 * stride] = s13;
+    o[12 * stride] = s22; o[13 * stride] = s23; o[14 * stride] = s33;
+    o[15 * stride] = S * s11; o[16 * stride] = S * s12; o[17 * stride] = S * s13;
+    o[18 * stride] = S * s22; o[19 * stride] = S * s23; o[20 * stride] = S * s33;
+  }
+}
+// Second filtered set: Q_ij inputs are products of the G-filtered velocities.
+__global__ void k_sd_qprep(const double* __restrict__ flt, double* qin, int nlev, size_t np) {
+  const size_t st = np * nlev;
+  GSTRIDE(t, st) {
+    const double ub = flt[t], vb = flt[t + st], wb = flt[t + 2 * st];
+    qin[t] = ub * ub; qin[t + st] = ub * vb; qin[t + 2 * st] = ub * wb;
+    qin[t + 3 * st] = vb * vb; qin[t + 4 * st] = vb * wb; qin[t + 5 * st] = wb * wb;
+  }
+}
+// per-level sums a1..e2 (10 sums) -> sums[lev*10 + q]; one CTA per level, fixed order
+__global__ void __launch_bounds__(256) k_sd_sums(const double* __restrict__ flt, const double* __restrict__ qf,
+                                                 double* sums, int ld, int nx, int ny, int nlev, size_t np, int jz0) {
+  __shared__ double sh[10][256];
+  const int lc = blockIdx.x;
+  const size_t st = np * nlev;
+  double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
+    const int jy = e / nx, jx = e - jy * nx;
+    const size_t t = (size_t)lc * np + (size_t)jy * ld + jx;
+    // G outputs q (0..20), GG outputs 21+q ; Q from qf (6 planes GG-filtered)
+    const double* G = flt + t;
+    const double* H = flt + t + 21 * st;
+    const double ub = G[0], vb = G[st], wb = G[2 * st];
+    const double uh = H[0], vh = H[st], wh = H[2 * st];
+    const double L[6] = {G[3 * st] - ub * ub, G[4 * st] - ub * vb, G[5 * st] - ub * wb,
+                         G[6 * st] - vb * vb, G[7 * st] - vb * wb, G[8 * st] - wb * wb};
+    const double Q[6] = {qf[t] - uh * uh, qf[t + st] - uh * vh, qf[t + 2 * st] - uh * wh,
+                         qf[t + 3 * st] - vh * vh, qf[t + 4 * st] - vh * wh, qf[t + 5 * st] - wh * wh};
+    double b[6], h[6], sb[6], sh_[6];
+    for (int q = 0; q < 6; ++q) { b[q] = G[(9 + q) * st]; h[q] = H[(9 + q) * st]; sb[q] = G[(15 + q) * st]; sh_[q] = H[(15 + q) * st]; }
+    const double Sb = smag(b[0], b[3], b[5], b[1], b[2], b[4]);
+    const double Sh = smag(h[0], h[3], h[5], h[1], h[2], h[4]);
+    acc[0] += Sb * (b[0] * L[0] + b[3] * L[3] + b[5] * L[5] + 2.0 * (b[1] * L[1] + b[2] * L[2] + b[4] * L[4]));
+    acc[1] += sb[0] * L[0] + sb[3] * L[3] + sb[5] * L[5] + 2.0 * (sb[1] * L[1] + sb[2] * L[2] + sb[4] * L[4]);
+    acc[2] += sb[0] * sb[0] + sb[3] * sb[3] + sb[5] * sb[5] + 2.0 * (sb[1] * sb[1] + sb[2] * sb[2] + sb[4] * sb[4]);
+    acc[3] += 0.5 * (Sb * Sb * Sb * Sb);
+    acc[4] += Sb * (b[0] * sb[0] + b[3] * sb[3] + b[5] * sb[5] + 2.0 * (b[1] * sb[1] + b[2] * sb[2] + b[4] * sb[4]));
+    acc[5] += Sh * (h[0] * Q[0] + h[3] * Q[3] + h[5] * Q[5] + 2.0 * (h[1] * Q[1] + h[2] * Q[2] + h[4] * Q[4]));
+    acc[6] += sh_[0] * Q[0] + sh_[3] * Q[3] + sh_[5] * Q[5] + 2.0 * (sh_[1] * Q[1] + sh_[2] * Q[2] + sh_[4] * Q[4]);
+    acc[7] += sh_[0] * sh_[0] + sh_[3] * sh_[3] + sh_[5] * sh_[5] + 2.0 * (sh_[1] * sh_[1] + sh_[2] * sh_[2] + sh_[4] * sh_[4]);
+    acc[8] += 0.5 * (Sh * Sh * Sh * Sh);
+    acc[9] += Sh * (h[0] * sh_[0] + h[3] * sh_[3] + h[5] * sh_[5] + 2.0 * (h[1] * sh_[1] + h[2] * sh_[2] + h[4] * sh_[4]));
+  }
+  for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 10; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 10) sums[(size_t)(jz0 - 1 + lc) * 10 + threadIdx.x] = sh[threadIdx.x][0];
+}
+// sgsmodule.f90:37-59 rtnewt and scaledep_dynamic.f90:187-244 second pass
+__device__ double rtnewt_d(const double* A) {
+  double r = 0.5 * (0.0 + 15.0);
+  for (int j = 1; j <= 100; ++j) {
+    const double f = A[0] + r * (A[1] + r * (A[2] + r * (A[3] + r * (A[4] + r * A[5]))));
+    const double df = A[1] + r * (2.0 * A[2] + r * (3.0 * A[3] + r * (4.0 * A[4] + r * (5.0 * A[5]))));
+    const double d = f / df;
+    r = r - d;
+    if (fabs(d) < 0.001) return r;
+  }
+  return 1.0;
+}
+__global__ void __launch_bounds__(256) k_sd_final(const double* __restrict__ flt, const double* __restrict__ sums,
+                                                  double* cs_z, int ld, int nx, int ny, int nlev, size_t np,
+                                                  int jz0, double delta) {
+  __shared__ double sn[256], sd[256];
+  __shared__ double beta_s;
+  const int lc = blockIdx.x;
+  const int jz = jz0 + lc;
+  const size_t st = np * nlev;
+  if (threadIdx.x == 0) {
+    const double* s = sums + (size_t)(jz - 1) * 10;
+    const double N2 = (double)(nx * ny);
+    const double d2 = delta * delta, t2 = (2.0 * d2) * (2.0 * d2);
+    const double a1 = -2.0 * d2 * 4.0 * s[0] / N2, b1 = -2.0 * d2 * s[1] / N2, c1 = t2 * s[2] / N2;
+    const double d1 = t2 * 16.0 * s[3] / N2, e1 = 2.0 * t2 * 4.0 * s[4] / N2;
+    const double a2 = -2.0 * d2 * 16.0 * s[5] / N2, b2 = -2.0 * d2 * s[6] / N2, c2 = t2 * s[7] / N2;
+    const double dd2 = t2 * 256.0 * s[8] / N2, e2 = 2.0 * t2 * 16.0 * s[9] / N2;
+    double A[6];
+    A[0] = b2 * c1 - b1 * c2;
+    A[1] = a1 * c2 - b2 * e1;
+    A[2] = b2 * d1 + b1 * e2 - a2 * c1;
+    A[3] = a2 * e1 - a1 * e2;
+    A[4] = -a2 * d1 - b1 * dd2;
+    A[5] = a1 * dd2;
+    beta_s = rtnewt_d(A);
+  }
+  __syncthreads();
+  const double beta = beta_s;
+  const double cst = 2.0 * (delta * delta);
+  double num = 0.0, den = 0.0;
+  for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
+    const int jy = e / nx, jx = e - jy * nx;
+    const size_t t = (size_t)lc * np + (size_t)jy * ld + jx;
+    const double* G = flt + t;
+    const double ub = G[0], vb = G[st], wb = G[2 * st];
+    const double L[6] = {G[3 * st] - ub * ub, G[4 * st] - ub * vb, G[5 * st] - ub * wb,
+                         G[6 * st] - vb * vb, G[7 * st] - vb * wb, G[8 * st] - wb * wb};
+    double b[6], sb[6];
+    for (int q = 0; q < 6; ++q) { b[q] = G[(9 + q) * st]; sb[q] = G[(15 + q) * st]; }
+    const double Sb = smag(b[0], b[3], b[5], b[1], b[2], b[4]);
+    double M[6];
+    for (int q = 0; q < 6; ++q) M[q] = cst * (sb[q] - 4.0 * beta * Sb * b[q]);
+    num += L[0] * M[0] + L[3] * M[3] + L[5] * M[5] + 2.0 * (L[1] * M[1] + L[2] * M[2] + L[4] * M[4]);
+    den += M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + 2.0 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+  }
+  sn[threadIdx.x] = num; sd[threadIdx.x] = den;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) { sn[threadIdx.x] += sn[threadIdx.x + w]; sd[threadIdx.x] += sd[threadIdx.x + w]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cs_z[jz - 1] = fmax(0.0, sn[0] / sd[0]);
+}
+int op_scaledep(les_ctx* c, double* cs_z, const double* const* S) {
+  const Grid& g = c->g;
+  Ptr6 Sp;
+  for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
+  double* sums = c->dred + 2 * (size_t)(g.nz + 8);
+  const int nch = c->lag_chunk;
+  for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
+    const int nl = std::min(nch, g.nz - jz0 + 1);
+    double* prep = c->tmp;
+    double* flt = c->tmp + (size_t)21 * nch * g.nplane;
+    k_sd_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W],
+                                                          Sp, prep, g.ld, g.nx, g.ny,
+                                                          jz0, nl, g.nplane);
+    const double* in[21];
+    for (int q = 0; q < 21; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
+    r2c(c, 21, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nl);
+    J.nin = 1; J.nout = 2; J.nf = 21;
+    J.in[0] = c->wsA; J.fs_in = (long)nl * g.C;
+    J.out[0] = c->wsB; J.out[1] = (C2*)c->wsB + (size_t)21 * nl * g.C; J.fs_out = (long)nl * g.C;
+    J.coef[0][0] = CC_G; J.coef[1][0] = CC_GG;
+    cols(c, J);
+    double* out[42];
+    for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
+    c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    // Q_ij inputs: products of the G-filtered velocities, then GG-filtered
+    double* qin = prep;  // reuse: 6 * nl planes
+    k_sd_qprep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(flt, qin, nl, g.nplane);
+    const double* qi[6];
+    double* qo[6];
+    for (int q = 0; q < 6; ++q) { qi[q] = qin + (size_t)q * nl * g.nplane; qo[q] = prep + (size_t)(6 + q) * nl * g.nplane; }
+    r2c(c, 6, nl, qi, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+    ColJob K = coljob(c, MAP_SAME, DIR_BOTH, nl);
+    K.nin = 1; K.nout = 1; K.nf = 6; K.in[0] = c->wsA; K.fs_in = (long)nl * g.C;
+    K.out[0] = c->wsB; K.fs_out = (long)nl * g.C; K.coef[0][0] = CC_GG;
+    cols(c, K);
+    c2r(c, 6, nl, c->wsB, qo, (long)g.nplane, false, g.lh);
+    k_sd_sums<<<nl, 256, 0, c->stream>>>(flt, prep + (size_t)6 * nl * g.nplane, sums, g.ld, g.nx, g.ny, nl,
+                                         g.nplane, jz0);
+    k_sd_final<<<nl, 256, 0, c->stream>>>(flt, sums, cs_z, g.ld, g.nx, g.ny, nl, g.nplane, jz0, g.delta);
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// divstress_uv.f90:1-63 and divstress_w.f90:4-86, with the horizontal
+// derivatives summed in spectral space (one inverse transform per component).
+__global__ void k_divstress_fin(double* __restrict__ divx, double* __restrict__ divy,
+                                double* __restrict__ divz, const double* __restrict__ hx,
+                                const double* __restrict__ hy, const double* __restrict__ hz,
+                                const double* __restrict__ txz, const double* __restrict__ tyz,
+                                const double* __restrict__ tzz, int ld, int nx, int ny, int nz, double cdz,
+                                int want) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
+    if (jz == nz) {
+      if (want & 1) divx[i] = LES_BOGUS;
+      if (want & 2) divy[i] = LES_BOGUS;
+      if (want & 4) divz[i] = (jx >= nx) ? 0.0 : hz[i] + 0.0;
+      continue;
+    }
+    if (jx >= nx) {
+      if (want & 1) divx[i] = 0.0;
+      if (want & 2) divy[i] = 0.0;
+      if (want & 4) divz[i] = 0.0;
+      continue;
+    }
+    if (want & 1) divx[i] = hx[i] + cdz * (txz[i + np] - txz[i]);
+    if (want & 2) divy[i] = hy[i] + cdz * (tyz[i + np] - tyz[i]);
+    if (want & 4) divz[i] = (jz == 1) ? hz[i] : hz[i] + cdz * (tzz[i] - tzz[i - np]);
+  }
+}
+int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz) {
+  const Grid& g = c->g;
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[5] = {c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ], c->f[LES_TYZ]};
+  double scs[5] = {sc, sc, sc, sc, sc};
+  r2c(c, 5, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  const long FS = (long)g.nz * g.C;
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
+  J.nin = 3; J.nout = 2;
+  J.in[0] = c->wsA; J.in[1] = (C2*)c->wsA + FS; J.in[2] = (C2*)c->wsA + 2 * FS;
+  J.out[0] = c->wsB; J.out[1] = (C2*)c->wsB + FS;
+  J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;   // d txx/dx + d txy/dy
+  J.coef[1][1] = CC_IKX; J.coef[1][2] = CC_IKY;   // d txy/dx + d tyy/dy
+  cols(c, J);
+  ColJob K = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
+  K.nin = 2; K.nout = 1;
+  K.in[0] = (C2*)c->wsA + 3 * FS; K.in[1] = (C2*)c->wsA + 4 * FS;
+  K.out[0] = (C2*)c->wsB + 2 * FS;
+  K.coef[0][0] = CC_IKX; K.coef[0][1] = CC_IKY;   // d txz/dx + d tyz/dy
+  cols(c, K);
+  double* h[3] = {c->tmp, c->tmp + g.nfield, c->tmp + 2 * g.nfield};
+  c2r(c, 3, g.nz, c->wsB, h, (long)g.nplane, false, g.lh);
+  k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divtx, divty, divtz, h[0], h[1], h[2], c->f[LES_TXZ],
+                                                         c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz,
+                                                         1.0 / g.dz, 7);
+  return 0;
+}
+// single divstress call with caller-supplied stresses (per-routine entry point)
+int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz,
+                     int w_variant) {
+  const Grid& g = c->g;
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[2] = {tx, ty};
+  double scs[2] = {sc, sc};
+  r2c(c, 2, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  const long FS = (long)g.nz * g.C;
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
+  J.nin = 2; J.nout = 1;
+  J.in[0] = c->wsA; J.in[1] = (C2*)c->wsA + FS; J.out[0] = c->wsB;
+  J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
+  cols(c, J);
+  double* h = c->tmp;
+  c2r(c, 1, g.nz, c->wsB, &h, (long)g.nplane, false, g.lh);
+  if (!w_variant)
+    k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divt, nullptr, nullptr, h, nullptr, nullptr, tz, nullptr,
+                                                           nullptr, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, 1);
+  else
+    k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(nullptr, nullptr, divt, nullptr, nullptr, h, nullptr,
+                                                           nullptr, tz, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, 4);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// convec.f90:67-114 vorticity inputs (already multiplied by 1/(nx*ny))
+__global__ void k_vort(const double* __restrict__ dudy, const double* __restrict__ dudz,
+                       const double* __restrict__ dvdx, const double* __restrict__ dvdz,
+                       const double* __restrict__ dwdx, const double* __restrict__ dwdy, double* o1,
+                       double* o2, double* o3, int ld, int ny, int nz, double cst) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    if (jz == 1) {  // lbc_mom = 'wall'
+      o1[i] = cst * (0.5 * (dwdy[i] + dwdy[i + np]) - dvdz[i]);
+      o2[i] = cst * (dudz[i] - 0.5 * (dwdx[i] + dwdx[i + np]));
+    } else {
+      o1[i] = cst * (dwdy[i] - dvdz[i]);
+      o2[i] = cst * (dudz[i] - dwdx[i]);
+    }
+    o3[i] = cst * (dvdx[i] - dudy[i]);
+  }
+}
+// convec.f90:117-217 products on the 3/2 grid, levels 1..nz-1
+__global__ void k_convec_prod(const double* __restrict__ u1, const double* __restrict__ u2,
+                              const double* __restrict__ u3, const double* __restrict__ w1,
+                              const double* __restrict__ w2, const double* __restrict__ w3, double* ccx,
+                              double* ccy, double* ccz, int ldb, int nx2, int ny2, int nz, double cst) {
+  const size_t np = (size_t)ldb * ny2;
+  GSTRIDE(i, np * (nz - 1)) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ldb);
+    if (jx >= nx2) continue;
+    const size_t ip = i + np;
+    if (jz == 1) {
+      ccx[i] = cst * (u2[i] * (-w3[i]) + 0.5 * u3[ip] * (w2[ip]));
+      ccy[i] = cst * (u1[i] * (w3[i]) + 0.5 * u3[ip] * (-w1[ip]));
+      ccz[i] = 0.0;
+    } else {
+      const size_t im = i - np;
+      ccx[i] = cst * (u2[i] * (-w3[i]) + 0.5 * (u3[ip] * (w2[ip]) + u3[i] * (w2[i])));
+      ccy[i] = cst * (u1[i] * (w3[i]) + 0.5 * (u3[ip] * (-w1[ip]) + u3[i] * (-w1[i])));
+      ccz[i] = cst * 0.5 * ((u1[i] + u1[im]) * (-w2[i]) + (u2[i] + u2[im]) * (w1[i]));
+    }
+  }
+}
+int op_convec(les_ctx* c, double* cx, double* cy, double* cz) {
+  const Grid& g = c->g;
+  const double cst = 1.0 / (double)(g.nx * g.ny);
+  double* vort[3] = {c->tmp, c->tmp + g.nfield, c->tmp + 2 * g.nfield};
+  k_vort<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDZ],
+                                                c->f[LES_DWDX], c->f[LES_DWDY], vort[0], vort[1], vort[2], g.ld,
+                                                g.ny, g.nz, cst);
+  const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], vort[0], vort[1], vort[2]};
+  double* bigf[9];
+  for (int q = 0; q < 9; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
+  // dealias1 semantics: scale 1/(nx*ny) for the velocities, vorticity already scaled
+  {
+    double sc[6] = {cst, cst, cst, 1.0, 1.0, 1.0};
+    r2c(c, 6, g.nz, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_PAD, DIR_BOTH, g.nz);
+    J.nin = 1; J.nout = 1; J.nf = 6;
+    J.in[0] = c->wsA; J.fs_in = (long)g.nz * g.C;
+    J.out[0] = c->wsB; J.fs_out = (long)g.nz * g.CB;
+    J.coef[0][0] = CC_ONE;
+    cols(c, J);
+    c2r(c, 6, g.nz, c->wsB, bigf, (long)g.nplane_big, true, g.nx / 2);
+  }
+  const double cst2 = 1.0 / (double)(g.nx2 * g.ny2);
+  k_convec_prod<<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
+      bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5], bigf[6], bigf[7], bigf[8], g.ld_big, g.nx2, g.ny2,
+      g.nz, cst2);
+  double* outs[3] = {cx, cy, cz};
+  const double* bins[3] = {bigf[6], bigf[7], bigf[8]};
+  op_dealias2(c, outs, bins, 3, g.nz - 1, 1.0);
+  const size_t top = (size_t)(g.nz - 1) * g.nplane;
+  fill(c, cx + top, g.nplane, LES_BOGUS);
+  fill(c, cy + top, g.nplane, LES_BOGUS);
+  fill(c, cz + top, g.nplane, LES_BOGUS);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// main.f90:309-390 : RHS assembly, buoyancy, Euler/AB2 predictor, u(nz)=BOGUS
+__global__ void k_rhs_ab2(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz, double* Rxf,
+                          double* Ryf, double* Rzf, const double* __restrict__ dx_, const double* __restrict__ dy_,
+                          const double* __restrict__ dz_, const double* __restrict__ bs, size_t nv, size_t np,
+                          double dt, int sflag, int euler) {
+  GSTRIDE(i, nv + np) {
+    if (i >= nv) { u[i] = LES_BOGUS; v[i] = LES_BOGUS; w[i] = LES_BOGUS; continue; }
+    const double rx = -Rx[i] - dx_[i];
+    const double ry = -Ry[i] - dy_[i];
+    double rz = -Rz[i] - dz_[i];
+    if (sflag) rz = rz + bs[i];
+    Rx[i] = rx; Ry[i] = ry; Rz[i] = rz;
+    double fx = Rxf[i], fy = Ryf[i], fz = Rzf[i];
+    if (euler) { fx = rx; fy = ry; fz = rz; Rxf[i] = rx; Ryf[i] = ry; Rzf[i] = rz; }
+    u[i] = u[i] + dt * (1.5 * rx + (1.0 - 1.5) * fx + 0.0);
+    v[i] = v[i] + dt * (1.5 * ry + (1.0 - 1.5) * fy);
+    w[i] = w[i] + dt * (1.5 * rz + (1.0 - 1.5) * fz);
+  }
+}
+
+// main.f90:403-410 + forcing.f90:128-219 project, one thread per (jx,jy)
+__global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz,
+                               const double* __restrict__ p, const double* __restrict__ dpdx,
+                               const double* __restrict__ dpdy, double* dpdz, int ld, int nx, int ny, int nz,
+                               double dz, double dt) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(r, np) {
+    const int jx = (int)(r % ld);
+    for (int jz = 1; jz <= nz - 1; ++jz) {
+      const size_t i = r + (size_t)(jz - 1) * np;
+      double pz = 0.0;
+      if (jx < nx) {
+        pz = (p[r + (size_t)jz * np] - p[r + (size_t)(jz - 1) * np]) / dz;
+        dpdz[i] = pz;
+      }
+      Rx[i] = Rx[i] - dpdx[i];
+      Ry[i] = Ry[i] - dpdy[i];
+      Rz[i] = Rz[i] - dpdz[i];
+      if (jx < nx) {
+        u[i] = (u[i] + dt * (-1.5 * dpdx[i] + 0.0));
+        v[i] = (v[i] + dt * (-1.5 * dpdy[i] + 0.0));
+        if (jz >= 2) w[i] = (w[i] + dt * (-1.5 * pz + 0.0));
+      }
+    }
+    const size_t top = r + (size_t)(nz - 1) * np, below = r + (size_t)(nz - 2) * np;
+    dpdz[top] = LES_BOGUS;
+    u[top] = u[below];
+    v[top] = v[below];
+    w[top] = 0.0;
+    w[r] = 0.0;
+  }
+}
+__global__ void k_project_only(double* u, double* v, double* w, const double* dpdx, const double* dpdy,
+                               const double* dpdz, int ld, int nx, int ny, int nz, double dt) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(r, np) {
+    const int jx = (int)(r % ld);
+    for (int jz = 1; jz <= nz - 1; ++jz) {
+      const size_t i = r + (size_t)(jz - 1) * np;
+      if (jx < nx) {
+        u[i] = (u[i] + dt * (-1.5 * dpdx[i] + 0.0));
+        v[i] = (v[i] + dt * (-1.5 * dpdy[i] + 0.0));
+        if (jz >= 2) w[i] = (w[i] + dt * (-1.5 * dpdz[i] + 0.0));
+      }
+    }
+    const size_t top = r + (size_t)(nz - 1) * np, below = r + (size_t)(nz - 2) * np;
+    u[top] = u[below];
+    v[top] = v[below];
+    w[top] = 0.0;
+    w[r] = 0.0;
+  }
+}
+
+int op_project(les_ctx* c) {
+  // stand-alone project (forcing.f90:128-219): dpdz is taken as given
+  const Grid& g = c->g;
+  k_project_only<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DPDX],
+                                                        c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz,
+                                                        c->cfg.dt);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// press_stag_array.f90:192-264 + tridag_array.f90:1-109: one thread per
+// wavenumber pair solves its z-tridiagonal (Thomas), building the RHS rows
+// from the spectra H on the fly.  Spectra are (level, ny, lh) complex.
+__global__ void k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy, const C2* __restrict__ Hz,
+                          const C2* __restrict__ bot, const C2* __restrict__ top, C2* P, double* gam,
+                          const double* __restrict__ kx, const double* __restrict__ ky, int lh, int ny, int nz,
+                          double dz, int* flag) {
+  const int nk = lh * ny;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nk) return;
+  const int jx = t % lh, jy = t / lh;
+  const size_t NK = (size_t)nk;
+  // Hz(nz) = 0 ; H levels are uvp 1..nz-1 at spectral index (lev-1)
+  auto HZ = [&](int lev) -> C2 { return (lev >= 1 && lev <= nz - 1) ? Hz[(size_t)(lev - 1) * NK + t] : make_double2(0.0, 0.0); };
+  if (jy == ny / 2 || jx == lh - 1) {  // Nyquist modes: zeroed (press_stag_array.f90:263-264)
+    for (int j = 0; j <= nz; ++j) P[(size_t)j * NK + t] = make_double2(0.0, 0.0);
+    return;
+  }
+  if (t == 0) {  // kx = ky = 0 : direct integration (:238-247)
+    C2 p = make_double2(0.0, 0.0);
+    P[0] = p;
+    const C2 b = bot[0];
+    C2 p1; p1.x = p.x - dz * b.x; p1.y = p.y - dz * b.y;
+    P[NK] = p1;
+    p = p1;
+    for (int jz = 2; jz <= nz; ++jz) {
+      const C2 h = HZ(jz);
+      p.x = p.x + h.x * dz; p.y = p.y + h.y * dz;
+      P[(size_t)jz * NK] = p;
+    }
+    return;
+  }
+  const double k_x = kx[t], k_y = ky[t];
+  const double idz2 = 1.0 / (dz * dz);
+  const double bmid = -(k_x * k_x + k_y * k_y + 2.0 / (dz * dz));
+  const int n = nz + 1;
+  // row 1: a = BOGUS, b = -1, c = 1, r = -dz * bottomw
+  double bet = -1.0;
+  C2 r1 = bot[t];
+  C2 up; up.x = (-dz * r1.x) / bet; up.y = (-dz * r1.y) / bet;
+  P[t] = up;
+  double cprev = 1.0;
+  C2 hz0 = HZ(1);
+  for (int j = 2; j <= n; ++j) {
+    double a, b;
+    C2 r;
+    if (j <= nz) {
+      a = idz2; b = bmid;
+      const C2 hx = Hx[(size_t)(j - 2) * NK + t];
+      const C2 hy = Hy[(size_t)(j - 2) * NK + t];
+      const C2 hz1 = HZ(j);
+      const double sr = k_x * hx.x + k_y * hy.x;
+      const double si = k_x * hx.y + k_y * hy.y;
+      r.x = -si + (hz1.x - hz0.x) / dz;
+      r.y = sr + (hz1.y - hz0.y) / dz;
+      hz0 = hz1;
+    } else {
+      a = -1.0; b = 1.0;
+      const C2 tp = top[t];
+      r.x = -tp.x * dz; r.y = -tp.y * dz;
+    }
+    const double gm = cprev / bet;
+    gam[(size_t)(j - 1) * NK + t] = gm;
+    bet = b - a * gm;
+    if (bet == 0.0) atomicOr(flag, 1);
+    C2 u; u.x = (r.x - a * up.x) / bet; u.y = (r.y - a * up.y) / bet;
+    P[(size_t)(j - 1) * NK + t] = u;
+    up = u;
+    cprev = (j <= nz) ? idz2 : 0.0;
+  }
+  for (int j = n - 1; j >= 1; --j) {
+    const double gm = gam[(size_t)j * NK + t];
+    C2 u = P[(size_t)(j - 1) * NK + t];
+    u.x = u.x - gm * up.x; u.y = u.y - gm * up.y;
+    P[(size_t)(j - 1) * NK + t] = u;
+    up = u;
+  }
+}
+
+int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  const int nz = g.nz;
+  const double cst = 1.0 / (double)(g.nx * g.ny);
+  // spectra of u*, v*, w* (levels 1..nz-1), (const/tadv1)*(u/dt)
+  const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  const double sc3[3] = {cst / 1.5, cst / 1.5, cst / 1.5};
+  const double dv3[3] = {k.dt, k.dt, k.dt};
+  r2c(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
+  C2* H = (C2*)c->wsP;                        // 3*(nz-1)*C
+  C2* BT = H + (size_t)3 * (nz - 1) * g.C;   // bottom, top
+  C2* P = BT + 2 * g.C;                       // (nz+1)*C
+  double* gam = (double*)(P + (size_t)(nz + 1) * g.C);  // (nz+1)*C doubles
+  ColJob J = coljob(c, MAP_SAME, DIR_FWD, nz - 1);
+  J.nin = 1; J.nout = 1; J.nf = 3;
+  J.in[0] = c->wsA; J.fs_in = (long)(nz - 1) * g.C;
+  J.out[0] = H; J.fs_out = (long)(nz - 1) * g.C;
+  J.coef[0][0] = CC_KILL;
+  cols(c, J);
+  // bottomw, topw from divtz(1), divtz(nz) scaled by 1/(nx*ny)
+  {
+    const double* bi[2] = {c->f[LES_DIVTZ], c->f[LES_DIVTZ] + (size_t)(nz - 1) * g.nplane};
+    const double sc2[2] = {cst, cst};
+    r2c(c, 2, 1, bi, (long)g.nplane, sc2, nullptr, (C2*)c->wsA, false, g.lh);
+    ColJob K = coljob(c, MAP_SAME, DIR_FWD, 1);
+    K.nin = 1; K.nout = 1; K.nf = 2;
+    K.in[0] = c->wsA; K.fs_in = (long)g.C;
+    K.out[0] = BT; K.fs_out = (long)g.C;
+    K.coef[0][0] = CC_KILL;
+    cols(c, K);
+  }
+  int* flag = reinterpret_cast<int*>(c->dscal + 8);
+  k_tridiag<<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(H, H + (size_t)(nz - 1) * g.C,
+                                                              H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, gam,
+                                                              c->kx, c->ky, g.lh, g.ny, nz, g.dz, flag);
+  // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
+  {
+    ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
+    K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
+    cols(c, K);
+    ColJob L = coljob(c, MAP_SAME, DIR_INV, nz - 1);
+    L.nin = 1; L.nout = 3; L.in[0] = P + g.C;
+    L.out[0] = (C2*)c->wsB + g.C;
+    L.out[1] = (C2*)c->wsB + g.C + (size_t)(nz - 1) * g.C;
+    L.out[2] = (C2*)c->wsB + g.C + (size_t)2 * (nz - 1) * g.C;
+    L.coef[0][0] = CC_ONE; L.coef[1][0] = CC_IKX; L.coef[2][0] = CC_IKY;
+    cols(c, L);
+    double* o0 = p;
+    c2r(c, 1, 1, c->wsB, &o0, (long)g.nplane, false, g.lh);
+    double* o1[3] = {p + g.nplane, dpdx, dpdy};
+    c2r(c, 3, nz - 1, (C2*)c->wsB + g.C, o1, (long)g.nplane, false, g.lh);
+  }
+  fill(c, dpdx + (size_t)(nz - 1) * g.nplane, g.nplane, LES_BOGUS);
+  fill(c, dpdy + (size_t)(nz - 1) * g.nplane, g.nplane, LES_BOGUS);
+  fill(c, p + (size_t)nz * g.nplane, g.nplane, LES_BOGUS);
+  return 0;
+}
+
+// tridag_array.f90:1-109 with caller-supplied coefficients (per-routine entry)
+__global__ void k_tridag_generic(const double* a, const double* b, const double* cc, const C2* r, C2* u,
+                                 double* gam, int lh, int ny, int n, int* flag) {
+  const int nk = lh * ny;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nk) return;
+  const int jx = t % lh, jy = t / lh;
+  const size_t NK = (size_t)nk;
+  double bet = b[t];
+  C2 up; up.x = r[t].x / bet; up.y = r[t].y / bet;
+  u[t] = up;
+  if (jy == ny / 2 || jx == lh - 1 || t == 0) return;
+  for (int j = 2; j <= n; ++j) {
+    const size_t o = (size_t)(j - 1) * NK + t;
+    const double gm = cc[o - NK] / bet;
+    gam[o] = gm;
+    bet = b[o] - a[o] * gm;
+    if (bet == 0.0) atomicOr(flag, 1);
+    C2 x; x.x = (r[o].x - a[o] * up.x) / bet; x.y = (r[o].y - a[o] * up.y) / bet;
+    u[o] = x;
+    up = x;
+  }
+  for (int j = n - 1; j >= 1; --j) {
+    const size_t o = (size_t)(j - 1) * NK + t;
+    const double gm = gam[o + NK];
+    C2 x = u[o];
+    x.x = x.x - gm * up.x; x.y = x.y - gm * up.y;
+    u[o] = x;
+    up = x;
+  }
+}
+int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, const double* r, double* u) {
+  const Grid& g = c->g;
+  int* flag = reinterpret_cast<int*>(c->dscal + 8);
+  double* gam = (double*)c->wsA;
+  k_tridag_generic<<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(a, b, cc, (const C2*)r, (C2*)u, gam, g.lh, g.ny,
+                                                                    g.nz + 1, flag);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// scalars_module.f90:254-283 surface flux and dsdz(1)
+__global__ void k_sflux(const double* __restrict__ theta, const double* __restrict__ wt_s,
+                        const double* __restrict__ phi_h, const double* __restrict__ ustar, double* dTdz,
+                        double* sgs_t3, int nx, int ny, int ld, double tsus, double vonk, double dz) {
+  GSTRIDE(s, (size_t)nx * ny) {
+    const int jy = (int)(s / nx), jx = (int)(s - (size_t)jy * nx);
+    const double sf = (theta[0] < 2.0) ? wt_s[s] / tsus : 0.0;
+    dTdz[(size_t)jy * ld + jx] = -phi_h[s] * sf / (ustar[s] * vonk * dz / 2.0);
+    sgs_t3[s] = sf;
+  }
+}
+// scalars_module.f90:321-346 advection product on the 3/2 grid
+__global__ void k_scalar_prod(const double* __restrict__ um, const double* __restrict__ vm,
+                              const double* __restrict__ wm, const double* __restrict__ sx,
+                              const double* __restrict__ sy, const double* __restrict__ sz, double* R, int ldb,
+                              int nx2, int ny2, int nz) {
+  const size_t np = (size_t)ldb * ny2;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ldb);
+    if (jx >= nx2) continue;
+    if (jz == 1) R[i] = um[i] * sx[i] + vm[i] * sy[i] + (0.5 * wm[i + np]) * sz[i + np];
+    else if (jz == nz) R[i] = um[i] * sx[i] + vm[i] * sy[i];
+    else R[i] = um[i] * sx[i] + vm[i] * sy[i] + (wm[i] * sz[i] + wm[i + np] * sz[i + np]) / 2.0;
+  }
+}
+// scalars_module.f90:364-407 horizontal SGS fluxes
+__global__ void k_scalar_temp_xy(const double* __restrict__ nut, const double* __restrict__ dsx,
+                                 const double* __restrict__ dsy, double* tx, double* ty, int ld, int nx, int ny,
+                                 int nz, double pr) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
+    if (jx >= nx) continue;
+    if (jz == nz) { tx[i] = 0.0; ty[i] = 0.0; continue; }
+    if (jz == 1) {
+      tx[i] = (1.0 / pr) * nut[i] * dsx[i];
+      ty[i] = (1.0 / pr) * nut[i] * dsy[i];
+    } else {
+      const double f = (1.0 / (0.5 * (pr + pr))) * 0.5 * (nut[i] + nut[i + np]);
+      tx[i] = f * dsx[i];
+      ty[i] = f * dsy[i];
+    }
+  }
+}
+// scalars_module.f90:385-452 RHS assembly with the SGS divergence
+__global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const double* __restrict__ nut,
+                             const double* __restrict__ dsz, const double* __restrict__ sgs_t3, int ld, int nx,
+                             int ny, int nz, double pr, double cdz) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * (nz - 1)) {
+    const int jz = (int)(i / np) + 1;
+    const size_t r = i - (size_t)(jz - 1) * np;
+    const int jx = (int)(r % ld);
+    if (jx >= nx) continue;
+    const int jy = (int)(r / ld);
+    // temp(k) = Nu_t dsdz / Pr on w-nodes, temp(1) = -surf_flux
+    const double t0 = (jz == 1) ? -1.0 * sgs_t3[(size_t)jy * nx + jx] : (1.0 / pr) * nut[i] * dsz[i];
+    const double t1 = (1.0 / pr) * nut[i + np] * dsz[i + np];
+    R[i] = (-1.0 * R[i] + dxy[i]) + cdz * (t1 - t0);
+  }
+}
+// scalars_module.f90:175-228 calcbeta from per-level plane sums
+__global__ void k_calcbeta(const double* __restrict__ theta, const double* __restrict__ sums, double* bs, int ld,
+                           int nx, int ny, int nz, double g_hat, double nxny) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    const int jz = (int)(i / np) + 1;
+    const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
+    if (jz == 1 || jz == nz || jx >= nx) { bs[i] = 0.0; continue; }
+    const double sb = sums[jz - 1] / nxny, sbm = sums[jz - 2] / nxny;
+    const double above = (theta[i] * 1.0 - sb) / sb;
+    const double below = (theta[i - np] * 1.0 - sbm) / sbm;
+    bs[i] = g_hat * (above + below) / 2.0;
+  }
+}
+// scalars_module.f90:457-504 step_scalar
+__global__ void k_step_scalar(double* theta, const double* __restrict__ R, const double* __restrict__ Rf, int ld,
+                              int nx, int ny, int nz, double dt, int top_grad, double inc) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(r, np) {
+    const int jx = (int)(r % ld);
+    if (jx < nx)
+      for (int jz = 1; jz <= nz - 1; ++jz) {
+        const size_t i = r + (size_t)(jz - 1) * np;
+        theta[i] = theta[i] + dt * (1.5 * R[i] - 0.5 * Rf[i]);
+      }
+    const size_t top = r + (size_t)(nz - 1) * np, below = r + (size_t)(nz - 2) * np;
+    theta[top] = top_grad ? theta[below] + inc : theta[below];
+  }
+}
+// scalars_module.f90:57-171 theta_all_in_one (S_FLAG, lbc = 1, model 5 Pr)
+int op_theta(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  const int nz = g.nz;
+  op_filt_da(c, c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY], nz);
+  op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
+  fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
+  // RHS_Tf = RHS_T (pointer swap; RHS_T is fully rewritten below)
+  std::swap(c->f[LES_RHS_T], c->f[LES_RHS_TF]);
+  k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
+                                                            c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
+                                                            c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
+                                                            k.t_scale * k.u_star, k.vonk, g.dz);
+  double* bigf[7];
+  for (int q = 0; q < 7; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
+  const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DTDX], c->f[LES_DTDY], c->f[LES_DTDZ]};
+  op_dealias1(c, in, bigf, 6, nz);
+  k_scalar_prod<<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
+                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz);
+  double* rt = c->f[LES_RHS_T];
+  const double* b6 = bigf[6];
+  op_dealias2(c, &rt, &b6, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+  // horizontal SGS flux divergence (ddx + ddy summed in spectral space)
+  double* tx = c->tmp;
+  double* ty = c->tmp + g.nfield;
+  double* dxy = c->tmp + 2 * g.nfield;
+  k_scalar_temp_xy<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
+                                                          g.ld, g.nx, g.ny, nz, k.pr);
+  {
+    const double sc = 1.0 / (double)(g.nx * g.ny);
+    const double* ii[2] = {tx, ty};
+    const double s2[2] = {sc, sc};
+    r2c(c, 2, nz, ii, (long)g.nplane, s2, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+    J.nin = 2; J.nout = 1; J.in[0] = c->wsA; J.in[1] = (C2*)c->wsA + (size_t)nz * g.C; J.out[0] = c->wsB;
+    J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
+    cols(c, J);
+    c2r(c, 1, nz, c->wsB, &dxy, (long)g.nplane, false, g.lh);
+  }
+  k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
+                                                                 c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
+                                                                 1.0 / g.dz);
+  // calcbeta on theta before the update
+  k_plane_sum<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred);
+  const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
+  k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], c->dred, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
+                                                    nz, g_hat, (double)(g.nx * g.ny));
+  if (c->jt == 1 && !k.initsc)
+    cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
+                    c->stream);
+  const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
+  k_step_scalar<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx,
+                                                       g.ny, nz, k.dt, topg, k.dtdz_top / k.t_scale * k.z_i * g.dz);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// rmsdiv.f90:93-100 (deterministic two-level sum) and timestep_conditions
+__global__ void __launch_bounds__(512) k_rmsdiv_part(const double* __restrict__ du, const double* __restrict__ dv,
+                                                     const double* __restrict__ dw, double* part, int ld, int nx,
+                                                     int ny) {
+  __shared__ double sh[512];
+  const size_t o = (size_t)blockIdx.x * ld * ny;
+  double s = 0.0;
+  for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
+    const int jy = e / nx, jx = e - jy * nx;
+    const size_t i = o + (size_t)jy * ld + jx;
+    s += fabs(du[i] + dv[i] + dw[i]);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 256; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+__global__ void k_rmsdiv_fin(const double* part, int n, double denom, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += part[i];
+    out[0] = s / denom;
+  }
+}
+int op_rmsdiv(les_ctx* c, double* out_dev) {
+  const Grid& g = c->g;
+  double* part = c->dred;
+  k_rmsdiv_part<<<g.nz - 1, 512, 0, c->stream>>>(c->f[LES_DUDX], c->f[LES_DVDY], c->f[LES_DWDZ], part, g.ld, g.nx,
+                                                g.ny);
+  k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev);
+  return 0;
+}
+__global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const double* __restrict__ v,
+                                             const double* __restrict__ w, const double* __restrict__ nut,
+                                             double* out, int ld, int nx, int ny, int nz) {
+  __shared__ double s1[512], s2[512];
+  double m1 = -1e300, m2 = -1e300;
+  const size_t n = (size_t)nx * ny * (nz - 1);
+  for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const size_t jx = e % nx, r = e / nx;
+    const size_t i = jx + (size_t)ld * r;
+    m1 = fmax(m1, u[i] * u[i] + v[i] * v[i] + w[i] * w[i]);
+    m2 = fmax(m2, nut[i]);
+  }
+  s1[threadIdx.x] = m1; s2[threadIdx.x] = m2;
+  __syncthreads();
+  for (int k = 256; k > 0; k >>= 1) {
+    if (threadIdx.x < k) {
+      s1[threadIdx.x] = fmax(s1[threadIdx.x], s1[threadIdx.x + k]);
+      s2[threadIdx.x] = fmax(s2[threadIdx.x], s2[threadIdx.x + k]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[0] = s1[0]; out[1] = s2[0]; }
+}
+int op_tsc(les_ctx* c, double* cflu, double* visc) {
+  const Grid& g = c->g;
+  k_tsc<<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_NU_T], c->dscal + 2, g.ld, g.nx,
+                                  g.ny, g.nz);
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 2, c->dscal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  const double delta = std::min(g.dx, g.dy);
+  *cflu = std::sqrt(c->host_scal[2]) * c->cfg.dt / g.dx;
+  *visc = c->cfg.dt * c->host_scal[3] / (delta * delta);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// main.f90:202-478, one iteration on the device-resident state
+int step_fp64(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  c->jt += 1;
+  c->jt_total += 1;
+  // RHS*_f = RHS* (main.f90:212-214): pointer swap, RHS* is fully rewritten by convec
+  std::swap(c->f[LES_RHSX], c->f[LES_RHSX_F]);
+  std::swap(c->f[LES_RHSY], c->f[LES_RHSY_F]);
+  std::swap(c->f[LES_RHSZ], c->f[LES_RHSZ_F]);
+  op_obukhov(c);
+  {
+    double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+    double* x3[3] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX]};
+    double* y3[3] = {c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
+    filt_da_multi(c, f3, x3, y3, 3, g.nz);
+  }
+  op_ddz(c, c->f[LES_DUDZ], c->f[LES_U], 1);
+  op_ddz(c, c->f[LES_DVDZ], c->f[LES_V], 1);
+  op_ddz(c, c->f[LES_DWDZ], c->f[LES_W], 0);
+  op_wallstress(c);
+  op_sgs_stag(c);
+  if (k.s_flag) op_theta(c);
+  else fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
+  op_divstress(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
+  op_convec(c, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
+  const size_t nv = g.nplane * (g.nz - 1);
+  k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
+      c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
+      c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL], nv,
+      g.nplane, k.dt, k.s_flag, (c->jt == 1 && !k.initu) ? 1 : 0);
+  op_press(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
+  k_dpdz_project<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
+                                                        c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX],
+                                                        c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
+                                                        k.dt);
+  LES_CUDA_CHECK(cudaGetLastError());
+  if (k.rmsdiv_every > 0 && c->jt % k.rmsdiv_every == 0) {
+    op_rmsdiv(c, c->dscal + 1);
+    LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 1, c->dscal + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    double cflu, visc;
+    int st = op_tsc(c, &cflu, &visc);
+    if (st) return st;
+    c->rmsdiv_last = c->host_scal[1];
+    if (cflu > 0.1 || cflu < 0.0) return LES_ERR_CFL;
+  }
+  return 0;
+}
+
+}  // namespace les

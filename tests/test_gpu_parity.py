@@ -1,0 +1,143 @@
+"""GPU (sm_103a library, through the C ABI) vs the CPU oracle on identical
+seeded inputs.  FP64 form: relative error <= 1e-12 on u, v, w, theta, Cs^2
+and rmsdiv (the benchmark spec's tolerance); routine-level checks at rounding level.
+"""
+import numpy as np
+import pytest
+
+import les_gb300 as lg
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def interior(cfg, a, lev=slice(0, -1)):
+    return a[lev, :, :cfg.nx]
+
+
+def pair(cfg, surf, seed=11):
+    from oracle.oracle import Oracle
+    st = lg.initial_state(cfg, surf, seed=seed)
+    g = lg.Context(cfg, surf)
+    o = Oracle(cfg, surf)
+    for k, v in st.items():
+        g.set(k, v)
+        o.set(k, v)
+    return g, o
+
+
+@pytest.fixture(scope="module")
+def libs(gpu_lib, oracle_lib):
+    return gpu_lib, oracle_lib
+
+
+@pytest.mark.parametrize("n", [32, 48])
+def test_fft_roundtrip_and_spectra(libs, n):
+    from oracle.oracle import Oracle
+    cfg = lg.make_config(n, n, 4)
+    d = lg.dims(cfg)
+    g = lg.Context(cfg)
+    o = Oracle(cfg)
+    rng = np.random.default_rng(3)
+    for big, nn, ld in [(0, n, d["ld"]), (1, 3 * n // 2, d["ld_big"])]:
+        x = rng.standard_normal((3, nn, ld))
+        a = x.copy(); b = x.copy()
+        g.call("fft_r2c", a, ints=(3, big))
+        o.call("fft_r2c", b, ints=(3, big))
+        assert rel(a, b) < 1e-14
+        g.call("fft_c2r", a, ints=(3, big))
+        o.call("fft_c2r", b, ints=(3, big))
+        assert rel(a[:, :, :nn], b[:, :, :nn]) < 1e-14
+        assert rel(a[:, :, :nn] / (nn * nn), x[:, :, :nn]) < 1e-14
+
+
+def test_derivatives_filters_dealias(libs):
+    from oracle.oracle import Oracle
+    cfg = lg.make_config(32, 32, 16)
+    d = lg.dims(cfg)
+    g = lg.Context(cfg)
+    o = Oracle(cfg)
+    rng = np.random.default_rng(5)
+    nz = cfg.nz
+    f = rng.standard_normal((nz, cfg.ny, d["ld"]))
+    for name in ["ddx", "ddy"]:
+        a = np.zeros_like(f); b = np.zeros_like(f)
+        g.call(name, a, f, ints=(nz,))
+        o.call(name, b, f, ints=(nz,))
+        assert rel(a[:, :, :32], b[:, :, :32]) < 1e-13, name
+    fa, fb = f.copy(), f.copy()
+    ax, ay = np.zeros_like(f), np.zeros_like(f)
+    bx, by = np.zeros_like(f), np.zeros_like(f)
+    g.call("filt_da", fa, ax, ay, ints=(nz,))
+    o.call("filt_da", fb, bx, by, ints=(nz,))
+    for p, q in [(fa, fb), (ax, bx), (ay, by)]:
+        assert rel(p[:, :, :32], q[:, :, :32]) < 1e-13
+    big_a = np.zeros((nz, d["ny2"], d["ld_big"]))
+    big_b = np.zeros_like(big_a)
+    g.call("dealias1", f, big_a, ints=(nz,))
+    o.call("dealias1", f.copy(), big_b, ints=(nz,))
+    assert rel(big_a[:, :, :d["nx2"]], big_b[:, :, :d["nx2"]]) < 1e-13
+    sa, sb = np.zeros_like(f), np.zeros_like(f)
+    g.call("dealias2", sa, big_a.copy(), ints=(nz,))
+    o.call("dealias2", sb, big_b.copy(), ints=(nz,))
+    assert rel(sa[:, :, :32], sb[:, :, :32]) < 1e-13
+
+
+def test_tridag_array(libs):
+    from oracle.oracle import Oracle
+    cfg = lg.make_config(16, 16, 12)
+    d = lg.dims(cfg)
+    g = lg.Context(cfg)
+    o = Oracle(cfg)
+    rng = np.random.default_rng(9)
+    n = cfg.nz + 1
+    shp = (n, cfg.ny, d["lh"])
+    a = rng.uniform(0.5, 1.0, shp); c = rng.uniform(0.5, 1.0, shp)
+    b = -(a + c + rng.uniform(0.1, 1.0, shp))
+    r = rng.standard_normal(shp + (2,))
+    ug = np.zeros_like(r); uo = np.zeros_like(r)
+    g.call("tridag_array", a, b, c, r, ug)
+    o.call("tridag_array", a, b, c, r, uo)
+    assert rel(ug, uo) < 1e-13
+
+
+@pytest.mark.parametrize("s_flag,jt0,model", [(0, 0, 5), (1, 0, 5), (1, 500, 5), (1, 500, 3)])
+def test_step_parity_32(libs, s_flag, jt0, model):
+    cfg = lg.make_config(32, s_flag=s_flag, jt_total0=jt0, model=model, rmsdiv_every=1)
+    surf = lg.striped_surface(cfg) if s_flag else lg.uniform_surface(cfg)
+    g, o = pair(cfg, surf)
+    for it in range(10):
+        g.step(1)
+        assert o.step(1) == 0
+    names = ["u", "v", "theta"] if s_flag else ["u", "v"]
+    for nm in names:
+        e = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
+        assert e < TOL, (nm, e)
+    e = rel(interior(cfg, g.get("w"), slice(None)), interior(cfg, o.get("w"), slice(None)))
+    assert e < TOL, ("w", e)
+    e = rel(interior(cfg, g.get("Cs_opt2")), interior(cfg, o.get("Cs_opt2")))
+    assert e < 1e-9, ("Cs_opt2", e)
+    rg, ro = g.rmsdiv(), o.rmsdiv()
+    assert abs(rg - ro) <= 1e-10 * max(abs(ro), 1e-300) + 1e-18, (rg, ro)
+
+
+def test_step_parity_128_theta(libs):
+    """128^3, active theta, striped z0 and heat flux; 20 steps."""
+    from oracle.oracle import Oracle
+    cfg = lg.make_config(128, s_flag=1, rmsdiv_every=10)
+    surf = lg.striped_surface(cfg)
+    g, o = pair(cfg, surf, seed=21)
+    Oracle.set_threads(max(1, Oracle.max_threads()))
+    g.step(20)
+    assert o.step(20) == 0
+    for nm in ["u", "v", "theta"]:
+        e = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
+        assert e < TOL, (nm, e)
+    e = rel(interior(cfg, g.get("w"), slice(None)), interior(cfg, o.get("w"), slice(None)))
+    assert e < TOL, ("w", e)
