@@ -112,6 +112,8 @@ size_t les_ctx_device_bytes(const les_ctx* ctx);
 /* Estimated device bytes for a configuration (admission control). */
 size_t les_estimate_device_bytes(const les_config* cfg);
 const char* les_last_error(void);
+/* Kernels launched by this library so far (all contexts, diagnostic). */
+unsigned long long les_kernel_launch_count(void);
 
 /* ---- state transfer ------------------------------------------------------ */
 /* bottombc.f90:23-59 (patches): zo = roughness / z_i (nondimensional), wt_s =

@@ -53,3 +53,7 @@ __device__ __forceinline__ double fmax32(double a, double b) {
   } while (0)
 
 void les_set_error(const char* fmt, ...);
+
+// Number of kernels this library has launched (diagnostic counter).
+extern unsigned long long g_les_launches;
+#define LES_COUNT_LAUNCH() (++g_les_launches)

@@ -206,7 +206,7 @@ int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(k_rows_r2c<T, TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(J, P, rpc);
+  k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -219,7 +219,7 @@ int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(k_rows_c2r<T, TOut>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_rows_c2r<T, TOut><<<grid, 256, sm, s>>>(J, P, rpc);
+  k_rows_c2r<T, TOut><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -232,7 +232,7 @@ int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, 
   dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(k_cols<T, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_cols<T, TX><<<grid, 256, sm, s>>>(J, Pin, Pout);
+  k_cols<T, TX><<<grid, 256, sm, s>>>(J, Pin, Pout); LES_COUNT_LAUNCH();
   return 0;
 }
 

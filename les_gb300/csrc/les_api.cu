@@ -8,6 +8,7 @@
 #include "les_internal.h"
 
 static thread_local char g_err[512] = "";
+unsigned long long g_les_launches = 0;
 void les_set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -169,6 +170,7 @@ using namespace les;
 extern "C" {
 
 const char* les_last_error(void) { return g_err; }
+unsigned long long les_kernel_launch_count(void) { return g_les_launches; }
 
 size_t les_estimate_device_bytes(const les_config* cfg) {
   if (!cfg) return 0;
@@ -663,7 +665,7 @@ int les_padd(les_ctx* c, double* u_big, const double* u, int nplanes) {
   const Grid& g = c->g;
   Arg B(c, u_big, g.nplane_big * nplanes), S(c, u, g.nplane * nplanes);
   CHK(B.alloc()); CHK(S.in());
-  k_padd<<<256, 256, 0, c->stream>>>((double2*)B.dev, (const double2*)S.dev, g.lh, g.ny, g.lh_big, g.ny2, g.nx, nplanes);
+  k_padd<<<256, 256, 0, c->stream>>>((double2*)B.dev, (const double2*)S.dev, g.lh, g.ny, g.lh_big, g.ny2, g.nx, nplanes); LES_COUNT_LAUNCH();
   CHK(B.out());
   return finish(c);
 }
@@ -672,7 +674,7 @@ int les_unpadd(les_ctx* c, double* cc, const double* cc_big, int nplanes) {
   const Grid& g = c->g;
   Arg S(c, cc, g.nplane * nplanes), B(c, cc_big, g.nplane_big * nplanes);
   CHK(S.alloc()); CHK(B.in());
-  k_unpadd<<<256, 256, 0, c->stream>>>((double2*)S.dev, (const double2*)B.dev, g.lh, g.ny, g.lh_big, g.ny2, g.nx, nplanes);
+  k_unpadd<<<256, 256, 0, c->stream>>>((double2*)S.dev, (const double2*)B.dev, g.lh, g.ny, g.lh_big, g.ny2, g.nx, nplanes); LES_COUNT_LAUNCH();
   CHK(S.out());
   return finish(c);
 }

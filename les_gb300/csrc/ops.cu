@@ -21,7 +21,7 @@ static inline dim3 grid1(size_t n, int bs = 256) {
 
 __global__ void k_fill(double* p, size_t n, double v) { GSTRIDE(i, n) p[i] = v; }
 static void fill(les_ctx* c, double* p, size_t n, double v) {
-  if (n) k_fill<<<grid1(n), 256, 0, c->stream>>>(p, n, v);
+  if (n) { k_fill<<<grid1(n), 256, 0, c->stream>>>(p, n, v); LES_COUNT_LAUNCH(); }
 }
 
 // ---------------------------------------------------------------------------
@@ -136,7 +136,7 @@ __global__ void k_ddz(double* __restrict__ dfdz, const double* __restrict__ f, i
 }
 int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv) {
   const Grid& g = c->g;
-  k_ddz<<<grid1(g.nfield), 256, 0, c->stream>>>(dfdz, f, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, uv);
+  k_ddz<<<grid1(g.nfield), 256, 0, c->stream>>>(dfdz, f, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, uv); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -321,11 +321,12 @@ int op_obukhov(les_ctx* c) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const size_t ns = (size_t)g.nx * g.ny;
-  if (c->jt == 1)  // SCAL_init = 1 (scalars_module.f90:525-542)
+  if (c->jt == 1) {  // SCAL_init = 1 (scalars_module.f90:525-542)
     k_obukhov_init<<<grid1(ns), 256, 0, c->stream>>>(c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PSI_H],
                                                      c->f[LES_PSI_H0], c->f[LES_SGS_T3_SFC], c->f[LES_WT_S],
-                                                     ns, k.initsc, k.u_star * k.t_scale);
-  k_plane_sum<<<1, 512, 0, c->stream>>>(c->f[LES_THETA], 0, g.ld, g.nx, g.ny, c->dscal + 0);
+                                                     ns, k.initsc, k.u_star * k.t_scale); LES_COUNT_LAUNCH();
+  }
+  k_plane_sum<<<1, 512, 0, c->stream>>>(c->f[LES_THETA], 0, g.ld, g.nx, g.ny, c->dscal + 0); LES_COUNT_LAUNCH();
   double* u1 = c->tmp;
   double* v1 = c->tmp + g.nplane;
   op_test_filter(c, u1, c->f[LES_U], 1, 1, (long)g.nplane);
@@ -335,7 +336,7 @@ int op_obukhov(les_ctx* c) {
                                               c->f[LES_SGS_T3_SFC], c->f[LES_USTAR_AVG], c->f[LES_PSI_M],
                                               c->f[LES_PSI_M0], c->f[LES_PSI_H], c->f[LES_PSI_H0],
                                               c->f[LES_PHI_M], c->f[LES_PHI_H], c->dscal + 0, g.nx, g.ny,
-                                              g.ld, g.dz, k.vonk, g_, (double)(float)(g.nx * g.ny));
+                                              g.ld, g.dz, k.vonk, g_, (double)(float)(g.nx * g.ny)); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -371,7 +372,7 @@ int op_wallstress(les_ctx* c) {
   k_wallstress<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(
       c->f[LES_U], c->f[LES_V], u1, v1, c->f[LES_ZO], c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PHI_M],
       c->f[LES_USTAR_AVG], c->f[LES_TXZ], c->f[LES_TYZ], c->f[LES_DUDZ], c->f[LES_DVDZ], g.nx, g.ny, g.ld,
-      g.dz, c->cfg.vonk);
+      g.dz, c->cfg.vonk); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -482,14 +483,14 @@ int op_sgs_stag(les_ctx* c) {
       c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
       c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
       c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
-      c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0);
+      c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0); LES_COUNT_LAUNCH();
   const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
   if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {  // sgs_stag.f90:120-160
     if (k.model == 3) {
       double* csz = c->dred;
       op_scaledep(c, csz, S);
       // Cs_opt2(:,:,jz) = ziko(jz)
-      k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield);
+      k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
     } else if (k.model == 5) {
       op_lagrange(c, S);
     }
@@ -503,10 +504,10 @@ int op_sgs_stag(les_ctx* c) {
   }
   const double delta = g.delta;
   k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
-                                               c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, delta * delta, ov, csov);
+                                               c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, delta * delta, ov, csov); LES_COUNT_LAUNCH();
   k_tau<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_NU_T],
                                                c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ],
-                                               c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz);
+                                               c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -577,7 +578,7 @@ int op_interpolag(les_ctx* c) {
   k_interpolag<<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
       c->f[LES_U_LAG], c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN],
       c->f[LES_F_NN], Fn[0], Fn[1], Fn[2], Fn[3], g.ld, g.nx, g.ny, g.nz, (double)k.cs_count, k.dt, g.dx, g.dy,
-      g.dz);
+      g.dz); LES_COUNT_LAUNCH();
   // interior values changed; padding columns are never read
   for (int q = 0; q < 4; ++q)
     cudaMemcpyAsync(c->f[LES_F_LM + q], Fn[q], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
@@ -707,7 +708,7 @@ int op_lagrange(les_ctx* c, const double* const* S) {
     double* flt = c->tmp + (size_t)21 * nch * g.nplane;  // 42 * nl planes
     k_lag_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W],
                                                            Sp, prep, g.ld, g.nx,
-                                                           g.ny, jz0, nl, g.nplane);
+                                                           g.ny, jz0, nl, g.nplane); LES_COUNT_LAUNCH();
     const double* in[21];
     for (int q = 0; q < 21; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
     r2c(c, 21, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
@@ -722,7 +723,7 @@ int op_lagrange(les_ctx* c, const double* const* S) {
     c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
     k_lag_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
-        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp);
+        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
   }
   // the level loop's pointer table must outlive the launches
   return 0;
@@ -894,7 +895,7 @@ int op_scaledep(les_ctx* c, double* cs_z, const double* const* S) {
     double* flt = c->tmp + (size_t)21 * nch * g.nplane;
     k_sd_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W],
                                                           Sp, prep, g.ld, g.nx, g.ny,
-                                                          jz0, nl, g.nplane);
+                                                          jz0, nl, g.nplane); LES_COUNT_LAUNCH();
     const double* in[21];
     for (int q = 0; q < 21; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
     r2c(c, 21, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
@@ -909,7 +910,7 @@ int op_scaledep(les_ctx* c, double* cs_z, const double* const* S) {
     c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
     // Q_ij inputs: products of the G-filtered velocities, then GG-filtered
     double* qin = prep;  // reuse: 6 * nl planes
-    k_sd_qprep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(flt, qin, nl, g.nplane);
+    k_sd_qprep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(flt, qin, nl, g.nplane); LES_COUNT_LAUNCH();
     const double* qi[6];
     double* qo[6];
     for (int q = 0; q < 6; ++q) { qi[q] = qin + (size_t)q * nl * g.nplane; qo[q] = prep + (size_t)(6 + q) * nl * g.nplane; }
@@ -920,8 +921,8 @@ int op_scaledep(les_ctx* c, double* cs_z, const double* const* S) {
     cols(c, K);
     c2r(c, 6, nl, c->wsB, qo, (long)g.nplane, false, g.lh);
     k_sd_sums<<<nl, 256, 0, c->stream>>>(flt, prep + (size_t)6 * nl * g.nplane, sums, g.ld, g.nx, g.ny, nl,
-                                         g.nplane, jz0);
-    k_sd_final<<<nl, 256, 0, c->stream>>>(flt, sums, cs_z, g.ld, g.nx, g.ny, nl, g.nplane, jz0, g.delta);
+                                         g.nplane, jz0); LES_COUNT_LAUNCH();
+    k_sd_final<<<nl, 256, 0, c->stream>>>(flt, sums, cs_z, g.ld, g.nx, g.ny, nl, g.nplane, jz0, g.delta); LES_COUNT_LAUNCH();
   }
   return 0;
 }
@@ -980,7 +981,7 @@ int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz) {
   c2r(c, 3, g.nz, c->wsB, h, (long)g.nplane, false, g.lh);
   k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divtx, divty, divtz, h[0], h[1], h[2], c->f[LES_TXZ],
                                                          c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz,
-                                                         1.0 / g.dz, 7);
+                                                         1.0 / g.dz, 7); LES_COUNT_LAUNCH();
   return 0;
 }
 // single divstress call with caller-supplied stresses (per-routine entry point)
@@ -999,12 +1000,13 @@ int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* t
   cols(c, J);
   double* h = c->tmp;
   c2r(c, 1, g.nz, c->wsB, &h, (long)g.nplane, false, g.lh);
-  if (!w_variant)
+  if (!w_variant) {
     k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divt, nullptr, nullptr, h, nullptr, nullptr, tz, nullptr,
-                                                           nullptr, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, 1);
-  else
+                                                           nullptr, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, 1); LES_COUNT_LAUNCH();
+  } else {
     k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(nullptr, nullptr, divt, nullptr, nullptr, h, nullptr,
-                                                           nullptr, tz, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, 4);
+                                                           nullptr, tz, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, 4); LES_COUNT_LAUNCH();
+  }
   return 0;
 }
 
@@ -1056,7 +1058,7 @@ int op_convec(les_ctx* c, double* cx, double* cy, double* cz) {
   double* vort[3] = {c->tmp, c->tmp + g.nfield, c->tmp + 2 * g.nfield};
   k_vort<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDZ],
                                                 c->f[LES_DWDX], c->f[LES_DWDY], vort[0], vort[1], vort[2], g.ld,
-                                                g.ny, g.nz, cst);
+                                                g.ny, g.nz, cst); LES_COUNT_LAUNCH();
   const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], vort[0], vort[1], vort[2]};
   double* bigf[9];
   for (int q = 0; q < 9; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
@@ -1075,7 +1077,7 @@ int op_convec(les_ctx* c, double* cx, double* cy, double* cz) {
   const double cst2 = 1.0 / (double)(g.nx2 * g.ny2);
   k_convec_prod<<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
       bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5], bigf[6], bigf[7], bigf[8], g.ld_big, g.nx2, g.ny2,
-      g.nz, cst2);
+      g.nz, cst2); LES_COUNT_LAUNCH();
   double* outs[3] = {cx, cy, cz};
   const double* bins[3] = {bigf[6], bigf[7], bigf[8]};
   op_dealias2(c, outs, bins, 3, g.nz - 1, 1.0);
@@ -1165,7 +1167,7 @@ int op_project(les_ctx* c) {
   const Grid& g = c->g;
   k_project_only<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DPDX],
                                                         c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz,
-                                                        c->cfg.dt);
+                                                        c->cfg.dt); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -1284,7 +1286,7 @@ int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
   int* flag = reinterpret_cast<int*>(c->dscal + 8);
   k_tridiag<<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(H, H + (size_t)(nz - 1) * g.C,
                                                               H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, gam,
-                                                              c->kx, c->ky, g.lh, g.ny, nz, g.dz, flag);
+                                                              c->kx, c->ky, g.lh, g.ny, nz, g.dz, flag); LES_COUNT_LAUNCH();
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
@@ -1344,7 +1346,7 @@ int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, co
   int* flag = reinterpret_cast<int*>(c->dscal + 8);
   double* gam = (double*)c->wsA;
   k_tridag_generic<<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(a, b, cc, (const C2*)r, (C2*)u, gam, g.lh, g.ny,
-                                                                    g.nz + 1, flag);
+                                                                    g.nz + 1, flag); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -1454,13 +1456,13 @@ int op_theta(les_ctx* c) {
   k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
                                                             c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
                                                             c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
-                                                            k.t_scale * k.u_star, k.vonk, g.dz);
+                                                            k.t_scale * k.u_star, k.vonk, g.dz); LES_COUNT_LAUNCH();
   double* bigf[7];
   for (int q = 0; q < 7; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
   const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DTDX], c->f[LES_DTDY], c->f[LES_DTDZ]};
   op_dealias1(c, in, bigf, 6, nz);
   k_scalar_prod<<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
-                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz);
+                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
   double* rt = c->f[LES_RHS_T];
   const double* b6 = bigf[6];
   op_dealias2(c, &rt, &b6, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
@@ -1469,7 +1471,7 @@ int op_theta(les_ctx* c) {
   double* ty = c->tmp + g.nfield;
   double* dxy = c->tmp + 2 * g.nfield;
   k_scalar_temp_xy<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
-                                                          g.ld, g.nx, g.ny, nz, k.pr);
+                                                          g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
   {
     const double sc = 1.0 / (double)(g.nx * g.ny);
     const double* ii[2] = {tx, ty};
@@ -1483,18 +1485,18 @@ int op_theta(les_ctx* c) {
   }
   k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
                                                                  c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
-                                                                 1.0 / g.dz);
+                                                                 1.0 / g.dz); LES_COUNT_LAUNCH();
   // calcbeta on theta before the update
-  k_plane_sum<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred);
+  k_plane_sum<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred); LES_COUNT_LAUNCH();
   const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
   k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], c->dred, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
-                                                    nz, g_hat, (double)(g.nx * g.ny));
+                                                    nz, g_hat, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
   if (c->jt == 1 && !k.initsc)
     cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
   const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
   k_step_scalar<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx,
-                                                       g.ny, nz, k.dt, topg, k.dtdz_top / k.t_scale * k.z_i * g.dz);
+                                                       g.ny, nz, k.dt, topg, k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -1530,8 +1532,8 @@ int op_rmsdiv(les_ctx* c, double* out_dev) {
   const Grid& g = c->g;
   double* part = c->dred;
   k_rmsdiv_part<<<g.nz - 1, 512, 0, c->stream>>>(c->f[LES_DUDX], c->f[LES_DVDY], c->f[LES_DWDZ], part, g.ld, g.nx,
-                                                g.ny);
-  k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev);
+                                                g.ny); LES_COUNT_LAUNCH();
+  k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev); LES_COUNT_LAUNCH();
   return 0;
 }
 __global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const double* __restrict__ v,
@@ -1560,7 +1562,7 @@ __global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const
 int op_tsc(les_ctx* c, double* cflu, double* visc) {
   const Grid& g = c->g;
   k_tsc<<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_NU_T], c->dscal + 2, g.ld, g.nx,
-                                  g.ny, g.nz);
+                                  g.ny, g.nz); LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 2, c->dscal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   const double delta = std::min(g.dx, g.dy);
@@ -1600,12 +1602,12 @@ int step_fp64(les_ctx* c) {
   k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
       c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
       c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL], nv,
-      g.nplane, k.dt, k.s_flag, (c->jt == 1 && !k.initu) ? 1 : 0);
+      g.nplane, k.dt, k.s_flag, (c->jt == 1 && !k.initu) ? 1 : 0); LES_COUNT_LAUNCH();
   op_press(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
   k_dpdz_project<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
                                                         c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX],
                                                         c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
-                                                        k.dt);
+                                                        k.dt); LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaGetLastError());
   if (k.rmsdiv_every > 0 && c->jt % k.rmsdiv_every == 0) {
     op_rmsdiv(c, c->dscal + 1);
