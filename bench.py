@@ -40,7 +40,7 @@ LEDGER_UNITS = {0: 152.6, 1: 227.0}
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=10)  # multiple of cs_count (5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -81,7 +81,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -268,7 +268,7 @@ def main():
             a[...] = ctx.get(nm)
             host[nm] = a
         nbytes = sum(a.nbytes for a in host.values())
-        ke = max(2, min(args.steps, 5))
+        ke = 5
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(ke):
