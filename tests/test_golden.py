@@ -1,0 +1,25 @@
+"""The oracle reproduces the committed golden fixtures (tests/golden/,
+generated by tests/golden/make_golden.py).  CPU only."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+
+@pytest.mark.parametrize("name", ["neutral_16_jt0", "theta_16_dyn", "theta_24_dyn"])
+def test_oracle_reproduces_golden(oracle_lib, name):
+    import make_golden as mg
+    ref = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    cfg, out = mg.run(name)
+    for k in mg.FIELDS:
+        a, b = out[k], ref[k]
+        lev = slice(0, -1) if k not in ("p",) else slice(0, -2)
+        a, b = a[lev], b[lev]
+        nb = np.linalg.norm(b)
+        err = np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+        # libm (log/pow/atan) may differ by an ulp between hosts
+        assert err < 1e-12, (k, err)

@@ -1,0 +1,263 @@
+"""Known-answer tests that pin the CPU oracle (the reference ships no tests or
+golden vectors and cannot be compiled here).  CPU only."""
+import numpy as np
+import pytest
+
+import les_gb300.config as C
+
+
+@pytest.fixture(scope="module")
+def O(oracle_lib):
+    return oracle_lib.Oracle
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.mark.parametrize("n", [8, 12, 16, 24, 32, 48, 64, 96, 128])
+def test_fft_matches_numpy(O, n):
+    """rfftwnd semantics (fft.f90:40-47): unnormalised r2c along x then y,
+    complex (lh,ny) over (ld,ny); c2r of an r2c returns nx*ny times the input."""
+    cfg = C.make_config(n, n, 4)
+    d = C.dims(cfg)
+    o = O(cfg)
+    rng = np.random.default_rng(n)
+    for big in (0, 1):
+        nn = 3 * n // 2 if big else n
+        ld = d["ld_big"] if big else d["ld"]
+        x = rng.standard_normal((2, nn, ld))
+        p = x.copy()
+        o.call("fft_r2c", p, ints=(2, big))
+        ref = np.fft.fft2(x[:, :, :nn])[:, :, :nn // 2 + 1]
+        assert rel(p.view(np.complex128), ref) < 1e-15 * 20
+        o.call("fft_c2r", p, ints=(2, big))
+        assert rel(p[:, :, :nn], nn * nn * x[:, :, :nn]) < 1e-15 * 20
+
+
+def test_c2r_ignores_imag_of_self_conjugate_columns(O):
+    """FFTW's halfcomplex pass drops Im of the kx = 0 and kx = nx/2 entries
+    after the y pass: a non-Hermitian kx=0 column gives Re(ifft) there."""
+    cfg = C.make_config(16, 16, 4)
+    o = O(cfg)
+    rng = np.random.default_rng(1)
+    spec = (rng.standard_normal((1, 16, 9)) + 1j * rng.standard_normal((1, 16, 9)))
+    p = np.ascontiguousarray(spec).view(np.float64).copy()
+    o.call("fft_c2r", p, ints=(1, 0))
+    # expected: y-inverse per column, then real inverse along x keeping Re of columns 0 and nx/2
+    t = np.fft.ifft(spec, axis=1) * 16
+    t[:, :, 0] = t[:, :, 0].real
+    t[:, :, 8] = t[:, :, 8].real
+    expect = np.fft.irfft(t, n=16, axis=2) * 16
+    assert rel(p[:, :, :16], expect) < 1e-14
+
+
+@pytest.mark.parametrize("kx,ky", [(1, 0), (3, 2), (5, -7), (0, 4)])
+def test_spectral_derivatives_of_modes(O, kx, ky):
+    """ddx/ddy (ddx.f90, ddy.f90) are exact for resolved trigonometric modes."""
+    n = 32
+    cfg = C.make_config(n, n, 4)
+    d = C.dims(cfg)
+    o = O(cfg)
+    x = np.arange(n) * 2 * np.pi / n
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    f = np.zeros((cfg.nz, n, d["ld"]))
+    f[:, :, :n] = np.sin(kx * X + ky * Y + 0.3)
+    dx = np.zeros_like(f); dy = np.zeros_like(f)
+    o.call("ddx", dx, f, ints=(cfg.nz,))
+    o.call("ddy", dy, f, ints=(cfg.nz,))
+    ex = kx * np.cos(kx * X + ky * Y + 0.3)
+    ey = ky * np.cos(kx * X + ky * Y + 0.3)
+    assert np.abs(dx[0, :, :n] - ex).max() < 1e-12
+    assert np.abs(dy[0, :, :n] - ey).max() < 1e-12
+
+
+def test_filt_da_kills_nyquist(O):
+    """filt_da (filt_da.f90:26-38) overwrites f with its Nyquist-filtered self."""
+    n = 16
+    cfg = C.make_config(n, n, 4)
+    d = C.dims(cfg)
+    o = O(cfg)
+    x = np.arange(n) * 2 * np.pi / n
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    base = np.sin(2 * X + Y)
+    f = np.zeros((cfg.nz, n, d["ld"]))
+    f[:, :, :n] = base + np.cos(8 * X) + np.cos(8 * Y)  # Nyquist in x and y
+    dx = np.zeros_like(f); dy = np.zeros_like(f)
+    o.call("filt_da", f, dx, dy, ints=(cfg.nz,))
+    assert np.abs(f[1, :, :n] - base).max() < 1e-13
+    assert np.abs(dx[1, :, :n] - 2 * np.cos(2 * X + Y)).max() < 1e-12
+
+
+def test_three_halves_rule_product_is_exact(O):
+    """dealias1 -> pointwise product on the 3/2 grid -> dealias2 equals the
+    exact product truncated to the resolved band (convec.f90, dealias1/2)."""
+    n = 16
+    cfg = C.make_config(n, n, 4)
+    d = C.dims(cfg)
+    o = O(cfg)
+    rng = np.random.default_rng(4)
+
+    def bandlimited():
+        s = np.zeros((n, n // 2 + 1), complex)
+        for ky in list(range(0, n // 2)) + list(range(n // 2 + 1, n)):
+            for kx in range(n // 2):
+                s[ky, kx] = rng.standard_normal() + 1j * rng.standard_normal()
+        s[0, 0] = s[0, 0].real
+        return np.fft.irfft2(s, s=(n, n))
+    a, b = bandlimited(), bandlimited()
+    fa = np.zeros((1, n, d["ld"])); fb = np.zeros_like(fa)
+    fa[0, :, :n] = a; fb[0, :, :n] = b
+    ba = np.zeros((1, d["ny2"], d["ld_big"])); bb = np.zeros_like(ba)
+    o.call("dealias1", fa, ba, ints=(1,))
+    o.call("dealias1", fb, bb, ints=(1,))
+    prod = np.zeros_like(ba)
+    prod[:, :, :d["nx2"]] = ba[:, :, :d["nx2"]] * bb[:, :, :d["nx2"]]
+    out = np.zeros_like(fa)
+    o.call("dealias2", out, prod, ints=(1,))
+    # exact: evaluate a, b on a 4n grid (exact for band-limited fields),
+    # multiply, and keep the modes padd/unpadd keep (|kx| < n/2, ky != n/2)
+    m = 4 * n
+
+    def up(f):
+        S = np.fft.rfft2(f)
+        Sb = np.zeros((m, m // 2 + 1), complex)
+        for ky in range(n):
+            kb = ky if ky < n // 2 else ky + (m - n)
+            Sb[kb, :n // 2] = S[ky, :n // 2]
+        return np.fft.irfft2(Sb * (m * m) / (n * n), s=(m, m))
+    Pb = np.fft.rfft2(up(a) * up(b)) * (n * n) / (m * m)
+    P = np.zeros((n, n // 2 + 1), complex)
+    for ky in range(n):
+        if ky == n // 2:
+            continue
+        kb = ky if ky < n // 2 else ky + (m - n)
+        P[ky, :n // 2] = Pb[kb, :n // 2]
+    exact = np.fft.irfft2(P, s=(n, n))
+    assert np.abs(out[0, :, :n] - exact).max() < 1e-12 * max(1.0, np.abs(exact).max())
+
+
+def test_tridag_array_vs_dense(O):
+    """tridag_array (tridag_array.f90) solves each (kx,ky) system; compare one
+    non-skipped mode with a dense solve."""
+    cfg = C.make_config(8, 8, 10)
+    d = C.dims(cfg)
+    o = O(cfg)
+    rng = np.random.default_rng(2)
+    n = cfg.nz + 1
+    shp = (n, cfg.ny, d["lh"])
+    a = rng.uniform(0.5, 1, shp); c = rng.uniform(0.5, 1, shp)
+    b = -(a + c + rng.uniform(0.2, 1, shp))
+    r = rng.standard_normal(shp + (2,))
+    u = np.zeros_like(r)
+    assert o.call("tridag_array", a, b, c, r, u) == 0
+    for jy, jx in [(1, 1), (2, 3), (7, 0)]:
+        M = np.diag(b[:, jy, jx]) + np.diag(a[1:, jy, jx], -1) + np.diag(c[:-1, jy, jx], 1)
+        rhs = r[:, jy, jx, 0] + 1j * r[:, jy, jx, 1]
+        sol = np.linalg.solve(M, rhs)
+        got = u[:, jy, jx, 0] + 1j * u[:, jy, jx, 1]
+        assert rel(got, sol) < 1e-13
+
+
+def test_test_filter_transfer(O):
+    """test_filter_init (test_filtermodule.f90:32-63): sharp cutoff at
+    k2 >= (pi/(alpha*delta))^2 with 1/(nx*ny) folded in; modes below the
+    cutoff pass unchanged, above vanish."""
+    n = 32
+    cfg = C.make_config(n, n, 4)
+    d = C.dims(cfg)
+    o = O(cfg)
+    G = np.zeros((cfg.ny, d["lh"]))
+    o.call("filter_G", G, ints=(0,))
+    kxs = np.zeros_like(G); kys = np.zeros_like(G)
+    o.call("wavenumbers", kxs, kys)
+    k2 = kxs ** 2 + kys ** 2
+    dx = 2 * np.pi / n
+    kc2 = (np.pi / (2 * dx)) ** 2
+    inside = (k2 < kc2)
+    inside[:, -1] = False
+    inside[n // 2, :] = False
+    assert np.all(G[inside] == 1.0 / (n * n))
+    assert np.all(G[~inside] == 0.0)
+    x = np.arange(n) * 2 * np.pi / n
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    for (kx, ky), keep in [((3, 4), True), ((9, 9), False)]:
+        f = np.zeros((n, d["ld"]))
+        f[:, :n] = np.cos(kx * X + ky * Y)
+        o.call("test_filter", f, ints=(0,))
+        expect = np.cos(kx * X + ky * Y) if keep else 0.0 * X
+        assert np.abs(f[:, :n] - expect).max() < 1e-13
+
+
+def test_interpolag_reproduces_linear_fields(O):
+    """interpolag_Sdep (interpolag_Sdep.f90:302-372): trilinear
+    interpolation is exact for F linear in (x,y,z) at interior points."""
+    n, nzl = 16, 12
+    cfg = C.make_config(n, n, nzl, dt=2e-4)
+    o = O(cfg)
+    nz = cfg.nz
+    jz, jy, jx = np.meshgrid(np.arange(nz), np.arange(n), np.arange(n + 2), indexing="ij")
+    F = 1.0 + 0.3 * jx + 0.2 * jy + 0.1 * jz
+    for nm in ["F_LM", "F_MM", "F_QN", "F_NN"]:
+        o.set(nm, F)
+    rng = np.random.default_rng(8)
+    dx = 2 * np.pi / n
+    dzz = 1.0 / (nz - 1)
+    # accumulated velocities over cs_count = 5 steps giving displacements < 1 cell
+    ul = rng.uniform(-0.4, 0.4, (nz, n, n + 2)) * dx / (2e-4)
+    vl = rng.uniform(-0.4, 0.4, (nz, n, n + 2)) * dx / (2e-4)
+    wl = rng.uniform(-0.4, 0.4, (nz, n, n + 2)) * dzz / (2e-4)
+    o.set("u_lag", ul); o.set("v_lag", vl); o.set("w_lag", wl)
+    o.call("interpolag_sdep")
+    got = o.get("F_LM")
+    # displacement as the reference forms it (u_lag/cs then level average)
+    ua = ul / 5.0
+    ua[1:] = 0.5 * (ua[1:] + ua[:-1])
+    va = vl / 5.0
+    va[1:] = 0.5 * (va[1:] + va[:-1])
+    xp = -ua * 2e-4 * 5 / dx
+    yp = -va * 2e-4 * 5 / dx
+    zp = -(wl / 5.0) * 2e-4 * 5 / dzz
+    expect = 1.0 + 0.3 * (jx + xp) + 0.2 * (jy + yp) + 0.1 * (jz + zp)
+    sl = (slice(2, nz - 2), slice(1, n - 1), slice(1, n - 1))
+    assert np.abs(got[sl] - expect[sl]).max() < 1e-12
+
+
+def _run(O, cfg, surf, steps, seed=5):
+    o = O(cfg, surf)
+    for k, v in C.initial_state(cfg, surf, seed=seed).items():
+        o.set(k, v)
+    assert o.step(steps) == 0
+    return o
+
+
+def test_projection_is_divergence_free(O):
+    """After press_stag_array + project the start-of-step divergence used by
+    rmsdiv (rmsdiv.f90:93-100) is at FP64 roundoff."""
+    cfg = C.make_config(16, 16, 16, rmsdiv_every=1)
+    o = _run(O, cfg, C.uniform_surface(cfg), 3)
+    assert o.rmsdiv() < 1e-12
+
+
+def test_pressure_zero_mode_closed_form(O):
+    """kx = ky = 0 mode by direct integration (press_stag_array.f90:238-247):
+    the plane-mean pressure increments by dz * mean(w*)/(1.5 dt)."""
+    cfg = C.make_config(16, 16, 8, rmsdiv_every=0)
+    d = C.dims(cfg)
+    o = O(cfg, C.uniform_surface(cfg))
+    rng = np.random.default_rng(6)
+    for nm in ["u", "v", "w"]:
+        a = np.zeros((cfg.nz, cfg.ny, d["ld"]))
+        a[:, :, :16] = rng.standard_normal((cfg.nz, cfg.ny, 16))
+        o.set(nm, a)
+    o.set("divtz", np.zeros((cfg.nz, cfg.ny, d["ld"])))
+    p = np.zeros((cfg.nz + 1, cfg.ny, d["ld"]))
+    dpx = np.zeros((cfg.nz, cfg.ny, d["ld"])); dpy = np.zeros_like(dpx)
+    assert o.call("press_stag_array", p, dpx, dpy) == 0
+    w = o.get("w")
+    dz = 1.0 / (cfg.nz - 1)
+    pm = p[:, :, :16].mean(axis=(1, 2))
+    wm = w[:, :, :16].mean(axis=(1, 2)) / (1.5 * cfg.dt)
+    for k in range(2, cfg.nz):
+        assert abs((pm[k] - pm[k - 1]) - wm[k - 1] * dz) < 1e-9 * max(1.0, abs(wm[k - 1] * dz))
