@@ -142,7 +142,9 @@ enum ColCoef {
   CC_GG = 3,      // x G_test_test
   CC_IKX = 4,     // x i kx         (ddx.f90:152)
   CC_IKY = 5,     // x i ky         (ddy.f90:183)
-  CC_KILL = 6     // copy with the Nyquist row/column zeroed (filt_da.f90:114-115)
+  CC_KILL = 6,    // copy with the Nyquist row/column zeroed (filt_da.f90:114-115)
+  CC_MASK = 7,    // G_test / (1/(nx*ny)): pass where G_test != 0 (input already scaled)
+  CC_MASK4 = 8    // G_test_test / (1/(nx*ny))
 };
 enum ColMap { MAP_SAME = 0, MAP_PAD = 1, MAP_UNPAD = 2 };
 enum ColDir { DIR_FWD = 1, DIR_INV = 2, DIR_BOTH = 3 };
@@ -155,7 +157,8 @@ struct ColJob {
   int nf;                 // independent field sets (grid z); set f uses
   long fs_in, fs_out;     // in[i] + f*fs_in and out[o] + f*fs_out
   int ny_in, ny_out;      // transform lengths
-  int map, dir;
+  int map, dir;           // dir & DIR_FWD: forward y pass on the inputs
+  unsigned inv_mask;      // bit o: inverse y pass on output o (else the spectrum is stored)
   int ncols;              // kx columns processed
   int ny_small;           // ny of the small grid (pad/unpad mapping)
   int wc_in, wc_out;      // row strides (complex)

@@ -114,6 +114,8 @@ __device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT
       if (jx == lhm1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
       return v;
     }
+    case CC_MASK: return J.G[ki] != 0.0 ? v : mk<T>((T)0, (T)0);
+    case CC_MASK4: return J.GG[ki] != 0.0 ? v : mk<T>((T)0, (T)0);
     default: return mk<T>((T)0, (T)0);
   }
 }
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
       A[t] = acc;
     }
     __syncthreads();
-    C* r = (J.dir & DIR_INV) ? fft_smem<T, true>(A, B, TX, 0, Pout, +1) : A;
+    C* r = ((J.inv_mask >> o) & 1u) ? fft_smem<T, true>(A, B, TX, 0, Pout, +1) : A;
     C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out;
     for (int t = threadIdx.x; t < J.ny_out * TX; t += blockDim.x) {
       const int row = t / TX, b = t - row * TX;

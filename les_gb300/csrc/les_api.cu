@@ -121,7 +121,7 @@ static Sizes sizes_of(const Grid& g) {
   s.fields = 0;
   for (int f = 0; f < LES_ZO; ++f) s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
   s.surf = (size_t)(LES_NUM_FIELDS - LES_ZO + 1) * g.nx * g.ny * sizeof(double);
-  s.spare = 4 * g.nfield * sizeof(double);
+  s.spare = 4 * g.nfield * sizeof(double) + (4 * nz + 4) * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double);
   return s;
 }
 
@@ -238,8 +238,13 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   if ((st = dalloc(c, &c->wsA, s.wsA)) || (st = dalloc(c, &c->wsB, s.wsB)) || (st = dalloc(c, &c->wsP, s.wsP)) ||
       (st = dalloc(c, (void**)&c->big, s.big)) || (st = dalloc(c, (void**)&c->tmp, s.tmp)) ||
       (st = dalloc(c, (void**)&c->spare, s.spare)) || (st = dalloc(c, (void**)&c->dscal, 64 * sizeof(double))) ||
-      (st = dalloc(c, (void**)&c->dred, 16 * (size_t)(g.nz + 8) * sizeof(double))))
+      (st = dalloc(c, (void**)&c->dred, 16 * (size_t)(g.nz + 8) * sizeof(double))) ||
+      (st = dalloc(c, (void**)&c->spec, 4 * (size_t)g.nz * g.C * sizeof(double2))) ||
+      (st = dalloc(c, (void**)&c->wspec, 4 * g.C * sizeof(double2))) ||
+      (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||
+      (st = dalloc(c, (void**)&c->gamt, (size_t)(g.nz + 1) * g.C * sizeof(double))))
     return fail(st);
+  if ((st = thomas_tables(c))) return fail(st);
   c->wsA_bytes = s.wsA; c->wsB_bytes = s.wsB; c->wsP_bytes = s.wsP;
   if (cudaMallocHost(&c->host_scal, 64 * sizeof(double)) != cudaSuccess) { les_set_error("pinned alloc failed"); return fail(LES_ERR_OOM); }
   if (cudaDeviceSynchronize() != cudaSuccess) { les_set_error("%s", cudaGetErrorString(cudaGetLastError())); return fail(LES_ERR_CUDA); }

@@ -66,6 +66,10 @@ struct les_ctx {
   double* big = nullptr;  int nbig = 0;        // big physical fields
   double* tmp = nullptr;  int ntmp = 0;        // small physical temp planes
   double* spare = nullptr;                     // 4 fields (interpolated F_*)
+  double2* spec = nullptr;                     // U, V, W, Theta spectra F(u/(nx*ny)), (nz,ny,lh) each
+  double2* wspec = nullptr;                    // wall-plane spectra: dudz(1), dvdz(1), dTdz(1), dTdz(nz)
+  double* ibet = nullptr;                      // Thomas 1/bet per (row, mode), FP64
+  double* gamt = nullptr;                      // Thomas gam per (row, mode), FP64
   int lag_chunk = 32;
   double* dscal = nullptr;                     // device scalars / reductions
   double* dred = nullptr;                      // per-level reduction results
@@ -100,4 +104,5 @@ int op_project(les_ctx* c);
 int op_rmsdiv(les_ctx* c, double* out);
 int op_tsc(les_ctx* c, double* cflu, double* visc);
 int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv);
+int thomas_tables(les_ctx* c);
 }  // namespace les

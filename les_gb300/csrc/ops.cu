@@ -76,6 +76,7 @@ static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
   const Grid& g = c->g;
   ColJob J{};
   J.nlev = nlev; J.map = map; J.dir = dir; J.nf = 1;
+  J.inv_mask = (dir & DIR_INV) ? 0xffffffffu : 0u;
   J.ny_small = g.ny;
   J.kx = c->kx; J.ky = c->ky; J.G = c->G; J.GG = c->GG; J.lh = g.lh;
   if (map == MAP_SAME) {
@@ -164,6 +165,32 @@ static int filt_da_multi(les_ctx* c, double* const* f, double* const* dx, double
   c2r(c, 3 * nf, nlev, c->wsB, out, (long)g.nplane, false, g.lh);
   return 0;
 }
+// filt_da with the Nyquist-filtered spectra F(f/(nx*ny)) also stored in
+// `spec` (field stride nlev*C) for reuse by the fused step
+int filt_da_multi_spec(les_ctx* c, double* const* f, double* const* dx, double* const* dy, int nf, int nlev,
+                       C2* spec) {
+  const Grid& g = c->g;
+  double sc[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) sc[i] = 1.0 / (double)(g.nx * g.ny);
+  const double* in[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) in[i] = f[i];
+  r2c(c, nf, nlev, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nlev);
+  J.nin = 1; J.nout = 4; J.nf = nf;
+  J.inv_mask = 7u;  // outputs 0..2 back to physical space, output 3 kept spectral
+  J.in[0] = c->wsA; J.fs_in = (long)nlev * g.C;
+  J.out[0] = c->wsB;
+  J.out[1] = (C2*)c->wsB + (size_t)nf * nlev * g.C;
+  J.out[2] = (C2*)c->wsB + (size_t)2 * nf * nlev * g.C;
+  J.out[3] = spec;
+  J.fs_out = (long)nlev * g.C;
+  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY; J.coef[3][0] = CC_KILL;
+  cols(c, J);
+  double* out[3 * JOB_MAXF];
+  for (int i = 0; i < nf; ++i) { out[i] = f[i]; out[nf + i] = dx[i]; out[2 * nf + i] = dy[i]; }
+  c2r(c, 3 * nf, nlev, c->wsB, out, (long)g.nplane, false, g.lh);
+  return 0;
+}
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev) {
   double* a[1] = {f}; double* b[1] = {dfdx}; double* d[1] = {dfdy};
   return filt_da_multi(c, a, b, d, 1, nlev);
@@ -207,6 +234,7 @@ int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse) {
   J.phys[0] = planes; J.work[0] = c->wsA; J.scale[0] = 1.0; J.div[0] = 0.0;
   ColJob K{};
   K.nin = 1; K.nout = 1; K.nlev = nplanes; K.nf = 1; K.ny_in = K.ny_out = nyy; K.map = MAP_SAME;
+  K.inv_mask = inverse ? 1u : 0u;
   K.ncols = lhh; K.ny_small = nyy; K.wc_in = K.wc_out = lhh; K.ps_in = K.ps_out = (long)nyy * lhh;
   K.coef[0][0] = CC_ONE; K.kx = c->kx; K.ky = c->ky; K.G = c->G; K.GG = c->GG; K.lh = g.lh;
   const HostRealPlan& rp = big ? c->rxb : c->rx;
@@ -1109,36 +1137,44 @@ __global__ void k_rhs_ab2(double* u, double* v, double* w, double* Rx, double* R
   }
 }
 
-// main.f90:403-410 + forcing.f90:128-219 project, one thread per (jx,jy)
+// main.f90:403-410 + forcing.f90:128-219 project, one thread per point of
+// levels 1..nz-1; the thread of level nz-1 also sets the top level and the
+// thread of level 1 the wall value of w.
 __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz,
                                const double* __restrict__ p, const double* __restrict__ dpdx,
                                const double* __restrict__ dpdy, double* dpdz, int ld, int nx, int ny, int nz,
                                double dz, double dt) {
   const size_t np = (size_t)ld * ny;
-  GSTRIDE(r, np) {
+  GSTRIDE(i, np * (nz - 1)) {
+    const int jz = (int)(i / np) + 1;
+    const size_t r = i - (size_t)(jz - 1) * np;
     const int jx = (int)(r % ld);
-    for (int jz = 1; jz <= nz - 1; ++jz) {
-      const size_t i = r + (size_t)(jz - 1) * np;
-      double pz = 0.0;
-      if (jx < nx) {
-        pz = (p[r + (size_t)jz * np] - p[r + (size_t)(jz - 1) * np]) / dz;
-        dpdz[i] = pz;
-      }
-      Rx[i] = Rx[i] - dpdx[i];
-      Ry[i] = Ry[i] - dpdy[i];
-      Rz[i] = Rz[i] - dpdz[i];
-      if (jx < nx) {
-        u[i] = (u[i] + dt * (-1.5 * dpdx[i] + 0.0));
-        v[i] = (v[i] + dt * (-1.5 * dpdy[i] + 0.0));
-        if (jz >= 2) w[i] = (w[i] + dt * (-1.5 * pz + 0.0));
-      }
+    double pz = 0.0;
+    if (jx < nx) {
+      pz = (p[r + (size_t)jz * np] - p[r + (size_t)(jz - 1) * np]) / dz;
+      dpdz[i] = pz;
+    } else {
+      pz = dpdz[i];
     }
-    const size_t top = r + (size_t)(nz - 1) * np, below = r + (size_t)(nz - 2) * np;
-    dpdz[top] = LES_BOGUS;
-    u[top] = u[below];
-    v[top] = v[below];
-    w[top] = 0.0;
-    w[r] = 0.0;
+    Rx[i] = Rx[i] - dpdx[i];
+    Ry[i] = Ry[i] - dpdy[i];
+    Rz[i] = Rz[i] - pz;
+    double uu = u[i], vv = v[i], ww = w[i];
+    if (jx < nx) {
+      uu = (uu + dt * (-1.5 * dpdx[i] + 0.0));
+      vv = (vv + dt * (-1.5 * dpdy[i] + 0.0));
+      if (jz >= 2) ww = (ww + dt * (-1.5 * pz + 0.0));
+      u[i] = uu; v[i] = vv;
+      if (jz >= 2) w[i] = ww;
+    }
+    if (jz == nz - 1) {
+      const size_t top = i + np;
+      dpdz[top] = LES_BOGUS;
+      u[top] = uu;
+      v[top] = vv;
+      w[top] = 0.0;
+    }
+    if (jz == 1) w[i] = 0.0;
   }
 }
 __global__ void k_project_only(double* u, double* v, double* w, const double* dpdx, const double* dpdy,
@@ -1175,17 +1211,16 @@ int op_project(les_ctx* c) {
 // press_stag_array.f90:192-264 + tridag_array.f90:1-109: one thread per
 // wavenumber pair solves its z-tridiagonal (Thomas), building the RHS rows
 // from the spectra H on the fly.  Spectra are (level, ny, lh) complex.
-__global__ void k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy, const C2* __restrict__ Hz,
-                          const C2* __restrict__ bot, const C2* __restrict__ top, C2* P, double* gam,
-                          const double* __restrict__ kx, const double* __restrict__ ky, int lh, int ny, int nz,
-                          double dz, int* flag) {
+__global__ void __launch_bounds__(128) k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy,
+                                                 const C2* __restrict__ Hz, const C2* __restrict__ bot,
+                                                 const C2* __restrict__ top, C2* P, const double* __restrict__ ibet,
+                                                 const double* __restrict__ gam, const double* __restrict__ kx,
+                                                 const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
   const int nk = lh * ny;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nk) return;
   const int jx = t % lh, jy = t / lh;
   const size_t NK = (size_t)nk;
-  // Hz(nz) = 0 ; H levels are uvp 1..nz-1 at spectral index (lev-1)
-  auto HZ = [&](int lev) -> C2 { return (lev >= 1 && lev <= nz - 1) ? Hz[(size_t)(lev - 1) * NK + t] : make_double2(0.0, 0.0); };
   if (jy == ny / 2 || jx == lh - 1) {  // Nyquist modes: zeroed (press_stag_array.f90:263-264)
     for (int j = 0; j <= nz; ++j) P[(size_t)j * NK + t] = make_double2(0.0, 0.0);
     return;
@@ -1198,7 +1233,7 @@ __global__ void k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy, 
     P[NK] = p1;
     p = p1;
     for (int jz = 2; jz <= nz; ++jz) {
-      const C2 h = HZ(jz);
+      const C2 h = (jz <= nz - 1) ? Hz[(size_t)(jz - 1) * NK] : make_double2(0.0, 0.0);
       p.x = p.x + h.x * dz; p.y = p.y + h.y * dz;
       P[(size_t)jz * NK] = p;
     }
@@ -1206,41 +1241,34 @@ __global__ void k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy, 
   }
   const double k_x = kx[t], k_y = ky[t];
   const double idz2 = 1.0 / (dz * dz);
-  const double bmid = -(k_x * k_x + k_y * k_y + 2.0 / (dz * dz));
   const int n = nz + 1;
-  // row 1: a = BOGUS, b = -1, c = 1, r = -dz * bottomw
-  double bet = -1.0;
-  C2 r1 = bot[t];
-  C2 up; up.x = (-dz * r1.x) / bet; up.y = (-dz * r1.y) / bet;
+  // row 1: a = BOGUS, b = -1, c = 1, r = -dz * bottomw ; u = r / bet
+  const C2 r1 = bot[t];
+  C2 up; up.x = (-dz * r1.x) * ibet[t]; up.y = (-dz * r1.y) * ibet[t];
   P[t] = up;
-  double cprev = 1.0;
-  C2 hz0 = HZ(1);
+  C2 hz0 = Hz[t];
   for (int j = 2; j <= n; ++j) {
-    double a, b;
+    double a;
     C2 r;
     if (j <= nz) {
-      a = idz2; b = bmid;
+      a = idz2;
       const C2 hx = Hx[(size_t)(j - 2) * NK + t];
       const C2 hy = Hy[(size_t)(j - 2) * NK + t];
-      const C2 hz1 = HZ(j);
+      const C2 hz1 = (j <= nz - 1) ? Hz[(size_t)(j - 1) * NK + t] : make_double2(0.0, 0.0);
       const double sr = k_x * hx.x + k_y * hy.x;
       const double si = k_x * hx.y + k_y * hy.y;
       r.x = -si + (hz1.x - hz0.x) / dz;
       r.y = sr + (hz1.y - hz0.y) / dz;
       hz0 = hz1;
     } else {
-      a = -1.0; b = 1.0;
+      a = -1.0;
       const C2 tp = top[t];
       r.x = -tp.x * dz; r.y = -tp.y * dz;
     }
-    const double gm = cprev / bet;
-    gam[(size_t)(j - 1) * NK + t] = gm;
-    bet = b - a * gm;
-    if (bet == 0.0) atomicOr(flag, 1);
-    C2 u; u.x = (r.x - a * up.x) / bet; u.y = (r.y - a * up.y) / bet;
+    const double ib = ibet[(size_t)(j - 1) * NK + t];
+    C2 u; u.x = (r.x - a * up.x) * ib; u.y = (r.y - a * up.y) * ib;
     P[(size_t)(j - 1) * NK + t] = u;
     up = u;
-    cprev = (j <= nz) ? idz2 : 0.0;
   }
   for (int j = n - 1; j >= 1; --j) {
     const double gm = gam[(size_t)j * NK + t];
@@ -1249,6 +1277,41 @@ __global__ void k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy, 
     P[(size_t)(j - 1) * NK + t] = u;
     up = u;
   }
+}
+
+// Thomas coefficients of press_stag_array.f90:144-210 for every (kx,ky):
+// they depend on k^2 and dz only, so they are formed once per context
+// (tridag_array.f90:41-69 recurrences, reciprocal of bet stored).
+int thomas_tables(les_ctx* c) {
+  const Grid& g = c->g;
+  const int nz = g.nz, n = nz + 1, lh = g.lh, ny = g.ny;
+  const size_t NK = (size_t)lh * ny;
+  std::vector<double> kx(NK), ky(NK), ib(NK * n, 0.0), gm(NK * n, 0.0);
+  cudaMemcpy(kx.data(), c->kx, NK * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaMemcpy(ky.data(), c->ky, NK * sizeof(double), cudaMemcpyDeviceToHost);
+  const double dz = g.dz, idz2 = 1.0 / (dz * dz);
+  for (size_t t = 0; t < NK; ++t) {
+    double bet = -1.0;
+    ib[t] = 1.0 / bet;
+    const double bmid = -(kx[t] * kx[t] + ky[t] * ky[t] + 2.0 / (dz * dz));
+    double cprev = 1.0;
+    for (int j = 2; j <= n; ++j) {
+      const double a = (j <= nz) ? idz2 : -1.0;
+      const double b = (j <= nz) ? bmid : 1.0;
+      const double gg = cprev / bet;
+      gm[(size_t)(j - 1) * NK + t] = gg;
+      bet = b - a * gg;
+      if (bet == 0.0) {  // tridag_array.f90:62-67 stops here
+        les_set_error("tridag_array failed at mode %zu, row %d: zero pivot", t, j);
+        return LES_ERR_PIVOT;
+      }
+      ib[(size_t)(j - 1) * NK + t] = 1.0 / bet;
+      cprev = (j <= nz) ? idz2 : 0.0;
+    }
+  }
+  LES_CUDA_CHECK(cudaMemcpy(c->ibet, ib.data(), ib.size() * sizeof(double), cudaMemcpyHostToDevice));
+  LES_CUDA_CHECK(cudaMemcpy(c->gamt, gm.data(), gm.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
 }
 
 int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
@@ -1264,7 +1327,6 @@ int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
   C2* H = (C2*)c->wsP;                        // 3*(nz-1)*C
   C2* BT = H + (size_t)3 * (nz - 1) * g.C;   // bottom, top
   C2* P = BT + 2 * g.C;                       // (nz+1)*C
-  double* gam = (double*)(P + (size_t)(nz + 1) * g.C);  // (nz+1)*C doubles
   ColJob J = coljob(c, MAP_SAME, DIR_FWD, nz - 1);
   J.nin = 1; J.nout = 1; J.nf = 3;
   J.in[0] = c->wsA; J.fs_in = (long)(nz - 1) * g.C;
@@ -1283,10 +1345,9 @@ int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
     K.coef[0][0] = CC_KILL;
     cols(c, K);
   }
-  int* flag = reinterpret_cast<int*>(c->dscal + 8);
   k_tridiag<<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(H, H + (size_t)(nz - 1) * g.C,
-                                                              H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, gam,
-                                                              c->kx, c->ky, g.lh, g.ny, nz, g.dz, flag); LES_COUNT_LAUNCH();
+                                                              H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P,
+                                                              c->ibet, c->gamt, c->kx, c->ky, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
@@ -1572,6 +1633,373 @@ int op_tsc(les_ctx* c, double* cflu, double* visc) {
 }
 
 // ---------------------------------------------------------------------------
+// Fused time step.  The per-routine versions above restate each routine on
+// arbitrary module state; inside one step the state is consistent, so the
+// fused step reuses the spectra filt_da already computes:
+//   * F(u/(nx*ny)) etc. (Nyquist removed) are saved by filt_da's y pass;
+//   * the padded velocities of convec (convec.f90:45-65) and of the scalar
+//     advection (scalars_module.f90:286-288) are the same fields: built once;
+//   * vorticity (convec.f90:67-114), the padded theta gradients
+//     (scalars_module.f90:289-291) and the G/G_test_test inputs u_bar, S_ij of
+//     lagrange_Sdep are linear in the saved spectra (vertical differences of
+//     spectra = spectra of vertical differences), so only the wall planes
+//     set by wallstress / the surface flux need transforms of their own.
+// Every identity is exact in exact arithmetic; results differ from the
+// per-routine path at the rounding level only.
+
+// one (ld,ny) plane of several fields -> full 2-D spectra (forward only)
+static void plane_spectra(les_ctx* c, int np, const double* const* planes, const double* scale, C2* out) {
+  const Grid& g = c->g;
+  r2c(c, np, 1, planes, (long)g.nplane, scale, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_FWD, 1);
+  J.nin = 1; J.nout = 1; J.nf = np;
+  J.in[0] = c->wsA; J.fs_in = (long)g.C;
+  J.out[0] = out; J.fs_out = (long)g.C;
+  J.coef[0][0] = CC_ONE;
+  cols(c, J);
+}
+
+// convec.f90:67-114 vorticity spectra (x 1/(nx*ny)) from U,V,W spectra
+__global__ void k_vort_spec(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
+                            const C2* __restrict__ D1, const C2* __restrict__ D2, C2* o1, C2* o2, C2* o3,
+                            const double* __restrict__ kx, const double* __restrict__ ky, int nk, int nz,
+                            double idz) {
+  GSTRIDE(t, (size_t)nk * nz) {
+    const int jz = (int)(t / nk) + 1;
+    const size_t m = t - (size_t)(jz - 1) * nk;
+    const double k_x = kx[m], k_y = ky[m];
+    const C2 w = W[t], u = U[t], v = V[t];
+    C2 a, b;
+    if (jz == 1) {
+      const C2 w2 = W[t + nk];
+      const C2 wy = cadd(ik(w, k_y), ik(w2, k_y));
+      const C2 wx = cadd(ik(w, k_x), ik(w2, k_x));
+      a = csub(cscale(wy, 0.5), D2[m]);
+      b = csub(D1[m], cscale(wx, 0.5));
+    } else if (jz == nz) {
+      a = ik(w, k_y);
+      b = cscale(ik(w, k_x), -1.0);
+    } else {
+      const C2 vz = cscale(csub(v, V[t - nk]), idz);
+      const C2 uz = cscale(csub(u, U[t - nk]), idz);
+      a = csub(ik(w, k_y), vz);
+      b = csub(uz, ik(w, k_x));
+    }
+    o1[t] = a;
+    o2[t] = b;
+    o3[t] = csub(ik(v, k_x), ik(u, k_y));
+  }
+}
+
+// scalars_module.f90:289-291 padded-gradient inputs: F(dTdx/(nx ny)),
+// F(dTdy/(nx ny)), F(dTdz/(nx ny)) from the theta spectrum; levels 1 and nz
+// of dTdz come from their own plane transforms (Z1, ZN)
+__global__ void k_dtheta_spec(const C2* __restrict__ T, const C2* __restrict__ Z1, const C2* __restrict__ ZN,
+                              C2* o1, C2* o2, C2* o3, const double* __restrict__ kx,
+                              const double* __restrict__ ky, int nk, int nz, double idz) {
+  GSTRIDE(t, (size_t)nk * nz) {
+    const int jz = (int)(t / nk) + 1;
+    const size_t m = t - (size_t)(jz - 1) * nk;
+    const C2 th = T[t];
+    o1[t] = ik(th, kx[m]);
+    o2[t] = ik(th, ky[m]);
+    if (jz == 1) o3[t] = Z1[m];
+    else if (jz == nz) o3[t] = ZN[m];
+    else o3[t] = cscale(csub(th, T[t - nk]), idz);
+  }
+}
+
+// lagrange_Sdep.f90:131-141, sgs_stag.f90:371-498 : spectra of u_bar, v_bar,
+// w_bar and S_ij (x 1/(nx*ny)) for the levels jz0..jz0+nl-1.
+// out layout: q = 0..8 (u_bar, v_bar, w_bar, S11, S12, S13, S22, S23, S33)
+__global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
+                           const C2* __restrict__ D1, const C2* __restrict__ D2, C2* out,
+                           const double* __restrict__ kx, const double* __restrict__ ky, int nk, int nz,
+                           int jz0, int nl, double idz) {
+  const size_t st = (size_t)nk * nl;
+  GSTRIDE(t, st) {
+    const int lc = (int)(t / nk);
+    const size_t m = t - (size_t)lc * nk;
+    const int jz = jz0 + lc;
+    const size_t i = (size_t)(jz - 1) * nk + m;
+    const double k_x = kx[m], k_y = ky[m];
+    C2 ub, vb, wb, ux, uy, uz, vx, vy, vz, wx, wy, wz;
+    // vertical differences as ddz_uv / ddz_w define them (top level 0)
+    auto ddz_uv = [&](const C2* F, int j) -> C2 {  // level j >= 2
+      if (j >= nz) return make_double2(0.0, 0.0);
+      return cscale(csub(F[(size_t)(j - 1) * nk + m], F[(size_t)(j - 2) * nk + m]), idz);
+    };
+    auto ddz_w = [&](int j) -> C2 {  // dwdz at level j
+      if (j >= nz) return make_double2(0.0, 0.0);
+      return cscale(csub(W[(size_t)j * nk + m], W[(size_t)(j - 1) * nk + m]), idz);
+    };
+    if (jz == 1) {
+      const C2 u1 = U[i], v1 = V[i], w1 = W[i], w2 = W[i + nk];
+      ub = u1; vb = v1; wb = cscale(w2, 0.25);
+      ux = ik(u1, k_x); uy = ik(u1, k_y); uz = D1[m];
+      vx = ik(v1, k_x); vy = ik(v1, k_y); vz = D2[m];
+      wx = cscale(cadd(ik(w1, k_x), ik(w2, k_x)), 0.5);
+      wy = cscale(cadd(ik(w1, k_y), ik(w2, k_y)), 0.5);
+      wz = ddz_w(1);
+    } else {
+      const C2 u0 = U[i], um = U[i - nk], v0 = V[i], vm = V[i - nk], w0 = W[i];
+      ub = cscale(cadd(u0, um), 0.5); vb = cscale(cadd(v0, vm), 0.5); wb = w0;
+      ux = cscale(cadd(ik(u0, k_x), ik(um, k_x)), 0.5);
+      uy = cscale(cadd(ik(u0, k_y), ik(um, k_y)), 0.5);
+      uz = ddz_uv(U, jz);
+      vx = cscale(cadd(ik(v0, k_x), ik(vm, k_x)), 0.5);
+      vy = cscale(cadd(ik(v0, k_y), ik(vm, k_y)), 0.5);
+      vz = ddz_uv(V, jz);
+      wx = ik(w0, k_x);
+      wy = ik(w0, k_y);
+      wz = cscale(cadd(ddz_w(jz), ddz_w(jz - 1)), 0.5);
+    }
+    out[t] = ub; out[t + st] = vb; out[t + 2 * st] = wb;
+    out[t + 3 * st] = ux;
+    out[t + 4 * st] = cscale(cadd(uy, vx), 0.5);
+    out[t + 5 * st] = cscale(cadd(uz, wx), 0.5);
+    out[t + 6 * st] = vy;
+    out[t + 7 * st] = cscale(cadd(vz, wy), 0.5);
+    out[t + 8 * st] = wz;
+  }
+}
+
+// lagrange_Sdep.f90:142-266 physical products (12 planes per level)
+__global__ void k_lag_prod(const double* __restrict__ u, const double* __restrict__ v,
+                           const double* __restrict__ w, Ptr6 Sp, double* out, int ld, int jz0, int nlev,
+                           size_t np) {
+  const size_t tot = np * nlev;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jz = jz0 + lc;
+    const size_t i = (size_t)(jz - 1) * np + r;
+    double ub, vb, wb;
+    if (jz == 1) { ub = u[i]; vb = v[i]; wb = 0.25 * w[i + np]; }
+    else { ub = 0.5 * (u[i] + u[i - np]); vb = 0.5 * (v[i] + v[i - np]); wb = w[i]; }
+    const size_t stride = np * nlev;
+    double* o = out + t;
+    o[0] = ub * ub; o[stride] = ub * vb; o[2 * stride] = ub * wb;
+    o[3 * stride] = vb * vb; o[4 * stride] = vb * wb; o[5 * stride] = wb * wb;
+    const double s11 = Sp.p[0][i], s12 = Sp.p[1][i], s13 = Sp.p[2][i], s22 = Sp.p[3][i], s23 = Sp.p[4][i], s33 = Sp.p[5][i];
+    const double S = smag(s11, s22, s33, s12, s13, s23);
+    o[6 * stride] = S * s11; o[7 * stride] = S * s12; o[8 * stride] = S * s13;
+    o[9 * stride] = S * s22; o[10 * stride] = S * s23; o[11 * stride] = S * s33;
+  }
+}
+
+static int lagrange_fused(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  op_interpolag(c);
+  const double delta = g.delta;
+  const double cst = 2.0 * (delta * delta);
+  const double opftdelta = 1.5 * delta;
+  const double lagran_dt = k.dt * (double)k.cs_count;
+  const double bexp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
+  const int bone = (bexp == 1.0) ? 1 : 0;
+  Ptr6 Sp;
+  const int sid[6] = {LES_S11, LES_S12, LES_S13, LES_S22, LES_S23, LES_S33};
+  for (int q = 0; q < 6; ++q) Sp.p[q] = c->f[sid[q]];
+  const C2* U = c->spec;
+  const C2* V = c->spec + (size_t)g.nz * g.C;
+  const C2* W = c->spec + (size_t)2 * g.nz * g.C;
+  const int nch = c->lag_chunk;
+  for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
+    const int nl = std::min(nch, g.nz - jz0 + 1);
+    const long FS = (long)nl * g.C;
+    double* prod = c->tmp;                                // 12 * nl planes
+    double* flt = c->tmp + (size_t)21 * nch * g.nplane;    // 42 * nl planes
+    // spectral inputs (9) in wsA after the product x-spectra (12)
+    C2* xs = (C2*)c->wsA;
+    C2* sp = xs + (size_t)12 * FS;
+    k_lag_spec<<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx, c->ky,
+                                                              (int)g.C, g.nz, jz0, nl, 1.0 / g.dz); LES_COUNT_LAUNCH();
+    k_lag_prod<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
+                                                           jz0, nl, g.nplane); LES_COUNT_LAUNCH();
+    const double* in[12];
+    for (int q = 0; q < 12; ++q) in[q] = prod + (size_t)q * nl * g.nplane;
+    r2c(c, 12, nl, in, (long)g.nplane, nullptr, nullptr, xs, false, g.lh);
+    C2* ob = (C2*)c->wsB;
+    // (input block, first input index in block, count, output q base)
+    struct Blk { C2* base; int dir; int code_g, code_gg; int count; int q0; };
+    const Blk blks[4] = {{sp, DIR_INV, CC_MASK, CC_MASK4, 3, 0},
+                         {sp + 3 * FS, DIR_INV, CC_MASK, CC_MASK4, 6, 9},
+                         {xs, DIR_BOTH, CC_G, CC_GG, 6, 3},
+                         {xs + 6 * FS, DIR_BOTH, CC_G, CC_GG, 6, 15}};
+    for (const Blk& b : blks) {
+      ColJob J = coljob(c, MAP_SAME, b.dir, nl);
+      J.inv_mask = 3u;
+      J.nin = 1; J.nout = 2; J.nf = b.count;
+      J.in[0] = b.base; J.fs_in = FS;
+      J.out[0] = ob + (size_t)b.q0 * FS;
+      J.out[1] = ob + (size_t)(21 + b.q0) * FS;
+      J.fs_out = FS;
+      J.coef[0][0] = b.code_g; J.coef[1][0] = b.code_gg;
+      cols(c, J);
+    }
+    double* out[42];
+    for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
+    c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    k_lag_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+        flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
+        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
+  }
+  return 0;
+}
+
+static int sgs_stag_fused(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  const bool lag = (k.model == 4 || k.model == 5 || k.model == 7);
+  k_calc_sij<<<grid1(g.nfield), 256, 0, c->stream>>>(
+      c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
+      c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
+      c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
+      c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0); LES_COUNT_LAUNCH();
+  const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
+  if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {
+    if (k.model == 3) {
+      double* csz = c->dred;
+      op_scaledep(c, csz, S);
+      k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
+    } else if (k.model == 5) {
+      lagrange_fused(c);
+    }
+  }
+  int ov = 0;
+  double csov = 0.0;
+  if ((k.model == 5 || k.model == 6 || k.model == 7) && c->jt_total < 500) {
+    ov = 1;
+    const float c016 = 0.16f;
+    csov = (double)(c016 * c016);
+  }
+  k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
+                                               c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, g.delta * g.delta, ov, csov); LES_COUNT_LAUNCH();
+  k_tau<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_NU_T],
+                                               c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ],
+                                               c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz); LES_COUNT_LAUNCH();
+  return 0;
+}
+
+// inverse-only 3/2 padding of full spectra: nf fields (field stride nz*C) -> big physical
+static void pad_from_spectra(les_ctx* c, const C2* spec, int nf, double* const* out) {
+  const Grid& g = c->g;
+  ColJob J = coljob(c, MAP_PAD, DIR_INV, g.nz);
+  J.nin = 1; J.nout = 1; J.nf = nf;
+  J.in[0] = spec; J.fs_in = (long)g.nz * g.C;
+  J.out[0] = c->wsB; J.fs_out = (long)g.nz * g.CB;
+  J.coef[0][0] = CC_ONE;
+  cols(c, J);
+  c2r(c, nf, g.nz, c->wsB, out, (long)g.nplane_big, true, g.nx / 2);
+}
+
+static int theta_fused(les_ctx* c, double* const* bigf) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  const int nz = g.nz;
+  {
+    double* f1[1] = {c->f[LES_THETA]};
+    double* x1[1] = {c->f[LES_DTDX]};
+    double* y1[1] = {c->f[LES_DTDY]};
+    filt_da_multi_spec(c, f1, x1, y1, 1, nz, c->spec + (size_t)3 * nz * g.C);
+  }
+  op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
+  fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
+  std::swap(c->f[LES_RHS_T], c->f[LES_RHS_TF]);
+  k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
+                                                            c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
+                                                            c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
+                                                            k.t_scale * k.u_star, k.vonk, g.dz); LES_COUNT_LAUNCH();
+  // spectra of the dTdz wall and top planes (dealias1 scaling 1/(nx*ny))
+  {
+    const double cs = 1.0 / (double)(g.nx * g.ny);
+    const double* pl[2] = {c->f[LES_DTDZ], c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane};
+    const double sc[2] = {cs, cs};
+    plane_spectra(c, 2, pl, sc, c->wspec + 2 * g.C);
+  }
+  C2* ds = (C2*)c->wsA;  // 3 derivative spectra (nz levels each)
+  const size_t FS = (size_t)nz * g.C;
+  k_dtheta_spec<<<grid1(FS), 256, 0, c->stream>>>(c->spec + 3 * FS, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds,
+                                                 ds + FS, ds + 2 * FS, c->kx, c->ky, (int)g.C, nz, 1.0 / g.dz); LES_COUNT_LAUNCH();
+  {
+    double* o3[3] = {bigf[3], bigf[4], bigf[5]};
+    // the spectra live in wsA; pad reads them and writes wsB
+    ColJob J = coljob(c, MAP_PAD, DIR_INV, nz);
+    J.nin = 1; J.nout = 1; J.nf = 3;
+    J.in[0] = ds; J.fs_in = (long)FS;
+    J.out[0] = c->wsB; J.fs_out = (long)nz * g.CB;
+    J.coef[0][0] = CC_ONE;
+    cols(c, J);
+    c2r(c, 3, nz, c->wsB, o3, (long)g.nplane_big, true, g.nx / 2);
+  }
+  k_scalar_prod<<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
+                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
+  double* rt = c->f[LES_RHS_T];
+  const double* b6 = bigf[6];
+  op_dealias2(c, &rt, &b6, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+  double* tx = c->tmp;
+  double* ty = c->tmp + g.nfield;
+  double* dxy = c->tmp + 2 * g.nfield;
+  k_scalar_temp_xy<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
+                                                          g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
+  {
+    const double sc = 1.0 / (double)(g.nx * g.ny);
+    const double* ii[2] = {tx, ty};
+    const double s2[2] = {sc, sc};
+    r2c(c, 2, nz, ii, (long)g.nplane, s2, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+    J.nin = 2; J.nout = 1; J.in[0] = c->wsA; J.in[1] = (C2*)c->wsA + (size_t)nz * g.C; J.out[0] = c->wsB;
+    J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
+    cols(c, J);
+    c2r(c, 1, nz, c->wsB, &dxy, (long)g.nplane, false, g.lh);
+  }
+  k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
+                                                                 c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
+                                                                 1.0 / g.dz); LES_COUNT_LAUNCH();
+  k_plane_sum<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred); LES_COUNT_LAUNCH();
+  const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
+  k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], c->dred, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
+                                                    nz, g_hat, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
+  if (c->jt == 1 && !k.initsc)
+    cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
+                    c->stream);
+  const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
+  k_step_scalar<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx,
+                                                       g.ny, nz, k.dt, topg, k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
+  return 0;
+}
+
+static int convec_fused(les_ctx* c, double* const* bigf, double* cx, double* cy, double* cz) {
+  const Grid& g = c->g;
+  const size_t FS = (size_t)g.nz * g.C;
+  C2* vs = (C2*)c->wsA;
+  k_vort_spec<<<grid1(FS), 256, 0, c->stream>>>(c->spec, c->spec + FS, c->spec + 2 * FS, c->wspec, c->wspec + g.C, vs,
+                                               vs + FS, vs + 2 * FS, c->kx, c->ky, (int)g.C, g.nz, 1.0 / g.dz); LES_COUNT_LAUNCH();
+  {
+    double* o3[3] = {bigf[3], bigf[4], bigf[5]};
+    ColJob J = coljob(c, MAP_PAD, DIR_INV, g.nz);
+    J.nin = 1; J.nout = 1; J.nf = 3;
+    J.in[0] = vs; J.fs_in = (long)FS;
+    J.out[0] = c->wsB; J.fs_out = (long)g.nz * g.CB;
+    J.coef[0][0] = CC_ONE;
+    cols(c, J);
+    c2r(c, 3, g.nz, c->wsB, o3, (long)g.nplane_big, true, g.nx / 2);
+  }
+  const double cst2 = 1.0 / (double)(g.nx2 * g.ny2);
+  k_convec_prod<<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
+      bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5], bigf[6], bigf[7], bigf[8], g.ld_big, g.nx2, g.ny2,
+      g.nz, cst2); LES_COUNT_LAUNCH();
+  double* outs[3] = {cx, cy, cz};
+  const double* bins[3] = {bigf[6], bigf[7], bigf[8]};
+  op_dealias2(c, outs, bins, 3, g.nz - 1, 1.0);
+  const size_t top = (size_t)(g.nz - 1) * g.nplane;
+  fill(c, cx + top, g.nplane, LES_BOGUS);
+  fill(c, cy + top, g.nplane, LES_BOGUS);
+  fill(c, cz + top, g.nplane, LES_BOGUS);
+  return 0;
+}
+
 // main.f90:202-478, one iteration on the device-resident state
 int step_fp64(les_ctx* c) {
   const Grid& g = c->g;
@@ -1587,24 +2015,33 @@ int step_fp64(les_ctx* c) {
     double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
     double* x3[3] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX]};
     double* y3[3] = {c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
-    filt_da_multi(c, f3, x3, y3, 3, g.nz);
+    filt_da_multi_spec(c, f3, x3, y3, 3, g.nz, c->spec);
   }
   op_ddz(c, c->f[LES_DUDZ], c->f[LES_U], 1);
   op_ddz(c, c->f[LES_DVDZ], c->f[LES_V], 1);
   op_ddz(c, c->f[LES_DWDZ], c->f[LES_W], 0);
   op_wallstress(c);
-  op_sgs_stag(c);
-  if (k.s_flag) op_theta(c);
+  {  // spectra of the wall planes dudz(1), dvdz(1) set by wallstress
+    const double cs = 1.0 / (double)(g.nx * g.ny);
+    const double* pl[2] = {c->f[LES_DUDZ], c->f[LES_DVDZ]};
+    const double sc[2] = {cs, cs};
+    plane_spectra(c, 2, pl, sc, c->wspec);
+  }
+  sgs_stag_fused(c);
+  double* bigf[9];
+  for (int q = 0; q < 9; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
+  pad_from_spectra(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
+  if (k.s_flag) theta_fused(c, bigf);
   else fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
   op_divstress(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
-  op_convec(c, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
+  convec_fused(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
   const size_t nv = g.nplane * (g.nz - 1);
   k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
       c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
       c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL], nv,
       g.nplane, k.dt, k.s_flag, (c->jt == 1 && !k.initu) ? 1 : 0); LES_COUNT_LAUNCH();
   op_press(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
-  k_dpdz_project<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
+  k_dpdz_project<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
                                                         c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX],
                                                         c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
                                                         k.dt); LES_COUNT_LAUNCH();
