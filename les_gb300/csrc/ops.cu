@@ -1291,8 +1291,11 @@ int thomas_tables(les_ctx* c) {
   cudaMemcpy(ky.data(), c->ky, NK * sizeof(double), cudaMemcpyDeviceToHost);
   const double dz = g.dz, idz2 = 1.0 / (dz * dz);
   for (size_t t = 0; t < NK; ++t) {
+    const int jx = (int)(t % lh), jy = (int)(t / lh);
     double bet = -1.0;
     ib[t] = 1.0 / bet;
+    // modes tridag_array skips: kx = ky = 0 and the Nyquist row / column
+    if (t == 0 || jy == ny / 2 || jx == lh - 1) continue;
     const double bmid = -(kx[t] * kx[t] + ky[t] * ky[t] + 2.0 / (dz * dz));
     double cprev = 1.0;
     for (int j = 2; j <= n; ++j) {
