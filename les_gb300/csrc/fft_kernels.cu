@@ -120,7 +120,7 @@ __device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT
   }
 }
 
-template <typename T, int TX>
+template <typename T, int TX, typename CIn>
 __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanDev Pout) {
   typedef typename CT<T>::type C;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -131,11 +131,16 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
   const int jx0 = blockIdx.x * TX;
   const int lev = blockIdx.y;
   for (int i = 0; i < J.nin; ++i) {
-    const C* src = reinterpret_cast<const C*>(J.in[i]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in;
+    const CIn* src = reinterpret_cast<const CIn*>(J.in[i]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in;
     for (int t = threadIdx.x; t < J.ny_in * TX; t += blockDim.x) {
       const int row = t / TX, b = t - row * TX;
       const int jx = jx0 + b;
-      IN[i * J.ny_in * TX + t] = jx < J.ncols ? src[(size_t)row * J.wc_in + jx] : mk<T>((T)0, (T)0);
+      C v = mk<T>((T)0, (T)0);
+      if (jx < J.ncols) {
+        const CIn x = src[(size_t)row * J.wc_in + jx];
+        v = mk<T>((T)x.x, (T)x.y);
+      }
+      IN[i * J.ny_in * TX + t] = v;
     }
   }
   __syncthreads();
@@ -225,26 +230,28 @@ int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   return 0;
 }
 
-template <typename T>
+template <typename T, typename CIn>
 int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  constexpr int TX = 4;
+  // FP64 tiles of 4 columns (64 B rows); FP32 tiles of 8 (64 B rows)
+  constexpr int TX = sizeof(T) == 8 ? 4 : 8;
   const int nymax = J.ny_in > J.ny_out ? J.ny_in : J.ny_out;
   const size_t sm = (size_t)(J.nin * J.ny_in + 2 * nymax) * TX * sizeof(C);
   dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
   if (sm > 48 * 1024)
-    cudaFuncSetAttribute(k_cols<T, TX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_cols<T, TX><<<grid, 256, sm, s>>>(J, Pin, Pout); LES_COUNT_LAUNCH();
+    cudaFuncSetAttribute(k_cols<T, TX, CIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_cols<T, TX, CIn><<<grid, 256, sm, s>>>(J, Pin, Pout); LES_COUNT_LAUNCH();
   return 0;
 }
 
 template int launch_rows_r2c<double, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_c2r<double, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
-template int launch_cols<double>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
+template int launch_cols<double, double2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 template int launch_rows_r2c<float, float>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_r2c<float, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_c2r<float, float>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_c2r<float, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
-template int launch_cols<float>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
+template int launch_cols<float, float2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
+template int launch_cols<float, double2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 
 }  // namespace les

@@ -336,7 +336,7 @@ int les_step(les_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return LES_ERR_ARG;
   if (!c->surface_set) { les_set_error("les_set_surface must be called before les_step"); return LES_ERR_STATE; }
   for (int i = 0; i < nsteps; ++i) {
-    int st = step_fp64(c);
+    int st = c->cfg.precision == 1 ? step_mixed(c) : step_fp64(c);
     if (st) return st;
   }
   cudaError_t e = cudaGetLastError();

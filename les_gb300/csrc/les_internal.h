@@ -12,7 +12,7 @@ template <typename T, typename TIn>
 int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s);
 template <typename T, typename TOut>
 int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s);
-template <typename T>
+template <typename T, typename CIn>
 int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s);
 
 // Host-side FFT plan: owns the device twiddle table.
@@ -82,6 +82,7 @@ struct les_ctx {
 
 namespace les {
 int step_fp64(les_ctx* c);
+int step_mixed(les_ctx* c);
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev);
 int op_ddxy(les_ctx* c, double* dfdx, double* dfdy, const double* f, int nlev);
 int op_test_filter(les_ctx* c, double* out, const double* in, int nplanes, int which, long pstride);

@@ -1,6 +1,7 @@
 // Per-routine device operations and the fused FP64 time step.
 // Every kernel cites the reference routine it restates (file:line).
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include "les_internal.h"
 
@@ -25,9 +26,11 @@ static void fill(les_ctx* c, double* p, size_t n, double v) {
 }
 
 // ---------------------------------------------------------------------------
-// spectral pipeline helpers
-static int r2c(les_ctx* c, int nf, int nlev, const double* const* in, long pstride,
-               const double* scale, const double* div, void* ws, bool big, int ncols) {
+// spectral pipeline helpers (T: transform precision; TIn/TOut: physical storage)
+template <typename T, typename TIn>
+static int r2cT(les_ctx* c, int nf, int nlev, const TIn* const* in, long pstride, const double* scale,
+                const double* div, void* ws, bool big, int ncols) {
+  typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   for (int f0 = 0; f0 < nf; f0 += JOB_MAXF) {
     const int n = std::min(JOB_MAXF, nf - f0);
@@ -41,16 +44,17 @@ static int r2c(les_ctx* c, int nf, int nlev, const double* const* in, long pstri
     J.pstride_work = (long)J.ny * J.wc;
     for (int f = 0; f < n; ++f) {
       J.phys[f] = in[f0 + f];
-      J.work[f] = (C2*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
+      J.work[f] = (CX*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
       J.scale[f] = scale ? scale[f0 + f] : 1.0;
       J.div[f] = div ? div[f0 + f] : 0.0;
     }
-    launch_rows_r2c<double, double>(J, big ? c->rxb.r : c->rx.r, c->stream);
+    launch_rows_r2c<T, TIn>(J, big ? c->rxb.r : c->rx.r, c->stream);
   }
   return 0;
 }
-static int c2r(les_ctx* c, int nf, int nlev, void* ws, double* const* out, long pstride, bool big,
-               int ncols) {
+template <typename T, typename TOut>
+static int c2rT(les_ctx* c, int nf, int nlev, void* ws, TOut* const* out, long pstride, bool big, int ncols) {
+  typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   for (int f0 = 0; f0 < nf; f0 += JOB_MAXF) {
     const int n = std::min(JOB_MAXF, nf - f0);
@@ -64,13 +68,21 @@ static int c2r(les_ctx* c, int nf, int nlev, void* ws, double* const* out, long 
     J.pstride_work = (long)J.ny * J.wc;
     for (int f = 0; f < n; ++f) {
       J.phys[f] = out[f0 + f];
-      J.work[f] = (C2*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
+      J.work[f] = (CX*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
       J.scale[f] = 1.0;
       J.div[f] = 0.0;
     }
-    launch_rows_c2r<double, double>(J, big ? c->rxb.r : c->rx.r, c->stream);
+    launch_rows_c2r<T, TOut>(J, big ? c->rxb.r : c->rx.r, c->stream);
   }
   return 0;
+}
+static int r2c(les_ctx* c, int nf, int nlev, const double* const* in, long pstride,
+               const double* scale, const double* div, void* ws, bool big, int ncols) {
+  return r2cT<double, double>(c, nf, nlev, in, pstride, scale, div, ws, big, ncols);
+}
+static int c2r(les_ctx* c, int nf, int nlev, void* ws, double* const* out, long pstride, bool big,
+               int ncols) {
+  return c2rT<double, double>(c, nf, nlev, ws, out, pstride, big, ncols);
 }
 static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
   const Grid& g = c->g;
@@ -90,11 +102,13 @@ static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
   J.ps_out = (long)J.ny_out * J.wc_out;
   return J;
 }
-static int cols(les_ctx* c, const ColJob& J) {
+template <typename T, typename CIn>
+static int colsT(les_ctx* c, const ColJob& J) {
   const FftPlanDev& Pin = (J.ny_in == c->g.ny) ? c->cy.c : c->cyb.c;
   const FftPlanDev& Pout = (J.ny_out == c->g.ny) ? c->cy.c : c->cyb.c;
-  return launch_cols<double>(J, Pin, Pout, c->stream);
+  return launch_cols<T, CIn>(J, Pin, Pout, c->stream);
 }
+static int cols(les_ctx* c, const ColJob& J) { return colsT<double, double2>(c, J); }
 
 // ---------------------------------------------------------------------------
 // deterministic reductions (fixed order: one CTA per plane, fixed tree)
@@ -242,7 +256,7 @@ int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse) {
   if (!inverse) {
     launch_rows_r2c<double, double>(J, rp.r, c->stream);
     K.dir = DIR_FWD; K.in[0] = c->wsA; K.out[0] = c->wsB;
-    launch_cols<double>(K, cp.c, cp.c, c->stream);
+    launch_cols<double, double2>(K, cp.c, cp.c, c->stream);
     // copy spectra back into the planes (complex view of (ld,ny))
     cudaMemcpy2DAsync(planes, (size_t)J.ld * sizeof(double), c->wsB, (size_t)lhh * sizeof(C2),
                       (size_t)lhh * sizeof(C2), (size_t)nyy * nplanes, cudaMemcpyDeviceToDevice, c->stream);
@@ -250,7 +264,7 @@ int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse) {
     cudaMemcpy2DAsync(c->wsA, (size_t)lhh * sizeof(C2), planes, (size_t)J.ld * sizeof(double),
                       (size_t)lhh * sizeof(C2), (size_t)nyy * nplanes, cudaMemcpyDeviceToDevice, c->stream);
     K.dir = DIR_INV; K.in[0] = c->wsA; K.out[0] = c->wsB;
-    launch_cols<double>(K, cp.c, cp.c, c->stream);
+    launch_cols<double, double2>(K, cp.c, cp.c, c->stream);
     J.work[0] = c->wsB;
     launch_rows_c2r<double, double>(J, rp.r, c->stream);
   }
@@ -646,7 +660,8 @@ __global__ void k_lag_prep(const double* __restrict__ u, const double* __restric
 __device__ __forceinline__ double pow_m18(double x) { return 1.0 / sqrt(sqrt(sqrt(x))); }
 
 // lagrange_Sdep.f90:268-421 from the 42 filtered planes (G: q, GG: 21+q)
-__global__ void k_lag_final(const double* __restrict__ flt, double* F_LM, double* F_MM, double* F_QN,
+template <typename S>
+__global__ void k_lag_final(const S* __restrict__ flt, double* F_LM, double* F_MM, double* F_QN,
                             double* F_NN, double* Beta, double* Cs, int ld, int nx, int ny, int nz, int jz0,
                             int nlev, size_t np, double cst, double opftdelta, double lagran_dt, int bexp_one,
                             double bexp) {
@@ -659,8 +674,8 @@ __global__ void k_lag_final(const double* __restrict__ flt, double* F_LM, double
     const size_t gi = (size_t)(jz - 1) * np + r;
     if (jx >= nx) { Cs[gi] = (double)1e-24f; continue; }
     const size_t st = np * nlev;
-    const double* G = flt + t;
-    const double* H = flt + t + 21 * st;
+    const S* G = flt + t;
+    const S* H = flt + t + 21 * st;
     const double ub = G[0], vb = G[st], wb = G[2 * st];
     const double uh = H[0], vh = H[st], wh = H[2 * st];
     const double Lq[6] = {G[3 * st] - ub * ub, G[4 * st] - ub * vb, G[5 * st] - ub * wb,
@@ -749,7 +764,7 @@ int op_lagrange(les_ctx* c, const double* const* S) {
     double* out[42];
     for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
     c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
-    k_lag_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+    k_lag_final<double><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
         c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
   }
@@ -1058,25 +1073,27 @@ __global__ void k_vort(const double* __restrict__ dudy, const double* __restrict
   }
 }
 // convec.f90:117-217 products on the 3/2 grid, levels 1..nz-1
-__global__ void k_convec_prod(const double* __restrict__ u1, const double* __restrict__ u2,
-                              const double* __restrict__ u3, const double* __restrict__ w1,
-                              const double* __restrict__ w2, const double* __restrict__ w3, double* ccx,
-                              double* ccy, double* ccz, int ldb, int nx2, int ny2, int nz, double cst) {
+template <typename S>
+__global__ void k_convec_prod(const S* __restrict__ u1, const S* __restrict__ u2,
+                              const S* __restrict__ u3, const S* __restrict__ w1,
+                              const S* __restrict__ w2, const S* __restrict__ w3, S* ccx,
+                              S* ccy, S* ccz, int ldb, int nx2, int ny2, int nz, S cst) {
   const size_t np = (size_t)ldb * ny2;
   GSTRIDE(i, np * (nz - 1)) {
     const int jz = (int)(i / np) + 1;
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ldb);
     if (jx >= nx2) continue;
     const size_t ip = i + np;
+    const S h = (S)0.5;
     if (jz == 1) {
-      ccx[i] = cst * (u2[i] * (-w3[i]) + 0.5 * u3[ip] * (w2[ip]));
-      ccy[i] = cst * (u1[i] * (w3[i]) + 0.5 * u3[ip] * (-w1[ip]));
-      ccz[i] = 0.0;
+      ccx[i] = cst * (u2[i] * (-w3[i]) + h * u3[ip] * (w2[ip]));
+      ccy[i] = cst * (u1[i] * (w3[i]) + h * u3[ip] * (-w1[ip]));
+      ccz[i] = (S)0;
     } else {
       const size_t im = i - np;
-      ccx[i] = cst * (u2[i] * (-w3[i]) + 0.5 * (u3[ip] * (w2[ip]) + u3[i] * (w2[i])));
-      ccy[i] = cst * (u1[i] * (w3[i]) + 0.5 * (u3[ip] * (-w1[ip]) + u3[i] * (-w1[i])));
-      ccz[i] = cst * 0.5 * ((u1[i] + u1[im]) * (-w2[i]) + (u2[i] + u2[im]) * (w1[i]));
+      ccx[i] = cst * (u2[i] * (-w3[i]) + h * (u3[ip] * (w2[ip]) + u3[i] * (w2[i])));
+      ccy[i] = cst * (u1[i] * (w3[i]) + h * (u3[ip] * (-w1[ip]) + u3[i] * (-w1[i])));
+      ccz[i] = cst * h * ((u1[i] + u1[im]) * (-w2[i]) + (u2[i] + u2[im]) * (w1[i]));
     }
   }
 }
@@ -1103,7 +1120,7 @@ int op_convec(les_ctx* c, double* cx, double* cy, double* cz) {
     c2r(c, 6, g.nz, c->wsB, bigf, (long)g.nplane_big, true, g.nx / 2);
   }
   const double cst2 = 1.0 / (double)(g.nx2 * g.ny2);
-  k_convec_prod<<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
+  k_convec_prod<double><<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
       bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5], bigf[6], bigf[7], bigf[8], g.ld_big, g.nx2, g.ny2,
       g.nz, cst2); LES_COUNT_LAUNCH();
   double* outs[3] = {cx, cy, cz};
@@ -1427,18 +1444,19 @@ __global__ void k_sflux(const double* __restrict__ theta, const double* __restri
   }
 }
 // scalars_module.f90:321-346 advection product on the 3/2 grid
-__global__ void k_scalar_prod(const double* __restrict__ um, const double* __restrict__ vm,
-                              const double* __restrict__ wm, const double* __restrict__ sx,
-                              const double* __restrict__ sy, const double* __restrict__ sz, double* R, int ldb,
+template <typename S>
+__global__ void k_scalar_prod(const S* __restrict__ um, const S* __restrict__ vm,
+                              const S* __restrict__ wm, const S* __restrict__ sx,
+                              const S* __restrict__ sy, const S* __restrict__ sz, S* R, int ldb,
                               int nx2, int ny2, int nz) {
   const size_t np = (size_t)ldb * ny2;
   GSTRIDE(i, np * nz) {
     const int jz = (int)(i / np) + 1;
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ldb);
     if (jx >= nx2) continue;
-    if (jz == 1) R[i] = um[i] * sx[i] + vm[i] * sy[i] + (0.5 * wm[i + np]) * sz[i + np];
+    if (jz == 1) R[i] = um[i] * sx[i] + vm[i] * sy[i] + ((S)0.5 * wm[i + np]) * sz[i + np];
     else if (jz == nz) R[i] = um[i] * sx[i] + vm[i] * sy[i];
-    else R[i] = um[i] * sx[i] + vm[i] * sy[i] + (wm[i] * sz[i] + wm[i + np] * sz[i + np]) / 2.0;
+    else R[i] = um[i] * sx[i] + vm[i] * sy[i] + (wm[i] * sz[i] + wm[i + np] * sz[i + np]) / (S)2;
   }
 }
 // scalars_module.f90:364-407 horizontal SGS fluxes
@@ -1525,7 +1543,7 @@ int op_theta(les_ctx* c) {
   for (int q = 0; q < 7; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
   const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DTDX], c->f[LES_DTDY], c->f[LES_DTDZ]};
   op_dealias1(c, in, bigf, 6, nz);
-  k_scalar_prod<<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
+  k_scalar_prod<double><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
                                                            bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
   double* rt = c->f[LES_RHS_T];
   const double* b6 = bigf[6];
@@ -1663,8 +1681,9 @@ static void plane_spectra(les_ctx* c, int np, const double* const* planes, const
 }
 
 // convec.f90:67-114 vorticity spectra (x 1/(nx*ny)) from U,V,W spectra
+template <typename CO>
 __global__ void k_vort_spec(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
-                            const C2* __restrict__ D1, const C2* __restrict__ D2, C2* o1, C2* o2, C2* o3,
+                            const C2* __restrict__ D1, const C2* __restrict__ D2, CO* o1, CO* o2, CO* o3,
                             const double* __restrict__ kx, const double* __restrict__ ky, int nk, int nz,
                             double idz) {
   GSTRIDE(t, (size_t)nk * nz) {
@@ -1688,35 +1707,42 @@ __global__ void k_vort_spec(const C2* __restrict__ U, const C2* __restrict__ V, 
       a = csub(ik(w, k_y), vz);
       b = csub(uz, ik(w, k_x));
     }
-    o1[t] = a;
-    o2[t] = b;
-    o3[t] = csub(ik(v, k_x), ik(u, k_y));
+    const C2 c3 = csub(ik(v, k_x), ik(u, k_y));
+    o1[t].x = a.x; o1[t].y = a.y;
+    o2[t].x = b.x; o2[t].y = b.y;
+    o3[t].x = c3.x; o3[t].y = c3.y;
   }
 }
 
 // scalars_module.f90:289-291 padded-gradient inputs: F(dTdx/(nx ny)),
 // F(dTdy/(nx ny)), F(dTdz/(nx ny)) from the theta spectrum; levels 1 and nz
 // of dTdz come from their own plane transforms (Z1, ZN)
-__global__ void k_dtheta_spec(const C2* __restrict__ T, const C2* __restrict__ Z1, const C2* __restrict__ ZN,
-                              C2* o1, C2* o2, C2* o3, const double* __restrict__ kx,
+template <typename CI, typename CO>
+__global__ void k_dtheta_spec(const CI* __restrict__ T, const C2* __restrict__ Z1, const C2* __restrict__ ZN,
+                              CO* o1, CO* o2, CO* o3, const double* __restrict__ kx,
                               const double* __restrict__ ky, int nk, int nz, double idz) {
   GSTRIDE(t, (size_t)nk * nz) {
     const int jz = (int)(t / nk) + 1;
     const size_t m = t - (size_t)(jz - 1) * nk;
-    const C2 th = T[t];
-    o1[t] = ik(th, kx[m]);
-    o2[t] = ik(th, ky[m]);
-    if (jz == 1) o3[t] = Z1[m];
-    else if (jz == nz) o3[t] = ZN[m];
-    else o3[t] = cscale(csub(th, T[t - nk]), idz);
+    const C2 th = make_double2(T[t].x, T[t].y);
+    const C2 a = ik(th, kx[m]);
+    const C2 b = ik(th, ky[m]);
+    C2 z;
+    if (jz == 1) z = Z1[m];
+    else if (jz == nz) z = ZN[m];
+    else z = cscale(csub(th, make_double2(T[t - nk].x, T[t - nk].y)), idz);
+    o1[t].x = a.x; o1[t].y = a.y;
+    o2[t].x = b.x; o2[t].y = b.y;
+    o3[t].x = z.x; o3[t].y = z.y;
   }
 }
 
 // lagrange_Sdep.f90:131-141, sgs_stag.f90:371-498 : spectra of u_bar, v_bar,
 // w_bar and S_ij (x 1/(nx*ny)) for the levels jz0..jz0+nl-1.
 // out layout: q = 0..8 (u_bar, v_bar, w_bar, S11, S12, S13, S22, S23, S33)
+template <typename CO>
 __global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
-                           const C2* __restrict__ D1, const C2* __restrict__ D2, C2* out,
+                           const C2* __restrict__ D1, const C2* __restrict__ D2, CO* out,
                            const double* __restrict__ kx, const double* __restrict__ ky, int nk, int nz,
                            int jz0, int nl, double idz) {
   const size_t st = (size_t)nk * nl;
@@ -1757,19 +1783,17 @@ __global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, c
       wy = ik(w0, k_y);
       wz = cscale(cadd(ddz_w(jz), ddz_w(jz - 1)), 0.5);
     }
-    out[t] = ub; out[t + st] = vb; out[t + 2 * st] = wb;
-    out[t + 3 * st] = ux;
-    out[t + 4 * st] = cscale(cadd(uy, vx), 0.5);
-    out[t + 5 * st] = cscale(cadd(uz, wx), 0.5);
-    out[t + 6 * st] = vy;
-    out[t + 7 * st] = cscale(cadd(vz, wy), 0.5);
-    out[t + 8 * st] = wz;
+    const C2 r[9] = {ub, vb, wb, ux, cscale(cadd(uy, vx), 0.5), cscale(cadd(uz, wx), 0.5),
+                     vy, cscale(cadd(vz, wy), 0.5), wz};
+#pragma unroll
+    for (int q = 0; q < 9; ++q) { out[t + q * st].x = r[q].x; out[t + q * st].y = r[q].y; }
   }
 }
 
 // lagrange_Sdep.f90:142-266 physical products (12 planes per level)
+template <typename S>
 __global__ void k_lag_prod(const double* __restrict__ u, const double* __restrict__ v,
-                           const double* __restrict__ w, Ptr6 Sp, double* out, int ld, int jz0, int nlev,
+                           const double* __restrict__ w, Ptr6 Sp, S* out, int ld, int jz0, int nlev,
                            size_t np) {
   const size_t tot = np * nlev;
   GSTRIDE(t, tot) {
@@ -1781,17 +1805,31 @@ __global__ void k_lag_prod(const double* __restrict__ u, const double* __restric
     if (jz == 1) { ub = u[i]; vb = v[i]; wb = 0.25 * w[i + np]; }
     else { ub = 0.5 * (u[i] + u[i - np]); vb = 0.5 * (v[i] + v[i - np]); wb = w[i]; }
     const size_t stride = np * nlev;
-    double* o = out + t;
-    o[0] = ub * ub; o[stride] = ub * vb; o[2 * stride] = ub * wb;
-    o[3 * stride] = vb * vb; o[4 * stride] = vb * wb; o[5 * stride] = wb * wb;
+    S* o = out + t;
+    o[0] = (S)(ub * ub); o[stride] = (S)(ub * vb); o[2 * stride] = (S)(ub * wb);
+    o[3 * stride] = (S)(vb * vb); o[4 * stride] = (S)(vb * wb); o[5 * stride] = (S)(wb * wb);
     const double s11 = Sp.p[0][i], s12 = Sp.p[1][i], s13 = Sp.p[2][i], s22 = Sp.p[3][i], s23 = Sp.p[4][i], s33 = Sp.p[5][i];
-    const double S = smag(s11, s22, s33, s12, s13, s23);
-    o[6 * stride] = S * s11; o[7 * stride] = S * s12; o[8 * stride] = S * s13;
-    o[9 * stride] = S * s22; o[10 * stride] = S * s23; o[11 * stride] = S * s33;
+    const double Sm = smag(s11, s22, s33, s12, s13, s23);
+    o[6 * stride] = (S)(Sm * s11); o[7 * stride] = (S)(Sm * s12); o[8 * stride] = (S)(Sm * s13);
+    o[9 * stride] = (S)(Sm * s22); o[10 * stride] = (S)(Sm * s23); o[11 * stride] = (S)(Sm * s33);
   }
 }
 
-static int lagrange_fused(les_ctx* c) {
+// Precision of the fused-step transforms: MX = false -> FP64 everywhere;
+// MX = true -> FP32 transforms and FP32 3/2-grid / filter temporaries for the
+// scalar, convective, stress-divergence and SGS terms (the projection path,
+// filt_da of u, v, w and the plane/wall quantities stay FP64).
+template <bool MX> struct PX {
+  typedef typename std::conditional<MX, float, double>::type T;     // transform precision
+  typedef typename CT<T>::type CX;                                   // its complex type
+  typedef T S;                                                       // temporary storage
+};
+
+template <bool MX>
+static int lagrangeT(les_ctx* c) {
+  typedef typename PX<MX>::T T;
+  typedef typename PX<MX>::CX CX;
+  typedef typename PX<MX>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   op_interpolag(c);
@@ -1808,24 +1846,23 @@ static int lagrange_fused(les_ctx* c) {
   const C2* V = c->spec + (size_t)g.nz * g.C;
   const C2* W = c->spec + (size_t)2 * g.nz * g.C;
   const int nch = c->lag_chunk;
+  S* tmpS = reinterpret_cast<S*>(c->tmp);
   for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
     const int nl = std::min(nch, g.nz - jz0 + 1);
     const long FS = (long)nl * g.C;
-    double* prod = c->tmp;                                // 12 * nl planes
-    double* flt = c->tmp + (size_t)21 * nch * g.nplane;    // 42 * nl planes
-    // spectral inputs (9) in wsA after the product x-spectra (12)
-    C2* xs = (C2*)c->wsA;
-    C2* sp = xs + (size_t)12 * FS;
-    k_lag_spec<<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx, c->ky,
-                                                              (int)g.C, g.nz, jz0, nl, 1.0 / g.dz); LES_COUNT_LAUNCH();
-    k_lag_prod<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
-                                                           jz0, nl, g.nplane); LES_COUNT_LAUNCH();
-    const double* in[12];
+    S* prod = tmpS;                                   // 12 * nl planes
+    S* flt = tmpS + (size_t)21 * nch * g.nplane;      // 42 * nl planes
+    CX* xs = (CX*)c->wsA;
+    CX* sp = xs + (size_t)12 * FS;
+    k_lag_spec<CX><<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx,
+                                                                  c->ky, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz); LES_COUNT_LAUNCH();
+    k_lag_prod<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
+                                                              jz0, nl, g.nplane); LES_COUNT_LAUNCH();
+    const S* in[12];
     for (int q = 0; q < 12; ++q) in[q] = prod + (size_t)q * nl * g.nplane;
-    r2c(c, 12, nl, in, (long)g.nplane, nullptr, nullptr, xs, false, g.lh);
-    C2* ob = (C2*)c->wsB;
-    // (input block, first input index in block, count, output q base)
-    struct Blk { C2* base; int dir; int code_g, code_gg; int count; int q0; };
+    r2cT<T, S>(c, 12, nl, in, (long)g.nplane, nullptr, nullptr, xs, false, g.lh);
+    CX* ob = (CX*)c->wsB;
+    struct Blk { CX* base; int dir; int code_g, code_gg; int count; int q0; };
     const Blk blks[4] = {{sp, DIR_INV, CC_MASK, CC_MASK4, 3, 0},
                          {sp + 3 * FS, DIR_INV, CC_MASK, CC_MASK4, 6, 9},
                          {xs, DIR_BOTH, CC_G, CC_GG, 6, 3},
@@ -1839,19 +1876,20 @@ static int lagrange_fused(les_ctx* c) {
       J.out[1] = ob + (size_t)(21 + b.q0) * FS;
       J.fs_out = FS;
       J.coef[0][0] = b.code_g; J.coef[1][0] = b.code_gg;
-      cols(c, J);
+      colsT<T, CX>(c, J);
     }
-    double* out[42];
+    S* out[42];
     for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
-    c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
-    k_lag_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+    c2rT<T, S>(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    k_lag_final<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
         c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
   }
   return 0;
 }
 
-static int sgs_stag_fused(les_ctx* c) {
+template <bool MX>
+static int sgs_stagT(les_ctx* c) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const bool lag = (k.model == 4 || k.model == 5 || k.model == 7);
@@ -1867,7 +1905,7 @@ static int sgs_stag_fused(les_ctx* c) {
       op_scaledep(c, csz, S);
       k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
     } else if (k.model == 5) {
-      lagrange_fused(c);
+      lagrangeT<MX>(c);
     }
   }
   int ov = 0;
@@ -1885,27 +1923,111 @@ static int sgs_stag_fused(les_ctx* c) {
   return 0;
 }
 
-// inverse-only 3/2 padding of full spectra: nf fields (field stride nz*C) -> big physical
-static void pad_from_spectra(les_ctx* c, const C2* spec, int nf, double* const* out) {
+// inverse-only 3/2 padding of full spectra (field stride nz*C) -> big physical
+template <bool MX, typename CIn>
+static void padT(les_ctx* c, const CIn* spec, int nf, typename PX<MX>::S* const* out) {
+  typedef typename PX<MX>::T T;
   const Grid& g = c->g;
   ColJob J = coljob(c, MAP_PAD, DIR_INV, g.nz);
   J.nin = 1; J.nout = 1; J.nf = nf;
   J.in[0] = spec; J.fs_in = (long)g.nz * g.C;
   J.out[0] = c->wsB; J.fs_out = (long)g.nz * g.CB;
   J.coef[0][0] = CC_ONE;
-  cols(c, J);
-  c2r(c, nf, g.nz, c->wsB, out, (long)g.nplane_big, true, g.nx / 2);
+  colsT<T, CIn>(c, J);
+  c2rT<T, typename PX<MX>::S>(c, nf, g.nz, c->wsB, out, (long)g.nplane_big, true, g.nx / 2);
 }
 
-static int theta_fused(les_ctx* c, double* const* bigf) {
+// dealias2 of nf big fields (already scaled) into FP64 small fields
+template <bool MX>
+static void unpadT(les_ctx* c, typename PX<MX>::S* const* in, double* const* out, int nf, int nlev, double scale) {
+  typedef typename PX<MX>::T T;
+  typedef typename PX<MX>::CX CX;
+  typedef typename PX<MX>::S S;
+  const Grid& g = c->g;
+  double sc[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) sc[i] = scale;
+  const S* ii[JOB_MAXF];
+  for (int i = 0; i < nf; ++i) ii[i] = in[i];
+  r2cT<T, S>(c, nf, nlev, ii, (long)g.nplane_big, sc, nullptr, c->wsA, true, g.nx / 2);
+  ColJob J = coljob(c, MAP_UNPAD, DIR_BOTH, nlev);
+  J.nin = 1; J.nout = 1; J.nf = nf;
+  J.in[0] = c->wsA; J.fs_in = (long)nlev * g.CB;
+  J.out[0] = c->wsB; J.fs_out = (long)nlev * g.C;
+  J.coef[0][0] = CC_ONE;
+  colsT<T, CX>(c, J);
+  c2rT<T, double>(c, nf, nlev, c->wsB, out, (long)g.nplane, false, g.nx / 2);
+}
+
+// ddx + ddy of two FP64 fields summed in spectral space (one inverse)
+template <bool MX>
+static void div_xyT(les_ctx* c, const double* tx, const double* ty, double* out, int nlev) {
+  typedef typename PX<MX>::T T;
+  typedef typename PX<MX>::CX CX;
+  const Grid& g = c->g;
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* ii[2] = {tx, ty};
+  const double s2[2] = {sc, sc};
+  r2cT<T, double>(c, 2, nlev, ii, (long)g.nplane, s2, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nlev);
+  J.nin = 2; J.nout = 1; J.in[0] = c->wsA; J.in[1] = (CX*)c->wsA + (size_t)nlev * g.C; J.out[0] = c->wsB;
+  J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
+  colsT<T, CX>(c, J);
+  c2rT<T, double>(c, 1, nlev, c->wsB, &out, (long)g.nplane, false, g.lh);
+}
+
+template <bool MX>
+static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
+  typedef typename PX<MX>::T T;
+  typedef typename PX<MX>::CX CX;
+  const Grid& g = c->g;
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[5] = {c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ], c->f[LES_TYZ]};
+  double scs[5] = {sc, sc, sc, sc, sc};
+  r2cT<T, double>(c, 5, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  const long FS = (long)g.nz * g.C;
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
+  J.nin = 3; J.nout = 2;
+  J.in[0] = c->wsA; J.in[1] = (CX*)c->wsA + FS; J.in[2] = (CX*)c->wsA + 2 * FS;
+  J.out[0] = c->wsB; J.out[1] = (CX*)c->wsB + FS;
+  J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
+  J.coef[1][1] = CC_IKX; J.coef[1][2] = CC_IKY;
+  colsT<T, CX>(c, J);
+  ColJob K = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
+  K.nin = 2; K.nout = 1;
+  K.in[0] = (CX*)c->wsA + 3 * FS; K.in[1] = (CX*)c->wsA + 4 * FS;
+  K.out[0] = (CX*)c->wsB + 2 * FS;
+  K.coef[0][0] = CC_IKX; K.coef[0][1] = CC_IKY;
+  colsT<T, CX>(c, K);
+  double* h[3] = {c->tmp, c->tmp + g.nfield, c->tmp + 2 * g.nfield};
+  c2rT<T, double>(c, 3, g.nz, c->wsB, h, (long)g.nplane, false, g.lh);
+  k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divtx, divty, divtz, h[0], h[1], h[2], c->f[LES_TXZ],
+                                                         c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz,
+                                                         1.0 / g.dz, 7); LES_COUNT_LAUNCH();
+  return 0;
+}
+
+template <bool MX>
+static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
+  typedef typename PX<MX>::T T;
+  typedef typename PX<MX>::CX CX;
+  typedef typename PX<MX>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const int nz = g.nz;
-  {
-    double* f1[1] = {c->f[LES_THETA]};
-    double* x1[1] = {c->f[LES_DTDX]};
-    double* y1[1] = {c->f[LES_DTDY]};
-    filt_da_multi_spec(c, f1, x1, y1, 1, nz, c->spec + (size_t)3 * nz * g.C);
+  const size_t FS = (size_t)nz * g.C;
+  CX* specT = reinterpret_cast<CX*>(c->spec + 3 * FS);  // theta spectrum (precision of the transform)
+  {  // filt_da(theta) with the spectrum saved
+    const double* in[1] = {c->f[LES_THETA]};
+    const double sc[1] = {1.0 / (double)(g.nx * g.ny)};
+    r2cT<T, double>(c, 1, nz, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+    J.nin = 1; J.nout = 4; J.inv_mask = 7u;
+    J.in[0] = c->wsA;
+    J.out[0] = c->wsB; J.out[1] = (CX*)c->wsB + FS; J.out[2] = (CX*)c->wsB + 2 * FS; J.out[3] = specT;
+    J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY; J.coef[3][0] = CC_KILL;
+    colsT<T, CX>(c, J);
+    double* out[3] = {c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY]};
+    c2rT<T, double>(c, 3, nz, c->wsB, out, (long)g.nplane, false, g.lh);
   }
   op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
   fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
@@ -1914,49 +2036,33 @@ static int theta_fused(les_ctx* c, double* const* bigf) {
                                                             c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
                                                             c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
                                                             k.t_scale * k.u_star, k.vonk, g.dz); LES_COUNT_LAUNCH();
-  // spectra of the dTdz wall and top planes (dealias1 scaling 1/(nx*ny))
   {
     const double cs = 1.0 / (double)(g.nx * g.ny);
     const double* pl[2] = {c->f[LES_DTDZ], c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane};
     const double sc[2] = {cs, cs};
     plane_spectra(c, 2, pl, sc, c->wspec + 2 * g.C);
   }
-  C2* ds = (C2*)c->wsA;  // 3 derivative spectra (nz levels each)
-  const size_t FS = (size_t)nz * g.C;
-  k_dtheta_spec<<<grid1(FS), 256, 0, c->stream>>>(c->spec + 3 * FS, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds,
-                                                 ds + FS, ds + 2 * FS, c->kx, c->ky, (int)g.C, nz, 1.0 / g.dz); LES_COUNT_LAUNCH();
+  CX* ds = (CX*)c->wsA;
+  k_dtheta_spec<CX, CX><<<grid1(FS), 256, 0, c->stream>>>(specT, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds, ds + FS,
+                                                         ds + 2 * FS, c->kx, c->ky, (int)g.C, nz, 1.0 / g.dz); LES_COUNT_LAUNCH();
   {
-    double* o3[3] = {bigf[3], bigf[4], bigf[5]};
-    // the spectra live in wsA; pad reads them and writes wsB
-    ColJob J = coljob(c, MAP_PAD, DIR_INV, nz);
-    J.nin = 1; J.nout = 1; J.nf = 3;
-    J.in[0] = ds; J.fs_in = (long)FS;
-    J.out[0] = c->wsB; J.fs_out = (long)nz * g.CB;
-    J.coef[0][0] = CC_ONE;
-    cols(c, J);
-    c2r(c, 3, nz, c->wsB, o3, (long)g.nplane_big, true, g.nx / 2);
+    S* o3[3] = {bigf[3], bigf[4], bigf[5]};
+    padT<MX, CX>(c, ds, 3, o3);
   }
-  k_scalar_prod<<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
-                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
+  k_scalar_prod<S><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
+                                                              bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
   double* rt = c->f[LES_RHS_T];
-  const double* b6 = bigf[6];
-  op_dealias2(c, &rt, &b6, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+  {
+    S* b6[1] = {bigf[6]};
+    double* o[1] = {rt};
+    unpadT<MX>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+  }
   double* tx = c->tmp;
   double* ty = c->tmp + g.nfield;
   double* dxy = c->tmp + 2 * g.nfield;
   k_scalar_temp_xy<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
                                                           g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
-  {
-    const double sc = 1.0 / (double)(g.nx * g.ny);
-    const double* ii[2] = {tx, ty};
-    const double s2[2] = {sc, sc};
-    r2c(c, 2, nz, ii, (long)g.nplane, s2, nullptr, c->wsA, false, g.lh);
-    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
-    J.nin = 2; J.nout = 1; J.in[0] = c->wsA; J.in[1] = (C2*)c->wsA + (size_t)nz * g.C; J.out[0] = c->wsB;
-    J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
-    cols(c, J);
-    c2r(c, 1, nz, c->wsB, &dxy, (long)g.nplane, false, g.lh);
-  }
+  div_xyT<MX>(c, tx, ty, dxy, nz);
   k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
                                                                  c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
                                                                  1.0 / g.dz); LES_COUNT_LAUNCH();
@@ -1973,29 +2079,29 @@ static int theta_fused(les_ctx* c, double* const* bigf) {
   return 0;
 }
 
-static int convec_fused(les_ctx* c, double* const* bigf, double* cx, double* cy, double* cz) {
+template <bool MX>
+static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, double* cy, double* cz) {
+  typedef typename PX<MX>::CX CX;
+  typedef typename PX<MX>::S S;
   const Grid& g = c->g;
   const size_t FS = (size_t)g.nz * g.C;
-  C2* vs = (C2*)c->wsA;
-  k_vort_spec<<<grid1(FS), 256, 0, c->stream>>>(c->spec, c->spec + FS, c->spec + 2 * FS, c->wspec, c->wspec + g.C, vs,
-                                               vs + FS, vs + 2 * FS, c->kx, c->ky, (int)g.C, g.nz, 1.0 / g.dz); LES_COUNT_LAUNCH();
+  CX* vs = (CX*)c->wsA;
+  k_vort_spec<CX><<<grid1(FS), 256, 0, c->stream>>>(c->spec, c->spec + FS, c->spec + 2 * FS, c->wspec, c->wspec + g.C,
+                                                   vs, vs + FS, vs + 2 * FS, c->kx, c->ky, (int)g.C, g.nz,
+                                                   1.0 / g.dz); LES_COUNT_LAUNCH();
   {
-    double* o3[3] = {bigf[3], bigf[4], bigf[5]};
-    ColJob J = coljob(c, MAP_PAD, DIR_INV, g.nz);
-    J.nin = 1; J.nout = 1; J.nf = 3;
-    J.in[0] = vs; J.fs_in = (long)FS;
-    J.out[0] = c->wsB; J.fs_out = (long)g.nz * g.CB;
-    J.coef[0][0] = CC_ONE;
-    cols(c, J);
-    c2r(c, 3, g.nz, c->wsB, o3, (long)g.nplane_big, true, g.nx / 2);
+    S* o3[3] = {bigf[3], bigf[4], bigf[5]};
+    padT<MX, CX>(c, vs, 3, o3);
   }
-  const double cst2 = 1.0 / (double)(g.nx2 * g.ny2);
-  k_convec_prod<<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
+  const S cst2 = (S)(1.0 / (double)(g.nx2 * g.ny2));
+  k_convec_prod<S><<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
       bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5], bigf[6], bigf[7], bigf[8], g.ld_big, g.nx2, g.ny2,
       g.nz, cst2); LES_COUNT_LAUNCH();
-  double* outs[3] = {cx, cy, cz};
-  const double* bins[3] = {bigf[6], bigf[7], bigf[8]};
-  op_dealias2(c, outs, bins, 3, g.nz - 1, 1.0);
+  {
+    S* bins[3] = {bigf[6], bigf[7], bigf[8]};
+    double* outs[3] = {cx, cy, cz};
+    unpadT<MX>(c, bins, outs, 3, g.nz - 1, 1.0);
+  }
   const size_t top = (size_t)(g.nz - 1) * g.nplane;
   fill(c, cx + top, g.nplane, LES_BOGUS);
   fill(c, cy + top, g.nplane, LES_BOGUS);
@@ -2004,7 +2110,9 @@ static int convec_fused(les_ctx* c, double* const* bigf, double* cx, double* cy,
 }
 
 // main.f90:202-478, one iteration on the device-resident state
-int step_fp64(les_ctx* c) {
+template <bool MX>
+static int stepT(les_ctx* c) {
+  typedef typename PX<MX>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   c->jt += 1;
@@ -2030,14 +2138,14 @@ int step_fp64(les_ctx* c) {
     const double sc[2] = {cs, cs};
     plane_spectra(c, 2, pl, sc, c->wspec);
   }
-  sgs_stag_fused(c);
-  double* bigf[9];
-  for (int q = 0; q < 9; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
-  pad_from_spectra(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
-  if (k.s_flag) theta_fused(c, bigf);
+  sgs_stagT<MX>(c);
+  S* bigf[9];
+  for (int q = 0; q < 9; ++q) bigf[q] = reinterpret_cast<S*>(c->big) + (size_t)q * g.nfield_big;
+  padT<MX, C2>(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
+  if (k.s_flag) thetaT<MX>(c, bigf);
   else fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
-  op_divstress(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
-  convec_fused(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
+  divstressT<MX>(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
+  convecT<MX>(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
   const size_t nv = g.nplane * (g.nz - 1);
   k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
       c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
@@ -2060,5 +2168,8 @@ int step_fp64(les_ctx* c) {
   }
   return 0;
 }
+
+int step_fp64(les_ctx* c) { return stepT<false>(c); }
+int step_mixed(les_ctx* c) { return stepT<true>(c); }
 
 }  // namespace les
