@@ -132,6 +132,8 @@ struct RowJob {
   void* work[JOB_MAXF];         // work buffer base (plane 0)
   double scale[JOB_MAXF];       // r2c: multiply input by scale before the transform
   double div[JOB_MAXF];         // r2c: when non-zero, input is (x / div) * scale
+  const double* off[JOB_MAXF];  // per-plane offsets: r2c subtracts off[plane] before
+                                // scaling, c2r adds it to the output (null: none)
 };
 
 // Spectral coefficient codes for the column operator.

@@ -19,10 +19,18 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
   const TIn* src = reinterpret_cast<const TIn*>(J.phys[f]) + (size_t)lev * J.pstride_phys;
   const T s = (T)J.scale[f];
   const T dv = (T)J.div[f];
+  const double off = J.off[f] ? J.off[f][lev] : 0.0;
   for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
     const int r = t / m, k = t - r * m;
     const TIn* row = src + (size_t)(row0 + r) * J.ld;
-    T a = (T)row[2 * k], b = (T)row[2 * k + 1];
+    T a, b;
+    if (J.off[f]) {  // subtract in double before rounding to T
+      a = (T)((double)row[2 * k] - off);
+      b = (T)((double)row[2 * k + 1] - off);
+    } else {
+      a = (T)row[2 * k];
+      b = (T)row[2 * k + 1];
+    }
     if (dv != (T)0) { a = a / dv; b = b / dv; }
     A[r * m + k] = mk<T>(a * s, b * s);
   }
@@ -81,13 +89,19 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
   __syncthreads();
   C* Z = fft_smem<T, false>(A, B, nrow, m, P.c, +1);
   TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys;
+  const double off = J.off[f] ? J.off[f][lev] : 0.0;
   for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
     const int r = t / (m + 1), k = t - r * (m + 1);
     TOut* row = dst + (size_t)(row0 + r) * J.ld;
     if (k < m) {
       const C z = Z[r * m + k];
-      row[2 * k] = (TOut)z.x;
-      row[2 * k + 1] = (TOut)z.y;
+      if (J.off[f]) {
+        row[2 * k] = (TOut)((double)z.x + off);
+        row[2 * k + 1] = (TOut)((double)z.y + off);
+      } else {
+        row[2 * k] = (TOut)z.x;
+        row[2 * k + 1] = (TOut)z.y;
+      }
     } else {  // padding columns ld-1:ld
       row[2 * m] = (TOut)0;
       row[2 * m + 1] = (TOut)0;

@@ -29,7 +29,7 @@ static void fill(les_ctx* c, double* p, size_t n, double v) {
 // spectral pipeline helpers (T: transform precision; TIn/TOut: physical storage)
 template <typename T, typename TIn>
 static int r2cT(les_ctx* c, int nf, int nlev, const TIn* const* in, long pstride, const double* scale,
-                const double* div, void* ws, bool big, int ncols) {
+                const double* div, void* ws, bool big, int ncols, const double* const* off = nullptr) {
   typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   for (int f0 = 0; f0 < nf; f0 += JOB_MAXF) {
@@ -47,13 +47,15 @@ static int r2cT(les_ctx* c, int nf, int nlev, const TIn* const* in, long pstride
       J.work[f] = (CX*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
       J.scale[f] = scale ? scale[f0 + f] : 1.0;
       J.div[f] = div ? div[f0 + f] : 0.0;
+      J.off[f] = off ? off[f0 + f] : nullptr;
     }
     launch_rows_r2c<T, TIn>(J, big ? c->rxb.r : c->rx.r, c->stream);
   }
   return 0;
 }
 template <typename T, typename TOut>
-static int c2rT(les_ctx* c, int nf, int nlev, void* ws, TOut* const* out, long pstride, bool big, int ncols) {
+static int c2rT(les_ctx* c, int nf, int nlev, void* ws, TOut* const* out, long pstride, bool big, int ncols,
+                const double* const* off = nullptr) {
   typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   for (int f0 = 0; f0 < nf; f0 += JOB_MAXF) {
@@ -71,6 +73,7 @@ static int c2rT(les_ctx* c, int nf, int nlev, void* ws, TOut* const* out, long p
       J.work[f] = (CX*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
       J.scale[f] = 1.0;
       J.div[f] = 0.0;
+      J.off[f] = off ? off[f0 + f] : nullptr;
     }
     launch_rows_c2r<T, TOut>(J, big ? c->rxb.r : c->rx.r, c->stream);
   }
@@ -129,6 +132,25 @@ __global__ void __launch_bounds__(512) k_plane_sum(const double* f, long pstride
     __syncthreads();
   }
   if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+// per-level plane means of f(1:nx,1:ny,lev) (same fixed order as k_plane_sum)
+__global__ void __launch_bounds__(512) k_plane_mean(const double* f, long pstride, int ld, int nx, int ny,
+                                                    double* out) {
+  __shared__ double sh[512];
+  const double* p = f + (size_t)blockIdx.x * pstride;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+    const int jy = i / nx, jx = i - jy * nx;
+    s += p[(size_t)jy * ld + jx];
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 256; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0] / (double)(nx * ny);
 }
 
 // ---------------------------------------------------------------------------
@@ -1720,7 +1742,8 @@ __global__ void k_vort_spec(const C2* __restrict__ U, const C2* __restrict__ V, 
 template <typename CI, typename CO>
 __global__ void k_dtheta_spec(const CI* __restrict__ T, const C2* __restrict__ Z1, const C2* __restrict__ ZN,
                               CO* o1, CO* o2, CO* o3, const double* __restrict__ kx,
-                              const double* __restrict__ ky, int nk, int nz, double idz) {
+                              const double* __restrict__ ky, int nk, int nz, double idz,
+                              const double* __restrict__ th0) {
   GSTRIDE(t, (size_t)nk * nz) {
     const int jz = (int)(t / nk) + 1;
     const size_t m = t - (size_t)(jz - 1) * nk;
@@ -1730,7 +1753,11 @@ __global__ void k_dtheta_spec(const CI* __restrict__ T, const C2* __restrict__ Z
     C2 z;
     if (jz == 1) z = Z1[m];
     else if (jz == nz) z = ZN[m];
-    else z = cscale(csub(th, make_double2(T[t - nk].x, T[t - nk].y)), idz);
+    else {
+      z = cscale(csub(th, make_double2(T[t - nk].x, T[t - nk].y)), idz);
+      // the spectra are of theta - th0(level): restore the mean gradient
+      if (th0 && m == 0) z.x += (th0[jz - 1] - th0[jz - 2]) * idz;
+    }
     o1[t].x = a.x; o1[t].y = a.y;
     o2[t].x = b.x; o2[t].y = b.y;
     o3[t].x = z.x; o3[t].y = z.y;
@@ -1744,7 +1771,7 @@ template <typename CO>
 __global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
                            const C2* __restrict__ D1, const C2* __restrict__ D2, CO* out,
                            const double* __restrict__ kx, const double* __restrict__ ky, int nk, int nz,
-                           int jz0, int nl, double idz) {
+                           int jz0, int nl, double idz, int shift) {
   const size_t st = (size_t)nk * nl;
   GSTRIDE(t, st) {
     const int lc = (int)(t / nk);
@@ -1783,6 +1810,10 @@ __global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, c
       wy = ik(w0, k_y);
       wz = cscale(cadd(ddz_w(jz), ddz_w(jz - 1)), 0.5);
     }
+    if (shift && m == 0) {  // filtered fluctuations about the plane mean
+      ub = make_double2(0.0, 0.0);
+      vb = make_double2(0.0, 0.0);
+    }
     const C2 r[9] = {ub, vb, wb, ux, cscale(cadd(uy, vx), 0.5), cscale(cadd(uz, wx), 0.5),
                      vy, cscale(cadd(vz, wy), 0.5), wz};
 #pragma unroll
@@ -1794,7 +1825,7 @@ __global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, c
 template <typename S>
 __global__ void k_lag_prod(const double* __restrict__ u, const double* __restrict__ v,
                            const double* __restrict__ w, Ptr6 Sp, S* out, int ld, int jz0, int nlev,
-                           size_t np) {
+                           size_t np, const C2* __restrict__ U, const C2* __restrict__ V, size_t nk) {
   const size_t tot = np * nlev;
   GSTRIDE(t, tot) {
     const int lc = (int)(t / np);
@@ -1804,6 +1835,12 @@ __global__ void k_lag_prod(const double* __restrict__ u, const double* __restric
     double ub, vb, wb;
     if (jz == 1) { ub = u[i]; vb = v[i]; wb = 0.25 * w[i + np]; }
     else { ub = 0.5 * (u[i] + u[i - np]); vb = 0.5 * (v[i] + v[i - np]); wb = w[i]; }
+    if (U) {  // L_ij is invariant to a constant shift: form it about the plane mean
+      const double u0 = (jz == 1) ? U[0].x : 0.5 * (U[(size_t)(jz - 1) * nk].x + U[(size_t)(jz - 2) * nk].x);
+      const double v0 = (jz == 1) ? V[0].x : 0.5 * (V[(size_t)(jz - 1) * nk].x + V[(size_t)(jz - 2) * nk].x);
+      ub -= u0;
+      vb -= v0;
+    }
     const size_t stride = np * nlev;
     S* o = out + t;
     o[0] = (S)(ub * ub); o[stride] = (S)(ub * vb); o[2 * stride] = (S)(ub * wb);
@@ -1855,9 +1892,11 @@ static int lagrangeT(les_ctx* c) {
     CX* xs = (CX*)c->wsA;
     CX* sp = xs + (size_t)12 * FS;
     k_lag_spec<CX><<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx,
-                                                                  c->ky, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz); LES_COUNT_LAUNCH();
+                                                                  c->ky, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz,
+                                                                  MX ? 1 : 0); LES_COUNT_LAUNCH();
     k_lag_prod<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
-                                                              jz0, nl, g.nplane); LES_COUNT_LAUNCH();
+                                                              jz0, nl, g.nplane, MX ? U : nullptr, MX ? V : nullptr,
+                                                              g.C); LES_COUNT_LAUNCH();
     const S* in[12];
     for (int q = 0; q < 12; ++q) in[q] = prod + (size_t)q * nl * g.nplane;
     r2cT<T, S>(c, 12, nl, in, (long)g.nplane, nullptr, nullptr, xs, false, g.lh);
@@ -2016,10 +2055,18 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   const int nz = g.nz;
   const size_t FS = (size_t)nz * g.C;
   CX* specT = reinterpret_cast<CX*>(c->spec + 3 * FS);  // theta spectrum (precision of the transform)
+  // FP32 transforms see theta - th0(level) (th0 = plane mean): the filter and
+  // the horizontal derivatives are unchanged by a per-level constant, and the
+  // perturbation keeps its precision; th0 is added back in FP64
+  double* th0 = MX ? c->dred + 14 * (size_t)(nz + 8) : nullptr;
+  if (MX) {
+    k_plane_mean<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, th0); LES_COUNT_LAUNCH();
+  }
   {  // filt_da(theta) with the spectrum saved
     const double* in[1] = {c->f[LES_THETA]};
     const double sc[1] = {1.0 / (double)(g.nx * g.ny)};
-    r2cT<T, double>(c, 1, nz, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh);
+    const double* offs[1] = {th0};
+    r2cT<T, double>(c, 1, nz, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh, offs);
     ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
     J.nin = 1; J.nout = 4; J.inv_mask = 7u;
     J.in[0] = c->wsA;
@@ -2027,7 +2074,8 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY; J.coef[3][0] = CC_KILL;
     colsT<T, CX>(c, J);
     double* out[3] = {c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY]};
-    c2rT<T, double>(c, 3, nz, c->wsB, out, (long)g.nplane, false, g.lh);
+    const double* offo[3] = {th0, nullptr, nullptr};
+    c2rT<T, double>(c, 3, nz, c->wsB, out, (long)g.nplane, false, g.lh, offo);
   }
   op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
   fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
@@ -2044,7 +2092,8 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   }
   CX* ds = (CX*)c->wsA;
   k_dtheta_spec<CX, CX><<<grid1(FS), 256, 0, c->stream>>>(specT, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds, ds + FS,
-                                                         ds + 2 * FS, c->kx, c->ky, (int)g.C, nz, 1.0 / g.dz); LES_COUNT_LAUNCH();
+                                                         ds + 2 * FS, c->kx, c->ky, (int)g.C, nz, 1.0 / g.dz,
+                                                         th0); LES_COUNT_LAUNCH();
   {
     S* o3[3] = {bigf[3], bigf[4], bigf[5]};
     padT<MX, CX>(c, ds, 3, o3);
