@@ -227,6 +227,50 @@ int filt_da_multi_spec(les_ctx* c, double* const* f, double* const* dx, double* 
   c2r(c, 3 * nf, nlev, c->wsB, out, (long)g.nplane, false, g.lh);
   return 0;
 }
+// Mixed-form filt_da of u, v, w: the filtered velocities and dudx, dvdy
+// (read by rmsdiv, rmsdiv.f90:93-100) in FP64; dudy, dvdx, dwdx, dwdy, which
+// only feed S_ij of the SGS model, from the saved FP64 spectra in FP32.
+static int filt_da_uvw_mixed(les_ctx* c) {
+  const Grid& g = c->g;
+  const int nz = g.nz;
+  const long FS = (long)nz * g.C;
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  const double scs[3] = {sc, sc, sc};
+  r2c(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  // FP64 y pass: filtered field (all three), spectrum saved (all three)
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+  J.nin = 1; J.nout = 2; J.nf = 3; J.inv_mask = 1u;
+  J.in[0] = c->wsA; J.fs_in = FS;
+  J.out[0] = c->wsB; J.out[1] = c->spec; J.fs_out = FS;
+  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_KILL;
+  cols(c, J);
+  // FP64 dudx and dvdy from the spectra (inverse only)
+  ColJob K = coljob(c, MAP_SAME, DIR_INV, nz);
+  K.nin = 1; K.nout = 1; K.nf = 1;
+  K.in[0] = c->spec; K.out[0] = (C2*)c->wsB + 3 * FS; K.coef[0][0] = CC_IKX;
+  cols(c, K);
+  K.in[0] = c->spec + FS; K.out[0] = (C2*)c->wsB + 4 * FS; K.coef[0][0] = CC_IKY;
+  cols(c, K);
+  double* o5[5] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DUDX], c->f[LES_DVDY]};
+  c2r(c, 5, nz, c->wsB, o5, (long)g.nplane, false, g.lh);
+  // FP32 derivatives for the SGS strain
+  float2* w32 = (float2*)c->wsA;
+  ColJob L = coljob(c, MAP_SAME, DIR_INV, nz);
+  L.nin = 1; L.nout = 1; L.nf = 1;
+  L.in[0] = c->spec; L.out[0] = w32; L.coef[0][0] = CC_IKY;                  // dudy
+  colsT<float, double2>(c, L);
+  L.in[0] = c->spec + FS; L.out[0] = w32 + FS; L.coef[0][0] = CC_IKX;        // dvdx
+  colsT<float, double2>(c, L);
+  L.in[0] = c->spec + 2 * FS;                                                // dwdx, dwdy
+  L.nout = 2; L.out[0] = w32 + 2 * FS; L.out[1] = w32 + 3 * FS;
+  L.coef[0][0] = CC_IKX; L.coef[1][0] = CC_IKY;
+  colsT<float, double2>(c, L);
+  double* o4[4] = {c->f[LES_DUDY], c->f[LES_DVDX], c->f[LES_DWDX], c->f[LES_DWDY]};
+  c2rT<float, double>(c, 4, nz, c->wsA, o4, (long)g.nplane, false, g.lh);
+  return 0;
+}
+
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev) {
   double* a[1] = {f}; double* b[1] = {dfdx}; double* d[1] = {dfdy};
   return filt_da_multi(c, a, b, d, 1, nlev);
@@ -1527,9 +1571,10 @@ __global__ void k_calcbeta(const double* __restrict__ theta, const double* __res
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
     if (jz == 1 || jz == nz || jx >= nx) { bs[i] = 0.0; continue; }
     const double sb = sums[jz - 1] / nxny, sbm = sums[jz - 2] / nxny;
-    const double above = (theta[i] * 1.0 - sb) / sb;
-    const double below = (theta[i - np] * 1.0 - sbm) / sbm;
-    bs[i] = g_hat * (above + below) / 2.0;
+    // (theta - sb)/sb as a product with 1/sb (one division per level, not per point)
+    const double above = (theta[i] * 1.0 - sb) * (1.0 / sb);
+    const double below = (theta[i - np] * 1.0 - sbm) * (1.0 / sbm);
+    bs[i] = g_hat * (above + below) * 0.5;
   }
 }
 // scalars_module.f90:457-504 step_scalar
@@ -2171,11 +2216,13 @@ static int stepT(les_ctx* c) {
   std::swap(c->f[LES_RHSY], c->f[LES_RHSY_F]);
   std::swap(c->f[LES_RHSZ], c->f[LES_RHSZ_F]);
   op_obukhov(c);
-  {
+  if (!MX) {
     double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
     double* x3[3] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX]};
     double* y3[3] = {c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
     filt_da_multi_spec(c, f3, x3, y3, 3, g.nz, c->spec);
+  } else {
+    filt_da_uvw_mixed(c);
   }
   op_ddz(c, c->f[LES_DUDZ], c->f[LES_U], 1);
   op_ddz(c, c->f[LES_DVDZ], c->f[LES_V], 1);
