@@ -24,12 +24,15 @@ struct FftPlanDev {
   int radix[FFT_MAX_STAGES];
   int twoff[FFT_MAX_STAGES];
   const double2* tw;  // forward twiddles, per stage (R-1)*Ns entries
+  const float2* twf;  // the same rounded to FP32 (FP32 kernels read these: a
+                      // double->float conversion runs on GB300's FP64 pipe)
 };
 
 struct RealPlanDev {
   FftPlanDev c;       // complex FFT of length m = nx/2
   int nx;
   const double2* w;   // exp(-2 pi i k / nx), k = 0..m
+  const float2* wf;   // the same in FP32
 };
 
 // ---- radix butterflies -----------------------------------------------------
@@ -59,9 +62,17 @@ template <typename C, typename T> __device__ __forceinline__ void dft3(C* v, int
   v[2] = csub(m, rot);
 }
 
-template <typename T> __device__ __forceinline__ typename CT<T>::type twid(const double2* tw, int idx, int sign) {
-  double2 w = __ldg(&tw[idx]);
-  return mk<T>((T)w.x, sign < 0 ? (T)w.y : (T)(-w.y));
+template <typename T> struct TwSel;
+template <> struct TwSel<double> {
+  static __device__ __forceinline__ double2 get(const FftPlanDev& P, int idx) { return __ldg(&P.tw[idx]); }
+};
+template <> struct TwSel<float> {
+  static __device__ __forceinline__ float2 get(const FftPlanDev& P, int idx) { return __ldg(&P.twf[idx]); }
+};
+template <typename T> __device__ __forceinline__ typename CT<T>::type twid(const FftPlanDev& P, int idx, int sign) {
+  typename CT<T>::type w = TwSel<T>::get(P, idx);
+  if (sign > 0) w.y = -w.y;
+  return w;
 }
 
 // One Stockham pass over all batches.  Element (b, i) lives at
@@ -70,7 +81,7 @@ template <typename T> __device__ __forceinline__ typename CT<T>::type twid(const
 template <typename T, bool COLS>
 __device__ __forceinline__ void fft_pass(const typename CT<T>::type* __restrict__ x,
                                          typename CT<T>::type* __restrict__ y, int n, int nb,
-                                         int bstride, int R, int Ns, const double2* tw, int sign) {
+                                         int bstride, int R, int Ns, const FftPlanDev& P, int toff, int sign) {
   typedef typename CT<T>::type C;
   const int m = n / R;
   const int total = m * nb;
@@ -86,7 +97,7 @@ __device__ __forceinline__ void fft_pass(const typename CT<T>::type* __restrict_
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < 4; ++r)
-        if (r < R) v[r] = cmul(v[r], twid<T>(tw, (r - 1) * Ns + k, sign));
+        if (r < R) v[r] = cmul(v[r], twid<T>(P, toff + (r - 1) * Ns + k, sign));
     }
     if (R == 4) dft4(v, sign);
     else if (R == 2) dft2(v);
@@ -108,7 +119,7 @@ __device__ typename CT<T>::type* fft_smem(typename CT<T>::type* x, typename CT<T
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.radix[s];
-    fft_pass<T, COLS>(x, y, P.n, nb, bstride, R, Ns, P.tw + P.twoff[s], sign);
+    fft_pass<T, COLS>(x, y, P.n, nb, bstride, R, Ns, P, P.twoff[s], sign);
     __syncthreads();
     typename CT<T>::type* t = x; x = y; y = t;
     Ns *= R;
@@ -172,6 +183,10 @@ struct ColJob {
   const double* ky;
   const double* G;        // G_test (lh,ny)
   const double* GG;       // G_test_test
+  const float* kxf;       // the same tables in FP32 for FP32 kernels
+  const float* kyf;
+  const float* Gf;
+  const float* GGf;
   int lh;                 // row stride of the (lh,ny) tables
 };
 

@@ -4,6 +4,25 @@
 
 namespace les {
 
+template <typename T> __device__ __forceinline__ typename CT<T>::type rw(const RealPlanDev& P, int k);
+template <> __device__ __forceinline__ double2 rw<double>(const RealPlanDev& P, int k) { return __ldg(&P.w[k]); }
+template <> __device__ __forceinline__ float2 rw<float>(const RealPlanDev& P, int k) { return __ldg(&P.wf[k]); }
+
+// spectral coefficient tables in the kernel's precision
+template <typename T> struct Tab;
+template <> struct Tab<double> {
+  static __device__ __forceinline__ double kx(const ColJob& J, size_t i) { return J.kx[i]; }
+  static __device__ __forceinline__ double ky(const ColJob& J, size_t i) { return J.ky[i]; }
+  static __device__ __forceinline__ double G(const ColJob& J, size_t i) { return J.G[i]; }
+  static __device__ __forceinline__ double GG(const ColJob& J, size_t i) { return J.GG[i]; }
+};
+template <> struct Tab<float> {
+  static __device__ __forceinline__ float kx(const ColJob& J, size_t i) { return J.kxf[i]; }
+  static __device__ __forceinline__ float ky(const ColJob& J, size_t i) { return J.kyf[i]; }
+  static __device__ __forceinline__ float G(const ColJob& J, size_t i) { return J.Gf[i]; }
+  static __device__ __forceinline__ float GG(const ColJob& J, size_t i) { return J.GGf[i]; }
+};
+
 // ---------------------------------------------------------------------------
 // rows_r2c: x-transform of `rpc` rows per CTA.  grid = (ceil(ny/rpc), nlev, nfield)
 template <typename T, typename TIn>
@@ -50,8 +69,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
       const C e = cscale(cadd(a, b), (T)0.5);
       const C d = cscale(csub(a, b), (T)0.5);
       const C o = cmulmi(d);  // d / i
-      const double2 wd = __ldg(&P.w[k]);
-      X = cadd(e, cmul(mk<T>((T)wd.x, (T)wd.y), o));
+      X = cadd(e, cmul(rw<T>(P, k), o));
     }
     out[(size_t)(row0 + r) * J.wc + k] = X;
   }
@@ -82,8 +100,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
     const C a = X[r * (m + 1) + k];
     const C b = cconj(X[r * (m + 1) + (m - k)]);
     const C e = cadd(a, b);
-    const double2 wd = __ldg(&P.w[k]);
-    const C d = cmul(csub(a, b), mk<T>((T)wd.x, (T)(-wd.y)));  // x exp(+2 pi i k/nx)
+    const C d = cmul(csub(a, b), cconj(rw<T>(P, k)));  // x exp(+2 pi i k/nx)
     A[t] = cadd(e, cmuli(d));
   }
   __syncthreads();
@@ -119,17 +136,17 @@ __device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT
   const size_t ki = (size_t)jx + (size_t)J.lh * js;
   switch (code) {
     case CC_ONE: return v;
-    case CC_G: return cscale(v, (T)J.G[ki]);
-    case CC_GG: return cscale(v, (T)J.GG[ki]);
-    case CC_IKX: return ik(v, (T)J.kx[ki]);
-    case CC_IKY: return ik(v, (T)J.ky[ki]);
+    case CC_G: return cscale(v, Tab<T>::G(J, ki));
+    case CC_GG: return cscale(v, Tab<T>::GG(J, ki));
+    case CC_IKX: return ik(v, Tab<T>::kx(J, ki));
+    case CC_IKY: return ik(v, Tab<T>::ky(J, ki));
     case CC_KILL: {
       const int lhm1 = J.lh - 1;
       if (jx == lhm1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
       return v;
     }
-    case CC_MASK: return J.G[ki] != 0.0 ? v : mk<T>((T)0, (T)0);
-    case CC_MASK4: return J.GG[ki] != 0.0 ? v : mk<T>((T)0, (T)0);
+    case CC_MASK: return Tab<T>::G(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
+    case CC_MASK4: return Tab<T>::GG(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
     default: return mk<T>((T)0, (T)0);
   }
 }

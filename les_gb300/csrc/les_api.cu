@@ -54,6 +54,12 @@ static int make_plan(les_ctx* c, int n, HostPlan& hp) {
   c->allocs.push_back(hp.dev);
   LES_CUDA_CHECK(cudaMemcpy(hp.dev, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
   P.tw = hp.dev;
+  std::vector<float2> twf(tw.size());
+  for (size_t i = 0; i < tw.size(); ++i) twf[i] = make_float2((float)tw[i].x, (float)tw[i].y);
+  LES_CUDA_CHECK(cudaMalloc(&hp.devf, twf.size() * sizeof(float2)));
+  c->allocs.push_back(hp.devf);
+  LES_CUDA_CHECK(cudaMemcpy(hp.devf, twf.data(), twf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  P.twf = hp.devf;
   return 0;
 }
 static int make_real_plan(les_ctx* c, int nx, HostRealPlan& rp) {
@@ -72,6 +78,12 @@ static int make_real_plan(les_ctx* c, int nx, HostRealPlan& rp) {
   c->allocs.push_back(rp.dev);
   LES_CUDA_CHECK(cudaMemcpy(rp.dev, w.data(), w.size() * sizeof(double2), cudaMemcpyHostToDevice));
   rp.r.w = rp.dev;
+  std::vector<float2> wf(w.size());
+  for (size_t i = 0; i < w.size(); ++i) wf[i] = make_float2((float)w[i].x, (float)w[i].y);
+  LES_CUDA_CHECK(cudaMalloc(&rp.devf, wf.size() * sizeof(float2)));
+  c->allocs.push_back(rp.devf);
+  LES_CUDA_CHECK(cudaMemcpy(rp.devf, wf.data(), wf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  rp.r.wf = rp.devf;
   return 0;
 }
 
@@ -228,6 +240,21 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   cudaMemcpy(c->ky, ky.data(), tb, cudaMemcpyHostToDevice);
   cudaMemcpy(c->G, G.data(), tb, cudaMemcpyHostToDevice);
   cudaMemcpy(c->GG, GG.data(), tb, cudaMemcpyHostToDevice);
+  {
+    const size_t tf = (size_t)g.lh * g.ny * sizeof(float);
+    if ((st = dalloc(c, (void**)&c->kxf, tf)) || (st = dalloc(c, (void**)&c->kyf, tf)) ||
+        (st = dalloc(c, (void**)&c->Gf, tf)) || (st = dalloc(c, (void**)&c->GGf, tf)))
+      return fail(st);
+    std::vector<float> a(kx.size());
+    for (size_t i = 0; i < a.size(); ++i) a[i] = (float)kx[i];
+    cudaMemcpy(c->kxf, a.data(), tf, cudaMemcpyHostToDevice);
+    for (size_t i = 0; i < a.size(); ++i) a[i] = (float)ky[i];
+    cudaMemcpy(c->kyf, a.data(), tf, cudaMemcpyHostToDevice);
+    for (size_t i = 0; i < a.size(); ++i) a[i] = (float)G[i];
+    cudaMemcpy(c->Gf, a.data(), tf, cudaMemcpyHostToDevice);
+    for (size_t i = 0; i < a.size(); ++i) a[i] = (float)GG[i];
+    cudaMemcpy(c->GGf, a.data(), tf, cudaMemcpyHostToDevice);
+  }
   if ((st = make_real_plan(c, g.nx, c->rx)) || (st = make_real_plan(c, g.nx2, c->rxb)) ||
       (st = make_plan(c, g.ny, c->cy)) || (st = make_plan(c, g.ny2, c->cyb)))
     return fail(st);

@@ -19,10 +19,12 @@ int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, 
 struct HostPlan {
   FftPlanDev c{};
   double2* dev = nullptr;
+  float2* devf = nullptr;
 };
 struct HostRealPlan {
   RealPlanDev r{};
   double2* dev = nullptr;
+  float2* devf = nullptr;
 };
 
 // Grid constants computed once on the host in the reference's expression
@@ -56,6 +58,7 @@ struct les_ctx {
   double* z_os = nullptr;
   // spectral tables (lh,ny)
   double *kx = nullptr, *ky = nullptr, *G = nullptr, *GG = nullptr;
+  float *kxf = nullptr, *kyf = nullptr, *Gf = nullptr, *GGf = nullptr;
   // FFT plans
   les::HostRealPlan rx, rxb;   // real x-transforms of length nx, nx2
   les::HostPlan cy, cyb;       // complex y-transforms of length ny, ny2

@@ -94,6 +94,7 @@ static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
   J.inv_mask = (dir & DIR_INV) ? 0xffffffffu : 0u;
   J.ny_small = g.ny;
   J.kx = c->kx; J.ky = c->ky; J.G = c->G; J.GG = c->GG; J.lh = g.lh;
+  J.kxf = c->kxf; J.kyf = c->kyf; J.Gf = c->Gf; J.GGf = c->GGf;
   if (map == MAP_SAME) {
     J.ny_in = J.ny_out = g.ny; J.ncols = g.lh; J.wc_in = J.wc_out = g.lh;
   } else if (map == MAP_PAD) {
@@ -317,6 +318,7 @@ int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse) {
   K.inv_mask = inverse ? 1u : 0u;
   K.ncols = lhh; K.ny_small = nyy; K.wc_in = K.wc_out = lhh; K.ps_in = K.ps_out = (long)nyy * lhh;
   K.coef[0][0] = CC_ONE; K.kx = c->kx; K.ky = c->ky; K.G = c->G; K.GG = c->GG; K.lh = g.lh;
+  K.kxf = c->kxf; K.kyf = c->kyf; K.Gf = c->Gf; K.GGf = c->GGf;
   const HostRealPlan& rp = big ? c->rxb : c->rx;
   const HostPlan& cp = big ? c->cyb : c->cy;
   if (!inverse) {
