@@ -138,6 +138,30 @@ int les_get_counters(les_ctx* ctx, int* jt, int* jt_total);
  * state (obukhov, filt_da, ddz, wallstress, sgs_stag, theta_all_in_one,
  * divstress, convec, AB2, press_stag_array, project, rmsdiv). */
 int les_step(les_ctx* ctx, int nsteps);
+/* Same as les_step, but every step (except the first, whose control flow is
+ * special, and the rmsdiv/CFL diagnostic steps, which synchronise) is replayed
+ * from a CUDA graph captured on first use; one graph per step variant
+ * (dynamic-model step or not, Cs^2 override on or off).  No counterpart in the
+ * reference (its time loop is main.f90:202-509). */
+int les_step_graph(les_ctx* ctx, int nsteps);
+/* Times candidate launch shapes of the plane-transform kernels for this grid
+ * size (kx columns per CTA of the y pass, rows per CTA of the x pass) and
+ * keeps the fastest; results are cached per grid size for the process.
+ * No counterpart in the reference. */
+int les_autotune(les_ctx* ctx, int* tx64, int* tx32, int* rpc_scale);
+
+/* ---- ensembles --------------------------------------------------------------
+ * Independent members (any sizes) advanced together: one CUDA graph launch
+ * per ensemble step runs one step of every member, each on its own stream
+ * branch, so the members' work overlaps on the device.  Members must share
+ * cs_count and the step counter.  No counterpart in the reference (nproc = 1
+ * runs one member per process). */
+typedef struct les_ensemble les_ensemble;
+int les_ensemble_create(les_ctx* const* members, int n, les_ensemble** out);
+int les_ensemble_step(les_ensemble* e, int nsteps);
+void* les_ensemble_stream(les_ensemble* e);
+int les_ensemble_destroy(les_ensemble* e);
+
 /* rmsdiv.f90:1-113 on the start-of-step derivatives of the last step, and
  * timestep_conditions (scalars_module2.f90:22-70): cfl[0]=CFLu, cfl[1]=visc. */
 int les_rmsdiv(les_ctx* ctx, double* rms);

@@ -140,6 +140,18 @@ class Context:
     def step(self, n=1):
         check(self.L.les_step(self.h, int(n)))
 
+    def step_graph(self, n=1):
+        """Advance n steps replaying captured CUDA graphs (les_step_graph)."""
+        check(self.L.les_step_graph(self.h, int(n)))
+
+    def autotune(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self.L.les_autotune(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"tx64": a.value, "tx32": b.value, "rpc_scale": c.value}
+
+    def synchronize(self):
+        check(self.L.les_rmsdiv(self.h, ctypes.byref(ctypes.c_double())))  # stream-ordered read
+
     def rmsdiv(self):
         r = ctypes.c_double()
         check(self.L.les_rmsdiv(self.h, ctypes.byref(r)))
@@ -160,6 +172,38 @@ class Context:
 
     def set_pointer_mode(self, device):
         check(self.L.les_ctx_set_pointer_mode(self.h, 1 if device else 0))
+
+
+class Ensemble:
+    """Independent members advanced together: one CUDA graph launch per
+    ensemble step runs one step of every member on its own stream branch."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        self.L = lib()
+        arr = (ctypes.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h = ctypes.c_void_p()
+        self.L.les_ensemble_stream.restype = ctypes.c_void_p
+        self.L.les_ensemble_stream.argtypes = [ctypes.c_void_p]
+        check(self.L.les_ensemble_create(arr, len(self.members), ctypes.byref(h)))
+        self.h = h
+
+    def step(self, n=1):
+        check(self.L.les_ensemble_step(self.h, int(n)))
+
+    def stream(self):
+        return self.L.les_ensemble_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.les_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def estimate_device_bytes(cfg):

@@ -145,6 +145,7 @@ struct RowJob {
   double div[JOB_MAXF];         // r2c: when non-zero, input is (x / div) * scale
   const double* off[JOB_MAXF];  // per-plane offsets: r2c subtracts off[plane] before
                                 // scaling, c2r adds it to the output (null: none)
+  int rpc;                      // rows per CTA (0: default for the size)
 };
 
 // Spectral coefficient codes for the column operator.
@@ -188,6 +189,7 @@ struct ColJob {
   const float* Gf;
   const float* GGf;
   int lh;                 // row stride of the (lh,ny) tables
+  int tx;                 // kx columns per CTA (0: default for the precision)
 };
 
 }  // namespace les

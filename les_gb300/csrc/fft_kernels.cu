@@ -239,11 +239,14 @@ static int rows_pc(int nx) {
 template <typename T, typename TIn>
 int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  const int rpc = rows_pc<T>(P.nx);
+  const int rpc = J.rpc > 0 ? J.rpc : rows_pc<T>(P.nx);
   const size_t sm = (size_t)2 * rpc * (P.nx / 2) * sizeof(C);
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
-  if (sm > 48 * 1024)
+  static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
+  if (sm > sm_set) {
     cudaFuncSetAttribute(k_rows_r2c<T, TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    sm_set = sm;
+  }
   k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
   return 0;
 }
@@ -251,28 +254,51 @@ int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
 template <typename T, typename TOut>
 int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  const int rpc = rows_pc<T>(P.nx);
+  const int rpc = J.rpc > 0 ? J.rpc : rows_pc<T>(P.nx);
   const int m = P.nx / 2;
   const size_t sm = (size_t)rpc * ((m + 1) + 2 * m) * sizeof(C);
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
-  if (sm > 48 * 1024)
+  static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
+  if (sm > sm_set) {
     cudaFuncSetAttribute(k_rows_c2r<T, TOut>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    sm_set = sm;
+  }
   k_rows_c2r<T, TOut><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
   return 0;
 }
 
-template <typename T, typename CIn>
-int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s) {
+template <typename T, int TX, typename CIn>
+static int launch_cols_tx(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  // FP64 tiles of 4 columns (64 B rows); FP32 tiles of 8 (64 B rows)
-  constexpr int TX = sizeof(T) == 8 ? 4 : 8;
   const int nymax = J.ny_in > J.ny_out ? J.ny_in : J.ny_out;
   const size_t sm = (size_t)(J.nin * J.ny_in + 2 * nymax) * TX * sizeof(C);
   dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
-  if (sm > 48 * 1024)
+  static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
+  if (sm > sm_set) {
     cudaFuncSetAttribute(k_cols<T, TX, CIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    sm_set = sm;
+  }
   k_cols<T, TX, CIn><<<grid, 256, sm, s>>>(J, Pin, Pout); LES_COUNT_LAUNCH();
   return 0;
+}
+
+// kx tile width: FP64 {2, 4, 8} (default 4), FP32 {4, 8, 16} (default 8);
+// the autotuner picks one per grid size
+template <typename T, typename CIn>
+int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s) {
+  if (sizeof(T) == 8) {
+    switch (J.tx) {
+      case 2: return launch_cols_tx<T, 2, CIn>(J, Pin, Pout, s);
+      case 8: return launch_cols_tx<T, 8, CIn>(J, Pin, Pout, s);
+      default: return launch_cols_tx<T, 4, CIn>(J, Pin, Pout, s);
+    }
+  } else {
+    switch (J.tx) {
+      case 4: return launch_cols_tx<T, 4, CIn>(J, Pin, Pout, s);
+      case 16: return launch_cols_tx<T, 16, CIn>(J, Pin, Pout, s);
+      default: return launch_cols_tx<T, 8, CIn>(J, Pin, Pout, s);
+    }
+  }
 }
 
 template int launch_rows_r2c<double, double>(const RowJob&, const RealPlanDev&, cudaStream_t);

@@ -5,6 +5,9 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include "les_internal.h"
 
 static thread_local char g_err[512] = "";
@@ -282,6 +285,9 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
 int les_ctx_destroy(les_ctx* c) {
   if (!c) return LES_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      if (c->gexec[a][b]) cudaGraphExecDestroy(c->gexec[a][b]);
   for (void* p : c->allocs) cudaFree(p);
   if (c->host_scal) cudaFreeHost(c->host_scal);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -368,6 +374,240 @@ int les_step(les_ctx* c, int nsteps) {
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { les_set_error("%s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
+  return LES_OK;
+}
+
+// ---- graphs, autotuning, ensembles -------------------------------------------
+static inline bool special_step(const les_ctx* c, int next_jt) {
+  const les_config& k = c->cfg;
+  return next_jt == 1 || (k.rmsdiv_every > 0 && next_jt % k.rmsdiv_every == 0);
+}
+static inline void step_key(const les_ctx* c, int next_jt, int next_total, int* lag, int* ov) {
+  const les_config& k = c->cfg;
+  *lag = (next_jt % k.cs_count == 0) ? 1 : 0;
+  *ov = ((k.model == 5 || k.model == 6 || k.model == 7) && next_total < 500) ? 1 : 0;
+}
+static int run_step(les_ctx* c) { return c->cfg.precision == 1 ? step_mixed(c) : step_fp64(c); }
+
+// capture one step of c on stream `s` (c->stream must be s or joined to it)
+static int capture_step(les_ctx* c, cudaGraph_t* graph) {
+  const int jt0 = c->jt, jtt0 = c->jt_total;
+  LES_CUDA_CHECK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int st = run_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, graph);
+  c->jt = jt0;
+  c->jt_total = jtt0;
+  if (st) return st;
+  if (e != cudaSuccess) { les_set_error("capture: %s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
+  return 0;
+}
+
+int les_step_graph(les_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return LES_ERR_ARG;
+  if (!c->surface_set) { les_set_error("les_set_surface must be called before les_step_graph"); return LES_ERR_STATE; }
+  for (int i = 0; i < nsteps; ++i) {
+    const int nj = c->jt + 1, nt = c->jt_total + 1;
+    if (special_step(c, nj)) {
+      int st = run_step(c);
+      if (st) return st;
+      continue;
+    }
+    int lag, ov;
+    step_key(c, nj, nt, &lag, &ov);
+    if (!c->gexec[lag][ov]) {
+      cudaGraph_t gr;
+      int st = capture_step(c, &gr);
+      if (st) return st;
+      cudaError_t e = cudaGraphInstantiate(&c->gexec[lag][ov], gr, 0);
+      cudaGraphDestroy(gr);
+      if (e != cudaSuccess) { les_set_error("instantiate: %s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
+    }
+    LES_CUDA_CHECK(cudaGraphLaunch(c->gexec[lag][ov], c->stream));
+    c->jt = nj;
+    c->jt_total = nt;
+  }
+  return LES_OK;
+}
+
+// process-wide cache of tuned launch shapes per (grid, precision)
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> g_tune;
+
+int les_autotune(les_ctx* c, int* tx64, int* tx32, int* rpc_scale) {
+  if (!c) return LES_ERR_ARG;
+  const auto key = std::make_tuple(c->g.nx, c->g.ny, c->g.nz, c->cfg.precision);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      c->tx64 = std::get<0>(it->second);
+      c->tx32 = std::get<1>(it->second);
+      c->rpc_scale = std::get<2>(it->second);
+    } else {
+      cudaEvent_t e0, e1;
+      LES_CUDA_CHECK(cudaEventCreate(&e0));
+      LES_CUDA_CHECK(cudaEventCreate(&e1));
+      auto rpc_of = [](int nx, int sc) {
+        int m = nx / 2, r = 1024 / (m / 4 > 0 ? m : 4);
+        r = std::max(1, std::min(16, r));
+        if (sc > 0) r = std::min(32, r * 2);
+        if (sc < 0) r = std::max(1, r / 2);
+        return r;
+      };
+      auto time_cfg = [&](int fp32, int tx, int sc) -> float {
+        if (fp32) c->tx32 = tx; else c->tx64 = tx;
+        const int r = rpc_of(c->g.nx, sc), rb = rpc_of(c->g.nx2, sc);
+        if (fp32) { c->rpc32 = r; c->rpcb32 = rb; } else { c->rpc64 = r; c->rpcb64 = rb; }
+        autotune_probe(c, fp32);  // warm-up (and smem opt-in)
+        cudaEventRecord(e0, c->stream);
+        for (int k = 0; k < 3; ++k) autotune_probe(c, fp32);
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+      };
+      int best[2][2] = {{4, 0}, {8, 0}};
+      const int txs[2][3] = {{2, 4, 8}, {4, 8, 16}};
+      for (int fp32 = 0; fp32 < 2; ++fp32) {
+        if (fp32 && c->cfg.precision != 1) continue;
+        float bt = 1e30f;
+        for (int a = 0; a < 3; ++a)
+          for (int sc = -1; sc <= 1; ++sc) {
+            const float t = time_cfg(fp32, txs[fp32][a], sc);
+            if (t < bt) { bt = t; best[fp32][0] = txs[fp32][a]; best[fp32][1] = sc; }
+          }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      LES_CUDA_CHECK(cudaGetLastError());
+      c->tx64 = best[0][0];
+      c->tx32 = best[1][0];
+      c->rpc_scale = best[0][1];  // one scale for both precisions: the FP64 choice
+      g_tune[key] = std::make_tuple(c->tx64, c->tx32, c->rpc_scale);
+    }
+  }
+  auto rpc_of = [](int nx, int sc) {
+    int m = nx / 2, r = 1024 / (m / 4 > 0 ? m : 4);
+    r = std::max(1, std::min(16, r));
+    if (sc > 0) r = std::min(32, r * 2);
+    if (sc < 0) r = std::max(1, r / 2);
+    return r;
+  };
+  c->rpc64 = c->rpc32 = rpc_of(c->g.nx, c->rpc_scale);
+  c->rpcb64 = c->rpcb32 = rpc_of(c->g.nx2, c->rpc_scale);
+  // graphs captured with the old shapes are stale
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      if (c->gexec[a][b]) { cudaGraphExecDestroy(c->gexec[a][b]); c->gexec[a][b] = nullptr; }
+  if (tx64) *tx64 = c->tx64;
+  if (tx32) *tx32 = c->tx32;
+  if (rpc_scale) *rpc_scale = c->rpc_scale;
+  return LES_OK;
+}
+
+}  // extern "C"
+
+struct les_ensemble {
+  std::vector<les_ctx*> m;
+  cudaStream_t root = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  std::map<std::vector<int>, cudaGraphExec_t> graphs;
+};
+
+extern "C" {
+
+int les_ensemble_create(les_ctx* const* members, int n, les_ensemble** out) {
+  if (!members || n < 1 || !out) return LES_ERR_ARG;
+  for (int i = 0; i < n; ++i) {
+    if (!members[i]) return LES_ERR_ARG;
+    if (members[i]->cfg.cs_count != members[0]->cfg.cs_count || members[i]->jt != members[0]->jt) {
+      les_set_error("ensemble members must share cs_count and the step counter");
+      return LES_ERR_ARG;
+    }
+  }
+  les_ensemble* e = new les_ensemble();
+  e->m.assign(members, members + n);
+  if (cudaStreamCreateWithFlags(&e->root, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
+    delete e; les_set_error("ensemble stream/event creation failed"); return LES_ERR_CUDA;
+  }
+  e->join.resize(n);
+  for (int i = 0; i < n; ++i)
+    if (cudaEventCreateWithFlags(&e->join[i], cudaEventDisableTiming) != cudaSuccess) {
+      les_set_error("ensemble event creation failed"); return LES_ERR_CUDA;
+    }
+  *out = e;
+  return LES_OK;
+}
+
+void* les_ensemble_stream(les_ensemble* e) { return e ? (void*)e->root : nullptr; }
+
+int les_ensemble_step(les_ensemble* e, int nsteps) {
+  if (!e || nsteps < 0) return LES_ERR_ARG;
+  const int n = (int)e->m.size();
+  for (int s = 0; s < nsteps; ++s) {
+    les_ctx* m0 = e->m[0];
+    const int nj = m0->jt + 1;
+    bool special = false;
+    for (les_ctx* c : e->m) {
+      if (!c->surface_set) { les_set_error("member without surface"); return LES_ERR_STATE; }
+      if (c->jt + 1 != nj) { les_set_error("ensemble members out of step"); return LES_ERR_STATE; }
+      special = special || special_step(c, nj);
+    }
+    if (special) {  // eager step on every member's stream, ordered after the root
+      LES_CUDA_CHECK(cudaEventRecord(e->fork, e->root));
+      for (int i = 0; i < n; ++i) {
+        LES_CUDA_CHECK(cudaStreamWaitEvent(e->m[i]->stream, e->fork, 0));
+        int st = run_step(e->m[i]);
+        if (st) return st;
+        LES_CUDA_CHECK(cudaEventRecord(e->join[i], e->m[i]->stream));
+        LES_CUDA_CHECK(cudaStreamWaitEvent(e->root, e->join[i], 0));
+      }
+      continue;
+    }
+    std::vector<int> key(2 * n);
+    for (int i = 0; i < n; ++i) step_key(e->m[i], nj, e->m[i]->jt_total + 1, &key[2 * i], &key[2 * i + 1]);
+    auto it = e->graphs.find(key);
+    if (it == e->graphs.end()) {
+      // capture: root forks to every member stream and joins them back
+      std::vector<int> jt0(n), jtt0(n);
+      for (int i = 0; i < n; ++i) { jt0[i] = e->m[i]->jt; jtt0[i] = e->m[i]->jt_total; }
+      LES_CUDA_CHECK(cudaStreamBeginCapture(e->root, cudaStreamCaptureModeThreadLocal));
+      cudaEventRecord(e->fork, e->root);
+      int st = 0;
+      for (int i = 0; i < n && !st; ++i) {
+        cudaStreamWaitEvent(e->m[i]->stream, e->fork, 0);
+        st = run_step(e->m[i]);
+        cudaEventRecord(e->join[i], e->m[i]->stream);
+        cudaStreamWaitEvent(e->root, e->join[i], 0);
+      }
+      cudaGraph_t gr;
+      cudaError_t ce = cudaStreamEndCapture(e->root, &gr);
+      for (int i = 0; i < n; ++i) { e->m[i]->jt = jt0[i]; e->m[i]->jt_total = jtt0[i]; }
+      if (st) return st;
+      if (ce != cudaSuccess) { les_set_error("ensemble capture: %s", cudaGetErrorString(ce)); return LES_ERR_CUDA; }
+      cudaGraphExec_t ex;
+      ce = cudaGraphInstantiate(&ex, gr, 0);
+      cudaGraphDestroy(gr);
+      if (ce != cudaSuccess) { les_set_error("ensemble instantiate: %s", cudaGetErrorString(ce)); return LES_ERR_CUDA; }
+      it = e->graphs.emplace(key, ex).first;
+    }
+    LES_CUDA_CHECK(cudaGraphLaunch(it->second, e->root));
+    for (les_ctx* c : e->m) { c->jt += 1; c->jt_total += 1; }
+  }
+  return LES_OK;
+}
+
+int les_ensemble_destroy(les_ensemble* e) {
+  if (!e) return LES_OK;
+  cudaStreamSynchronize(e->root);
+  for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
+  for (cudaEvent_t ev : e->join) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->root) cudaStreamDestroy(e->root);
+  delete e;
   return LES_OK;
 }
 

@@ -81,6 +81,12 @@ struct les_ctx {
   std::vector<void*> allocs;
   double rmsdiv_last = 0.0;
   int status_flags = 0;
+  // launch shapes chosen by the autotuner (0: built-in defaults)
+  int tx64 = 0, tx32 = 0;       // kx columns per CTA of the y-pass kernels
+  int rpc_scale = 0;            // rows per CTA of the x-pass kernels: default * 2^rpc_scale
+  int rpc64 = 0, rpc32 = 0, rpcb64 = 0, rpcb32 = 0;   // resolved rows per CTA (small/big planes)
+  // CUDA graphs of one step, by variant (dynamic-model step, Cs override)
+  cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
 };
 
 namespace les {
@@ -109,4 +115,5 @@ int op_rmsdiv(les_ctx* c, double* out);
 int op_tsc(les_ctx* c, double* cflu, double* visc);
 int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv);
 int thomas_tables(les_ctx* c);
+void autotune_probe(les_ctx* c, int fp32);
 }  // namespace les

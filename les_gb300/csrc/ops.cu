@@ -42,6 +42,7 @@ static int r2cT(les_ctx* c, int nf, int nlev, const TIn* const* in, long pstride
     J.ncols = ncols;
     J.pstride_phys = pstride;
     J.pstride_work = (long)J.ny * J.wc;
+    J.rpc = sizeof(T) == 8 ? (big ? c->rpcb64 : c->rpc64) : (big ? c->rpcb32 : c->rpc32);
     for (int f = 0; f < n; ++f) {
       J.phys[f] = in[f0 + f];
       J.work[f] = (CX*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
@@ -68,6 +69,7 @@ static int c2rT(les_ctx* c, int nf, int nlev, void* ws, TOut* const* out, long p
     J.ncols = ncols;
     J.pstride_phys = pstride;
     J.pstride_work = (long)J.ny * J.wc;
+    J.rpc = sizeof(T) == 8 ? (big ? c->rpcb64 : c->rpc64) : (big ? c->rpcb32 : c->rpc32);
     for (int f = 0; f < n; ++f) {
       J.phys[f] = out[f0 + f];
       J.work[f] = (CX*)ws + (size_t)(f0 + f) * nlev * J.pstride_work;
@@ -107,7 +109,9 @@ static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
   return J;
 }
 template <typename T, typename CIn>
-static int colsT(les_ctx* c, const ColJob& J) {
+static int colsT(les_ctx* c, const ColJob& J0) {
+  ColJob J = J0;
+  J.tx = sizeof(T) == 8 ? c->tx64 : c->tx32;
   const FftPlanDev& Pin = (J.ny_in == c->g.ny) ? c->cy.c : c->cyb.c;
   const FftPlanDev& Pout = (J.ny_out == c->g.ny) ? c->cy.c : c->cyb.c;
   return launch_cols<T, CIn>(J, Pin, Pout, c->stream);
@@ -1603,7 +1607,7 @@ int op_theta(les_ctx* c) {
   op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
   fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
   // RHS_Tf = RHS_T (pointer swap; RHS_T is fully rewritten below)
-  std::swap(c->f[LES_RHS_T], c->f[LES_RHS_TF]);
+  cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
                                                             c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
                                                             c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
@@ -2126,7 +2130,7 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   }
   op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
   fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
-  std::swap(c->f[LES_RHS_T], c->f[LES_RHS_TF]);
+  cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
                                                             c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
                                                             c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
@@ -2213,10 +2217,11 @@ static int stepT(les_ctx* c) {
   const les_config& k = c->cfg;
   c->jt += 1;
   c->jt_total += 1;
-  // RHS*_f = RHS* (main.f90:212-214): pointer swap, RHS* is fully rewritten by convec
-  std::swap(c->f[LES_RHSX], c->f[LES_RHSX_F]);
-  std::swap(c->f[LES_RHSY], c->f[LES_RHSY_F]);
-  std::swap(c->f[LES_RHSZ], c->f[LES_RHSZ_F]);
+  // RHS*_f = RHS* (main.f90:212-214); device copies keep every buffer address
+  // fixed from step to step, so a step can be captured in a CUDA graph
+  cudaMemcpyAsync(c->f[LES_RHSX_F], c->f[LES_RHSX], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(c->f[LES_RHSY_F], c->f[LES_RHSY], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(c->f[LES_RHSZ_F], c->f[LES_RHSZ], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   op_obukhov(c);
   if (!MX) {
     double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
@@ -2265,6 +2270,38 @@ static int stepT(les_ctx* c) {
     if (cflu > 0.1 || cflu < 0.0) return LES_ERR_CFL;
   }
   return 0;
+}
+
+// One representative transform batch (filt_da of three fields) on scratch
+// planes in the given precision; used by the autotuner.
+template <typename T>
+static void tune_probe(les_ctx* c) {
+  typedef typename CT<T>::type CX;
+  const Grid& g = c->g;
+  const int nz = g.nz;
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  const double scs[3] = {sc, sc, sc};
+  r2cT<T, double>(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+  J.nin = 1; J.nout = 3; J.nf = 3;
+  J.in[0] = c->wsA; J.fs_in = (long)nz * g.C;
+  J.out[0] = c->wsB; J.out[1] = (CX*)c->wsB + 3 * (size_t)nz * g.C; J.out[2] = (CX*)c->wsB + 6 * (size_t)nz * g.C;
+  J.fs_out = (long)nz * g.C;
+  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY;
+  colsT<T, CX>(c, J);
+  double* out[9];
+  for (int q = 0; q < 9; ++q) out[q] = c->big + (size_t)q * g.nfield;  // scratch (the 3/2-grid pool)
+  c2rT<T, double>(c, 9, nz, c->wsB, out, (long)g.nplane, false, g.lh);
+  // the padded size too
+  const double* bi[3] = {c->big, c->big + g.nfield_big, c->big + 2 * g.nfield_big};
+  r2cT<T, double>(c, 3, nz, bi, (long)g.nplane_big, nullptr, nullptr, c->wsA, true, g.nx / 2);
+  double* bo[3] = {c->big + 3 * g.nfield_big, c->big + 4 * g.nfield_big, c->big + 5 * g.nfield_big};
+  c2rT<T, double>(c, 3, nz, c->wsA, bo, (long)g.nplane_big, true, g.nx / 2);
+}
+void autotune_probe(les_ctx* c, int fp32) {
+  if (fp32) tune_probe<float>(c);
+  else tune_probe<double>(c);
 }
 
 int step_fp64(les_ctx* c) { return stepT<false>(c); }
