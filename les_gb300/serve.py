@@ -1,0 +1,356 @@
+"""Continuous-batching server for ensemble members.
+
+Requests are "advance member M by N steps".  Member state stays resident on
+the device between requests.  A new member is admitted only when its
+estimated footprint (les_estimate_device_bytes) fits in the memory budget;
+members that are idle are evicted least-recently-used when room is needed.
+Every tick the scheduler launches one step of every active request, each on
+its member's own stream, so steps of different members overlap on the GPU;
+requests that arrive while others run join at the next tick (continuous
+batching, not a queue).  Step latency is measured from launch to completion
+of each step (CUDA events), request latency from arrival to completion.
+
+The scheduler is pure host logic and runs against an executor: GpuExecutor
+(les_gb300 contexts, graph-replayed steps) or FakeExecutor (deterministic
+timings, for CPU tests of admission, cancellation and failure handling).
+"""
+import collections
+import heapq
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SIZES = [(32, 32, 32), (64, 64, 64), (96, 96, 64), (128, 128, 128), (192, 192, 128)]
+WEIGHTS = [0.3, 0.3, 0.2, 0.15, 0.05]
+
+
+@dataclass
+class Request:
+    rid: int
+    member: int           # member id (seeded state + surface)
+    size: tuple           # (nx, ny, nz_levels)
+    nsteps: int
+    arrival: float        # seconds, trace time
+    arrival_wall: float = None
+    done_steps: int = 0
+    inflight: int = 0
+    started: float = None
+    finished: float = None
+    status: str = "pending"   # pending | active | done | cancelled | rejected | failed
+    error: str = None
+
+
+@dataclass
+class Metrics:
+    step_lat: list = field(default_factory=list)            # seconds
+    step_lat_by_size: dict = field(default_factory=lambda: collections.defaultdict(list))
+    req_lat: list = field(default_factory=list)
+    pt_steps: float = 0.0
+    admitted: int = 0
+    rejected: int = 0
+    evicted: int = 0
+
+    def summary(self, wall):
+        def pct(a, q):
+            return float(np.percentile(a, q)) if len(a) else None
+        out = {"steps": len(self.step_lat),
+               "step_p50_ms": None if not self.step_lat else 1e3 * pct(self.step_lat, 50),
+               "step_p99_ms": None if not self.step_lat else 1e3 * pct(self.step_lat, 99),
+               "req_p50_ms": None if not self.req_lat else 1e3 * pct(self.req_lat, 50),
+               "req_p99_ms": None if not self.req_lat else 1e3 * pct(self.req_lat, 99),
+               "pt_steps_per_s": self.pt_steps / wall if wall > 0 else None,
+               "admitted": self.admitted, "rejected": self.rejected, "evicted": self.evicted,
+               "by_size": {}}
+        for sz, lat in sorted(self.step_lat_by_size.items()):
+            out["by_size"]["%dx%dx%d" % sz] = {"n": len(lat), "p50_ms": 1e3 * pct(lat, 50),
+                                              "p99_ms": 1e3 * pct(lat, 99)}
+        return out
+
+
+def poisson_trace(n_requests, rate, seed, n_members=64, sizes=SIZES, weights=WEIGHTS, nmax=50):
+    """Poisson arrivals of 'advance N' requests (N ~ U{1..nmax}) over a pool
+    of members whose sizes are drawn with the given weights."""
+    rng = np.random.default_rng(seed)
+    msize = [sizes[i] for i in rng.choice(len(sizes), size=n_members, p=weights)]
+    t = 0.0
+    reqs = []
+    for r in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        m = int(rng.integers(n_members))
+        reqs.append(Request(rid=r, member=m, size=msize[m], nsteps=int(rng.integers(1, nmax + 1)), arrival=t))
+    return reqs
+
+
+class Scheduler:
+    def __init__(self, executor, budget_bytes, max_inflight_per_member=1, clock=time.perf_counter):
+        self.ex = executor
+        self.budget = budget_bytes
+        self.used = 0
+        self.resident = collections.OrderedDict()   # member -> bytes (LRU order)
+        self.busy = collections.Counter()          # member -> active requests
+        self.pending = collections.deque()
+        self.active = []
+        self.metrics = Metrics()
+        self.clock = clock
+        self.max_inflight = max_inflight_per_member
+        self.done = []
+
+    # ---- admission ----------------------------------------------------------
+    def _admit_member(self, req):
+        if req.member in self.resident:
+            self.resident.move_to_end(req.member)
+            return True
+        need = self.ex.footprint(req.size)
+        if need > self.budget:
+            req.status = "rejected"
+            req.error = "footprint %d B exceeds the memory budget %d B" % (need, self.budget)
+            self.metrics.rejected += 1
+            return False
+        # evict idle members, least recently used first
+        while self.used + need > self.budget:
+            victim = next((m for m in self.resident if self.busy[m] == 0), None)
+            if victim is None:
+                return False  # wait for memory to free up
+            self.used -= self.resident.pop(victim)
+            self.ex.evict(victim)
+            self.metrics.evicted += 1
+        try:
+            self.ex.load(req.member, req.size)
+        except MemoryError as e:  # allocation failure: reject, keep serving
+            req.status = "rejected"
+            req.error = str(e)
+            self.metrics.rejected += 1
+            return False
+        self.resident[req.member] = need
+        self.used += need
+        self.metrics.admitted += 1
+        return True
+
+    def submit(self, req):
+        self.pending.append(req)
+
+    def cancel(self, rid):
+        for q in list(self.pending):
+            if q.rid == rid:
+                self.pending.remove(q)
+                q.status = "cancelled"
+                self.done.append(q)
+                return True
+        for q in self.active:
+            if q.rid == rid:
+                q.status = "cancelled"  # retired once its in-flight steps complete
+                return True
+        return False
+
+    # ---- one tick -----------------------------------------------------------
+    def tick(self, now):
+        # admit in arrival order; a request whose member does not fit waits
+        waiting = collections.deque()
+        while self.pending:
+            req = self.pending.popleft()
+            if req.status == "rejected":
+                continue
+            if self._admit_member(req):
+                req.status = "active"
+                req.started = now
+                self.busy[req.member] += 1
+                self.active.append(req)
+            elif req.status == "rejected":
+                self.done.append(req)
+            else:
+                waiting.append(req)
+        self.pending = waiting
+        # one step per active request per tick; requests on one member run in
+        # arrival order (the oldest owns the member until it completes)
+        owned = set()
+        for req in self.active:
+            if req.status != "active" or req.member in owned:
+                continue
+            owned.add(req.member)
+            if req.done_steps + req.inflight >= req.nsteps or req.inflight >= self.max_inflight:
+                continue
+            self.ex.launch(req, self.clock())
+            if req.status == "active":
+                req.inflight += 1
+
+    def poll(self):
+        for req, t_launch, t_done, pts in self.ex.completed():
+            req.inflight -= 1
+            req.done_steps += 1
+            if req.status == "cancelled":
+                continue
+            lat = t_done - t_launch
+            self.metrics.step_lat.append(lat)
+            self.metrics.step_lat_by_size[req.size].append(lat)
+            self.metrics.pt_steps += pts
+        still = []
+        for req in self.active:
+            if req.status == "failed":
+                self.busy[req.member] -= 1
+                self.done.append(req)
+            elif req.inflight == 0 and (req.done_steps >= req.nsteps or req.status == "cancelled"):
+                req.finished = self.clock()
+                if req.status != "cancelled":
+                    req.status = "done"
+                    t_arr = req.arrival_wall if req.arrival_wall is not None else req.started
+                    self.metrics.req_lat.append(req.finished - t_arr)
+                self.busy[req.member] -= 1
+                self.done.append(req)
+            else:
+                still.append(req)
+        self.active = still
+
+    def idle(self):
+        return not self.pending and not self.active
+
+    def run(self, trace, time_scale=1.0, max_wall=600.0):
+        """Replay a trace in real time (arrival times x time_scale)."""
+        t0 = self.clock()
+        arrivals = sorted(trace, key=lambda r: r.arrival)
+        i = 0
+        while i < len(arrivals) or not self.idle():
+            now = self.clock() - t0
+            while i < len(arrivals) and arrivals[i].arrival * time_scale <= now:
+                arrivals[i].arrival_wall = t0 + arrivals[i].arrival * time_scale
+                self.submit(arrivals[i])
+                i += 1
+            self.tick(now)
+            self.poll()
+            if now > max_wall:
+                break
+            if not self.active and i < len(arrivals):
+                dtw = arrivals[i].arrival * time_scale - (self.clock() - t0)
+                if dtw > 0:
+                    time.sleep(min(dtw, 0.01))
+            else:
+                self.ex.wait_any(0.0005)
+        wall = self.clock() - t0
+        return self.metrics.summary(wall), wall
+
+
+class FakeExecutor:
+    """Deterministic executor for host-side tests: a step of an nx*ny*nz
+    member takes `ns_per_pt` ns per grid point; allocation can be made to
+    fail; a member can be marked to fail (NaN detected) on its next step."""
+
+    def __init__(self, ns_per_pt=0.1, fail_alloc=(), fail_step=(), clock=None):
+        self.ns = ns_per_pt
+        self.fail_alloc = set(fail_alloc)
+        self.fail_step = set(fail_step)
+        self.t = 0.0
+        self.inflight = []
+        self.loaded = {}
+        self.steps = collections.Counter()
+
+    def footprint(self, size):
+        nx, ny, nz = size
+        return int(1200 * nx * ny * (nz + 1))
+
+    def load(self, member, size):
+        if member in self.fail_alloc:
+            raise MemoryError("injected allocation failure for member %d" % member)
+        self.loaded[member] = size
+
+    def evict(self, member):
+        self.loaded.pop(member, None)
+
+    def launch(self, req, t):
+        nx, ny, nz = req.size
+        if req.member in self.fail_step:
+            req.status = "failed"
+            req.error = "non-finite state detected"
+            return
+        dur = self.ns * 1e-9 * nx * ny * nz
+        self.inflight.append((req, t, t + dur, nx * ny * nz, False))
+        self.steps[req.member] += 1
+
+    def completed(self):
+        out = [(r, a, b, p) for (r, a, b, p, f) in self.inflight]
+        self.inflight = []
+        return out
+
+    def wait_any(self, dt):
+        pass
+
+
+class GpuExecutor:
+    """les_gb300 contexts on the GPU; one CUDA event per launched step."""
+
+    def __init__(self, precision=1, seed0=1000, use_graphs=True, autotune=True):
+        import torch  # events on the members' streams
+        import les_gb300 as lg
+        self.torch = torch
+        self.lg = lg
+        self.precision = precision
+        self.seed0 = seed0
+        self.use_graphs = use_graphs
+        self.autotune = autotune
+        self.ctx = {}
+        self.streams = {}
+        self.inflight = collections.deque()
+        self.tuned = set()
+
+    def config(self, size):
+        nx, ny, nz = size
+        return self.lg.make_config(nx, ny, nz, s_flag=1, jt_total0=500, precision=self.precision,
+                                   rmsdiv_every=0)
+
+    def footprint(self, size):
+        return int(self.lg.estimate_device_bytes(self.config(size)))
+
+    def load(self, member, size):
+        lg = self.lg
+        cfg = self.config(size)
+        surf = lg.patch_surface(cfg, self.seed0 + member)
+        surf.wt_s[:] = 0.05
+        try:
+            ctx = lg.Context(cfg, surf)
+        except lg.LesError as e:
+            if e.code == -3:
+                raise MemoryError(str(e))
+            raise
+        for k, v in lg.initial_state(cfg, surf, seed=self.seed0 + member).items():
+            ctx.set(k, v)
+        if self.autotune:
+            ctx.autotune()
+        self.ctx[member] = ctx
+        self.streams[member] = self.torch.cuda.ExternalStream(ctx.stream())
+
+    def evict(self, member):
+        ctx = self.ctx.pop(member, None)
+        self.streams.pop(member, None)
+        if ctx is not None:
+            ctx.close()
+
+    def launch(self, req, t):
+        ctx = self.ctx[req.member]
+        if self.use_graphs:
+            ctx.step_graph(1)
+        else:
+            ctx.step(1)
+        ev = self.torch.cuda.Event()
+        ev.record(self.streams[req.member])
+        nx, ny, nz = req.size
+        self.inflight.append((req, t, ev, nx * ny * nz))
+
+    def completed(self):
+        out = []
+        now = time.perf_counter()
+        keep = collections.deque()
+        while self.inflight:
+            req, t, ev, pts = self.inflight.popleft()
+            if ev.query():
+                out.append((req, t, now, pts))
+            else:
+                keep.append((req, t, ev, pts))
+        self.inflight = keep
+        return out
+
+    def wait_any(self, dt):
+        time.sleep(dt)
+
+    def state(self, member, names=("u", "v", "w", "theta")):
+        ctx = self.ctx[member]
+        return {k: ctx.get(k) for k in names}

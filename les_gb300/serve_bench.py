@@ -1,0 +1,59 @@
+"""Serving measurement: Poisson arrivals (mean 200/s) of 'advance N steps'
+requests (N ~ U{1..50}) over a pool of 64 members with sizes drawn from
+{32^3, 64^3, 96^2x64, 128^3, 192^2x128} (weights 0.3/0.3/0.2/0.15/0.05),
+FP32-mixed steps replayed from CUDA graphs, admission by estimated footprint
+against free device memory.  Reports p50/p99 step and request latency and
+aggregate pt-steps/s, beside an unbatched FP64 baseline (the same requests
+served one at a time, eager FP64 steps).
+
+  python -m les_gb300.serve_bench [--requests 200] [--rate 200]
+"""
+import argparse
+import json
+import time
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--budget-gb", type=float, default=0.0, help="0: 90%% of free device memory")
+    ap.add_argument("--baseline-requests", type=int, default=60)
+    args = ap.parse_args()
+    import torch
+    from les_gb300.serve import GpuExecutor, Scheduler, poisson_trace
+    free, total = torch.cuda.mem_get_info()
+    budget = int(args.budget_gb * 2 ** 30) if args.budget_gb > 0 else int(0.9 * free)
+    trace = poisson_trace(args.requests, args.rate, args.seed)
+    ex = GpuExecutor(precision=1, autotune=True)
+    sched = Scheduler(ex, budget_bytes=budget)
+    summary, wall = sched.run(trace)
+    status = {}
+    for r in sched.done:
+        status[r.status] = status.get(r.status, 0) + 1
+    for m in list(ex.ctx):
+        ex.evict(m)
+    # unbatched FP64 baseline on a prefix of the same trace
+    base = GpuExecutor(precision=0, autotune=False, use_graphs=False)
+    nb = min(args.baseline_requests, len(trace))
+    pts = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in trace[:nb]:
+        if r.member not in base.ctx:
+            base.load(r.member, r.size)
+        base.ctx[r.member].step(r.nsteps)
+        base.ctx[r.member].synchronize()
+        nx, ny, nz = r.size
+        pts += nx * ny * nz * r.nsteps
+    tb = time.perf_counter() - t0
+    out = {"requests": len(trace), "rate_per_s": args.rate, "wall_s": wall, "status": status,
+           "budget_gb": budget / 2 ** 30, "serving": summary,
+           "fp64_unbatched_pt_steps_per_s": pts / tb, "fp64_unbatched_requests": nb}
+    out["speedup_vs_fp64_unbatched"] = summary["pt_steps_per_s"] / out["fp64_unbatched_pt_steps_per_s"]
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,107 @@
+"""Host-side tests of the continuous-batching scheduler against a fake
+executor (no GPU): admission by footprint, eviction, rejection, injected
+allocation failure, cancellation, a failing member, continuous batching."""
+from les_gb300.serve import FakeExecutor, Request, Scheduler, poisson_trace
+
+
+def R(rid, member, n=3, size=(32, 32, 32), t=0.0):
+    return Request(rid=rid, member=member, size=size, nsteps=n, arrival=t)
+
+
+def drain(s, limit=1000):
+    for _ in range(limit):
+        if s.idle():
+            return
+        s.tick(0.0)
+        s.poll()
+    raise AssertionError("scheduler did not drain")
+
+
+def test_concurrent_requests_share_ticks():
+    ex = FakeExecutor()
+    s = Scheduler(ex, budget_bytes=10 ** 12)
+    for i in range(4):
+        s.submit(R(i, member=i, n=5))
+    s.tick(0.0)
+    assert len(s.active) == 4                      # all four run in the same tick
+    assert sum(r.inflight for r in s.active) == 4
+    s.poll()
+    s.submit(R(9, member=9, n=2))                  # arrives while others run
+    s.tick(0.0)
+    assert any(r.rid == 9 and r.status == "active" for r in s.active)
+    drain(s)
+    assert all(r.status == "done" for r in s.done)
+    assert ex.steps[0] == 5 and ex.steps[9] == 2
+
+
+def test_admission_waits_for_memory_and_evicts_idle():
+    ex = FakeExecutor()
+    fp = ex.footprint((32, 32, 32))
+    s = Scheduler(ex, budget_bytes=2 * fp + 1)
+    s.submit(R(0, 0, n=3)); s.submit(R(1, 1, n=3)); s.submit(R(2, 2, n=3))
+    s.tick(0.0)
+    assert {r.member for r in s.active} == {0, 1}
+    assert len(s.pending) == 1                     # member 2 waits for room
+    drain(s)
+    assert [r.status for r in sorted(s.done, key=lambda r: r.rid)] == ["done"] * 3
+    assert s.metrics.evicted >= 1 and s.used <= s.budget
+
+
+def test_oversized_member_rejected():
+    ex = FakeExecutor()
+    s = Scheduler(ex, budget_bytes=ex.footprint((32, 32, 32)))
+    s.submit(R(0, 0, size=(128, 128, 128)))
+    s.submit(R(1, 1))
+    drain(s)
+    st = {r.rid: r.status for r in s.done}
+    assert st == {0: "rejected", 1: "done"}
+
+
+def test_injected_allocation_failure_is_rejected_not_fatal():
+    ex = FakeExecutor(fail_alloc={3})
+    s = Scheduler(ex, budget_bytes=10 ** 12)
+    s.submit(R(0, 3)); s.submit(R(1, 4))
+    drain(s)
+    st = {r.rid: (r.status, r.error) for r in s.done}
+    assert st[0][0] == "rejected" and "allocation" in st[0][1]
+    assert st[1][0] == "done"
+
+
+def test_cancel_pending_and_active():
+    ex = FakeExecutor()
+    s = Scheduler(ex, budget_bytes=ex.footprint((32, 32, 32)) + 1)
+    s.submit(R(0, 0, n=50)); s.submit(R(1, 1, n=5))
+    s.tick(0.0)
+    assert s.cancel(1)                              # still pending (no room)
+    assert s.cancel(0)                              # active
+    drain(s)
+    st = {r.rid: r.status for r in s.done}
+    assert st == {0: "cancelled", 1: "cancelled"}
+    assert ex.steps[0] < 50
+
+
+def test_failing_member_does_not_stop_others():
+    ex = FakeExecutor(fail_step={7})
+    s = Scheduler(ex, budget_bytes=10 ** 12)
+    s.submit(R(0, 7)); s.submit(R(1, 8))
+    drain(s)
+    st = {r.rid: r.status for r in s.done}
+    assert st == {0: "failed", 1: "done"}
+
+
+def test_requests_on_one_member_run_in_order():
+    ex = FakeExecutor()
+    s = Scheduler(ex, budget_bytes=10 ** 12)
+    s.submit(R(0, 5, n=4)); s.submit(R(1, 5, n=2))
+    s.tick(0.0)
+    assert sum(r.inflight for r in s.active) == 1   # only the older request steps
+    drain(s)
+    order = [r.rid for r in s.done]
+    assert order == [0, 1]
+
+
+def test_poisson_trace_shape():
+    tr = poisson_trace(200, rate=200.0, seed=1)
+    assert len(tr) == 200 and all(1 <= r.nsteps <= 50 for r in tr)
+    gaps = [b.arrival - a.arrival for a, b in zip(tr, tr[1:])]
+    assert 0.002 < sum(gaps) / len(gaps) < 0.01
