@@ -1,0 +1,60 @@
+"""Precision study: the FP32-mixed step against the FP64 step on the same
+seeded 256^3 member (active theta, x-striped z0 1e-4/1e-2 and heat flux
+0.05/0.15 K m/s), both on the GPU; every `--every` steps it reports the
+per-field relative L2 error and max-abs error relative to max|field|, and
+both forms' rmsdiv.
+
+  python -m les_gb300.precision_study [--grid 256] [--steps 500] [--every 50]
+"""
+import argparse
+import json
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--every", type=int, default=50)
+    ap.add_argument("--jt0", type=int, default=500)
+    args = ap.parse_args()
+    import les_gb300 as lg
+    ctxs = {}
+    for prec in (0, 1):
+        # rmsdiv is read directly (les_rmsdiv) so the reference's CFL stop
+        # (main.f90:455-458, CFLu > 0.1) does not end the study
+        cfg = lg.make_config(args.grid, s_flag=1, precision=prec, jt_total0=args.jt0, rmsdiv_every=0)
+        surf = lg.striped_surface(cfg)
+        c = lg.Context(cfg, surf)
+        for k, v in lg.initial_state(cfg, surf, seed=2024).items():
+            c.set(k, v)
+        ctxs[prec] = c
+    n = args.grid
+    rows = []
+    done = 0
+    while done < args.steps:
+        for c in ctxs.values():
+            c.step_graph(args.every)
+        done += args.every
+        rec = {"step": done}
+        for nm in ("u", "v", "w", "theta", "Cs_opt2"):
+            a = ctxs[1].get(nm)[:-1, :, :n]
+            b = ctxs[0].get(nm)[:-1, :, :n]
+            d = a - b
+            rec[nm] = {"rel_l2": float(np.linalg.norm(d) / np.linalg.norm(b)),
+                       "rel_max": float(np.abs(d).max() / np.abs(b).max())}
+        vel_a = np.concatenate([ctxs[1].get(k)[:-1, :, :n].ravel() for k in "uvw"])
+        vel_b = np.concatenate([ctxs[0].get(k)[:-1, :, :n].ravel() for k in "uvw"])
+        rec["velocity_rel_l2"] = float(np.linalg.norm(vel_a - vel_b) / np.linalg.norm(vel_b))
+        rec["rmsdiv_mixed"] = ctxs[1].rmsdiv()
+        rec["rmsdiv_fp64"] = ctxs[0].rmsdiv()
+        rec["cflu"], rec["visc_stab"] = ctxs[0].timestep_conditions()
+        rows.append(rec)
+        print(json.dumps(rec), flush=True)
+    for c in ctxs.values():
+        c.close()
+
+
+if __name__ == "__main__":
+    main()
