@@ -241,12 +241,8 @@ def main():
     ck = clocks.stop()
     launches = int(lib.les_kernel_launch_count() - n0)
     barrier()
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = pts * args.steps * world / (ms_max / 1e3)
+    from les_gb300.dist import aggregate
+    ms_max, _, value = aggregate(ms, pts * args.steps, device="cuda")
 
     # per-step kernel profile (dominant kernel = the whole step here: HBM ledger)
     hbm, src = measured_peaks()
