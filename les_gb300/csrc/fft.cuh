@@ -18,11 +18,26 @@ namespace les {
 
 constexpr int FFT_MAX_STAGES = 12;
 
+// q = n / d by one multiply-high: with inv = ceil(2^32/d) = (2^32 + e)/d,
+// 0 <= e < d, umulhi(n, inv) = floor(n/d + n*e/(d*2^32)), which is exact
+// while n*e < 2^32.  Plans are limited to lengths <= 4096 and thread indices
+// stay below 2^20, so n*d < 2^32 holds everywhere it is used.
+struct FastDiv {
+  unsigned inv;  // ceil(2^32 / d)
+  unsigned d;
+  __host__ __device__ FastDiv() : inv(0), d(1) {}
+  __host__ FastDiv(unsigned dd) : inv((unsigned)((((unsigned long long)1 << 32) + dd - 1) / dd)), d(dd) {}
+  __device__ __forceinline__ unsigned div(unsigned n) const { return d == 1 ? n : __umulhi(n, inv); }
+  __device__ __forceinline__ unsigned mod(unsigned n) const { return n - div(n) * d; }
+};
+
 struct FftPlanDev {
   int n;
   int nst;
   int radix[FFT_MAX_STAGES];
   int twoff[FFT_MAX_STAGES];
+  FastDiv dm[FFT_MAX_STAGES];   // n / radix of each stage (butterflies per transform)
+  FastDiv dns[FFT_MAX_STAGES];  // Ns of each stage (product of the previous radices)
   const double2* tw;  // forward twiddles, per stage (R-1)*Ns entries
   const float2* twf;  // the same rounded to FP32 (FP32 kernels read these: a
                       // double->float conversion runs on GB300's FP64 pipe)
@@ -31,6 +46,7 @@ struct FftPlanDev {
 struct RealPlanDev {
   FftPlanDev c;       // complex FFT of length m = nx/2
   int nx;
+  FastDiv dm, dm1;    // m and m + 1
   const double2* w;   // exp(-2 pi i k / nx), k = 0..m
   const float2* wf;   // the same in FP32
 };
@@ -81,15 +97,18 @@ template <typename T> __device__ __forceinline__ typename CT<T>::type twid(const
 template <typename T, bool COLS>
 __device__ __forceinline__ void fft_pass(const typename CT<T>::type* __restrict__ x,
                                          typename CT<T>::type* __restrict__ y, int n, int nb,
-                                         int bstride, int R, int Ns, const FftPlanDev& P, int toff, int sign) {
+                                         int bstride, int R, int Ns, const FftPlanDev& P, int st, int sign) {
   typedef typename CT<T>::type C;
   const int m = n / R;
   const int total = m * nb;
+  const int toff = P.twoff[st];
+  const FastDiv dm = P.dm[st], dns = P.dns[st];
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     int b, j;
-    if (COLS) { b = t % nb; j = t / nb; }
-    else { j = t % m; b = t / m; }
-    const int k = j % Ns;
+    if (COLS) { b = t % nb; j = t / nb; }  // nb is a compile-time tile width at the call sites
+    else { b = (int)dm.div((unsigned)t); j = t - b * m; }
+    const int jq = (int)dns.div((unsigned)j);
+    const int k = j - jq * Ns;
     C v[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -102,7 +121,7 @@ __device__ __forceinline__ void fft_pass(const typename CT<T>::type* __restrict_
     if (R == 4) dft4(v, sign);
     else if (R == 2) dft2(v);
     else dft3<C, T>(v, sign);
-    const int base = (j / Ns) * Ns * R + k;
+    const int base = jq * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
       if (r < R) {
@@ -119,7 +138,7 @@ __device__ typename CT<T>::type* fft_smem(typename CT<T>::type* x, typename CT<T
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.radix[s];
-    fft_pass<T, COLS>(x, y, P.n, nb, bstride, R, Ns, P, P.twoff[s], sign);
+    fft_pass<T, COLS>(x, y, P.n, nb, bstride, R, Ns, P, s, sign);
     __syncthreads();
     typename CT<T>::type* t = x; x = y; y = t;
     Ns *= R;
@@ -146,6 +165,7 @@ struct RowJob {
   const double* off[JOB_MAXF];  // per-plane offsets: r2c subtracts off[plane] before
                                 // scaling, c2r adds it to the output (null: none)
   int rpc;                      // rows per CTA (0: default for the size)
+  FastDiv dnc;                  // ncols
 };
 
 // Spectral coefficient codes for the column operator.

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
   const T dv = (T)J.div[f];
   const double off = J.off[f] ? J.off[f][lev] : 0.0;
   for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
-    const int r = t / m, k = t - r * m;
+    const int r = (int)P.dm.div((unsigned)t), k = t - r * m;
     const TIn* row = src + (size_t)(row0 + r) * J.ld;
     T a, b;
     if (J.off[f]) {  // subtract in double before rounding to T
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
   C* Z = fft_smem<T, false>(A, B, nrow, m, P.c, -1);
   C* out = reinterpret_cast<C*>(J.work[f]) + (size_t)lev * J.pstride_work;
   for (int t = threadIdx.x; t < nrow * J.ncols; t += blockDim.x) {
-    const int r = t / J.ncols, k = t - r * J.ncols;
+    const int r = (int)J.dnc.div((unsigned)t), k = t - r * J.ncols;
     const C* z = Z + r * m;
     C X;
     if (k == 0 || k == m) {
@@ -89,14 +89,14 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
   const int nrow = min(rpc, J.ny - row0);
   const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work;
   for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
-    const int r = t / (m + 1), k = t - r * (m + 1);
+    const int r = (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
     C v = k < J.ncols ? in[(size_t)(row0 + r) * J.wc + k] : mk<T>((T)0, (T)0);
     if (k == 0 || k == m) v.y = (T)0;  // halfcomplex pass ignores these imaginary parts
     X[t] = v;
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
-    const int r = t / m, k = t - r * m;
+    const int r = (int)P.dm.div((unsigned)t), k = t - r * m;
     const C a = X[r * (m + 1) + k];
     const C b = cconj(X[r * (m + 1) + (m - k)]);
     const C e = cadd(a, b);
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
   TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys;
   const double off = J.off[f] ? J.off[f][lev] : 0.0;
   for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
-    const int r = t / (m + 1), k = t - r * (m + 1);
+    const int r = (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
     TOut* row = dst + (size_t)(row0 + r) * J.ld;
     if (k < m) {
       const C z = Z[r * m + k];
@@ -241,13 +241,15 @@ int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   typedef typename CT<T>::type C;
   const int rpc = J.rpc > 0 ? J.rpc : rows_pc<T>(P.nx);
   const size_t sm = (size_t)2 * rpc * (P.nx / 2) * sizeof(C);
+  RowJob JJ = J;
+  JJ.dnc = FastDiv((unsigned)J.ncols);
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
   static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
   if (sm > sm_set) {
     cudaFuncSetAttribute(k_rows_r2c<T, TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     sm_set = sm;
   }
-  k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
+  k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(JJ, P, rpc); LES_COUNT_LAUNCH();
   return 0;
 }
 

@@ -39,10 +39,13 @@ static int make_plan(les_ctx* c, int n, HostPlan& hp) {
   while (m % 2 == 0) { P.radix[P.nst++] = 2; m /= 2; }
   while (m % 3 == 0) { P.radix[P.nst++] = 3; m /= 3; }
   if (m != 1 || P.nst > FFT_MAX_STAGES) { les_set_error("FFT size %d is not 2^a 3^b", n); return LES_ERR_UNSUPPORTED; }
+  if (n > 4096) { les_set_error("FFT size %d exceeds 4096", n); return LES_ERR_UNSUPPORTED; }
   std::vector<double2> tw;
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.radix[s];
+    P.dm[s] = FastDiv((unsigned)(n / R));
+    P.dns[s] = FastDiv((unsigned)Ns);
     P.twoff[s] = (int)tw.size();
     for (int r = 1; r < R; ++r)
       for (int k = 0; k < Ns; ++k) {
@@ -72,6 +75,8 @@ static int make_real_plan(les_ctx* c, int nx, HostRealPlan& rp) {
   rp.r.c = hp.c;
   rp.r.nx = nx;
   const int m = nx / 2;
+  rp.r.dm = FastDiv((unsigned)m);
+  rp.r.dm1 = FastDiv((unsigned)(m + 1));
   std::vector<double2> w(m + 1);
   for (int k = 0; k <= m; ++k) {
     const long double ang = -2.0L * 3.14159265358979323846264338327950288L * k / (long double)nx;
