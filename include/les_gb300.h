@@ -197,6 +197,24 @@ int les_fft_c2r(les_ctx* ctx, double* planes, int nplanes, int big);
 /* tridag_array.f90:1-109 : a,b,c (lh,ny,nz+1) real; r,u (lh,ny,nz+1) complex. */
 int les_tridag_array(les_ctx* ctx, const double* a, const double* b, const double* c,
                      const double* r, double* u);
+/* No counterpart in the reference.  les_tridag_array without any device
+ * allocation, for callers that cannot call cudaMalloc or let a library do it
+ * for them: applications whose device memory is all handed out by their own
+ * pool or arena, and code that must not allocate mid-run.  It needs no
+ * les_ctx (creating one allocates).  a, b, c (lh,ny,n) real and r, u
+ * (lh,ny,n) complex are device pointers on the current device (r, u 16-byte
+ * aligned); n = nz+1 in the reference's call.  The Thomas coefficients go to
+ * a fixed scratch array compiled into the library, held on every GPU that
+ * loads it until the process exits: lh*ny*n <= LES_NOALLOC_TRIDAG_MAX_ELEMS
+ * (2^21, 16 MiB of doubles), larger sizes return LES_ERR_ARG.  The first call
+ * on each device looks up that array's address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams or host threads on the same device) race; serialise them.  Runs
+ * on `stream` (a cudaStream_t, 0 for the default stream) and waits for it
+ * to finish, to report a zero pivot as LES_ERR_PIVOT. */
+#define LES_NOALLOC_TRIDAG_MAX_ELEMS (1u << 21)
+int les_tridag_array_noalloc(const double* a, const double* b, const double* c, const double* r,
+                             double* u, int lh, int ny, int n, void* stream);
 /* Routines that read the module arrays bound to the context. */
 /* convec.f90:1-248 -> cx, cy, cz (ld,ny,nz), valid 1:nz-1. */
 int les_convec(les_ctx* ctx, double* cx, double* cy, double* cz);

@@ -1502,6 +1502,12 @@ int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, co
                                                                     g.nz + 1, flag); LES_COUNT_LAUNCH();
   return 0;
 }
+// The same kernel with caller-supplied scratch (gam: lh*ny*n doubles, flag: one int).
+void launch_tridag_generic(const double* a, const double* b, const double* cc, const double* r, double* u,
+                           double* gam, int lh, int ny, int n, int* flag, cudaStream_t s) {
+  k_tridag_generic<<<(lh * ny + 127) / 128, 128, 0, s>>>(a, b, cc, (const C2*)r, (C2*)u, gam, lh, ny, n, flag);
+  LES_COUNT_LAUNCH();
+}
 
 // ---------------------------------------------------------------------------
 // scalars_module.f90:254-283 surface flux and dsdz(1)
