@@ -125,7 +125,7 @@ static void grid_of(const les_config& k, Grid& g) {
 }
 
 struct Sizes {
-  size_t wsA, wsB, wsP, big, tmp, fields, surf, spare;
+  size_t wsA, wsB, wsP, big, tmp, fields, surf, spare, aux;
   int lag_chunk, ntmp;
 };
 static Sizes sizes_of(const Grid& g) {
@@ -142,6 +142,10 @@ static Sizes sizes_of(const Grid& g) {
   for (int f = 0; f < LES_ZO; ++f) s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
   s.surf = (size_t)(LES_NUM_FIELDS - LES_ZO + 1) * g.nx * g.ny * sizeof(double);
   s.spare = 4 * g.nfield * sizeof(double) + (4 * nz + 4) * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double);
+  // saved spectra, wall-plane spectra, Thomas tables, reductions, wavenumber
+  // and filter tables (FP64 + FP32)
+  s.aux = 4 * nz * C * sizeof(double2) + 4 * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double) +
+          (20 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float);
   return s;
 }
 
@@ -197,7 +201,7 @@ size_t les_estimate_device_bytes(const les_config* cfg) {
   Grid g;
   grid_of(*cfg, g);
   Sizes s = sizes_of(g);
-  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + (1u << 20);
+  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + (1u << 20);
 }
 
 int les_ctx_create(const les_config* cfg, les_ctx** out) {
@@ -273,7 +277,7 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   if ((st = dalloc(c, &c->wsA, s.wsA)) || (st = dalloc(c, &c->wsB, s.wsB)) || (st = dalloc(c, &c->wsP, s.wsP)) ||
       (st = dalloc(c, (void**)&c->big, s.big)) || (st = dalloc(c, (void**)&c->tmp, s.tmp)) ||
       (st = dalloc(c, (void**)&c->spare, s.spare)) || (st = dalloc(c, (void**)&c->dscal, 64 * sizeof(double))) ||
-      (st = dalloc(c, (void**)&c->dred, 16 * (size_t)(g.nz + 8) * sizeof(double))) ||
+      (st = dalloc(c, (void**)&c->dred, 20 * (size_t)(g.nz + 8) * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->spec, 4 * (size_t)g.nz * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->wspec, 4 * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||
@@ -517,6 +521,7 @@ struct les_ensemble {
   std::vector<les_ctx*> m;
   cudaStream_t root = nullptr;
   cudaEvent_t fork = nullptr;
+  cudaEvent_t done = nullptr;  // end of the last graph launch, waited on by every member stream
   std::vector<cudaEvent_t> join;
   std::map<std::vector<int>, cudaGraphExec_t> graphs;
 };
@@ -535,7 +540,8 @@ int les_ensemble_create(les_ctx* const* members, int n, les_ensemble** out) {
   les_ensemble* e = new les_ensemble();
   e->m.assign(members, members + n);
   if (cudaStreamCreateWithFlags(&e->root, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming) != cudaSuccess) {
     delete e; les_set_error("ensemble stream/event creation failed"); return LES_ERR_CUDA;
   }
   e->join.resize(n);
@@ -599,7 +605,16 @@ int les_ensemble_step(les_ensemble* e, int nsteps) {
       if (ce != cudaSuccess) { les_set_error("ensemble instantiate: %s", cudaGetErrorString(ce)); return LES_ERR_CUDA; }
       it = e->graphs.emplace(key, ex).first;
     }
+    // the graph runs on the root stream: it starts after work already queued
+    // on the members' streams, and what is queued on them later (a field
+    // read, a per-member step) starts after it
+    for (int i = 0; i < n; ++i) {
+      LES_CUDA_CHECK(cudaEventRecord(e->join[i], e->m[i]->stream));
+      LES_CUDA_CHECK(cudaStreamWaitEvent(e->root, e->join[i], 0));
+    }
     LES_CUDA_CHECK(cudaGraphLaunch(it->second, e->root));
+    LES_CUDA_CHECK(cudaEventRecord(e->done, e->root));
+    for (les_ctx* c : e->m) LES_CUDA_CHECK(cudaStreamWaitEvent(c->stream, e->done, 0));
     for (les_ctx* c : e->m) { c->jt += 1; c->jt_total += 1; }
   }
   return LES_OK;
@@ -611,6 +626,7 @@ int les_ensemble_destroy(les_ensemble* e) {
   for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
   for (cudaEvent_t ev : e->join) cudaEventDestroy(ev);
   if (e->fork) cudaEventDestroy(e->fork);
+  if (e->done) cudaEventDestroy(e->done);
   if (e->root) cudaStreamDestroy(e->root);
   delete e;
   return LES_OK;
@@ -618,7 +634,8 @@ int les_ensemble_destroy(les_ensemble* e) {
 
 int les_rmsdiv(les_ctx* c, double* rms) {
   if (!c || !rms) return LES_ERR_ARG;
-  op_rmsdiv(c, c->dscal + 1);
+  if (c->cfg.precision == 1) op_rmsdiv_state(c, c->dscal + 1);
+  else op_rmsdiv(c, c->dscal + 1);
   LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 1, c->dscal + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   *rms = c->host_scal[1];

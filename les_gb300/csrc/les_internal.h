@@ -98,6 +98,7 @@ int op_test_filter(les_ctx* c, double* out, const double* in, int nplanes, int w
 int op_dealias1(les_ctx* c, const double* const* in, double* const* out, int nf, int nlev);
 int op_dealias2(les_ctx* c, double* const* out, const double* const* in, int nf, int nlev, double scale);
 int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse);
+int op_rmsdiv_state(les_ctx* c, double* out_dev);
 int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, const double* r, double* u);
 void launch_tridag_generic(const double* a, const double* b, const double* cc, const double* r, double* u,
                            double* gam, int lh, int ny, int n, int* flag, cudaStream_t s);

@@ -232,47 +232,205 @@ int filt_da_multi_spec(les_ctx* c, double* const* f, double* const* dx, double* 
   c2r(c, 3 * nf, nlev, c->wsB, out, (long)g.nplane, false, g.lh);
   return 0;
 }
-// Mixed-form filt_da of u, v, w: the filtered velocities and dudx, dvdy
-// (read by rmsdiv, rmsdiv.f90:93-100) in FP64; dudy, dvdx, dwdx, dwdy, which
-// only feed S_ij of the SGS model, from the saved FP64 spectra in FP32.
+// filt_da.f90:3-42 Nyquist removal done in physical space, in FP64.  With
+// a(x) = (1/ny) sum_y (-1)^y f(x,y), b(y) = (1/nx) sum_x (-1)^x f(x,y) and
+// c = (1/nx) sum_x (-1)^x a(x), the part of f on the modes ky = ny/2 (every
+// kx) and kx = nx/2 (every ky) is (-1)^y a(x) + (-1)^x b(y) - (-1)^(x+y) c,
+// which is what the forward transform, the zeroing of those modes and the
+// inverse transform remove; here it is removed exactly, up to FP64
+// rounding, with no transform.  Three kernels, every sum in a fixed order
+// (deterministic), no FP64 work on idle lanes (the FP64 pipe is the scarce
+// unit on this part):
+//   k_nyq_part   per (16-row chunk, level, field): the chunk's partial
+//                a(x) (unnormalised), b(y) of its rows, its plain sum;
+//   k_nyq_comb   per (level, field): a(x) -/+ c for even/odd x, the mean;
+//   k_nyq_apply  every point: f -= (-1)^y (a - (-1)^x c) + (-1)^x b.
+constexpr int NYQ_ROWS = 16;
+struct NyqScratch {
+  double* apart;  // [field][level][chunk][nx]
+  double* b;      // [field][level][ny]
+  double* spart;  // [field][level][chunk]
+  double* ac;     // [field][level][nx]  a(x) - c (x even), a(x) + c (x odd)
+};
+template <int K>
+__global__ void k_nyq_part(const double* f0, const double* f1, const double* f2, NyqScratch S, int ld, int nx,
+                           int ny, long ps, int nlev, int nch) {
+  __shared__ double ws[8][NYQ_ROWS], wd[8][NYQ_ROWS];
+  const int ch = blockIdx.x, lev = blockIdx.y, fld = blockIdx.z;
+  const double* f = (fld == 0 ? f0 : fld == 1 ? f1 : f2) + (size_t)lev * ps;
+  const int np = nx / 2, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int y0 = ch * NYQ_ROWS, nr = min(NYQ_ROWS, ny - y0);
+  double2 acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = make_double2(0.0, 0.0);
+#pragma unroll 4
+  for (int r = 0; r < nr; ++r) {
+    const int y = y0 + r;
+    const double2* row = reinterpret_cast<const double2*>(f + (size_t)y * ld);
+    double se = 0.0, so = 0.0;  // sums over even / odd x
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int p = threadIdx.x + k * blockDim.x;
+      if (p < np) {
+        const double2 v = row[p];
+        if (y & 1) { acc[k].x -= v.x; acc[k].y -= v.y; }
+        else { acc[k].x += v.x; acc[k].y += v.y; }
+        se += v.x;
+        so += v.y;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      se += __shfl_xor_sync(0xffffffffu, se, o);
+      so += __shfl_xor_sync(0xffffffffu, so, o);
+    }
+    if (lane == 0) { ws[wid][r] = se + so; wd[wid][r] = se - so; }
+  }
+  const size_t pl = (size_t)fld * nlev + lev;
+  double* ap = S.apart + (pl * nch + ch) * nx;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int p = threadIdx.x + k * blockDim.x;
+    if (p < np) reinterpret_cast<double2*>(ap)[p] = acc[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    double b = 0.0;
+    for (int w = 0; w < nw; ++w) b += wd[w][threadIdx.x];
+    S.b[pl * ny + y0 + threadIdx.x] = b / (double)nx;
+  }
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int r = 0; r < nr; ++r)
+      for (int w = 0; w < nw; ++w) t += ws[w][r];
+    S.spart[pl * nch + ch] = t;
+  }
+}
+__global__ void __launch_bounds__(256) k_nyq_comb(NyqScratch S, double* mean, int mstride, int nx, int ny, int nlev,
+                                                  int nch) {
+  __shared__ double red[256];
+  const int lev = blockIdx.x, fld = blockIdx.y;
+  const size_t pl = (size_t)fld * nlev + lev;
+  const double iny = 1.0 / (double)ny;
+  double cp = 0.0;
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+    double a = 0.0;
+    for (int ch = 0; ch < nch; ++ch) a += S.apart[(pl * nch + ch) * nx + x];
+    a *= iny;
+    S.ac[pl * nx + x] = a;
+    cp += (x & 1) ? -a : a;
+  }
+  red[threadIdx.x] = cp;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double c = red[0] / (double)nx;
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) S.ac[pl * nx + x] += (x & 1) ? c : -c;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int ch = 0; ch < nch; ++ch) t += S.spart[pl * nch + ch];
+    mean[(size_t)fld * mstride + lev] = t / ((double)nx * (double)ny);
+  }
+}
+__global__ void k_nyq_apply(double* f0, double* f1, double* f2, NyqScratch S, int ld, int nx, int ny, long ps,
+                            int nlev, int nf) {
+  const int np1 = nx / 2 + 1;  // pairs per row, the last one the padding columns
+  const size_t per = (size_t)ny * np1;
+  GSTRIDE(t, per * nlev * nf) {
+    const size_t pl = t / per;
+    const size_t r = t - pl * per;
+    const int y = (int)(r / np1), p = (int)(r - (size_t)y * np1);
+    const int fld = (int)(pl / nlev), lev = (int)(pl - (size_t)fld * nlev);
+    double* f = (fld == 0 ? f0 : fld == 1 ? f1 : f2) + (size_t)lev * ps + (size_t)y * ld;
+    double2* q = reinterpret_cast<double2*>(f) + p;
+    if (p == np1 - 1) { *q = make_double2(0.0, 0.0); continue; }  // padding columns ld-1:ld
+    const double2 ac = reinterpret_cast<const double2*>(S.ac + pl * nx)[p];
+    const double b = S.b[pl * ny + y];
+    const double ae = (y & 1) ? -ac.x : ac.x, ao = (y & 1) ? -ac.y : ac.y;
+    double2 v = *q;
+    v.x = (v.x - ae) - b;
+    v.y = (v.y - ao) + b;
+    *q = v;
+  }
+}
+// nf <= 3 fields of nlev levels, in place; plane means to mean[f*mstride+lev];
+// scratch (a few MB) in the given work buffer
+static void nyq_kill(les_ctx* c, double* const* f, int nf, int nlev, double* mean, int mstride, void* scratch) {
+  const Grid& g = c->g;
+  const int nch = (g.ny + NYQ_ROWS - 1) / NYQ_ROWS;
+  const size_t npl = (size_t)nf * nlev;
+  NyqScratch S;
+  S.apart = static_cast<double*>(scratch);
+  S.b = S.apart + npl * nch * g.nx;
+  S.spart = S.b + npl * g.ny;
+  S.ac = S.spart + npl * nch + 2;  // keeps ac 16-byte aligned (npl*nch even or padded)
+  if ((reinterpret_cast<uintptr_t>(S.ac) & 15) != 0) S.ac += 1;
+  double* f0 = f[0];
+  double* f1 = nf > 1 ? f[1] : f[0];
+  double* f2 = nf > 2 ? f[2] : f[0];
+  const int np = g.nx / 2;
+  const int bt = std::min(256, (np + 31) / 32 * 32);
+  const int K = (np + bt - 1) / bt;  // <= 16: nx <= 8192 (the transforms allow less)
+  const dim3 grid(nch, nlev, nf);
+  const long ps = (long)g.nplane;
+  switch (K) {
+    case 1: k_nyq_part<1><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+    case 2: k_nyq_part<2><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+    case 3: case 4: k_nyq_part<4><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+    case 5: case 6: case 7: case 8:
+      k_nyq_part<8><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+    default: k_nyq_part<16><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+  }
+  LES_COUNT_LAUNCH();
+  k_nyq_comb<<<dim3(nlev, nf), 256, 0, c->stream>>>(S, mean, mstride, g.nx, g.ny, nlev, nch); LES_COUNT_LAUNCH();
+  k_nyq_apply<<<grid1(npl * g.ny * (np + 1)), 256, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nf);
+  LES_COUNT_LAUNCH();
+}
+
+// FP32 spectra of f - mean(level) -> the FP64 spectra F(f/(nx*ny)) the fused
+// step reads: the (0,0) mode is the FP64 plane mean itself
+__global__ void k_spec_widen(const float2* __restrict__ s, double2* __restrict__ d, const double* __restrict__ mean,
+                             int mstride, size_t fs, size_t nk, int nf) {
+  GSTRIDE(t, fs * nf) {
+    const size_t fld = t / fs, r = t - fld * fs;
+    const size_t lev = r / nk, m = r - lev * nk;
+    const float2 v = s[t];
+    d[t] = m == 0 ? make_double2(mean[fld * mstride + lev], 0.0) : make_double2((double)v.x, (double)v.y);
+  }
+}
+
+// Mixed-form filt_da of u, v, w: the Nyquist removal in FP64 in physical
+// space (the velocities keep FP64 accuracy); the six horizontal
+// derivatives, which feed only the SGS strain (S_ij), and the saved spectra,
+// which feed the FP32 convective, SGS and padding transforms, from one FP32
+// transform of f - plane mean.  rmsdiv's FP64 dudx + dvdy are formed on the
+// steps that report it (step_rmsdiv_mixed).
 static int filt_da_uvw_mixed(les_ctx* c) {
   const Grid& g = c->g;
   const int nz = g.nz;
   const long FS = (long)nz * g.C;
+  double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  const int ms = nz + 8;
+  double* mean = c->dred + 16 * (size_t)ms;  // u, v, w plane means
+  nyq_kill(c, f3, 3, nz, mean, ms, c->wsB);
   const double sc = 1.0 / (double)(g.nx * g.ny);
-  const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  const double* in[3] = {f3[0], f3[1], f3[2]};
   const double scs[3] = {sc, sc, sc};
-  r2c(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
-  // FP64 y pass: filtered field (all three), spectrum saved (all three)
+  const double* offs[3] = {mean, mean + ms, mean + 2 * ms};
+  r2cT<float, double>(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh, offs);
+  float2* ob = (float2*)c->wsB;
   ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
-  J.nin = 1; J.nout = 2; J.nf = 3; J.inv_mask = 1u;
+  J.nin = 1; J.nout = 3; J.nf = 3; J.inv_mask = 6u;  // output 0 (the spectrum) stays spectral
   J.in[0] = c->wsA; J.fs_in = FS;
-  J.out[0] = c->wsB; J.out[1] = c->spec; J.fs_out = FS;
-  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_KILL;
-  cols(c, J);
-  // FP64 dudx and dvdy from the spectra (inverse only)
-  ColJob K = coljob(c, MAP_SAME, DIR_INV, nz);
-  K.nin = 1; K.nout = 1; K.nf = 1;
-  K.in[0] = c->spec; K.out[0] = (C2*)c->wsB + 3 * FS; K.coef[0][0] = CC_IKX;
-  cols(c, K);
-  K.in[0] = c->spec + FS; K.out[0] = (C2*)c->wsB + 4 * FS; K.coef[0][0] = CC_IKY;
-  cols(c, K);
-  double* o5[5] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DUDX], c->f[LES_DVDY]};
-  c2r(c, 5, nz, c->wsB, o5, (long)g.nplane, false, g.lh);
-  // FP32 derivatives for the SGS strain
-  float2* w32 = (float2*)c->wsA;
-  ColJob L = coljob(c, MAP_SAME, DIR_INV, nz);
-  L.nin = 1; L.nout = 1; L.nf = 1;
-  L.in[0] = c->spec; L.out[0] = w32; L.coef[0][0] = CC_IKY;                  // dudy
-  colsT<float, double2>(c, L);
-  L.in[0] = c->spec + FS; L.out[0] = w32 + FS; L.coef[0][0] = CC_IKX;        // dvdx
-  colsT<float, double2>(c, L);
-  L.in[0] = c->spec + 2 * FS;                                                // dwdx, dwdy
-  L.nout = 2; L.out[0] = w32 + 2 * FS; L.out[1] = w32 + 3 * FS;
-  L.coef[0][0] = CC_IKX; L.coef[1][0] = CC_IKY;
-  colsT<float, double2>(c, L);
-  double* o4[4] = {c->f[LES_DUDY], c->f[LES_DVDX], c->f[LES_DWDX], c->f[LES_DWDY]};
-  c2rT<float, double>(c, 4, nz, c->wsA, o4, (long)g.nplane, false, g.lh);
+  J.out[0] = ob + 6 * FS; J.out[1] = ob; J.out[2] = ob + 3 * FS; J.fs_out = FS;
+  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY;
+  colsT<float, float2>(c, J);
+  k_spec_widen<<<grid1(3 * (size_t)FS), 256, 0, c->stream>>>(ob + 6 * FS, c->spec, mean, ms, (size_t)FS, g.C, 3);
+  LES_COUNT_LAUNCH();
+  double* o6[6] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX], c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
+  c2rT<float, double>(c, 6, nz, c->wsB, o6, (long)g.nplane, false, g.lh);
   return 0;
 }
 
@@ -1672,7 +1830,7 @@ __global__ void __launch_bounds__(512) k_rmsdiv_part(const double* __restrict__ 
   for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
     const int jy = e / nx, jx = e - jy * nx;
     const size_t i = o + (size_t)jy * ld + jx;
-    s += fabs(du[i] + dv[i] + dw[i]);
+    s += fabs(du[i] + (dv ? dv[i] : 0.0) + dw[i]);  // dv null: du holds dudx + dvdy
   }
   sh[threadIdx.x] = s;
   __syncthreads();
@@ -1912,7 +2070,8 @@ __global__ void k_lag_prod(const double* __restrict__ u, const double* __restric
 // Precision of the fused-step transforms: MX = false -> FP64 everywhere;
 // MX = true -> FP32 transforms and FP32 3/2-grid / filter temporaries for the
 // scalar, convective, stress-divergence and SGS terms (the projection path,
-// filt_da of u, v, w and the plane/wall quantities stay FP64).
+// the Nyquist filtering of u, v, w, rmsdiv and the plane/wall quantities
+// stay FP64).
 template <bool MX> struct PX {
   typedef typename std::conditional<MX, float, double>::type T;     // transform precision
   typedef typename CT<T>::type CX;                                   // its complex type
@@ -2069,6 +2228,32 @@ static void div_xyT(les_ctx* c, const double* tx, const double* ty, double* out,
   J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
   colsT<T, CX>(c, J);
   c2rT<T, double>(c, 1, nlev, c->wsB, &out, (long)g.nplane, false, g.lh);
+}
+
+// rmsdiv.f90:93-100 for the mixed form: its SGS-only dudx, dvdy are FP32
+// accurate, so dudx + dvdy is formed here in FP64 (one spectral sum, one
+// inverse) into dh (one field) from the filtered u, v.
+static void rmsdiv_mixed(les_ctx* c, double* dh, const double* dwdz, double* out_dev) {
+  const Grid& g = c->g;
+  div_xyT<false>(c, c->f[LES_U], c->f[LES_V], dh, g.nz);
+  double* part = c->dred;
+  k_rmsdiv_part<<<g.nz - 1, 512, 0, c->stream>>>(dh, nullptr, dwdz, part, g.ld, g.nx, g.ny); LES_COUNT_LAUNCH();
+  k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev); LES_COUNT_LAUNCH();
+}
+// les_rmsdiv between steps in the mixed form: the FP64 divergence of the
+// current state as the next step's filt_da sees it (w Nyquist-filtered; the
+// horizontal derivatives ignore the Nyquist modes by construction).
+int op_rmsdiv_state(les_ctx* c, double* out_dev) {
+  const Grid& g = c->g;
+  double* dh = c->tmp;
+  double* wf = c->tmp + g.nfield;
+  double* dwz = c->tmp + 2 * g.nfield;
+  cudaMemcpyAsync(wf, c->f[LES_W], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  double* f1[1] = {wf};
+  nyq_kill(c, f1, 1, g.nz, c->dred + 16 * (size_t)(g.nz + 8), g.nz + 8, c->wsB);
+  op_ddz(c, dwz, wf, 0);
+  rmsdiv_mixed(c, dh, dwz, out_dev);
+  return 0;
 }
 
 template <bool MX>
@@ -2240,6 +2425,8 @@ static int stepT(les_ctx* c) {
   op_ddz(c, c->f[LES_DUDZ], c->f[LES_U], 1);
   op_ddz(c, c->f[LES_DVDZ], c->f[LES_V], 1);
   op_ddz(c, c->f[LES_DWDZ], c->f[LES_W], 0);
+  const bool rms_step = k.rmsdiv_every > 0 && c->jt % k.rmsdiv_every == 0;
+  if (MX && rms_step) rmsdiv_mixed(c, c->tmp, c->f[LES_DWDZ], c->dscal + 1);
   op_wallstress(c);
   {  // spectra of the wall planes dudz(1), dvdz(1) set by wallstress
     const double cs = 1.0 / (double)(g.nx * g.ny);
@@ -2266,8 +2453,8 @@ static int stepT(les_ctx* c) {
                                                         c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
                                                         k.dt); LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaGetLastError());
-  if (k.rmsdiv_every > 0 && c->jt % k.rmsdiv_every == 0) {
-    op_rmsdiv(c, c->dscal + 1);
+  if (rms_step) {
+    if (!MX) op_rmsdiv(c, c->dscal + 1);
     LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 1, c->dscal + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     double cflu, visc;
     int st = op_tsc(c, &cflu, &visc);

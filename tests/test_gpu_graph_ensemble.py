@@ -52,10 +52,12 @@ def test_ensemble_member_equals_alone(gpu_lib):
     shapes = [(32, 32, None), (32, 24, None), (48, 32, None), (64, 16, 48)]
     ens_members = [member(n, z, 100 + i, ny=ny) for i, (n, z, ny) in enumerate(shapes)]
     alone = [member(n, z, 100 + i, ny=ny) for i, (n, z, ny) in enumerate(shapes)]
-    ens = lg.Ensemble(ens_members)
-    ens.step(11)
     for m in alone:
         m.step(11)
+    ens = lg.Ensemble(ens_members)
+    ens.step(11)
+    # read right after the ensemble step: a member's field read (on its own
+    # stream) must be ordered after the graph launched on the ensemble stream
     for m, a in zip(ens_members, alone):
         sm, sa = state(m), state(a)
         for k in sm:
