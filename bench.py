@@ -1,20 +1,23 @@
 """Benchmark of the per-timestep spectral core (pt-steps/s = Nx*Ny*Nz*steps / s).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|mixed]
-                  [--impl ours|reference] [--grid 256]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|fp64]
+                  [--impl ours|reference] [--grid 256] [--no-fp64] [--no-e2e] [--no-cpu]
 
-Workload: the 256^3 member of the precision study (box 2pi x 2pi x 1, active
-theta, x-striped z0 = 1e-4/1e-2 and surface heat flux 0.05/0.15 K m/s,
-Lagrangian scale-dependent SGS, dt = 2e-4), seeded synthetic initial state.
-A step is one call of the fused time step (main.f90:202-478) on the
-device-resident member.  With N > 1 (torchrun) every rank advances its own
-independent member: replicas only, no collective (weak scaling).
+Workload: 256^3 LES member (box 2pi x 2pi x 1, active theta, x-striped
+z0 = 1e-4/1e-2 and surface heat flux 0.05/0.15 K m/s in stripes of width
+Nx/8, Lagrangian scale-dependent SGS, dt = 2e-4), seeded synthetic initial
+state.  A step is one call of the fused time step (main.f90:202-478) on the
+device-resident member; the headline is the FP32-mixed step, with the FP64
+step of the same member timed beside it (and the velocity error and rmsdiv
+of the mixed state after the same steps).  With N > 1 (torchrun) every rank
+advances its own independent member: replicas only, no collective.
 
 `--impl reference` times the CPU restatement of the reference step (the
 oracle; the Fortran reference has no compiler here) on all host cores on the
 same configuration.
 """
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -27,14 +30,20 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "pt-steps/s at 256³: FP32-mixed vs FP64 (≤1e-5 err); p99 ensemble step latency"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-FP64_PEAK_TFLOPS = 1.197  # measured FP64 FMA rate on this machine's GB300 (profiles/)
 
-# Algorithmic bytes per grid point per step: the routine I/O ledger (each
-# routine reads each interface array once and writes each output once;
-# padded 3/2 arrays count x2.25).  Velocity only 152.6 field units, velocity
-# plus theta 227 units; 8 B (FP64) per unit.
-LEDGER_UNITS = {0: 152.6, 1: 227.0}
+# Dominant kernel of each form's step (largest share of the ncu launch list
+# of the 256^3 step): the FP32 y-pass transforms (k_cols<float,...>) in the
+# mixed form, the FP64 y-pass transforms (k_cols<double,...>) in the FP64
+# form; les_profile_begin family ids.
+DOMINANT = {"mixed": (2, "k_cols<float> (FP32 y-pass transforms)"),
+            "fp64": (1, "k_cols<double> (FP64 y-pass transforms)")}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
+# byte of the dominant family, from one ncu capture (1 pass) of the same
+# 256^3 run's timed launches; scales the live algorithmic bytes per launch
+# to the traffic per launch.  Only valid at 256^3.
+TRAFFIC_RATIO = {"mixed": 0.8454, "fp64": 0.9214}
 
 
 def parse():
@@ -42,9 +51,10 @@ def parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)  # multiple of cs_count (5)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--grid", type=int, default=256)
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 step timed beside the mixed one")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
@@ -86,6 +96,7 @@ class ClockSampler:
         except Exception:
             self.proc = None
             return
+
         def rd():
             for line in self.proc.stdout:
                 self.samples.append([x.strip() for x in line.split(",")])
@@ -106,7 +117,8 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for s in self.samples:
             try:
-                sm.append(float(s[0])); mx.append(float(s[1]))
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
                 for k, nm in enumerate(names):
                     if s[3 + k].lower().startswith("active"):
                         reasons.add(nm)
@@ -117,33 +129,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def workload_config(args, lg):
-    precision = 1 if args.form == "mixed" else 0
-    cfg = lg.make_config(args.grid, s_flag=1, precision=precision, rmsdiv_every=0)
+def workload_config(lg, grid, form):
+    cfg = lg.make_config(grid, s_flag=1, precision=1 if form == "mixed" else 0, rmsdiv_every=0)
     surf = lg.striped_surface(cfg)
     return cfg, surf
 
 
-def cpu_baseline(args, lg, rank):
-    """Oracle (CPU restatement) timed on the host cores on one step of the
-    same workload (bounded sample)."""
-    from oracle.oracle import Oracle
-    oracle_build()
-    cfg, surf = workload_config(args, lg)
-    cfg.precision = 0
-    o = Oracle(cfg, surf)
-    cores = Oracle.max_threads()
-    st = lg.initial_state(cfg, surf, seed=1234)
-    for k, v in st.items():
-        o.set(k, v)
-    o.step(1)  # first (Euler) step, untimed
-    t0 = time.perf_counter()
-    o.step(1)
-    dt = time.perf_counter() - t0
-    pts = cfg.nx * cfg.ny * (cfg.nz - 1)
-    return {"value": pts / dt, "unit": "pt-steps/s", "cores": cores, "kind": "port",
-            "sample": "1 FP64 step of the %dx%dx%d workload after one untimed step (%.2f s)"
-                      % (cfg.nx, cfg.ny, cfg.nz - 1, dt)}
+def workload_name(cfg):
+    return "les %dx%dx%d theta striped-surface lagrangian-sdep" % (cfg.nx, cfg.ny, cfg.nz - 1)
 
 
 def oracle_build():
@@ -151,24 +144,37 @@ def oracle_build():
     o.build()
 
 
+def cpu_baseline(lg, grid):
+    """Oracle (CPU restatement) timed on the host cores on one step of the
+    same workload (bounded sample)."""
+    from oracle.oracle import Oracle
+    oracle_build()
+    cfg, surf = workload_config(lg, grid, "fp64")
+    o = Oracle(cfg, surf)
+    cores = Oracle.max_threads()
+    for k, v in lg.initial_state(cfg, surf, seed=1234).items():
+        o.set(k, v)
+    o.step(1)  # first (Euler) step, untimed
+    t0 = time.perf_counter()
+    o.step(1)
+    dt = time.perf_counter() - t0
+    pts = cfg.nx * cfg.ny * (cfg.nz - 1)
+    return {"value": pts / dt, "unit": "pt-steps/s", "cores": cores, "kind": "port",
+            "sample": "1 FP64 step of the %dx%dx%d workload after one untimed step (%.2f s), %d threads"
+                      % (cfg.nx, cfg.ny, cfg.nz - 1, dt, cores)}
+
+
 def run_reference(args):
-    import les_gb300.config as cfgmod
+    import les_gb300.config as lg
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle.oracle import Oracle
     oracle_build()
-
-    class LG:  # config helpers only
-        make_config = staticmethod(cfgmod.make_config)
-        striped_surface = staticmethod(cfgmod.striped_surface)
-        initial_state = staticmethod(cfgmod.initial_state)
-    cfg, surf = workload_config(args, LG)
-    cfg.precision = 0
+    cfg, surf = workload_config(lg, args.grid, "fp64")
     o = Oracle(cfg, surf)
     cores = Oracle.max_threads()
-    st = cfgmod.initial_state(cfg, surf, seed=1234)
-    for k, v in st.items():
+    for k, v in lg.initial_state(cfg, surf, seed=1234).items():
         o.set(k, v)
     for _ in range(max(args.warmup, 0)):
         o.step(1)
@@ -180,17 +186,46 @@ def run_reference(args):
     tot = sum(ts)
     pts = cfg.nx * cfg.ny * (cfg.nz - 1)
     val = pts * args.steps / tot
-    line = {"metric": "pt-steps/s at %d^3 (%s step)" % (args.grid, "FP64"), "value": val,
-            "unit": "pt-steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": "les %dx%dx%d theta striped-surface lagrangian-sdep" % (cfg.nx, cfg.ny, cfg.nz - 1),
-                       "grid": [cfg.nx, cfg.ny, cfg.nz - 1], "form": "fp64"},
+    line = {"metric": METRIC, "value": val, "unit": "pt-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": workload_name(cfg), "grid": [cfg.nx, cfg.ny, cfg.nz - 1], "form": "fp64",
+                       "parallelism": "replicas x1"},
             "cpu_baseline": {"value": val, "unit": "pt-steps/s", "cores": cores, "kind": "port",
                              "sample": "%d FP64 steps of the workload on %d host threads (CPU restatement "
                                        "of the reference; no Fortran compiler available)" % (args.steps, cores)},
             "e2e": {"value": val, "unit": "pt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def new_member(lg, grid, form, seed):
+    cfg, surf = workload_config(lg, grid, form)
+    ctx = lg.Context(cfg, surf)
+    for k, v in lg.initial_state(cfg, surf, seed=seed).items():
+        ctx.set(k, v)
+    return cfg, ctx
+
+
+def timed_steps(torch, lg, ctx, steps, prof_family=None):
+    """Advance `steps` steps; returns (total ms, per-step ms list, profile)."""
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    L = lg.lib()
+    if prof_family is not None:
+        lg.check(L.les_profile_begin(ctx.h, prof_family, 64 * steps))
+    ev[0].record(stream)
+    for i in range(steps):
+        ctx.step(1)
+        ev[i + 1].record(stream)
+    ev[-1].synchronize()
+    prof = None
+    if prof_family is not None:
+        n, ms, by = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        lg.check(L.les_profile_end(ctx.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(by)))
+        prof = (n.value, ms.value, by.value)
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+    return ev[0].elapsed_time(ev[-1]), per, prof
 
 
 def main():
@@ -202,19 +237,18 @@ def main():
     import torch
     import les_gb300 as lg
     from les_gb300 import build as b
+    from les_gb300.dist import aggregate
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     b.build()
-    cfg, surf = workload_config(args, lg)
-    ctx = lg.Context(cfg, surf)
-    st = lg.initial_state(cfg, surf, seed=1234 + rank)
-    for k, v in st.items():
-        ctx.set(k, v)
-    stream = torch.cuda.ExternalStream(ctx.stream())
+    L = lg.lib()
+    L.les_kernel_launch_count.restype = ctypes.c_ulonglong
+    cfg, ctx = new_member(lg, args.grid, args.form, 1234 + rank)
     pts = cfg.nx * cfg.ny * (cfg.nz - 1)
-    for _ in range(max(args.warmup, 3)):
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
         ctx.step(1)
     torch.cuda.synchronize()
 
@@ -222,41 +256,34 @@ def main():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
+    fam, fam_name = DOMINANT[args.form]
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
     clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    lib = lg.lib()
-    lib.les_kernel_launch_count.restype = __import__("ctypes").c_ulonglong
-    n0 = lib.les_kernel_launch_count()
-    e0.record(stream)
-    for _ in range(args.steps):
-        ctx.step(1)
-    e1.record(stream)
-    e1.synchronize()
+    n0 = L.les_kernel_launch_count()
+    ms, per, prof = timed_steps(torch, lg, ctx, args.steps, prof_family=fam)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    launches = int(L.les_kernel_launch_count() - n0)
     ck = clocks.stop()
-    launches = int(lib.les_kernel_launch_count() - n0)
     barrier()
-    from les_gb300.dist import aggregate
     ms_max, _, value = aggregate(ms, pts * args.steps, device="cuda")
 
-    # per-step kernel profile (dominant kernel = the whole step here: HBM ledger)
     hbm, src = measured_peaks()
-    units = LEDGER_UNITS[1]
-    bytes_per_step = units * 8.0 * pts
-    achieved = bytes_per_step / (ms_max / args.steps / 1e3) / 1e9
+    n_l, ms_l, bytes_l = prof
+    achieved = (bytes_l / n_l) / (ms_l / n_l / 1e3) / 1e9 if n_l else None
+    ratio = TRAFFIC_RATIO[args.form]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_source": src,
-                "scope": "whole step, algorithmic ledger bytes (227 FP64 field units per point)"}
+                "frac": achieved / hbm if achieved else None,
+                "traffic": (ratio * bytes_l / n_l) if (ratio and n_l and args.grid == 256) else None,
+                "peak_source": src, "kernel": fam_name, "launches_timed": n_l,
+                "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
+                "algorithmic_bytes_per_launch": bytes_l / n_l if n_l else None}
 
-    # e2e through the public API with pinned host buffers: H2D of the
-    # prognostic fields, one step, D2H of the prognostic fields
     e2e = None
     if not args.no_e2e:
+        # end to end through the public API: H2D of the prognostic fields from
+        # pinned host buffers, one step, D2H of the prognostic fields
         names = ["u", "v", "w", "theta"]
         host = {}
         for nm in names:
@@ -269,34 +296,64 @@ def main():
         t0 = time.perf_counter()
         for _ in range(ke):
             for nm in names:
-                lg.check(ctx.L.les_set_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
+                lg.check(L.les_set_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
             ctx.step(1)
             for nm in names:
-                lg.check(ctx.L.les_get_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
+                lg.check(L.les_get_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
         dt = time.perf_counter() - t0
         e2e = {"value": pts * ke * world / dt, "unit": "pt-steps/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes}
+
+    compare = None
+    if rank == 0 and args.form == "mixed" and not args.no_fp64:
+        # the FP64 step of the same member, same warm-up and step count
+        ctx.close()
+        ctx = None
+        cfg_m, ctx_m = new_member(lg, args.grid, "mixed", 1234)
+        cfg_d, ctx_d = new_member(lg, args.grid, "fp64", 1234)
+        for _ in range(warm):
+            ctx_d.step(1)
+            ctx_m.step(1)
+        torch.cuda.synchronize()
+        ms_d, per_d, _ = timed_steps(torch, lg, ctx_d, args.steps)
+        ctx_m.step(args.steps)
+        err = {}
+        for nm in ("u", "v", "w"):
+            a = ctx_m.get(nm)[:-1, :, :cfg.nx]
+            d = ctx_d.get(nm)[:-1, :, :cfg.nx]
+            err[nm] = (float(np.linalg.norm(a - d)), float(np.linalg.norm(d)))
+        vel = float(np.sqrt(sum(e[0] ** 2 for e in err.values())) / np.sqrt(sum(e[1] ** 2 for e in err.values())))
+        compare = {"fp64_ms_per_step": ms_d / args.steps, "fp64_value": pts * args.steps / (ms_d / 1e3),
+                   "mixed_over_fp64": (pts * args.steps / (ms / 1e3)) / (pts * args.steps / (ms_d / 1e3)),
+                   "steps_compared": warm + args.steps, "velocity_rel_err": vel,
+                   "rmsdiv_mixed": ctx_m.rmsdiv()}
+        ctx_m.close()
+        ctx_d.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            cpu = cpu_baseline(args, lg, rank)
+            cpu = cpu_baseline(lg, args.grid)
         except Exception as ex:  # reported, never fatal
             cpu = {"value": None, "error": str(ex)[:200]}
     if rank == 0:
-        line = {"metric": "pt-steps/s at %d^3 (%s step)" % (args.grid, "FP32-mixed" if args.form == "mixed" else "FP64"),
-                "value": value, "unit": "pt-steps/s", "n_gpus": world, "steps": args.steps,
-                "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        line = {"metric": METRIC, "value": value, "unit": "pt-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": warm, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.form == "fp64" else "f32/f64-mixed",
                 "data": "synthetic (seeded SplitMix64 initial state, x-striped surface)",
-                "config": {"workload": "les %dx%dx%d theta striped-surface lagrangian-sdep" % (cfg.nx, cfg.ny, cfg.nz - 1),
-                           "grid": [cfg.nx, cfg.ny, cfg.nz - 1], "form": args.form, "dt": cfg.dt,
-                           "l2": "inputs larger than L2 (state %.1f GB resident)" % (ctx.device_bytes() / 1e9),
+                "config": {"workload": workload_name(cfg), "grid": [cfg.nx, cfg.ny, cfg.nz - 1],
+                           "form": args.form, "dt": cfg.dt,
+                           "l2": "inputs larger than L2 (member state %.1f GB resident)"
+                                 % (lg.estimate_device_bytes(cfg) / 1e9),
                            "parallelism": "replicas x%d" % world},
+                "step_latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                                    "max": float(max(per))},
+                "fp64_comparison": compare,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": ck,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

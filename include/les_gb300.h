@@ -194,6 +194,16 @@ int les_test_filter_init(les_ctx* ctx, double alpha, double* G);
  * fft.f90:40-47); big = 1 selects the 3/2-padded plan. */
 int les_fft_r2c(les_ctx* ctx, double* planes, int nplanes, int big);
 int les_fft_c2r(les_ctx* ctx, double* planes, int nplanes, int big);
+/* Measurement (no counterpart in the reference): between les_profile_begin
+ * and les_profile_end, every launch of one transform-kernel family on the
+ * context's stream (eager steps, not graph replays) is bracketed by CUDA
+ * events.  family: 1 FP64 y-pass, 2 FP32 y-pass, 3 FP64 x-pass, 4 FP32
+ * x-pass; at most max_launches launches are measured.  end returns the
+ * launches measured, their summed device time (ms) and summed algorithmic
+ * bytes (each launch's inputs read once and outputs written once).  One
+ * session per process at a time. */
+int les_profile_begin(les_ctx* ctx, int family, int max_launches);
+int les_profile_end(les_ctx* ctx, int* launches, double* ms, double* bytes);
 /* tridag_array.f90:1-109 : a,b,c (lh,ny,nz+1) real; r,u (lh,ny,nz+1) complex. */
 int les_tridag_array(les_ctx* ctx, const double* a, const double* b, const double* c,
                      const double* r, double* u);

@@ -57,3 +57,22 @@ void les_set_error(const char* fmt, ...);
 // Number of kernels this library has launched (diagnostic counter).
 extern unsigned long long g_les_launches;
 #define LES_COUNT_LAUNCH() (++g_les_launches)
+
+namespace les {
+// Measurement hook (les_profile_begin/end): while a session is open, every
+// launch of one kernel family on the session's stream is bracketed by CUDA
+// events and its algorithmic bytes (inputs read once + outputs written once)
+// are summed.  Families: 1 FP64 y-pass, 2 FP32 y-pass, 3 FP64 x-pass,
+// 4 FP32 x-pass (forward and inverse).
+enum ProfFamily { PROF_COLS64 = 1, PROF_COLS32 = 2, PROF_ROWS64 = 3, PROF_ROWS32 = 4 };
+struct ProfSession {
+  int family = 0;
+  cudaStream_t stream = nullptr;
+  int n = 0, cap = 0;
+  cudaEvent_t* ev = nullptr;
+  double bytes = 0.0;
+};
+extern ProfSession* g_prof;
+bool prof_mark(int family, cudaStream_t s);         // true: the launch that follows is measured
+void prof_done(cudaStream_t s, double bytes);       // after that launch
+}  // namespace les

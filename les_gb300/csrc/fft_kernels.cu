@@ -249,7 +249,10 @@ int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
     cudaFuncSetAttribute(k_rows_r2c<T, TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     sm_set = sm;
   }
+  const bool pr = g_prof && prof_mark(sizeof(T) == 8 ? PROF_ROWS64 : PROF_ROWS32, s);
   k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(JJ, P, rpc); LES_COUNT_LAUNCH();
+  if (pr)
+    prof_done(s, (double)J.nfield * J.nlev * J.ny * ((double)P.nx * sizeof(TIn) + (double)J.ncols * sizeof(C)));
   return 0;
 }
 
@@ -265,7 +268,10 @@ int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
     cudaFuncSetAttribute(k_rows_c2r<T, TOut>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     sm_set = sm;
   }
+  const bool pr = g_prof && prof_mark(sizeof(T) == 8 ? PROF_ROWS64 : PROF_ROWS32, s);
   k_rows_c2r<T, TOut><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
+  if (pr)
+    prof_done(s, (double)J.nfield * J.nlev * J.ny * ((double)J.ncols * sizeof(C) + (double)J.ld * sizeof(TOut)));
   return 0;
 }
 
@@ -280,7 +286,13 @@ static int launch_cols_tx(const ColJob& J, const FftPlanDev& Pin, const FftPlanD
     cudaFuncSetAttribute(k_cols<T, TX, CIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     sm_set = sm;
   }
+  const bool pr = g_prof && prof_mark(sizeof(T) == 8 ? PROF_COLS64 : PROF_COLS32, s);
   k_cols<T, TX, CIn><<<grid, 256, sm, s>>>(J, Pin, Pout); LES_COUNT_LAUNCH();
+  if (pr) {
+    const double nf = J.nf > 0 ? J.nf : 1;
+    prof_done(s, nf * J.nlev * J.ncols *
+                     ((double)J.nin * J.ny_in * sizeof(CIn) + (double)J.nout * J.ny_out * sizeof(C)));
+  }
   return 0;
 }
 

@@ -12,6 +12,24 @@
 
 static thread_local char g_err[512] = "";
 unsigned long long g_les_launches = 0;
+namespace les {
+ProfSession* g_prof = nullptr;
+bool prof_mark(int family, cudaStream_t s) {
+  ProfSession* p = g_prof;
+  if (!p || p->family != family || p->stream != s || p->n >= p->cap) return false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+  return cudaEventRecord(p->ev[2 * p->n], s) == cudaSuccess;
+}
+void prof_done(cudaStream_t s, double bytes) {
+  ProfSession* p = g_prof;
+  if (!p) return;
+  if (cudaEventRecord(p->ev[2 * p->n + 1], s) == cudaSuccess) {
+    p->bytes += bytes;
+    p->n += 1;
+  }
+}
+}  // namespace les
 void les_set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -632,6 +650,47 @@ int les_ensemble_destroy(les_ensemble* e) {
   return LES_OK;
 }
 
+int les_profile_begin(les_ctx* c, int family, int max_launches) {
+  if (!c || family < PROF_COLS64 || family > PROF_ROWS32 || max_launches < 1) return LES_ERR_ARG;
+  if (g_prof) { les_set_error("a profiling session is already open"); return LES_ERR_STATE; }
+  ProfSession* p = new ProfSession();
+  p->family = family;
+  p->stream = c->stream;
+  p->cap = max_launches;
+  p->ev = new cudaEvent_t[2 * (size_t)max_launches]();
+  for (int i = 0; i < 2 * max_launches; ++i)
+    if (cudaEventCreate(&p->ev[i]) != cudaSuccess) {
+      for (int j = 0; j < i; ++j) cudaEventDestroy(p->ev[j]);
+      delete[] p->ev;
+      delete p;
+      les_set_error("event creation failed");
+      return LES_ERR_CUDA;
+    }
+  g_prof = p;
+  return LES_OK;
+}
+int les_profile_end(les_ctx* c, int* launches, double* ms, double* bytes) {
+  if (!c || !launches || !ms || !bytes) return LES_ERR_ARG;
+  ProfSession* p = g_prof;
+  if (!p || p->stream != c->stream) { les_set_error("no profiling session open on this context"); return LES_ERR_STATE; }
+  g_prof = nullptr;
+  int st = LES_OK;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) st = LES_ERR_CUDA;
+  double tot = 0.0;
+  for (int i = 0; i < p->n && !st; ++i) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, p->ev[2 * i], p->ev[2 * i + 1]) != cudaSuccess) st = LES_ERR_CUDA;
+    tot += t;
+  }
+  *launches = p->n;
+  *ms = tot;
+  *bytes = p->bytes;
+  for (int i = 0; i < 2 * p->cap; ++i) cudaEventDestroy(p->ev[i]);
+  delete[] p->ev;
+  delete p;
+  if (st) les_set_error("profiling: %s", cudaGetErrorString(cudaGetLastError()));
+  return st;
+}
 int les_rmsdiv(les_ctx* c, double* rms) {
   if (!c || !rms) return LES_ERR_ARG;
   if (c->cfg.precision == 1) op_rmsdiv_state(c, c->dscal + 1);
