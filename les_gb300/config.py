@@ -174,11 +174,14 @@ def initial_state(cfg, surface, seed=1234, noise=0.1, theta_k=300.0, theta_noise
 
 # Named workloads (one per configuration of the benchmark definition).
 def workload(name):
-    """Return (config, surface-builder) for a named workload."""
-    if name == "c1_32":
+    """Return (config, surface-builder) for a named workload:
+    neutral_32 (32^3 FP64, uniform z0 = 1e-4, no scalar), theta_striped_128
+    (128^3 FP64, theta, x-striped z0 and heat flux) and theta_striped_256_mixed
+    (256^3, the same surface, FP32-mixed)."""
+    if name == "neutral_32":
         return make_config(32), lambda c: uniform_surface(c, 1e-4, 0.0)
-    if name == "c2_128":
+    if name == "theta_striped_128":
         return make_config(128, s_flag=1), lambda c: striped_surface(c)
-    if name == "c3_256":
+    if name == "theta_striped_256_mixed":
         return make_config(256, s_flag=1, precision=1), lambda c: striped_surface(c)
     raise KeyError(name)
