@@ -75,7 +75,11 @@ struct les_ctx {
   double* gamt = nullptr;                      // Thomas gam per (row, mode), FP64
   int lag_chunk = 32;
   double* dscal = nullptr;                     // device scalars / reductions
-  double* dred = nullptr;                      // per-level reduction results
+  // per-level reduction results, 24 slots of nz+8 doubles: 0 plane sums /
+  // rmsdiv partials / model-3 Cs(z); 2..11 scaledep sums; 14 theta plane
+  // mean (mixed); 16..18 u, v, w plane means (mixed filt_da); 20..21 theta
+  // level mean and its reciprocal (calcbeta)
+  double* dred = nullptr;
   double* host_scal = nullptr;                 // pinned host mirror
   size_t bytes = 0;
   std::vector<void*> allocs;

@@ -888,13 +888,24 @@ __global__ void k_lag_prep(const double* __restrict__ u, const double* __restric
 }
 
 __device__ __forceinline__ double pow_m18(double x) { return 1.0 / sqrt(sqrt(sqrt(x))); }
+__device__ __forceinline__ float pow_m18(float x) { return 1.0f / sqrtf(sqrtf(sqrtf(x))); }
+// max(real(a), real(b)) of the reference: FP32 comparison, result widened
+__device__ __forceinline__ double fmax32r(double a, double b) { return fmax32(a, b); }
+__device__ __forceinline__ float fmax32r(float a, float b) { return a > b ? a : b; }
+template <typename R>
+__device__ __forceinline__ R smagR(R a11, R a22, R a33, R a12, R a13, R a23) {
+  return sqrt((R)2 * (a11 * a11 + a22 * a22 + a33 * a33 + (R)2 * (a12 * a12 + a13 * a13 + a23 * a23)));
+}
 
-// lagrange_Sdep.f90:268-421 from the 42 filtered planes (G: q, GG: 21+q)
-template <typename S>
+// lagrange_Sdep.f90:268-421 from the 42 filtered planes (G: q, GG: 21+q).
+// S: storage of the filtered planes; R: arithmetic (double in the FP64
+// form; float in the mixed form, where the planes are FP32 and the
+// reference truncates F_LM, F_QN and Cs^2 to FP32 itself).  The module
+// arrays stay FP64.
+template <typename S, typename R>
 __global__ void k_lag_final(const S* __restrict__ flt, double* F_LM, double* F_MM, double* F_QN,
                             double* F_NN, double* Beta, double* Cs, int ld, int nx, int ny, int nz, int jz0,
-                            int nlev, size_t np, double cst, double opftdelta, double lagran_dt, int bexp_one,
-                            double bexp) {
+                            int nlev, size_t np, R cst, R opftdelta, R lagran_dt, int bexp_one, R bexp) {
   const size_t tot = np * nlev;
   GSTRIDE(t, tot) {
     const int lc = (int)(t / np);
@@ -906,58 +917,58 @@ __global__ void k_lag_final(const S* __restrict__ flt, double* F_LM, double* F_M
     const size_t st = np * nlev;
     const S* G = flt + t;
     const S* H = flt + t + 21 * st;
-    const double ub = G[0], vb = G[st], wb = G[2 * st];
-    const double uh = H[0], vh = H[st], wh = H[2 * st];
-    const double Lq[6] = {G[3 * st] - ub * ub, G[4 * st] - ub * vb, G[5 * st] - ub * wb,
-                          G[6 * st] - vb * vb, G[7 * st] - vb * wb, G[8 * st] - wb * wb};
-    const double Qq[6] = {H[3 * st] - uh * uh, H[4 * st] - uh * vh, H[5 * st] - uh * wh,
-                          H[6 * st] - vh * vh, H[7 * st] - vh * wh, H[8 * st] - wh * wh};
-    double Sb_[6], Sh_[6], SSb[6], SSh[6];
+    const R ub = G[0], vb = G[st], wb = G[2 * st];
+    const R uh = H[0], vh = H[st], wh = H[2 * st];
+    const R Lq[6] = {(R)G[3 * st] - ub * ub, (R)G[4 * st] - ub * vb, (R)G[5 * st] - ub * wb,
+                     (R)G[6 * st] - vb * vb, (R)G[7 * st] - vb * wb, (R)G[8 * st] - wb * wb};
+    const R Qq[6] = {(R)H[3 * st] - uh * uh, (R)H[4 * st] - uh * vh, (R)H[5 * st] - uh * wh,
+                     (R)H[6 * st] - vh * vh, (R)H[7 * st] - vh * wh, (R)H[8 * st] - wh * wh};
+    R Sb_[6], Sh_[6], SSb[6], SSh[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
       Sb_[q] = G[(9 + q) * st]; Sh_[q] = H[(9 + q) * st];
       SSb[q] = G[(15 + q) * st]; SSh[q] = H[(15 + q) * st];
     }
-    const double Sb = smag(Sb_[0], Sb_[3], Sb_[5], Sb_[1], Sb_[2], Sb_[4]);
-    const double Sh = smag(Sh_[0], Sh_[3], Sh_[5], Sh_[1], Sh_[2], Sh_[4]);
-    double M[6], N[6];
+    const R Sb = smagR<R>(Sb_[0], Sb_[3], Sb_[5], Sb_[1], Sb_[2], Sb_[4]);
+    const R Sh = smagR<R>(Sh_[0], Sh_[3], Sh_[5], Sh_[1], Sh_[2], Sh_[4]);
+    R M[6], N[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      M[q] = cst * (SSb[q] - 4.0 * Sb * Sb_[q]);
-      N[q] = cst * (SSh[q] - 16.0 * Sh * Sh_[q]);
+      M[q] = cst * (SSb[q] - (R)4 * Sb * Sb_[q]);
+      N[q] = cst * (SSh[q] - (R)16 * Sh * Sh_[q]);
     }
-    const double LM = Lq[0] * M[0] + Lq[3] * M[3] + Lq[5] * M[5] + 2.0 * (Lq[1] * M[1] + Lq[2] * M[2] + Lq[4] * M[4]);
-    const double MM = M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + 2.0 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
-    const double QN = Qq[0] * N[0] + Qq[3] * N[3] + Qq[5] * N[5] + 2.0 * (Qq[1] * N[1] + Qq[2] * N[2] + Qq[4] * N[4]);
-    const double NN = N[0] * N[0] + N[3] * N[3] + N[5] * N[5] + 2.0 * (N[1] * N[1] + N[2] * N[2] + N[4] * N[4]);
-    const double e24 = (double)1e-24f;
-    double flm = F_LM[gi], fmm = F_MM[gi];
-    double Tn = fmax32(flm * fmm, e24);
+    const R LM = Lq[0] * M[0] + Lq[3] * M[3] + Lq[5] * M[5] + (R)2 * (Lq[1] * M[1] + Lq[2] * M[2] + Lq[4] * M[4]);
+    const R MM = M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + (R)2 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+    const R QN = Qq[0] * N[0] + Qq[3] * N[3] + Qq[5] * N[5] + (R)2 * (Qq[1] * N[1] + Qq[2] * N[2] + Qq[4] * N[4]);
+    const R NN = N[0] * N[0] + N[3] * N[3] + N[5] * N[5] + (R)2 * (N[1] * N[1] + N[2] * N[2] + N[4] * N[4]);
+    const R e24 = (R)1e-24f;
+    R flm = (R)F_LM[gi], fmm = (R)F_MM[gi];
+    R Tn = fmax32r(flm * fmm, e24);
     Tn = opftdelta * pow_m18(Tn);
-    Tn = fmax32(e24, Tn);
-    double dumfac = lagran_dt / Tn;
-    double epsi = dumfac / (1.0 + dumfac);
-    flm = (epsi * LM + (1.0 - epsi) * flm);
-    fmm = (epsi * MM + (1.0 - epsi) * fmm);
-    flm = fmax32(e24, flm);
-    double cs2d = fmax32(e24, flm / fmm);
+    Tn = fmax32r(e24, Tn);
+    R dumfac = lagran_dt / Tn;
+    R epsi = dumfac / ((R)1 + dumfac);
+    flm = (epsi * LM + ((R)1 - epsi) * flm);
+    fmm = (epsi * MM + ((R)1 - epsi) * fmm);
+    flm = fmax32r(e24, flm);
+    R cs2d = fmax32r(e24, flm / fmm);
     F_LM[gi] = flm; F_MM[gi] = fmm;
-    double fqn = F_QN[gi], fnn = F_NN[gi];
-    Tn = fmax32(fqn * fnn, e24);
+    R fqn = (R)F_QN[gi], fnn = (R)F_NN[gi];
+    Tn = fmax32r(fqn * fnn, e24);
     Tn = opftdelta * pow_m18(Tn);
-    Tn = fmax32(e24, Tn);
+    Tn = fmax32r(e24, Tn);
     dumfac = lagran_dt / Tn;
-    epsi = dumfac / (1.0 + dumfac);
-    fqn = (epsi * QN + (1.0 - epsi) * fqn);
-    fnn = (epsi * NN + (1.0 - epsi) * fnn);
-    fqn = fmax32(e24, fqn);
-    double cs4d = fmax32(e24, fqn / fnn);
+    epsi = dumfac / ((R)1 + dumfac);
+    fqn = (epsi * QN + ((R)1 - epsi) * fqn);
+    fnn = (epsi * NN + ((R)1 - epsi) * fnn);
+    fqn = fmax32r(e24, fqn);
+    R cs4d = fmax32r(e24, fqn / fnn);
     F_QN[gi] = fqn; F_NN[gi] = fnn;
-    double beta = bexp_one ? cs4d / cs2d : pow(cs4d / cs2d, bexp);
-    if (jz == nz) beta = 1.0;
+    R beta = bexp_one ? cs4d / cs2d : pow(cs4d / cs2d, bexp);
+    if (jz == nz) beta = (R)1;
     Beta[gi] = beta;
-    const double betaclip = fmax32(beta, 1.0 / (2.0 * 4.0));
-    Cs[gi] = fmax32(e24, cs2d / betaclip);
+    const R betaclip = fmax32r(beta, (R)1 / ((R)2 * (R)4));
+    Cs[gi] = fmax32r(e24, cs2d / betaclip);
   }
 }
 
@@ -994,7 +1005,7 @@ int op_lagrange(les_ctx* c, const double* const* S) {
     double* out[42];
     for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
     c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
-    k_lag_final<double><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+    k_lag_final<double, double><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
         c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
   }
@@ -1733,19 +1744,38 @@ __global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const do
   }
 }
 // scalars_module.f90:175-228 calcbeta from per-level plane sums
-__global__ void k_calcbeta(const double* __restrict__ theta, const double* __restrict__ sums, double* bs, int ld,
-                           int nx, int ny, int nz, double g_hat, double nxny) {
+// per level: sb = plane mean of theta, 1/sb (the divisions once per level)
+__global__ void k_calcbeta_levels(const double* __restrict__ sums, double* sbr, int nz, double nxny) {
+  for (int j = threadIdx.x; j < nz; j += blockDim.x) {
+    const double sb = sums[j] / nxny;
+    sbr[2 * j] = sb;
+    sbr[2 * j + 1] = 1.0 / sb;
+  }
+}
+__global__ void k_calcbeta(const double* __restrict__ theta, const double* __restrict__ sbr, double* bs, int ld,
+                           int nx, int ny, int nz, double g_hat) {
   const size_t np = (size_t)ld * ny;
   GSTRIDE(i, np * nz) {
     const int jz = (int)(i / np) + 1;
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
     if (jz == 1 || jz == nz || jx >= nx) { bs[i] = 0.0; continue; }
-    const double sb = sums[jz - 1] / nxny, sbm = sums[jz - 2] / nxny;
-    // (theta - sb)/sb as a product with 1/sb (one division per level, not per point)
-    const double above = (theta[i] * 1.0 - sb) * (1.0 / sb);
-    const double below = (theta[i - np] * 1.0 - sbm) * (1.0 / sbm);
+    const double sb = sbr[2 * (jz - 1)], rsb = sbr[2 * (jz - 1) + 1];
+    const double sbm = sbr[2 * (jz - 2)], rsbm = sbr[2 * (jz - 2) + 1];
+    // (theta - sb)/sb as a product with 1/sb
+    const double above = (theta[i] * 1.0 - sb) * rsb;
+    const double below = (theta[i - np] * 1.0 - sbm) * rsbm;
     bs[i] = g_hat * (above + below) * 0.5;
   }
+}
+static void calcbeta(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  double* sbr = c->dred + 20 * (size_t)(g.nz + 8);  // 2 * nz values
+  k_plane_sum<<<g.nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred); LES_COUNT_LAUNCH();
+  k_calcbeta_levels<<<1, 256, 0, c->stream>>>(c->dred, sbr, g.nz, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
+  const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
+  k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], sbr, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
+                                                    g.nz, g_hat); LES_COUNT_LAUNCH();
 }
 // scalars_module.f90:457-504 step_scalar
 __global__ void k_step_scalar(double* theta, const double* __restrict__ R, const double* __restrict__ Rf, int ld,
@@ -1806,10 +1836,7 @@ int op_theta(les_ctx* c) {
                                                                  c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
                                                                  1.0 / g.dz); LES_COUNT_LAUNCH();
   // calcbeta on theta before the update
-  k_plane_sum<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred); LES_COUNT_LAUNCH();
-  const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
-  k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], c->dred, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
-                                                    nz, g_hat, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
+  calcbeta(c);
   if (c->jt == 1 && !k.initsc)
     cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
@@ -2136,9 +2163,10 @@ static int lagrangeT(les_ctx* c) {
     S* out[42];
     for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
     c2rT<T, S>(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
-    k_lag_final<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+    k_lag_final<S, S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
-        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
+        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, (S)cst, (S)opftdelta, (S)lagran_dt, bone,
+        (S)bexp); LES_COUNT_LAUNCH();
   }
   return 0;
 }
@@ -2357,10 +2385,7 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
                                                                  c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
                                                                  1.0 / g.dz); LES_COUNT_LAUNCH();
-  k_plane_sum<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred); LES_COUNT_LAUNCH();
-  const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
-  k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], c->dred, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
-                                                    nz, g_hat, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
+  calcbeta(c);
   if (c->jt == 1 && !k.initsc)
     cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
