@@ -146,6 +146,76 @@ __device__ typename CT<T>::type* fft_smem(typename CT<T>::type* x, typename CT<T
   return x;
 }
 
+// ---- fixed-length transforms -------------------------------------------------
+// The same Stockham passes with the length known at compile time: the radix
+// sequence (4..4, 2, 3..3, as the runtime plan orders it, so the plan's
+// twiddle table serves both), the butterfly count, every index division and
+// twiddle offset become constants, and the twiddles are read from a copy of
+// the table in shared memory.  Used for the FP32 kernels at the lengths the
+// workloads use; other lengths take the runtime path above.
+constexpr int ct_nst4(int n) { return (n % 4 == 0) ? 1 + ct_nst4(n / 4) : 0; }
+constexpr int ct_pow4(int c) { return c == 0 ? 1 : 4 * ct_pow4(c - 1); }
+constexpr int ct_radix(int n, int s) {
+  return s < ct_nst4(n) ? 4 : (((n / ct_pow4(ct_nst4(n))) % 2 == 0 && s == ct_nst4(n)) ? 2 : 3);
+}
+constexpr bool ct_ok(int n) {  // n = 4^a 2^b 3^c, b <= 1 after the 4s
+  int m = n;
+  while (m % 4 == 0) m /= 4;
+  if (m % 2 == 0) m /= 2;
+  while (m % 3 == 0) m /= 3;
+  return m == 1;
+}
+
+// One pass.  COLS: element (b, i) at x[i * NB + b]; rows: x[b * N + i] for
+// nbr batches.  SIGN -1 forward, +1 inverse (conjugated twiddles).
+template <typename T, bool COLS, int N, int NB, int R, int NS, int TOFF, int SIGN, int NT>
+__device__ __forceinline__ void fft_pass_ct(const typename CT<T>::type* __restrict__ x,
+                                            typename CT<T>::type* __restrict__ y,
+                                            const typename CT<T>::type* __restrict__ tw, int nbr) {
+  typedef typename CT<T>::type C;
+  constexpr int M = N / R;
+  const int total = M * (COLS ? NB : nbr);
+  for (int t = threadIdx.x; t < total; t += NT) {
+    int b, j;
+    if (COLS) { b = t % NB; j = t / NB; }
+    else { b = t / M; j = t - b * M; }
+    const int jq = j / NS, k = j - jq * NS;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = COLS ? x[(j + r * M) * NB + b] : x[b * N + j + r * M];
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = tw[TOFF + (r - 1) * NS + k];
+        if (SIGN > 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    if constexpr (R == 4) dft4(v, SIGN);
+    else if constexpr (R == 2) dft2(v);
+    else dft3<C, T>(v, SIGN);
+    const int base = jq * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (COLS) y[(base + r * NS) * NB + b] = v[r];
+      else y[b * N + base + r * NS] = v[r];
+    }
+  }
+}
+// All passes from stage S on; returns the buffer holding the result.
+template <typename T, bool COLS, int N, int NB, int SIGN, int NT, int S = 0, int NS = 1, int TOFF = 0>
+__device__ __forceinline__ typename CT<T>::type* fft_ct(typename CT<T>::type* x, typename CT<T>::type* y,
+                                                        const typename CT<T>::type* tw, int nbr) {
+  if constexpr (NS >= N) {
+    return x;
+  } else {
+    constexpr int R = ct_radix(N, S);
+    fft_pass_ct<T, COLS, N, NB, R, NS, TOFF, SIGN, NT>(x, y, tw, nbr);
+    __syncthreads();
+    return fft_ct<T, COLS, N, NB, SIGN, NT, S + 1, NS * R, TOFF + (R - 1) * NS>(y, x, tw, nbr);
+  }
+}
+
 // ---- job descriptors --------------------------------------------------------
 constexpr int JOB_MAXF = 24;
 

@@ -1,240 +1,11 @@
 // Batched plane FFT kernels (rows_r2c, cols, rows_c2r); see fft.cuh.
-#include "fft.cuh"
+#include "fft_kernels.cuh"
 #include "les_internal.h"
 
 namespace les {
 
-template <typename T> __device__ __forceinline__ typename CT<T>::type rw(const RealPlanDev& P, int k);
-template <> __device__ __forceinline__ double2 rw<double>(const RealPlanDev& P, int k) { return __ldg(&P.w[k]); }
-template <> __device__ __forceinline__ float2 rw<float>(const RealPlanDev& P, int k) { return __ldg(&P.wf[k]); }
-
-// spectral coefficient tables in the kernel's precision
-template <typename T> struct Tab;
-template <> struct Tab<double> {
-  static __device__ __forceinline__ double kx(const ColJob& J, size_t i) { return J.kx[i]; }
-  static __device__ __forceinline__ double ky(const ColJob& J, size_t i) { return J.ky[i]; }
-  static __device__ __forceinline__ double G(const ColJob& J, size_t i) { return J.G[i]; }
-  static __device__ __forceinline__ double GG(const ColJob& J, size_t i) { return J.GG[i]; }
-};
-template <> struct Tab<float> {
-  static __device__ __forceinline__ float kx(const ColJob& J, size_t i) { return J.kxf[i]; }
-  static __device__ __forceinline__ float ky(const ColJob& J, size_t i) { return J.kyf[i]; }
-  static __device__ __forceinline__ float G(const ColJob& J, size_t i) { return J.Gf[i]; }
-  static __device__ __forceinline__ float GG(const ColJob& J, size_t i) { return J.GGf[i]; }
-};
-
-// ---------------------------------------------------------------------------
-// rows_r2c: x-transform of `rpc` rows per CTA.  grid = (ceil(ny/rpc), nlev, nfield)
-template <typename T, typename TIn>
-__global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int rpc) {
-  typedef typename CT<T>::type C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  C* A = reinterpret_cast<C*>(smraw);
-  const int m = P.nx / 2;
-  C* B = A + rpc * m;
-  const int f = blockIdx.z, lev = blockIdx.y;
-  const int row0 = blockIdx.x * rpc;
-  const int nrow = min(rpc, J.ny - row0);
-  const TIn* src = reinterpret_cast<const TIn*>(J.phys[f]) + (size_t)lev * J.pstride_phys;
-  const T s = (T)J.scale[f];
-  const T dv = (T)J.div[f];
-  const double off = J.off[f] ? J.off[f][lev] : 0.0;
-  for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
-    const int r = (int)P.dm.div((unsigned)t), k = t - r * m;
-    const TIn* row = src + (size_t)(row0 + r) * J.ld;
-    T a, b;
-    if (J.off[f]) {  // subtract in double before rounding to T
-      a = (T)((double)row[2 * k] - off);
-      b = (T)((double)row[2 * k + 1] - off);
-    } else {
-      a = (T)row[2 * k];
-      b = (T)row[2 * k + 1];
-    }
-    if (dv != (T)0) { a = a / dv; b = b / dv; }
-    A[r * m + k] = mk<T>(a * s, b * s);
-  }
-  __syncthreads();
-  C* Z = fft_smem<T, false>(A, B, nrow, m, P.c, -1);
-  C* out = reinterpret_cast<C*>(J.work[f]) + (size_t)lev * J.pstride_work;
-  for (int t = threadIdx.x; t < nrow * J.ncols; t += blockDim.x) {
-    const int r = (int)J.dnc.div((unsigned)t), k = t - r * J.ncols;
-    const C* z = Z + r * m;
-    C X;
-    if (k == 0 || k == m) {
-      const C z0 = z[0];
-      X = mk<T>(k == 0 ? z0.x + z0.y : z0.x - z0.y, (T)0);
-    } else {
-      const C a = z[k];
-      const C b = cconj(z[m - k]);
-      const C e = cscale(cadd(a, b), (T)0.5);
-      const C d = cscale(csub(a, b), (T)0.5);
-      const C o = cmulmi(d);  // d / i
-      X = cadd(e, cmul(rw<T>(P, k), o));
-    }
-    out[(size_t)(row0 + r) * J.wc + k] = X;
-  }
-}
-
-// rows_c2r: inverse x-transform.  Reads J.ncols complex columns (rest zero).
-template <typename T, typename TOut>
-__global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int rpc) {
-  typedef typename CT<T>::type C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int m = P.nx / 2;
-  C* X = reinterpret_cast<C*>(smraw);  // rpc x (m+1)
-  C* A = X + rpc * (m + 1);
-  C* B = A + rpc * m;
-  const int f = blockIdx.z, lev = blockIdx.y;
-  const int row0 = blockIdx.x * rpc;
-  const int nrow = min(rpc, J.ny - row0);
-  const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work;
-  for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
-    const int r = (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
-    C v = k < J.ncols ? in[(size_t)(row0 + r) * J.wc + k] : mk<T>((T)0, (T)0);
-    if (k == 0 || k == m) v.y = (T)0;  // halfcomplex pass ignores these imaginary parts
-    X[t] = v;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
-    const int r = (int)P.dm.div((unsigned)t), k = t - r * m;
-    const C a = X[r * (m + 1) + k];
-    const C b = cconj(X[r * (m + 1) + (m - k)]);
-    const C e = cadd(a, b);
-    const C d = cmul(csub(a, b), cconj(rw<T>(P, k)));  // x exp(+2 pi i k/nx)
-    A[t] = cadd(e, cmuli(d));
-  }
-  __syncthreads();
-  C* Z = fft_smem<T, false>(A, B, nrow, m, P.c, +1);
-  TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys;
-  const double off = J.off[f] ? J.off[f][lev] : 0.0;
-  for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
-    const int r = (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
-    TOut* row = dst + (size_t)(row0 + r) * J.ld;
-    if (k < m) {
-      const C z = Z[r * m + k];
-      if (J.off[f]) {
-        row[2 * k] = (TOut)((double)z.x + off);
-        row[2 * k + 1] = (TOut)((double)z.y + off);
-      } else {
-        row[2 * k] = (TOut)z.x;
-        row[2 * k + 1] = (TOut)z.y;
-      }
-    } else {  // padding columns ld-1:ld
-      row[2 * m] = (TOut)0;
-      row[2 * m + 1] = (TOut)0;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// cols: y-transform of TX kx columns per CTA, all fields of the job.
-// grid = (ceil(ncols/TX), nlev, nf)
-template <typename T>
-__device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT<T>::type v, int jx,
-                                                           int js, const ColJob& J) {
-  typedef typename CT<T>::type C;
-  const size_t ki = (size_t)jx + (size_t)J.lh * js;
-  switch (code) {
-    case CC_ONE: return v;
-    case CC_G: return cscale(v, Tab<T>::G(J, ki));
-    case CC_GG: return cscale(v, Tab<T>::GG(J, ki));
-    case CC_IKX: return ik(v, Tab<T>::kx(J, ki));
-    case CC_IKY: return ik(v, Tab<T>::ky(J, ki));
-    case CC_KILL: {
-      const int lhm1 = J.lh - 1;
-      if (jx == lhm1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
-      return v;
-    }
-    case CC_MASK: return Tab<T>::G(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
-    case CC_MASK4: return Tab<T>::GG(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
-    default: return mk<T>((T)0, (T)0);
-  }
-}
-
-template <typename T, int TX, typename CIn>
-__global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanDev Pout) {
-  typedef typename CT<T>::type C;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int nymax = max(J.ny_in, J.ny_out);
-  C* IN = reinterpret_cast<C*>(smraw);
-  C* A = IN + J.nin * J.ny_in * TX;
-  C* B = A + nymax * TX;
-  const int jx0 = blockIdx.x * TX;
-  const int lev = blockIdx.y;
-  for (int i = 0; i < J.nin; ++i) {
-    const CIn* src = reinterpret_cast<const CIn*>(J.in[i]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in;
-    for (int t = threadIdx.x; t < J.ny_in * TX; t += blockDim.x) {
-      const int row = t / TX, b = t - row * TX;
-      const int jx = jx0 + b;
-      C v = mk<T>((T)0, (T)0);
-      if (jx < J.ncols) {
-        const CIn x = src[(size_t)row * J.wc_in + jx];
-        v = mk<T>((T)x.x, (T)x.y);
-      }
-      IN[i * J.ny_in * TX + t] = v;
-    }
-  }
-  __syncthreads();
-  if (J.dir & DIR_FWD) {
-    for (int i = 0; i < J.nin; ++i) {
-      C* xi = IN + i * J.ny_in * TX;
-      C* r = fft_smem<T, true>(xi, A, TX, 0, Pin, -1);
-      if (r != xi) {
-        for (int t = threadIdx.x; t < J.ny_in * TX; t += blockDim.x) xi[t] = r[t];
-        __syncthreads();
-      }
-    }
-  }
-  const int nys = J.ny_small;
-  const int nyb = (J.map == MAP_SAME) ? nys : (J.map == MAP_PAD ? J.ny_out : J.ny_in);
-  for (int o = 0; o < J.nout; ++o) {
-    for (int t = threadIdx.x; t < J.ny_out * TX; t += blockDim.x) {
-      const int row = t / TX, b = t - row * TX;
-      const int jx = jx0 + b;
-      int rin, js;
-      if (J.map == MAP_SAME) { rin = row; js = row; }
-      else if (J.map == MAP_PAD) {  // padd.f90:123-133
-        if (row < nys / 2) rin = row;
-        else if (row > nyb - nys / 2) rin = row - (nyb - nys);
-        else rin = -1;
-        js = rin;
-      } else {  // unpadd.f90:143-155
-        if (row < nys / 2) rin = row;
-        else if (row == nys / 2) rin = -1;
-        else rin = row + (nyb - nys);
-        js = row;
-      }
-      C acc = mk<T>((T)0, (T)0);
-      if (rin >= 0 && jx < J.ncols) {
-        for (int i = 0; i < J.nin; ++i) {
-          const int code = J.coef[o][i];
-          if (code != CC_NONE) acc = cadd(acc, apply_coef<T>(code, IN[i * J.ny_in * TX + rin * TX + b], jx, js, J));
-        }
-      }
-      A[t] = acc;
-    }
-    __syncthreads();
-    C* r = ((J.inv_mask >> o) & 1u) ? fft_smem<T, true>(A, B, TX, 0, Pout, +1) : A;
-    C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out;
-    for (int t = threadIdx.x; t < J.ny_out * TX; t += blockDim.x) {
-      const int row = t / TX, b = t - row * TX;
-      const int jx = jx0 + b;
-      if (jx < J.ncols) dst[(size_t)row * J.wc_out + jx] = r[t];
-    }
-    __syncthreads();
-  }
-}
-
 // ---------------------------------------------------------------------------
 // host launchers
-template <typename T>
-static int rows_pc(int nx) {
-  const int m = nx / 2;
-  int r = 256 / (m / 4 > 0 ? m / 4 : 1);
-  if (r < 1) r = 1;
-  if (r > 16) r = 16;
-  return r;
-}
 
 template <typename T, typename TIn>
 int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
@@ -244,13 +15,16 @@ int launch_rows_r2c(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   RowJob JJ = J;
   JJ.dnc = FastDiv((unsigned)J.ncols);
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
-  static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
-  if (sm > sm_set) {
-    cudaFuncSetAttribute(k_rows_r2c<T, TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    sm_set = sm;
-  }
   const bool pr = g_prof && prof_mark(sizeof(T) == 8 ? PROF_ROWS64 : PROF_ROWS32, s);
-  k_rows_r2c<T, TIn><<<grid, 256, sm, s>>>(JJ, P, rpc); LES_COUNT_LAUNCH();
+  if (!launch_rows_r2c_fixed<T, TIn>(JJ, P, rpc, sm, s)) {
+    static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
+    if (sm > sm_set) {
+      cudaFuncSetAttribute(k_rows_r2c<T, TIn, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      sm_set = sm;
+    }
+    k_rows_r2c<T, TIn, 0><<<grid, 256, sm, s>>>(JJ, P, rpc);
+  }
+  LES_COUNT_LAUNCH();
   if (pr)
     prof_done(s, (double)J.nfield * J.nlev * J.ny * ((double)P.nx * sizeof(TIn) + (double)J.ncols * sizeof(C)));
   return 0;
@@ -263,13 +37,16 @@ int launch_rows_c2r(const RowJob& J, const RealPlanDev& P, cudaStream_t s) {
   const int m = P.nx / 2;
   const size_t sm = (size_t)rpc * ((m + 1) + 2 * m) * sizeof(C);
   dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
-  static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
-  if (sm > sm_set) {
-    cudaFuncSetAttribute(k_rows_c2r<T, TOut>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    sm_set = sm;
-  }
   const bool pr = g_prof && prof_mark(sizeof(T) == 8 ? PROF_ROWS64 : PROF_ROWS32, s);
-  k_rows_c2r<T, TOut><<<grid, 256, sm, s>>>(J, P, rpc); LES_COUNT_LAUNCH();
+  if (!launch_rows_c2r_fixed<T, TOut>(J, P, rpc, sm, s)) {
+    static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
+    if (sm > sm_set) {
+      cudaFuncSetAttribute(k_rows_c2r<T, TOut, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      sm_set = sm;
+    }
+    k_rows_c2r<T, TOut, 0><<<grid, 256, sm, s>>>(J, P, rpc);
+  }
+  LES_COUNT_LAUNCH();
   if (pr)
     prof_done(s, (double)J.nfield * J.nlev * J.ny * ((double)J.ncols * sizeof(C) + (double)J.ld * sizeof(TOut)));
   return 0;
@@ -281,13 +58,16 @@ static int launch_cols_tx(const ColJob& J, const FftPlanDev& Pin, const FftPlanD
   const int nymax = J.ny_in > J.ny_out ? J.ny_in : J.ny_out;
   const size_t sm = (size_t)(J.nin * J.ny_in + 2 * nymax) * TX * sizeof(C);
   dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
-  static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
-  if (sm > sm_set) {
-    cudaFuncSetAttribute(k_cols<T, TX, CIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    sm_set = sm;
-  }
   const bool pr = g_prof && prof_mark(sizeof(T) == 8 ? PROF_COLS64 : PROF_COLS32, s);
-  k_cols<T, TX, CIn><<<grid, 256, sm, s>>>(J, Pin, Pout); LES_COUNT_LAUNCH();
+  if (!launch_cols_fixed<T, TX, CIn>(J, Pin, Pout, sm, grid, s)) {
+    static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
+    if (sm > sm_set) {
+      cudaFuncSetAttribute(k_cols<T, TX, CIn, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      sm_set = sm;
+    }
+    k_cols<T, TX, CIn, 0, 0><<<grid, 256, sm, s>>>(J, Pin, Pout);
+  }
+  LES_COUNT_LAUNCH();
   if (pr) {
     const double nf = J.nf > 0 ? J.nf : 1;
     prof_done(s, nf * J.nlev * J.ncols *

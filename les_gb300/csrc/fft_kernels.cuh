@@ -1,0 +1,283 @@
+// Batched plane FFT kernel templates (rows_r2c, cols, rows_c2r), shared by
+// the runtime-length instantiations (fft_kernels.cu) and the fixed-length
+// FP32 instantiations (fft_fixed.cu).
+#pragma once
+#include "fft.cuh"
+
+namespace les {
+
+template <typename T> __device__ __forceinline__ typename CT<T>::type rw(const RealPlanDev& P, int k);
+template <> __device__ __forceinline__ double2 rw<double>(const RealPlanDev& P, int k) { return __ldg(&P.w[k]); }
+template <> __device__ __forceinline__ float2 rw<float>(const RealPlanDev& P, int k) { return __ldg(&P.wf[k]); }
+
+// spectral coefficient tables in the kernel's precision
+template <typename T> struct Tab;
+template <> struct Tab<double> {
+  static __device__ __forceinline__ double kx(const ColJob& J, size_t i) { return J.kx[i]; }
+  static __device__ __forceinline__ double ky(const ColJob& J, size_t i) { return J.ky[i]; }
+  static __device__ __forceinline__ double G(const ColJob& J, size_t i) { return J.G[i]; }
+  static __device__ __forceinline__ double GG(const ColJob& J, size_t i) { return J.GG[i]; }
+};
+template <> struct Tab<float> {
+  static __device__ __forceinline__ float kx(const ColJob& J, size_t i) { return J.kxf[i]; }
+  static __device__ __forceinline__ float ky(const ColJob& J, size_t i) { return J.kyf[i]; }
+  static __device__ __forceinline__ float G(const ColJob& J, size_t i) { return J.Gf[i]; }
+  static __device__ __forceinline__ float GG(const ColJob& J, size_t i) { return J.GGf[i]; }
+};
+
+// ---------------------------------------------------------------------------
+// rows_r2c: x-transform of `rpc` rows per CTA.  grid = (ceil(ny/rpc), nlev, nfield)
+// NF > 0: the half length m = nx/2 is NF at compile time (fixed-length
+// transform, twiddles staged in shared memory after the work buffers).
+template <typename T, typename TIn, int NF>
+__global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int rpc) {
+  typedef typename CT<T>::type C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* A = reinterpret_cast<C*>(smraw);
+  const int m = NF > 0 ? NF : P.nx / 2;
+  C* B = A + rpc * m;
+  C* tws = B + rpc * m;  // NF > 0: complex-FFT twiddles (NF) then post-processing twiddles (NF + 1)
+  if constexpr (NF > 0) {
+    for (int t = threadIdx.x; t < NF - 1; t += 256) tws[t] = TwSel<T>::get(P.c, t);
+    for (int t = threadIdx.x; t <= NF; t += 256) tws[NF + t] = rw<T>(P, t);
+  }
+  const int f = blockIdx.z, lev = blockIdx.y;
+  const int row0 = blockIdx.x * rpc;
+  const int nrow = min(rpc, J.ny - row0);
+  const TIn* src = reinterpret_cast<const TIn*>(J.phys[f]) + (size_t)lev * J.pstride_phys;
+  const T s = (T)J.scale[f];
+  const T dv = (T)J.div[f];
+  const double off = J.off[f] ? J.off[f][lev] : 0.0;
+  for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
+    const int r = NF > 0 ? t / NF : (int)P.dm.div((unsigned)t), k = t - r * m;
+    const TIn* row = src + (size_t)(row0 + r) * J.ld;
+    T a, b;
+    if (J.off[f]) {  // subtract in double before rounding to T
+      a = (T)((double)row[2 * k] - off);
+      b = (T)((double)row[2 * k + 1] - off);
+    } else {
+      a = (T)row[2 * k];
+      b = (T)row[2 * k + 1];
+    }
+    if (dv != (T)0) { a = a / dv; b = b / dv; }
+    A[r * m + k] = mk<T>(a * s, b * s);
+  }
+  __syncthreads();
+  C* Z;
+  if constexpr (NF > 0) Z = fft_ct<T, false, NF, 1, -1, 256>(A, B, tws, nrow);
+  else Z = fft_smem<T, false>(A, B, nrow, m, P.c, -1);
+  C* out = reinterpret_cast<C*>(J.work[f]) + (size_t)lev * J.pstride_work;
+  for (int t = threadIdx.x; t < nrow * J.ncols; t += blockDim.x) {
+    const int r = (int)J.dnc.div((unsigned)t), k = t - r * J.ncols;
+    const C* z = Z + r * m;
+    C X;
+    if (k == 0 || k == m) {
+      const C z0 = z[0];
+      X = mk<T>(k == 0 ? z0.x + z0.y : z0.x - z0.y, (T)0);
+    } else {
+      const C a = z[k];
+      const C b = cconj(z[m - k]);
+      const C e = cscale(cadd(a, b), (T)0.5);
+      const C d = cscale(csub(a, b), (T)0.5);
+      const C o = cmulmi(d);  // d / i
+      X = cadd(e, cmul(NF > 0 ? tws[NF + k] : rw<T>(P, k), o));
+    }
+    out[(size_t)(row0 + r) * J.wc + k] = X;
+  }
+}
+
+// rows_c2r: inverse x-transform.  Reads J.ncols complex columns (rest zero).
+template <typename T, typename TOut, int NF>
+__global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int rpc) {
+  typedef typename CT<T>::type C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int m = NF > 0 ? NF : P.nx / 2;
+  C* X = reinterpret_cast<C*>(smraw);  // rpc x (m+1)
+  C* A = X + rpc * (m + 1);
+  C* B = A + rpc * m;
+  C* tws = B + rpc * m;  // NF > 0: complex-FFT twiddles (NF) then post-processing twiddles (NF + 1)
+  if constexpr (NF > 0) {
+    for (int t = threadIdx.x; t < NF - 1; t += 256) tws[t] = TwSel<T>::get(P.c, t);
+    for (int t = threadIdx.x; t <= NF; t += 256) tws[NF + t] = rw<T>(P, t);
+  }
+  const int f = blockIdx.z, lev = blockIdx.y;
+  const int row0 = blockIdx.x * rpc;
+  const int nrow = min(rpc, J.ny - row0);
+  const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work;
+  for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
+    const int r = NF > 0 ? t / (NF + 1) : (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
+    C v = k < J.ncols ? in[(size_t)(row0 + r) * J.wc + k] : mk<T>((T)0, (T)0);
+    if (k == 0 || k == m) v.y = (T)0;  // halfcomplex pass ignores these imaginary parts
+    X[t] = v;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
+    const int r = NF > 0 ? t / NF : (int)P.dm.div((unsigned)t), k = t - r * m;
+    const C a = X[r * (m + 1) + k];
+    const C b = cconj(X[r * (m + 1) + (m - k)]);
+    const C e = cadd(a, b);
+    const C d = cmul(csub(a, b), cconj(NF > 0 ? tws[NF + k] : rw<T>(P, k)));  // x exp(+2 pi i k/nx)
+    A[t] = cadd(e, cmuli(d));
+  }
+  __syncthreads();
+  C* Z;
+  if constexpr (NF > 0) Z = fft_ct<T, false, NF, 1, +1, 256>(A, B, tws, nrow);
+  else Z = fft_smem<T, false>(A, B, nrow, m, P.c, +1);
+  TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys;
+  const double off = J.off[f] ? J.off[f][lev] : 0.0;
+  for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
+    const int r = NF > 0 ? t / (NF + 1) : (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
+    TOut* row = dst + (size_t)(row0 + r) * J.ld;
+    if (k < m) {
+      const C z = Z[r * m + k];
+      if (J.off[f]) {
+        row[2 * k] = (TOut)((double)z.x + off);
+        row[2 * k + 1] = (TOut)((double)z.y + off);
+      } else {
+        row[2 * k] = (TOut)z.x;
+        row[2 * k + 1] = (TOut)z.y;
+      }
+    } else {  // padding columns ld-1:ld
+      row[2 * m] = (TOut)0;
+      row[2 * m + 1] = (TOut)0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// cols: y-transform of TX kx columns per CTA, all fields of the job.
+// grid = (ceil(ncols/TX), nlev, nf)
+template <typename T>
+__device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT<T>::type v, int jx,
+                                                           int js, const ColJob& J) {
+  typedef typename CT<T>::type C;
+  const size_t ki = (size_t)jx + (size_t)J.lh * js;
+  switch (code) {
+    case CC_ONE: return v;
+    case CC_G: return cscale(v, Tab<T>::G(J, ki));
+    case CC_GG: return cscale(v, Tab<T>::GG(J, ki));
+    case CC_IKX: return ik(v, Tab<T>::kx(J, ki));
+    case CC_IKY: return ik(v, Tab<T>::ky(J, ki));
+    case CC_KILL: {
+      const int lhm1 = J.lh - 1;
+      if (jx == lhm1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
+      return v;
+    }
+    case CC_MASK: return Tab<T>::G(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
+    case CC_MASK4: return Tab<T>::GG(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
+    default: return mk<T>((T)0, (T)0);
+  }
+}
+
+// NIN, NOUT > 0: the input and output lengths (ny_in, ny_out) at compile time,
+// twiddles of both plans staged in shared memory after the work buffers.
+template <typename T, int TX, typename CIn, int NIN, int NOUT>
+__global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanDev Pout) {
+  typedef typename CT<T>::type C;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr bool FIX = NIN > 0 && NOUT > 0;
+  const int ny_in = FIX ? NIN : J.ny_in, ny_out = FIX ? NOUT : J.ny_out;
+  const int nymax = max(ny_in, ny_out);
+  C* IN = reinterpret_cast<C*>(smraw);
+  C* A = IN + J.nin * ny_in * TX;
+  C* B = A + nymax * TX;
+  C* twi = B + nymax * TX;  // FIX: input-length twiddles (NIN), output-length twiddles (NOUT)
+  C* two = twi + NIN;
+  if constexpr (FIX) {
+    for (int t = threadIdx.x; t < NIN - 1; t += 256) twi[t] = TwSel<T>::get(Pin, t);
+    for (int t = threadIdx.x; t < NOUT - 1; t += 256) two[t] = TwSel<T>::get(Pout, t);
+  }
+  const int jx0 = blockIdx.x * TX;
+  const int lev = blockIdx.y;
+  for (int i = 0; i < J.nin; ++i) {
+    const CIn* src = reinterpret_cast<const CIn*>(J.in[i]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in;
+    for (int t = threadIdx.x; t < ny_in * TX; t += blockDim.x) {
+      const int row = t / TX, b = t - row * TX;
+      const int jx = jx0 + b;
+      C v = mk<T>((T)0, (T)0);
+      if (jx < J.ncols) {
+        const CIn x = src[(size_t)row * J.wc_in + jx];
+        v = mk<T>((T)x.x, (T)x.y);
+      }
+      IN[i * ny_in * TX + t] = v;
+    }
+  }
+  __syncthreads();
+  if (J.dir & DIR_FWD) {
+    for (int i = 0; i < J.nin; ++i) {
+      C* xi = IN + i * ny_in * TX;
+      C* r;
+      if constexpr (FIX) r = fft_ct<T, true, NIN, TX, -1, 256>(xi, A, twi, TX);
+      else r = fft_smem<T, true>(xi, A, TX, 0, Pin, -1);
+      if (r != xi) {
+        for (int t = threadIdx.x; t < ny_in * TX; t += blockDim.x) xi[t] = r[t];
+        __syncthreads();
+      }
+    }
+  }
+  const int nys = J.ny_small;
+  const int nyb = (J.map == MAP_SAME) ? nys : (J.map == MAP_PAD ? ny_out : ny_in);
+  for (int o = 0; o < J.nout; ++o) {
+    for (int t = threadIdx.x; t < ny_out * TX; t += blockDim.x) {
+      const int row = t / TX, b = t - row * TX;
+      const int jx = jx0 + b;
+      int rin, js;
+      if (J.map == MAP_SAME) { rin = row; js = row; }
+      else if (J.map == MAP_PAD) {  // padd.f90:123-133
+        if (row < nys / 2) rin = row;
+        else if (row > nyb - nys / 2) rin = row - (nyb - nys);
+        else rin = -1;
+        js = rin;
+      } else {  // unpadd.f90:143-155
+        if (row < nys / 2) rin = row;
+        else if (row == nys / 2) rin = -1;
+        else rin = row + (nyb - nys);
+        js = row;
+      }
+      C acc = mk<T>((T)0, (T)0);
+      if (rin >= 0 && jx < J.ncols) {
+        for (int i = 0; i < J.nin; ++i) {
+          const int code = J.coef[o][i];
+          if (code != CC_NONE) acc = cadd(acc, apply_coef<T>(code, IN[i * ny_in * TX + rin * TX + b], jx, js, J));
+        }
+      }
+      A[t] = acc;
+    }
+    __syncthreads();
+    C* r = A;
+    if ((J.inv_mask >> o) & 1u) {
+      if constexpr (FIX) r = fft_ct<T, true, NOUT, TX, +1, 256>(A, B, two, TX);
+      else r = fft_smem<T, true>(A, B, TX, 0, Pout, +1);
+    }
+    C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out;
+    for (int t = threadIdx.x; t < ny_out * TX; t += blockDim.x) {
+      const int row = t / TX, b = t - row * TX;
+      const int jx = jx0 + b;
+      if (jx < J.ncols) dst[(size_t)row * J.wc_out + jx] = r[t];
+    }
+    __syncthreads();
+  }
+}
+
+
+// rows per CTA of the x-pass kernels (default when a job gives none)
+template <typename T>
+inline int rows_pc(int nx) {
+  const int m = nx / 2;
+  int r = 256 / (m / 4 > 0 ? m / 4 : 1);
+  if (r < 1) r = 1;
+  if (r > 16) r = 16;
+  return r;
+}
+
+// fixed-length launchers (fft_fixed.cu): true when the job's length has a
+// fixed-length instantiation and it was launched
+template <typename T, typename TIn>
+bool launch_rows_r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_t sm, cudaStream_t s);
+template <typename T, typename TOut>
+bool launch_rows_c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_t sm, cudaStream_t s);
+template <typename T, int TX, typename CIn>
+bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, size_t sm, dim3 grid,
+                       cudaStream_t s);
+
+}  // namespace les
