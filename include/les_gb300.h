@@ -202,6 +202,11 @@ int les_fft_c2r(les_ctx* ctx, double* planes, int nplanes, int big);
  * launches measured, their summed device time (ms) and summed algorithmic
  * bytes (each launch's inputs read once and outputs written once).  One
  * session per process at a time. */
+/* Self-test (no counterpart in the reference): compares the library's
+ * integer-pipe float<->double conversions with the hardware conversions on n
+ * generated values (random bit patterns, the float range, halfway cases);
+ * *mismatches receives the number of results whose bits differ. */
+int les_selftest_conversions(size_t n, unsigned long long seed, unsigned long long* mismatches);
 int les_profile_begin(les_ctx* ctx, int family, int max_launches);
 int les_profile_end(les_ctx* ctx, int* launches, double* ms, double* bytes);
 /* tridag_array.f90:1-109 : a,b,c (lh,ny,nz+1) real; r,u (lh,ny,nz+1) complex. */

@@ -41,6 +41,44 @@ __device__ __forceinline__ double fmax32(double a, double b) {
   return (double)(fa > fb ? fa : fb);
 }
 
+// IEEE-754 binary32 <-> binary64 conversions done with integer operations.
+// On this part a hardware float<->double conversion issues on the FP64 pipe,
+// which is as scarce as FP64 arithmetic; these run on the integer pipe for
+// the normal range and zeros, and fall back to the hardware conversion for
+// the rest (subnormals, overflow, infinities, NaN).  Results are identical
+// to the hardware's: exact widening; narrowing rounds to nearest, ties to
+// even, from the definition of the two formats.
+__device__ __forceinline__ double cvt_f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) {
+    if ((u << 1) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));  // +-0
+    return (double)f;
+  }
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+__device__ __forceinline__ float cvt_d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+  const int fe = (int)((b >> 52) & 0x7ffu) - 896;  // binary32 biased exponent
+  if (fe <= 0 || fe >= 255) {
+    if ((b << 1) == 0ull) return __uint_as_float(sgn);  // +-0
+    return (float)x;
+  }
+  const unsigned m23 = (unsigned)(b >> 29) & 0x7fffffu;
+  const unsigned rem = (unsigned)b & 0x1fffffffu;  // the 29 dropped mantissa bits
+  unsigned r = sgn | ((unsigned)fe << 23) | m23;
+  if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // a carry rounds into the exponent
+  return __uint_as_float(r);
+}
+// element conversions between a transform's precision and the storage type
+template <typename To, typename From> __device__ __forceinline__ To cvt(From v) { return (To)v; }
+template <> __device__ __forceinline__ double cvt<double, float>(float v) { return cvt_f2d(v); }
+template <> __device__ __forceinline__ float cvt<float, double>(double v) { return cvt_d2f(v); }
+
 }  // namespace les
 
 #define LES_CUDA_CHECK(expr)                                                           \

@@ -53,11 +53,11 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
     const TIn* row = src + (size_t)(row0 + r) * J.ld;
     T a, b;
     if (J.off[f]) {  // subtract in double before rounding to T
-      a = (T)((double)row[2 * k] - off);
-      b = (T)((double)row[2 * k + 1] - off);
+      a = cvt<T, double>(cvt<double, TIn>(row[2 * k]) - off);
+      b = cvt<T, double>(cvt<double, TIn>(row[2 * k + 1]) - off);
     } else {
-      a = (T)row[2 * k];
-      b = (T)row[2 * k + 1];
+      a = cvt<T, TIn>(row[2 * k]);
+      b = cvt<T, TIn>(row[2 * k + 1]);
     }
     if (dv != (T)0) { a = a / dv; b = b / dv; }
     A[r * m + k] = mk<T>(a * s, b * s);
@@ -131,11 +131,11 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
     if (k < m) {
       const C z = Z[r * m + k];
       if (J.off[f]) {
-        row[2 * k] = (TOut)((double)z.x + off);
-        row[2 * k + 1] = (TOut)((double)z.y + off);
+        row[2 * k] = cvt<TOut, double>(cvt<double, T>(z.x) + off);
+        row[2 * k + 1] = cvt<TOut, double>(cvt<double, T>(z.y) + off);
       } else {
-        row[2 * k] = (TOut)z.x;
-        row[2 * k + 1] = (TOut)z.y;
+        row[2 * k] = cvt<TOut, T>(z.x);
+        row[2 * k + 1] = cvt<TOut, T>(z.y);
       }
     } else {  // padding columns ld-1:ld
       row[2 * m] = (TOut)0;
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
       C v = mk<T>((T)0, (T)0);
       if (jx < J.ncols) {
         const CIn x = src[(size_t)row * J.wc_in + jx];
-        v = mk<T>((T)x.x, (T)x.y);
+        v = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
       }
       IN[i * ny_in * TX + t] = v;
     }

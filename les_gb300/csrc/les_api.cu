@@ -691,6 +691,17 @@ int les_profile_end(les_ctx* c, int* launches, double* ms, double* bytes) {
   if (st) les_set_error("profiling: %s", cudaGetErrorString(cudaGetLastError()));
   return st;
 }
+int les_selftest_conversions(size_t n, unsigned long long seed, unsigned long long* mismatches) {
+  if (!mismatches) return LES_ERR_ARG;
+  unsigned long long* d = nullptr;
+  LES_CUDA_CHECK(cudaMalloc(&d, sizeof(*d)));
+  cudaMemset(d, 0, sizeof(*d));
+  op_cvt_selftest(n, seed, d, 0);
+  cudaError_t e = cudaMemcpy(mismatches, d, sizeof(*d), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) { les_set_error("%s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
+  return LES_OK;
+}
 int les_rmsdiv(les_ctx* c, double* rms) {
   if (!c || !rms) return LES_ERR_ARG;
   if (c->cfg.precision == 1) op_rmsdiv_state(c, c->dscal + 1);

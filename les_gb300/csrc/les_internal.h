@@ -103,6 +103,7 @@ int op_dealias1(les_ctx* c, const double* const* in, double* const* out, int nf,
 int op_dealias2(les_ctx* c, double* const* out, const double* const* in, int nf, int nlev, double scale);
 int op_fft(les_ctx* c, double* planes, int nplanes, int big, int inverse);
 int op_rmsdiv_state(les_ctx* c, double* out_dev);
+int op_cvt_selftest(size_t n, unsigned long long seed, unsigned long long* bad_dev, cudaStream_t s);
 int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, const double* r, double* u);
 void launch_tridag_generic(const double* a, const double* b, const double* cc, const double* r, double* u,
                            double* gam, int lh, int ny, int n, int* flag, cudaStream_t s);

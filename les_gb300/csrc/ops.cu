@@ -11,6 +11,40 @@ typedef double2 C2;
 struct Ptr6 { const double* p[6]; };
 
 // ---------------------------------------------------------------------------
+// self-test of the integer-pipe conversions against the hardware ones:
+// n doubles built from SplitMix64 bit patterns (all exponents, both signs),
+// halfway cases between adjacent floats, and every float rebuilt from the
+// same patterns; counts results whose bits differ
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+__global__ void k_cvt_selftest(size_t n, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long nb = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long r = splitmix64(seed + i);
+    double x = __longlong_as_double((long long)r);
+    if ((i & 3) == 1) {  // a double near the float range
+      x = __longlong_as_double((long long)((r & 0x800fffffffffffffull) | ((0x380ull + (r >> 40) % 0x100ull) << 52)));
+    } else if ((i & 3) == 2) {  // exactly halfway between two floats
+      const unsigned fb = (unsigned)(r >> 32) & 0x7f7fffffu;
+      const double lo = (double)__uint_as_float(fb), hi = (double)__uint_as_float(fb + 1u);
+      x = 0.5 * (lo + hi);
+    }
+    if (__float_as_uint(cvt_d2f(x)) != __float_as_uint((float)x) && !(x != x)) ++nb;
+    const float f = __uint_as_float((unsigned)r);
+    if (__double_as_longlong(cvt_f2d(f)) != __double_as_longlong((double)f) && !(f != f)) ++nb;
+  }
+  if (nb) atomicAdd(bad, nb);
+}
+int op_cvt_selftest(size_t n, unsigned long long seed, unsigned long long* bad_dev, cudaStream_t s) {
+  k_cvt_selftest<<<152 * 4, 256, 0, s>>>(n, seed, bad_dev); LES_COUNT_LAUNCH();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // launch helpers
 static inline dim3 grid1(size_t n, int bs = 256) {
   size_t b = (n + bs - 1) / bs;
