@@ -74,10 +74,72 @@ __device__ __forceinline__ float cvt_d2f(double x) {
   if (rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u))) r += 1u;  // a carry rounds into the exponent
   return __uint_as_float(r);
 }
+// Float-float number ("double-single"): value hi + lo with |lo| <= ulp(hi)/2,
+// about 48 significant bits, computed on the FP32 pipe with error-free
+// transformations (Knuth's two-sum for additions, products through fused
+// multiply-add, Dekker).  The mixed form runs its projection-path transforms
+// in it: FP64-like accuracy at FP32-pipe throughput.
+struct __align__(8) dfloat {
+  float hi, lo;
+  __host__ __device__ dfloat() {}
+  __host__ __device__ constexpr dfloat(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr dfloat(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ constexpr dfloat(int i) : hi((float)i), lo(0.f) {}
+};
+struct __align__(16) dcomplex {
+  dfloat x, y;
+};
+template <> struct CT<dfloat> { typedef dcomplex type; };
+__device__ __forceinline__ dfloat df_quick(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return dfloat(s, b - (s - a));
+}
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
+  return df_quick(s, e);
+}
+__device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_quick(p, e);
+}
+__device__ __forceinline__ dfloat operator/(dfloat a, dfloat b) {
+  const float q1 = a.hi / b.hi;
+  const dfloat r = a - b * dfloat(q1, 0.f);
+  const float q2 = r.hi / b.hi;
+  return df_quick(q1, q2);
+}
+__device__ __forceinline__ dfloat& operator+=(dfloat& a, dfloat b) { return a = a + b; }
+__device__ __forceinline__ dfloat& operator-=(dfloat& a, dfloat b) { return a = a - b; }
+__device__ __forceinline__ dfloat& operator*=(dfloat& a, dfloat b) { return a = a * b; }
+__device__ __forceinline__ bool operator!=(dfloat a, dfloat b) { return a.hi != b.hi || a.lo != b.lo; }
+
 // element conversions between a transform's precision and the storage type
 template <typename To, typename From> __device__ __forceinline__ To cvt(From v) { return (To)v; }
 template <> __device__ __forceinline__ double cvt<double, float>(float v) { return cvt_f2d(v); }
 template <> __device__ __forceinline__ float cvt<float, double>(double v) { return cvt_d2f(v); }
+template <> __device__ __forceinline__ dfloat cvt<dfloat, double>(double v) {
+  const float h = cvt_d2f(v);
+  return dfloat(h, cvt_d2f(v - cvt_f2d(h)));
+}
+template <> __device__ __forceinline__ double cvt<double, dfloat>(dfloat v) { return cvt_f2d(v.hi) + cvt_f2d(v.lo); }
+template <> __device__ __forceinline__ dfloat cvt<dfloat, dfloat>(dfloat v) { return v; }
+__device__ __forceinline__ double2 to_d2(double2 v) { return v; }
+__device__ __forceinline__ double2 to_d2(dcomplex v) { return make_double2(cvt<double>(v.x), cvt<double>(v.y)); }
+template <typename CO> __device__ __forceinline__ CO from_d2(double2 v);
+template <> __device__ __forceinline__ double2 from_d2<double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ dcomplex from_d2<dcomplex>(double2 v) {
+  dcomplex r;
+  r.x = cvt<dfloat>(v.x);
+  r.y = cvt<dfloat>(v.y);
+  return r;
+}
 
 }  // namespace les
 

@@ -41,6 +41,7 @@ struct FftPlanDev {
   const double2* tw;  // forward twiddles, per stage (R-1)*Ns entries
   const float2* twf;  // the same rounded to FP32 (FP32 kernels read these: a
                       // double->float conversion runs on GB300's FP64 pipe)
+  const float4* twd;  // the same as float-float pairs (re.hi, re.lo, im.hi, im.lo)
 };
 
 struct RealPlanDev {
@@ -49,6 +50,7 @@ struct RealPlanDev {
   FastDiv dm, dm1;    // m and m + 1
   const double2* w;   // exp(-2 pi i k / nx), k = 0..m
   const float2* wf;   // the same in FP32
+  const float4* wd;   // the same as float-float pairs
 };
 
 // ---- radix butterflies -----------------------------------------------------
@@ -84,6 +86,15 @@ template <> struct TwSel<double> {
 };
 template <> struct TwSel<float> {
   static __device__ __forceinline__ float2 get(const FftPlanDev& P, int idx) { return __ldg(&P.twf[idx]); }
+};
+template <> struct TwSel<dfloat> {
+  static __device__ __forceinline__ dcomplex get(const FftPlanDev& P, int idx) {
+    const float4 v = __ldg(&P.twd[idx]);
+    dcomplex r;
+    r.x = dfloat(v.x, v.y);
+    r.y = dfloat(v.z, v.w);
+    return r;
+  }
 };
 template <typename T> __device__ __forceinline__ typename CT<T>::type twid(const FftPlanDev& P, int idx, int sign) {
   typename CT<T>::type w = TwSel<T>::get(P, idx);
@@ -278,6 +289,8 @@ struct ColJob {
   const float* kyf;
   const float* Gf;
   const float* GGf;
+  const float2* kxd;      // kx, ky as float-float pairs (float-float kernels)
+  const float2* kyd;
   int lh;                 // row stride of the (lh,ny) tables
   int tx;                 // kx columns per CTA (0: default for the precision)
 };

@@ -1,6 +1,6 @@
-// Fixed-length FP32 instantiations of the transform kernels.  The launchers
-// return false for lengths (or precisions) without an instantiation; the
-// caller then launches the runtime-length kernel.
+// Fixed-length FP32 and float-float instantiations of the transform
+// kernels.  The launchers return false for lengths (or precisions) without an
+// instantiation; the caller then launches the runtime-length kernel.
 #include "fft_kernels.cuh"
 #include "les_internal.h"
 
@@ -51,7 +51,7 @@ void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, 
 
 template <typename T, typename TIn>
 bool launch_rows_r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_t sm, cudaStream_t s) {
-  if constexpr (sizeof(T) == 8) {
+  if constexpr (std::is_same<T, double>::value) {
     return false;
   } else {
     switch (P.nx / 2) {
@@ -65,7 +65,7 @@ bool launch_rows_r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_
 }
 template <typename T, typename TOut>
 bool launch_rows_c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_t sm, cudaStream_t s) {
-  if constexpr (sizeof(T) == 8) {
+  if constexpr (std::is_same<T, double>::value) {
     return false;
   } else {
     switch (P.nx / 2) {
@@ -85,13 +85,14 @@ bool launch_rows_c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_
   X(144, 96) X(128, 128) X(128, 192) X(192, 128) X(192, 192) X(192, 288) X(288, 192) \
   X(256, 256) X(256, 384) X(384, 256)
 
+// float-float y pass (the projection path): same-length pairs, kx tile 4
+#define LES_COL_SAME(X) X(32, 32) X(64, 64) X(96, 96) X(128, 128) X(192, 192) X(256, 256)
+
 template <typename T, int TX, typename CIn>
 bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, size_t sm, dim3 grid,
                        cudaStream_t s) {
-  if constexpr (sizeof(T) == 8 || TX != 8 || !std::is_same<CIn, float2>::value) {
-    return false;
-  } else {
-    const int key = J.ny_in * 10000 + J.ny_out;
+  const int key = J.ny_in * 10000 + J.ny_out;
+  if constexpr (std::is_same<T, float>::value && TX == 8 && std::is_same<CIn, float2>::value) {
     switch (key) {
 #define LES_CASE(a, b) \
   case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
@@ -99,6 +100,16 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
 #undef LES_CASE
       default: return false;
     }
+  } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 && std::is_same<CIn, dcomplex>::value) {
+    switch (key) {
+#define LES_CASE(a, b) \
+  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
+      LES_COL_SAME(LES_CASE)
+#undef LES_CASE
+      default: return false;
+    }
+  } else {
+    return false;
   }
 }
 
@@ -108,6 +119,8 @@ template bool launch_rows_r2c_fixed<float, double>(const RowJob&, const RealPlan
 template bool launch_rows_c2r_fixed<double, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 template bool launch_rows_c2r_fixed<float, float>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 template bool launch_rows_c2r_fixed<float, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
+template bool launch_rows_r2c_fixed<dfloat, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
+template bool launch_rows_c2r_fixed<dfloat, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 #define LES_INST_COLS(T, TX, CIn)                                                                   \
   template bool launch_cols_fixed<T, TX, CIn>(const ColJob&, const FftPlanDev&, const FftPlanDev&, \
                                               size_t, dim3, cudaStream_t);
@@ -120,5 +133,8 @@ LES_INST_COLS(float, 16, float2)
 LES_INST_COLS(float, 4, double2)
 LES_INST_COLS(float, 8, double2)
 LES_INST_COLS(float, 16, double2)
+LES_INST_COLS(dfloat, 2, dcomplex)
+LES_INST_COLS(dfloat, 4, dcomplex)
+LES_INST_COLS(dfloat, 8, dcomplex)
 
 }  // namespace les

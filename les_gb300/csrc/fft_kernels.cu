@@ -76,8 +76,8 @@ static int launch_cols_tx(const ColJob& J, const FftPlanDev& Pin, const FftPlanD
   return 0;
 }
 
-// kx tile width: FP64 {2, 4, 8} (default 4), FP32 {4, 8, 16} (default 8);
-// the autotuner picks one per grid size
+// kx tile width: 8-byte reals (FP64, float-float) {2, 4, 8} (default 4),
+// FP32 {4, 8, 16} (default 8); the autotuner picks one per grid size
 template <typename T, typename CIn>
 int launch_cols(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s) {
   if (sizeof(T) == 8) {
@@ -104,5 +104,8 @@ template int launch_rows_c2r<float, float>(const RowJob&, const RealPlanDev&, cu
 template int launch_rows_c2r<float, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_cols<float, float2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 template int launch_cols<float, double2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
+template int launch_rows_r2c<dfloat, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
+template int launch_rows_c2r<dfloat, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
+template int launch_cols<dfloat, dcomplex>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 
 }  // namespace les

@@ -9,6 +9,13 @@ namespace les {
 template <typename T> __device__ __forceinline__ typename CT<T>::type rw(const RealPlanDev& P, int k);
 template <> __device__ __forceinline__ double2 rw<double>(const RealPlanDev& P, int k) { return __ldg(&P.w[k]); }
 template <> __device__ __forceinline__ float2 rw<float>(const RealPlanDev& P, int k) { return __ldg(&P.wf[k]); }
+template <> __device__ __forceinline__ dcomplex rw<dfloat>(const RealPlanDev& P, int k) {
+  const float4 v = __ldg(&P.wd[k]);
+  dcomplex r;
+  r.x = dfloat(v.x, v.y);
+  r.y = dfloat(v.z, v.w);
+  return r;
+}
 
 // spectral coefficient tables in the kernel's precision
 template <typename T> struct Tab;
@@ -17,6 +24,12 @@ template <> struct Tab<double> {
   static __device__ __forceinline__ double ky(const ColJob& J, size_t i) { return J.ky[i]; }
   static __device__ __forceinline__ double G(const ColJob& J, size_t i) { return J.G[i]; }
   static __device__ __forceinline__ double GG(const ColJob& J, size_t i) { return J.GG[i]; }
+};
+template <> struct Tab<dfloat> {
+  static __device__ __forceinline__ dfloat kx(const ColJob& J, size_t i) { const float2 v = __ldg(&J.kxd[i]); return dfloat(v.x, v.y); }
+  static __device__ __forceinline__ dfloat ky(const ColJob& J, size_t i) { const float2 v = __ldg(&J.kyd[i]); return dfloat(v.x, v.y); }
+  static __device__ __forceinline__ dfloat G(const ColJob& J, size_t i) { return cvt<dfloat>(J.G[i]); }
+  static __device__ __forceinline__ dfloat GG(const ColJob& J, size_t i) { return cvt<dfloat>(J.GG[i]); }
 };
 template <> struct Tab<float> {
   static __device__ __forceinline__ float kx(const ColJob& J, size_t i) { return J.kxf[i]; }

@@ -46,6 +46,12 @@ static bool is_2a3b(int n) {
   return n == 1;
 }
 
+// (re, im) as float-float pairs: hi = the nearest float, lo = the nearest
+// float to the remainder
+static float4 ff_pair(long double re, long double im) {
+  const float rh = (float)re, ih = (float)im;
+  return make_float4(rh, (float)(re - (long double)rh), ih, (float)(im - (long double)ih));
+}
 // Stockham plan for a complex FFT of length n: radix 4, then 2, then 3.
 // Twiddles exp(-2 pi i k r / (Ns R)) are evaluated in long double.
 static int make_plan(les_ctx* c, int n, HostPlan& hp) {
@@ -59,6 +65,7 @@ static int make_plan(les_ctx* c, int n, HostPlan& hp) {
   if (m != 1 || P.nst > FFT_MAX_STAGES) { les_set_error("FFT size %d is not 2^a 3^b", n); return LES_ERR_UNSUPPORTED; }
   if (n > 4096) { les_set_error("FFT size %d exceeds 4096", n); return LES_ERR_UNSUPPORTED; }
   std::vector<double2> tw;
+  std::vector<float4> twd;
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.radix[s];
@@ -69,11 +76,20 @@ static int make_plan(les_ctx* c, int n, HostPlan& hp) {
       for (int k = 0; k < Ns; ++k) {
         const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)((long long)k * r) /
                                 (long double)((long long)Ns * R);
-        tw.push_back(make_double2((double)cosl(ang), (double)sinl(ang)));
+        const long double cr = cosl(ang), ci = sinl(ang);
+        tw.push_back(make_double2((double)cr, (double)ci));
+        twd.push_back(ff_pair(cr, ci));
       }
     Ns *= R;
   }
-  if (tw.empty()) tw.push_back(make_double2(1.0, 0.0));
+  if (tw.empty()) {
+    tw.push_back(make_double2(1.0, 0.0));
+    twd.push_back(ff_pair(1.0L, 0.0L));
+  }
+  LES_CUDA_CHECK(cudaMalloc(&hp.devd, twd.size() * sizeof(float4)));
+  c->allocs.push_back(hp.devd);
+  LES_CUDA_CHECK(cudaMemcpy(hp.devd, twd.data(), twd.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  P.twd = static_cast<const float4*>(hp.devd);
   LES_CUDA_CHECK(cudaMalloc(&hp.dev, tw.size() * sizeof(double2)));
   c->allocs.push_back(hp.dev);
   LES_CUDA_CHECK(cudaMemcpy(hp.dev, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
@@ -96,10 +112,16 @@ static int make_real_plan(les_ctx* c, int nx, HostRealPlan& rp) {
   rp.r.dm = FastDiv((unsigned)m);
   rp.r.dm1 = FastDiv((unsigned)(m + 1));
   std::vector<double2> w(m + 1);
+  std::vector<float4> wd(m + 1);
   for (int k = 0; k <= m; ++k) {
     const long double ang = -2.0L * 3.14159265358979323846264338327950288L * k / (long double)nx;
     w[k] = make_double2((double)cosl(ang), (double)sinl(ang));
+    wd[k] = ff_pair(cosl(ang), sinl(ang));
   }
+  LES_CUDA_CHECK(cudaMalloc(&rp.devd, wd.size() * sizeof(float4)));
+  c->allocs.push_back(rp.devd);
+  LES_CUDA_CHECK(cudaMemcpy(rp.devd, wd.data(), wd.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  rp.r.wd = static_cast<const float4*>(rp.devd);
   LES_CUDA_CHECK(cudaMalloc(&rp.dev, w.size() * sizeof(double2)));
   c->allocs.push_back(rp.dev);
   LES_CUDA_CHECK(cudaMemcpy(rp.dev, w.data(), w.size() * sizeof(double2), cudaMemcpyHostToDevice));
@@ -163,7 +185,8 @@ static Sizes sizes_of(const Grid& g) {
   // saved spectra, wall-plane spectra, Thomas tables, reductions, wavenumber
   // and filter tables (FP64 + FP32)
   s.aux = 4 * nz * C * sizeof(double2) + 4 * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double) +
-          (24 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float);
+          (24 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float) +
+          2 * C * sizeof(float2);
   return s;
 }
 
@@ -284,6 +307,13 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     cudaMemcpy(c->Gf, a.data(), tf, cudaMemcpyHostToDevice);
     for (size_t i = 0; i < a.size(); ++i) a[i] = (float)GG[i];
     cudaMemcpy(c->GGf, a.data(), tf, cudaMemcpyHostToDevice);
+    const size_t td = kx.size() * sizeof(float2);
+    if ((st = dalloc(c, (void**)&c->kxd, td)) || (st = dalloc(c, (void**)&c->kyd, td))) return fail(st);
+    std::vector<float2> p2(kx.size());
+    for (size_t i = 0; i < p2.size(); ++i) p2[i] = make_float2((float)kx[i], (float)(kx[i] - (double)(float)kx[i]));
+    cudaMemcpy(c->kxd, p2.data(), td, cudaMemcpyHostToDevice);
+    for (size_t i = 0; i < p2.size(); ++i) p2[i] = make_float2((float)ky[i], (float)(ky[i] - (double)(float)ky[i]));
+    cudaMemcpy(c->kyd, p2.data(), td, cudaMemcpyHostToDevice);
   }
   if ((st = make_real_plan(c, g.nx, c->rx)) || (st = make_real_plan(c, g.nx2, c->rxb)) ||
       (st = make_plan(c, g.ny, c->cy)) || (st = make_plan(c, g.ny2, c->cyb)))

@@ -20,11 +20,13 @@ struct HostPlan {
   FftPlanDev c{};
   double2* dev = nullptr;
   float2* devf = nullptr;
+  void* devd = nullptr;  // float-float twiddles (float4)
 };
 struct HostRealPlan {
   RealPlanDev r{};
   double2* dev = nullptr;
   float2* devf = nullptr;
+  void* devd = nullptr;
 };
 
 // Grid constants computed once on the host in the reference's expression
@@ -59,6 +61,7 @@ struct les_ctx {
   // spectral tables (lh,ny)
   double *kx = nullptr, *ky = nullptr, *G = nullptr, *GG = nullptr;
   float *kxf = nullptr, *kyf = nullptr, *Gf = nullptr, *GGf = nullptr;
+  float2 *kxd = nullptr, *kyd = nullptr;  // kx, ky as float-float pairs
   // FFT plans
   les::HostRealPlan rx, rxb;   // real x-transforms of length nx, nx2
   les::HostPlan cy, cyb;       // complex y-transforms of length ny, ny2

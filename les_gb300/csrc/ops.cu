@@ -131,6 +131,7 @@ static ColJob coljob(les_ctx* c, int map, int dir, int nlev) {
   J.ny_small = g.ny;
   J.kx = c->kx; J.ky = c->ky; J.G = c->G; J.GG = c->GG; J.lh = g.lh;
   J.kxf = c->kxf; J.kyf = c->kyf; J.Gf = c->Gf; J.GGf = c->GGf;
+  J.kxd = c->kxd; J.kyd = c->kyd;
   if (map == MAP_SAME) {
     J.ny_in = J.ny_out = g.ny; J.ncols = g.lh; J.wc_in = J.wc_out = g.lh;
   } else if (map == MAP_PAD) {
@@ -1503,9 +1504,12 @@ int op_project(les_ctx* c) {
 // press_stag_array.f90:192-264 + tridag_array.f90:1-109: one thread per
 // wavenumber pair solves its z-tridiagonal (Thomas), building the RHS rows
 // from the spectra H on the fly.  Spectra are (level, ny, lh) complex.
-__global__ void __launch_bounds__(128) k_tridiag(const C2* __restrict__ Hx, const C2* __restrict__ Hy,
-                                                 const C2* __restrict__ Hz, const C2* __restrict__ bot,
-                                                 const C2* __restrict__ top, C2* P, const double* __restrict__ ibet,
+// HC, PC: storage of the spectra H and p-hat (double2, or float-float in the
+// mixed form); the solve itself is FP64.
+template <typename HC, typename PC>
+__global__ void __launch_bounds__(128) k_tridiag(const HC* __restrict__ Hx, const HC* __restrict__ Hy,
+                                                 const HC* __restrict__ Hz, const C2* __restrict__ bot,
+                                                 const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
                                                  const double* __restrict__ gam, const double* __restrict__ kx,
                                                  const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
   const int nk = lh * ny;
@@ -1514,20 +1518,20 @@ __global__ void __launch_bounds__(128) k_tridiag(const C2* __restrict__ Hx, cons
   const int jx = t % lh, jy = t / lh;
   const size_t NK = (size_t)nk;
   if (jy == ny / 2 || jx == lh - 1) {  // Nyquist modes: zeroed (press_stag_array.f90:263-264)
-    for (int j = 0; j <= nz; ++j) P[(size_t)j * NK + t] = make_double2(0.0, 0.0);
+    for (int j = 0; j <= nz; ++j) P[(size_t)j * NK + t] = from_d2<PC>(make_double2(0.0, 0.0));
     return;
   }
   if (t == 0) {  // kx = ky = 0 : direct integration (:238-247)
     C2 p = make_double2(0.0, 0.0);
-    P[0] = p;
+    P[0] = from_d2<PC>(p);
     const C2 b = bot[0];
     C2 p1; p1.x = p.x - dz * b.x; p1.y = p.y - dz * b.y;
-    P[NK] = p1;
+    P[NK] = from_d2<PC>(p1);
     p = p1;
     for (int jz = 2; jz <= nz; ++jz) {
-      const C2 h = (jz <= nz - 1) ? Hz[(size_t)(jz - 1) * NK] : make_double2(0.0, 0.0);
+      const C2 h = (jz <= nz - 1) ? to_d2(Hz[(size_t)(jz - 1) * NK]) : make_double2(0.0, 0.0);
       p.x = p.x + h.x * dz; p.y = p.y + h.y * dz;
-      P[(size_t)jz * NK] = p;
+      P[(size_t)jz * NK] = from_d2<PC>(p);
     }
     return;
   }
@@ -1537,16 +1541,16 @@ __global__ void __launch_bounds__(128) k_tridiag(const C2* __restrict__ Hx, cons
   // row 1: a = BOGUS, b = -1, c = 1, r = -dz * bottomw ; u = r / bet
   const C2 r1 = bot[t];
   C2 up; up.x = (-dz * r1.x) * ibet[t]; up.y = (-dz * r1.y) * ibet[t];
-  P[t] = up;
-  C2 hz0 = Hz[t];
+  P[t] = from_d2<PC>(up);
+  C2 hz0 = to_d2(Hz[t]);
   for (int j = 2; j <= n; ++j) {
     double a;
     C2 r;
     if (j <= nz) {
       a = idz2;
-      const C2 hx = Hx[(size_t)(j - 2) * NK + t];
-      const C2 hy = Hy[(size_t)(j - 2) * NK + t];
-      const C2 hz1 = (j <= nz - 1) ? Hz[(size_t)(j - 1) * NK + t] : make_double2(0.0, 0.0);
+      const C2 hx = to_d2(Hx[(size_t)(j - 2) * NK + t]);
+      const C2 hy = to_d2(Hy[(size_t)(j - 2) * NK + t]);
+      const C2 hz1 = (j <= nz - 1) ? to_d2(Hz[(size_t)(j - 1) * NK + t]) : make_double2(0.0, 0.0);
       const double sr = k_x * hx.x + k_y * hy.x;
       const double si = k_x * hx.y + k_y * hy.y;
       r.x = -si + (hz1.x - hz0.x) / dz;
@@ -1559,14 +1563,14 @@ __global__ void __launch_bounds__(128) k_tridiag(const C2* __restrict__ Hx, cons
     }
     const double ib = ibet[(size_t)(j - 1) * NK + t];
     C2 u; u.x = (r.x - a * up.x) * ib; u.y = (r.y - a * up.y) * ib;
-    P[(size_t)(j - 1) * NK + t] = u;
+    P[(size_t)(j - 1) * NK + t] = from_d2<PC>(u);
     up = u;
   }
   for (int j = n - 1; j >= 1; --j) {
     const double gm = gam[(size_t)j * NK + t];
-    C2 u = P[(size_t)(j - 1) * NK + t];
+    C2 u = to_d2(P[(size_t)(j - 1) * NK + t]);
     u.x = u.x - gm * up.x; u.y = u.y - gm * up.y;
-    P[(size_t)(j - 1) * NK + t] = u;
+    P[(size_t)(j - 1) * NK + t] = from_d2<PC>(u);
     up = u;
   }
 }
@@ -1609,7 +1613,12 @@ int thomas_tables(les_ctx* c) {
   return 0;
 }
 
-int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
+// T: transform precision of the three field transforms and the spectra H,
+// p-hat (double: FP64 form and the per-routine entry; dfloat: mixed form).
+// The wall planes' spectra and the tridiagonal solve are FP64 in both.
+template <typename T>
+static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
+  typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const int nz = g.nz;
@@ -1618,16 +1627,16 @@ int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
   const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
   const double sc3[3] = {cst / 1.5, cst / 1.5, cst / 1.5};
   const double dv3[3] = {k.dt, k.dt, k.dt};
-  r2c(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
-  C2* H = (C2*)c->wsP;                        // 3*(nz-1)*C
-  C2* BT = H + (size_t)3 * (nz - 1) * g.C;   // bottom, top
-  C2* P = BT + 2 * g.C;                       // (nz+1)*C
+  r2cT<T, double>(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
+  CX* H = (CX*)c->wsP;                                       // 3*(nz-1)*C
+  C2* BT = reinterpret_cast<C2*>(H + (size_t)3 * (nz - 1) * g.C);  // bottom, top
+  CX* P = reinterpret_cast<CX*>(BT + 2 * g.C);              // (nz+1)*C
   ColJob J = coljob(c, MAP_SAME, DIR_FWD, nz - 1);
   J.nin = 1; J.nout = 1; J.nf = 3;
   J.in[0] = c->wsA; J.fs_in = (long)(nz - 1) * g.C;
   J.out[0] = H; J.fs_out = (long)(nz - 1) * g.C;
   J.coef[0][0] = CC_KILL;
-  cols(c, J);
+  colsT<T, CX>(c, J);
   // bottomw, topw from divtz(1), divtz(nz) scaled by 1/(nx*ny)
   {
     const double* bi[2] = {c->f[LES_DIVTZ], c->f[LES_DIVTZ] + (size_t)(nz - 1) * g.nplane};
@@ -1640,31 +1649,32 @@ int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) {
     K.coef[0][0] = CC_KILL;
     cols(c, K);
   }
-  k_tridiag<<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(H, H + (size_t)(nz - 1) * g.C,
-                                                              H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P,
-                                                              c->ibet, c->gamt, c->kx, c->ky, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
+  k_tridiag<CX, CX><<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
+      H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky,
+      g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
     K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
-    cols(c, K);
+    colsT<T, CX>(c, K);
     ColJob L = coljob(c, MAP_SAME, DIR_INV, nz - 1);
     L.nin = 1; L.nout = 3; L.in[0] = P + g.C;
-    L.out[0] = (C2*)c->wsB + g.C;
-    L.out[1] = (C2*)c->wsB + g.C + (size_t)(nz - 1) * g.C;
-    L.out[2] = (C2*)c->wsB + g.C + (size_t)2 * (nz - 1) * g.C;
+    L.out[0] = (CX*)c->wsB + g.C;
+    L.out[1] = (CX*)c->wsB + g.C + (size_t)(nz - 1) * g.C;
+    L.out[2] = (CX*)c->wsB + g.C + (size_t)2 * (nz - 1) * g.C;
     L.coef[0][0] = CC_ONE; L.coef[1][0] = CC_IKX; L.coef[2][0] = CC_IKY;
-    cols(c, L);
+    colsT<T, CX>(c, L);
     double* o0 = p;
-    c2r(c, 1, 1, c->wsB, &o0, (long)g.nplane, false, g.lh);
+    c2rT<T, double>(c, 1, 1, c->wsB, &o0, (long)g.nplane, false, g.lh);
     double* o1[3] = {p + g.nplane, dpdx, dpdy};
-    c2r(c, 3, nz - 1, (C2*)c->wsB + g.C, o1, (long)g.nplane, false, g.lh);
+    c2rT<T, double>(c, 3, nz - 1, (CX*)c->wsB + g.C, o1, (long)g.nplane, false, g.lh);
   }
   fill(c, dpdx + (size_t)(nz - 1) * g.nplane, g.nplane, LES_BOGUS);
   fill(c, dpdy + (size_t)(nz - 1) * g.nplane, g.nplane, LES_BOGUS);
   fill(c, p + (size_t)nz * g.nplane, g.nplane, LES_BOGUS);
   return 0;
 }
+int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy) { return pressT<double>(c, p, dpdx, dpdy); }
 
 // tridag_array.f90:1-109 with caller-supplied coefficients (per-routine entry)
 __global__ void k_tridag_generic(const double* a, const double* b, const double* cc, const C2* r, C2* u,
@@ -2506,7 +2516,7 @@ static int stepT(les_ctx* c) {
       c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
       c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL], nv,
       g.nplane, k.dt, k.s_flag, (c->jt == 1 && !k.initu) ? 1 : 0); LES_COUNT_LAUNCH();
-  op_press(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
+  pressT<typename std::conditional<MX, dfloat, double>::type>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
   k_dpdz_project<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
                                                         c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX],
                                                         c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
