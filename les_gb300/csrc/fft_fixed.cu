@@ -85,6 +85,9 @@ bool launch_rows_c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_
   X(144, 96) X(128, 128) X(128, 192) X(192, 128) X(192, 192) X(192, 288) X(288, 192) \
   X(256, 256) X(256, 384) X(384, 256)
 
+// padding from the saved spectra: (ny, 3ny/2)
+#define LES_COL_PAD(X) X(32, 48) X(64, 96) X(96, 144) X(128, 192) X(192, 288) X(256, 384)
+
 // float-float y pass (the projection path): same-length pairs, kx tile 4
 #define LES_COL_SAME(X) X(32, 32) X(64, 64) X(96, 96) X(128, 128) X(192, 192) X(256, 256)
 
@@ -97,6 +100,14 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
 #define LES_CASE(a, b) \
   case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
       LES_COL_PAIRS(LES_CASE)
+#undef LES_CASE
+      default: return false;
+    }
+  } else if constexpr (std::is_same<T, float>::value && TX == 8 && std::is_same<CIn, double2>::value) {
+    switch (key) {  // FP32 transforms of the saved FP64-layout spectra (padding to the 3/2 grid)
+#define LES_CASE(a, b) \
+  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
+      LES_COL_PAD(LES_CASE)
 #undef LES_CASE
       default: return false;
     }

@@ -242,7 +242,8 @@ size_t les_estimate_device_bytes(const les_config* cfg) {
   Grid g;
   grid_of(*cfg, g);
   Sizes s = sizes_of(g);
-  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + (1u << 20);
+  const size_t ffd = cfg->precision == 1 ? 2 * (size_t)(g.nz + 1) * g.C * sizeof(float2) : 0;
+  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + ffd + (1u << 20);
 }
 
 int les_ctx_create(const les_config* cfg, les_ctx** out) {
@@ -330,6 +331,10 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
       (st = dalloc(c, (void**)&c->wspec, 4 * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->gamt, (size_t)(g.nz + 1) * g.C * sizeof(double))))
+    return fail(st);
+  if (k.precision == 1 &&
+      ((st = dalloc(c, (void**)&c->ibetd, (size_t)(g.nz + 1) * g.C * sizeof(float2))) ||
+       (st = dalloc(c, (void**)&c->gamtd, (size_t)(g.nz + 1) * g.C * sizeof(float2)))))
     return fail(st);
   if ((st = thomas_tables(c))) return fail(st);
   c->wsA_bytes = s.wsA; c->wsB_bytes = s.wsB; c->wsP_bytes = s.wsP;

@@ -341,6 +341,66 @@ __global__ void k_nyq_part(const double* f0, const double* f1, const double* f2,
     S.spart[pl * nch + ch] = t;
   }
 }
+// The same partial sums with whole rows per warp: 4 warps, warp w takes rows
+// w, w+4, .. of the chunk; lane l the column pairs l + 32k, k < KP.  Each
+// lane sums its pairs before one warp reduction per row, and the four warps'
+// column partials are combined once per chunk (fewer FP64 adds per element
+// than one warp reduction per row across all the columns).
+template <int KP>
+__global__ void __launch_bounds__(128) k_nyq_part_rows(const double* f0, const double* f1, const double* f2,
+                                                      NyqScratch S, int ld, int nx, int ny, long ps, int nlev,
+                                                      int nch) {
+  __shared__ double ws[NYQ_ROWS], wd[NYQ_ROWS];
+  extern __shared__ double2 wacc[];  // [4][np]
+  const int ch = blockIdx.x, lev = blockIdx.y, fld = blockIdx.z;
+  const double* f = (fld == 0 ? f0 : fld == 1 ? f1 : f2) + (size_t)lev * ps;
+  const int np = nx / 2, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int y0 = ch * NYQ_ROWS, nr = min(NYQ_ROWS, ny - y0);
+  double2 acc[KP];
+#pragma unroll
+  for (int k = 0; k < KP; ++k) acc[k] = make_double2(0.0, 0.0);
+  for (int r = wid; r < nr; r += 4) {
+    const int y = y0 + r;
+    const double2* row = reinterpret_cast<const double2*>(f + (size_t)y * ld);
+    double se = 0.0, so = 0.0;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+      const int p = lane + 32 * k;
+      if (p < np) {
+        const double2 v = row[p];
+        if (y & 1) { acc[k].x -= v.x; acc[k].y -= v.y; }
+        else { acc[k].x += v.x; acc[k].y += v.y; }
+        se += v.x;
+        so += v.y;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      se += __shfl_xor_sync(0xffffffffu, se, o);
+      so += __shfl_xor_sync(0xffffffffu, so, o);
+    }
+    if (lane == 0) { ws[r] = se + so; wd[r] = se - so; }
+  }
+#pragma unroll
+  for (int k = 0; k < KP; ++k) {
+    const int p = lane + 32 * k;
+    if (p < np) wacc[wid * np + p] = acc[k];
+  }
+  __syncthreads();
+  const size_t pl = (size_t)fld * nlev + lev;
+  double2* ap = reinterpret_cast<double2*>(S.apart + (pl * nch + ch) * nx);
+  for (int p = threadIdx.x; p < np; p += 128) {
+    double2 a = wacc[p];
+    for (int w = 1; w < 4; ++w) { a.x += wacc[w * np + p].x; a.y += wacc[w * np + p].y; }
+    ap[p] = a;
+  }
+  if (threadIdx.x < nr) S.b[pl * ny + y0 + threadIdx.x] = wd[threadIdx.x] / (double)nx;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int r = 0; r < nr; ++r) t += ws[r];
+    S.spart[pl * nch + ch] = t;
+  }
+}
 __global__ void __launch_bounds__(256) k_nyq_comb(NyqScratch S, double* mean, int mstride, int nx, int ny, int nlev,
                                                   int nch) {
   __shared__ double red[256];
@@ -410,7 +470,16 @@ static void nyq_kill(les_ctx* c, double* const* f, int nf, int nlev, double* mea
   const int K = (np + bt - 1) / bt;  // <= 16: nx <= 8192 (the transforms allow less)
   const dim3 grid(nch, nlev, nf);
   const long ps = (long)g.nplane;
-  switch (K) {
+  const int KP = (np + 31) / 32;
+  const size_t smr = (size_t)4 * np * sizeof(double2);
+  if (KP <= 8) {
+    switch (KP) {
+      case 1: k_nyq_part_rows<1><<<grid, 128, smr, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+      case 2: k_nyq_part_rows<2><<<grid, 128, smr, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+      case 3: case 4: k_nyq_part_rows<4><<<grid, 128, smr, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+      default: k_nyq_part_rows<8><<<grid, 128, smr, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
+    }
+  } else switch (K) {
     case 1: k_nyq_part<1><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
     case 2: k_nyq_part<2><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
     case 3: case 4: k_nyq_part<4><<<grid, bt, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nch); break;
@@ -876,6 +945,94 @@ __global__ void k_interpolag(const double* __restrict__ ul, const double* __rest
     oNN[i] = LAGI(FNN);
 #undef LAGI
   }
+}
+// Mixed form: the same back-trajectory interpolation in FP32, gathering from
+// FP32 copies of F_LM, F_MM, F_QN, F_NN (the reference itself truncates
+// F_LM and F_QN to FP32), results widened to the FP64 state.  The
+// displacement -u_lag dt / dx is formed without the cs factor that the
+// reference divides out and multiplies back (:260-262); u_lag is the sum
+// over the cs_count steps, so the displacement is -u_lag dt / dx.
+__global__ void k_to_f32x4(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                           const double* __restrict__ d, float* o, size_t n) {
+  GSTRIDE(i, n) {
+    o[i] = cvt_d2f(a[i]);
+    o[i + n] = cvt_d2f(b[i]);
+    o[i + 2 * n] = cvt_d2f(c[i]);
+    o[i + 3 * n] = cvt_d2f(d[i]);
+  }
+}
+__global__ void k_interpolag32(const double* __restrict__ ul, const double* __restrict__ vl,
+                               const double* __restrict__ wl, const float* __restrict__ F4, double* oLM,
+                               double* oMM, double* oQN, double* oNN, int ld, int nx, int ny, int nz, size_t nf,
+                               float sx, float sy, float sz) {
+  const size_t np = (size_t)ld * ny;
+  const float* FLM = F4;
+  const float* FMM = F4 + nf;
+  const float* FQN = F4 + 2 * nf;
+  const float* FNN = F4 + 3 * nf;
+  GSTRIDE(t, (size_t)nx * ny * nz) {
+    const int jx = (int)(t % nx);
+    const int jy = (int)((t / nx) % ny);
+    const int jz = (int)(t / ((size_t)nx * ny)) + 1;
+    const size_t i = (size_t)jx + (size_t)ld * jy + np * (jz - 1);
+    float ua = cvt_d2f(ul[i]), va = cvt_d2f(vl[i]);
+    if (jz >= 2) {
+      ua = 0.5f * (ua + cvt_d2f(ul[i - np]));
+      va = 0.5f * (va + cvt_d2f(vl[i - np]));
+    }
+    const float xp = -ua * sx, yp = -va * sy;
+    float zp;
+    {
+      const size_t i2 = (size_t)jx + (size_t)ld * jy + np;
+      if (jz <= 2) {
+        float z2 = -cvt_d2f(wl[i2]) * sz;
+        z2 = z2 + fminf(z2, 0.0f);
+        z2 = fminf(1.0f, z2);
+        z2 = fmaxf(-1.0f, z2);
+        zp = z2;
+      } else {
+        zp = -cvt_d2f(wl[i]) * sz;
+      }
+    }
+    const int addx = (xp < 0.0f) ? -1 : 1;
+    const int addy = (yp < 0.0f) ? -1 : 1;
+    const int addz = (zp < 0.0f) ? -1 : 1;
+    int xa = jx + addx; if (xa < 0) xa = nx - 1; if (xa >= nx) xa = 0;
+    int ya = jy + addy; if (ya < 0) ya = ny - 1; if (ya >= ny) ya = 0;
+    int za = (jz - 1) + addz; if (za < 0) za = 0; if (za >= nz) za = nz - 1;
+    const float cx = fabsf(xp), cy = fabsf(yp), cz = fabsf(zp);
+    const float fx = 1.0f - cx, fy = 1.0f - cy, fz = 1.0f - cz;
+    const size_t z0 = np * (jz - 1), z1 = np * za;
+    const size_t a00 = (size_t)jx + (size_t)ld * jy, a01 = (size_t)jx + (size_t)ld * ya;
+    const size_t a10 = (size_t)xa + (size_t)ld * jy, a11 = (size_t)xa + (size_t)ld * ya;
+#define LAGI(F)                                                                      \
+  (fx * fy * (F[a00 + z0] * fz + F[a00 + z1] * cz) + fx * cy * (F[a01 + z0] * fz + F[a01 + z1] * cz) + \
+   cx * fy * (F[a10 + z0] * fz + F[a10 + z1] * cz) + cx * cy * (F[a11 + z0] * fz + F[a11 + z1] * cz))
+    oLM[i] = cvt_f2d(LAGI(FLM));
+    oMM[i] = cvt_f2d(LAGI(FMM));
+    oQN[i] = cvt_f2d(LAGI(FQN));
+    oNN[i] = cvt_f2d(LAGI(FNN));
+#undef LAGI
+  }
+}
+static int op_interpolag32(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  double* Fn[4];
+  for (int q = 0; q < 4; ++q) Fn[q] = c->spare + (size_t)q * g.nfield;
+  float* F4 = reinterpret_cast<float*>(c->tmp);  // 4 * nfield floats, free until the filtering below
+  k_to_f32x4<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN],
+                                                     F4, g.nfield); LES_COUNT_LAUNCH();
+  // u_lag holds the sum over cs_count steps: (sum / cs_count) * (dt * cs_count) / dx
+  k_interpolag32<<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
+      c->f[LES_U_LAG], c->f[LES_V_LAG], c->f[LES_W_LAG], F4, Fn[0], Fn[1], Fn[2], Fn[3], g.ld, g.nx, g.ny, g.nz,
+      g.nfield, (float)(k.dt / g.dx), (float)(k.dt / g.dy), (float)(k.dt / g.dz)); LES_COUNT_LAUNCH();
+  for (int q = 0; q < 4; ++q)
+    cudaMemcpyAsync(c->f[LES_F_LM + q], Fn[q], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemsetAsync(c->f[LES_U_LAG], 0, g.nfield * sizeof(double), c->stream);
+  cudaMemsetAsync(c->f[LES_V_LAG], 0, g.nfield * sizeof(double), c->stream);
+  cudaMemsetAsync(c->f[LES_W_LAG], 0, g.nfield * sizeof(double), c->stream);
+  return 0;
 }
 int op_interpolag(les_ctx* c) {
   const Grid& g = c->g;
@@ -1505,16 +1662,14 @@ int op_project(les_ctx* c) {
 // wavenumber pair solves its z-tridiagonal (Thomas), building the RHS rows
 // from the spectra H on the fly.  Spectra are (level, ny, lh) complex.
 // HC, PC: storage of the spectra H and p-hat (double2, or float-float in the
-// mixed form); the solve itself is FP64.
+// mixed form); the solve itself is FP64.  One mode t.
 template <typename HC, typename PC>
-__global__ void __launch_bounds__(128) k_tridiag(const HC* __restrict__ Hx, const HC* __restrict__ Hy,
+__device__ __forceinline__ void tridiag_mode(int t, const HC* __restrict__ Hx, const HC* __restrict__ Hy,
                                                  const HC* __restrict__ Hz, const C2* __restrict__ bot,
                                                  const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
                                                  const double* __restrict__ gam, const double* __restrict__ kx,
                                                  const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
   const int nk = lh * ny;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nk) return;
   const int jx = t % lh, jy = t / lh;
   const size_t NK = (size_t)nk;
   if (jy == ny / 2 || jx == lh - 1) {  // Nyquist modes: zeroed (press_stag_array.f90:263-264)
@@ -1575,6 +1730,94 @@ __global__ void __launch_bounds__(128) k_tridiag(const HC* __restrict__ Hx, cons
   }
 }
 
+template <typename HC, typename PC>
+__global__ void __launch_bounds__(128) k_tridiag(const HC* __restrict__ Hx, const HC* __restrict__ Hy,
+                                                 const HC* __restrict__ Hz, const C2* __restrict__ bot,
+                                                 const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
+                                                 const double* __restrict__ gam, const double* __restrict__ kx,
+                                                 const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= lh * ny) return;
+  tridiag_mode<HC, PC>(t, Hx, Hy, Hz, bot, top, P, ibet, gam, kx, ky, lh, ny, nz, dz);
+}
+
+// Mixed form: the kx = ky = 0 mode, the Nyquist modes and the lowest-|k|
+// modes (|kx|, |ky| <= 2 in wavenumber index: the near-singular Neumann
+// systems) are solved in FP64 as above; every other mode runs the same
+// Thomas recurrences in float-float arithmetic on the FP32 pipe, with the
+// coefficient tables split into float-float pairs.
+__device__ __forceinline__ dfloat dfl(float2 v) { return dfloat(v.x, v.y); }
+__device__ __forceinline__ dcomplex dcx(C2 v) { dcomplex r; r.x = cvt<dfloat>(v.x); r.y = cvt<dfloat>(v.y); return r; }
+__global__ void __launch_bounds__(128) k_tridiag_mixed(const dcomplex* __restrict__ Hx, const dcomplex* __restrict__ Hy,
+                                                       const dcomplex* __restrict__ Hz, const C2* __restrict__ bot,
+                                                       const C2* __restrict__ top, dcomplex* P,
+                                                       const double* __restrict__ ibet, const double* __restrict__ gam,
+                                                       const float2* __restrict__ ibetd, const float2* __restrict__ gamd,
+                                                       const double* __restrict__ kx, const double* __restrict__ ky,
+                                                       const float2* __restrict__ kxd, const float2* __restrict__ kyd,
+                                                       int lh, int ny, int nz, double dz, float2 dzd, float2 idzd,
+                                                       float2 idz2d) {
+  // two threads per mode: part 0 the real, part 1 the imaginary part of p-hat
+  // (a, b, c are real, so the two recurrences are independent)
+  const int nk = lh * ny;
+  const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = g2 >> 1, part = g2 & 1;
+  if (t >= nk) return;
+  const int jx = t % lh, jy = t / lh;
+  const int jyi = jy <= ny / 2 ? jy : ny - jy;
+  if (t == 0 || jy == ny / 2 || jx == lh - 1 || (jx <= 2 && jyi <= 2)) {
+    if (part == 0) tridiag_mode<dcomplex, dcomplex>(t, Hx, Hy, Hz, bot, top, P, ibet, gam, kx, ky, lh, ny, nz, dz);
+    return;
+  }
+  const size_t NK = (size_t)nk;
+  // this part's p-hat component reads: Re p <- Im(kx Hx + ky Hy), Re Hz;
+  // Im p <- Re(kx Hx + ky Hy), Im Hz
+  const dfloat* hxc = reinterpret_cast<const dfloat*>(Hx) + (part == 0 ? 1 : 0);
+  const dfloat* hyc = reinterpret_cast<const dfloat*>(Hy) + (part == 0 ? 1 : 0);
+  const dfloat* hzc = reinterpret_cast<const dfloat*>(Hz) + part;
+  dfloat* pc = reinterpret_cast<dfloat*>(P) + part;
+  const dfloat sgn = part == 0 ? dfloat(-1.f, 0.f) : dfloat(1.f, 0.f);  // r.x = dHz - si ; r.y = sr + dHz
+  const dfloat k_x = dfl(kxd[t]), k_y = dfl(kyd[t]);
+  const dfloat ddz = dfl(dzd), idz = dfl(idzd), idz2 = dfl(idz2d);
+  const int n = nz + 1;
+  const C2 b1 = bot[t];
+  const dfloat r1 = cvt<dfloat>(part == 0 ? b1.x : b1.y);
+  dfloat up = (-(ddz * r1)) * dfl(ibetd[t]);
+  pc[2 * (size_t)t] = up;
+  dfloat hz0 = hzc[2 * (size_t)t];
+  // level j's inputs, loaded one level ahead
+  dfloat hxn = hxc[2 * (size_t)t], hyn = hyc[2 * (size_t)t];
+  dfloat hzn = nz - 1 >= 2 ? hzc[2 * (NK + t)] : dfloat(0.f, 0.f);
+  for (int j = 2; j <= n; ++j) {
+    const dfloat ib = dfl(ibetd[(size_t)(j - 1) * NK + t]);
+    dfloat a, r;
+    if (j <= nz) {
+      const dfloat hx = hxn, hy = hyn, hz1 = (j <= nz - 1) ? hzn : dfloat(0.f, 0.f);
+      if (j + 1 <= nz) {
+        hxn = hxc[2 * ((size_t)(j - 1) * NK + t)];
+        hyn = hyc[2 * ((size_t)(j - 1) * NK + t)];
+        if (j <= nz - 2) hzn = hzc[2 * ((size_t)j * NK + t)];
+      }
+      a = idz2;
+      r = (hz1 - hz0) * idz + sgn * (k_x * hx + k_y * hy);
+      hz0 = hz1;
+    } else {
+      a = dfloat(-1.f, 0.f);
+      const C2 tp = top[t];
+      r = -(cvt<dfloat>(part == 0 ? tp.x : tp.y) * ddz);
+    }
+    const dfloat u = (r - a * up) * ib;
+    pc[2 * ((size_t)(j - 1) * NK + t)] = u;
+    up = u;
+  }
+  for (int j = n - 1; j >= 1; --j) {
+    const dfloat gm = dfl(gamd[(size_t)j * NK + t]);
+    const dfloat u = pc[2 * ((size_t)(j - 1) * NK + t)] - gm * up;
+    pc[2 * ((size_t)(j - 1) * NK + t)] = u;
+    up = u;
+  }
+}
+
 // Thomas coefficients of press_stag_array.f90:144-210 for every (kx,ky):
 // they depend on k^2 and dz only, so they are formed once per context
 // (tridag_array.f90:41-69 recurrences, reciprocal of bet stored).
@@ -1610,6 +1853,13 @@ int thomas_tables(les_ctx* c) {
   }
   LES_CUDA_CHECK(cudaMemcpy(c->ibet, ib.data(), ib.size() * sizeof(double), cudaMemcpyHostToDevice));
   LES_CUDA_CHECK(cudaMemcpy(c->gamt, gm.data(), gm.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (c->ibetd) {  // float-float copies for the mixed form
+    std::vector<float2> f2(ib.size());
+    for (size_t i = 0; i < ib.size(); ++i) f2[i] = make_float2((float)ib[i], (float)(ib[i] - (double)(float)ib[i]));
+    LES_CUDA_CHECK(cudaMemcpy(c->ibetd, f2.data(), f2.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < gm.size(); ++i) f2[i] = make_float2((float)gm[i], (float)(gm[i] - (double)(float)gm[i]));
+    LES_CUDA_CHECK(cudaMemcpy(c->gamtd, f2.data(), f2.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  }
   return 0;
 }
 
@@ -1649,9 +1899,17 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
     K.coef[0][0] = CC_KILL;
     cols(c, K);
   }
-  k_tridiag<CX, CX><<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
-      H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky,
-      g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
+  if constexpr (std::is_same<T, dfloat>::value) {
+    auto ff = [](double v) { return make_float2((float)v, (float)(v - (double)(float)v)); };
+    k_tridiag_mixed<<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
+        H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->ibetd,
+        c->gamtd, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz, ff(g.dz), ff(1.0 / g.dz),
+        ff(1.0 / (g.dz * g.dz))); LES_COUNT_LAUNCH();
+  } else {
+    k_tridiag<CX, CX><<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
+        H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx,
+        c->ky, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
+  }
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
@@ -2156,7 +2414,8 @@ static int lagrangeT(les_ctx* c) {
   typedef typename PX<MX>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
-  op_interpolag(c);
+  if (MX) op_interpolag32(c);
+  else op_interpolag(c);
   const double delta = g.delta;
   const double cst = 2.0 * (delta * delta);
   const double opftdelta = 1.5 * delta;
