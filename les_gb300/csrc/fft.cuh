@@ -42,6 +42,8 @@ struct FftPlanDev {
   const float2* twf;  // the same rounded to FP32 (FP32 kernels read these: a
                       // double->float conversion runs on GB300's FP64 pipe)
   const float4* twd;  // the same as float-float pairs (re.hi, re.lo, im.hi, im.lo)
+  const float2* unitf;  // exp(-2 pi i m / n), m < n, in FP32 (fixed-length kernels)
+  const float4* unitd;  // the same as float-float pairs
 };
 
 struct RealPlanDev {
@@ -158,33 +160,97 @@ __device__ typename CT<T>::type* fft_smem(typename CT<T>::type* x, typename CT<T
 }
 
 // ---- fixed-length transforms -------------------------------------------------
-// The same Stockham passes with the length known at compile time: the radix
-// sequence (4..4, 2, 3..3, as the runtime plan orders it, so the plan's
-// twiddle table serves both), the butterfly count, every index division and
-// twiddle offset become constants, and the twiddles are read from a copy of
-// the table in shared memory.  Used for the FP32 kernels at the lengths the
+// Stockham passes with the length known at compile time: every index,
+// butterfly count and twiddle offset is a constant; the butterflies are
+// radix 16 (4 x 4), 8 (4 x 2), 4, 2 and 3, evaluated in registers, so a
+// 256-point transform takes two passes through shared memory; twiddles come
+// from a unit-circle table exp(-2 pi i m / N), m < N, staged in shared
+// memory.  Shared-memory element i of a transform sits at sk(i) = i + i/16,
+// which spreads the stride-16 accesses of the radix-16 passes over the
+// banks.  Used for the FP32 and float-float kernels at the lengths the
 // workloads use; other lengths take the runtime path above.
-constexpr int ct_nst4(int n) { return (n % 4 == 0) ? 1 + ct_nst4(n / 4) : 0; }
-constexpr int ct_pow4(int c) { return c == 0 ? 1 : 4 * ct_pow4(c - 1); }
-constexpr int ct_radix(int n, int s) {
-  return s < ct_nst4(n) ? 4 : (((n / ct_pow4(ct_nst4(n))) % 2 == 0 && s == ct_nst4(n)) ? 2 : 3);
+__host__ __device__ constexpr int sk(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int skn(int n) { return n + (n >> 4); }  // padded length
+constexpr int ct2_radix(int n, int s, int maxr) {
+  int m = n, st = 0;
+  while (m > 1) {
+    int r = 0;
+    if (maxr >= 16 && m % 16 == 0) r = 16;
+    else if (maxr >= 8 && m % 8 == 0) r = 8;
+    else if (m % 4 == 0) r = 4;
+    else if (m % 2 == 0) r = 2;
+    else if (m % 3 == 0) r = 3;
+    else return 0;
+    if (st == s) return r;
+    m /= r;
+    ++st;
+  }
+  return 0;
 }
-constexpr bool ct_ok(int n) {  // n = 4^a 2^b 3^c, b <= 1 after the 4s
-  int m = n;
-  while (m % 4 == 0) m /= 4;
-  if (m % 2 == 0) m /= 2;
-  while (m % 3 == 0) m /= 3;
-  return m == 1;
+constexpr bool ct_ok(int n) { return ct2_radix(n, 0, 4) != 0 || n == 1; }
+
+template <typename C, typename T> __device__ __forceinline__ C cmulc(C a, T wr, T wi) {
+  C r;
+  r.x = a.x * wr - a.y * wi;
+  r.y = a.x * wi + a.y * wr;
+  return r;
+}
+// natural-order DFT8 (r = 2a + b: two DFT4 over a, twiddles W8^c, DFT2 over b)
+template <typename C, typename T> __device__ __forceinline__ void dft8(C* v, int sign) {
+  const T c2 = (T)0.70710678118654752440084436210485;
+  const T sc2 = sign < 0 ? -c2 : c2;
+  C e[4] = {v[0], v[2], v[4], v[6]};
+  C o[4] = {v[1], v[3], v[5], v[7]};
+  dft4(e, sign);
+  dft4(o, sign);
+  o[1] = cmulc(o[1], c2, sc2);
+  o[2] = sign < 0 ? cmulmi(o[2]) : cmuli(o[2]);
+  o[3] = cmulc(o[3], -c2, sc2);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    v[c] = cadd(e[c], o[c]);
+    v[c + 4] = csub(e[c], o[c]);
+  }
+}
+// natural-order DFT16 (r = 4a + b: four DFT4 over a, twiddles W16^(bc),
+// four DFT4 over b; output q = c + 4d)
+template <typename C, typename T> __device__ __forceinline__ void dft16(C* v, int sign) {
+  const T c1 = (T)0.92387953251128675612818318939679;  // cos(pi/8)
+  const T s1 = (T)0.38268343236508977172845998403040;  // sin(pi/8)
+  const T c2 = (T)0.70710678118654752440084436210485;  // cos(pi/4)
+  const T gs1 = sign < 0 ? -s1 : s1, gc1 = sign < 0 ? -c1 : c1, gc2 = sign < 0 ? -c2 : c2;
+  C t[4][4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    t[b][0] = v[b]; t[b][1] = v[b + 4]; t[b][2] = v[b + 8]; t[b][3] = v[b + 12];
+    dft4(t[b], sign);
+  }
+  t[1][1] = cmulc(t[1][1], c1, gs1);   // W16^1
+  t[1][2] = cmulc(t[1][2], c2, gc2);   // W16^2
+  t[1][3] = cmulc(t[1][3], s1, gc1);   // W16^3
+  t[2][1] = cmulc(t[2][1], c2, gc2);   // W16^2
+  t[2][2] = sign < 0 ? cmulmi(t[2][2]) : cmuli(t[2][2]);  // W16^4
+  t[2][3] = cmulc(t[2][3], -c2, gc2);  // W16^6
+  t[3][1] = cmulc(t[3][1], s1, gc1);   // W16^3
+  t[3][2] = cmulc(t[3][2], -c2, gc2);  // W16^6
+  t[3][3] = cmulc(t[3][3], -c1, -gs1);  // W16^9
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    C u[4] = {t[0][c], t[1][c], t[2][c], t[3][c]};
+    dft4(u, sign);
+    v[c] = u[0]; v[c + 4] = u[1]; v[c + 8] = u[2]; v[c + 12] = u[3];
+  }
 }
 
-// One pass.  COLS: element (b, i) at x[i * NB + b]; rows: x[b * N + i] for
-// nbr batches.  SIGN -1 forward, +1 inverse (conjugated twiddles).
-template <typename T, bool COLS, int N, int NB, int R, int NS, int TOFF, int SIGN, int NT>
+// One pass.  COLS: element (b, i) at x[sk(i) * NB + b]; rows: x[b * skn(N)
+// + sk(i)] for nbr batches.  SIGN -1 forward, +1 inverse (conjugated
+// twiddles); tw: the unit-circle table of length N.
+template <typename T, bool COLS, int N, int NB, int R, int NS, int SIGN, int NT>
 __device__ __forceinline__ void fft_pass_ct(const typename CT<T>::type* __restrict__ x,
                                             typename CT<T>::type* __restrict__ y,
                                             const typename CT<T>::type* __restrict__ tw, int nbr) {
   typedef typename CT<T>::type C;
-  constexpr int M = N / R;
+  constexpr int M = N / R, PN = skn(N), TS = N / (NS * R);
   const int total = M * (COLS ? NB : nbr);
   for (int t = threadIdx.x; t < total; t += NT) {
     int b, j;
@@ -193,39 +259,65 @@ __device__ __forceinline__ void fft_pass_ct(const typename CT<T>::type* __restri
     const int jq = j / NS, k = j - jq * NS;
     C v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = COLS ? x[(j + r * M) * NB + b] : x[b * N + j + r * M];
+    for (int r = 0; r < R; ++r) v[r] = COLS ? x[sk(j + r * M) * NB + b] : x[b * PN + sk(j + r * M)];
     if (NS > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        C w = tw[TOFF + (r - 1) * NS + k];
+        C w = tw[r * k * TS];
         if (SIGN > 0) w.y = -w.y;
         v[r] = cmul(v[r], w);
       }
     }
-    if constexpr (R == 4) dft4(v, SIGN);
+    if constexpr (R == 16) dft16<C, T>(v, SIGN);
+    else if constexpr (R == 8) dft8<C, T>(v, SIGN);
+    else if constexpr (R == 4) dft4(v, SIGN);
     else if constexpr (R == 2) dft2(v);
     else dft3<C, T>(v, SIGN);
     const int base = jq * NS * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      if (COLS) y[(base + r * NS) * NB + b] = v[r];
-      else y[b * N + base + r * NS] = v[r];
+      if (COLS) y[sk(base + r * NS) * NB + b] = v[r];
+      else y[b * PN + sk(base + r * NS)] = v[r];
     }
   }
 }
 // All passes from stage S on; returns the buffer holding the result.
-template <typename T, bool COLS, int N, int NB, int SIGN, int NT, int S = 0, int NS = 1, int TOFF = 0>
+// MAXR: largest radix.
+template <typename T, bool COLS, int N, int NB, int SIGN, int NT, int MAXR, int S = 0, int NS = 1>
 __device__ __forceinline__ typename CT<T>::type* fft_ct(typename CT<T>::type* x, typename CT<T>::type* y,
                                                         const typename CT<T>::type* tw, int nbr) {
   if constexpr (NS >= N) {
     return x;
   } else {
-    constexpr int R = ct_radix(N, S);
-    fft_pass_ct<T, COLS, N, NB, R, NS, TOFF, SIGN, NT>(x, y, tw, nbr);
+    constexpr int R = ct2_radix(N, S, MAXR);
+    fft_pass_ct<T, COLS, N, NB, R, NS, SIGN, NT>(x, y, tw, nbr);
     __syncthreads();
-    return fft_ct<T, COLS, N, NB, SIGN, NT, S + 1, NS * R, TOFF + (R - 1) * NS>(y, x, tw, nbr);
+    return fft_ct<T, COLS, N, NB, SIGN, NT, MAXR, S + 1, NS * R>(y, x, tw, nbr);
   }
 }
+// largest radix of the y pass (FP32: 16; float-float: 4, register use);
+// the x pass uses radix <= 4 (its many short rows keep more blocks resident)
+template <typename T> struct CtMaxR { static constexpr int v = 16; };
+template <> struct CtMaxR<dfloat> { static constexpr int v = 4; };
+constexpr int CT_MAXR_ROWS = 4;
+
+// unit-circle table entry m of a plan, in the kernel's precision
+template <typename T> struct UnitSel;
+template <> struct UnitSel<float> {
+  static __device__ __forceinline__ float2 get(const FftPlanDev& P, int m) { return __ldg(&P.unitf[m]); }
+};
+template <> struct UnitSel<dfloat> {
+  static __device__ __forceinline__ dcomplex get(const FftPlanDev& P, int m) {
+    const float4 v = __ldg(&P.unitd[m]);
+    dcomplex r;
+    r.x = dfloat(v.x, v.y);
+    r.y = dfloat(v.z, v.w);
+    return r;
+  }
+};
+template <> struct UnitSel<double> {  // not used by the fixed-length kernels
+  static __device__ __forceinline__ double2 get(const FftPlanDev& P, int m) { return make_double2(0.0, 0.0); }
+};
 
 // ---- job descriptors --------------------------------------------------------
 constexpr int JOB_MAXF = 24;

@@ -16,28 +16,28 @@ void raise_smem(K kernel, size_t sm, size_t& set) {
 }
 
 template <typename T, typename TIn, int NF>
-void r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_t sm, cudaStream_t s) {
+void r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  const size_t smf = sm + (size_t)(2 * NF + 1) * sizeof(C);
+  const size_t smf = ((size_t)2 * rpc * skn(NF) + 2 * NF + 1) * sizeof(C);
   static size_t set = 48 * 1024;
   raise_smem(k_rows_r2c<T, TIn, NF>, smf, set);
   const dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
   k_rows_r2c<T, TIn, NF><<<grid, 256, smf, s>>>(J, P, rpc);
 }
 template <typename T, typename TOut, int NF>
-void c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_t sm, cudaStream_t s) {
+void c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  const size_t smf = sm + (size_t)(2 * NF + 1) * sizeof(C);
+  const size_t smf = ((size_t)rpc * (NF + 1) + (size_t)2 * rpc * skn(NF) + 2 * NF + 1) * sizeof(C);
   static size_t set = 48 * 1024;
   raise_smem(k_rows_c2r<T, TOut, NF>, smf, set);
   const dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
   k_rows_c2r<T, TOut, NF><<<grid, 256, smf, s>>>(J, P, rpc);
 }
 template <typename T, int TX, typename CIn, int NIN, int NOUT>
-void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, size_t sm, dim3 grid,
-                cudaStream_t s) {
+void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, dim3 grid, cudaStream_t s) {
   typedef typename CT<T>::type C;
-  const size_t smf = sm + (size_t)(NIN + NOUT) * sizeof(C);
+  constexpr int PMAX = skn(NIN > NOUT ? NIN : NOUT);
+  const size_t smf = ((size_t)(J.nin * skn(NIN) + 2 * PMAX) * TX + NIN + NOUT) * sizeof(C);
   static size_t set = 48 * 1024;
   raise_smem(k_cols<T, TX, CIn, NIN, NOUT>, smf, set);
   k_cols<T, TX, CIn, NIN, NOUT><<<grid, 256, smf, s>>>(J, Pin, Pout);
@@ -56,7 +56,7 @@ bool launch_rows_r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_
   } else {
     switch (P.nx / 2) {
 #define LES_CASE(n) \
-  case n: r2c_fixed<T, TIn, n>(J, P, rpc, sm, s); return true;
+  case n: r2c_fixed<T, TIn, n>(J, P, rpc, s); return true;
       LES_ROW_SIZES(LES_CASE)
 #undef LES_CASE
       default: return false;
@@ -70,7 +70,7 @@ bool launch_rows_c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_
   } else {
     switch (P.nx / 2) {
 #define LES_CASE(n) \
-  case n: c2r_fixed<T, TOut, n>(J, P, rpc, sm, s); return true;
+  case n: c2r_fixed<T, TOut, n>(J, P, rpc, s); return true;
       LES_ROW_SIZES(LES_CASE)
 #undef LES_CASE
       default: return false;
@@ -98,7 +98,7 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
   if constexpr (std::is_same<T, float>::value && TX == 8 && std::is_same<CIn, float2>::value) {
     switch (key) {
 #define LES_CASE(a, b) \
-  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
+  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, grid, s); return true;
       LES_COL_PAIRS(LES_CASE)
 #undef LES_CASE
       default: return false;
@@ -106,7 +106,7 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
   } else if constexpr (std::is_same<T, float>::value && TX == 8 && std::is_same<CIn, double2>::value) {
     switch (key) {  // FP32 transforms of the saved FP64-layout spectra (padding to the 3/2 grid)
 #define LES_CASE(a, b) \
-  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
+  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, grid, s); return true;
       LES_COL_PAD(LES_CASE)
 #undef LES_CASE
       default: return false;
@@ -114,7 +114,7 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
   } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 && std::is_same<CIn, dcomplex>::value) {
     switch (key) {
 #define LES_CASE(a, b) \
-  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, sm, grid, s); return true;
+  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, grid, s); return true;
       LES_COL_SAME(LES_CASE)
 #undef LES_CASE
       default: return false;

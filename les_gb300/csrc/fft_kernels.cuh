@@ -48,10 +48,11 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
   extern __shared__ __align__(16) unsigned char smraw[];
   C* A = reinterpret_cast<C*>(smraw);
   const int m = NF > 0 ? NF : P.nx / 2;
-  C* B = A + rpc * m;
-  C* tws = B + rpc * m;  // NF > 0: complex-FFT twiddles (NF) then post-processing twiddles (NF + 1)
+  const int rs = NF > 0 ? skn(NF) : m;  // row stride of A, B (skewed when NF > 0)
+  C* B = A + rpc * rs;
+  C* tws = B + rpc * rs;  // NF > 0: unit-circle table (NF) then post-processing twiddles (NF + 1)
   if constexpr (NF > 0) {
-    for (int t = threadIdx.x; t < NF - 1; t += 256) tws[t] = TwSel<T>::get(P.c, t);
+    for (int t = threadIdx.x; t < NF; t += 256) tws[t] = UnitSel<T>::get(P.c, t);
     for (int t = threadIdx.x; t <= NF; t += 256) tws[NF + t] = rw<T>(P, t);
   }
   const int f = blockIdx.z, lev = blockIdx.y;
@@ -73,23 +74,23 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
       b = cvt<T, TIn>(row[2 * k + 1]);
     }
     if (dv != (T)0) { a = a / dv; b = b / dv; }
-    A[r * m + k] = mk<T>(a * s, b * s);
+    A[r * rs + (NF > 0 ? sk(k) : k)] = mk<T>(a * s, b * s);
   }
   __syncthreads();
   C* Z;
-  if constexpr (NF > 0) Z = fft_ct<T, false, NF, 1, -1, 256>(A, B, tws, nrow);
+  if constexpr (NF > 0) Z = fft_ct<T, false, NF, 1, -1, 256, CT_MAXR_ROWS>(A, B, tws, nrow);
   else Z = fft_smem<T, false>(A, B, nrow, m, P.c, -1);
   C* out = reinterpret_cast<C*>(J.work[f]) + (size_t)lev * J.pstride_work;
   for (int t = threadIdx.x; t < nrow * J.ncols; t += blockDim.x) {
     const int r = (int)J.dnc.div((unsigned)t), k = t - r * J.ncols;
-    const C* z = Z + r * m;
+    const C* z = Z + r * rs;
     C X;
     if (k == 0 || k == m) {
       const C z0 = z[0];
       X = mk<T>(k == 0 ? z0.x + z0.y : z0.x - z0.y, (T)0);
     } else {
-      const C a = z[k];
-      const C b = cconj(z[m - k]);
+      const C a = z[NF > 0 ? sk(k) : k];
+      const C b = cconj(z[NF > 0 ? sk(m - k) : m - k]);
       const C e = cscale(cadd(a, b), (T)0.5);
       const C d = cscale(csub(a, b), (T)0.5);
       const C o = cmulmi(d);  // d / i
@@ -105,12 +106,13 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
   typedef typename CT<T>::type C;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int m = NF > 0 ? NF : P.nx / 2;
+  const int rs = NF > 0 ? skn(NF) : m;  // row stride of A, B (skewed when NF > 0)
   C* X = reinterpret_cast<C*>(smraw);  // rpc x (m+1)
   C* A = X + rpc * (m + 1);
-  C* B = A + rpc * m;
-  C* tws = B + rpc * m;  // NF > 0: complex-FFT twiddles (NF) then post-processing twiddles (NF + 1)
+  C* B = A + rpc * rs;
+  C* tws = B + rpc * rs;  // NF > 0: unit-circle table (NF) then post-processing twiddles (NF + 1)
   if constexpr (NF > 0) {
-    for (int t = threadIdx.x; t < NF - 1; t += 256) tws[t] = TwSel<T>::get(P.c, t);
+    for (int t = threadIdx.x; t < NF; t += 256) tws[t] = UnitSel<T>::get(P.c, t);
     for (int t = threadIdx.x; t <= NF; t += 256) tws[NF + t] = rw<T>(P, t);
   }
   const int f = blockIdx.z, lev = blockIdx.y;
@@ -130,11 +132,11 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
     const C b = cconj(X[r * (m + 1) + (m - k)]);
     const C e = cadd(a, b);
     const C d = cmul(csub(a, b), cconj(NF > 0 ? tws[NF + k] : rw<T>(P, k)));  // x exp(+2 pi i k/nx)
-    A[t] = cadd(e, cmuli(d));
+    A[r * rs + (NF > 0 ? sk(k) : k)] = cadd(e, cmuli(d));
   }
   __syncthreads();
   C* Z;
-  if constexpr (NF > 0) Z = fft_ct<T, false, NF, 1, +1, 256>(A, B, tws, nrow);
+  if constexpr (NF > 0) Z = fft_ct<T, false, NF, 1, +1, 256, CT_MAXR_ROWS>(A, B, tws, nrow);
   else Z = fft_smem<T, false>(A, B, nrow, m, P.c, +1);
   TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys;
   const double off = J.off[f] ? J.off[f][lev] : 0.0;
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
     const int r = NF > 0 ? t / (NF + 1) : (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
     TOut* row = dst + (size_t)(row0 + r) * J.ld;
     if (k < m) {
-      const C z = Z[r * m + k];
+      const C z = Z[r * rs + (NF > 0 ? sk(k) : k)];
       if (J.off[f]) {
         row[2 * k] = cvt<TOut, double>(cvt<double, T>(z.x) + off);
         row[2 * k + 1] = cvt<TOut, double>(cvt<double, T>(z.y) + off);
@@ -191,14 +193,16 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
   constexpr bool FIX = NIN > 0 && NOUT > 0;
   const int ny_in = FIX ? NIN : J.ny_in, ny_out = FIX ? NOUT : J.ny_out;
   const int nymax = max(ny_in, ny_out);
+  // row slots per buffer (skewed layout when FIX: row i at sk(i))
+  const int pin = FIX ? skn(NIN) : ny_in, pmax = FIX ? skn(NIN > NOUT ? NIN : NOUT) : nymax;
   C* IN = reinterpret_cast<C*>(smraw);
-  C* A = IN + J.nin * ny_in * TX;
-  C* B = A + nymax * TX;
-  C* twi = B + nymax * TX;  // FIX: input-length twiddles (NIN), output-length twiddles (NOUT)
+  C* A = IN + J.nin * pin * TX;
+  C* B = A + pmax * TX;
+  C* twi = B + pmax * TX;  // FIX: unit-circle tables of the input (NIN) and output (NOUT) lengths
   C* two = twi + NIN;
   if constexpr (FIX) {
-    for (int t = threadIdx.x; t < NIN - 1; t += 256) twi[t] = TwSel<T>::get(Pin, t);
-    for (int t = threadIdx.x; t < NOUT - 1; t += 256) two[t] = TwSel<T>::get(Pout, t);
+    for (int t = threadIdx.x; t < NIN; t += 256) twi[t] = UnitSel<T>::get(Pin, t);
+    for (int t = threadIdx.x; t < NOUT; t += 256) two[t] = UnitSel<T>::get(Pout, t);
   }
   const int jx0 = blockIdx.x * TX;
   const int lev = blockIdx.y;
@@ -212,18 +216,18 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
         const CIn x = src[(size_t)row * J.wc_in + jx];
         v = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
       }
-      IN[i * ny_in * TX + t] = v;
+      IN[i * pin * TX + (FIX ? sk(row) : row) * TX + b] = v;
     }
   }
   __syncthreads();
   if (J.dir & DIR_FWD) {
     for (int i = 0; i < J.nin; ++i) {
-      C* xi = IN + i * ny_in * TX;
+      C* xi = IN + i * pin * TX;
       C* r;
-      if constexpr (FIX) r = fft_ct<T, true, NIN, TX, -1, 256>(xi, A, twi, TX);
+      if constexpr (FIX) r = fft_ct<T, true, NIN, TX, -1, 256, CtMaxR<T>::v>(xi, A, twi, TX);
       else r = fft_smem<T, true>(xi, A, TX, 0, Pin, -1);
       if (r != xi) {
-        for (int t = threadIdx.x; t < ny_in * TX; t += blockDim.x) xi[t] = r[t];
+        for (int t = threadIdx.x; t < pin * TX; t += blockDim.x) xi[t] = r[t];
         __syncthreads();
       }
     }
@@ -251,22 +255,23 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
       if (rin >= 0 && jx < J.ncols) {
         for (int i = 0; i < J.nin; ++i) {
           const int code = J.coef[o][i];
-          if (code != CC_NONE) acc = cadd(acc, apply_coef<T>(code, IN[i * ny_in * TX + rin * TX + b], jx, js, J));
+          if (code != CC_NONE)
+            acc = cadd(acc, apply_coef<T>(code, IN[i * pin * TX + (FIX ? sk(rin) : rin) * TX + b], jx, js, J));
         }
       }
-      A[t] = acc;
+      A[(FIX ? sk(row) : row) * TX + b] = acc;
     }
     __syncthreads();
     C* r = A;
     if ((J.inv_mask >> o) & 1u) {
-      if constexpr (FIX) r = fft_ct<T, true, NOUT, TX, +1, 256>(A, B, two, TX);
+      if constexpr (FIX) r = fft_ct<T, true, NOUT, TX, +1, 256, CtMaxR<T>::v>(A, B, two, TX);
       else r = fft_smem<T, true>(A, B, TX, 0, Pout, +1);
     }
     C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out;
     for (int t = threadIdx.x; t < ny_out * TX; t += blockDim.x) {
       const int row = t / TX, b = t - row * TX;
       const int jx = jx0 + b;
-      if (jx < J.ncols) dst[(size_t)row * J.wc_out + jx] = r[t];
+      if (jx < J.ncols) dst[(size_t)row * J.wc_out + jx] = r[(FIX ? sk(row) : row) * TX + b];
     }
     __syncthreads();
   }

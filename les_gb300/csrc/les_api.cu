@@ -90,6 +90,23 @@ static int make_plan(les_ctx* c, int n, HostPlan& hp) {
   c->allocs.push_back(hp.devd);
   LES_CUDA_CHECK(cudaMemcpy(hp.devd, twd.data(), twd.size() * sizeof(float4), cudaMemcpyHostToDevice));
   P.twd = static_cast<const float4*>(hp.devd);
+  {  // unit-circle tables exp(-2 pi i m / n), m < n
+    std::vector<float2> uf(n);
+    std::vector<float4> ud(n);
+    for (int mm = 0; mm < n; ++mm) {
+      const long double ang = -2.0L * 3.14159265358979323846264338327950288L * mm / (long double)n;
+      uf[mm] = make_float2((float)cosl(ang), (float)sinl(ang));
+      ud[mm] = ff_pair(cosl(ang), sinl(ang));
+    }
+    LES_CUDA_CHECK(cudaMalloc(&hp.devuf, uf.size() * sizeof(float2)));
+    c->allocs.push_back(hp.devuf);
+    LES_CUDA_CHECK(cudaMemcpy(hp.devuf, uf.data(), uf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    LES_CUDA_CHECK(cudaMalloc(&hp.devud, ud.size() * sizeof(float4)));
+    c->allocs.push_back(hp.devud);
+    LES_CUDA_CHECK(cudaMemcpy(hp.devud, ud.data(), ud.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    P.unitf = static_cast<const float2*>(hp.devuf);
+    P.unitd = static_cast<const float4*>(hp.devud);
+  }
   LES_CUDA_CHECK(cudaMalloc(&hp.dev, tw.size() * sizeof(double2)));
   c->allocs.push_back(hp.dev);
   LES_CUDA_CHECK(cudaMemcpy(hp.dev, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
@@ -242,8 +259,7 @@ size_t les_estimate_device_bytes(const les_config* cfg) {
   Grid g;
   grid_of(*cfg, g);
   Sizes s = sizes_of(g);
-  const size_t ffd = cfg->precision == 1 ? 2 * (size_t)(g.nz + 1) * g.C * sizeof(float2) : 0;
-  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + ffd + (1u << 20);
+  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + (1u << 20);
 }
 
 int les_ctx_create(const les_config* cfg, les_ctx** out) {
@@ -331,10 +347,6 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
       (st = dalloc(c, (void**)&c->wspec, 4 * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->gamt, (size_t)(g.nz + 1) * g.C * sizeof(double))))
-    return fail(st);
-  if (k.precision == 1 &&
-      ((st = dalloc(c, (void**)&c->ibetd, (size_t)(g.nz + 1) * g.C * sizeof(float2))) ||
-       (st = dalloc(c, (void**)&c->gamtd, (size_t)(g.nz + 1) * g.C * sizeof(float2)))))
     return fail(st);
   if ((st = thomas_tables(c))) return fail(st);
   c->wsA_bytes = s.wsA; c->wsB_bytes = s.wsB; c->wsP_bytes = s.wsP;

@@ -21,6 +21,8 @@ struct HostPlan {
   double2* dev = nullptr;
   float2* devf = nullptr;
   void* devd = nullptr;  // float-float twiddles (float4)
+  void* devuf = nullptr;  // unit-circle tables (float2, float4)
+  void* devud = nullptr;
 };
 struct HostRealPlan {
   RealPlanDev r{};
@@ -62,7 +64,6 @@ struct les_ctx {
   double *kx = nullptr, *ky = nullptr, *G = nullptr, *GG = nullptr;
   float *kxf = nullptr, *kyf = nullptr, *Gf = nullptr, *GGf = nullptr;
   float2 *kxd = nullptr, *kyd = nullptr;  // kx, ky as float-float pairs
-  float2 *ibetd = nullptr, *gamtd = nullptr;  // Thomas tables as float-float pairs (mixed form)
   // FFT plans
   les::HostRealPlan rx, rxb;   // real x-transforms of length nx, nx2
   les::HostPlan cy, cyb;       // complex y-transforms of length ny, ny2

@@ -1730,90 +1730,85 @@ __device__ __forceinline__ void tridiag_mode(int t, const HC* __restrict__ Hx, c
   }
 }
 
-template <typename HC, typename PC>
-__global__ void __launch_bounds__(128) k_tridiag(const HC* __restrict__ Hx, const HC* __restrict__ Hy,
-                                                 const HC* __restrict__ Hz, const C2* __restrict__ bot,
-                                                 const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
-                                                 const double* __restrict__ gam, const double* __restrict__ kx,
-                                                 const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= lh * ny) return;
-  tridiag_mode<HC, PC>(t, Hx, Hy, Hz, bot, top, P, ibet, gam, kx, ky, lh, ny, nz, dz);
+// The same solve with two threads per mode: part 0 the real, part 1 the
+// imaginary part of p-hat (a, b, c are real, so the two recurrences are
+// independent), each load issued one level ahead; the arithmetic and its
+// order are those of tridiag_mode.  The kx = ky = 0 and Nyquist modes run
+// tridiag_mode on part 0.
+template <typename HC> __device__ __forceinline__ double ld1(const HC* p, size_t i, int comp);
+template <> __device__ __forceinline__ double ld1<double2>(const double2* p, size_t i, int comp) {
+  return reinterpret_cast<const double*>(p)[2 * i + comp];
 }
-
-// Mixed form: the kx = ky = 0 mode, the Nyquist modes and the lowest-|k|
-// modes (|kx|, |ky| <= 2 in wavenumber index: the near-singular Neumann
-// systems) are solved in FP64 as above; every other mode runs the same
-// Thomas recurrences in float-float arithmetic on the FP32 pipe, with the
-// coefficient tables split into float-float pairs.
-__device__ __forceinline__ dfloat dfl(float2 v) { return dfloat(v.x, v.y); }
-__device__ __forceinline__ dcomplex dcx(C2 v) { dcomplex r; r.x = cvt<dfloat>(v.x); r.y = cvt<dfloat>(v.y); return r; }
-__global__ void __launch_bounds__(128) k_tridiag_mixed(const dcomplex* __restrict__ Hx, const dcomplex* __restrict__ Hy,
-                                                       const dcomplex* __restrict__ Hz, const C2* __restrict__ bot,
-                                                       const C2* __restrict__ top, dcomplex* P,
-                                                       const double* __restrict__ ibet, const double* __restrict__ gam,
-                                                       const float2* __restrict__ ibetd, const float2* __restrict__ gamd,
-                                                       const double* __restrict__ kx, const double* __restrict__ ky,
-                                                       const float2* __restrict__ kxd, const float2* __restrict__ kyd,
-                                                       int lh, int ny, int nz, double dz, float2 dzd, float2 idzd,
-                                                       float2 idz2d) {
-  // two threads per mode: part 0 the real, part 1 the imaginary part of p-hat
-  // (a, b, c are real, so the two recurrences are independent)
+template <> __device__ __forceinline__ double ld1<dcomplex>(const dcomplex* p, size_t i, int comp) {
+  return cvt<double>(reinterpret_cast<const dfloat*>(p)[2 * i + comp]);
+}
+__device__ __forceinline__ void st1(double2* p, size_t i, int comp, double v) {
+  reinterpret_cast<double*>(p)[2 * i + comp] = v;
+}
+__device__ __forceinline__ void st1(dcomplex* p, size_t i, int comp, double v) {
+  reinterpret_cast<dfloat*>(p)[2 * i + comp] = cvt<dfloat>(v);
+}
+template <typename HC, typename PC>
+__global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, const HC* __restrict__ Hy,
+                                                  const HC* __restrict__ Hz, const C2* __restrict__ bot,
+                                                  const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
+                                                  const double* __restrict__ gam, const double* __restrict__ kx,
+                                                  const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
   const int nk = lh * ny;
   const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = g2 >> 1, part = g2 & 1;
   if (t >= nk) return;
   const int jx = t % lh, jy = t / lh;
-  const int jyi = jy <= ny / 2 ? jy : ny - jy;
-  if (t == 0 || jy == ny / 2 || jx == lh - 1 || (jx <= 2 && jyi <= 2)) {
-    if (part == 0) tridiag_mode<dcomplex, dcomplex>(t, Hx, Hy, Hz, bot, top, P, ibet, gam, kx, ky, lh, ny, nz, dz);
+  if (t == 0 || jy == ny / 2 || jx == lh - 1) {
+    if (part == 0) tridiag_mode<HC, PC>(t, Hx, Hy, Hz, bot, top, P, ibet, gam, kx, ky, lh, ny, nz, dz);
     return;
   }
   const size_t NK = (size_t)nk;
-  // this part's p-hat component reads: Re p <- Im(kx Hx + ky Hy), Re Hz;
-  // Im p <- Re(kx Hx + ky Hy), Im Hz
-  const dfloat* hxc = reinterpret_cast<const dfloat*>(Hx) + (part == 0 ? 1 : 0);
-  const dfloat* hyc = reinterpret_cast<const dfloat*>(Hy) + (part == 0 ? 1 : 0);
-  const dfloat* hzc = reinterpret_cast<const dfloat*>(Hz) + part;
-  dfloat* pc = reinterpret_cast<dfloat*>(P) + part;
-  const dfloat sgn = part == 0 ? dfloat(-1.f, 0.f) : dfloat(1.f, 0.f);  // r.x = dHz - si ; r.y = sr + dHz
-  const dfloat k_x = dfl(kxd[t]), k_y = dfl(kyd[t]);
-  const dfloat ddz = dfl(dzd), idz = dfl(idzd), idz2 = dfl(idz2d);
+  const int ch = part == 0 ? 1 : 0;  // component of Hx, Hy feeding this part
+  const double k_x = kx[t], k_y = ky[t];
+  const double idz2 = 1.0 / (dz * dz);
   const int n = nz + 1;
   const C2 b1 = bot[t];
-  const dfloat r1 = cvt<dfloat>(part == 0 ? b1.x : b1.y);
-  dfloat up = (-(ddz * r1)) * dfl(ibetd[t]);
-  pc[2 * (size_t)t] = up;
-  dfloat hz0 = hzc[2 * (size_t)t];
-  // level j's inputs, loaded one level ahead
-  dfloat hxn = hxc[2 * (size_t)t], hyn = hyc[2 * (size_t)t];
-  dfloat hzn = nz - 1 >= 2 ? hzc[2 * (NK + t)] : dfloat(0.f, 0.f);
+  double up = (-dz * (part == 0 ? b1.x : b1.y)) * ibet[t];
+  st1(P, t, part, up);
+  double hz0 = ld1<HC>(Hz, t, part);
+  double hxn = ld1<HC>(Hx, t, ch), hyn = ld1<HC>(Hy, t, ch);
+  double hzn = nz - 1 >= 2 ? ld1<HC>(Hz, NK + t, part) : 0.0;
+  double ibn = ibet[NK + t];
   for (int j = 2; j <= n; ++j) {
-    const dfloat ib = dfl(ibetd[(size_t)(j - 1) * NK + t]);
-    dfloat a, r;
+    const double ib = ibn;
+    if (j + 1 <= n) ibn = ibet[(size_t)j * NK + t];
+    double a, r;
     if (j <= nz) {
-      const dfloat hx = hxn, hy = hyn, hz1 = (j <= nz - 1) ? hzn : dfloat(0.f, 0.f);
-      if (j + 1 <= nz) {
-        hxn = hxc[2 * ((size_t)(j - 1) * NK + t)];
-        hyn = hyc[2 * ((size_t)(j - 1) * NK + t)];
-        if (j <= nz - 2) hzn = hzc[2 * ((size_t)j * NK + t)];
-      }
       a = idz2;
-      r = (hz1 - hz0) * idz + sgn * (k_x * hx + k_y * hy);
+      const double hx = hxn, hy = hyn, hz1 = (j <= nz - 1) ? hzn : 0.0;
+      if (j + 1 <= nz) {
+        hxn = ld1<HC>(Hx, (size_t)(j - 1) * NK + t, ch);
+        hyn = ld1<HC>(Hy, (size_t)(j - 1) * NK + t, ch);
+        if (j <= nz - 2) hzn = ld1<HC>(Hz, (size_t)j * NK + t, part);
+      }
+      const double s = k_x * hx + k_y * hy;
+      r = part == 0 ? -s + (hz1 - hz0) / dz : s + (hz1 - hz0) / dz;
       hz0 = hz1;
     } else {
-      a = dfloat(-1.f, 0.f);
+      a = -1.0;
       const C2 tp = top[t];
-      r = -(cvt<dfloat>(part == 0 ? tp.x : tp.y) * ddz);
+      r = -(part == 0 ? tp.x : tp.y) * dz;
     }
-    const dfloat u = (r - a * up) * ib;
-    pc[2 * ((size_t)(j - 1) * NK + t)] = u;
+    const double u = (r - a * up) * ib;
+    st1(P, (size_t)(j - 1) * NK + t, part, u);
     up = u;
   }
+  double gmn = gam[(size_t)(n - 1) * NK + t];
+  double pn = ld1<PC>(P, (size_t)(n - 2) * NK + t, part);
   for (int j = n - 1; j >= 1; --j) {
-    const dfloat gm = dfl(gamd[(size_t)j * NK + t]);
-    const dfloat u = pc[2 * ((size_t)(j - 1) * NK + t)] - gm * up;
-    pc[2 * ((size_t)(j - 1) * NK + t)] = u;
+    const double gm = gmn, pv = pn;
+    if (j - 1 >= 1) {
+      gmn = gam[(size_t)(j - 1) * NK + t];
+      pn = ld1<PC>(P, (size_t)(j - 2) * NK + t, part);
+    }
+    const double u = pv - gm * up;
+    st1(P, (size_t)(j - 1) * NK + t, part, u);
     up = u;
   }
 }
@@ -1853,13 +1848,6 @@ int thomas_tables(les_ctx* c) {
   }
   LES_CUDA_CHECK(cudaMemcpy(c->ibet, ib.data(), ib.size() * sizeof(double), cudaMemcpyHostToDevice));
   LES_CUDA_CHECK(cudaMemcpy(c->gamt, gm.data(), gm.size() * sizeof(double), cudaMemcpyHostToDevice));
-  if (c->ibetd) {  // float-float copies for the mixed form
-    std::vector<float2> f2(ib.size());
-    for (size_t i = 0; i < ib.size(); ++i) f2[i] = make_float2((float)ib[i], (float)(ib[i] - (double)(float)ib[i]));
-    LES_CUDA_CHECK(cudaMemcpy(c->ibetd, f2.data(), f2.size() * sizeof(float2), cudaMemcpyHostToDevice));
-    for (size_t i = 0; i < gm.size(); ++i) f2[i] = make_float2((float)gm[i], (float)(gm[i] - (double)(float)gm[i]));
-    LES_CUDA_CHECK(cudaMemcpy(c->gamtd, f2.data(), f2.size() * sizeof(float2), cudaMemcpyHostToDevice));
-  }
   return 0;
 }
 
@@ -1899,17 +1887,9 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
     K.coef[0][0] = CC_KILL;
     cols(c, K);
   }
-  if constexpr (std::is_same<T, dfloat>::value) {
-    auto ff = [](double v) { return make_float2((float)v, (float)(v - (double)(float)v)); };
-    k_tridiag_mixed<<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
-        H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->ibetd,
-        c->gamtd, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz, ff(g.dz), ff(1.0 / g.dz),
-        ff(1.0 / (g.dz * g.dz))); LES_COUNT_LAUNCH();
-  } else {
-    k_tridiag<CX, CX><<<(g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
-        H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx,
-        c->ky, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
-  }
+  k_tridiag2<CX, CX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
+      H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky,
+      g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
