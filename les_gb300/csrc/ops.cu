@@ -1766,50 +1766,74 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
   const size_t NK = (size_t)nk;
   const int ch = part == 0 ? 1 : 0;  // component of Hx, Hy feeding this part
   const double k_x = kx[t], k_y = ky[t];
-  const double idz2 = 1.0 / (dz * dz);
+  const double idz2 = 1.0 / (dz * dz), idz = 1.0 / dz;
   const int n = nz + 1;
   const C2 b1 = bot[t];
   double up = (-dz * (part == 0 ? b1.x : b1.y)) * ibet[t];
   st1(P, t, part, up);
   double hz0 = ld1<HC>(Hz, t, part);
-  double hxn = ld1<HC>(Hx, t, ch), hyn = ld1<HC>(Hy, t, ch);
-  double hzn = nz - 1 >= 2 ? ld1<HC>(Hz, NK + t, part) : 0.0;
-  double ibn = ibet[NK + t];
-  for (int j = 2; j <= n; ++j) {
-    const double ib = ibn;
-    if (j + 1 <= n) ibn = ibet[(size_t)j * NK + t];
-    double a, r;
+  // level j's inputs in ring slot (j - 2) % 4, loaded four levels ahead
+  constexpr int D = 4;
+  double bx[D], by[D], bz[D], bi[D];
+  auto load = [&](int j, double& x, double& y, double& z, double& ib) {
+    if (j <= n) ib = ibet[(size_t)(j - 1) * NK + t];
     if (j <= nz) {
-      a = idz2;
-      const double hx = hxn, hy = hyn, hz1 = (j <= nz - 1) ? hzn : 0.0;
-      if (j + 1 <= nz) {
-        hxn = ld1<HC>(Hx, (size_t)(j - 1) * NK + t, ch);
-        hyn = ld1<HC>(Hy, (size_t)(j - 1) * NK + t, ch);
-        if (j <= nz - 2) hzn = ld1<HC>(Hz, (size_t)j * NK + t, part);
+      x = ld1<HC>(Hx, (size_t)(j - 2) * NK + t, ch);
+      y = ld1<HC>(Hy, (size_t)(j - 2) * NK + t, ch);
+    }
+    z = (j <= nz - 1) ? ld1<HC>(Hz, (size_t)(j - 1) * NK + t, part) : 0.0;
+  };
+#pragma unroll
+  for (int q = 0; q < D; ++q) load(2 + q, bx[q], by[q], bz[q], bi[q]);
+  for (int jb = 2; jb <= n; jb += D) {
+#pragma unroll
+    for (int q = 0; q < D; ++q) {
+      const int j = jb + q;
+      if (j <= n) {
+        const double hx = bx[q], hy = by[q], hz1 = bz[q], ib = bi[q];
+        load(j + D, bx[q], by[q], bz[q], bi[q]);
+        double a, r;
+        if (j <= nz) {
+          a = idz2;
+          const double s = k_x * hx + k_y * hy;
+          // the FP64 form divides as the reference does; the mixed form
+          // multiplies by 1/dz
+          const double dh = std::is_same<HC, dcomplex>::value ? (hz1 - hz0) * idz : (hz1 - hz0) / dz;
+          r = part == 0 ? -s + dh : s + dh;
+          hz0 = hz1;
+        } else {
+          a = -1.0;
+          const C2 tp = top[t];
+          r = -(part == 0 ? tp.x : tp.y) * dz;
+        }
+        const double u = (r - a * up) * ib;
+        st1(P, (size_t)(j - 1) * NK + t, part, u);
+        up = u;
       }
-      const double s = k_x * hx + k_y * hy;
-      r = part == 0 ? -s + (hz1 - hz0) / dz : s + (hz1 - hz0) / dz;
-      hz0 = hz1;
-    } else {
-      a = -1.0;
-      const C2 tp = top[t];
-      r = -(part == 0 ? tp.x : tp.y) * dz;
     }
-    const double u = (r - a * up) * ib;
-    st1(P, (size_t)(j - 1) * NK + t, part, u);
-    up = u;
   }
-  double gmn = gam[(size_t)(n - 1) * NK + t];
-  double pn = ld1<PC>(P, (size_t)(n - 2) * NK + t, part);
-  for (int j = n - 1; j >= 1; --j) {
-    const double gm = gmn, pv = pn;
-    if (j - 1 >= 1) {
-      gmn = gam[(size_t)(j - 1) * NK + t];
-      pn = ld1<PC>(P, (size_t)(j - 2) * NK + t, part);
+  // back substitution, level j's gamma and forward value in slot (n-1-j) % 4
+  double bg[D], bp[D];
+  auto loadb = [&](int j, double& g, double& pv) {
+    if (j >= 1) {
+      g = gam[(size_t)j * NK + t];
+      pv = ld1<PC>(P, (size_t)(j - 1) * NK + t, part);
     }
-    const double u = pv - gm * up;
-    st1(P, (size_t)(j - 1) * NK + t, part, u);
-    up = u;
+  };
+#pragma unroll
+  for (int q = 0; q < D; ++q) loadb(n - 1 - q, bg[q], bp[q]);
+  for (int jb = n - 1; jb >= 1; jb -= D) {
+#pragma unroll
+    for (int q = 0; q < D; ++q) {
+      const int j = jb - q;
+      if (j >= 1) {
+        const double gm = bg[q], pv = bp[q];
+        loadb(j - D, bg[q], bp[q]);
+        const double u = pv - gm * up;
+        st1(P, (size_t)(j - 1) * NK + t, part, u);
+        up = u;
+      }
+    }
   }
 }
 
