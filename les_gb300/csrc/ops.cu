@@ -810,6 +810,24 @@ __global__ void k_nut(const double* __restrict__ S11, const double* __restrict__
     Nu_t[i] = S * Cs[i] * l2;
   }
 }
+// Mixed form: the same in FP32 (the strain there comes from FP32 transforms),
+// conversions on the integer pipe
+__global__ void k_nut32(const double* __restrict__ S11, const double* __restrict__ S12,
+                        const double* __restrict__ S13, const double* __restrict__ S22,
+                        const double* __restrict__ S23, const double* __restrict__ S33, double* Cs,
+                        double* Nu_t, int ld, int nx, int ny, int nz, float l2, int override_cs, double cs_ov) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * nz) {
+    if (override_cs) Cs[i] = cs_ov;
+    const int jx = (int)(i % ld);
+    if (jx >= nx) continue;
+    const float a11 = cvt_d2f(S11[i]), a22 = cvt_d2f(S22[i]), a33 = cvt_d2f(S33[i]);
+    const float a12 = cvt_d2f(S12[i]), a13 = cvt_d2f(S13[i]), a23 = cvt_d2f(S23[i]);
+    const float S = sqrtf(2.0f * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0f * (a12 * a12 + a13 * a13 + a23 * a23)));
+    const float cs = override_cs ? cvt_d2f(cs_ov) : cvt_d2f(Cs[i]);
+    Nu_t[i] = cvt_f2d(S * cs * l2);
+  }
+}
 // sgs_stag.f90:218-364 (tau_ij, 'wall', molec = .false.)
 __global__ void k_tau(const double* __restrict__ S11, const double* __restrict__ S12,
                       const double* __restrict__ S13, const double* __restrict__ S22,
@@ -1593,15 +1611,19 @@ __global__ void k_rhs_ab2(double* u, double* v, double* w, double* Rx, double* R
 __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz,
                                const double* __restrict__ p, const double* __restrict__ dpdx,
                                const double* __restrict__ dpdy, double* dpdz, int ld, int nx, int ny, int nz,
-                               double dz, double dt) {
+                               double dz, double dt, int recip) {
+  // recip: the mixed form multiplies by 1/dz; the FP64 form divides as the
+  // reference does
   const size_t np = (size_t)ld * ny;
+  const double idz = 1.0 / dz;
   GSTRIDE(i, np * (nz - 1)) {
     const int jz = (int)(i / np) + 1;
     const size_t r = i - (size_t)(jz - 1) * np;
     const int jx = (int)(r % ld);
     double pz = 0.0;
     if (jx < nx) {
-      pz = (p[r + (size_t)jz * np] - p[r + (size_t)(jz - 1) * np]) / dz;
+      const double dp = p[r + (size_t)jz * np] - p[r + (size_t)(jz - 1) * np];
+      pz = recip ? dp * idz : dp / dz;
       dpdz[i] = pz;
     } else {
       pz = dpdz[i];
@@ -2505,8 +2527,14 @@ static int sgs_stagT(les_ctx* c) {
     const float c016 = 0.16f;
     csov = (double)(c016 * c016);
   }
-  k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
-                                               c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, g.delta * g.delta, ov, csov); LES_COUNT_LAUNCH();
+  if (MX)
+    k_nut32<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
+                                                   c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, (float)(g.delta * g.delta),
+                                                   ov, csov);
+  else
+    k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
+                                                 c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, g.delta * g.delta, ov, csov);
+  LES_COUNT_LAUNCH();
   k_tau<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_NU_T],
                                                c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ],
                                                c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz); LES_COUNT_LAUNCH();
@@ -2783,7 +2811,7 @@ static int stepT(les_ctx* c) {
   k_dpdz_project<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
                                                         c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX],
                                                         c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
-                                                        k.dt); LES_COUNT_LAUNCH();
+                                                        k.dt, MX ? 1 : 0); LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaGetLastError());
   if (rms_step) {
     if (!MX) op_rmsdiv(c, c->dscal + 1);
