@@ -2272,6 +2272,68 @@ static void plane_spectra(les_ctx* c, int np, const double* const* planes, const
   cols(c, J);
 }
 
+// complex value of a FP64-layout spectrum in arithmetic type R (FP32: the
+// narrowing on the integer pipe), and a store into the output type
+template <typename R> __device__ __forceinline__ typename CT<R>::type ldR(const C2* p, size_t i);
+template <> __device__ __forceinline__ double2 ldR<double>(const C2* p, size_t i) { return p[i]; }
+template <> __device__ __forceinline__ float2 ldR<float>(const C2* p, size_t i) {
+  const double2 v = p[i];
+  return make_float2(cvt_d2f(v.x), cvt_d2f(v.y));
+}
+template <typename CO, typename CI> __device__ __forceinline__ void stC(CO* o, CI v) {
+  o->x = cvt<decltype(o->x)>(v.x);
+  o->y = cvt<decltype(o->y)>(v.y);
+}
+
+// convec.f90:67-114 vorticity spectra (x 1/(nx*ny)) from U,V,W spectra.
+// R: arithmetic (FP32 in the mixed form, where the spectra are FP32-accurate
+// except the (0,0) mode, which carries the plane means and is done in FP64)
+template <typename R>
+__device__ __forceinline__ void vort_point(size_t t, int jz, size_t m, const C2* __restrict__ U,
+                                           const C2* __restrict__ V, const C2* __restrict__ W,
+                                           const C2* __restrict__ D1, const C2* __restrict__ D2, R k_x, R k_y,
+                                           int nk, int nz, R idz, typename CT<R>::type* o) {
+  typedef typename CT<R>::type CR;
+  const CR w = ldR<R>(W, t), u = ldR<R>(U, t), v = ldR<R>(V, t);
+  CR a, b;
+  if (jz == 1) {
+    const CR w2 = ldR<R>(W, t + nk);
+    const CR wy = cadd(ik(w, k_y), ik(w2, k_y));
+    const CR wx = cadd(ik(w, k_x), ik(w2, k_x));
+    a = csub(cscale(wy, (R)0.5), ldR<R>(D2, m));
+    b = csub(ldR<R>(D1, m), cscale(wx, (R)0.5));
+  } else if (jz == nz) {
+    a = ik(w, k_y);
+    b = cscale(ik(w, k_x), (R)-1.0);
+  } else {
+    const CR vz = cscale(csub(v, ldR<R>(V, t - nk)), idz);
+    const CR uz = cscale(csub(u, ldR<R>(U, t - nk)), idz);
+    a = csub(ik(w, k_y), vz);
+    b = csub(uz, ik(w, k_x));
+  }
+  o[0] = a;
+  o[1] = b;
+  o[2] = csub(ik(v, k_x), ik(u, k_y));
+}
+template <typename CO, typename R>
+__global__ void k_vort_spec32(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
+                              const C2* __restrict__ D1, const C2* __restrict__ D2, CO* o1, CO* o2, CO* o3,
+                              const R* __restrict__ kx, const R* __restrict__ ky, int nk, int nz, double idz) {
+  GSTRIDE(t, (size_t)nk * nz) {
+    const int jz = (int)(t / nk) + 1;
+    const size_t m = t - (size_t)(jz - 1) * nk;
+    if (m == 0) {
+      double2 r[3];
+      vort_point<double>(t, jz, m, U, V, W, D1, D2, 0.0, 0.0, nk, nz, idz, r);
+      stC(o1 + t, r[0]); stC(o2 + t, r[1]); stC(o3 + t, r[2]);
+    } else {
+      typename CT<R>::type r[3];
+      vort_point<R>(t, jz, m, U, V, W, D1, D2, kx[m], ky[m], nk, nz, (R)idz, r);
+      stC(o1 + t, r[0]); stC(o2 + t, r[1]); stC(o3 + t, r[2]);
+    }
+  }
+}
+
 // convec.f90:67-114 vorticity spectra (x 1/(nx*ny)) from U,V,W spectra
 template <typename CO>
 __global__ void k_vort_spec(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
@@ -2391,6 +2453,104 @@ __global__ void k_lag_spec(const C2* __restrict__ U, const C2* __restrict__ V, c
   }
 }
 
+// The same in arithmetic type R (mixed form: FP32, the (0,0) mode in FP64)
+template <typename R>
+__device__ __forceinline__ void lag_spec_point(int jz, size_t m, size_t i, const C2* __restrict__ U,
+                                               const C2* __restrict__ V, const C2* __restrict__ W,
+                                               const C2* __restrict__ D1, const C2* __restrict__ D2, R k_x, R k_y,
+                                               int nk, int nz, R idz, int shift, typename CT<R>::type* r) {
+  typedef typename CT<R>::type CR;
+  const CR z = mk<R>((R)0, (R)0);
+  auto ddz_uv = [&](const C2* F, int j) -> CR {  // level j >= 2
+    if (j >= nz) return z;
+    return cscale(csub(ldR<R>(F, (size_t)(j - 1) * nk + m), ldR<R>(F, (size_t)(j - 2) * nk + m)), idz);
+  };
+  auto ddz_w = [&](int j) -> CR {  // dwdz at level j
+    if (j >= nz) return z;
+    return cscale(csub(ldR<R>(W, (size_t)j * nk + m), ldR<R>(W, (size_t)(j - 1) * nk + m)), idz);
+  };
+  CR ub, vb, wb, ux, uy, uz, vx, vy, vz, wx, wy, wz;
+  const R h = (R)0.5;
+  if (jz == 1) {
+    const CR u1 = ldR<R>(U, i), v1 = ldR<R>(V, i), w1 = ldR<R>(W, i), w2 = ldR<R>(W, i + nk);
+    ub = u1; vb = v1; wb = cscale(w2, (R)0.25);
+    ux = ik(u1, k_x); uy = ik(u1, k_y); uz = ldR<R>(D1, m);
+    vx = ik(v1, k_x); vy = ik(v1, k_y); vz = ldR<R>(D2, m);
+    wx = cscale(cadd(ik(w1, k_x), ik(w2, k_x)), h);
+    wy = cscale(cadd(ik(w1, k_y), ik(w2, k_y)), h);
+    wz = ddz_w(1);
+  } else {
+    const CR u0 = ldR<R>(U, i), um = ldR<R>(U, i - nk), v0 = ldR<R>(V, i), vm = ldR<R>(V, i - nk), w0 = ldR<R>(W, i);
+    ub = cscale(cadd(u0, um), h); vb = cscale(cadd(v0, vm), h); wb = w0;
+    ux = cscale(cadd(ik(u0, k_x), ik(um, k_x)), h);
+    uy = cscale(cadd(ik(u0, k_y), ik(um, k_y)), h);
+    uz = ddz_uv(U, jz);
+    vx = cscale(cadd(ik(v0, k_x), ik(vm, k_x)), h);
+    vy = cscale(cadd(ik(v0, k_y), ik(vm, k_y)), h);
+    vz = ddz_uv(V, jz);
+    wx = ik(w0, k_x);
+    wy = ik(w0, k_y);
+    wz = cscale(cadd(ddz_w(jz), ddz_w(jz - 1)), h);
+  }
+  if (shift && m == 0) { ub = z; vb = z; }
+  r[0] = ub; r[1] = vb; r[2] = wb; r[3] = ux; r[4] = cscale(cadd(uy, vx), h); r[5] = cscale(cadd(uz, wx), h);
+  r[6] = vy; r[7] = cscale(cadd(vz, wy), h); r[8] = wz;
+}
+template <typename CO, typename R>
+__global__ void k_lag_spec32(const C2* __restrict__ U, const C2* __restrict__ V, const C2* __restrict__ W,
+                             const C2* __restrict__ D1, const C2* __restrict__ D2, CO* out,
+                             const R* __restrict__ kx, const R* __restrict__ ky, int nk, int nz, int jz0, int nl,
+                             double idz, int shift) {
+  const size_t st = (size_t)nk * nl;
+  GSTRIDE(t, st) {
+    const int lc = (int)(t / nk);
+    const size_t m = t - (size_t)lc * nk;
+    const int jz = jz0 + lc;
+    const size_t i = (size_t)(jz - 1) * nk + m;
+    if (m == 0) {
+      double2 r[9];
+      lag_spec_point<double>(jz, m, i, U, V, W, D1, D2, 0.0, 0.0, nk, nz, idz, shift, r);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) stC(out + t + q * st, r[q]);
+    } else {
+      typename CT<R>::type r[9];
+      lag_spec_point<R>(jz, m, i, U, V, W, D1, D2, kx[m], ky[m], nk, nz, (R)idz, shift, r);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) stC(out + t + q * st, r[q]);
+    }
+  }
+}
+
+// Mixed form lagrange_Sdep.f90:142-266 products: the shift about the plane
+// mean in FP64, the products and |S| S_ij in FP32
+__global__ void k_lag_prod32(const double* __restrict__ u, const double* __restrict__ v,
+                             const double* __restrict__ w, Ptr6 Sp, float* out, int ld, int jz0, int nlev,
+                             size_t np, const C2* __restrict__ U, const C2* __restrict__ V, size_t nk) {
+  const size_t tot = np * nlev;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jz = jz0 + lc;
+    const size_t i = (size_t)(jz - 1) * np + r;
+    double ubd, vbd;
+    float wb;
+    if (jz == 1) { ubd = u[i]; vbd = v[i]; wb = 0.25f * cvt_d2f(w[i + np]); }
+    else { ubd = 0.5 * (u[i] + u[i - np]); vbd = 0.5 * (v[i] + v[i - np]); wb = cvt_d2f(w[i]); }
+    const double u0 = (jz == 1) ? U[0].x : 0.5 * (U[(size_t)(jz - 1) * nk].x + U[(size_t)(jz - 2) * nk].x);
+    const double v0 = (jz == 1) ? V[0].x : 0.5 * (V[(size_t)(jz - 1) * nk].x + V[(size_t)(jz - 2) * nk].x);
+    const float ub = cvt_d2f(ubd - u0), vb = cvt_d2f(vbd - v0);
+    const size_t stride = np * nlev;
+    float* o = out + t;
+    o[0] = ub * ub; o[stride] = ub * vb; o[2 * stride] = ub * wb;
+    o[3 * stride] = vb * vb; o[4 * stride] = vb * wb; o[5 * stride] = wb * wb;
+    const float s11 = cvt_d2f(Sp.p[0][i]), s12 = cvt_d2f(Sp.p[1][i]), s13 = cvt_d2f(Sp.p[2][i]);
+    const float s22 = cvt_d2f(Sp.p[3][i]), s23 = cvt_d2f(Sp.p[4][i]), s33 = cvt_d2f(Sp.p[5][i]);
+    const float Sm = sqrtf(2.0f * (s11 * s11 + s22 * s22 + s33 * s33 + 2.0f * (s12 * s12 + s13 * s13 + s23 * s23)));
+    o[6 * stride] = Sm * s11; o[7 * stride] = Sm * s12; o[8 * stride] = Sm * s13;
+    o[9 * stride] = Sm * s22; o[10 * stride] = Sm * s23; o[11 * stride] = Sm * s33;
+  }
+}
+
 // lagrange_Sdep.f90:142-266 physical products (12 planes per level)
 template <typename S>
 __global__ void k_lag_prod(const double* __restrict__ u, const double* __restrict__ v,
@@ -2463,10 +2623,18 @@ static int lagrangeT(les_ctx* c) {
     S* flt = tmpS + (size_t)21 * nch * g.nplane;      // 42 * nl planes
     CX* xs = (CX*)c->wsA;
     CX* sp = xs + (size_t)12 * FS;
-    k_lag_spec<CX><<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx,
+    if (MX)
+      k_lag_spec32<CX, float><<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(
+          U, V, W, c->wspec, c->wspec + g.C, sp, c->kxf, c->kyf, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz, 1);
+    else
+      k_lag_spec<CX><<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx,
                                                                   c->ky, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz,
                                                                   MX ? 1 : 0); LES_COUNT_LAUNCH();
-    k_lag_prod<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
+    if constexpr (MX)
+      k_lag_prod32<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod,
+                                                                g.ld, jz0, nl, g.nplane, U, V, g.C);
+    else
+      k_lag_prod<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
                                                               jz0, nl, g.nplane, MX ? U : nullptr, MX ? V : nullptr,
                                                               g.C); LES_COUNT_LAUNCH();
     const S* in[12];
@@ -2737,7 +2905,12 @@ static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, doub
   const Grid& g = c->g;
   const size_t FS = (size_t)g.nz * g.C;
   CX* vs = (CX*)c->wsA;
-  k_vort_spec<CX><<<grid1(FS), 256, 0, c->stream>>>(c->spec, c->spec + FS, c->spec + 2 * FS, c->wspec, c->wspec + g.C,
+  if (MX)
+    k_vort_spec32<CX, float><<<grid1(FS), 256, 0, c->stream>>>(c->spec, c->spec + FS, c->spec + 2 * FS, c->wspec,
+                                                              c->wspec + g.C, vs, vs + FS, vs + 2 * FS, c->kxf,
+                                                              c->kyf, (int)g.C, g.nz, 1.0 / g.dz);
+  else
+    k_vort_spec<CX><<<grid1(FS), 256, 0, c->stream>>>(c->spec, c->spec + FS, c->spec + 2 * FS, c->wspec, c->wspec + g.C,
                                                    vs, vs + FS, vs + 2 * FS, c->kx, c->ky, (int)g.C, g.nz,
                                                    1.0 / g.dz); LES_COUNT_LAUNCH();
   {
