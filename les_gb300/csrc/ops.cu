@@ -2395,6 +2395,32 @@ __global__ void k_dtheta_spec(const CI* __restrict__ T, const C2* __restrict__ Z
     o3[t].x = z.x; o3[t].y = z.y;
   }
 }
+// Mixed form: the same in FP32 (theta's spectrum is FP32 there); the (0,0)
+// mode, which restores the mean gradient from th0, and the wall planes' FP64
+// spectra are narrowed on the integer pipe after FP64 arithmetic
+__global__ void k_dtheta_spec32(const float2* __restrict__ T, const C2* __restrict__ Z1, const C2* __restrict__ ZN,
+                                float2* o1, float2* o2, float2* o3, const float* __restrict__ kx,
+                                const float* __restrict__ ky, int nk, int nz, double idz,
+                                const double* __restrict__ th0) {
+  GSTRIDE(t, (size_t)nk * nz) {
+    const int jz = (int)(t / nk) + 1;
+    const size_t m = t - (size_t)(jz - 1) * nk;
+    const float2 th = T[t];
+    o1[t] = ik(th, kx[m]);
+    o2[t] = ik(th, ky[m]);
+    if (jz == 1) stC(o3 + t, Z1[m]);
+    else if (jz == nz) stC(o3 + t, ZN[m]);
+    else if (m == 0) {
+      const double2 tp = make_double2(cvt_f2d(th.x), cvt_f2d(th.y));
+      const double2 tm = make_double2(cvt_f2d(T[t - nk].x), cvt_f2d(T[t - nk].y));
+      double2 z = cscale(csub(tp, tm), idz);
+      z.x += (th0[jz - 1] - th0[jz - 2]) * idz;
+      stC(o3 + t, z);
+    } else {
+      o3[t] = cscale(csub(th, T[t - nk]), (float)idz);
+    }
+  }
+}
 
 // lagrange_Sdep.f90:131-141, sgs_stag.f90:371-498 : spectra of u_bar, v_bar,
 // w_bar and S_ij (x 1/(nx*ny)) for the levels jz0..jz0+nl-1.
@@ -2864,7 +2890,11 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     plane_spectra(c, 2, pl, sc, c->wspec + 2 * g.C);
   }
   CX* ds = (CX*)c->wsA;
-  k_dtheta_spec<CX, CX><<<grid1(FS), 256, 0, c->stream>>>(specT, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds, ds + FS,
+  if constexpr (MX)
+    k_dtheta_spec32<<<grid1(FS), 256, 0, c->stream>>>(specT, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds, ds + FS,
+                                                      ds + 2 * FS, c->kxf, c->kyf, (int)g.C, nz, 1.0 / g.dz, th0);
+  else
+    k_dtheta_spec<CX, CX><<<grid1(FS), 256, 0, c->stream>>>(specT, c->wspec + 2 * g.C, c->wspec + 3 * g.C, ds, ds + FS,
                                                          ds + 2 * FS, c->kx, c->ky, (int)g.C, nz, 1.0 / g.dz,
                                                          th0); LES_COUNT_LAUNCH();
   {
