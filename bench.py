@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 step timed beside the mixed one")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--prof-family", type=int, default=0,
+                   help="transform family for the roofline object: 1 FP64/float-float y pass, 2 FP32 y pass, "
+                        "3 FP64/float-float x pass, 4 FP32 x pass (default: the form's dominant kernel)")
     return p.parse_args()
 
 
@@ -257,6 +260,10 @@ def main():
             import torch.distributed as dist
             dist.barrier()
     fam, fam_name = DOMINANT[args.form]
+    if args.prof_family:
+        fam = args.prof_family
+        fam_name = {1: "k_cols (FP64 / float-float y pass)", 2: "k_cols (FP32 y pass)",
+                    3: "k_rows (FP64 / float-float x pass)", 4: "k_rows (FP32 x pass)"}[fam]
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
@@ -272,7 +279,7 @@ def main():
     hbm, src = measured_peaks()
     n_l, ms_l, bytes_l = prof
     achieved = (bytes_l / n_l) / (ms_l / n_l / 1e3) / 1e9 if n_l else None
-    ratio = TRAFFIC_RATIO[args.form]
+    ratio = TRAFFIC_RATIO[args.form] if not args.prof_family else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm if achieved else None,
                 "traffic": (ratio * bytes_l / n_l) if (ratio and n_l and args.grid == 256) else None,
