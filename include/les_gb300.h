@@ -103,7 +103,9 @@ typedef struct les_ctx les_ctx;
  * static module storage does. */
 int les_ctx_create(const les_config* cfg, les_ctx** out);
 int les_ctx_destroy(les_ctx* ctx);
-/* 0 = per-routine array arguments are host pointers (default), 1 = device. */
+/* 0 = per-routine array arguments are host pointers (default), 1 = device
+ * pointers, each 16-byte aligned (cudaMalloc'd arrays and whole-plane offsets
+ * into them are); a misaligned one returns LES_ERR_ARG. */
 int les_ctx_set_pointer_mode(les_ctx* ctx, int device_pointers);
 /* Stream the context launches on (a cudaStream_t, passed as void*). */
 void* les_ctx_stream(les_ctx* ctx);

@@ -39,8 +39,8 @@ void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, 
   constexpr int PMAX = skn(NIN > NOUT ? NIN : NOUT);
   const size_t smf = ((size_t)(J.nin * skn(NIN) + 2 * PMAX) * TX + NIN + NOUT) * sizeof(C);
   static size_t set = 48 * 1024;
-  raise_smem(k_cols<T, TX, CIn, NIN, NOUT>, smf, set);
-  k_cols<T, TX, CIn, NIN, NOUT><<<grid, 256, smf, s>>>(J, Pin, Pout);
+  raise_smem(k_colsf<T, TX, CIn, NIN, NOUT>, smf, set);
+  k_colsf<T, TX, CIn, NIN, NOUT><<<grid, 256, smf, s>>>(J, Pin, Pout);
 }
 
 }  // namespace

@@ -65,13 +65,15 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
   for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
     const int r = NF > 0 ? t / NF : (int)P.dm.div((unsigned)t), k = t - r * m;
     const TIn* row = src + (size_t)(row0 + r) * J.ld;
+    // the pair (2k, 2k+1) in one access: rows start on even offsets
+    const typename CT<TIn>::type pr = reinterpret_cast<const typename CT<TIn>::type*>(row)[k];
     T a, b;
     if (J.off[f]) {  // subtract in double before rounding to T
-      a = cvt<T, double>(cvt<double, TIn>(row[2 * k]) - off);
-      b = cvt<T, double>(cvt<double, TIn>(row[2 * k + 1]) - off);
+      a = cvt<T, double>(cvt<double, TIn>(pr.x) - off);
+      b = cvt<T, double>(cvt<double, TIn>(pr.y) - off);
     } else {
-      a = cvt<T, TIn>(row[2 * k]);
-      b = cvt<T, TIn>(row[2 * k + 1]);
+      a = cvt<T, TIn>(pr.x);
+      b = cvt<T, TIn>(pr.y);
     }
     if (dv != (T)0) { a = a / dv; b = b / dv; }
     A[r * rs + (NF > 0 ? sk(k) : k)] = mk<T>(a * s, b * s);
@@ -142,20 +144,22 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
   const double off = J.off[f] ? J.off[f][lev] : 0.0;
   for (int t = threadIdx.x; t < nrow * (m + 1); t += blockDim.x) {
     const int r = NF > 0 ? t / (NF + 1) : (int)P.dm1.div((unsigned)t), k = t - r * (m + 1);
-    TOut* row = dst + (size_t)(row0 + r) * J.ld;
+    typename CT<TOut>::type* row = reinterpret_cast<typename CT<TOut>::type*>(dst + (size_t)(row0 + r) * J.ld);
+    typename CT<TOut>::type pw;
     if (k < m) {
       const C z = Z[r * rs + (NF > 0 ? sk(k) : k)];
       if (J.off[f]) {
-        row[2 * k] = cvt<TOut, double>(cvt<double, T>(z.x) + off);
-        row[2 * k + 1] = cvt<TOut, double>(cvt<double, T>(z.y) + off);
+        pw.x = cvt<TOut, double>(cvt<double, T>(z.x) + off);
+        pw.y = cvt<TOut, double>(cvt<double, T>(z.y) + off);
       } else {
-        row[2 * k] = cvt<TOut, T>(z.x);
-        row[2 * k + 1] = cvt<TOut, T>(z.y);
+        pw.x = cvt<TOut, T>(z.x);
+        pw.y = cvt<TOut, T>(z.y);
       }
     } else {  // padding columns ld-1:ld
-      row[2 * m] = (TOut)0;
-      row[2 * m + 1] = (TOut)0;
+      pw.x = (TOut)0;
+      pw.y = (TOut)0;
     }
+    row[k] = pw;  // the pair (2k, 2k+1) in one access
   }
 }
 
@@ -277,6 +281,140 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
   }
 }
 
+
+// Fixed-length y pass (NIN, NOUT at compile time).  Thread t owns column
+// b = t % TX of the tile and the rows r0 = t / TX + k * (256 / TX): global
+// loads and stores walk the column by pointer increments, the row map of
+// padd/unpadd follows from NIN, NOUT, and for single-input jobs the
+// coefficient code is dispatched once per output instead of per element.
+template <typename T, int CODE>
+__device__ __forceinline__ typename CT<T>::type apply_coef_ct(typename CT<T>::type v, int jx, int js,
+                                                              const ColJob& J) {
+  typedef typename CT<T>::type C;
+  const size_t ki = (size_t)jx + (size_t)J.lh * js;
+  if constexpr (CODE == CC_ONE) return v;
+  else if constexpr (CODE == CC_G) return cscale(v, Tab<T>::G(J, ki));
+  else if constexpr (CODE == CC_GG) return cscale(v, Tab<T>::GG(J, ki));
+  else if constexpr (CODE == CC_IKX) return ik(v, Tab<T>::kx(J, ki));
+  else if constexpr (CODE == CC_IKY) return ik(v, Tab<T>::ky(J, ki));
+  else if constexpr (CODE == CC_KILL) {
+    if (jx == J.lh - 1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
+    return v;
+  } else if constexpr (CODE == CC_MASK) return Tab<T>::G(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
+  else if constexpr (CODE == CC_MASK4) return Tab<T>::GG(J, ki) != (T)0 ? v : mk<T>((T)0, (T)0);
+  else return mk<T>((T)0, (T)0);
+}
+template <int NIN, int NOUT>
+__device__ __forceinline__ void row_map(int row, int nys, int& rin, int& js) {
+  if constexpr (NIN == NOUT) {
+    rin = row; js = row;
+  } else if constexpr (NOUT > NIN) {  // padd.f90:123-133
+    if (row < nys / 2) rin = row;
+    else if (row > NOUT - nys / 2) rin = row - (NOUT - nys);
+    else rin = -1;
+    js = rin;
+  } else {  // unpadd.f90:143-155
+    if (row < nys / 2) rin = row;
+    else if (row == nys / 2) rin = -1;
+    else rin = row + (NIN - nys);
+    js = row;
+  }
+}
+template <typename T, int TX, int NIN, int NOUT, int CODE>
+__device__ __forceinline__ void coef_rows(const typename CT<T>::type* __restrict__ in, typename CT<T>::type* a,
+                                          int b, int r0, int jx, bool colok, const ColJob& J) {
+  typedef typename CT<T>::type C;
+  constexpr int RS = 256 / TX;
+  for (int row = r0; row < NOUT; row += RS) {
+    int rin, js;
+    row_map<NIN, NOUT>(row, J.ny_small, rin, js);
+    C v = mk<T>((T)0, (T)0);
+    if (rin >= 0 && colok) v = apply_coef_ct<T, CODE>(in[sk(rin) * TX + b], jx, js, J);
+    a[sk(row) * TX + b] = v;
+  }
+}
+template <typename T, int TX, typename CIn, int NIN, int NOUT>
+__global__ void __launch_bounds__(256) k_colsf(ColJob J, FftPlanDev Pin, FftPlanDev Pout) {
+  typedef typename CT<T>::type C;
+  static_assert(256 % TX == 0, "tile width divides the block");
+  constexpr int RS = 256 / TX;
+  constexpr int PIN = skn(NIN), PMAX = skn(NIN > NOUT ? NIN : NOUT);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* IN = reinterpret_cast<C*>(smraw);
+  C* A = IN + J.nin * PIN * TX;
+  C* B = A + PMAX * TX;
+  C* twi = B + PMAX * TX;
+  C* two = twi + NIN;
+  for (int t = threadIdx.x; t < NIN; t += 256) twi[t] = UnitSel<T>::get(Pin, t);
+  for (int t = threadIdx.x; t < NOUT; t += 256) two[t] = UnitSel<T>::get(Pout, t);
+  const int b = threadIdx.x % TX, r0 = threadIdx.x / TX;
+  const int jx = blockIdx.x * TX + b;
+  const bool colok = jx < J.ncols;
+  const int lev = blockIdx.y;
+  for (int i = 0; i < J.nin; ++i) {
+    const CIn* src = reinterpret_cast<const CIn*>(J.in[i]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in +
+                     jx + (size_t)r0 * J.wc_in;
+    const int step = RS * J.wc_in;
+    C* xi = IN + i * PIN * TX;
+    for (int row = r0; row < NIN; row += RS, src += step) {
+      C v = mk<T>((T)0, (T)0);
+      if (colok) {
+        const CIn x = *src;
+        v = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
+      }
+      xi[sk(row) * TX + b] = v;
+    }
+  }
+  __syncthreads();
+  if (J.dir & DIR_FWD) {
+    for (int i = 0; i < J.nin; ++i) {
+      C* xi = IN + i * PIN * TX;
+      C* r = fft_ct<T, true, NIN, TX, -1, 256, CtMaxR<T>::v>(xi, A, twi, TX);
+      if (r != xi) {
+        for (int t = threadIdx.x; t < PIN * TX; t += 256) xi[t] = r[t];
+        __syncthreads();
+      }
+    }
+  }
+  for (int o = 0; o < J.nout; ++o) {
+    if (J.nin == 1) {
+      switch (J.coef[o][0]) {
+        case CC_ONE: coef_rows<T, TX, NIN, NOUT, CC_ONE>(IN, A, b, r0, jx, colok, J); break;
+        case CC_G: coef_rows<T, TX, NIN, NOUT, CC_G>(IN, A, b, r0, jx, colok, J); break;
+        case CC_GG: coef_rows<T, TX, NIN, NOUT, CC_GG>(IN, A, b, r0, jx, colok, J); break;
+        case CC_IKX: coef_rows<T, TX, NIN, NOUT, CC_IKX>(IN, A, b, r0, jx, colok, J); break;
+        case CC_IKY: coef_rows<T, TX, NIN, NOUT, CC_IKY>(IN, A, b, r0, jx, colok, J); break;
+        case CC_KILL: coef_rows<T, TX, NIN, NOUT, CC_KILL>(IN, A, b, r0, jx, colok, J); break;
+        case CC_MASK: coef_rows<T, TX, NIN, NOUT, CC_MASK>(IN, A, b, r0, jx, colok, J); break;
+        case CC_MASK4: coef_rows<T, TX, NIN, NOUT, CC_MASK4>(IN, A, b, r0, jx, colok, J); break;
+        default: coef_rows<T, TX, NIN, NOUT, CC_NONE>(IN, A, b, r0, jx, colok, J); break;
+      }
+    } else {
+      for (int row = r0; row < NOUT; row += RS) {
+        int rin, js;
+        row_map<NIN, NOUT>(row, J.ny_small, rin, js);
+        C acc = mk<T>((T)0, (T)0);
+        if (rin >= 0 && colok) {
+          for (int i = 0; i < J.nin; ++i) {
+            const int code = J.coef[o][i];
+            if (code != CC_NONE) acc = cadd(acc, apply_coef<T>(code, IN[i * PIN * TX + sk(rin) * TX + b], jx, js, J));
+          }
+        }
+        A[sk(row) * TX + b] = acc;
+      }
+    }
+    __syncthreads();
+    C* r = A;
+    if ((J.inv_mask >> o) & 1u) r = fft_ct<T, true, NOUT, TX, +1, 256, CtMaxR<T>::v>(A, B, two, TX);
+    if (colok) {
+      C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out + jx +
+               (size_t)r0 * J.wc_out;
+      const int step = RS * J.wc_out;
+      for (int row = r0; row < NOUT; row += RS, dst += step) *dst = r[sk(row) * TX + b];
+    }
+    __syncthreads();
+  }
+}
 
 // rows per CTA of the x-pass kernels (default when a job gives none)
 template <typename T>

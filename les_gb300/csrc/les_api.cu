@@ -775,15 +775,24 @@ struct Arg {
   size_t n;
   bool owned = false;
   Arg(les_ctx* c_, const void* u, size_t n_) : c(c_), user(u), n(n_) {}
+  // caller device arrays are read and written as pairs of doubles (16 bytes)
+  int take_user() {
+    if (reinterpret_cast<uintptr_t>(user) & 15u) {
+      les_set_error("device array %p is not 16-byte aligned", user);
+      return LES_ERR_ARG;
+    }
+    dev = (double*)user;
+    return 0;
+  }
   int in() {
-    if (c->ptr_mode) { dev = (double*)user; return 0; }
+    if (c->ptr_mode) return take_user();
     if (cudaMalloc(&dev, n * sizeof(double)) != cudaSuccess) { les_set_error("staging alloc failed"); return LES_ERR_OOM; }
     owned = true;
     if (cudaMemcpyAsync(dev, user, n * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) return LES_ERR_CUDA;
     return 0;
   }
   int alloc() {
-    if (c->ptr_mode) { dev = (double*)user; return 0; }
+    if (c->ptr_mode) return take_user();
     if (cudaMalloc(&dev, n * sizeof(double)) != cudaSuccess) { les_set_error("staging alloc failed"); return LES_ERR_OOM; }
     owned = true;
     cudaMemsetAsync(dev, 0, n * sizeof(double), c->stream);
