@@ -1754,9 +1754,15 @@ __device__ __forceinline__ void tridiag_mode(int t, const HC* __restrict__ Hx, c
 
 // The same solve with two threads per mode: part 0 the real, part 1 the
 // imaginary part of p-hat (a, b, c are real, so the two recurrences are
-// independent), each load issued one level ahead; the arithmetic and its
+// independent), each load issued four levels ahead; the arithmetic and its
 // order are those of tridiag_mode.  The kx = ky = 0 and Nyquist modes run
 // tridiag_mode on part 0.
+// Mixed form (float-float spectra): the right-hand side
+// -(kx Hx + ky Hy) + (Hz(k) - Hz(k-1))/dz is formed in float-float on the
+// FP32 pipe (the inputs carry float-float precision), the recurrences run in
+// FP64, and the forward sweep parks its FP64 value in the 8-byte float-float
+// slot of p-hat that the back sweep reads and overwrites, so each level
+// costs five FP64 instructions instead of fourteen.
 template <typename HC> __device__ __forceinline__ double ld1(const HC* p, size_t i, int comp);
 template <> __device__ __forceinline__ double ld1<double2>(const double2* p, size_t i, int comp) {
   return reinterpret_cast<const double*>(p)[2 * i + comp];
@@ -1770,12 +1776,23 @@ __device__ __forceinline__ void st1(double2* p, size_t i, int comp, double v) {
 __device__ __forceinline__ void st1(dcomplex* p, size_t i, int comp, double v) {
   reinterpret_cast<dfloat*>(p)[2 * i + comp] = cvt<dfloat>(v);
 }
+__device__ __forceinline__ dfloat ldf(const dcomplex* p, size_t i, int comp) {
+  return reinterpret_cast<const dfloat*>(p)[2 * i + comp];
+}
+// an FP64 value parked in the 8-byte slot of one float-float component
+__device__ __forceinline__ void st_park(dcomplex* p, size_t i, int comp, double v) {
+  reinterpret_cast<double*>(p)[2 * i + comp] = v;
+}
+__device__ __forceinline__ double ld_park(const dcomplex* p, size_t i, int comp) {
+  return reinterpret_cast<const double*>(p)[2 * i + comp];
+}
 template <typename HC, typename PC>
 __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, const HC* __restrict__ Hy,
                                                   const HC* __restrict__ Hz, const C2* __restrict__ bot,
                                                   const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
                                                   const double* __restrict__ gam, const double* __restrict__ kx,
-                                                  const double* __restrict__ ky, int lh, int ny, int nz, double dz) {
+                                                  const double* __restrict__ ky, const float2* __restrict__ kxd,
+                                                  const float2* __restrict__ kyd, int lh, int ny, int nz, double dz) {
   const int nk = lh * ny;
   const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = g2 >> 1, part = g2 & 1;
@@ -1787,73 +1804,143 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
   }
   const size_t NK = (size_t)nk;
   const int ch = part == 0 ? 1 : 0;  // component of Hx, Hy feeding this part
-  const double k_x = kx[t], k_y = ky[t];
-  const double idz2 = 1.0 / (dz * dz), idz = 1.0 / dz;
   const int n = nz + 1;
   const C2 b1 = bot[t];
   double up = (-dz * (part == 0 ? b1.x : b1.y)) * ibet[t];
-  st1(P, t, part, up);
-  double hz0 = ld1<HC>(Hz, t, part);
-  // level j's inputs in ring slot (j - 2) % 4, loaded four levels ahead
   constexpr int D = 4;
-  double bx[D], by[D], bz[D], bi[D];
-  auto load = [&](int j, double& x, double& y, double& z, double& ib) {
-    if (j <= n) ib = ibet[(size_t)(j - 1) * NK + t];
-    if (j <= nz) {
-      x = ld1<HC>(Hx, (size_t)(j - 2) * NK + t, ch);
-      y = ld1<HC>(Hy, (size_t)(j - 2) * NK + t, ch);
-    }
-    z = (j <= nz - 1) ? ld1<HC>(Hz, (size_t)(j - 1) * NK + t, part) : 0.0;
-  };
+  if constexpr (std::is_same<HC, dcomplex>::value && std::is_same<PC, dcomplex>::value) {
+    const dfloat k_x(kxd[t].x, kxd[t].y), k_y(kyd[t].x, kyd[t].y);
+    const dfloat idzf(1.0 / dz);
+    const double idz2 = 1.0 / (dz * dz);
+    st_park(P, t, part, up);
+    dfloat hz0 = ldf(Hz, t, part);
+    const dfloat zero(0.f, 0.f);
+    // level j's inputs in ring slot (j - 2) % 4, loaded four levels ahead
+    dfloat bx[D], by[D], bz[D];
+    double bi[D];
+    auto load = [&](int j, dfloat& x, dfloat& y, dfloat& z, double& ib) {
+      if (j <= n) ib = ibet[(size_t)(j - 1) * NK + t];
+      if (j <= nz) {
+        x = ldf(Hx, (size_t)(j - 2) * NK + t, ch);
+        y = ldf(Hy, (size_t)(j - 2) * NK + t, ch);
+      }
+      z = (j <= nz - 1) ? ldf(Hz, (size_t)(j - 1) * NK + t, part) : zero;
+    };
 #pragma unroll
-  for (int q = 0; q < D; ++q) load(2 + q, bx[q], by[q], bz[q], bi[q]);
-  for (int jb = 2; jb <= n; jb += D) {
+    for (int q = 0; q < D; ++q) load(2 + q, bx[q], by[q], bz[q], bi[q]);
+    for (int jb = 2; jb <= n; jb += D) {
 #pragma unroll
-    for (int q = 0; q < D; ++q) {
-      const int j = jb + q;
-      if (j <= n) {
-        const double hx = bx[q], hy = by[q], hz1 = bz[q], ib = bi[q];
-        load(j + D, bx[q], by[q], bz[q], bi[q]);
-        double a, r;
-        if (j <= nz) {
-          a = idz2;
-          const double s = k_x * hx + k_y * hy;
-          // the FP64 form divides as the reference does; the mixed form
-          // multiplies by 1/dz
-          const double dh = std::is_same<HC, dcomplex>::value ? (hz1 - hz0) * idz : (hz1 - hz0) / dz;
-          r = part == 0 ? -s + dh : s + dh;
-          hz0 = hz1;
-        } else {
-          a = -1.0;
-          const C2 tp = top[t];
-          r = -(part == 0 ? tp.x : tp.y) * dz;
+      for (int q = 0; q < D; ++q) {
+        const int j = jb + q;
+        if (j <= n) {
+          const dfloat hx = bx[q], hy = by[q], hz1 = bz[q];
+          const double ib = bi[q];
+          load(j + D, bx[q], by[q], bz[q], bi[q]);
+          double u;
+          if (j <= nz) {
+            const dfloat sxy = k_x * hx + k_y * hy;
+            const dfloat dh = (hz1 - hz0) * idzf;
+            const double r = cvt<double>(part == 0 ? dh - sxy : sxy + dh);
+            hz0 = hz1;
+            u = (r - idz2 * up) * ib;
+          } else {
+            const C2 tp = top[t];
+            const double r = -(part == 0 ? tp.x : tp.y) * dz;
+            u = (r + up) * ib;
+          }
+          if (j < n) st_park(P, (size_t)(j - 1) * NK + t, part, u);
+          else st1(P, (size_t)(j - 1) * NK + t, part, u);  // level n: final (the back sweep starts below it)
+          up = u;
         }
-        const double u = (r - a * up) * ib;
-        st1(P, (size_t)(j - 1) * NK + t, part, u);
-        up = u;
       }
     }
-  }
-  // back substitution, level j's gamma and forward value in slot (n-1-j) % 4
-  double bg[D], bp[D];
-  auto loadb = [&](int j, double& g, double& pv) {
-    if (j >= 1) {
-      g = gam[(size_t)j * NK + t];
-      pv = ld1<PC>(P, (size_t)(j - 1) * NK + t, part);
-    }
-  };
-#pragma unroll
-  for (int q = 0; q < D; ++q) loadb(n - 1 - q, bg[q], bp[q]);
-  for (int jb = n - 1; jb >= 1; jb -= D) {
-#pragma unroll
-    for (int q = 0; q < D; ++q) {
-      const int j = jb - q;
+    // back substitution, level j's gamma and parked forward value in slot (n-1-j) % 4
+    double bg[D], bp[D];
+    auto loadb = [&](int j, double& g, double& pv) {
       if (j >= 1) {
-        const double gm = bg[q], pv = bp[q];
-        loadb(j - D, bg[q], bp[q]);
-        const double u = pv - gm * up;
-        st1(P, (size_t)(j - 1) * NK + t, part, u);
-        up = u;
+        g = gam[(size_t)j * NK + t];
+        pv = ld_park(P, (size_t)(j - 1) * NK + t, part);
+      }
+    };
+#pragma unroll
+    for (int q = 0; q < D; ++q) loadb(n - 1 - q, bg[q], bp[q]);
+    for (int jb = n - 1; jb >= 1; jb -= D) {
+#pragma unroll
+      for (int q = 0; q < D; ++q) {
+        const int j = jb - q;
+        if (j >= 1) {
+          const double gm = bg[q], pv = bp[q];
+          loadb(j - D, bg[q], bp[q]);
+          const double u = pv - gm * up;
+          st1(P, (size_t)(j - 1) * NK + t, part, u);
+          up = u;
+        }
+      }
+    }
+    return;
+  } else {
+    const double k_x = kx[t], k_y = ky[t];
+    const double idz2 = 1.0 / (dz * dz);
+    st1(P, t, part, up);
+    double hz0 = ld1<HC>(Hz, t, part);
+    // level j's inputs in ring slot (j - 2) % 4, loaded four levels ahead
+    double bx[D], by[D], bz[D], bi[D];
+    auto load = [&](int j, double& x, double& y, double& z, double& ib) {
+      if (j <= n) ib = ibet[(size_t)(j - 1) * NK + t];
+      if (j <= nz) {
+        x = ld1<HC>(Hx, (size_t)(j - 2) * NK + t, ch);
+        y = ld1<HC>(Hy, (size_t)(j - 2) * NK + t, ch);
+      }
+      z = (j <= nz - 1) ? ld1<HC>(Hz, (size_t)(j - 1) * NK + t, part) : 0.0;
+    };
+#pragma unroll
+    for (int q = 0; q < D; ++q) load(2 + q, bx[q], by[q], bz[q], bi[q]);
+    for (int jb = 2; jb <= n; jb += D) {
+#pragma unroll
+      for (int q = 0; q < D; ++q) {
+        const int j = jb + q;
+        if (j <= n) {
+          const double hx = bx[q], hy = by[q], hz1 = bz[q], ib = bi[q];
+          load(j + D, bx[q], by[q], bz[q], bi[q]);
+          double a, r;
+          if (j <= nz) {
+            a = idz2;
+            const double s = k_x * hx + k_y * hy;
+            const double dh = (hz1 - hz0) / dz;  // divides as the reference does
+            r = part == 0 ? -s + dh : s + dh;
+            hz0 = hz1;
+          } else {
+            a = -1.0;
+            const C2 tp = top[t];
+            r = -(part == 0 ? tp.x : tp.y) * dz;
+          }
+          const double u = (r - a * up) * ib;
+          st1(P, (size_t)(j - 1) * NK + t, part, u);
+          up = u;
+        }
+      }
+    }
+    // back substitution, level j's gamma and forward value in slot (n-1-j) % 4
+    double bg[D], bp[D];
+    auto loadb = [&](int j, double& g, double& pv) {
+      if (j >= 1) {
+        g = gam[(size_t)j * NK + t];
+        pv = ld1<PC>(P, (size_t)(j - 1) * NK + t, part);
+      }
+    };
+#pragma unroll
+    for (int q = 0; q < D; ++q) loadb(n - 1 - q, bg[q], bp[q]);
+    for (int jb = n - 1; jb >= 1; jb -= D) {
+#pragma unroll
+      for (int q = 0; q < D; ++q) {
+        const int j = jb - q;
+        if (j >= 1) {
+          const double gm = bg[q], pv = bp[q];
+          loadb(j - D, bg[q], bp[q]);
+          const double u = pv - gm * up;
+          st1(P, (size_t)(j - 1) * NK + t, part, u);
+          up = u;
+        }
       }
     }
   }
@@ -1935,7 +2022,7 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
   }
   k_tridiag2<CX, CX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
       H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky,
-      g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
+      c->kxd, c->kyd, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
