@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--grid", type=int, default=256)
+    p.add_argument("--levels", type=int, default=None,
+                   help="uvp levels (default: the grid size); fewer make small ncu captures")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 step timed beside the mixed one")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -132,8 +134,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+LEVELS = None  # --levels: uvp levels when not the grid size (small profiling captures)
+
+
 def workload_config(lg, grid, form):
-    cfg = lg.make_config(grid, s_flag=1, precision=1 if form == "mixed" else 0, rmsdiv_every=0)
+    cfg = lg.make_config(grid, nz_levels=LEVELS, s_flag=1, precision=1 if form == "mixed" else 0,
+                         rmsdiv_every=0)
     surf = lg.striped_surface(cfg)
     return cfg, surf
 
@@ -232,7 +238,9 @@ def timed_steps(torch, lg, ctx, steps, prof_family=None):
 
 
 def main():
+    global LEVELS
     args = parse()
+    LEVELS = args.levels
     if args.impl == "reference":
         run_reference(args)
         return
@@ -282,7 +290,7 @@ def main():
     ratio = TRAFFIC_RATIO[args.form] if not args.prof_family else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm if achieved else None,
-                "traffic": (ratio * bytes_l / n_l) if (ratio and n_l and args.grid == 256) else None,
+                "traffic": (ratio * bytes_l / n_l) if (ratio and n_l and args.grid == 256 and LEVELS is None) else None,
                 "peak_source": src, "kernel": fam_name, "launches_timed": n_l,
                 "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                 "algorithmic_bytes_per_launch": bytes_l / n_l if n_l else None}

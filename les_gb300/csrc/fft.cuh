@@ -242,6 +242,43 @@ template <typename C, typename T> __device__ __forceinline__ void dft16(C* v, in
   }
 }
 
+// natural-order DFT12 (n = a + 4b: four DFT3 over b, twiddles W12^(ac),
+// three DFT4 over a; output k = c + 3d)
+template <typename C, typename T> __device__ __forceinline__ void dft12(C* v, int sign) {
+  const T h = (T)0.5;
+  const T s3 = (T)0.86602540378443864676372317075294;  // sin(pi/3)
+  const T gh = sign < 0 ? -h : h, gs3 = sign < 0 ? -s3 : s3;
+  C t[4][3];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    t[a][0] = v[a]; t[a][1] = v[a + 4]; t[a][2] = v[a + 8];
+    dft3<C, T>(t[a], sign);
+  }
+  t[1][1] = cmulc(t[1][1], s3, gh);   // W12^1
+  t[1][2] = cmulc(t[1][2], h, gs3);   // W12^2
+  t[2][1] = cmulc(t[2][1], h, gs3);   // W12^2
+  t[2][2] = cmulc(t[2][2], -h, gs3);  // W12^4
+  t[3][1] = sign < 0 ? cmulmi(t[3][1]) : cmuli(t[3][1]);  // W12^3
+  t[3][2].x = -t[3][2].x; t[3][2].y = -t[3][2].y;         // W12^6
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    C u[4] = {t[0][c], t[1][c], t[2][c], t[3][c]};
+    dft4(u, sign);
+    v[c] = u[0]; v[c + 3] = u[1]; v[c + 6] = u[2]; v[c + 9] = u[3];
+  }
+}
+// natural-order DFT of a compile-time length in registers
+template <typename T, int N> __device__ __forceinline__ void dft_n(typename CT<T>::type* v, int sign) {
+  typedef typename CT<T>::type C;
+  if constexpr (N == 16) dft16<C, T>(v, sign);
+  else if constexpr (N == 12) dft12<C, T>(v, sign);
+  else if constexpr (N == 8) dft8<C, T>(v, sign);
+  else if constexpr (N == 4) dft4(v, sign);
+  else if constexpr (N == 3) dft3<C, T>(v, sign);
+  else if constexpr (N == 2) dft2(v);
+  else static_assert(N == 1, "register DFT length");
+}
+
 // One pass.  COLS: element (b, i) at x[sk(i) * NB + b]; rows: x[b * skn(N)
 // + sk(i)] for nbr batches.  SIGN -1 forward, +1 inverse (conjugated
 // twiddles); tw: the unit-circle table of length N.

@@ -15,9 +15,32 @@ void raise_smem(K kernel, size_t sm, size_t& set) {
   }
 }
 
+// register-resident x pass (FP32): factors (N1, N2) of the half length M,
+// 0 when the length has none
+template <int M> struct RowSplit { static constexpr int n1 = 0, n2 = 0; };
+template <> struct RowSplit<32> { static constexpr int n1 = 8, n2 = 4; };
+template <> struct RowSplit<48> { static constexpr int n1 = 16, n2 = 3; };
+template <> struct RowSplit<128> { static constexpr int n1 = 16, n2 = 8; };
+template <> struct RowSplit<192> { static constexpr int n1 = 16, n2 = 12; };
+template <typename T, int N1, int N2>
+struct RegRows {
+  static constexpr int TT = N1 > N2 ? N1 : N2;
+  static constexpr int RPB = 256 / TT, NT = RPB * TT, M = N1 * N2;
+  static size_t smem() { return (size_t)(RPB * N2 * (N1 + 1) + 2 * M + 1) * sizeof(typename CT<T>::type); }
+};
+
 template <typename T, typename TIn, int NF>
 void r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
   typedef typename CT<T>::type C;
+  constexpr int N1 = RowSplit<NF>::n1, N2 = RowSplit<NF>::n2;
+  if constexpr (N1 > 0 && std::is_same<T, float>::value) {
+    typedef RegRows<T, N1, N2> G;
+    static size_t set = 48 * 1024;
+    raise_smem(k_r2c_reg<T, TIn, N1, N2, G::NT>, G::smem(), set);
+    const dim3 grid((J.ny + G::RPB - 1) / G::RPB, J.nlev, J.nfield);
+    k_r2c_reg<T, TIn, N1, N2, G::NT><<<grid, G::NT, G::smem(), s>>>(J, P);
+    return;
+  }
   const size_t smf = ((size_t)2 * rpc * skn(NF) + 2 * NF + 1) * sizeof(C);
   static size_t set = 48 * 1024;
   raise_smem(k_rows_r2c<T, TIn, NF>, smf, set);
@@ -27,15 +50,45 @@ void r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
 template <typename T, typename TOut, int NF>
 void c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
   typedef typename CT<T>::type C;
+  constexpr int N1 = RowSplit<NF>::n1, N2 = RowSplit<NF>::n2;
+  if constexpr (N1 > 0 && std::is_same<T, float>::value) {
+    typedef RegRows<T, N1, N2> G;
+    static size_t set = 48 * 1024;
+    raise_smem(k_c2r_reg<T, TOut, N1, N2, G::NT>, G::smem(), set);
+    const dim3 grid((J.ny + G::RPB - 1) / G::RPB, J.nlev, J.nfield);
+    k_c2r_reg<T, TOut, N1, N2, G::NT><<<grid, G::NT, G::smem(), s>>>(J, P);
+    return;
+  }
   const size_t smf = ((size_t)rpc * (NF + 1) + (size_t)2 * rpc * skn(NF) + 2 * NF + 1) * sizeof(C);
   static size_t set = 48 * 1024;
   raise_smem(k_rows_c2r<T, TOut, NF>, smf, set);
   const dim3 grid((J.ny + rpc - 1) / rpc, J.nlev, J.nfield);
   k_rows_c2r<T, TOut, NF><<<grid, 256, smf, s>>>(J, P, rpc);
 }
+// register-resident y pass (FP32, one input, same length N = R * R), 16 kx
+// columns per CTA.  The float-float transforms keep the shared-memory
+// kernels: their arithmetic is heavy enough that the idle lanes and the
+// register pressure of the register-resident form cost more than they save.
+template <typename T, typename CIn, int R>
+void cols_reg(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
+  typedef typename CT<T>::type C;
+  constexpr int TX = 16, N = R * R;
+  const size_t smf = (size_t)(N * TX + N) * sizeof(C);
+  static size_t set = 48 * 1024;
+  raise_smem(k_colsr<T, TX, CIn, R>, smf, set);
+  const dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
+  k_colsr<T, TX, CIn, R><<<grid, TX * R, smf, s>>>(J, P);
+}
+
 template <typename T, int TX, typename CIn, int NIN, int NOUT>
 void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, dim3 grid, cudaStream_t s) {
   typedef typename CT<T>::type C;
+  if constexpr (NIN == NOUT && (NIN == 256 || NIN == 64) && std::is_same<T, float>::value) {
+    if (J.nin == 1 && J.map == MAP_SAME) {
+      cols_reg<T, CIn, NIN == 256 ? 16 : 8>(J, Pin, s);
+      return;
+    }
+  }
   constexpr int PMAX = skn(NIN > NOUT ? NIN : NOUT);
   const size_t smf = ((size_t)(J.nin * skn(NIN) + 2 * PMAX) * TX + NIN + NOUT) * sizeof(C);
   static size_t set = 48 * 1024;

@@ -164,6 +164,179 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
 }
 
 // ---------------------------------------------------------------------------
+// Register-resident x pass, half length M = N1 * N2.  A row is served by
+// TT = max(N1, N2) threads.  Forward (r2c): n = n1 + N1 n2, k = k2 + N2 k1;
+// thread n1 loads the pairs z[n1 + N1 n2] straight from the row, DFT_N2 in
+// registers, twiddle W_M^(n1 k2), one exchange through shared memory
+// (element (n1, k2) at k2 (N1 + 1) + n1: conflict-free both ways), DFT_N1 in
+// registers; the Hermitian post-processing pairs Z[k] with Z[M - k] through a
+// second, natural-order trip.  Inverse (c2r): thread k1 forms the
+// pre-processed A[k1 + N1 k2] from X[k] and X[M - k] read from the work
+// buffer, inverse DFT_N2, twiddle, exchange, inverse DFT_N1, and thread n2
+// writes the real pairs n2 + N2 n1 of the row.
+template <typename T, typename TIn, int N1, int N2, int NT>
+__global__ void __launch_bounds__(NT) k_r2c_reg(RowJob J, RealPlanDev P) {
+  typedef typename CT<T>::type C;
+  typedef typename CT<TIn>::type CI;
+  constexpr int M = N1 * N2, TT = N1 > N2 ? N1 : N2, RPB = NT / TT, MS = N2 * (N1 + 1);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // RPB rows x MS
+  C* tw = S + RPB * MS;                // exp(-2 pi i j / M), j < M
+  C* wr = tw + M;                      // exp(-2 pi i k / nx), k <= M
+  for (int t = threadIdx.x; t < M; t += NT) tw[t] = UnitSel<T>::get(P.c, t);
+  for (int t = threadIdx.x; t <= M; t += NT) wr[t] = rw<T>(P, t);
+  const int q = threadIdx.x % TT, r = threadIdx.x / TT;
+  const int f = blockIdx.z, lev = blockIdx.y;
+  const int row = blockIdx.x * RPB + r;
+  const bool rowok = r < RPB && row < J.ny;
+  C* Sr = S + (r < RPB ? r : 0) * MS;
+  C v[TT];
+  if (q < N1) {
+    const T s = (T)J.scale[f];
+    const T dv = (T)J.div[f];
+    const bool hasoff = J.off[f] != nullptr;
+    const double off = hasoff ? J.off[f][lev] : 0.0;
+    const CI* src = reinterpret_cast<const CI*>(reinterpret_cast<const TIn*>(J.phys[f]) +
+                                                (size_t)lev * J.pstride_phys + (size_t)(rowok ? row : 0) * J.ld) + q;
+#pragma unroll
+    for (int i = 0; i < N2; ++i) {
+      v[i] = mk<T>((T)0, (T)0);
+      if (rowok) {
+        const CI pr = src[N1 * i];
+        T a, b;
+        if (hasoff) {  // subtract in double before rounding to T
+          a = cvt<T, double>(cvt<double, TIn>(pr.x) - off);
+          b = cvt<T, double>(cvt<double, TIn>(pr.y) - off);
+        } else {
+          a = cvt<T, TIn>(pr.x);
+          b = cvt<T, TIn>(pr.y);
+        }
+        if (dv != (T)0) { a = a / dv; b = b / dv; }
+        v[i] = mk<T>(a * s, b * s);
+      }
+    }
+  }
+  __syncthreads();  // tables
+  if (q < N1) {
+    dft_n<T, N2>(v, -1);  // over n2: v[i] = y[n1 = q][k2 = i]
+#pragma unroll
+    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], tw[q * i]);
+    if (r < RPB) {
+#pragma unroll
+      for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + q] = v[i];
+    }
+  }
+  __syncthreads();
+  if (q < N2 && r < RPB) {
+#pragma unroll
+    for (int i = 0; i < N1; ++i) v[i] = Sr[q * (N1 + 1) + i];
+    dft_n<T, N1>(v, -1);  // over n1: v[i] = Z[q + N2 i]
+  }
+  __syncthreads();
+  if (q < N2 && r < RPB) {
+#pragma unroll
+    for (int i = 0; i < N1; ++i) Sr[q + N2 * i] = v[i];  // natural order
+  }
+  __syncthreads();
+  if (q < N2 && rowok) {
+    C* out = reinterpret_cast<C*>(J.work[f]) + (size_t)lev * J.pstride_work + (size_t)row * J.wc;
+    const int nc = J.ncols;
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      const int k = q + N2 * i;
+      const C a = v[i];
+      C X;
+      if (k == 0) {
+        X = mk<T>(a.x + a.y, (T)0);
+        if (M < nc) out[M] = mk<T>(a.x - a.y, (T)0);
+      } else {
+        const C b = cconj(Sr[M - k]);
+        const C e = cscale(cadd(a, b), (T)0.5);
+        const C d = cscale(csub(a, b), (T)0.5);
+        X = cadd(e, cmul(wr[k], cmulmi(d)));  // (d / i) x exp(-2 pi i k / nx)
+      }
+      if (k < nc) out[k] = X;
+    }
+  }
+}
+
+template <typename T, typename TOut, int N1, int N2, int NT>
+__global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
+  typedef typename CT<T>::type C;
+  typedef typename CT<TOut>::type CO;
+  constexpr int M = N1 * N2, TT = N1 > N2 ? N1 : N2, RPB = NT / TT, MS = N2 * (N1 + 1);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // RPB rows x MS
+  C* tw = S + RPB * MS;                // exp(-2 pi i j / M), j < M
+  C* wr = tw + M;                      // exp(-2 pi i k / nx), k <= M
+  for (int t = threadIdx.x; t < M; t += NT) tw[t] = UnitSel<T>::get(P.c, t);
+  for (int t = threadIdx.x; t <= M; t += NT) wr[t] = rw<T>(P, t);
+  const int q = threadIdx.x % TT, r = threadIdx.x / TT;
+  const int f = blockIdx.z, lev = blockIdx.y;
+  const int row = blockIdx.x * RPB + r;
+  const bool rowok = r < RPB && row < J.ny;
+  C* Sr = S + (r < RPB ? r : 0) * MS;
+  C v[TT];
+  __syncthreads();  // tables
+  if (q < N1) {
+    const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work +
+                  (size_t)(rowok ? row : 0) * J.wc;
+    const int nc = J.ncols;
+#pragma unroll
+    for (int i = 0; i < N2; ++i) {
+      const int k = q + N1 * i, km = M - k;
+      C a = mk<T>((T)0, (T)0), bb = mk<T>((T)0, (T)0);
+      if (rowok) {
+        if (k < nc) a = in[k];
+        if (km < nc) bb = in[km];
+      }
+      if (k == 0) { a.y = (T)0; bb.y = (T)0; }  // the halfcomplex pass ignores Im of X[0], X[M]
+      const C b = cconj(bb);
+      const C e = cadd(a, b);
+      const C d = cmul(csub(a, b), cconj(wr[k]));  // x exp(+2 pi i k / nx)
+      v[i] = cadd(e, cmuli(d));
+    }
+    dft_n<T, N2>(v, +1);  // over k2: v[i] = y[k1 = q][n2 = i]
+#pragma unroll
+    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(tw[q * i]));
+    if (r < RPB) {
+#pragma unroll
+      for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + q] = v[i];
+    }
+  }
+  __syncthreads();
+  if (q < N2 && rowok) {
+#pragma unroll
+    for (int i = 0; i < N1; ++i) v[i] = Sr[q * (N1 + 1) + i];
+    dft_n<T, N1>(v, +1);  // over k1: v[i] = z[q + N2 i]
+    TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys +
+                (size_t)row * J.ld;
+    CO* pairs = reinterpret_cast<CO*>(dst);
+    const bool hasoff = J.off[f] != nullptr;
+    const double off = hasoff ? J.off[f][lev] : 0.0;
+#pragma unroll
+    for (int i = 0; i < N1; ++i) {
+      const C z = v[i];
+      CO pw;
+      if (hasoff) {
+        pw.x = cvt<TOut, double>(cvt<double, T>(z.x) + off);
+        pw.y = cvt<TOut, double>(cvt<double, T>(z.y) + off);
+      } else {
+        pw.x = cvt<TOut, T>(z.x);
+        pw.y = cvt<TOut, T>(z.y);
+      }
+      pairs[q + N2 * i] = pw;
+    }
+    if (q == 0) {  // padding columns ld-1:ld
+      CO pz;
+      pz.x = (TOut)0;
+      pz.y = (TOut)0;
+      pairs[M] = pz;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // cols: y-transform of TX kx columns per CTA, all fields of the job.
 // grid = (ceil(ncols/TX), nlev, nf)
 template <typename T>
@@ -413,6 +586,95 @@ __global__ void __launch_bounds__(256) k_colsf(ColJob J, FftPlanDev Pin, FftPlan
       for (int row = r0; row < NOUT; row += RS, dst += step) *dst = r[sk(row) * TX + b];
     }
     __syncthreads();
+  }
+}
+
+// Register-resident y pass for one input and same-length outputs, N = R * R
+// (R = 16: 256 points; R = 8: 64).  Four-step split n = n1 + R n2,
+// k = k2 + R k1: thread q of a column holds the R elements x[q + R i]
+// (n1 = q) or X[q + R i] (k2 = q), so global loads and stores touch rows
+// q + R i in both layouts.  Forward: DFT_R over n2 in registers, twiddle
+// W_N^(n1 k2), one exchange through shared memory, DFT_R over n1; the
+// spectrum then sits in registers, the coefficient of each output is
+// applied there, and the inverse runs the same steps in reverse order
+// (DFT_R over k1, twiddle, exchange, DFT_R over k2).  Two trips through
+// shared memory per transform instead of one per radix pass; every thread
+// has its R loads in flight at once.
+template <typename T, int R>
+__device__ __forceinline__ void dft_r(typename CT<T>::type* v, int sign) {
+  typedef typename CT<T>::type C;
+  if constexpr (R == 16) dft16<C, T>(v, sign);
+  else if constexpr (R == 8) dft8<C, T>(v, sign);
+  else dft4(v, sign);
+}
+template <typename T, int R, int CODE>
+__device__ __forceinline__ void coef_reg(typename CT<T>::type* y, const typename CT<T>::type* v, int q, int jx,
+                                         bool colok, const ColJob& J) {
+#pragma unroll
+  for (int i = 0; i < R; ++i) y[i] = colok ? apply_coef_ct<T, CODE>(v[i], jx, q + R * i, J) : mk<T>((T)0, (T)0);
+}
+template <typename T, int TX, typename CIn, int R>
+__global__ void __launch_bounds__(TX * R, (sizeof(T) == 4 && R == 16) ? 2 : 1) k_colsr(ColJob J, FftPlanDev P) {
+  typedef typename CT<T>::type C;
+  constexpr int N = R * R;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // exchange: element (i, q) of column b at (i * R + q) * TX + b
+  C* tw = S + N * TX;                  // exp(-2 pi i m / N), m < N
+  for (int t = threadIdx.x; t < N; t += TX * R) tw[t] = UnitSel<T>::get(P, t);
+  const int b = threadIdx.x % TX, q = threadIdx.x / TX;
+  const int jx = blockIdx.x * TX + b;
+  const bool colok = jx < J.ncols;
+  const int lev = blockIdx.y;
+  C v[R];
+  {
+    const CIn* src = reinterpret_cast<const CIn*>(J.in[0]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in +
+                     jx + (size_t)q * J.wc_in;
+    const size_t step = (size_t)R * J.wc_in;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      v[i] = mk<T>((T)0, (T)0);
+      if (colok) {
+        const CIn x = src[i * step];
+        v[i] = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
+      }
+    }
+  }
+  __syncthreads();  // twiddle table
+  if (J.dir & DIR_FWD) {
+    dft_r<T, R>(v, -1);  // over n2: v[i] = y[n1 = q][k2 = i]
+#pragma unroll
+    for (int i = 1; i < R; ++i) v[i] = cmul(v[i], tw[q * i]);
+#pragma unroll
+    for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = S[(q * R + i) * TX + b];  // y[n1 = i][k2 = q]
+    dft_r<T, R>(v, -1);  // over n1: v[i] = X[q + R i]
+  }
+  for (int o = 0; o < J.nout; ++o) {
+    C y[R];
+    const int code = J.coef[o][0];
+#pragma unroll
+    for (int i = 0; i < R; ++i) y[i] = colok ? apply_coef<T>(code, v[i], jx, q + R * i, J) : mk<T>((T)0, (T)0);
+    if ((J.inv_mask >> o) & 1u) {
+      dft_r<T, R>(y, +1);  // over k1: y[i] = z[k2 = q][n1 = i]
+#pragma unroll
+      for (int i = 1; i < R; ++i) y[i] = cmul(y[i], cconj(tw[q * i]));
+      __syncthreads();  // earlier readers of S are done
+#pragma unroll
+      for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = y[i];
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < R; ++i) y[i] = S[(q * R + i) * TX + b];  // z[k2 = i][n1 = q]
+      dft_r<T, R>(y, +1);  // over k2: y[i] = x[q + R i]
+    }
+    if (colok) {
+      C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out + jx +
+               (size_t)q * J.wc_out;
+      const size_t step = (size_t)R * J.wc_out;
+#pragma unroll
+      for (int i = 0; i < R; ++i) dst[i * step] = y[i];
+    }
   }
 }
 
