@@ -1,6 +1,7 @@
 // Fixed-length FP32 and float-float instantiations of the transform
 // kernels.  The launchers return false for lengths (or precisions) without an
 // instantiation; the caller then launches the runtime-length kernel.
+#include <algorithm>
 #include "fft_kernels.cuh"
 #include "les_internal.h"
 
@@ -73,11 +74,20 @@ template <typename T, typename CIn, int R>
 void cols_reg(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
   typedef typename CT<T>::type C;
   constexpr int TX = 16, N = R * R;
-  const size_t smf = (size_t)(N * TX + N) * sizeof(C);
+  const size_t smf = (size_t)N * TX * (sizeof(C) + sizeof(CIn)) + (size_t)N * sizeof(C);
   static size_t set = 48 * 1024;
   raise_smem(k_colsr<T, TX, CIn, R>, smf, set);
-  const dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
-  k_colsr<T, TX, CIn, R><<<grid, TX * R, smf, s>>>(J, P);
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 1;
+  }
+  const int ntile = (J.ncols + TX - 1) / TX;
+  const int nitems = ntile * J.nlev * (J.nf > 0 ? J.nf : 1);
+  const int nblk = std::min(nitems, 2 * nsm);  // two resident CTAs per SM (registers, shared memory)
+  k_colsr<T, TX, CIn, R><<<nblk, TX * R, smf, s>>>(J, P, ntile, nitems);
 }
 
 template <typename T, int TX, typename CIn, int NIN, int NOUT>

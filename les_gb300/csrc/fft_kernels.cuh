@@ -607,75 +607,97 @@ __device__ __forceinline__ void dft_r(typename CT<T>::type* v, int sign) {
   else if constexpr (R == 8) dft8<C, T>(v, sign);
   else dft4(v, sign);
 }
-template <typename T, int R, int CODE>
-__device__ __forceinline__ void coef_reg(typename CT<T>::type* y, const typename CT<T>::type* v, int q, int jx,
-                                         bool colok, const ColJob& J) {
-#pragma unroll
-  for (int i = 0; i < R; ++i) y[i] = colok ? apply_coef_ct<T, CODE>(v[i], jx, q + R * i, J) : mk<T>((T)0, (T)0);
+// Asynchronous 8-byte global -> shared copies (zero-filled when src_bytes is 0).
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Persistent form: a CTA walks the (kx tile, level, field set) items of the
+// job with stride gridDim.x; each thread stages its R input elements of the
+// next item into shared memory with cp.async while the current item is
+// transformed, so the loads of one item overlap the arithmetic of the
+// previous one.  A thread reads back only what it staged itself, so the
+// staging needs no barrier.  8-byte elements (FP32 complex).
 template <typename T, int TX, typename CIn, int R>
-__global__ void __launch_bounds__(TX * R, (sizeof(T) == 4 && R == 16) ? 2 : 1) k_colsr(ColJob J, FftPlanDev P) {
+__global__ void __launch_bounds__(TX * R, 2) k_colsr(ColJob J, FftPlanDev P, int ntile, int nitems) {
   typedef typename CT<T>::type C;
+  static_assert(sizeof(CIn) == 8 && sizeof(C) == 8, "8-byte complex elements");
   constexpr int N = R * R;
   extern __shared__ __align__(16) unsigned char smraw[];
-  C* S = reinterpret_cast<C*>(smraw);  // exchange: element (i, q) of column b at (i * R + q) * TX + b
-  C* tw = S + N * TX;                  // exp(-2 pi i m / N), m < N
+  C* S = reinterpret_cast<C*>(smraw);          // exchange: element (i, q) of column b at (i * R + q) * TX + b
+  CIn* G = reinterpret_cast<CIn*>(S + N * TX);  // staged input, same index
+  C* tw = reinterpret_cast<C*>(G + N * TX);    // exp(-2 pi i m / N), m < N
   for (int t = threadIdx.x; t < N; t += TX * R) tw[t] = UnitSel<T>::get(P, t);
   const int b = threadIdx.x % TX, q = threadIdx.x / TX;
-  const int jx = blockIdx.x * TX + b;
-  const bool colok = jx < J.ncols;
-  const int lev = blockIdx.y;
-  C v[R];
-  {
-    const CIn* src = reinterpret_cast<const CIn*>(J.in[0]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in +
-                     jx + (size_t)q * J.wc_in;
+  const int nlev = J.nlev;
+  auto stage = [&](int item) {
+    const int tile = item % ntile, rest = item / ntile;
+    const int lev = rest % nlev, z = rest / nlev;
+    const int jx = tile * TX + b;
+    const bool ok = jx < J.ncols;
+    const CIn* src = reinterpret_cast<const CIn*>(J.in[0]) + (size_t)lev * J.ps_in + (size_t)z * J.fs_in +
+                     (ok ? jx : 0) + (size_t)q * J.wc_in;
     const size_t step = (size_t)R * J.wc_in;
 #pragma unroll
+    for (int i = 0; i < R; ++i) cp_async8(&G[(i * R + q) * TX + b], src + i * step, ok ? 8 : 0);
+    cp_async_commit();
+  };
+  if ((int)blockIdx.x < nitems) stage(blockIdx.x);
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int tile = item % ntile, rest = item / ntile;
+    const int lev = rest % nlev, z = rest / nlev;
+    const int jx = tile * TX + b;
+    const bool colok = jx < J.ncols;
+    C v[R];
+    cp_async_wait_all();
+#pragma unroll
     for (int i = 0; i < R; ++i) {
-      v[i] = mk<T>((T)0, (T)0);
+      const CIn x = G[(i * R + q) * TX + b];
+      v[i] = mk<T>(x.x, x.y);
+    }
+    if (item + (int)gridDim.x < nitems) stage(item + gridDim.x);
+    __syncthreads();  // the previous item's readers of S are done (and the twiddle table is in place)
+    if (J.dir & DIR_FWD) {
+      dft_r<T, R>(v, -1);  // over n2: v[i] = y[n1 = q][k2 = i]
+#pragma unroll
+      for (int i = 1; i < R; ++i) v[i] = cmul(v[i], tw[q * i]);
+#pragma unroll
+      for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = v[i];
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[i] = S[(q * R + i) * TX + b];  // y[n1 = i][k2 = q]
+      dft_r<T, R>(v, -1);  // over n1: v[i] = X[q + R i]
+    }
+    for (int o = 0; o < J.nout; ++o) {
+      C y[R];
+      const int code = J.coef[o][0];
+#pragma unroll
+      for (int i = 0; i < R; ++i) y[i] = colok ? apply_coef<T>(code, v[i], jx, q + R * i, J) : mk<T>((T)0, (T)0);
+      if ((J.inv_mask >> o) & 1u) {
+        dft_r<T, R>(y, +1);  // over k1: y[i] = z[k2 = q][n1 = i]
+#pragma unroll
+        for (int i = 1; i < R; ++i) y[i] = cmul(y[i], cconj(tw[q * i]));
+        __syncthreads();  // earlier readers of S are done
+#pragma unroll
+        for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = y[i];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < R; ++i) y[i] = S[(q * R + i) * TX + b];  // z[k2 = i][n1 = q]
+        dft_r<T, R>(y, +1);  // over k2: y[i] = x[q + R i]
+      }
       if (colok) {
-        const CIn x = src[i * step];
-        v[i] = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
+        C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)z * J.fs_out + jx +
+                 (size_t)q * J.wc_out;
+        const size_t step = (size_t)R * J.wc_out;
+#pragma unroll
+        for (int i = 0; i < R; ++i) dst[i * step] = y[i];
       }
     }
   }
-  __syncthreads();  // twiddle table
-  if (J.dir & DIR_FWD) {
-    dft_r<T, R>(v, -1);  // over n2: v[i] = y[n1 = q][k2 = i]
-#pragma unroll
-    for (int i = 1; i < R; ++i) v[i] = cmul(v[i], tw[q * i]);
-#pragma unroll
-    for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = v[i];
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = S[(q * R + i) * TX + b];  // y[n1 = i][k2 = q]
-    dft_r<T, R>(v, -1);  // over n1: v[i] = X[q + R i]
-  }
-  for (int o = 0; o < J.nout; ++o) {
-    C y[R];
-    const int code = J.coef[o][0];
-#pragma unroll
-    for (int i = 0; i < R; ++i) y[i] = colok ? apply_coef<T>(code, v[i], jx, q + R * i, J) : mk<T>((T)0, (T)0);
-    if ((J.inv_mask >> o) & 1u) {
-      dft_r<T, R>(y, +1);  // over k1: y[i] = z[k2 = q][n1 = i]
-#pragma unroll
-      for (int i = 1; i < R; ++i) y[i] = cmul(y[i], cconj(tw[q * i]));
-      __syncthreads();  // earlier readers of S are done
-#pragma unroll
-      for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = y[i];
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < R; ++i) y[i] = S[(q * R + i) * TX + b];  // z[k2 = i][n1 = q]
-      dft_r<T, R>(y, +1);  // over k2: y[i] = x[q + R i]
-    }
-    if (colok) {
-      C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out + jx +
-               (size_t)q * J.wc_out;
-      const size_t step = (size_t)R * J.wc_out;
-#pragma unroll
-      for (int i = 0; i < R; ++i) dst[i * step] = y[i];
-    }
-  }
+  cp_async_wait_all();  // nothing in flight at exit
 }
 
 // rows per CTA of the x-pass kernels (default when a job gives none)

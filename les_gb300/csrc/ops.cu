@@ -195,25 +195,27 @@ __global__ void __launch_bounds__(512) k_plane_mean(const double* f, long pstrid
 
 // ---------------------------------------------------------------------------
 // ddz_uv.f90:36-55 and ddz_w.f90:81-106 (non-MPI)
-__global__ void k_ddz(double* __restrict__ dfdz, const double* __restrict__ f, int ld, int nx, int ny,
-                      int nz, double cst, int uv) {
-  const size_t np = (size_t)ld * ny;
-  GSTRIDE(i, np * nz) {
-    const int jz = (int)(i / np) + 1;
-    const size_t r = i - (size_t)(jz - 1) * np;
-    const int jx = (int)(r % ld);
-    if (jz == nz) { dfdz[i] = 0.0; continue; }
-    if (jx >= nx) continue;
-    if (uv) {
-      if (jz >= 2) dfdz[i] = cst * (f[i] - f[i - np]);
-    } else {
-      dfdz[i] = cst * (f[i + np] - f[i]);
-    }
+// grid (ceil(np/256), nz): no 64-bit index division
+__global__ void __launch_bounds__(256) k_ddz(double* __restrict__ dfdz, const double* __restrict__ f, int ld,
+                                             int nx, int ny, int nz, double cst, int uv) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned r = blockIdx.x * 256u + threadIdx.x;
+  if (r >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + r;
+  if (jz == nz) { dfdz[i] = 0.0; return; }
+  if ((int)(r % (unsigned)ld) >= nx) return;
+  if (uv) {
+    if (jz >= 2) dfdz[i] = cst * (f[i] - f[i - np]);
+  } else {
+    dfdz[i] = cst * (f[i + np] - f[i]);
   }
 }
 int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv) {
   const Grid& g = c->g;
-  k_ddz<<<grid1(g.nfield), 256, 0, c->stream>>>(dfdz, f, g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, uv); LES_COUNT_LAUNCH();
+  k_ddz<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)g.nz), 256, 0, c->stream>>>(dfdz, f, g.ld, g.nx, g.ny,
+                                                                                      g.nz, 1.0 / g.dz, uv);
+  LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -350,7 +352,9 @@ template <int KP>
 __global__ void __launch_bounds__(128) k_nyq_part_rows(const double* f0, const double* f1, const double* f2,
                                                       NyqScratch S, int ld, int nx, int ny, long ps, int nlev,
                                                       int nch) {
-  __shared__ double ws[NYQ_ROWS], wd[NYQ_ROWS];
+  // per-lane partial row sums over even / odd x, summed once per row below
+  // (31 adds per row instead of a 5-step warp reduction on every lane)
+  __shared__ double pse[NYQ_ROWS][33], pso[NYQ_ROWS][33], ws[NYQ_ROWS];
   extern __shared__ double2 wacc[];  // [4][np]
   const int ch = blockIdx.x, lev = blockIdx.y, fld = blockIdx.z;
   const double* f = (fld == 0 ? f0 : fld == 1 ? f1 : f2) + (size_t)lev * ps;
@@ -362,24 +366,21 @@ __global__ void __launch_bounds__(128) k_nyq_part_rows(const double* f0, const d
   for (int r = wid; r < nr; r += 4) {
     const int y = y0 + r;
     const double2* row = reinterpret_cast<const double2*>(f + (size_t)y * ld);
+    const double sg = (y & 1) ? -1.0 : 1.0;  // one FMA per element, no predicated pair
     double se = 0.0, so = 0.0;
 #pragma unroll
     for (int k = 0; k < KP; ++k) {
       const int p = lane + 32 * k;
       if (p < np) {
         const double2 v = row[p];
-        if (y & 1) { acc[k].x -= v.x; acc[k].y -= v.y; }
-        else { acc[k].x += v.x; acc[k].y += v.y; }
+        acc[k].x = fma(sg, v.x, acc[k].x);
+        acc[k].y = fma(sg, v.y, acc[k].y);
         se += v.x;
         so += v.y;
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      se += __shfl_xor_sync(0xffffffffu, se, o);
-      so += __shfl_xor_sync(0xffffffffu, so, o);
-    }
-    if (lane == 0) { ws[r] = se + so; wd[r] = se - so; }
+    pse[r][lane] = se;
+    pso[r][lane] = so;
   }
 #pragma unroll
   for (int k = 0; k < KP; ++k) {
@@ -394,7 +395,13 @@ __global__ void __launch_bounds__(128) k_nyq_part_rows(const double* f0, const d
     for (int w = 1; w < 4; ++w) { a.x += wacc[w * np + p].x; a.y += wacc[w * np + p].y; }
     ap[p] = a;
   }
-  if (threadIdx.x < nr) S.b[pl * ny + y0 + threadIdx.x] = wd[threadIdx.x] / (double)nx;
+  if (threadIdx.x < nr) {
+    double e = 0.0, o = 0.0;
+    for (int l = 0; l < 32; ++l) { e += pse[threadIdx.x][l]; o += pso[threadIdx.x][l]; }
+    ws[threadIdx.x] = e + o;
+    S.b[pl * ny + y0 + threadIdx.x] = (e - o) / (double)nx;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int r = 0; r < nr; ++r) t += ws[r];
@@ -429,26 +436,27 @@ __global__ void __launch_bounds__(256) k_nyq_comb(NyqScratch S, double* mean, in
     mean[(size_t)fld * mstride + lev] = t / ((double)nx * (double)ny);
   }
 }
-__global__ void k_nyq_apply(double* f0, double* f1, double* f2, NyqScratch S, int ld, int nx, int ny, long ps,
-                            int nlev, int nf) {
+// f -= (-1)^y a(x) + (-1)^x b(y) in FP64 (an FP32 correction would leave
+// rounding noise in every mode, divergence included).  grid (ceil(ny (nx/2+1)
+// / 256), nf nlev).
+__global__ void __launch_bounds__(256) k_nyq_apply(double* f0, double* f1, double* f2, NyqScratch S, int ld,
+                                                   int nx, int ny, long ps, int nlev) {
   const int np1 = nx / 2 + 1;  // pairs per row, the last one the padding columns
-  const size_t per = (size_t)ny * np1;
-  GSTRIDE(t, per * nlev * nf) {
-    const size_t pl = t / per;
-    const size_t r = t - pl * per;
-    const int y = (int)(r / np1), p = (int)(r - (size_t)y * np1);
-    const int fld = (int)(pl / nlev), lev = (int)(pl - (size_t)fld * nlev);
-    double* f = (fld == 0 ? f0 : fld == 1 ? f1 : f2) + (size_t)lev * ps + (size_t)y * ld;
-    double2* q = reinterpret_cast<double2*>(f) + p;
-    if (p == np1 - 1) { *q = make_double2(0.0, 0.0); continue; }  // padding columns ld-1:ld
-    const double2 ac = reinterpret_cast<const double2*>(S.ac + pl * nx)[p];
-    const double b = S.b[pl * ny + y];
-    const double ae = (y & 1) ? -ac.x : ac.x, ao = (y & 1) ? -ac.y : ac.y;
-    double2 v = *q;
-    v.x = (v.x - ae) - b;
-    v.y = (v.y - ao) + b;
-    *q = v;
-  }
+  const unsigned r = blockIdx.x * 256u + threadIdx.x;
+  if (r >= (unsigned)ny * np1) return;
+  const int pl = blockIdx.y;
+  const int y = (int)(r / (unsigned)np1), p = (int)(r - (unsigned)y * np1);
+  const int fld = pl / nlev, lev = pl - fld * nlev;
+  double* f = (fld == 0 ? f0 : fld == 1 ? f1 : f2) + (size_t)lev * ps + (size_t)y * ld;
+  double2* q = reinterpret_cast<double2*>(f) + p;
+  if (p == np1 - 1) { *q = make_double2(0.0, 0.0); return; }  // padding columns ld-1:ld
+  const double2 ac = reinterpret_cast<const double2*>(S.ac + (size_t)pl * nx)[p];
+  const double b = S.b[(size_t)pl * ny + y];
+  const double sg = (y & 1) ? -1.0 : 1.0;
+  double2 v = *q;
+  v.x = v.x - fma(sg, ac.x, b);   // even x: (-1)^x = +1
+  v.y = v.y - fma(sg, ac.y, -b);  // odd x
+  *q = v;
 }
 // nf <= 3 fields of nlev levels, in place; plane means to mean[f*mstride+lev];
 // scratch (a few MB) in the given work buffer
@@ -489,7 +497,8 @@ static void nyq_kill(les_ctx* c, double* const* f, int nf, int nlev, double* mea
   }
   LES_COUNT_LAUNCH();
   k_nyq_comb<<<dim3(nlev, nf), 256, 0, c->stream>>>(S, mean, mstride, g.nx, g.ny, nlev, nch); LES_COUNT_LAUNCH();
-  k_nyq_apply<<<grid1(npl * g.ny * (np + 1)), 256, 0, c->stream>>>(f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev, nf);
+  k_nyq_apply<<<dim3((unsigned)((g.ny * (np + 1) + 255) / 256), (unsigned)npl), 256, 0, c->stream>>>(
+      f0, f1, f2, S, g.ld, g.nx, g.ny, ps, nlev);
   LES_COUNT_LAUNCH();
 }
 
@@ -792,6 +801,46 @@ __global__ void k_calc_sij(const double* __restrict__ dudx, const double* __rest
   }
 }
 
+// Mixed form: the same strain in FP32 arithmetic (the gradients come from
+// FP32 transforms), conversions on the integer pipe; the Lagrangian
+// accumulation of u, v, w stays FP64.  grid (ceil(np/256), nz): no 64-bit
+// index division.
+__global__ void __launch_bounds__(256) k_calc_sij32(
+    const double* __restrict__ dudx, const double* __restrict__ dudy, const double* __restrict__ dudz,
+    const double* __restrict__ dvdx, const double* __restrict__ dvdy, const double* __restrict__ dvdz,
+    const double* __restrict__ dwdx, const double* __restrict__ dwdy, const double* __restrict__ dwdz, double* S11,
+    double* S12, double* S13, double* S22, double* S23, double* S33, const double* __restrict__ u,
+    const double* __restrict__ v, const double* __restrict__ w, double* ul, double* vl, double* wl, int ld, int nx,
+    int ny, int lag) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned p = blockIdx.x * 256u + threadIdx.x;
+  if (p >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + p;
+  if (lag) { ul[i] += u[i]; vl[i] += v[i]; wl[i] += w[i]; }
+  if ((int)(p % (unsigned)ld) >= nx) return;
+  float ux, uy, uz, vx, vy, vz, wx, wy, wz;
+  if (jz == 1) {
+    ux = cvt_d2f(dudx[i]); uy = cvt_d2f(dudy[i]); uz = cvt_d2f(dudz[i]);
+    vx = cvt_d2f(dvdx[i]); vy = cvt_d2f(dvdy[i]); vz = cvt_d2f(dvdz[i]);
+    wx = 0.5f * (cvt_d2f(dwdx[i]) + cvt_d2f(dwdx[i + np]));
+    wy = 0.5f * (cvt_d2f(dwdy[i]) + cvt_d2f(dwdy[i + np]));
+    wz = cvt_d2f(dwdz[i]);
+  } else {
+    ux = 0.5f * (cvt_d2f(dudx[i]) + cvt_d2f(dudx[i - np]));
+    uy = 0.5f * (cvt_d2f(dudy[i]) + cvt_d2f(dudy[i - np]));
+    uz = cvt_d2f(dudz[i]);
+    vx = 0.5f * (cvt_d2f(dvdx[i]) + cvt_d2f(dvdx[i - np]));
+    vy = 0.5f * (cvt_d2f(dvdy[i]) + cvt_d2f(dvdy[i - np]));
+    vz = cvt_d2f(dvdz[i]);
+    wx = cvt_d2f(dwdx[i]);
+    wy = cvt_d2f(dwdy[i]);
+    wz = 0.5f * (cvt_d2f(dwdz[i]) + cvt_d2f(dwdz[i - np]));
+  }
+  S11[i] = cvt_f2d(ux); S12[i] = cvt_f2d(0.5f * (uy + vx)); S13[i] = cvt_f2d(0.5f * (uz + wx));
+  S22[i] = cvt_f2d(vy); S23[i] = cvt_f2d(0.5f * (vz + wy)); S33[i] = cvt_f2d(wz);
+}
+
 __device__ __forceinline__ double smag(double a11, double a22, double a33, double a12, double a13, double a23) {
   return sqrt(2.0 * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0 * (a12 * a12 + a13 * a13 + a23 * a23)));
 }
@@ -808,24 +857,6 @@ __global__ void k_nut(const double* __restrict__ S11, const double* __restrict__
     if (jx >= nx) continue;
     const double S = smag(S11[i], S22[i], S33[i], S12[i], S13[i], S23[i]);
     Nu_t[i] = S * Cs[i] * l2;
-  }
-}
-// Mixed form: the same in FP32 (the strain there comes from FP32 transforms),
-// conversions on the integer pipe
-__global__ void k_nut32(const double* __restrict__ S11, const double* __restrict__ S12,
-                        const double* __restrict__ S13, const double* __restrict__ S22,
-                        const double* __restrict__ S23, const double* __restrict__ S33, double* Cs,
-                        double* Nu_t, int ld, int nx, int ny, int nz, float l2, int override_cs, double cs_ov) {
-  const size_t np = (size_t)ld * ny;
-  GSTRIDE(i, np * nz) {
-    if (override_cs) Cs[i] = cs_ov;
-    const int jx = (int)(i % ld);
-    if (jx >= nx) continue;
-    const float a11 = cvt_d2f(S11[i]), a22 = cvt_d2f(S22[i]), a33 = cvt_d2f(S33[i]);
-    const float a12 = cvt_d2f(S12[i]), a13 = cvt_d2f(S13[i]), a23 = cvt_d2f(S23[i]);
-    const float S = sqrtf(2.0f * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0f * (a12 * a12 + a13 * a13 + a23 * a23)));
-    const float cs = override_cs ? cvt_d2f(cs_ov) : cvt_d2f(Cs[i]);
-    Nu_t[i] = cvt_f2d(S * cs * l2);
   }
 }
 // sgs_stag.f90:218-364 (tau_ij, 'wall', molec = .false.)
@@ -862,6 +893,62 @@ __global__ void k_tau(const double* __restrict__ S11, const double* __restrict__
       txz[i] = -2.0 * (c2 + nu) * S13[i];
       tyz[i] = -2.0 * (c2 + nu) * S23[i];
     }
+  }
+}
+
+// Mixed form: the eddy viscosity (k_nut) and tau (k_tau) in one pass, FP32
+// arithmetic (the strain comes from FP32 transforms), conversions on the
+// integer pipe.  The thread of level jz forms Nu_t at its own level (stored,
+// as sgs_stag.f90:166-211) and again at level jz+1 for the staggered
+// averages of tau (the strain of both levels is read anyway), so Nu_t is not
+// re-read.  grid (ceil(np/256), nz).
+__device__ __forceinline__ float nut32_at(const double* const* S, size_t i, float cs, float l2) {
+  const float a11 = cvt_d2f(S[0][i]), a12 = cvt_d2f(S[1][i]), a13 = cvt_d2f(S[2][i]);
+  const float a22 = cvt_d2f(S[3][i]), a23 = cvt_d2f(S[4][i]), a33 = cvt_d2f(S[5][i]);
+  const float sm = sqrtf(2.0f * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0f * (a12 * a12 + a13 * a13 + a23 * a23)));
+  return sm * cs * l2;
+}
+struct Ptr6c { const double* p[6]; };
+__global__ void __launch_bounds__(256) k_nut_tau32(Ptr6c Sp, double* Cs, double* Nu_t, double* txx, double* txy,
+                                                   double* tyy, double* txz, double* tyz, double* tzz, int ld,
+                                                   int nx, int ny, int nz, float l2, int override_cs, double cs_ov) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned p = blockIdx.x * 256u + threadIdx.x;
+  if (p >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + p;
+  if (override_cs) Cs[i] = cs_ov;
+  const bool inx = (int)(p % (unsigned)ld) < nx;
+  const float csov = cvt_d2f(cs_ov);
+  float nu = 0.0f;
+  if (inx) {
+    nu = nut32_at(Sp.p, i, override_cs ? csov : cvt_d2f(Cs[i]), l2);
+    Nu_t[i] = cvt_f2d(nu);
+  }
+  if (jz == nz) {
+    txx[i] = LES_BOGUS; txy[i] = LES_BOGUS; tyy[i] = LES_BOGUS; tzz[i] = LES_BOGUS;
+    txz[i] = 0.0; tyz[i] = 0.0;
+    return;
+  }
+  if (!inx) return;
+  const double* const* S = Sp.p;
+  if (jz == 1) {
+    const float c = -2.0f * nu;
+    txx[i] = cvt_f2d(c * cvt_d2f(S[0][i]));
+    txy[i] = cvt_f2d(c * cvt_d2f(S[1][i]));
+    tyy[i] = cvt_f2d(c * cvt_d2f(S[3][i]));
+    tzz[i] = cvt_f2d(c * cvt_d2f(S[5][i]));
+    // txz, tyz at the wall come from wallstress
+  } else {
+    const size_t ip = i + np;
+    const float nup = nut32_at(S, ip, override_cs ? csov : cvt_d2f(Cs[ip]), l2);
+    const float c = -2.0f * (0.5f * (nu + nup)) * 0.5f;
+    txx[i] = cvt_f2d(c * (cvt_d2f(S[0][i]) + cvt_d2f(S[0][ip])));
+    txy[i] = cvt_f2d(c * (cvt_d2f(S[1][i]) + cvt_d2f(S[1][ip])));
+    tyy[i] = cvt_f2d(c * (cvt_d2f(S[3][i]) + cvt_d2f(S[3][ip])));
+    tzz[i] = cvt_f2d(c * (cvt_d2f(S[5][i]) + cvt_d2f(S[5][ip])));
+    txz[i] = cvt_f2d(-2.0f * nu * cvt_d2f(S[2][i]));
+    tyz[i] = cvt_f2d(-2.0f * nu * cvt_d2f(S[4][i]));
   }
 }
 
@@ -1605,17 +1692,50 @@ __global__ void k_rhs_ab2(double* u, double* v, double* w, double* Rx, double* R
   }
 }
 
+// Mixed form: the horizontal right-hand sides come from FP32 transforms, so
+// they and their AB2 increments are formed in FP32 (conversions on the
+// integer pipe) and only u + increment is an FP64 addition.  The vertical
+// component keeps the FP64 arithmetic of k_rhs_ab2: the pressure solve takes
+// its wall and lid conditions from the same vertical stress divergence, and
+// an FP32-rounded w right-hand side leaves a divergence the projection cannot
+// remove (rmsdiv 1e-10 instead of 1e-13 at 32^3).
+__global__ void k_rhs_ab2_32(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz, double* Rxf,
+                             double* Ryf, double* Rzf, const double* __restrict__ dx_,
+                             const double* __restrict__ dy_, const double* __restrict__ dz_,
+                             const double* __restrict__ bs, size_t nv, size_t np, double dt, int sflag, int euler) {
+  const float dtf = (float)dt;
+  GSTRIDE(i, nv + np) {
+    if (i >= nv) { u[i] = LES_BOGUS; v[i] = LES_BOGUS; w[i] = LES_BOGUS; continue; }
+    double rz = -Rz[i] - dz_[i];
+    if (sflag) rz = rz + bs[i];
+    Rz[i] = rz;
+    double fz = Rzf[i];
+    if (euler) { fz = rz; Rzf[i] = rz; }
+    w[i] = w[i] + dt * (1.5 * rz + (1.0 - 1.5) * fz);
+    const float rx = -cvt_d2f(Rx[i]) - cvt_d2f(dx_[i]);
+    const float ry = -cvt_d2f(Ry[i]) - cvt_d2f(dy_[i]);
+    const double drx = cvt_f2d(rx), dry = cvt_f2d(ry);
+    Rx[i] = drx; Ry[i] = dry;
+    float fx, fy;
+    if (euler) {
+      fx = rx; fy = ry;
+      Rxf[i] = drx; Ryf[i] = dry;
+    } else {
+      fx = cvt_d2f(Rxf[i]); fy = cvt_d2f(Ryf[i]);
+    }
+    u[i] = u[i] + cvt_f2d(dtf * (1.5f * rx - 0.5f * fx));
+    v[i] = v[i] + cvt_f2d(dtf * (1.5f * ry - 0.5f * fy));
+  }
+}
+
 // main.f90:403-410 + forcing.f90:128-219 project, one thread per point of
 // levels 1..nz-1; the thread of level nz-1 also sets the top level and the
 // thread of level 1 the wall value of w.
 __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz,
                                const double* __restrict__ p, const double* __restrict__ dpdx,
                                const double* __restrict__ dpdy, double* dpdz, int ld, int nx, int ny, int nz,
-                               double dz, double dt, int recip) {
-  // recip: the mixed form multiplies by 1/dz; the FP64 form divides as the
-  // reference does
+                               double dz, double dt) {
   const size_t np = (size_t)ld * ny;
-  const double idz = 1.0 / dz;
   GSTRIDE(i, np * (nz - 1)) {
     const int jz = (int)(i / np) + 1;
     const size_t r = i - (size_t)(jz - 1) * np;
@@ -1623,7 +1743,7 @@ __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, doub
     double pz = 0.0;
     if (jx < nx) {
       const double dp = p[r + (size_t)jz * np] - p[r + (size_t)(jz - 1) * np];
-      pz = recip ? dp * idz : dp / dz;
+      pz = dp / dz;
       dpdz[i] = pz;
     } else {
       pz = dpdz[i];
@@ -1649,6 +1769,50 @@ __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, doub
     if (jz == 1) w[i] = 0.0;
   }
 }
+// Mixed form: dpdz and the projection in FP64 with the fused factor
+// -1.5 dt (the pressure comes from float-float transforms and the projection
+// sets the divergence); the horizontal RHS bookkeeping R -= grad p in FP32,
+// the vertical one in FP64 (see k_rhs_ab2_32).  grid (ceil(np/256), nz-1).
+__global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, double* w, double* Rx, double* Ry,
+                                                        double* Rz, const double* __restrict__ p,
+                                                        const double* __restrict__ dpdx,
+                                                        const double* __restrict__ dpdy, double* dpdz, int ld,
+                                                        int nx, int ny, int nz, double idz, double dt) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned r = blockIdx.x * 256u + threadIdx.x;
+  if (r >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + r;
+  const bool inx = (int)(r % (unsigned)ld) < nx;
+  const double c = -1.5 * dt;
+  double pz;
+  if (inx) {
+    pz = (p[i + np] - p[i]) * idz;
+    dpdz[i] = pz;
+  } else {
+    pz = dpdz[i];
+  }
+  const double gx = dpdx[i], gy = dpdy[i];
+  Rx[i] = cvt_f2d(cvt_d2f(Rx[i]) - cvt_d2f(gx));
+  Ry[i] = cvt_f2d(cvt_d2f(Ry[i]) - cvt_d2f(gy));
+  Rz[i] = Rz[i] - pz;
+  double uu = u[i], vv = v[i], ww = w[i];
+  if (inx) {
+    uu = fma(c, gx, uu);
+    vv = fma(c, gy, vv);
+    u[i] = uu; v[i] = vv;
+    if (jz >= 2) { ww = fma(c, pz, ww); w[i] = ww; }
+  }
+  if (jz == nz - 1) {
+    const size_t top = i + np;
+    dpdz[top] = LES_BOGUS;
+    u[top] = uu;
+    v[top] = vv;
+    w[top] = 0.0;
+  }
+  if (jz == 1) w[i] = 0.0;
+}
+
 __global__ void k_project_only(double* u, double* v, double* w, const double* dpdx, const double* dpdy,
                                const double* dpdz, int ld, int nx, int ny, int nz, double dt) {
   const size_t np = (size_t)ld * ny;
@@ -2190,7 +2354,8 @@ static void calcbeta(les_ctx* c) {
   k_calcbeta_levels<<<1, 256, 0, c->stream>>>(c->dred, sbr, g.nz, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
   const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
   k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], sbr, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
-                                                    g.nz, g_hat); LES_COUNT_LAUNCH();
+                                                    g.nz, g_hat);
+  LES_COUNT_LAUNCH();
 }
 // scalars_module.f90:457-504 step_scalar
 __global__ void k_step_scalar(double* theta, const double* __restrict__ R, const double* __restrict__ Rf, int ld,
@@ -2786,11 +2951,20 @@ static int sgs_stagT(les_ctx* c) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const bool lag = (k.model == 4 || k.model == 5 || k.model == 7);
-  k_calc_sij<<<grid1(g.nfield), 256, 0, c->stream>>>(
-      c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
-      c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
-      c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
-      c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0); LES_COUNT_LAUNCH();
+  const dim3 gpl((unsigned)((g.nplane + 255) / 256), (unsigned)g.nz);
+  if (MX)
+    k_calc_sij32<<<gpl, 256, 0, c->stream>>>(
+        c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
+        c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
+        c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
+        c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, lag ? 1 : 0);
+  else
+    k_calc_sij<<<grid1(g.nfield), 256, 0, c->stream>>>(
+        c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
+        c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
+        c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
+        c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0);
+  LES_COUNT_LAUNCH();
   const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
   if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {
     if (k.model == 3) {
@@ -2808,13 +2982,16 @@ static int sgs_stagT(les_ctx* c) {
     const float c016 = 0.16f;
     csov = (double)(c016 * c016);
   }
-  if (MX)
-    k_nut32<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
-                                                   c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, (float)(g.delta * g.delta),
-                                                   ov, csov);
-  else
-    k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
-                                                 c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, g.delta * g.delta, ov, csov);
+  if (MX) {
+    Ptr6c Sp;
+    for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
+    k_nut_tau32<<<gpl, 256, 0, c->stream>>>(Sp, c->f[LES_CS_OPT2], c->f[LES_NU_T], c->f[LES_TXX], c->f[LES_TXY],
+                                            c->f[LES_TYY], c->f[LES_TXZ], c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx,
+                                            g.ny, g.nz, (float)(g.delta * g.delta), ov, csov); LES_COUNT_LAUNCH();
+    return 0;
+  }
+  k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
+                                               c->f[LES_NU_T], g.ld, g.nx, g.ny, g.nz, g.delta * g.delta, ov, csov);
   LES_COUNT_LAUNCH();
   k_tau<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_NU_T],
                                                c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ],
@@ -2927,7 +3104,8 @@ static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
   c2rT<T, double>(c, 3, g.nz, c->wsB, h, (long)g.nplane, false, g.lh);
   k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divtx, divty, divtz, h[0], h[1], h[2], c->f[LES_TXZ],
                                                          c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz,
-                                                         1.0 / g.dz, 7); LES_COUNT_LAUNCH();
+                                                         1.0 / g.dz, 7);
+  LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -3093,15 +3271,28 @@ static int stepT(les_ctx* c) {
   divstressT<MX>(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
   convecT<MX>(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
   const size_t nv = g.nplane * (g.nz - 1);
-  k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
-      c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
-      c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL], nv,
-      g.nplane, k.dt, k.s_flag, (c->jt == 1 && !k.initu) ? 1 : 0); LES_COUNT_LAUNCH();
+  const int euler = (c->jt == 1 && !k.initu) ? 1 : 0;
+  if (MX)
+    k_rhs_ab2_32<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
+        c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL],
+        nv, g.nplane, k.dt, k.s_flag, euler);
+  else
+    k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
+        c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL],
+        nv, g.nplane, k.dt, k.s_flag, euler);
+  LES_COUNT_LAUNCH();
   pressT<typename std::conditional<MX, dfloat, double>::type>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
-  k_dpdz_project<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX],
-                                                        c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX],
-                                                        c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz,
-                                                        k.dt, MX ? 1 : 0); LES_COUNT_LAUNCH();
+  if (MX)
+    k_dpdz_project32<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)(g.nz - 1)), 256, 0, c->stream>>>(
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P],
+        c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, k.dt);
+  else
+    k_dpdz_project<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P],
+        c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz, k.dt);
+  LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaGetLastError());
   if (rms_step) {
     if (!MX) op_rmsdiv(c, c->dscal + 1);
