@@ -276,6 +276,10 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   }
   if (k.precision != 0 && k.precision != 1) { les_set_error("precision must be 0 or 1"); return LES_ERR_ARG; }
   if (k.model != 5 && k.model != 3) { les_set_error("model must be 5 or 3"); return LES_ERR_UNSUPPORTED; }
+  if (k.precision == 1 && k.model != 5) {  // model 3's plane sums read S_ij in FP64
+    les_set_error("the FP32-mixed form (precision 1) runs model 5");
+    return LES_ERR_UNSUPPORTED;
+  }
   les_ctx* c = new les_ctx();
   c->cfg = k;
   c->jt_total = k.jt_total0;
@@ -393,15 +397,44 @@ int les_set_surface(les_ctx* c, const double* zo, const double* wt_s) {
   return LES_OK;
 }
 
+// host <-> device copy of one field; the FP32-held fields of a mixed
+// context are narrowed / widened on the host
+static bool f32_held(const les_ctx* c, int f) { return c->cfg.precision == 1 && mixed_f32_field(f); }
+static int field_in(les_ctx* c, int f, const double* host) {
+  const size_t n = c->fsize[f];
+  if (f32_held(c, f)) {
+    std::vector<float> t(n);
+    for (size_t i = 0; i < n; ++i) t[i] = (float)host[i];
+    LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], t.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    return LES_OK;
+  }
+  LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  return LES_OK;
+}
+static int field_out(les_ctx* c, int f, double* host) {
+  const size_t n = c->fsize[f];
+  if (f32_held(c, f)) {
+    std::vector<float> t(n);
+    LES_CUDA_CHECK(cudaMemcpyAsync(t.data(), c->f[f], n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) host[i] = (double)t[i];
+    return LES_OK;
+  }
+  LES_CUDA_CHECK(cudaMemcpyAsync(host, c->f[f], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return LES_OK;
+}
 int les_set_field(les_ctx* c, les_field f, const double* host) {
   if (!c || !host || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
-  LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], host, c->fsize[f] * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int st = field_in(c, f, host);
+  if (st) return st;
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   return LES_OK;
 }
 int les_get_field(les_ctx* c, les_field f, double* host) {
   if (!c || !host || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
-  LES_CUDA_CHECK(cudaMemcpyAsync(host, c->f[f], c->fsize[f] * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  int st = field_out(c, f, host);
+  if (st) return st;
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   return LES_OK;
 }
@@ -421,14 +454,20 @@ int les_register_field(les_ctx* c, les_field f, double* host) {
 int les_sync_from_host(les_ctx* c) {
   if (!c) return LES_ERR_ARG;
   for (int f = 0; f < LES_NUM_FIELDS; ++f)
-    if (c->reg[f]) LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], c->reg[f], c->fsize[f] * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (c->reg[f]) {
+      int st = field_in(c, f, c->reg[f]);
+      if (st) return st;
+    }
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   return LES_OK;
 }
 int les_sync_to_host(les_ctx* c) {
   if (!c) return LES_ERR_ARG;
   for (int f = 0; f < LES_NUM_FIELDS; ++f)
-    if (c->reg[f]) LES_CUDA_CHECK(cudaMemcpyAsync(c->reg[f], c->f[f], c->fsize[f] * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (c->reg[f]) {
+      int st = field_out(c, f, c->reg[f]);
+      if (st) return st;
+    }
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   return LES_OK;
 }
@@ -936,8 +975,10 @@ int les_tridag_array(les_ctx* c, const double* a, const double* b, const double*
   if (fl) { les_set_error("tridag_array failed: zero pivot"); return LES_ERR_PIVOT; }
   return LES_OK;
 }
+static int need_fp64(const les_ctx* c, const char* name);
 int les_convec(les_ctx* c, double* cx, double* cy, double* cz) {
   if (!c || !cx || !cy || !cz) return LES_ERR_ARG;
+  if (int st = need_fp64(c, "les_convec")) return st;
   const size_t n = c->g.nfield;
   Arg X(c, cx, n), Y(c, cy, n), Z(c, cz, n);
   CHK(X.alloc()); CHK(Y.alloc()); CHK(Z.alloc());
@@ -980,6 +1021,7 @@ int les_press_stag_array(les_ctx* c, double* p_hat, double* dfdx, double* dfdy) 
 }
 int les_sgs_stag(les_ctx* c) {
   if (!c) return LES_ERR_ARG;
+  if (int st = need_fp64(c, "les_sgs_stag")) return st;
   op_sgs_stag(c);
   return finish(c);
 }
@@ -1009,10 +1051,28 @@ int les_scaledep_dynamic(les_ctx* c, double* cs_opt2, const double* S11, const d
   CHK(o.out());
   return finish(c);
 }
-int les_wallstress(les_ctx* c) { if (!c) return LES_ERR_ARG; op_wallstress(c); return finish(c); }
+// The per-routine module operations below read or write S_ij, Nu_t, tau_ij or
+// the velocity gradients in FP64; on an FP32-mixed context those are held in
+// FP32, so these entries need a precision-0 context.
+static int need_fp64(const les_ctx* c, const char* name) {
+  if (c->cfg.precision == 0) return LES_OK;
+  les_set_error("%s: needs a precision-0 context (the mixed form holds S_ij, Nu_t, tau_ij in FP32)", name);
+  return LES_ERR_ARG;
+}
+int les_wallstress(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  if (int st = need_fp64(c, "les_wallstress")) return st;
+  op_wallstress(c);
+  return finish(c);
+}
 int les_obukhov(les_ctx* c) { if (!c) return LES_ERR_ARG; op_obukhov(c); return finish(c); }
 int les_project(les_ctx* c) { if (!c) return LES_ERR_ARG; op_project(c); return finish(c); }
-int les_theta_all_in_one(les_ctx* c) { if (!c) return LES_ERR_ARG; op_theta(c); return finish(c); }
+int les_theta_all_in_one(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  if (int st = need_fp64(c, "les_theta_all_in_one")) return st;
+  op_theta(c);
+  return finish(c);
+}
 
 int les_test_filter(les_ctx* c, double* f, const double* G, int nplanes) {
   if (!c || !f || !G || nplanes < 1) return LES_ERR_ARG;

@@ -99,6 +99,22 @@ struct les_ctx {
 };
 
 namespace les {
+// An FP32-mixed context (precision 1) holds these SGS intermediates in FP32:
+// the horizontal velocity gradients (FP32 transforms), S_ij, Nu_t and
+// tau_ij.  Each keeps its FP64 allocation and (ld, ny, nz) layout; the FP32
+// values sit in the first half.  les_get_field / les_set_field convert.
+inline bool mixed_f32_field(int f) {
+  switch (f) {
+    case LES_DUDX: case LES_DUDY: case LES_DVDX: case LES_DVDY: case LES_DWDX: case LES_DWDY:
+    case LES_S11: case LES_S12: case LES_S13: case LES_S22: case LES_S23: case LES_S33:
+    case LES_NU_T:
+    case LES_TXX: case LES_TXY: case LES_TYY: case LES_TXZ: case LES_TYZ: case LES_TZZ:
+      return true;
+    default:
+      return false;
+  }
+}
+inline float* f32(les_ctx* c, int f) { return reinterpret_cast<float*>(c->f[f]); }
 int step_fp64(les_ctx* c);
 int step_mixed(les_ctx* c);
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev);
@@ -125,7 +141,7 @@ int op_convec(les_ctx* c, double* cx, double* cy, double* cz);
 int op_press(les_ctx* c, double* p, double* dpdx, double* dpdy);
 int op_project(les_ctx* c);
 int op_rmsdiv(les_ctx* c, double* out);
-int op_tsc(les_ctx* c, double* cflu, double* visc);
+int op_tsc(les_ctx* c, double* cflu, double* visc);  // Nu_t read in the context's storage precision
 int op_ddz(les_ctx* c, double* dfdz, const double* f, int uv);
 int thomas_tables(les_ctx* c);
 void autotune_probe(les_ctx* c, int fp32);

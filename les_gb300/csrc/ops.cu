@@ -542,8 +542,9 @@ static int filt_da_uvw_mixed(les_ctx* c) {
   colsT<float, float2>(c, J);
   k_spec_widen<<<grid1(3 * (size_t)FS), 256, 0, c->stream>>>(ob + 6 * FS, c->spec, mean, ms, (size_t)FS, g.C, 3);
   LES_COUNT_LAUNCH();
-  double* o6[6] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX], c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
-  c2rT<float, double>(c, 6, nz, c->wsB, o6, (long)g.nplane, false, g.lh);
+  float* o6[6] = {f32(c, LES_DUDX), f32(c, LES_DVDX), f32(c, LES_DWDX), f32(c, LES_DUDY), f32(c, LES_DVDY),
+                  f32(c, LES_DWDY)};  // FP32-held in the mixed form
+  c2rT<float, float>(c, 6, nz, c->wsB, o6, (long)g.nplane, false, g.lh);
   return 0;
 }
 
@@ -726,11 +727,12 @@ int op_obukhov(les_ctx* c) {
 }
 
 // wallstress.f90:5-69 ('wall')
+template <typename TT>  // storage of txz, tyz (FP32 in the mixed form)
 __global__ void k_wallstress(const double* __restrict__ u, const double* __restrict__ v,
                              const double* __restrict__ u1, const double* __restrict__ v1,
                              const double* __restrict__ zo, const double* __restrict__ psi_m,
                              const double* __restrict__ psi_m0, const double* __restrict__ phi_m,
-                             double* ustar_avg, double* txz, double* tyz, double* dudz, double* dvdz,
+                             double* ustar_avg, TT* txz, TT* tyz, double* dudz, double* dvdz,
                              int nx, int ny, int ld, double dz, double vonk) {
   GSTRIDE(s, (size_t)nx * ny) {
     const int jy = (int)(s / nx), jx = (int)(s - (size_t)jy * nx);
@@ -740,8 +742,8 @@ __global__ void k_wallstress(const double* __restrict__ u, const double* __restr
     const double us = u_avg * vonk / denom;
     ustar_avg[s] = us;
     const double cst = -(us * us) / u_avg;
-    txz[i] = cst * u1[i];
-    tyz[i] = cst * v1[i];
+    txz[i] = cvt<TT, double>(cst * u1[i]);
+    tyz[i] = cvt<TT, double>(cst * v1[i]);
     const double a = us / (0.5 * dz * vonk) * u1[i] / u_avg * phi_m[s];
     const double b = us / (0.5 * dz * vonk) * v1[i] / u_avg * phi_m[s];
     dudz[i] = (u[i] == 0.0) ? 0.0 : a;
@@ -754,10 +756,17 @@ int op_wallstress(les_ctx* c) {
   double* v1 = c->tmp + g.nplane;
   op_test_filter(c, u1, c->f[LES_U], 1, 1, (long)g.nplane);
   op_test_filter(c, v1, c->f[LES_V], 1, 1, (long)g.nplane);
-  k_wallstress<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(
-      c->f[LES_U], c->f[LES_V], u1, v1, c->f[LES_ZO], c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PHI_M],
-      c->f[LES_USTAR_AVG], c->f[LES_TXZ], c->f[LES_TYZ], c->f[LES_DUDZ], c->f[LES_DVDZ], g.nx, g.ny, g.ld,
-      g.dz, c->cfg.vonk); LES_COUNT_LAUNCH();
+  if (c->cfg.precision == 1)
+    k_wallstress<float><<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(
+        c->f[LES_U], c->f[LES_V], u1, v1, c->f[LES_ZO], c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PHI_M],
+        c->f[LES_USTAR_AVG], f32(c, LES_TXZ), f32(c, LES_TYZ), c->f[LES_DUDZ], c->f[LES_DVDZ], g.nx, g.ny, g.ld,
+        g.dz, c->cfg.vonk);
+  else
+    k_wallstress<double><<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(
+        c->f[LES_U], c->f[LES_V], u1, v1, c->f[LES_ZO], c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PHI_M],
+        c->f[LES_USTAR_AVG], c->f[LES_TXZ], c->f[LES_TYZ], c->f[LES_DUDZ], c->f[LES_DVDZ], g.nx, g.ny, g.ld,
+        g.dz, c->cfg.vonk);
+  LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -801,15 +810,15 @@ __global__ void k_calc_sij(const double* __restrict__ dudx, const double* __rest
   }
 }
 
-// Mixed form: the same strain in FP32 arithmetic (the gradients come from
-// FP32 transforms), conversions on the integer pipe; the Lagrangian
-// accumulation of u, v, w stays FP64.  grid (ceil(np/256), nz): no 64-bit
-// index division.
+// Mixed form: the same strain in FP32 from the FP32-held horizontal
+// gradients (FP32 transforms) and the FP64 vertical ones, stored in FP32;
+// the Lagrangian accumulation of u, v, w stays FP64.  grid (ceil(np/256),
+// nz): no 64-bit index division.
 __global__ void __launch_bounds__(256) k_calc_sij32(
-    const double* __restrict__ dudx, const double* __restrict__ dudy, const double* __restrict__ dudz,
-    const double* __restrict__ dvdx, const double* __restrict__ dvdy, const double* __restrict__ dvdz,
-    const double* __restrict__ dwdx, const double* __restrict__ dwdy, const double* __restrict__ dwdz, double* S11,
-    double* S12, double* S13, double* S22, double* S23, double* S33, const double* __restrict__ u,
+    const float* __restrict__ dudx, const float* __restrict__ dudy, const double* __restrict__ dudz,
+    const float* __restrict__ dvdx, const float* __restrict__ dvdy, const double* __restrict__ dvdz,
+    const float* __restrict__ dwdx, const float* __restrict__ dwdy, const double* __restrict__ dwdz, float* S11,
+    float* S12, float* S13, float* S22, float* S23, float* S33, const double* __restrict__ u,
     const double* __restrict__ v, const double* __restrict__ w, double* ul, double* vl, double* wl, int ld, int nx,
     int ny, int lag) {
   const unsigned np = (unsigned)ld * ny;
@@ -821,24 +830,24 @@ __global__ void __launch_bounds__(256) k_calc_sij32(
   if ((int)(p % (unsigned)ld) >= nx) return;
   float ux, uy, uz, vx, vy, vz, wx, wy, wz;
   if (jz == 1) {
-    ux = cvt_d2f(dudx[i]); uy = cvt_d2f(dudy[i]); uz = cvt_d2f(dudz[i]);
-    vx = cvt_d2f(dvdx[i]); vy = cvt_d2f(dvdy[i]); vz = cvt_d2f(dvdz[i]);
-    wx = 0.5f * (cvt_d2f(dwdx[i]) + cvt_d2f(dwdx[i + np]));
-    wy = 0.5f * (cvt_d2f(dwdy[i]) + cvt_d2f(dwdy[i + np]));
+    ux = dudx[i]; uy = dudy[i]; uz = cvt_d2f(dudz[i]);
+    vx = dvdx[i]; vy = dvdy[i]; vz = cvt_d2f(dvdz[i]);
+    wx = 0.5f * (dwdx[i] + dwdx[i + np]);
+    wy = 0.5f * (dwdy[i] + dwdy[i + np]);
     wz = cvt_d2f(dwdz[i]);
   } else {
-    ux = 0.5f * (cvt_d2f(dudx[i]) + cvt_d2f(dudx[i - np]));
-    uy = 0.5f * (cvt_d2f(dudy[i]) + cvt_d2f(dudy[i - np]));
+    ux = 0.5f * (dudx[i] + dudx[i - np]);
+    uy = 0.5f * (dudy[i] + dudy[i - np]);
     uz = cvt_d2f(dudz[i]);
-    vx = 0.5f * (cvt_d2f(dvdx[i]) + cvt_d2f(dvdx[i - np]));
-    vy = 0.5f * (cvt_d2f(dvdy[i]) + cvt_d2f(dvdy[i - np]));
+    vx = 0.5f * (dvdx[i] + dvdx[i - np]);
+    vy = 0.5f * (dvdy[i] + dvdy[i - np]);
     vz = cvt_d2f(dvdz[i]);
-    wx = cvt_d2f(dwdx[i]);
-    wy = cvt_d2f(dwdy[i]);
+    wx = dwdx[i];
+    wy = dwdy[i];
     wz = 0.5f * (cvt_d2f(dwdz[i]) + cvt_d2f(dwdz[i - np]));
   }
-  S11[i] = cvt_f2d(ux); S12[i] = cvt_f2d(0.5f * (uy + vx)); S13[i] = cvt_f2d(0.5f * (uz + wx));
-  S22[i] = cvt_f2d(vy); S23[i] = cvt_f2d(0.5f * (vz + wy)); S33[i] = cvt_f2d(wz);
+  S11[i] = ux; S12[i] = 0.5f * (uy + vx); S13[i] = 0.5f * (uz + wx);
+  S22[i] = vy; S23[i] = 0.5f * (vz + wy); S33[i] = wz;
 }
 
 __device__ __forceinline__ double smag(double a11, double a22, double a33, double a12, double a13, double a23) {
@@ -897,20 +906,19 @@ __global__ void k_tau(const double* __restrict__ S11, const double* __restrict__
 }
 
 // Mixed form: the eddy viscosity (k_nut) and tau (k_tau) in one pass, FP32
-// arithmetic (the strain comes from FP32 transforms), conversions on the
-// integer pipe.  The thread of level jz forms Nu_t at its own level (stored,
+// arithmetic on the FP32-held strain, Nu_t and tau stored in FP32.  The thread of level jz forms Nu_t at its own level (stored,
 // as sgs_stag.f90:166-211) and again at level jz+1 for the staggered
 // averages of tau (the strain of both levels is read anyway), so Nu_t is not
 // re-read.  grid (ceil(np/256), nz).
-__device__ __forceinline__ float nut32_at(const double* const* S, size_t i, float cs, float l2) {
-  const float a11 = cvt_d2f(S[0][i]), a12 = cvt_d2f(S[1][i]), a13 = cvt_d2f(S[2][i]);
-  const float a22 = cvt_d2f(S[3][i]), a23 = cvt_d2f(S[4][i]), a33 = cvt_d2f(S[5][i]);
+__device__ __forceinline__ float nut32_at(const float* const* S, size_t i, float cs, float l2) {
+  const float a11 = S[0][i], a12 = S[1][i], a13 = S[2][i];
+  const float a22 = S[3][i], a23 = S[4][i], a33 = S[5][i];
   const float sm = sqrtf(2.0f * (a11 * a11 + a22 * a22 + a33 * a33 + 2.0f * (a12 * a12 + a13 * a13 + a23 * a23)));
   return sm * cs * l2;
 }
-struct Ptr6c { const double* p[6]; };
-__global__ void __launch_bounds__(256) k_nut_tau32(Ptr6c Sp, double* Cs, double* Nu_t, double* txx, double* txy,
-                                                   double* tyy, double* txz, double* tyz, double* tzz, int ld,
+struct Ptr6f { const float* p[6]; };
+__global__ void __launch_bounds__(256) k_nut_tau32(Ptr6f Sp, double* Cs, float* Nu_t, float* txx, float* txy,
+                                                   float* tyy, float* txz, float* tyz, float* tzz, int ld,
                                                    int nx, int ny, int nz, float l2, int override_cs, double cs_ov) {
   const unsigned np = (unsigned)ld * ny;
   const unsigned p = blockIdx.x * 256u + threadIdx.x;
@@ -923,32 +931,32 @@ __global__ void __launch_bounds__(256) k_nut_tau32(Ptr6c Sp, double* Cs, double*
   float nu = 0.0f;
   if (inx) {
     nu = nut32_at(Sp.p, i, override_cs ? csov : cvt_d2f(Cs[i]), l2);
-    Nu_t[i] = cvt_f2d(nu);
+    Nu_t[i] = nu;
   }
   if (jz == nz) {
-    txx[i] = LES_BOGUS; txy[i] = LES_BOGUS; tyy[i] = LES_BOGUS; tzz[i] = LES_BOGUS;
-    txz[i] = 0.0; tyz[i] = 0.0;
+    txx[i] = (float)LES_BOGUS; txy[i] = (float)LES_BOGUS; tyy[i] = (float)LES_BOGUS; tzz[i] = (float)LES_BOGUS;
+    txz[i] = 0.0f; tyz[i] = 0.0f;
     return;
   }
   if (!inx) return;
-  const double* const* S = Sp.p;
+  const float* const* S = Sp.p;
   if (jz == 1) {
     const float c = -2.0f * nu;
-    txx[i] = cvt_f2d(c * cvt_d2f(S[0][i]));
-    txy[i] = cvt_f2d(c * cvt_d2f(S[1][i]));
-    tyy[i] = cvt_f2d(c * cvt_d2f(S[3][i]));
-    tzz[i] = cvt_f2d(c * cvt_d2f(S[5][i]));
+    txx[i] = c * S[0][i];
+    txy[i] = c * S[1][i];
+    tyy[i] = c * S[3][i];
+    tzz[i] = c * S[5][i];
     // txz, tyz at the wall come from wallstress
   } else {
     const size_t ip = i + np;
     const float nup = nut32_at(S, ip, override_cs ? csov : cvt_d2f(Cs[ip]), l2);
     const float c = -2.0f * (0.5f * (nu + nup)) * 0.5f;
-    txx[i] = cvt_f2d(c * (cvt_d2f(S[0][i]) + cvt_d2f(S[0][ip])));
-    txy[i] = cvt_f2d(c * (cvt_d2f(S[1][i]) + cvt_d2f(S[1][ip])));
-    tyy[i] = cvt_f2d(c * (cvt_d2f(S[3][i]) + cvt_d2f(S[3][ip])));
-    tzz[i] = cvt_f2d(c * (cvt_d2f(S[5][i]) + cvt_d2f(S[5][ip])));
-    txz[i] = cvt_f2d(-2.0f * nu * cvt_d2f(S[2][i]));
-    tyz[i] = cvt_f2d(-2.0f * nu * cvt_d2f(S[4][i]));
+    txx[i] = c * (S[0][i] + S[0][ip]);
+    txy[i] = c * (S[1][i] + S[1][ip]);
+    tyy[i] = c * (S[3][i] + S[3][ip]);
+    tzz[i] = c * (S[5][i] + S[5][ip]);
+    txz[i] = -2.0f * nu * S[2][i];
+    tyz[i] = -2.0f * nu * S[4][i];
   }
 }
 
@@ -2286,7 +2294,8 @@ __global__ void k_scalar_prod(const S* __restrict__ um, const S* __restrict__ vm
   }
 }
 // scalars_module.f90:364-407 horizontal SGS fluxes
-__global__ void k_scalar_temp_xy(const double* __restrict__ nut, const double* __restrict__ dsx,
+template <typename NT>
+__global__ void k_scalar_temp_xy(const NT* __restrict__ nut, const double* __restrict__ dsx,
                                  const double* __restrict__ dsy, double* tx, double* ty, int ld, int nx, int ny,
                                  int nz, double pr) {
   const size_t np = (size_t)ld * ny;
@@ -2295,18 +2304,20 @@ __global__ void k_scalar_temp_xy(const double* __restrict__ nut, const double* _
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
     if (jx >= nx) continue;
     if (jz == nz) { tx[i] = 0.0; ty[i] = 0.0; continue; }
+    const double nu = cvt<double, NT>(nut[i]);
     if (jz == 1) {
-      tx[i] = (1.0 / pr) * nut[i] * dsx[i];
-      ty[i] = (1.0 / pr) * nut[i] * dsy[i];
+      tx[i] = (1.0 / pr) * nu * dsx[i];
+      ty[i] = (1.0 / pr) * nu * dsy[i];
     } else {
-      const double f = (1.0 / (0.5 * (pr + pr))) * 0.5 * (nut[i] + nut[i + np]);
+      const double f = (1.0 / (0.5 * (pr + pr))) * 0.5 * (nu + cvt<double, NT>(nut[i + np]));
       tx[i] = f * dsx[i];
       ty[i] = f * dsy[i];
     }
   }
 }
 // scalars_module.f90:385-452 RHS assembly with the SGS divergence
-__global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const double* __restrict__ nut,
+template <typename NT>
+__global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const NT* __restrict__ nut,
                              const double* __restrict__ dsz, const double* __restrict__ sgs_t3, int ld, int nx,
                              int ny, int nz, double pr, double cdz) {
   const size_t np = (size_t)ld * ny;
@@ -2317,13 +2328,43 @@ __global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const do
     if (jx >= nx) continue;
     const int jy = (int)(r / ld);
     // temp(k) = Nu_t dsdz / Pr on w-nodes, temp(1) = -surf_flux
-    const double t0 = (jz == 1) ? -1.0 * sgs_t3[(size_t)jy * nx + jx] : (1.0 / pr) * nut[i] * dsz[i];
-    const double t1 = (1.0 / pr) * nut[i + np] * dsz[i + np];
+    const double t0 =
+        (jz == 1) ? -1.0 * sgs_t3[(size_t)jy * nx + jx] : (1.0 / pr) * cvt<double, NT>(nut[i]) * dsz[i];
+    const double t1 = (1.0 / pr) * cvt<double, NT>(nut[i + np]) * dsz[i + np];
     R[i] = (-1.0 * R[i] + dxy[i]) + cdz * (t1 - t0);
   }
 }
 // scalars_module.f90:175-228 calcbeta from per-level plane sums
 // per level: sb = plane mean of theta, 1/sb (the divisions once per level)
+// Mixed form: the same from FP32 inputs (the horizontal divergences h from
+// FP32 transforms, the FP32-held tau) in FP32 arithmetic, the FP64 outputs
+// widened exactly.  grid (ceil(np/256), nz).
+__global__ void __launch_bounds__(256) k_divstress_fin32(double* __restrict__ divx, double* __restrict__ divy,
+                                                         double* __restrict__ divz, const float* __restrict__ hx,
+                                                         const float* __restrict__ hy,
+                                                         const float* __restrict__ hz,
+                                                         const float* __restrict__ txz,
+                                                         const float* __restrict__ tyz,
+                                                         const float* __restrict__ tzz, int ld, int nx, int ny,
+                                                         int nz, float cdz) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned r = blockIdx.x * 256u + threadIdx.x;
+  if (r >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + r;
+  const bool inx = (int)(r % (unsigned)ld) < nx;
+  if (jz == nz) {
+    divx[i] = LES_BOGUS;
+    divy[i] = LES_BOGUS;
+    divz[i] = inx ? cvt_f2d(hz[i]) : 0.0;
+    return;
+  }
+  if (!inx) { divx[i] = 0.0; divy[i] = 0.0; divz[i] = 0.0; return; }
+  divx[i] = cvt_f2d(hx[i] + cdz * (txz[i + np] - txz[i]));
+  divy[i] = cvt_f2d(hy[i] + cdz * (tyz[i + np] - tyz[i]));
+  divz[i] = cvt_f2d((jz == 1) ? hz[i] : hz[i] + cdz * (tzz[i] - tzz[i - np]));
+}
+
 __global__ void k_calcbeta_levels(const double* __restrict__ sums, double* sbr, int nz, double nxny) {
   for (int j = threadIdx.x; j < nz; j += blockDim.x) {
     const double sb = sums[j] / nxny;
@@ -2399,7 +2440,7 @@ int op_theta(les_ctx* c) {
   double* tx = c->tmp;
   double* ty = c->tmp + g.nfield;
   double* dxy = c->tmp + 2 * g.nfield;
-  k_scalar_temp_xy<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
+  k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
                                                           g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
   {
     const double sc = 1.0 / (double)(g.nx * g.ny);
@@ -2412,7 +2453,7 @@ int op_theta(les_ctx* c) {
     cols(c, J);
     c2r(c, 1, nz, c->wsB, &dxy, (long)g.nplane, false, g.lh);
   }
-  k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
+  k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
                                                                  c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
                                                                  1.0 / g.dz); LES_COUNT_LAUNCH();
   // calcbeta on theta before the update
@@ -2462,8 +2503,9 @@ int op_rmsdiv(les_ctx* c, double* out_dev) {
   k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev); LES_COUNT_LAUNCH();
   return 0;
 }
+template <typename NT>
 __global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const double* __restrict__ v,
-                                             const double* __restrict__ w, const double* __restrict__ nut,
+                                             const double* __restrict__ w, const NT* __restrict__ nut,
                                              double* out, int ld, int nx, int ny, int nz) {
   __shared__ double s1[512], s2[512];
   double m1 = -1e300, m2 = -1e300;
@@ -2472,7 +2514,7 @@ __global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const
     const size_t jx = e % nx, r = e / nx;
     const size_t i = jx + (size_t)ld * r;
     m1 = fmax(m1, u[i] * u[i] + v[i] * v[i] + w[i] * w[i]);
-    m2 = fmax(m2, nut[i]);
+    m2 = fmax(m2, cvt<double, NT>(nut[i]));
   }
   s1[threadIdx.x] = m1; s2[threadIdx.x] = m2;
   __syncthreads();
@@ -2487,8 +2529,13 @@ __global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const
 }
 int op_tsc(les_ctx* c, double* cflu, double* visc) {
   const Grid& g = c->g;
-  k_tsc<<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_NU_T], c->dscal + 2, g.ld, g.nx,
-                                  g.ny, g.nz); LES_COUNT_LAUNCH();
+  if (c->cfg.precision == 1)
+    k_tsc<float><<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], f32(c, LES_NU_T), c->dscal + 2,
+                                           g.ld, g.nx, g.ny, g.nz);
+  else
+    k_tsc<double><<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_NU_T], c->dscal + 2,
+                                            g.ld, g.nx, g.ny, g.nz);
+  LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 2, c->dscal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   const double delta = std::min(g.dx, g.dy);
@@ -2802,7 +2849,7 @@ __global__ void k_lag_spec32(const C2* __restrict__ U, const C2* __restrict__ V,
 // Mixed form lagrange_Sdep.f90:142-266 products: the shift about the plane
 // mean in FP64, the products and |S| S_ij in FP32
 __global__ void k_lag_prod32(const double* __restrict__ u, const double* __restrict__ v,
-                             const double* __restrict__ w, Ptr6 Sp, float* out, int ld, int jz0, int nlev,
+                             const double* __restrict__ w, Ptr6f Sp, float* out, int ld, int jz0, int nlev,
                              size_t np, const C2* __restrict__ U, const C2* __restrict__ V, size_t nk) {
   const size_t tot = np * nlev;
   GSTRIDE(t, tot) {
@@ -2821,8 +2868,8 @@ __global__ void k_lag_prod32(const double* __restrict__ u, const double* __restr
     float* o = out + t;
     o[0] = ub * ub; o[stride] = ub * vb; o[2 * stride] = ub * wb;
     o[3 * stride] = vb * vb; o[4 * stride] = vb * wb; o[5 * stride] = wb * wb;
-    const float s11 = cvt_d2f(Sp.p[0][i]), s12 = cvt_d2f(Sp.p[1][i]), s13 = cvt_d2f(Sp.p[2][i]);
-    const float s22 = cvt_d2f(Sp.p[3][i]), s23 = cvt_d2f(Sp.p[4][i]), s33 = cvt_d2f(Sp.p[5][i]);
+    const float s11 = Sp.p[0][i], s12 = Sp.p[1][i], s13 = Sp.p[2][i];
+    const float s22 = Sp.p[3][i], s23 = Sp.p[4][i], s33 = Sp.p[5][i];
     const float Sm = sqrtf(2.0f * (s11 * s11 + s22 * s22 + s33 * s33 + 2.0f * (s12 * s12 + s13 * s13 + s23 * s23)));
     o[6 * stride] = Sm * s11; o[7 * stride] = Sm * s12; o[8 * stride] = Sm * s13;
     o[9 * stride] = Sm * s22; o[10 * stride] = Sm * s23; o[11 * stride] = Sm * s33;
@@ -2889,6 +2936,8 @@ static int lagrangeT(les_ctx* c) {
   Ptr6 Sp;
   const int sid[6] = {LES_S11, LES_S12, LES_S13, LES_S22, LES_S23, LES_S33};
   for (int q = 0; q < 6; ++q) Sp.p[q] = c->f[sid[q]];
+  Ptr6f Sf;  // the mixed form's FP32-held strain
+  for (int q = 0; q < 6; ++q) Sf.p[q] = f32(c, sid[q]);
   const C2* U = c->spec;
   const C2* V = c->spec + (size_t)g.nz * g.C;
   const C2* W = c->spec + (size_t)2 * g.nz * g.C;
@@ -2909,7 +2958,7 @@ static int lagrangeT(les_ctx* c) {
                                                                   c->ky, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz,
                                                                   MX ? 1 : 0); LES_COUNT_LAUNCH();
     if constexpr (MX)
-      k_lag_prod32<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod,
+      k_lag_prod32<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sf, prod,
                                                                 g.ld, jz0, nl, g.nplane, U, V, g.C);
     else
       k_lag_prod<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
@@ -2954,9 +3003,9 @@ static int sgs_stagT(les_ctx* c) {
   const dim3 gpl((unsigned)((g.nplane + 255) / 256), (unsigned)g.nz);
   if (MX)
     k_calc_sij32<<<gpl, 256, 0, c->stream>>>(
-        c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
-        c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
-        c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
+        f32(c, LES_DUDX), f32(c, LES_DUDY), c->f[LES_DUDZ], f32(c, LES_DVDX), f32(c, LES_DVDY), c->f[LES_DVDZ],
+        f32(c, LES_DWDX), f32(c, LES_DWDY), c->f[LES_DWDZ], f32(c, LES_S11), f32(c, LES_S12), f32(c, LES_S13),
+        f32(c, LES_S22), f32(c, LES_S23), f32(c, LES_S33), c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
         c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, lag ? 1 : 0);
   else
     k_calc_sij<<<grid1(g.nfield), 256, 0, c->stream>>>(
@@ -2983,11 +3032,13 @@ static int sgs_stagT(les_ctx* c) {
     csov = (double)(c016 * c016);
   }
   if (MX) {
-    Ptr6c Sp;
-    for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
-    k_nut_tau32<<<gpl, 256, 0, c->stream>>>(Sp, c->f[LES_CS_OPT2], c->f[LES_NU_T], c->f[LES_TXX], c->f[LES_TXY],
-                                            c->f[LES_TYY], c->f[LES_TXZ], c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx,
-                                            g.ny, g.nz, (float)(g.delta * g.delta), ov, csov); LES_COUNT_LAUNCH();
+    Ptr6f Sp;
+    const int sid[6] = {LES_S11, LES_S12, LES_S13, LES_S22, LES_S23, LES_S33};
+    for (int q = 0; q < 6; ++q) Sp.p[q] = f32(c, sid[q]);
+    k_nut_tau32<<<gpl, 256, 0, c->stream>>>(Sp, c->f[LES_CS_OPT2], f32(c, LES_NU_T), f32(c, LES_TXX),
+                                            f32(c, LES_TXY), f32(c, LES_TYY), f32(c, LES_TXZ), f32(c, LES_TYZ),
+                                            f32(c, LES_TZZ), g.ld, g.nx, g.ny, g.nz, (float)(g.delta * g.delta), ov,
+                                            csov); LES_COUNT_LAUNCH();
     return 0;
   }
   k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
@@ -3081,11 +3132,14 @@ template <bool MX>
 static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
   typedef typename PX<MX>::T T;
   typedef typename PX<MX>::CX CX;
+  typedef typename std::conditional<MX, float, double>::type TS;  // tau and h storage
   const Grid& g = c->g;
   const double sc = 1.0 / (double)(g.nx * g.ny);
-  const double* in[5] = {c->f[LES_TXX], c->f[LES_TXY], c->f[LES_TYY], c->f[LES_TXZ], c->f[LES_TYZ]};
+  const TS* in[5];
+  const int tid[5] = {LES_TXX, LES_TXY, LES_TYY, LES_TXZ, LES_TYZ};
+  for (int q = 0; q < 5; ++q) in[q] = reinterpret_cast<const TS*>(c->f[tid[q]]);
   double scs[5] = {sc, sc, sc, sc, sc};
-  r2cT<T, double>(c, 5, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  r2cT<T, TS>(c, 5, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
   const long FS = (long)g.nz * g.C;
   ColJob J = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
   J.nin = 3; J.nout = 2;
@@ -3100,11 +3154,17 @@ static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
   K.out[0] = (CX*)c->wsB + 2 * FS;
   K.coef[0][0] = CC_IKX; K.coef[0][1] = CC_IKY;
   colsT<T, CX>(c, K);
-  double* h[3] = {c->tmp, c->tmp + g.nfield, c->tmp + 2 * g.nfield};
-  c2rT<T, double>(c, 3, g.nz, c->wsB, h, (long)g.nplane, false, g.lh);
-  k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divtx, divty, divtz, h[0], h[1], h[2], c->f[LES_TXZ],
-                                                         c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz,
-                                                         1.0 / g.dz, 7);
+  TS* tmpS = reinterpret_cast<TS*>(c->tmp);
+  TS* h[3] = {tmpS, tmpS + g.nfield, tmpS + 2 * g.nfield};
+  c2rT<T, TS>(c, 3, g.nz, c->wsB, h, (long)g.nplane, false, g.lh);
+  if constexpr (MX)
+    k_divstress_fin32<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)g.nz), 256, 0, c->stream>>>(
+        divtx, divty, divtz, h[0], h[1], h[2], f32(c, LES_TXZ), f32(c, LES_TYZ), f32(c, LES_TZZ), g.ld, g.nx, g.ny,
+        g.nz, (float)(1.0 / g.dz));
+  else
+    k_divstress_fin<<<grid1(g.nfield), 256, 0, c->stream>>>(divtx, divty, divtz, h[0], h[1], h[2], c->f[LES_TXZ],
+                                                           c->f[LES_TYZ], c->f[LES_TZZ], g.ld, g.nx, g.ny, g.nz,
+                                                           1.0 / g.dz, 7);
   LES_COUNT_LAUNCH();
   return 0;
 }
@@ -3177,10 +3237,12 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   double* tx = c->tmp;
   double* ty = c->tmp + g.nfield;
   double* dxy = c->tmp + 2 * g.nfield;
-  k_scalar_temp_xy<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
+  typedef typename std::conditional<MX, float, double>::type NUT;  // Nu_t storage
+  const NUT* nut = reinterpret_cast<const NUT*>(c->f[LES_NU_T]);
+  k_scalar_temp_xy<NUT><<<grid1(g.nfield), 256, 0, c->stream>>>(nut, c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
                                                           g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
   div_xyT<MX>(c, tx, ty, dxy, nz);
-  k_scalar_rhs<<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
+  k_scalar_rhs<NUT><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, nut, c->f[LES_DTDZ],
                                                                  c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
                                                                  1.0 / g.dz); LES_COUNT_LAUNCH();
   calcbeta(c);
