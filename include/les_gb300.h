@@ -123,8 +123,8 @@ unsigned long long les_kernel_launch_count(void);
 int les_set_surface(les_ctx* ctx, const double* zo, const double* wt_s);
 /* Copy one module array host -> device / device -> host.  Real fields are
  * (ld,ny,nz), LES_P is (ld,ny,nz+1), surface planes are (nx,ny).  A
- * precision-1 context holds the horizontal velocity gradients, S_ij, Nu_t
- * and tau_ij in FP32 (same layout, FP32 values in the first half of the
+ * precision-1 context holds the horizontal velocity and theta gradients,
+ * S_ij, Nu_t and tau_ij in FP32 (same layout, FP32 values in the first half of the
  * array); these copies and les_sync_* narrow / widen them, and
  * les_field_device_ptr returns that FP32 storage.  The per-routine entries
  * les_convec, les_sgs_stag, les_wallstress and les_theta_all_in_one need a

@@ -86,7 +86,7 @@ void cols_reg(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
   }
   const int ntile = (J.ncols + TX - 1) / TX;
   const int nitems = ntile * J.nlev * (J.nf > 0 ? J.nf : 1);
-  const int nblk = std::min(nitems, 2 * nsm);  // two resident CTAs per SM (registers, shared memory)
+  const int nblk = std::min(nitems, 3 * nsm);  // three resident CTAs per SM (registers, shared memory)
   k_colsr<T, TX, CIn, R><<<nblk, TX * R, smf, s>>>(J, P, ntile, nitems);
 }
 

@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
   const TIn* src = reinterpret_cast<const TIn*>(J.phys[f]) + (size_t)lev * J.pstride_phys;
   const T s = (T)J.scale[f];
   const T dv = (T)J.div[f];
+  const T sd = (T)(J.div[f] != 0.0 ? J.scale[f] / J.div[f] : J.scale[f]);
   const double off = J.off[f] ? J.off[f][lev] : 0.0;
   for (int t = threadIdx.x; t < nrow * m; t += blockDim.x) {
     const int r = NF > 0 ? t / NF : (int)P.dm.div((unsigned)t), k = t - r * m;
@@ -75,8 +76,12 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
       a = cvt<T, TIn>(pr.x);
       b = cvt<T, TIn>(pr.y);
     }
-    if (dv != (T)0) { a = a / dv; b = b / dv; }
-    A[r * rs + (NF > 0 ? sk(k) : k)] = mk<T>(a * s, b * s);
+    if constexpr (std::is_same<T, double>::value) {  // the reference's division, then the scale
+      if (dv != (T)0) { a = a / dv; b = b / dv; }
+      A[r * rs + (NF > 0 ? sk(k) : k)] = mk<T>(a * s, b * s);
+    } else {  // FP32 / float-float: one product with scale/div (formed in FP64)
+      A[r * rs + (NF > 0 ? sk(k) : k)] = mk<T>(a * sd, b * sd);
+    }
   }
   __syncthreads();
   C* Z;
@@ -192,8 +197,7 @@ __global__ void __launch_bounds__(NT) k_r2c_reg(RowJob J, RealPlanDev P) {
   C* Sr = S + (r < RPB ? r : 0) * MS;
   C v[TT];
   if (q < N1) {
-    const T s = (T)J.scale[f];
-    const T dv = (T)J.div[f];
+    const T sd = (T)(J.div[f] != 0.0 ? J.scale[f] / J.div[f] : J.scale[f]);  // scale/div, one product
     const bool hasoff = J.off[f] != nullptr;
     const double off = hasoff ? J.off[f][lev] : 0.0;
     const CI* src = reinterpret_cast<const CI*>(reinterpret_cast<const TIn*>(J.phys[f]) +
@@ -211,8 +215,7 @@ __global__ void __launch_bounds__(NT) k_r2c_reg(RowJob J, RealPlanDev P) {
           a = cvt<T, TIn>(pr.x);
           b = cvt<T, TIn>(pr.y);
         }
-        if (dv != (T)0) { a = a / dv; b = b / dv; }
-        v[i] = mk<T>(a * s, b * s);
+        v[i] = mk<T>(a * sd, b * sd);
       }
     }
   }
@@ -622,7 +625,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // previous one.  A thread reads back only what it staged itself, so the
 // staging needs no barrier.  8-byte elements (FP32 complex).
 template <typename T, int TX, typename CIn, int R>
-__global__ void __launch_bounds__(TX * R, 2) k_colsr(ColJob J, FftPlanDev P, int ntile, int nitems) {
+__global__ void __launch_bounds__(TX * R, 3) k_colsr(ColJob J, FftPlanDev P, int ntile, int nitems) {
   typedef typename CT<T>::type C;
   static_assert(sizeof(CIn) == 8 && sizeof(C) == 8, "8-byte complex elements");
   constexpr int N = R * R;

@@ -100,8 +100,8 @@ struct les_ctx {
 
 namespace les {
 // An FP32-mixed context (precision 1) holds these SGS intermediates in FP32:
-// the horizontal velocity gradients (FP32 transforms), S_ij, Nu_t and
-// tau_ij.  Each keeps its FP64 allocation and (ld, ny, nz) layout; the FP32
+// the horizontal velocity and theta gradients (FP32 transforms), S_ij, Nu_t
+// and tau_ij.  Each keeps its FP64 allocation and (ld, ny, nz) layout; the FP32
 // values sit in the first half.  les_get_field / les_set_field convert.
 inline bool mixed_f32_field(int f) {
   switch (f) {
@@ -109,6 +109,7 @@ inline bool mixed_f32_field(int f) {
     case LES_S11: case LES_S12: case LES_S13: case LES_S22: case LES_S23: case LES_S33:
     case LES_NU_T:
     case LES_TXX: case LES_TXY: case LES_TYY: case LES_TXZ: case LES_TYZ: case LES_TZZ:
+    case LES_DTDX: case LES_DTDY:
       return true;
     default:
       return false;

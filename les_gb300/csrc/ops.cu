@@ -156,41 +156,41 @@ static int cols(les_ctx* c, const ColJob& J) { return colsT<double, double2>(c, 
 // ---------------------------------------------------------------------------
 // deterministic reductions (fixed order: one CTA per plane, fixed tree)
 // mode 0: sum f[plane](1:nx,1:ny)
-__global__ void __launch_bounds__(512) k_plane_sum(const double* f, long pstride, int ld, int nx, int ny,
-                                                   double* out) {
-  __shared__ double sh[512];
-  const double* p = f + (size_t)blockIdx.x * pstride;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
-    const int jy = i / nx, jx = i - jy * nx;
-    s += p[(size_t)jy * ld + jx];
+// Sum of f(1:nx,1:ny) of one plane per block (512 threads): warp w takes rows
+// w, w+16, ..; lane l the columns l, l+32, ..; four independent partial sums
+// per thread, then a fixed-order tree, so the result is deterministic.
+__device__ __forceinline__ double plane_sum_block(const double* p, int ld, int nx, int ny, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  for (int jy = wid; jy < ny; jy += 16) {
+    const double* row = p + (size_t)jy * ld;
+    int jx = lane;
+    for (; jx + 96 < nx; jx += 128) {
+      a0 += row[jx]; a1 += row[jx + 32]; a2 += row[jx + 64]; a3 += row[jx + 96];
+    }
+    for (; jx < nx; jx += 32) a0 += row[jx];
   }
-  sh[threadIdx.x] = s;
+  sh[threadIdx.x] = (a0 + a1) + (a2 + a3);
   __syncthreads();
   for (int w = 256; w > 0; w >>= 1) {
     if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+  return sh[0];
+}
+__global__ void __launch_bounds__(512) k_plane_sum(const double* f, long pstride, int ld, int nx, int ny,
+                                                   double* out) {
+  __shared__ double sh[512];
+  const double t = plane_sum_block(f + (size_t)blockIdx.x * pstride, ld, nx, ny, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = t;
 }
 
 // per-level plane means of f(1:nx,1:ny,lev) (same fixed order as k_plane_sum)
 __global__ void __launch_bounds__(512) k_plane_mean(const double* f, long pstride, int ld, int nx, int ny,
                                                     double* out) {
   __shared__ double sh[512];
-  const double* p = f + (size_t)blockIdx.x * pstride;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
-    const int jy = i / nx, jx = i - jy * nx;
-    s += p[(size_t)jy * ld + jx];
-  }
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = 256; w > 0; w >>= 1) {
-    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[blockIdx.x] = sh[0] / (double)(nx * ny);
+  const double t = plane_sum_block(f + (size_t)blockIdx.x * pstride, ld, nx, ny, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = t / (double)(nx * ny);
 }
 
 // ---------------------------------------------------------------------------
@@ -2365,6 +2365,41 @@ __global__ void __launch_bounds__(256) k_divstress_fin32(double* __restrict__ di
   divz[i] = cvt_f2d((jz == 1) ? hz[i] : hz[i] + cdz * (tzz[i] - tzz[i - np]));
 }
 
+// Mixed-form scalar flux kernels, grid (ceil(np/256), levels): FP32 inputs
+// (Nu_t, the theta gradients, the advection term and the flux divergence
+// come from FP32 arithmetic and transforms), FP32 arithmetic; dsz (theta
+// differences, FP64) and the surface flux are read in FP64 and narrowed.
+__global__ void __launch_bounds__(256) k_scalar_temp_xy32(const float* __restrict__ nut,
+                                                          const float* __restrict__ dsx,
+                                                          const float* __restrict__ dsy, float* tx, float* ty,
+                                                          int ld, int nx, int ny, int nz, float ipr) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned r = blockIdx.x * 256u + threadIdx.x;
+  if (r >= np || (int)(r % (unsigned)ld) >= nx) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + r;
+  if (jz == nz) { tx[i] = 0.0f; ty[i] = 0.0f; return; }
+  const float f = (jz == 1) ? ipr * nut[i] : ipr * 0.5f * (nut[i] + nut[i + np]);
+  tx[i] = f * dsx[i];
+  ty[i] = f * dsy[i];
+}
+__global__ void __launch_bounds__(256) k_scalar_rhs32(double* R, const float* __restrict__ adv,
+                                                      const float* __restrict__ dxy, const float* __restrict__ nut,
+                                                      const double* __restrict__ dsz,
+                                                      const double* __restrict__ sgs_t3, int ld, int nx, int ny,
+                                                      float ipr, float cdz) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned r = blockIdx.x * 256u + threadIdx.x;
+  if (r >= np) return;
+  const int jy = (int)(r / (unsigned)ld), jx = (int)(r - (unsigned)jy * ld);
+  if (jx >= nx) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + r;
+  const float t0 = (jz == 1) ? -cvt_d2f(sgs_t3[(size_t)jy * nx + jx]) : ipr * nut[i] * cvt_d2f(dsz[i]);
+  const float t1 = ipr * nut[i + np] * cvt_d2f(dsz[i + np]);
+  R[i] = cvt_f2d((-adv[i] + dxy[i]) + cdz * (t1 - t0));
+}
+
 __global__ void k_calcbeta_levels(const double* __restrict__ sums, double* sbr, int nz, double nxny) {
   for (int j = threadIdx.x; j < nz; j += blockDim.x) {
     const double sb = sums[j] / nxny;
@@ -3065,8 +3100,8 @@ static void padT(les_ctx* c, const CIn* spec, int nf, typename PX<MX>::S* const*
 }
 
 // dealias2 of nf big fields (already scaled) into FP64 small fields
-template <bool MX>
-static void unpadT(les_ctx* c, typename PX<MX>::S* const* in, double* const* out, int nf, int nlev, double scale) {
+template <bool MX, typename TO = double>
+static void unpadT(les_ctx* c, typename PX<MX>::S* const* in, TO* const* out, int nf, int nlev, double scale) {
   typedef typename PX<MX>::T T;
   typedef typename PX<MX>::CX CX;
   typedef typename PX<MX>::S S;
@@ -3082,24 +3117,25 @@ static void unpadT(les_ctx* c, typename PX<MX>::S* const* in, double* const* out
   J.out[0] = c->wsB; J.fs_out = (long)nlev * g.C;
   J.coef[0][0] = CC_ONE;
   colsT<T, CX>(c, J);
-  c2rT<T, double>(c, nf, nlev, c->wsB, out, (long)g.nplane, false, g.nx / 2);
+  c2rT<T, TO>(c, nf, nlev, c->wsB, out, (long)g.nplane, false, g.nx / 2);
 }
 
-// ddx + ddy of two FP64 fields summed in spectral space (one inverse)
-template <bool MX>
-static void div_xyT(les_ctx* c, const double* tx, const double* ty, double* out, int nlev) {
+// ddx + ddy of two fields summed in spectral space (one inverse); TS: their
+// storage (FP64, or FP32 in the mixed form's scalar flux)
+template <bool MX, typename TS = double>
+static void div_xyT(les_ctx* c, const TS* tx, const TS* ty, TS* out, int nlev) {
   typedef typename PX<MX>::T T;
   typedef typename PX<MX>::CX CX;
   const Grid& g = c->g;
   const double sc = 1.0 / (double)(g.nx * g.ny);
-  const double* ii[2] = {tx, ty};
+  const TS* ii[2] = {tx, ty};
   const double s2[2] = {sc, sc};
-  r2cT<T, double>(c, 2, nlev, ii, (long)g.nplane, s2, nullptr, c->wsA, false, g.lh);
+  r2cT<T, TS>(c, 2, nlev, ii, (long)g.nplane, s2, nullptr, c->wsA, false, g.lh);
   ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nlev);
   J.nin = 2; J.nout = 1; J.in[0] = c->wsA; J.in[1] = (CX*)c->wsA + (size_t)nlev * g.C; J.out[0] = c->wsB;
   J.coef[0][0] = CC_IKX; J.coef[0][1] = CC_IKY;
   colsT<T, CX>(c, J);
-  c2rT<T, double>(c, 1, nlev, c->wsB, &out, (long)g.nplane, false, g.lh);
+  c2rT<T, TS>(c, 1, nlev, c->wsB, &out, (long)g.nplane, false, g.lh);
 }
 
 // rmsdiv.f90:93-100 for the mixed form: its SGS-only dudx, dvdy are FP32
@@ -3197,9 +3233,17 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     J.out[0] = c->wsB; J.out[1] = (CX*)c->wsB + FS; J.out[2] = (CX*)c->wsB + 2 * FS; J.out[3] = specT;
     J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY; J.coef[3][0] = CC_KILL;
     colsT<T, CX>(c, J);
-    double* out[3] = {c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY]};
-    const double* offo[3] = {th0, nullptr, nullptr};
-    c2rT<T, double>(c, 3, nz, c->wsB, out, (long)g.nplane, false, g.lh, offo);
+    if constexpr (MX) {  // theta in FP64 (plane mean added back), the gradients FP32-held
+      double* o1[1] = {c->f[LES_THETA]};
+      const double* offo[1] = {th0};
+      c2rT<T, double>(c, 1, nz, c->wsB, o1, (long)g.nplane, false, g.lh, offo);
+      float* o2[2] = {f32(c, LES_DTDX), f32(c, LES_DTDY)};
+      c2rT<T, float>(c, 2, nz, (CX*)c->wsB + FS, o2, (long)g.nplane, false, g.lh);
+    } else {
+      double* out[3] = {c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY]};
+      const double* offo[3] = {th0, nullptr, nullptr};
+      c2rT<T, double>(c, 3, nz, c->wsB, out, (long)g.nplane, false, g.lh, offo);
+    }
   }
   op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
   fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
@@ -3228,23 +3272,45 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   }
   k_scalar_prod<S><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
                                                               bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
-  double* rt = c->f[LES_RHS_T];
-  {
-    S* b6[1] = {bigf[6]};
-    double* o[1] = {rt};
-    unpadT<MX>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+  if constexpr (MX) {
+    // FP32 scalar flux: the advection term, tx, ty and their divergence in
+    // FP32 scratch (tmp), the theta RHS itself FP64
+    float* tf = reinterpret_cast<float*>(c->tmp);
+    float* tx = tf;
+    float* ty = tf + g.nfield;
+    float* dxy = tf + 2 * g.nfield;
+    float* rtf = tf + 3 * g.nfield;
+    {
+      S* b6[1] = {bigf[6]};
+      float* o[1] = {rtf};
+      unpadT<MX, float>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+    }
+    const dim3 gpl((unsigned)((g.nplane + 255) / 256), (unsigned)nz);
+    k_scalar_temp_xy32<<<gpl, 256, 0, c->stream>>>(f32(c, LES_NU_T), f32(c, LES_DTDX), f32(c, LES_DTDY), tx, ty,
+                                                   g.ld, g.nx, g.ny, nz, (float)(1.0 / k.pr)); LES_COUNT_LAUNCH();
+    div_xyT<MX, float>(c, tx, ty, dxy, nz);
+    k_scalar_rhs32<<<dim3(gpl.x, (unsigned)(nz - 1)), 256, 0, c->stream>>>(
+        c->f[LES_RHS_T], rtf, dxy, f32(c, LES_NU_T), c->f[LES_DTDZ], c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny,
+        (float)(1.0 / k.pr), (float)(1.0 / g.dz)); LES_COUNT_LAUNCH();
+  } else {
+    double* rt = c->f[LES_RHS_T];
+    {
+      S* b6[1] = {bigf[6]};
+      double* o[1] = {rt};
+      unpadT<MX>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+    }
+    double* tx = c->tmp;
+    double* ty = c->tmp + g.nfield;
+    double* dxy = c->tmp + 2 * g.nfield;
+    k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX],
+                                                                    c->f[LES_DTDY], tx, ty, g.ld, g.nx, g.ny, nz,
+                                                                    k.pr); LES_COUNT_LAUNCH();
+    div_xyT<MX>(c, tx, ty, dxy, nz);
+    k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T],
+                                                                           c->f[LES_DTDZ], c->f[LES_SGS_T3_SFC],
+                                                                           g.ld, g.nx, g.ny, nz, k.pr, 1.0 / g.dz);
+    LES_COUNT_LAUNCH();
   }
-  double* tx = c->tmp;
-  double* ty = c->tmp + g.nfield;
-  double* dxy = c->tmp + 2 * g.nfield;
-  typedef typename std::conditional<MX, float, double>::type NUT;  // Nu_t storage
-  const NUT* nut = reinterpret_cast<const NUT*>(c->f[LES_NU_T]);
-  k_scalar_temp_xy<NUT><<<grid1(g.nfield), 256, 0, c->stream>>>(nut, c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
-                                                          g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
-  div_xyT<MX>(c, tx, ty, dxy, nz);
-  k_scalar_rhs<NUT><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, nut, c->f[LES_DTDZ],
-                                                                 c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
-                                                                 1.0 / g.dz); LES_COUNT_LAUNCH();
   calcbeta(c);
   if (c->jt == 1 && !k.initsc)
     cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
