@@ -90,12 +90,28 @@ void cols_reg(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
   k_colsr<T, TX, CIn, R><<<nblk, TX * R, smf, s>>>(J, P, ntile, nitems);
 }
 
+// several inputs summed into at most two outputs, same length N = R * R
+template <typename T, typename CIn, int R>
+void cols_reg_sum(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
+  typedef typename CT<T>::type C;
+  constexpr int TX = 16, N = R * R;
+  const size_t smf = (size_t)(3 * N * TX + N) * sizeof(C);
+  static size_t set = 48 * 1024;
+  raise_smem(k_colsr_sum<T, TX, CIn, R, 2>, smf, set);
+  const dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
+  k_colsr_sum<T, TX, CIn, R, 2><<<grid, TX * R, smf, s>>>(J, P);
+}
+
 template <typename T, int TX, typename CIn, int NIN, int NOUT>
 void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, dim3 grid, cudaStream_t s) {
   typedef typename CT<T>::type C;
   if constexpr (NIN == NOUT && (NIN == 256 || NIN == 64) && std::is_same<T, float>::value) {
     if (J.nin == 1 && J.map == MAP_SAME) {
       cols_reg<T, CIn, NIN == 256 ? 16 : 8>(J, Pin, s);
+      return;
+    }
+    if (J.nin > 1 && J.nout <= 2 && J.map == MAP_SAME) {
+      cols_reg_sum<T, CIn, NIN == 256 ? 16 : 8>(J, Pin, s);
       return;
     }
   }

@@ -703,6 +703,92 @@ __global__ void __launch_bounds__(TX * R, 3) k_colsr(ColJob J, FftPlanDev P, int
   cp_async_wait_all();  // nothing in flight at exit
 }
 
+// Several inputs summed per output (the stress and flux divergences:
+// out_o = sum_i coef(o,i) * in_i), at most NO outputs: each input is loaded
+// and transformed in turn and its contributions are accumulated in shared
+// memory (each thread owns its accumulator slots, so no barrier guards
+// them), so every input is read once and no spectrum goes through global
+// memory.  Same four-step split and exchange as k_colsr.
+template <typename T, int TX, typename CIn, int R, int NO>
+__global__ void __launch_bounds__(TX * R, 2) k_colsr_sum(ColJob J, FftPlanDev P) {
+  typedef typename CT<T>::type C;
+  constexpr int N = R * R;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // exchange: element (i, q) of column b at (i * R + q) * TX + b
+  C* A = S + N * TX;                   // NO accumulators, same index
+  C* tw = A + NO * N * TX;             // exp(-2 pi i m / N), m < N
+  for (int t = threadIdx.x; t < N; t += TX * R) tw[t] = UnitSel<T>::get(P, t);
+  const int b = threadIdx.x % TX, q = threadIdx.x / TX;
+  const int jx = blockIdx.x * TX + b;
+  const bool colok = jx < J.ncols;
+  const int lev = blockIdx.y;
+#pragma unroll
+  for (int o = 0; o < NO; ++o)
+#pragma unroll
+    for (int i = 0; i < R; ++i) A[o * N * TX + (i * R + q) * TX + b] = mk<T>((T)0, (T)0);
+  for (int in = 0; in < J.nin; ++in) {
+    C v[R];
+    const CIn* src = reinterpret_cast<const CIn*>(J.in[in]) + (size_t)lev * J.ps_in + (size_t)blockIdx.z * J.fs_in +
+                     (colok ? jx : 0) + (size_t)q * J.wc_in;
+    const size_t step = (size_t)R * J.wc_in;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      v[i] = mk<T>((T)0, (T)0);
+      if (colok) {
+        const CIn x = src[i * step];
+        v[i] = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
+      }
+    }
+    __syncthreads();  // the previous input's readers of S are done (and the twiddle table is in place)
+    if (J.dir & DIR_FWD) {
+      dft_r<T, R>(v, -1);
+#pragma unroll
+      for (int i = 1; i < R; ++i) v[i] = cmul(v[i], tw[q * i]);
+#pragma unroll
+      for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = v[i];
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < R; ++i) v[i] = S[(q * R + i) * TX + b];
+      dft_r<T, R>(v, -1);  // v[i] = X_in[q + R i]
+    }
+    if (colok) {
+#pragma unroll 1
+      for (int o = 0; o < NO; ++o) {
+        const int code = o < J.nout ? J.coef[o][in] : CC_NONE;
+        if (code != CC_NONE) {
+          C* a = A + o * N * TX + q * TX + b;
+#pragma unroll
+          for (int i = 0; i < R; ++i) a[i * R * TX] = cadd(a[i * R * TX], apply_coef<T>(code, v[i], jx, q + R * i, J));
+        }
+      }
+    }
+  }
+  for (int o = 0; o < J.nout && o < NO; ++o) {
+    C y[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) y[i] = A[o * N * TX + (i * R + q) * TX + b];
+    if ((J.inv_mask >> o) & 1u) {
+      dft_r<T, R>(y, +1);
+#pragma unroll
+      for (int i = 1; i < R; ++i) y[i] = cmul(y[i], cconj(tw[q * i]));
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < R; ++i) S[(i * R + q) * TX + b] = y[i];
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < R; ++i) y[i] = S[(q * R + i) * TX + b];
+      dft_r<T, R>(y, +1);
+    }
+    if (colok) {
+      C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out + jx +
+               (size_t)q * J.wc_out;
+      const size_t step = (size_t)R * J.wc_out;
+#pragma unroll
+      for (int i = 0; i < R; ++i) dst[i * step] = y[i];
+    }
+  }
+}
+
 // rows per CTA of the x-pass kernels (default when a job gives none)
 template <typename T>
 inline int rows_pc(int nx) {
