@@ -34,16 +34,16 @@ METRIC = "pt-steps/s at 256³: FP32-mixed vs FP64 (≤1e-5 err); p99 ensemble st
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 # Dominant kernel of each form's step (largest share of the ncu launch list
-# of the 256^3 step): the FP32 y-pass transforms (k_cols<float,...>) in the
-# mixed form, the FP64 y-pass transforms (k_cols<double,...>) in the FP64
-# form; les_profile_begin family ids.
-DOMINANT = {"mixed": (2, "k_cols<float> (FP32 y-pass transforms)"),
+# of the 256^3 step): the FP32 y-pass transforms (k_colsr, k_colsr_sum,
+# k_colsf<float,...>) in the mixed form, the FP64 y-pass transforms
+# (k_cols<double,...>) in the FP64 form; les_profile_begin family ids.
+DOMINANT = {"mixed": (2, "k_colsr/k_colsr_sum/k_colsf<float> (FP32 y-pass transforms)"),
             "fp64": (1, "k_cols<double> (FP64 y-pass transforms)")}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of the dominant family, from one ncu capture (1 pass) of the same
 # 256^3 run's timed launches; scales the live algorithmic bytes per launch
 # to the traffic per launch.  Only valid at 256^3.
-TRAFFIC_RATIO = {"mixed": 0.8472, "fp64": 0.9209}
+TRAFFIC_RATIO = {"mixed": 0.8714, "fp64": 0.9209}
 
 
 def parse():
