@@ -306,6 +306,17 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   wavenumbers(k, g, kx, ky, k2);
   filter_G(g, k2, 2.0 * 1.0, G);   // main.f90:166 (filter_size = 1)
   filter_G(g, k2, 4.0 * 1.0, GG);  // main.f90:169
+  {  // the filters are cutoffs: columns beyond the last nonzero one are zero for every ky
+    auto ncols = [&](const std::vector<double>& T) {
+      int n = 0;
+      for (int jy = 0; jy < g.ny; ++jy)
+        for (int jx = 0; jx < g.lh; ++jx)
+          if (T[(size_t)jy * g.lh + jx] != 0.0 && jx + 1 > n) n = jx + 1;
+      return n;
+    };
+    c->ncG = ncols(G);
+    c->ncGG = ncols(GG);
+  }
   const size_t tb = (size_t)g.lh * g.ny * sizeof(double);
   if ((st = dalloc(c, (void**)&c->kx, tb)) || (st = dalloc(c, (void**)&c->ky, tb)) ||
       (st = dalloc(c, (void**)&c->G, tb)) || (st = dalloc(c, (void**)&c->GG, tb)))

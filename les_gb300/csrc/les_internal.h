@@ -63,6 +63,7 @@ struct les_ctx {
   // spectral tables (lh,ny)
   double *kx = nullptr, *ky = nullptr, *G = nullptr, *GG = nullptr;
   float *kxf = nullptr, *kyf = nullptr, *Gf = nullptr, *GGf = nullptr;
+  int ncG = 0, ncGG = 0;  // kx columns holding a nonzero G_test / G_test_test (the rest are zero)
   float2 *kxd = nullptr, *kyd = nullptr;  // kx, ky as float-float pairs
   // FFT plans
   les::HostRealPlan rx, rxb;   // real x-transforms of length nx, nx2

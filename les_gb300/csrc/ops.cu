@@ -3001,7 +3001,11 @@ static int lagrangeT(les_ctx* c) {
                                                               g.C); LES_COUNT_LAUNCH();
     const S* in[12];
     for (int q = 0; q < 12; ++q) in[q] = prod + (size_t)q * nl * g.nplane;
-    r2cT<T, S>(c, 12, nl, in, (long)g.nplane, nullptr, nullptr, xs, false, g.lh);
+    // G_test and G_test_test are cutoffs: only the first ncG (ncGG) kx columns of
+    // the filtered spectra are nonzero, so the x pass stores, the y pass
+    // transforms and the inverse x pass reads only those
+    const int nG = c->ncG, nGG = c->ncGG;
+    r2cT<T, S>(c, 12, nl, in, (long)g.nplane, nullptr, nullptr, xs, false, nG);
     CX* ob = (CX*)c->wsB;
     struct Blk { CX* base; int dir; int code_g, code_gg; int count; int q0; };
     const Blk blks[4] = {{sp, DIR_INV, CC_MASK, CC_MASK4, 3, 0},
@@ -3017,11 +3021,13 @@ static int lagrangeT(les_ctx* c) {
       J.out[1] = ob + (size_t)(21 + b.q0) * FS;
       J.fs_out = FS;
       J.coef[0][0] = b.code_g; J.coef[1][0] = b.code_gg;
+      J.ncols = nG;
       colsT<T, CX>(c, J);
     }
     S* out[42];
     for (int q = 0; q < 42; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
-    c2rT<T, S>(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    c2rT<T, S>(c, 21, nl, c->wsB, out, (long)g.nplane, false, nG);              // G_test outputs
+    c2rT<T, S>(c, 21, nl, ob + (size_t)21 * FS, out + 21, (long)g.nplane, false, nGG);  // G_test_test
     k_lag_final<S, S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
         c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, (S)cst, (S)opftdelta, (S)lagran_dt, bone,
