@@ -62,10 +62,10 @@ static int launch_cols_tx(const ColJob& J, const FftPlanDev& Pin, const FftPlanD
   if (!launch_cols_fixed<T, TX, CIn>(J, Pin, Pout, sm, grid, s)) {
     static size_t sm_set = 48 * 1024;  // opt-in raised once per instantiation (not during capture)
     if (sm > sm_set) {
-      cudaFuncSetAttribute(k_cols<T, TX, CIn, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(k_cols<T, TX, CIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       sm_set = sm;
     }
-    k_cols<T, TX, CIn, 0, 0><<<grid, 256, sm, s>>>(J, Pin, Pout);
+    k_cols<T, TX, CIn><<<grid, 256, sm, s>>>(J, Pin, Pout);
   }
   LES_COUNT_LAUNCH();
   if (pr) {

@@ -364,26 +364,17 @@ __device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT
   }
 }
 
-// NIN, NOUT > 0: the input and output lengths (ny_in, ny_out) at compile time,
-// twiddles of both plans staged in shared memory after the work buffers.
-template <typename T, int TX, typename CIn, int NIN, int NOUT>
+// Runtime lengths (plans Pin, Pout): the fixed-length kernels below cover
+// the lengths the workloads use.
+template <typename T, int TX, typename CIn>
 __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanDev Pout) {
   typedef typename CT<T>::type C;
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr bool FIX = NIN > 0 && NOUT > 0;
-  const int ny_in = FIX ? NIN : J.ny_in, ny_out = FIX ? NOUT : J.ny_out;
+  const int ny_in = J.ny_in, ny_out = J.ny_out;
   const int nymax = max(ny_in, ny_out);
-  // row slots per buffer (skewed layout when FIX: row i at sk(i))
-  const int pin = FIX ? skn(NIN) : ny_in, pmax = FIX ? skn(NIN > NOUT ? NIN : NOUT) : nymax;
   C* IN = reinterpret_cast<C*>(smraw);
-  C* A = IN + J.nin * pin * TX;
-  C* B = A + pmax * TX;
-  C* twi = B + pmax * TX;  // FIX: unit-circle tables of the input (NIN) and output (NOUT) lengths
-  C* two = twi + NIN;
-  if constexpr (FIX) {
-    for (int t = threadIdx.x; t < NIN; t += 256) twi[t] = UnitSel<T>::get(Pin, t);
-    for (int t = threadIdx.x; t < NOUT; t += 256) two[t] = UnitSel<T>::get(Pout, t);
-  }
+  C* A = IN + J.nin * ny_in * TX;
+  C* B = A + nymax * TX;
   const int jx0 = blockIdx.x * TX;
   const int lev = blockIdx.y;
   for (int i = 0; i < J.nin; ++i) {
@@ -396,18 +387,16 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
         const CIn x = src[(size_t)row * J.wc_in + jx];
         v = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
       }
-      IN[i * pin * TX + (FIX ? sk(row) : row) * TX + b] = v;
+      IN[i * ny_in * TX + row * TX + b] = v;
     }
   }
   __syncthreads();
   if (J.dir & DIR_FWD) {
     for (int i = 0; i < J.nin; ++i) {
-      C* xi = IN + i * pin * TX;
-      C* r;
-      if constexpr (FIX) r = fft_ct<T, true, NIN, TX, -1, 256, CtMaxR<T>::v>(xi, A, twi, TX);
-      else r = fft_smem<T, true>(xi, A, TX, 0, Pin, -1);
+      C* xi = IN + i * ny_in * TX;
+      C* r = fft_smem<T, true>(xi, A, TX, 0, Pin, -1);
       if (r != xi) {
-        for (int t = threadIdx.x; t < pin * TX; t += blockDim.x) xi[t] = r[t];
+        for (int t = threadIdx.x; t < ny_in * TX; t += blockDim.x) xi[t] = r[t];
         __syncthreads();
       }
     }
@@ -435,23 +424,19 @@ __global__ void __launch_bounds__(256) k_cols(ColJob J, FftPlanDev Pin, FftPlanD
       if (rin >= 0 && jx < J.ncols) {
         for (int i = 0; i < J.nin; ++i) {
           const int code = J.coef[o][i];
-          if (code != CC_NONE)
-            acc = cadd(acc, apply_coef<T>(code, IN[i * pin * TX + (FIX ? sk(rin) : rin) * TX + b], jx, js, J));
+          if (code != CC_NONE) acc = cadd(acc, apply_coef<T>(code, IN[i * ny_in * TX + rin * TX + b], jx, js, J));
         }
       }
-      A[(FIX ? sk(row) : row) * TX + b] = acc;
+      A[row * TX + b] = acc;
     }
     __syncthreads();
     C* r = A;
-    if ((J.inv_mask >> o) & 1u) {
-      if constexpr (FIX) r = fft_ct<T, true, NOUT, TX, +1, 256, CtMaxR<T>::v>(A, B, two, TX);
-      else r = fft_smem<T, true>(A, B, TX, 0, Pout, +1);
-    }
+    if ((J.inv_mask >> o) & 1u) r = fft_smem<T, true>(A, B, TX, 0, Pout, +1);
     C* dst = reinterpret_cast<C*>(J.out[o]) + (size_t)lev * J.ps_out + (size_t)blockIdx.z * J.fs_out;
     for (int t = threadIdx.x; t < ny_out * TX; t += blockDim.x) {
       const int row = t / TX, b = t - row * TX;
       const int jx = jx0 + b;
-      if (jx < J.ncols) dst[(size_t)row * J.wc_out + jx] = r[(FIX ? sk(row) : row) * TX + b];
+      if (jx < J.ncols) dst[(size_t)row * J.wc_out + jx] = r[row * TX + b];
     }
     __syncthreads();
   }

@@ -5,6 +5,8 @@ transforms in FP32 with FP32 3/2-grid and filter temporaries; u, v, w, theta,
 the AB2 update, filt_da of the velocity, the pressure solve and the plane
 (wall-stress, mean-profile) quantities stay FP64.  Targets: relative error
 <= 1e-5 on the velocity field, rmsdiv <= 1e-10."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -17,14 +19,16 @@ def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-def run(n, steps, prec, seed=3):
-    cfg = lg.make_config(n, s_flag=1, jt_total0=500, precision=prec, rmsdiv_every=10)
+def run(n, steps, prec, seed=3, levels=None, rmsdiv_every=10):
+    cfg = lg.make_config(n, nz_levels=levels, s_flag=1, jt_total0=500, precision=prec,
+                         rmsdiv_every=rmsdiv_every)
     surf = lg.striped_surface(cfg)
     ctx = lg.Context(cfg, surf)
     for k, v in lg.initial_state(cfg, surf, seed=seed).items():
         ctx.set(k, v)
     ctx.step(steps)
     out = {nm: ctx.get(nm)[:-1, :, :n] for nm in ["u", "v", "w", "theta", "Cs_opt2"]}
+    out["Nu_t"] = ctx.get("Nu_t")[:-1, :, :n]  # FP32-held in the mixed form, read back widened
     out["rmsdiv"] = ctx.rmsdiv()
     ctx.close()
     return out
@@ -44,3 +48,39 @@ def test_mixed_vs_fp64(gpu_lib, n, steps):
     assert errs["velocity"] <= 1e-5, errs
     assert errs["theta"] <= 1e-5, errs
     assert a["rmsdiv"] <= 1e-10, a["rmsdiv"]
+
+
+def test_mixed_vs_fp64_256_lengths(gpu_lib):
+    """256 x 256 x 32: the register-resident FP32 transforms of the 256^3
+    workload (y pass 256 = 16 x 16, x passes of half lengths 128 and 192) and
+    the Lagrangian filters restricted to the nonzero kx columns (a Lagrangian
+    step at step 5 and 10), against the FP64 form."""
+    # the seeded 256-wide state runs at CFL 0.109, above the in-step check's
+    # 0.1, so the step-10 diagnostic is off; rmsdiv is read after the steps
+    a, b = run(256, 10, 1, levels=32, rmsdiv_every=0), run(256, 10, 0, levels=32, rmsdiv_every=0)
+    vel_a = np.concatenate([a[k].ravel() for k in ("u", "v", "w")])
+    vel_b = np.concatenate([b[k].ravel() for k in ("u", "v", "w")])
+    ev = rel(vel_a, vel_b)
+    et = rel(a["theta"], b["theta"])
+    ecs = rel(a["Cs_opt2"], b["Cs_opt2"])
+    enu = rel(a["Nu_t"], b["Nu_t"])
+    print("mixed vs fp64 256x256x32", ev, et, ecs, enu, "rmsdiv", a["rmsdiv"], b["rmsdiv"])
+    assert ev <= 1e-5 and et <= 1e-5, (ev, et)
+    assert ecs <= 1e-3, ecs  # dynamic coefficient from FP32 filters (the reference truncates it to FP32)
+    assert enu <= 1e-3, enu  # FP32-held eddy viscosity, read back widened
+    assert a["rmsdiv"] <= 1e-10, a["rmsdiv"]
+
+
+def test_mixed_context_refuses_fp64_module_routines(gpu_lib):
+    """The per-routine entries that read S_ij, Nu_t or tau_ij in FP64 need a
+    precision-0 context; on a mixed context they return LES_ERR_ARG."""
+    cfg = lg.make_config(32, s_flag=1, precision=1)
+    surf = lg.striped_surface(cfg)
+    ctx = lg.Context(cfg, surf)
+    L = lg.lib()
+    for name in ("les_sgs_stag", "les_wallstress", "les_theta_all_in_one"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p]
+        assert f(ctx.h) == -1, name
+    ctx.close()
