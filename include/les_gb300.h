@@ -131,7 +131,9 @@ int les_set_surface(les_ctx* ctx, const double* zo, const double* wt_s);
  * precision-0 context.  Precision 1 runs model 5. */
 int les_set_field(les_ctx* ctx, les_field f, const double* host);
 int les_get_field(les_ctx* ctx, les_field f, double* host);
-/* Device address of a module array (for zero-copy use by the caller). */
+/* Device address of a module array (for zero-copy use by the caller).  The
+ * fused step takes RHSx_f = RHSx (and RHSy, RHSz, RHS_T) by exchanging the
+ * two buffers, so those addresses alternate from step to step. */
 double* les_field_device_ptr(les_ctx* ctx, les_field f);
 size_t les_field_elems(const les_ctx* ctx, les_field f);
 /* Bind Fortran module arrays once; les_sync_* then copy all bound arrays. */

@@ -376,7 +376,8 @@ int les_ctx_destroy(les_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b)
-      if (c->gexec[a][b]) cudaGraphExecDestroy(c->gexec[a][b]);
+      for (int p = 0; p < 2; ++p)
+        if (c->gexec[a][b][p]) cudaGraphExecDestroy(c->gexec[a][b][p]);
   for (void* p : c->allocs) cudaFree(p);
   if (c->host_scal) cudaFreeHost(c->host_scal);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -513,14 +514,16 @@ static inline void step_key(const les_ctx* c, int next_jt, int next_total, int* 
 }
 static int run_step(les_ctx* c) { return c->cfg.precision == 1 ? step_mixed(c) : step_fp64(c); }
 
-// capture one step of c on stream `s` (c->stream must be s or joined to it)
+// capture one step of c on stream `s` (c->stream must be s or joined to it);
+// the host state (counters, RHS buffer exchange) is left as before the step
 static int capture_step(les_ctx* c, cudaGraph_t* graph) {
-  const int jt0 = c->jt, jtt0 = c->jt_total;
+  const int jt0 = c->jt, jtt0 = c->jt_total, par0 = c->rhs_par;
   LES_CUDA_CHECK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int st = run_step(c);
   cudaError_t e = cudaStreamEndCapture(c->stream, graph);
   c->jt = jt0;
   c->jt_total = jtt0;
+  if (c->rhs_par != par0) rhs_swap(c);
   if (st) return st;
   if (e != cudaSuccess) { les_set_error("capture: %s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
   return 0;
@@ -538,15 +541,17 @@ int les_step_graph(les_ctx* c, int nsteps) {
     }
     int lag, ov;
     step_key(c, nj, nt, &lag, &ov);
-    if (!c->gexec[lag][ov]) {
+    const int par = c->rhs_par;
+    if (!c->gexec[lag][ov][par]) {
       cudaGraph_t gr;
       int st = capture_step(c, &gr);
       if (st) return st;
-      cudaError_t e = cudaGraphInstantiate(&c->gexec[lag][ov], gr, 0);
+      cudaError_t e = cudaGraphInstantiate(&c->gexec[lag][ov][par], gr, 0);
       cudaGraphDestroy(gr);
       if (e != cudaSuccess) { les_set_error("instantiate: %s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
     }
-    LES_CUDA_CHECK(cudaGraphLaunch(c->gexec[lag][ov], c->stream));
+    LES_CUDA_CHECK(cudaGraphLaunch(c->gexec[lag][ov][par], c->stream));
+    rhs_swap(c);  // what the replayed step did
     c->jt = nj;
     c->jt_total = nt;
   }
@@ -623,7 +628,8 @@ int les_autotune(les_ctx* c, int* tx64, int* tx32, int* rpc_scale) {
   // graphs captured with the old shapes are stale
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b)
-      if (c->gexec[a][b]) { cudaGraphExecDestroy(c->gexec[a][b]); c->gexec[a][b] = nullptr; }
+      for (int p = 0; p < 2; ++p)
+        if (c->gexec[a][b][p]) { cudaGraphExecDestroy(c->gexec[a][b][p]); c->gexec[a][b][p] = nullptr; }
   if (tx64) *tx64 = c->tx64;
   if (tx32) *tx32 = c->tx32;
   if (rpc_scale) *rpc_scale = c->rpc_scale;
@@ -693,13 +699,16 @@ int les_ensemble_step(les_ensemble* e, int nsteps) {
       }
       continue;
     }
-    std::vector<int> key(2 * n);
-    for (int i = 0; i < n; ++i) step_key(e->m[i], nj, e->m[i]->jt_total + 1, &key[2 * i], &key[2 * i + 1]);
+    std::vector<int> key(3 * n);
+    for (int i = 0; i < n; ++i) {
+      step_key(e->m[i], nj, e->m[i]->jt_total + 1, &key[3 * i], &key[3 * i + 1]);
+      key[3 * i + 2] = e->m[i]->rhs_par;
+    }
     auto it = e->graphs.find(key);
     if (it == e->graphs.end()) {
       // capture: root forks to every member stream and joins them back
-      std::vector<int> jt0(n), jtt0(n);
-      for (int i = 0; i < n; ++i) { jt0[i] = e->m[i]->jt; jtt0[i] = e->m[i]->jt_total; }
+      std::vector<int> jt0(n), jtt0(n), par0(n);
+      for (int i = 0; i < n; ++i) { jt0[i] = e->m[i]->jt; jtt0[i] = e->m[i]->jt_total; par0[i] = e->m[i]->rhs_par; }
       LES_CUDA_CHECK(cudaStreamBeginCapture(e->root, cudaStreamCaptureModeThreadLocal));
       cudaEventRecord(e->fork, e->root);
       int st = 0;
@@ -711,7 +720,11 @@ int les_ensemble_step(les_ensemble* e, int nsteps) {
       }
       cudaGraph_t gr;
       cudaError_t ce = cudaStreamEndCapture(e->root, &gr);
-      for (int i = 0; i < n; ++i) { e->m[i]->jt = jt0[i]; e->m[i]->jt_total = jtt0[i]; }
+      for (int i = 0; i < n; ++i) {
+        e->m[i]->jt = jt0[i];
+        e->m[i]->jt_total = jtt0[i];
+        if (e->m[i]->rhs_par != par0[i]) rhs_swap(e->m[i]);
+      }
       if (st) return st;
       if (ce != cudaSuccess) { les_set_error("ensemble capture: %s", cudaGetErrorString(ce)); return LES_ERR_CUDA; }
       cudaGraphExec_t ex;
@@ -730,7 +743,7 @@ int les_ensemble_step(les_ensemble* e, int nsteps) {
     LES_CUDA_CHECK(cudaGraphLaunch(it->second, e->root));
     LES_CUDA_CHECK(cudaEventRecord(e->done, e->root));
     for (les_ctx* c : e->m) LES_CUDA_CHECK(cudaStreamWaitEvent(c->stream, e->done, 0));
-    for (les_ctx* c : e->m) { c->jt += 1; c->jt_total += 1; }
+    for (les_ctx* c : e->m) { c->jt += 1; c->jt_total += 1; rhs_swap(c); }
   }
   return LES_OK;
 }

@@ -96,7 +96,11 @@ struct les_ctx {
   int rpc_scale = 0;            // rows per CTA of the x-pass kernels: default * 2^rpc_scale
   int rpc64 = 0, rpc32 = 0, rpcb64 = 0, rpcb32 = 0;   // resolved rows per CTA (small/big planes)
   // CUDA graphs of one step, by variant (dynamic-model step, Cs override)
-  cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaGraphExec_t gexec[2][2][2] = {};  // [Lagrangian step][Cs^2 override][rhs_par]
+  // The fused step takes RHS*_f = RHS* (main.f90:212-214) by exchanging the
+  // two arrays' buffers instead of copying; rhs_par is the exchange parity
+  // (a captured step graph holds the buffer addresses of one parity).
+  int rhs_par = 0;
 };
 
 namespace les {
@@ -117,6 +121,7 @@ inline bool mixed_f32_field(int f) {
   }
 }
 inline float* f32(les_ctx* c, int f) { return reinterpret_cast<float*>(c->f[f]); }
+void rhs_swap(les_ctx* c);  // exchange RHSx/RHSx_f, RHSy/.., RHSz/.., RHS_T/RHS_Tf buffers
 int step_fp64(les_ctx* c);
 int step_mixed(les_ctx* c);
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev);

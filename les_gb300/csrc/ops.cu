@@ -3253,7 +3253,7 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   }
   op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
   fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
-  cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  // RHS_Tf = RHS_T: exchanged with the momentum RHS at the start of the step
   k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
                                                             c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
                                                             c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
@@ -3363,6 +3363,14 @@ static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, doub
 }
 
 // main.f90:202-478, one iteration on the device-resident state
+void rhs_swap(les_ctx* c) {
+  std::swap(c->f[LES_RHSX], c->f[LES_RHSX_F]);
+  std::swap(c->f[LES_RHSY], c->f[LES_RHSY_F]);
+  std::swap(c->f[LES_RHSZ], c->f[LES_RHSZ_F]);
+  std::swap(c->f[LES_RHS_T], c->f[LES_RHS_TF]);
+  c->rhs_par ^= 1;
+}
+
 template <bool MX>
 static int stepT(les_ctx* c) {
   typedef typename PX<MX>::S S;
@@ -3370,11 +3378,9 @@ static int stepT(les_ctx* c) {
   const les_config& k = c->cfg;
   c->jt += 1;
   c->jt_total += 1;
-  // RHS*_f = RHS* (main.f90:212-214); device copies keep every buffer address
-  // fixed from step to step, so a step can be captured in a CUDA graph
-  cudaMemcpyAsync(c->f[LES_RHSX_F], c->f[LES_RHSX], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  cudaMemcpyAsync(c->f[LES_RHSY_F], c->f[LES_RHSY], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  cudaMemcpyAsync(c->f[LES_RHSZ_F], c->f[LES_RHSZ], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  // RHS*_f = RHS* (main.f90:212-214, and RHS_Tf = RHS_T of the scalar): the
+  // buffers are exchanged; RHS* is rewritten below before it is read
+  rhs_swap(c);
   op_obukhov(c);
   if (!MX) {
     double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
