@@ -94,11 +94,15 @@ __device__ __forceinline__ dfloat df_quick(float a, float b) {  // |a| >= |b|
   const float s = a + b;
   return dfloat(s, b - (s - a));
 }
+// Sums and products are left unnormalised (hi = the rounded leading term,
+// lo = its exact error plus the low parts, |lo| a few ulp(hi) at most): the
+// next operation's two-sum / FMA product absorbs it, and a conversion to
+// FP64 adds the two.  Saves the quick-two-sum on the FP32 pipe.
 __device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
   const float s = a.hi + b.hi;
   const float bb = s - a.hi;
   const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
-  return df_quick(s, e);
+  return dfloat(s, e);
 }
 __device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
 __device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
@@ -107,7 +111,7 @@ __device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.hi, b.lo, e);
   e = fmaf(a.lo, b.hi, e);
-  return df_quick(p, e);
+  return dfloat(p, e);
 }
 __device__ __forceinline__ dfloat operator/(dfloat a, dfloat b) {
   const float q1 = a.hi / b.hi;
