@@ -30,9 +30,28 @@ struct RegRows {
   static size_t smem() { return (size_t)(RPB * N2 * (N1 + 1) + 2 * M + 1) * sizeof(typename CT<T>::type); }
 };
 
+// FP32 x pass, half length 128 = 16 x 8 with eight threads per row (every
+// lane busy in both steps)
+template <typename T, int NF> struct RowSplit2 { static constexpr int n1 = 0, n2 = 0, tt = 0; };
+template <> struct RowSplit2<float, 128> { static constexpr int n1 = 16, n2 = 8, tt = 8; };
+template <typename T, int N1, int N2, int TT>
+struct RegRows2 {
+  static constexpr int NT = 256, RPB = NT / TT, M = N1 * N2;
+  static size_t smem() { return (size_t)(RPB * N2 * (N1 + 1) + 2 * M + 1) * sizeof(typename CT<T>::type); }
+};
+
 template <typename T, typename TIn, int NF>
 void r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
   typedef typename CT<T>::type C;
+  constexpr int A1 = RowSplit2<T, NF>::n1, A2 = RowSplit2<T, NF>::n2, AT = RowSplit2<T, NF>::tt;
+  if constexpr (A1 > 0) {
+    typedef RegRows2<T, A1, A2, AT> G;
+    static size_t set2 = 48 * 1024;
+    raise_smem(k_r2c_reg2<T, TIn, A1, A2, AT, G::NT>, G::smem(), set2);
+    const dim3 grid((J.ny + G::RPB - 1) / G::RPB, J.nlev, J.nfield);
+    k_r2c_reg2<T, TIn, A1, A2, AT, G::NT><<<grid, G::NT, G::smem(), s>>>(J, P);
+    return;
+  }
   constexpr int N1 = RowSplit<NF>::n1, N2 = RowSplit<NF>::n2;
   if constexpr (N1 > 0 && std::is_same<T, float>::value) {
     typedef RegRows<T, N1, N2> G;
@@ -51,6 +70,15 @@ void r2c_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
 template <typename T, typename TOut, int NF>
 void c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, cudaStream_t s) {
   typedef typename CT<T>::type C;
+  constexpr int A1 = RowSplit2<T, NF>::n1, A2 = RowSplit2<T, NF>::n2, AT = RowSplit2<T, NF>::tt;
+  if constexpr (A1 > 0) {
+    typedef RegRows2<T, A1, A2, AT> G;
+    static size_t set2 = 48 * 1024;
+    raise_smem(k_c2r_reg2<T, TOut, A1, A2, AT, G::NT>, G::smem(), set2);
+    const dim3 grid((J.ny + G::RPB - 1) / G::RPB, J.nlev, J.nfield);
+    k_c2r_reg2<T, TOut, A1, A2, AT, G::NT><<<grid, G::NT, G::smem(), s>>>(J, P);
+    return;
+  }
   constexpr int N1 = RowSplit<NF>::n1, N2 = RowSplit<NF>::n2;
   if constexpr (N1 > 0 && std::is_same<T, float>::value) {
     typedef RegRows<T, N1, N2> G;

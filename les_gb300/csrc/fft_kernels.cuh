@@ -339,6 +339,183 @@ __global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
   }
 }
 
+// The same x pass with TT threads per row, TT dividing N1 and N2: thread q
+// takes the N1/TT first-step transforms n1 = q + TT j and the N2/TT
+// second-step transforms k2 = q + TT j, so every lane works in both steps
+// and in the Hermitian pre/post-processing (half length 128 = 16 x 8 with
+// eight threads per row).
+template <typename T, typename TIn, int N1, int N2, int TT, int NT>
+__global__ void __launch_bounds__(NT) k_r2c_reg2(RowJob J, RealPlanDev P) {
+  typedef typename CT<T>::type C;
+  typedef typename CT<TIn>::type CI;
+  static_assert(N1 % TT == 0 && N2 % TT == 0 && NT % TT == 0, "thread split");
+  constexpr int M = N1 * N2, RPB = NT / TT, MS = N2 * (N1 + 1), J1 = N1 / TT, J2 = N2 / TT;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // RPB rows x MS
+  C* tw = S + RPB * MS;                // exp(-2 pi i j / M), j < M
+  C* wr = tw + M;                      // exp(-2 pi i k / nx), k <= M
+  for (int t = threadIdx.x; t < M; t += NT) tw[t] = UnitSel<T>::get(P.c, t);
+  for (int t = threadIdx.x; t <= M; t += NT) wr[t] = rw<T>(P, t);
+  const int q = threadIdx.x % TT, r = threadIdx.x / TT;
+  const int f = blockIdx.z, lev = blockIdx.y;
+  const int row = blockIdx.x * RPB + r;
+  const bool rowok = row < J.ny;
+  C* Sr = S + r * MS;
+  const T sd = (T)(J.div[f] != 0.0 ? J.scale[f] / J.div[f] : J.scale[f]);  // scale/div, one product
+  const bool hasoff = J.off[f] != nullptr;
+  const double off = hasoff ? J.off[f][lev] : 0.0;
+  const CI* src = reinterpret_cast<const CI*>(reinterpret_cast<const TIn*>(J.phys[f]) +
+                                              (size_t)lev * J.pstride_phys + (size_t)(rowok ? row : 0) * J.ld);
+  C v[J1][N2];
+#pragma unroll
+  for (int j = 0; j < J1; ++j)
+#pragma unroll
+    for (int i = 0; i < N2; ++i) {
+      v[j][i] = mk<T>((T)0, (T)0);
+      if (rowok) {
+        const CI pr = src[q + TT * j + N1 * i];
+        T a, b;
+        if (hasoff) {  // subtract in double before rounding to T
+          a = cvt<T, double>(cvt<double, TIn>(pr.x) - off);
+          b = cvt<T, double>(cvt<double, TIn>(pr.y) - off);
+        } else {
+          a = cvt<T, TIn>(pr.x);
+          b = cvt<T, TIn>(pr.y);
+        }
+        v[j][i] = mk<T>(a * sd, b * sd);
+      }
+    }
+  __syncthreads();  // tables
+#pragma unroll
+  for (int j = 0; j < J1; ++j) {
+    const int n1 = q + TT * j;
+    dft_n<T, N2>(v[j], -1);  // over n2: v[j][i] = y[n1][k2 = i]
+#pragma unroll
+    for (int i = 1; i < N2; ++i) v[j][i] = cmul(v[j][i], tw[n1 * i]);
+#pragma unroll
+    for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + n1] = v[j][i];
+  }
+  __syncthreads();
+  C w[J2][N1];
+#pragma unroll
+  for (int j = 0; j < J2; ++j) {
+    const int k2 = q + TT * j;
+#pragma unroll
+    for (int i = 0; i < N1; ++i) w[j][i] = Sr[k2 * (N1 + 1) + i];
+    dft_n<T, N1>(w[j], -1);  // over n1: w[j][i] = Z[k2 + N2 i]
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < J2; ++j)
+#pragma unroll
+    for (int i = 0; i < N1; ++i) Sr[q + TT * j + N2 * i] = w[j][i];  // natural order
+  __syncthreads();
+  if (rowok) {
+    C* out = reinterpret_cast<C*>(J.work[f]) + (size_t)lev * J.pstride_work + (size_t)row * J.wc;
+    const int nc = J.ncols;
+#pragma unroll
+    for (int j = 0; j < J2; ++j)
+#pragma unroll
+      for (int i = 0; i < N1; ++i) {
+        const int k = q + TT * j + N2 * i;
+        const C a = w[j][i];
+        C X;
+        if (k == 0) {
+          X = mk<T>(a.x + a.y, (T)0);
+          if (M < nc) out[M] = mk<T>(a.x - a.y, (T)0);
+        } else {
+          const C b = cconj(Sr[M - k]);
+          const C e = cscale(cadd(a, b), (T)0.5);
+          const C d = cscale(csub(a, b), (T)0.5);
+          X = cadd(e, cmul(wr[k], cmulmi(d)));  // (d / i) x exp(-2 pi i k / nx)
+        }
+        if (k < nc) out[k] = X;
+      }
+  }
+}
+
+template <typename T, typename TOut, int N1, int N2, int TT, int NT>
+__global__ void __launch_bounds__(NT) k_c2r_reg2(RowJob J, RealPlanDev P) {
+  typedef typename CT<T>::type C;
+  typedef typename CT<TOut>::type CO;
+  static_assert(N1 % TT == 0 && N2 % TT == 0 && NT % TT == 0, "thread split");
+  constexpr int M = N1 * N2, RPB = NT / TT, MS = N2 * (N1 + 1), J1 = N1 / TT, J2 = N2 / TT;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // RPB rows x MS
+  C* tw = S + RPB * MS;                // exp(-2 pi i j / M), j < M
+  C* wr = tw + M;                      // exp(-2 pi i k / nx), k <= M
+  for (int t = threadIdx.x; t < M; t += NT) tw[t] = UnitSel<T>::get(P.c, t);
+  for (int t = threadIdx.x; t <= M; t += NT) wr[t] = rw<T>(P, t);
+  const int q = threadIdx.x % TT, r = threadIdx.x / TT;
+  const int f = blockIdx.z, lev = blockIdx.y;
+  const int row = blockIdx.x * RPB + r;
+  const bool rowok = row < J.ny;
+  C* Sr = S + r * MS;
+  const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work +
+                (size_t)(rowok ? row : 0) * J.wc;
+  const int nc = J.ncols;
+  __syncthreads();  // tables
+#pragma unroll
+  for (int j = 0; j < J1; ++j) {
+    const int k1 = q + TT * j;
+    C v[N2];
+#pragma unroll
+    for (int i = 0; i < N2; ++i) {
+      const int k = k1 + N1 * i, km = M - k;
+      C a = mk<T>((T)0, (T)0), bb = mk<T>((T)0, (T)0);
+      if (rowok) {
+        if (k < nc) a = in[k];
+        if (km < nc) bb = in[km];
+      }
+      if (k == 0) { a.y = (T)0; bb.y = (T)0; }  // the halfcomplex pass ignores Im of X[0], X[M]
+      const C b = cconj(bb);
+      const C e = cadd(a, b);
+      const C d = cmul(csub(a, b), cconj(wr[k]));  // x exp(+2 pi i k / nx)
+      v[i] = cadd(e, cmuli(d));
+    }
+    dft_n<T, N2>(v, +1);  // over k2: v[i] = y[k1][n2 = i]
+#pragma unroll
+    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(tw[k1 * i]));
+#pragma unroll
+    for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + k1] = v[i];
+  }
+  __syncthreads();
+  if (rowok) {
+    TOut* dst = reinterpret_cast<TOut*>(const_cast<void*>(J.phys[f])) + (size_t)lev * J.pstride_phys +
+                (size_t)row * J.ld;
+    CO* pairs = reinterpret_cast<CO*>(dst);
+    const bool hasoff = J.off[f] != nullptr;
+    const double off = hasoff ? J.off[f][lev] : 0.0;
+#pragma unroll
+    for (int j = 0; j < J2; ++j) {
+      const int n2 = q + TT * j;
+      C w[N1];
+#pragma unroll
+      for (int i = 0; i < N1; ++i) w[i] = Sr[n2 * (N1 + 1) + i];
+      dft_n<T, N1>(w, +1);  // over k1: w[i] = z[n2 + N2 i]
+#pragma unroll
+      for (int i = 0; i < N1; ++i) {
+        const C z = w[i];
+        CO pw;
+        if (hasoff) {
+          pw.x = cvt<TOut, double>(cvt<double, T>(z.x) + off);
+          pw.y = cvt<TOut, double>(cvt<double, T>(z.y) + off);
+        } else {
+          pw.x = cvt<TOut, T>(z.x);
+          pw.y = cvt<TOut, T>(z.y);
+        }
+        pairs[n2 + N2 * i] = pw;
+      }
+    }
+    if (q == 0) {  // padding columns ld-1:ld
+      CO pz;
+      pz.x = (TOut)0;
+      pz.y = (TOut)0;
+      pairs[M] = pz;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // cols: y-transform of TX kx columns per CTA, all fields of the job.
 // grid = (ceil(ncols/TX), nlev, nf)
