@@ -43,7 +43,7 @@ DOMINANT = {"mixed": (2, "k_colsr/k_colsr_sum/k_colsf<float> (FP32 y-pass transf
 # byte of the dominant family, from one ncu capture (1 pass) of the same
 # 256^3 run's timed launches; scales the live algorithmic bytes per launch
 # to the traffic per launch.  Only valid at 256^3.
-TRAFFIC_RATIO = {"mixed": 0.8714, "fp64": 0.9209}
+TRAFFIC_RATIO = {"mixed": 0.8841, "fp64": 0.9209}
 
 
 def parse():
