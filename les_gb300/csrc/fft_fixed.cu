@@ -218,7 +218,8 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
 #undef LES_CASE
       default: return false;
     }
-  } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 && std::is_same<CIn, dcomplex>::value) {
+  } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 &&
+                       (std::is_same<CIn, dcomplex>::value || std::is_same<CIn, double2>::value)) {
     switch (key) {
 #define LES_CASE(a, b) \
   case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, grid, s); return true;
@@ -254,5 +255,8 @@ LES_INST_COLS(float, 16, double2)
 LES_INST_COLS(dfloat, 2, dcomplex)
 LES_INST_COLS(dfloat, 4, dcomplex)
 LES_INST_COLS(dfloat, 8, dcomplex)
+LES_INST_COLS(dfloat, 2, double2)
+LES_INST_COLS(dfloat, 4, double2)
+LES_INST_COLS(dfloat, 8, double2)
 
 }  // namespace les

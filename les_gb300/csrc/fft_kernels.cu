@@ -107,5 +107,6 @@ template int launch_cols<float, double2>(const ColJob&, const FftPlanDev&, const
 template int launch_rows_r2c<dfloat, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_c2r<dfloat, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_cols<dfloat, dcomplex>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
+template int launch_cols<dfloat, double2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 
 }  // namespace les

@@ -1951,11 +1951,11 @@ __device__ __forceinline__ void st1(dcomplex* p, size_t i, int comp, double v) {
 __device__ __forceinline__ dfloat ldf(const dcomplex* p, size_t i, int comp) {
   return reinterpret_cast<const dfloat*>(p)[2 * i + comp];
 }
-// an FP64 value parked in the 8-byte slot of one float-float component
-__device__ __forceinline__ void st_park(dcomplex* p, size_t i, int comp, double v) {
+// an FP64 value parked in the 8-byte slot of one component
+template <typename PC> __device__ __forceinline__ void st_park(PC* p, size_t i, int comp, double v) {
   reinterpret_cast<double*>(p)[2 * i + comp] = v;
 }
-__device__ __forceinline__ double ld_park(const dcomplex* p, size_t i, int comp) {
+template <typename PC> __device__ __forceinline__ double ld_park(const PC* p, size_t i, int comp) {
   return reinterpret_cast<const double*>(p)[2 * i + comp];
 }
 template <typename HC, typename PC>
@@ -1980,7 +1980,7 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
   const C2 b1 = bot[t];
   double up = (-dz * (part == 0 ? b1.x : b1.y)) * ibet[t];
   constexpr int D = 4;
-  if constexpr (std::is_same<HC, dcomplex>::value && std::is_same<PC, dcomplex>::value) {
+  if constexpr (std::is_same<HC, dcomplex>::value) {
     const dfloat k_x(kxd[t].x, kxd[t].y), k_y(kyd[t].x, kyd[t].y);
     const dfloat idzf(1.0 / dz);
     const double idz2 = 1.0 / (dz * dz);
@@ -2173,7 +2173,10 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
   r2cT<T, double>(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
   CX* H = (CX*)c->wsP;                                       // 3*(nz-1)*C
   C2* BT = reinterpret_cast<C2*>(H + (size_t)3 * (nz - 1) * g.C);  // bottom, top
-  CX* P = reinterpret_cast<CX*>(BT + 2 * g.C);              // (nz+1)*C
+  // p-hat: FP64 in the mixed form (the inverse float-float y pass widens it
+  // on load, so the solve stores its FP64 values as they are)
+  typedef typename std::conditional<std::is_same<T, dfloat>::value, double2, CX>::type PCX;
+  PCX* P = reinterpret_cast<PCX*>(BT + 2 * g.C);            // (nz+1)*C
   ColJob J = coljob(c, MAP_SAME, DIR_FWD, nz - 1);
   J.nin = 1; J.nout = 1; J.nf = 3;
   J.in[0] = c->wsA; J.fs_in = (long)(nz - 1) * g.C;
@@ -2192,21 +2195,21 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
     K.coef[0][0] = CC_KILL;
     cols(c, K);
   }
-  k_tridiag2<CX, CX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
+  k_tridiag2<CX, PCX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
       H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky,
       c->kxd, c->kyd, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
     K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
-    colsT<T, CX>(c, K);
+    colsT<T, PCX>(c, K);
     ColJob L = coljob(c, MAP_SAME, DIR_INV, nz - 1);
     L.nin = 1; L.nout = 3; L.in[0] = P + g.C;
     L.out[0] = (CX*)c->wsB + g.C;
     L.out[1] = (CX*)c->wsB + g.C + (size_t)(nz - 1) * g.C;
     L.out[2] = (CX*)c->wsB + g.C + (size_t)2 * (nz - 1) * g.C;
     L.coef[0][0] = CC_ONE; L.coef[1][0] = CC_IKX; L.coef[2][0] = CC_IKY;
-    colsT<T, CX>(c, L);
+    colsT<T, PCX>(c, L);
     double* o0 = p;
     c2rT<T, double>(c, 1, 1, c->wsB, &o0, (long)g.nplane, false, g.lh);
     double* o1[3] = {p + g.nplane, dpdx, dpdy};
