@@ -21,7 +21,6 @@ void raise_smem(K kernel, size_t sm, size_t& set) {
 template <int M> struct RowSplit { static constexpr int n1 = 0, n2 = 0; };
 template <> struct RowSplit<32> { static constexpr int n1 = 8, n2 = 4; };
 template <> struct RowSplit<48> { static constexpr int n1 = 16, n2 = 3; };
-template <> struct RowSplit<128> { static constexpr int n1 = 16, n2 = 8; };
 template <> struct RowSplit<192> { static constexpr int n1 = 16, n2 = 12; };
 template <typename T, int N1, int N2>
 struct RegRows {
