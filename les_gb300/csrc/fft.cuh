@@ -267,10 +267,46 @@ template <typename C, typename T> __device__ __forceinline__ void dft12(C* v, in
     v[c] = u[0]; v[c + 3] = u[1]; v[c + 6] = u[2]; v[c + 9] = u[3];
   }
 }
+// natural-order DFT24 (n = a + 8b: eight DFT3 over b, twiddles W24^(ac),
+// three DFT8 over a; output k = c + 3d)
+template <typename C, typename T> __device__ __forceinline__ void dft24(C* v, int sign) {
+  // cos / sin of 15 degrees x m, m = 0..14
+  constexpr double cs[15] = {1.0, 0.96592582628906828675, 0.86602540378443864676, 0.70710678118654752440, 0.5,
+                             0.25881904510252076235, 0.0, -0.25881904510252076235, -0.5, -0.70710678118654752440,
+                             -0.86602540378443864676, -0.96592582628906828675, -1.0, -0.96592582628906828675,
+                             -0.86602540378443864676};
+  constexpr double sn[15] = {0.0, 0.25881904510252076235, 0.5, 0.70710678118654752440, 0.86602540378443864676,
+                             0.96592582628906828675, 1.0, 0.96592582628906828675, 0.86602540378443864676,
+                             0.70710678118654752440, 0.5, 0.25881904510252076235, 0.0, -0.25881904510252076235,
+                             -0.5};
+  C t[8][3];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    t[a][0] = v[a]; t[a][1] = v[a + 8]; t[a][2] = v[a + 16];
+    dft3<C, T>(t[a], sign);
+  }
+#pragma unroll
+  for (int a = 1; a < 8; ++a)
+#pragma unroll
+    for (int c = 1; c < 3; ++c) {
+      const int m = a * c;
+      t[a][c] = cmulc(t[a][c], (T)cs[m], sign < 0 ? (T)(-sn[m]) : (T)sn[m]);
+    }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    C u[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) u[a] = t[a][c];
+    dft8<C, T>(u, sign);
+#pragma unroll
+    for (int d = 0; d < 8; ++d) v[c + 3 * d] = u[d];
+  }
+}
 // natural-order DFT of a compile-time length in registers
 template <typename T, int N> __device__ __forceinline__ void dft_n(typename CT<T>::type* v, int sign) {
   typedef typename CT<T>::type C;
-  if constexpr (N == 16) dft16<C, T>(v, sign);
+  if constexpr (N == 24) dft24<C, T>(v, sign);
+  else if constexpr (N == 16) dft16<C, T>(v, sign);
   else if constexpr (N == 12) dft12<C, T>(v, sign);
   else if constexpr (N == 8) dft8<C, T>(v, sign);
   else if constexpr (N == 4) dft4(v, sign);

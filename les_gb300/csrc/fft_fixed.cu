@@ -129,6 +129,19 @@ void cols_reg_sum(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
   k_colsr_sum<T, TX, CIn, R, 2><<<grid, TX * R, smf, s>>>(J, P);
 }
 
+// register-resident 3/2 padding / truncation (FP32), 16 kx columns per CTA
+template <typename T, typename CIn, int NIN, int NOUT>
+void cols_pad(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, cudaStream_t s) {
+  typedef typename CT<T>::type C;
+  typedef PadShape<NIN, NOUT> PS;
+  constexpr int TX = 16;
+  const size_t smf = (size_t)(16 * PS::b * TX + PS::ns + PS::nb) * sizeof(C);
+  static size_t set = 48 * 1024;
+  raise_smem(k_colsr_pad<T, TX, CIn, NIN, NOUT>, smf, set);
+  const dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);
+  k_colsr_pad<T, TX, CIn, NIN, NOUT><<<grid, TX * PS::tt, smf, s>>>(J, Pin, Pout);
+}
+
 template <typename T, int TX, typename CIn, int NIN, int NOUT>
 void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, dim3 grid, cudaStream_t s) {
   typedef typename CT<T>::type C;
@@ -139,6 +152,15 @@ void cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, 
     }
     if (J.nin > 1 && J.nout <= 2 && J.map == MAP_SAME) {
       cols_reg_sum<T, CIn, NIN == 256 ? 16 : 8>(J, Pin, s);
+      return;
+    }
+  }
+  if constexpr (std::is_same<T, float>::value && NIN != NOUT &&
+                ((NIN < NOUT ? NIN : NOUT) == 256 || (NIN < NOUT ? NIN : NOUT) == 128)) {
+    const bool pad = NOUT > NIN;
+    if (J.nin == 1 && J.nout == 1 && J.coef[0][0] == CC_ONE && (J.inv_mask & 1u) &&
+        J.map == (pad ? MAP_PAD : MAP_UNPAD) && J.ny_small == (pad ? NIN : NOUT) && (pad || (J.dir & DIR_FWD))) {
+      cols_pad<T, CIn, NIN, NOUT>(J, Pin, Pout, s);
       return;
     }
   }

@@ -865,6 +865,127 @@ __global__ void __launch_bounds__(TX * R, 3) k_colsr(ColJob J, FftPlanDev P, int
   cp_async_wait_all();  // nothing in flight at exit
 }
 
+// Register-resident 3/2 padding and truncation (one input, one output, unit
+// coefficient): small length NS = 16 A, big length NB = 16 B, B = 3A/2.  A
+// transform of length N = 16 L splits as n = n1 + L n2, k = k2 + 16 k1, so
+// thread q < 16 of a column holds the spectral rows q + 16 k1 (k1 < L) and
+// thread t < L the physical rows t + L n2 (n2 < 16); one exchange through
+// shared memory turns one layout into the other.  In the spectral layout
+// the padding and truncation maps (padd.f90:123-133, unpadd.f90:143-155)
+// stay inside a thread: small row q + 16 i is big row q + 16 i for i < A/2
+// and q + 16 (i + B - A) for i >= A/2, and the small Nyquist row (q = 0,
+// i = A/2) is dropped.  The padded spectrum's zero rows are never loaded.
+template <typename T, int TX, int L, int M>
+__device__ __forceinline__ void fwd_16l(typename CT<T>::type (&v)[M], typename CT<T>::type* S,
+                                        const typename CT<T>::type* tw, int r, int b) {
+  // on entry thread r < L holds x[r + L n2] in v[n2]; on exit thread r < 16
+  // holds X[r + 16 k1] in v[k1]
+  __syncthreads();  // the twiddle table is in place and earlier readers of S are done
+  if (r < L) {
+    dft_n<T, 16>(v, -1);  // over n2: v[k2] = y[n1 = r][k2]
+#pragma unroll
+    for (int k2 = 1; k2 < 16; ++k2) v[k2] = cmul(v[k2], tw[r * k2]);
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) S[(r * 16 + k2) * TX + b] = v[k2];
+  }
+  __syncthreads();
+  if (r < 16) {
+#pragma unroll
+    for (int n1 = 0; n1 < L; ++n1) v[n1] = S[(n1 * 16 + r) * TX + b];
+    dft_n<T, L>(v, -1);  // over n1: v[k1] = X[r + 16 k1]
+  }
+}
+template <typename T, int TX, int L, int M>
+__device__ __forceinline__ void inv_16l(typename CT<T>::type (&v)[M], typename CT<T>::type* S,
+                                        const typename CT<T>::type* tw, int r, int b) {
+  // unnormalised inverse: on entry thread r < 16 holds X[r + 16 k1] in
+  // v[k1]; on exit thread r < L holds x[r + L n2] in v[n2]
+  __syncthreads();
+  if (r < 16) {
+    dft_n<T, L>(v, +1);  // over k1: v[n1] = z[k2 = r][n1]
+#pragma unroll
+    for (int n1 = 1; n1 < L; ++n1) v[n1] = cmul(v[n1], cconj(tw[r * n1]));
+#pragma unroll
+    for (int n1 = 0; n1 < L; ++n1) S[(n1 * 16 + r) * TX + b] = v[n1];
+  }
+  __syncthreads();
+  if (r < L) {
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) v[k2] = S[(r * 16 + k2) * TX + b];
+    dft_n<T, 16>(v, +1);  // over k2: v[n2] = x[r + L n2]
+  }
+}
+template <int NIN, int NOUT> struct PadShape {
+  static constexpr bool pad = NOUT > NIN;
+  static constexpr int ns = pad ? NIN : NOUT, nb = pad ? NOUT : NIN, a = ns / 16, b = nb / 16;
+  static constexpr int tt = b > 16 ? b : 16;  // threads per column (and register array length)
+};
+template <typename T, int TX, typename CIn, int NIN, int NOUT>
+__global__ void __launch_bounds__(TX * PadShape<NIN, NOUT>::tt, 2) k_colsr_pad(ColJob J, FftPlanDev Pin,
+                                                                                 FftPlanDev Pout) {
+  typedef typename CT<T>::type C;
+  typedef PadShape<NIN, NOUT> PS;
+  constexpr int A = PS::a, B = PS::b, NS = PS::ns, NB = PS::nb, TT = PS::tt;
+  static_assert(NS == 16 * A && NB == 16 * B && 2 * B == 3 * A && A % 2 == 0, "3/2 padding of 16 A rows");
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* S = reinterpret_cast<C*>(smraw);  // element (n1, k2) of column b at (n1 * 16 + k2) * TX + b
+  C* tws = S + 16 * B * TX;            // exp(-2 pi i m / NS), m < NS
+  C* twb = tws + NS;                   // exp(-2 pi i m / NB), m < NB
+  for (int t = threadIdx.x; t < NS; t += TX * TT) tws[t] = UnitSel<T>::get(PS::pad ? Pin : Pout, t);
+  for (int t = threadIdx.x; t < NB; t += TX * TT) twb[t] = UnitSel<T>::get(PS::pad ? Pout : Pin, t);
+  const int b = threadIdx.x % TX, r = threadIdx.x / TX;
+  const int jx = blockIdx.x * TX + b;
+  const bool colok = jx < J.ncols;
+  const CIn* src = reinterpret_cast<const CIn*>(J.in[0]) + (size_t)blockIdx.y * J.ps_in +
+                   (size_t)blockIdx.z * J.fs_in + (colok ? jx : 0);
+  C* dst = reinterpret_cast<C*>(J.out[0]) + (size_t)blockIdx.y * J.ps_out + (size_t)blockIdx.z * J.fs_out + jx;
+  auto load = [&](C& d, int row) {
+    const CIn x = src[(size_t)row * J.wc_in];
+    d = mk<T>(cvt<T, decltype(x.x)>(x.x), cvt<T, decltype(x.y)>(x.y));
+  };
+  C v[TT];
+  if constexpr (PS::pad) {
+    if (J.dir & DIR_FWD) {
+      if (r < A) {
+#pragma unroll
+        for (int n2 = 0; n2 < 16; ++n2) load(v[n2], r + A * n2);
+      }
+      fwd_16l<T, TX, A>(v, S, tws, r, b);
+    } else if (r < 16) {
+#pragma unroll
+      for (int i = 0; i < A; ++i) load(v[i], r + 16 * i);
+    }
+    if (r < 16) {  // v[m] = padded X[r + 16 m], m < B
+#pragma unroll
+      for (int i = A / 2; i < A; ++i) v[i + B - A] = v[i];
+#pragma unroll
+      for (int m = A / 2; m < B - A / 2; ++m) v[m] = mk<T>((T)0, (T)0);
+      if (r == 0) v[B - A / 2] = mk<T>((T)0, (T)0);
+    }
+    inv_16l<T, TX, B>(v, S, twb, r, b);
+    if (colok && r < B) {
+#pragma unroll
+      for (int n2 = 0; n2 < 16; ++n2) dst[(size_t)(r + B * n2) * J.wc_out] = v[n2];
+    }
+  } else {
+    if (r < B) {
+#pragma unroll
+      for (int n2 = 0; n2 < 16; ++n2) load(v[n2], r + B * n2);
+    }
+    fwd_16l<T, TX, B>(v, S, twb, r, b);
+    if (r < 16) {  // v[i] = truncated X[r + 16 i], i < A
+#pragma unroll
+      for (int i = A / 2; i < A; ++i) v[i] = v[i + B - A];
+      if (r == 0) v[A / 2] = mk<T>((T)0, (T)0);
+    }
+    inv_16l<T, TX, A>(v, S, tws, r, b);
+    if (colok && r < A) {
+#pragma unroll
+      for (int n2 = 0; n2 < 16; ++n2) dst[(size_t)(r + A * n2) * J.wc_out] = v[n2];
+    }
+  }
+}
+
 // Several inputs summed per output (the stress and flux divergences:
 // out_o = sum_i coef(o,i) * in_i), at most NO outputs: each input is loaded
 // and transformed in turn and its contributions are accumulated in shared
