@@ -951,6 +951,23 @@ __global__ void __launch_bounds__(TX * PadShape<NIN, NOUT>::tt, 2) k_colsr_pad(C
         for (int n2 = 0; n2 < 16; ++n2) load(v[n2], r + A * n2);
       }
       fwd_16l<T, TX, A>(v, S, tws, r, b);
+    } else if constexpr (sizeof(CIn) > 8) {
+      // 16-byte inputs: every thread row loads (about NS / TT rows each) and
+      // stages them in S, so the loads in flight fit the register budget
+#pragma unroll
+      for (int k = 0; k < (NS + TT - 1) / TT; ++k) {
+        const int row = r + k * TT;
+        if (row < NS) {
+          C x;
+          load(x, row);
+          S[row * TX + b] = x;
+        }
+      }
+      __syncthreads();
+      if (r < 16) {
+#pragma unroll
+        for (int i = 0; i < A; ++i) v[i] = S[(r + 16 * i) * TX + b];
+      }
     } else if (r < 16) {
 #pragma unroll
       for (int i = 0; i < A; ++i) load(v[i], r + 16 * i);

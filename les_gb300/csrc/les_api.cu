@@ -202,7 +202,7 @@ static Sizes sizes_of(const Grid& g) {
   // saved spectra, wall-plane spectra, Thomas tables, reductions, wavenumber
   // and filter tables (FP64 + FP32)
   s.aux = 4 * nz * C * sizeof(double2) + 4 * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double) +
-          (24 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float) +
+          (28 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float) +
           2 * C * sizeof(float2);
   return s;
 }
@@ -357,7 +357,7 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   if ((st = dalloc(c, &c->wsA, s.wsA)) || (st = dalloc(c, &c->wsB, s.wsB)) || (st = dalloc(c, &c->wsP, s.wsP)) ||
       (st = dalloc(c, (void**)&c->big, s.big)) || (st = dalloc(c, (void**)&c->tmp, s.tmp)) ||
       (st = dalloc(c, (void**)&c->spare, s.spare)) || (st = dalloc(c, (void**)&c->dscal, 64 * sizeof(double))) ||
-      (st = dalloc(c, (void**)&c->dred, 24 * (size_t)(g.nz + 8) * sizeof(double))) ||
+      (st = dalloc(c, (void**)&c->dred, 28 * (size_t)(g.nz + 8) * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->spec, 4 * (size_t)g.nz * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->wspec, 4 * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||

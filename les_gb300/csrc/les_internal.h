@@ -135,8 +135,8 @@ int op_cvt_selftest(size_t n, unsigned long long seed, unsigned long long* bad_d
 int op_tridag(les_ctx* c, const double* a, const double* b, const double* cc, const double* r, double* u);
 void launch_tridag_generic(const double* a, const double* b, const double* cc, const double* r, double* u,
                            double* gam, int lh, int ny, int n, int* flag, cudaStream_t s);
-int op_obukhov(les_ctx* c);
-int op_wallstress(les_ctx* c);
+int op_obukhov(les_ctx* c, const double* uv1 = nullptr);     // uv1: filtered surface u, v (null: filtered here)
+int op_wallstress(les_ctx* c, const double* uv1 = nullptr);
 int op_sgs_stag(les_ctx* c);
 int op_lagrange(les_ctx* c, const double* const* S);
 int op_interpolag(les_ctx* c);

@@ -154,15 +154,15 @@ static int colsT(les_ctx* c, const ColJob& J0) {
 static int cols(les_ctx* c, const ColJob& J) { return colsT<double, double2>(c, J); }
 
 // ---------------------------------------------------------------------------
-// deterministic reductions (fixed order: one CTA per plane, fixed tree)
-// mode 0: sum f[plane](1:nx,1:ny)
-// Sum of f(1:nx,1:ny) of one plane per block (512 threads): warp w takes rows
-// w, w+16, ..; lane l the columns l, l+32, ..; four independent partial sums
-// per thread, then a fixed-order tree, so the result is deterministic.
-__device__ __forceinline__ double plane_sum_block(const double* p, int ld, int nx, int ny, double* sh) {
+// deterministic reductions (fixed order, fixed tree)
+// Sum of f(1:nx, r0+1:r1) of one plane per block (512 threads): warp w takes
+// rows r0+w, r0+w+16, ..; lane l the columns l, l+32, ..; four independent
+// partial sums per thread, then a fixed-order tree, so the result is
+// deterministic.
+__device__ __forceinline__ double plane_sum_block(const double* p, int ld, int nx, int r0, int r1, double* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-  for (int jy = wid; jy < ny; jy += 16) {
+  for (int jy = r0 + wid; jy < r1; jy += 16) {
     const double* row = p + (size_t)jy * ld;
     int jx = lane;
     for (; jx + 96 < nx; jx += 128) {
@@ -178,19 +178,34 @@ __device__ __forceinline__ double plane_sum_block(const double* p, int ld, int n
   }
   return sh[0];
 }
-__global__ void __launch_bounds__(512) k_plane_sum(const double* f, long pstride, int ld, int nx, int ny,
-                                                   double* out) {
+// Row-split plane sums: block (q, j) sums rows [q rows, (q+1) rows) of plane
+// j into part[j nsplit + q]; k_plane_fin adds the nsplit partial sums of a
+// plane in order and divides by div (1: sums; nx*ny: means).  Several blocks
+// per plane keep more loads in flight than one block per plane; the order
+// stays fixed, so the result is deterministic.
+__global__ void __launch_bounds__(512) k_plane_part(const double* f, long pstride, int ld, int nx, int ny, int rows,
+                                                    double* part) {
   __shared__ double sh[512];
-  const double t = plane_sum_block(f + (size_t)blockIdx.x * pstride, ld, nx, ny, sh);
-  if (threadIdx.x == 0) out[blockIdx.x] = t;
+  const int r0 = blockIdx.x * rows, r1 = min(r0 + rows, ny);
+  const double t = plane_sum_block(f + (size_t)blockIdx.y * pstride, ld, nx, r0, r1, sh);
+  if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = t;
 }
-
-// per-level plane means of f(1:nx,1:ny,lev) (same fixed order as k_plane_sum)
-__global__ void __launch_bounds__(512) k_plane_mean(const double* f, long pstride, int ld, int nx, int ny,
-                                                    double* out) {
-  __shared__ double sh[512];
-  const double t = plane_sum_block(f + (size_t)blockIdx.x * pstride, ld, nx, ny, sh);
-  if (threadIdx.x == 0) out[blockIdx.x] = t / (double)(nx * ny);
+__global__ void k_plane_fin(const double* __restrict__ part, int nsplit, int nplanes, double div, double* out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nplanes) {
+    double s = 0.0;
+    for (int q = 0; q < nsplit; ++q) s += part[(size_t)j * nsplit + q];
+    out[j] = s / div;
+  }
+}
+// sums (div 1) or means (div nx*ny) of f(1:nx,1:ny) over nplanes planes;
+// nsplit * nplanes <= 4 (nz + 8)
+static void plane_sums(les_ctx* c, const double* f, long pstride, int nplanes, int nsplit, double div, double* out) {
+  const Grid& g = c->g;
+  double* part = c->dred + 24 * (size_t)(g.nz + 8);
+  const int rows = (g.ny + nsplit - 1) / nsplit;
+  k_plane_part<<<dim3(nsplit, nplanes), 512, 0, c->stream>>>(f, pstride, g.ld, g.nx, g.ny, rows, part); LES_COUNT_LAUNCH();
+  k_plane_fin<<<(nplanes + 127) / 128, 128, 0, c->stream>>>(part, nsplit, nplanes, div, out); LES_COUNT_LAUNCH();
 }
 
 // ---------------------------------------------------------------------------
@@ -703,7 +718,25 @@ __global__ void k_obukhov_init(double* psi_m, double* psi_m0, double* psi_h, dou
     if (!initsc) sgs_t3[s] = wt_s[s] / div;
   }
 }
-int op_obukhov(les_ctx* c) {
+// G_test_test-filtered surface u, v (test_filtermodule.f90:13-30 on the
+// first level; obukhov and wallstress filter the same planes) as one
+// two-field job: u1 at uv1, v1 at uv1 + nplane
+static void surface_uv_filtered(les_ctx* c, double* uv1) {
+  const Grid& g = c->g;
+  const double* in[2] = {c->f[LES_U], c->f[LES_V]};
+  r2c(c, 2, 1, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, 1);
+  J.nin = 1; J.nout = 1; J.nf = 2;
+  J.in[0] = c->wsA; J.fs_in = (long)g.C;
+  J.out[0] = c->wsB; J.fs_out = (long)g.C;
+  J.coef[0][0] = CC_GG;
+  cols(c, J);
+  double* out[2] = {uv1, uv1 + g.nplane};
+  c2r(c, 2, 1, c->wsB, out, (long)g.nplane, false, g.lh);
+}
+// uv1: the filtered surface planes when the caller already has them, else
+// null (filtered here into the first two temp planes)
+int op_obukhov(les_ctx* c, const double* uv1) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const size_t ns = (size_t)g.nx * g.ny;
@@ -712,11 +745,13 @@ int op_obukhov(les_ctx* c) {
                                                      c->f[LES_PSI_H0], c->f[LES_SGS_T3_SFC], c->f[LES_WT_S],
                                                      ns, k.initsc, k.u_star * k.t_scale); LES_COUNT_LAUNCH();
   }
-  k_plane_sum<<<1, 512, 0, c->stream>>>(c->f[LES_THETA], 0, g.ld, g.nx, g.ny, c->dscal + 0); LES_COUNT_LAUNCH();
-  double* u1 = c->tmp;
-  double* v1 = c->tmp + g.nplane;
-  op_test_filter(c, u1, c->f[LES_U], 1, 1, (long)g.nplane);
-  op_test_filter(c, v1, c->f[LES_V], 1, 1, (long)g.nplane);
+  plane_sums(c, c->f[LES_THETA], 0, 1, 16, 1.0, c->dscal + 0);
+  if (!uv1) {
+    surface_uv_filtered(c, c->tmp);
+    uv1 = c->tmp;
+  }
+  const double* u1 = uv1;
+  const double* v1 = uv1 + g.nplane;
   const double g_ = (k.g * k.z_i) / (k.u_star * k.u_star);
   k_obukhov<<<grid1(ns), 256, 0, c->stream>>>(u1, v1, c->f[LES_THETA], c->f[LES_ZO], c->z_os,
                                               c->f[LES_SGS_T3_SFC], c->f[LES_USTAR_AVG], c->f[LES_PSI_M],
@@ -750,12 +785,14 @@ __global__ void k_wallstress(const double* __restrict__ u, const double* __restr
     dvdz[i] = (v[i] == 0.0) ? 0.0 : b;
   }
 }
-int op_wallstress(les_ctx* c) {
+int op_wallstress(les_ctx* c, const double* uv1) {
   const Grid& g = c->g;
-  double* u1 = c->tmp;
-  double* v1 = c->tmp + g.nplane;
-  op_test_filter(c, u1, c->f[LES_U], 1, 1, (long)g.nplane);
-  op_test_filter(c, v1, c->f[LES_V], 1, 1, (long)g.nplane);
+  if (!uv1) {
+    surface_uv_filtered(c, c->tmp);
+    uv1 = c->tmp;
+  }
+  const double* u1 = uv1;
+  const double* v1 = uv1 + g.nplane;
   if (c->cfg.precision == 1)
     k_wallstress<float><<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(
         c->f[LES_U], c->f[LES_V], u1, v1, c->f[LES_ZO], c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PHI_M],
@@ -2403,53 +2440,69 @@ __global__ void __launch_bounds__(256) k_scalar_rhs32(double* R, const float* __
   R[i] = cvt_f2d((-adv[i] + dxy[i]) + cdz * (t1 - t0));
 }
 
-__global__ void k_calcbeta_levels(const double* __restrict__ sums, double* sbr, int nz, double nxny) {
+__global__ void k_calcbeta_levels(const double* __restrict__ sums, double* sbr, int nz, double nxny, double gh) {
   for (int j = threadIdx.x; j < nz; j += blockDim.x) {
     const double sb = sums[j] / nxny;
     sbr[2 * j] = sb;
-    sbr[2 * j + 1] = 1.0 / sb;
+    sbr[2 * j + 1] = gh / sb;
   }
 }
-__global__ void k_calcbeta(const double* __restrict__ theta, const double* __restrict__ sbr, double* bs, int ld,
-                           int nx, int ny, int nz, double g_hat) {
-  const size_t np = (size_t)ld * ny;
-  GSTRIDE(i, np * nz) {
-    const int jz = (int)(i / np) + 1;
-    const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
-    if (jz == 1 || jz == nz || jx >= nx) { bs[i] = 0.0; continue; }
-    const double sb = sbr[2 * (jz - 1)], rsb = sbr[2 * (jz - 1) + 1];
-    const double sbm = sbr[2 * (jz - 2)], rsbm = sbr[2 * (jz - 2) + 1];
-    // (theta - sb)/sb as a product with 1/sb
-    const double above = (theta[i] * 1.0 - sb) * rsb;
-    const double below = (theta[i - np] * 1.0 - sbm) * rsbm;
-    bs[i] = g_hat * (above + below) * 0.5;
+// grid (ceil(np/256), ceil(nz/KZ)): a thread takes KZ consecutive levels of
+// one plane point, so each level's g_hat/2 (theta - sb)/sb is formed once and
+// is both the 'above' term of its level and the 'below' term of the next; the
+// kernel is bound by the FP64 pipe, and this takes three FP64 operations per
+// point instead of six.  sbr holds sb and g_hat / (2 sb) per level.
+template <int KZ>
+__global__ void k_calcbeta(const double* __restrict__ theta, const double* __restrict__ sbr, double* __restrict__ bs,
+                           int ld, int nx, int ny, int nz) {
+  const int np = ld * ny;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= np) return;
+  const int z0 = blockIdx.y * KZ;  // plane index (level - 1) of the thread's first level
+  const bool inx = r % ld < nx;
+  double qb = 0.0;  // g_hat/2 (theta - sb) / sb of the plane below
+  if (inx && z0 > 0) qb = (theta[(size_t)(z0 - 1) * np + r] - sbr[2 * (z0 - 1)]) * sbr[2 * (z0 - 1) + 1];
+#pragma unroll
+  for (int k = 0; k < KZ; ++k) {
+    const int p = z0 + k;
+    if (p < nz) {
+      const size_t i = (size_t)p * np + r;
+      double qa = 0.0;
+      if (inx) qa = (theta[i] - sbr[2 * p]) * sbr[2 * p + 1];
+      bs[i] = (inx && p > 0 && p < nz - 1) ? qa + qb : 0.0;
+      qb = qa;
+    }
   }
 }
 static void calcbeta(les_ctx* c) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   double* sbr = c->dred + 20 * (size_t)(g.nz + 8);  // 2 * nz values
-  k_plane_sum<<<g.nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, c->dred); LES_COUNT_LAUNCH();
-  k_calcbeta_levels<<<1, 256, 0, c->stream>>>(c->dred, sbr, g.nz, (double)(g.nx * g.ny)); LES_COUNT_LAUNCH();
+  plane_sums(c, c->f[LES_THETA], (long)g.nplane, g.nz, 4, 1.0, c->dred);
   const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
-  k_calcbeta<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], sbr, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny,
-                                                    g.nz, g_hat);
+  k_calcbeta_levels<<<1, 256, 0, c->stream>>>(c->dred, sbr, g.nz, (double)(g.nx * g.ny), 0.5 * g_hat); LES_COUNT_LAUNCH();
+  k_calcbeta<8><<<dim3((unsigned)((g.nplane + 255) / 256), (g.nz + 7) / 8), 256, 0, c->stream>>>(
+      c->f[LES_THETA], sbr, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny, g.nz);
   LES_COUNT_LAUNCH();
 }
 // scalars_module.f90:457-504 step_scalar
-__global__ void k_step_scalar(double* theta, const double* __restrict__ R, const double* __restrict__ Rf, int ld,
-                              int nx, int ny, int nz, double dt, int top_grad, double inc) {
-  const size_t np = (size_t)ld * ny;
-  GSTRIDE(r, np) {
-    const int jx = (int)(r % ld);
-    if (jx < nx)
-      for (int jz = 1; jz <= nz - 1; ++jz) {
-        const size_t i = r + (size_t)(jz - 1) * np;
-        theta[i] = theta[i] + dt * (1.5 * R[i] - 0.5 * Rf[i]);
-      }
-    const size_t top = r + (size_t)(nz - 1) * np, below = r + (size_t)(nz - 2) * np;
-    theta[top] = top_grad ? theta[below] + inc : theta[below];
+// grid (ceil(np/256), nz-1): one element per thread (a column walk per
+// thread serialises the levels behind the stores); the thread of level
+// nz-1 also sets the top level from the value it has just written
+__global__ void k_step_scalar(double* __restrict__ theta, const double* __restrict__ R,
+                              const double* __restrict__ Rf, int ld, int nx, int ny, int nz, double dt,
+                              int top_grad, double inc) {
+  const int np = ld * ny;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = r + (size_t)(jz - 1) * np;
+  double t = theta[i];
+  if (r % ld < nx) {
+    t = t + dt * (1.5 * R[i] - 0.5 * Rf[i]);
+    theta[i] = t;
   }
+  if (jz == nz - 1) theta[i + np] = top_grad ? t + inc : t;
 }
 // scalars_module.f90:57-171 theta_all_in_one (S_FLAG, lbc = 1, model 5 Pr)
 int op_theta(les_ctx* c) {
@@ -2500,8 +2553,9 @@ int op_theta(les_ctx* c) {
     cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
   const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
-  k_step_scalar<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx,
-                                                       g.ny, nz, k.dt, topg, k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
+  k_step_scalar<<<dim3((unsigned)((g.nplane + 255) / 256), nz - 1), 256, 0, c->stream>>>(
+      c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx, g.ny, nz, k.dt, topg,
+      k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -3229,7 +3283,7 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   // perturbation keeps its precision; th0 is added back in FP64
   double* th0 = MX ? c->dred + 14 * (size_t)(nz + 8) : nullptr;
   if (MX) {
-    k_plane_mean<<<nz, 512, 0, c->stream>>>(c->f[LES_THETA], (long)g.nplane, g.ld, g.nx, g.ny, th0); LES_COUNT_LAUNCH();
+    plane_sums(c, c->f[LES_THETA], (long)g.nplane, nz, 4, (double)(g.nx * g.ny), th0);
   }
   {  // filt_da(theta) with the spectrum saved
     const double* in[1] = {c->f[LES_THETA]};
@@ -3325,8 +3379,9 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
   const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
-  k_step_scalar<<<grid1(g.nplane), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx,
-                                                       g.ny, nz, k.dt, topg, k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
+  k_step_scalar<<<dim3((unsigned)((g.nplane + 255) / 256), nz - 1), 256, 0, c->stream>>>(
+      c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx, g.ny, nz, k.dt, topg,
+      k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -3384,7 +3439,11 @@ static int stepT(les_ctx* c) {
   // RHS*_f = RHS* (main.f90:212-214, and RHS_Tf = RHS_T of the scalar): the
   // buffers are exchanged; RHS* is rewritten below before it is read
   rhs_swap(c);
-  op_obukhov(c);
+  // filtered surface u, v for obukhov and wallstress (u, v do not change in
+  // between): the last two temp planes, which nothing before wallstress uses
+  const double* uv1 = c->tmp + (size_t)(c->ntmp - 2) * g.nplane;
+  surface_uv_filtered(c, const_cast<double*>(uv1));
+  op_obukhov(c, uv1);
   if (!MX) {
     double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
     double* x3[3] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX]};
@@ -3398,7 +3457,7 @@ static int stepT(les_ctx* c) {
   op_ddz(c, c->f[LES_DWDZ], c->f[LES_W], 0);
   const bool rms_step = k.rmsdiv_every > 0 && c->jt % k.rmsdiv_every == 0;
   if (MX && rms_step) rmsdiv_mixed(c, c->tmp, c->f[LES_DWDZ], c->dscal + 1);
-  op_wallstress(c);
+  op_wallstress(c, uv1);
   {  // spectra of the wall planes dudz(1), dvdz(1) set by wallstress
     const double cs = 1.0 / (double)(g.nx * g.ny);
     const double* pl[2] = {c->f[LES_DUDZ], c->f[LES_DVDZ]};
