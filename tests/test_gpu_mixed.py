@@ -50,21 +50,24 @@ def test_mixed_vs_fp64(gpu_lib, n, steps):
     assert a["rmsdiv"] <= 1e-10, a["rmsdiv"]
 
 
-def test_mixed_vs_fp64_256_lengths(gpu_lib):
-    """256 x 256 x 32: the register-resident FP32 transforms of the 256^3
-    workload (y pass 256 = 16 x 16, x passes of half lengths 128 and 192) and
-    the Lagrangian filters restricted to the nonzero kx columns (a Lagrangian
-    step at step 5 and 10), against the FP64 form."""
+@pytest.mark.parametrize("n", [256, 128])
+def test_mixed_vs_fp64_256_lengths(gpu_lib, n):
+    """n x n x 32 for n = 256 and 128: the register-resident FP32 transforms
+    of the 256^3 workload (y pass 256 = 16 x 16, x passes of half lengths 128
+    and 192, the 3/2 padding and truncation y passes 256 <-> 384 = 16 x 24)
+    and of the 128^3 ensemble members (padding 128 <-> 192 = 16 x 12), and the
+    Lagrangian filters restricted to the nonzero kx columns (a Lagrangian step
+    at step 5 and 10), against the FP64 form."""
     # the seeded 256-wide state runs at CFL 0.109, above the in-step check's
     # 0.1, so the step-10 diagnostic is off; rmsdiv is read after the steps
-    a, b = run(256, 10, 1, levels=32, rmsdiv_every=0), run(256, 10, 0, levels=32, rmsdiv_every=0)
+    a, b = run(n, 10, 1, levels=32, rmsdiv_every=0), run(n, 10, 0, levels=32, rmsdiv_every=0)
     vel_a = np.concatenate([a[k].ravel() for k in ("u", "v", "w")])
     vel_b = np.concatenate([b[k].ravel() for k in ("u", "v", "w")])
     ev = rel(vel_a, vel_b)
     et = rel(a["theta"], b["theta"])
     ecs = rel(a["Cs_opt2"], b["Cs_opt2"])
     enu = rel(a["Nu_t"], b["Nu_t"])
-    print("mixed vs fp64 256x256x32", ev, et, ecs, enu, "rmsdiv", a["rmsdiv"], b["rmsdiv"])
+    print("mixed vs fp64 %dx%dx32" % (n, n), ev, et, ecs, enu, "rmsdiv", a["rmsdiv"], b["rmsdiv"])
     assert ev <= 1e-5 and et <= 1e-5, (ev, et)
     assert ecs <= 1e-3, ecs  # dynamic coefficient from FP32 filters (the reference truncates it to FP32)
     assert enu <= 1e-3, enu  # FP32-held eddy viscosity, read back widened
