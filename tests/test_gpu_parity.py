@@ -1,6 +1,7 @@
 """GPU (sm_103a library, through the C ABI) vs the CPU oracle on identical
 seeded inputs.  FP64 form: relative error <= 1e-12 on u, v, w, theta, Cs^2
-and rmsdiv (the benchmark spec's tolerance); routine-level checks at rounding level.
+and rmsdiv (the FP64 parity tolerance of the step); routine-level checks at
+rounding level.
 """
 import numpy as np
 import pytest
