@@ -43,7 +43,8 @@ typedef enum les_status {
   LES_ERR_NAN = -6,         /* non-finite value detected in the state          */
   LES_ERR_TIMEOUT = -7,     /* bounded device wait expired                     */
   LES_ERR_STATE = -8,       /* call made before the required set-up            */
-  LES_ERR_UNSUPPORTED = -9  /* size or mode not supported                      */
+  LES_ERR_UNSUPPORTED = -9, /* size or mode not supported                      */
+  LES_ERR_IO = -10          /* file open / read / write failed, bad record     */
 } les_status;
 
 /* Run configuration.  Mirrors the compile-time parameters of param.f90 and
@@ -142,6 +143,39 @@ int les_sync_from_host(les_ctx* ctx);
 int les_sync_to_host(les_ctx* ctx);
 /* Step counters (param.f90:147-148). */
 int les_get_counters(les_ctx* ctx, int* jt, int* jt_total);
+
+/* ---- checkpoint record ----------------------------------------------------- */
+/* io.f90:1314-1338 `checkpoint` (written by output_final, io.f90:1347-1383,
+ * and into output/vel_scNNNNNN.out, io.f90:223-233) and its reader
+ * initial.f90:54-114 (with scalars) / :128-160 (without), model 5, not
+ * inilag: one Fortran unformatted sequential record holding, with scalars,
+ *   u, v, w, theta, qmix, RHSx, RHSy, RHSz, RHS_T, RHS_q   (ld,ny,1:nz) each,
+ *   sgs_t3(:,:,1), sgs_q3(:,:,1)                          (ld,ny),
+ *   psi_m, psi_m0, psi_h, psi_h0                          (nx,ny),
+ *   Cs_opt2, F_LM, F_MM, F_QN, F_NN, G_LM, G_MM, G_QN, G_NN, Pr_t (ld,ny,nz);
+ * without scalars u, v, w, RHSx, RHSy, RHSz, Cs_opt2, F_LM, F_MM, F_QN, F_NN.
+ * Arrays this build does not carry are written as a model-5 run of the
+ * reference holds them (qmix, RHS_q, sgs_q3 and G_* zero, Pr_t = Pr) and
+ * skipped on reading.  The record keeps no step counters (the reference keeps
+ * jt_total in total_time.dat): a restart creates its context with
+ * jt_total0 = the steps taken, initu = 1 and initsc = 1, then reads the file.
+ * Record format: gfortran / Intel Fortran unformatted sequential, 4-byte
+ * little-endian markers around subrecords of at most 2147483639 bytes (a
+ * negative leading marker: another subrecord follows; a negative trailing
+ * marker: one precedes).  No counterpart in the reference for the functions
+ * themselves (its Fortran runtime does this I/O). */
+int les_checkpoint_write(les_ctx* ctx, const char* path);
+int les_checkpoint_read(les_ctx* ctx, const char* path);
+/* The record layer alone (host only, needs no context or GPU): write the
+ * concatenation of nparts buffers as one record (append 0: new file;
+ * max_subrecord <= 0: the standard 2147483639 bytes), or read the record at
+ * byte offset into the buffers -- the record must hold at least their total;
+ * the rest is skipped, as a Fortran read of a shorter list does -- returning
+ * the record's length and the offset of the next record. */
+int les_fortran_record_write(const char* path, int append, const void* const* parts, const size_t* nbytes,
+                             int nparts, long long max_subrecord);
+int les_fortran_record_read(const char* path, long long offset, void* const* parts, const size_t* nbytes,
+                            int nparts, long long* record_bytes, long long* next_offset);
 
 /* ---- fused time step ------------------------------------------------------ */
 /* main.f90:202-478: nsteps iterations of the time loop on the device-resident

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "liblesgb300.so")
 
 STATUS = {0: "LES_OK", -1: "LES_ERR_ARG", -2: "LES_ERR_CUDA", -3: "LES_ERR_OOM",
           -4: "LES_ERR_PIVOT", -5: "LES_ERR_CFL", -6: "LES_ERR_NAN", -7: "LES_ERR_TIMEOUT",
-          -8: "LES_ERR_STATE", -9: "LES_ERR_UNSUPPORTED"}
+          -8: "LES_ERR_STATE", -9: "LES_ERR_UNSUPPORTED", -10: "LES_ERR_IO"}
 
 
 class LesError(RuntimeError):
@@ -63,6 +63,15 @@ def lib():
         L.les_set_surface.argtypes = [vp, dp, dp]
         L.les_rmsdiv.argtypes = [vp, dp]
         L.les_ctx_set_pointer_mode.argtypes = [vp, ip]
+        cp, ll = ctypes.c_char_p, ctypes.c_longlong
+        for name in ["les_checkpoint_write", "les_checkpoint_read", "les_fortran_record_write",
+                     "les_fortran_record_read"]:
+            getattr(L, name).restype = ip
+        L.les_checkpoint_write.argtypes = [vp, cp]
+        L.les_checkpoint_read.argtypes = [vp, cp]
+        L.les_fortran_record_write.argtypes = [cp, ip, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t), ip, ll]
+        L.les_fortran_record_read.argtypes = [cp, ll, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t), ip,
+                                              ctypes.POINTER(ll), ctypes.POINTER(ll)]
         _lib = L
     return _lib
 
@@ -172,6 +181,37 @@ class Context:
 
     def set_pointer_mode(self, device):
         check(self.L.les_ctx_set_pointer_mode(self.h, 1 if device else 0))
+
+    # --- checkpoint record (io.f90:1314-1338, initial.f90:54-160) ------------
+    def checkpoint_write(self, path):
+        check(self.L.les_checkpoint_write(self.h, os.fsencode(path)))
+
+    def checkpoint_read(self, path):
+        check(self.L.les_checkpoint_read(self.h, os.fsencode(path)))
+
+
+def fortran_record_write(path, parts, append=False, max_subrecord=0):
+    """Write the concatenation of the byte buffers in parts as one Fortran
+    unformatted sequential record (les_fortran_record_write)."""
+    L = lib()
+    bufs = [np.ascontiguousarray(p).view(np.uint8).ravel() for p in parts]
+    ptrs = (ctypes.c_void_p * max(1, len(bufs)))(*[b.ctypes.data for b in bufs])
+    sizes = (ctypes.c_size_t * max(1, len(bufs)))(*[b.nbytes for b in bufs])
+    check(L.les_fortran_record_write(os.fsencode(path), 1 if append else 0, ptrs, sizes, len(bufs),
+                                     ctypes.c_longlong(max_subrecord)))
+
+
+def fortran_record_read(path, nbytes, offset=0):
+    """Read the record at byte offset into buffers of the given sizes;
+    returns (buffers, record length, offset of the next record)."""
+    L = lib()
+    bufs = [np.empty(int(n), dtype=np.uint8) for n in nbytes]
+    ptrs = (ctypes.c_void_p * max(1, len(bufs)))(*[b.ctypes.data for b in bufs])
+    sizes = (ctypes.c_size_t * max(1, len(bufs)))(*[b.nbytes for b in bufs])
+    rec, nxt = ctypes.c_longlong(), ctypes.c_longlong()
+    check(L.les_fortran_record_read(os.fsencode(path), ctypes.c_longlong(offset), ptrs, sizes, len(bufs),
+                                    ctypes.byref(rec), ctypes.byref(nxt)))
+    return bufs, rec.value, nxt.value
 
 
 class Ensemble:
