@@ -53,7 +53,8 @@ typedef enum les_status {
 typedef struct les_config {
   int nx, ny, nz;       /* param.f90:56   grid; nz = uvp levels + 1             */
   int model;            /* param.f90:115  5 = Lagrangian scale-dependent,
-                                          3 = plane-averaged scale-dependent    */
+                                          3 = plane-averaged scale-dependent,
+                                          2 = standard dynamic (plane-averaged) */
   int s_flag;           /* param.f90:158  1 = active potential temperature      */
   int initu;            /* param.f90:79   0 = Euler first momentum step         */
   int initsc;           /* param.f90:79   0 = Euler first scalar step           */
@@ -297,6 +298,10 @@ int les_interpolag_sdep(les_ctx* ctx);
 int les_scaledep_dynamic(les_ctx* ctx, double* cs_opt2, const double* S11, const double* S12,
                          const double* S13, const double* S22, const double* S23,
                          const double* S33);
+/* std_dynamic.f90:1-136 (model 2) -> cs_opt2 (nz) with S_ij (ld,ny,nz) and
+ * the context's u, v, w. */
+int les_std_dynamic(les_ctx* ctx, double* cs_opt2, const double* S11, const double* S12, const double* S13,
+                    const double* S22, const double* S23, const double* S33);
 /* wallstress.f90:5-69, scalars_module.f90:508-690 (obukhov),
  * forcing.f90:128-219 (project), scalars_module.f90:57-171 (theta_all_in_one). */
 int les_wallstress(les_ctx* ctx);

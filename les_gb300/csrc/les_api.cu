@@ -275,8 +275,11 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     return LES_ERR_ARG;
   }
   if (k.precision != 0 && k.precision != 1) { les_set_error("precision must be 0 or 1"); return LES_ERR_ARG; }
-  if (k.model != 5 && k.model != 3) { les_set_error("model must be 5 or 3"); return LES_ERR_UNSUPPORTED; }
-  if (k.precision == 1 && k.model != 5) {  // model 3's plane sums read S_ij in FP64
+  if (k.model != 5 && k.model != 3 && k.model != 2) {
+    les_set_error("model must be 5, 3 or 2");
+    return LES_ERR_UNSUPPORTED;
+  }
+  if (k.precision == 1 && k.model != 5) {  // the plane-averaged models read S_ij in FP64
     les_set_error("the FP32-mixed form (precision 1) runs model 5");
     return LES_ERR_UNSUPPORTED;
   }
@@ -1072,6 +1075,17 @@ int les_scaledep_dynamic(les_ctx* c, double* cs_opt2, const double* S11, const d
   CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in()); CHK(o.alloc());
   const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
   op_scaledep(c, o.dev, S);
+  CHK(o.out());
+  return finish(c);
+}
+int les_std_dynamic(les_ctx* c, double* cs_opt2, const double* S11, const double* S12, const double* S13,
+                    const double* S22, const double* S23, const double* S33) {
+  if (!c || !cs_opt2 || !S11 || !S12 || !S13 || !S22 || !S23 || !S33) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg a(c, S11, n), b(c, S12, n), d(c, S13, n), e(c, S22, n), f(c, S23, n), h(c, S33, n), o(c, cs_opt2, c->g.nz);
+  CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in()); CHK(o.alloc());
+  const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
+  op_stddyn(c, o.dev, S);
   CHK(o.out());
   return finish(c);
 }

@@ -141,6 +141,7 @@ int op_sgs_stag(les_ctx* c);
 int op_lagrange(les_ctx* c, const double* const* S);
 int op_interpolag(les_ctx* c);
 int op_scaledep(les_ctx* c, double* cs_z_dev, const double* const* S);
+int op_stddyn(les_ctx* c, double* cs_z_dev, const double* const* S);
 int op_theta(les_ctx* c);
 int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz);
 int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz, int w_variant);

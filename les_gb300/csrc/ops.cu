@@ -1012,9 +1012,10 @@ int op_sgs_stag(les_ctx* c) {
       c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0); LES_COUNT_LAUNCH();
   const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
   if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {  // sgs_stag.f90:120-160
-    if (k.model == 3) {
+    if (k.model == 2 || k.model == 3) {
       double* csz = c->dred;
-      op_scaledep(c, csz, S);
+      if (k.model == 2) op_stddyn(c, csz, S);
+      else op_scaledep(c, csz, S);
       // Cs_opt2(:,:,jz) = ziko(jz)
       k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
     } else if (k.model == 5) {
@@ -1465,7 +1466,8 @@ __global__ void __launch_bounds__(256) k_sd_final(const double* __restrict__ flt
   const int lc = blockIdx.x;
   const int jz = jz0 + lc;
   const size_t st = np * nlev;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && !sums) beta_s = 1.0;  // std_dynamic.f90:120-127: no scale dependence
+  if (threadIdx.x == 0 && sums) {
     const double* s = sums + (size_t)(jz - 1) * 10;
     const double N2 = (double)(nx * ny);
     const double d2 = delta * delta, t2 = (2.0 * d2) * (2.0 * d2);
@@ -1508,6 +1510,38 @@ __global__ void __launch_bounds__(256) k_sd_final(const double* __restrict__ flt
     __syncthreads();
   }
   if (threadIdx.x == 0) cs_z[jz - 1] = fmax(0.0, sn[0] / sd[0]);
+}
+// std_dynamic.f90:1-136 (model 2) -> cs_z (device, nz): the 21 planes of
+// k_sd_prep G_test-filtered, then k_sd_final with beta = 1 and
+// delta = (dx dy dz)^(1/3) (std_dynamic.f90:28)
+int op_stddyn(les_ctx* c, double* cs_z, const double* const* S) {
+  const Grid& g = c->g;
+  Ptr6 Sp;
+  for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
+  const double delta3 = std::pow(g.dx * g.dy * g.dz, 1.0 / 3.0);
+  const int nch = c->lag_chunk;
+  for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
+    const int nl = std::min(nch, g.nz - jz0 + 1);
+    double* prep = c->tmp;
+    double* flt = c->tmp + (size_t)21 * nch * g.nplane;
+    k_sd_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W],
+                                                          Sp, prep, g.ld, g.nx, g.ny,
+                                                          jz0, nl, g.nplane); LES_COUNT_LAUNCH();
+    const double* in[21];
+    for (int q = 0; q < 21; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
+    r2c(c, 21, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nl);
+    J.nin = 1; J.nout = 1; J.nf = 21;
+    J.in[0] = c->wsA; J.fs_in = (long)nl * g.C;
+    J.out[0] = c->wsB; J.fs_out = (long)nl * g.C;
+    J.coef[0][0] = CC_G;
+    cols(c, J);
+    double* out[21];
+    for (int q = 0; q < 21; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
+    c2r(c, 21, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    k_sd_final<<<nl, 256, 0, c->stream>>>(flt, nullptr, cs_z, g.ld, g.nx, g.ny, nl, g.nplane, jz0, delta3); LES_COUNT_LAUNCH();
+  }
+  return 0;
 }
 int op_scaledep(les_ctx* c, double* cs_z, const double* const* S) {
   const Grid& g = c->g;
@@ -3114,9 +3148,10 @@ static int sgs_stagT(les_ctx* c) {
   LES_COUNT_LAUNCH();
   const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
   if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {
-    if (k.model == 3) {
+    if (k.model == 2 || k.model == 3) {
       double* csz = c->dred;
-      op_scaledep(c, csz, S);
+      if (k.model == 2) op_stddyn(c, csz, S);
+      else op_scaledep(c, csz, S);
       k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
     } else if (k.model == 5) {
       lagrangeT<MX>(c);

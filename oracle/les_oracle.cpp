@@ -467,9 +467,12 @@ struct Oracle {
     }
     const double l = delta;  // :109
     if ((jt >= 1 || initu) && (jt % cs_count == 0)) {  // :120-121, DYN_init = 1
-      if (model == 3) {
+      if (model == 2 || model == 3) {  // sgs_stag.f90:124-135
         std::vector<double> ziko(nz);
-        scaledep_dynamic(ziko.data(), S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
+        if (model == 2)
+          std_dynamic(ziko.data(), S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
+        else
+          scaledep_dynamic(ziko.data(), S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
         for (int jz = 1; jz <= nz; ++jz)
           for (size_t i = 0; i < nplane; ++i) Cs_opt2[(size_t)(jz - 1) * nplane + i] = ziko[jz - 1];
       } else if (model == 5) {
@@ -739,6 +742,73 @@ struct Oracle {
       if (std::fabs(d) < xacc) return r;
     }
     return 1.0;
+  }
+
+  // std_dynamic.f90:1-136 (model 2): per level, u, v, w on w-nodes and their
+  // products (:33-61), G_test (2 delta) filtered, L_ij = (uu)~ - u~u~
+  // (:64-78); S_ij and |S| S_ij filtered (:83-117); M_ij = 2 delta^2
+  // (|S|S_ij~ - 4 |S~| S_ij~) (:120-127) with delta = filter_size
+  // (dx dy dz)^(1/3) (:28, unlike the (dx dy)^(1/2) of sgs_stag and
+  // scaledep_dynamic); Cs^2(jz) = max(0, sum L_ij M_ij / sum M_ij M_ij)
+  // (:130-133).  The sums
+  // run over 1:nx: the (ld,ny) sums of the reference add the two padding
+  // columns, which hold zero after the test filter (G_test's kx = nx/2
+  // column is zero).
+  void std_dynamic(double* cs_z, const double* s11, const double* s12, const double* s13, const double* s22,
+                   const double* s23, const double* s33) {
+    const double delta = 1.0 * std::pow(dx * dy * dz, 1.0 / 3.0);
+#pragma omp parallel for schedule(static)
+    for (int jz = 1; jz <= nz; ++jz) {
+      const size_t NP = nplane, o = (size_t)(jz - 1) * NP;
+      std::vector<double> buf(NP * 21);
+      auto pl = [&](int q) { return buf.data() + (size_t)q * NP; };
+      for (size_t i = 0; i < NP; ++i) {  // :33-61
+        double ub, vb, wb;
+        if (jz == 1) {
+          ub = u[i]; vb = v[i]; wb = 0.25 * w[NP + i];
+          pl(3)[i] = u[i] * u[i]; pl(4)[i] = u[i] * v[i]; pl(5)[i] = u[i] * 0.25 * w[NP + i];
+          pl(6)[i] = v[i] * v[i]; pl(7)[i] = v[i] * 0.25 * w[NP + i];
+          const double t = 0.25 * w[NP + i];
+          pl(8)[i] = t * t;
+        } else {
+          ub = 0.5 * (u[o + i] + u[o - NP + i]);
+          vb = 0.5 * (v[o + i] + v[o - NP + i]);
+          wb = w[o + i];
+          pl(3)[i] = 0.5 * (u[o + i] + u[o - NP + i]) * 0.5 * (u[o + i] + u[o - NP + i]);
+          pl(4)[i] = 0.5 * (u[o + i] + u[o - NP + i]) * 0.5 * (v[o + i] + v[o - NP + i]);
+          pl(5)[i] = 0.5 * (u[o + i] + u[o - NP + i]) * w[o + i];
+          pl(6)[i] = 0.5 * (v[o + i] + v[o - NP + i]) * 0.5 * (v[o + i] + v[o - NP + i]);
+          pl(7)[i] = 0.5 * (v[o + i] + v[o - NP + i]) * w[o + i];
+          pl(8)[i] = w[o + i] * w[o + i];
+        }
+        pl(0)[i] = ub; pl(1)[i] = vb; pl(2)[i] = wb;
+      }
+      const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+      for (int q = 0; q < 3; ++q) test_filter(pl(q), G_test);
+      for (int q = 0; q < 6; ++q) {  // :64-78
+        test_filter(pl(3 + q), G_test);
+        for (size_t i = 0; i < NP; ++i) pl(3 + q)[i] = pl(3 + q)[i] - pl(ia[q])[i] * pl(ib[q])[i];
+      }
+      const double* Sp[6] = {s11 + o, s12 + o, s13 + o, s22 + o, s23 + o, s33 + o};
+      for (size_t i = 0; i < NP; ++i) {  // :83-111
+        const double S = smag(Sp[0][i], Sp[3][i], Sp[5][i], Sp[1][i], Sp[2][i], Sp[4][i]);
+        for (int q = 0; q < 6; ++q) { pl(9 + q)[i] = Sp[q][i]; pl(15 + q)[i] = S * Sp[q][i]; }
+      }
+      for (int q = 0; q < 12; ++q) test_filter(pl(9 + q), G_test);
+      const double cst = 2.0 * (delta * delta);
+      double num = 0.0, den = 0.0;
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= nx; ++jx) {
+          const size_t i = (size_t)(jx - 1) + (size_t)ld * (jy - 1);
+          double b[6], sb[6], Lq[6], M[6];
+          for (int q = 0; q < 6; ++q) { b[q] = pl(9 + q)[i]; sb[q] = pl(15 + q)[i]; Lq[q] = pl(3 + q)[i]; }
+          const double Sb = smag(b[0], b[3], b[5], b[1], b[2], b[4]);  // :102-103
+          for (int q = 0; q < 6; ++q) M[q] = cst * (sb[q] - 4.0 * Sb * b[q]);
+          num += Lq[0] * M[0] + Lq[3] * M[3] + Lq[5] * M[5] + 2.0 * (Lq[1] * M[1] + Lq[2] * M[2] + Lq[4] * M[4]);
+          den += M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + 2.0 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+        }
+      cs_z[jz - 1] = std::max(0.0, num / den);
+    }
   }
 
   // scaledep_dynamic.f90:4-255 (sums over 1:nx)
@@ -1542,6 +1612,10 @@ void lo_interpolag_sdep(void* h) { ((Oracle*)h)->interpolag_Sdep(); }
 void lo_scaledep_dynamic(void* h, double* cs_z) {
   Oracle* o = (Oracle*)h;
   o->scaledep_dynamic(cs_z, o->S11.data(), o->S12.data(), o->S13.data(), o->S22.data(), o->S23.data(), o->S33.data());
+}
+void lo_std_dynamic(void* h, double* cs_z, const double* s11, const double* s12, const double* s13,
+                    const double* s22, const double* s23, const double* s33) {
+  ((Oracle*)h)->std_dynamic(cs_z, s11, s12, s13, s22, s23, s33);
 }
 void lo_wallstress(void* h) { ((Oracle*)h)->wallstress(); }
 void lo_obukhov(void* h) { ((Oracle*)h)->obukhov(); }

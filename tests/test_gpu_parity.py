@@ -164,6 +164,53 @@ def test_step_parity_32_plane_scaledep(libs):
         assert e < 1e-5, (nm, e)
 
 
+def test_std_dynamic_routine(libs):
+    """std_dynamic.f90:1-136 (model 2) on the same u, v, w and S_ij: the
+    per-level Cs^2 of the GPU (plane sums in a fixed tree order) against the
+    oracle (sequential sums)."""
+    cfg = lg.make_config(32, 32, 20, model=2, s_flag=0)
+    surf = lg.uniform_surface(cfg)
+    g, o = pair(cfg, surf, seed=5)
+    rng = np.random.default_rng(6)
+    shp = lg.field_shape(cfg, "u")
+    S = []
+    for q in range(6):  # smooth strain-like fields (a few low modes per level)
+        a = np.zeros(shp)
+        x = np.arange(cfg.nx) * 2 * np.pi / cfg.nx
+        X, Y = np.meshgrid(x, x)
+        for k in range(shp[0]):
+            a[k, :, :cfg.nx] = sum(rng.standard_normal() * np.cos(i * X + j * Y + rng.uniform(0, 6.3))
+                                   for i in range(4) for j in range(-3, 4)) / 10.0
+        S.append(a)
+    cg, co = np.zeros(cfg.nz), np.zeros(cfg.nz)
+    g.call("std_dynamic", cg, *S)
+    o.call("std_dynamic", co, *S)
+    assert np.all(co >= 0) and np.any(co > 0)
+    assert rel(cg, co) < TOL, (cg, co)
+
+
+def test_step_parity_32_std_dynamic(libs):
+    """model = 2 (standard dynamic, plane-averaged Cs^2 from the 2 delta test
+    filter, std_dynamic.f90): 10 steps with active theta; the dynamic Cs^2 is
+    computed at steps 5 and 10 and feeds back.  Velocities and theta are held
+    to 1e-12.  Cs^2(z) is a ratio of plane sums whose numerator cancels: the
+    oracle built with and without FMA contraction differs by up to 2.8e-11
+    per level after these 10 steps (u, v, w by 6e-14 at most), so Cs^2 is
+    held to that rounding sensitivity (1e-9), not 1e-12."""
+    cfg = lg.make_config(32, s_flag=1, jt_total0=500, model=2, rmsdiv_every=1)
+    surf = lg.striped_surface(cfg)
+    g, o = pair(cfg, surf)
+    g.step(10)
+    assert o.step(10) == 0
+    for nm in ["u", "v", "theta"]:
+        e = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
+        assert e < TOL, (nm, e)
+    e = rel(interior(cfg, g.get("w"), slice(None)), interior(cfg, o.get("w"), slice(None)))
+    assert e < TOL, ("w", e)
+    cg, co = interior(cfg, g.get("Cs_opt2"), slice(None)), interior(cfg, o.get("Cs_opt2"), slice(None))
+    assert np.any(co > 0) and rel(cg, co) < 1e-9, rel(cg, co)
+
+
 def test_step_parity_128_theta(libs):
     """128^3, active theta, striped z0 and heat flux; 20 steps."""
     from oracle.oracle import Oracle

@@ -261,3 +261,56 @@ def test_pressure_zero_mode_closed_form(O):
     wm = w[:, :, :16].mean(axis=(1, 2)) / (1.5 * cfg.dt)
     for k in range(2, cfg.nz):
         assert abs((pm[k] - pm[k - 1]) - wm[k - 1] * dz) < 1e-9 * max(1.0, abs(wm[k - 1] * dz))
+
+
+def _std_dynamic(O, u, v, w, S, nz):
+    """Oracle std_dynamic (model 2) on given velocities and S_ij."""
+    cfg = C.make_config(16, 16, nz - 1, model=2)
+    o = O(cfg)
+    o.set("u", u); o.set("v", v); o.set("w", w)
+    cs = np.zeros(nz)
+    o.call("std_dynamic", cs, *S)
+    return cs
+
+
+def _smooth_state(seed, nz):
+    """Band-limited velocities and strain-like fields on a 16 x 16 x nz grid."""
+    rng = np.random.default_rng(seed)
+    ld, n = 18, 16
+    x = np.arange(n) * 2 * np.pi / n
+    X, Y = np.meshgrid(x, x)  # (ny, nx)
+    out = []
+    for q in range(9):
+        a = np.zeros((nz, n, ld))
+        for k in range(nz):
+            f = sum(rng.standard_normal() * np.cos(kx * X + ky * Y + rng.uniform(0, 6.3))
+                    for kx in range(0, 6) for ky in range(-5, 6))
+            a[k, :, :n] = f / 30.0
+        out.append(a)
+    return out[:3], out[3:]
+
+
+def test_std_dynamic_scale_invariance(O):
+    """std_dynamic.f90: Cs^2 = <L M>/<M M> with L quadratic in the velocity
+    and M quadratic in S_ij, so scaling u, v, w and S_ij by a common factor
+    leaves Cs^2 unchanged; Cs^2 >= 0 (the clip of :133)."""
+    nz = 6
+    (u, v, w), S = _smooth_state(3, nz)
+    a = _std_dynamic(O, u, v, w, S, nz)
+    b = _std_dynamic(O, 2.5 * u, 2.5 * v, 2.5 * w, [2.5 * s for s in S], nz)
+    assert np.all(a >= 0) and np.any(a > 0)
+    assert rel(b, a) < 1e-12, (a, b)
+
+
+def test_std_dynamic_galilean_invariance(O):
+    """A uniform velocity passes the spectral test filter unchanged (G_test's
+    (0,0) entry is 1/(nx ny)), so L_ij = (u_i u_j)~ - u_i~ u_j~ and Cs^2 do not
+    change when a constant is added to u and v."""
+    nz = 6
+    (u, v, w), S = _smooth_state(4, nz)
+    a = _std_dynamic(O, u, v, w, S, nz)
+    u2, v2 = u.copy(), v.copy()
+    u2[:, :, :16] += 0.7
+    v2[:, :, :16] -= 0.3
+    b = _std_dynamic(O, u2, v2, w, S, nz)
+    assert rel(b, a) < 1e-10, (a, b)
