@@ -53,6 +53,7 @@ typedef enum les_status {
 typedef struct les_config {
   int nx, ny, nz;       /* param.f90:56   grid; nz = uvp levels + 1             */
   int model;            /* param.f90:115  5 = Lagrangian scale-dependent,
+                                          4 = Lagrangian scale-invariant,
                                           3 = plane-averaged scale-dependent,
                                           2 = standard dynamic (plane-averaged) */
   int s_flag;           /* param.f90:158  1 = active potential temperature      */
@@ -294,6 +295,12 @@ int les_lagrange_sdep(les_ctx* ctx, const double* S11, const double* S12, const 
                       const double* S22, const double* S23, const double* S33);
 /* interpolag_Sdep.f90:2-380 on the context's F_* and u/v/w_lag. */
 int les_interpolag_sdep(les_ctx* ctx);
+/* lagrange_Ssim.f90:1-335 (model 4, calls interpolag_Ssim) with S_ij
+ * (ld,ny,nz); interpolag_Ssim.f90:2-212 on the context's F_LM, F_MM and
+ * u/v/w_lag. */
+int les_lagrange_ssim(les_ctx* ctx, const double* S11, const double* S12, const double* S13,
+                      const double* S22, const double* S23, const double* S33);
+int les_interpolag_ssim(les_ctx* ctx);
 /* scaledep_dynamic.f90:4-255 -> cs_opt2 (nz) with S_ij (ld,ny,nz). */
 int les_scaledep_dynamic(les_ctx* ctx, double* cs_opt2, const double* S11, const double* S12,
                          const double* S13, const double* S22, const double* S23,

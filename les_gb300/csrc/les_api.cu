@@ -275,8 +275,8 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     return LES_ERR_ARG;
   }
   if (k.precision != 0 && k.precision != 1) { les_set_error("precision must be 0 or 1"); return LES_ERR_ARG; }
-  if (k.model != 5 && k.model != 3 && k.model != 2) {
-    les_set_error("model must be 5, 3 or 2");
+  if (k.model != 5 && k.model != 4 && k.model != 3 && k.model != 2) {
+    les_set_error("model must be 5, 4, 3 or 2");
     return LES_ERR_UNSUPPORTED;
   }
   if (k.precision == 1 && k.model != 5) {  // the plane-averaged models read S_ij in FP64
@@ -1060,6 +1060,21 @@ int les_lagrange_sdep(les_ctx* c, const double* S11, const double* S12, const do
   CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in());
   const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
   op_lagrange(c, S);
+  return finish(c);
+}
+int les_lagrange_ssim(les_ctx* c, const double* S11, const double* S12, const double* S13, const double* S22,
+                      const double* S23, const double* S33) {
+  if (!c || !S11 || !S12 || !S13 || !S22 || !S23 || !S33) return LES_ERR_ARG;
+  const size_t n = c->g.nfield;
+  Arg a(c, S11, n), b(c, S12, n), d(c, S13, n), e(c, S22, n), f(c, S23, n), h(c, S33, n);
+  CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in());
+  const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
+  op_lagrange_ssim(c, S);
+  return finish(c);
+}
+int les_interpolag_ssim(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  op_interpolag_n(c, 2);
   return finish(c);
 }
 int les_interpolag_sdep(les_ctx* c) {

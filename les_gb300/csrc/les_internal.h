@@ -140,6 +140,8 @@ int op_wallstress(les_ctx* c, const double* uv1 = nullptr);
 int op_sgs_stag(les_ctx* c);
 int op_lagrange(les_ctx* c, const double* const* S);
 int op_interpolag(les_ctx* c);
+int op_interpolag_n(les_ctx* c, int nf);  // nf 4: interpolag_Sdep, 2: interpolag_Ssim
+int op_lagrange_ssim(les_ctx* c, const double* const* S);
 int op_scaledep(les_ctx* c, double* cs_z_dev, const double* const* S);
 int op_stddyn(les_ctx* c, double* cs_z_dev, const double* const* S);
 int op_theta(les_ctx* c);

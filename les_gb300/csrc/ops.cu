@@ -1018,6 +1018,8 @@ int op_sgs_stag(les_ctx* c) {
       else op_scaledep(c, csz, S);
       // Cs_opt2(:,:,jz) = ziko(jz)
       k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
+    } else if (k.model == 4) {
+      op_lagrange_ssim(c, S);
     } else if (k.model == 5) {
       op_lagrange(c, S);
     }
@@ -1047,6 +1049,10 @@ __device__ __forceinline__ double lag_disp_u(const double* ul, size_t i, size_t 
   const double ua = (jz >= 2) ? 0.5 * (a + ul[i - np] / cs) : a;
   return -ua * dt * cs / dxx;
 }
+// NF: F_* fields carried (4: interpolag_Sdep, 2: interpolag_Ssim, which
+// also lacks the near-wall clip of :285-293, so its level 1 keeps
+// 0.25 w_lag(2), doubled when positive).
+template <int NF, bool SDEP>
 __global__ void k_interpolag(const double* __restrict__ ul, const double* __restrict__ vl,
                              const double* __restrict__ wl, const double* __restrict__ FLM,
                              const double* __restrict__ FMM, const double* __restrict__ FQN,
@@ -1066,12 +1072,18 @@ __global__ void k_interpolag(const double* __restrict__ ul, const double* __rest
       // level 2 after the near-wall doubling and clipping (:285-293);
       // level 1 takes level 2's final value
       const size_t i2 = (size_t)jx + (size_t)ld * jy + np;
-      if (jz <= 2) {
+      if (SDEP && jz <= 2) {
         double z2 = -(wl[i2] / cs) * dt * cs / dz;
         z2 = z2 + fmin(z2, 0.0);
         z2 = fmin(1.0, z2);
         z2 = fmax(-1.0, z2);
         zp = z2;
+      } else if (!SDEP && jz == 2) {
+        const double z2 = -(wl[i2] / cs) * dt * cs / dz;
+        zp = z2 + fmin(z2, 0.0);
+      } else if (!SDEP && jz == 1) {
+        const double z1 = -(0.25 * (wl[i2] / cs)) * dt * cs / dz;
+        zp = z1 + fmax(z1, 0.0);
       } else {
         zp = -(wl[i] / cs) * dt * cs / dz;
       }
@@ -1092,8 +1104,10 @@ __global__ void k_interpolag(const double* __restrict__ ul, const double* __rest
    cx * fy * (F[a10 + z0] * fz + F[a10 + z1] * cz) + cx * cy * (F[a11 + z0] * fz + F[a11 + z1] * cz))
     oLM[i] = LAGI(FLM);
     oMM[i] = LAGI(FMM);
-    oQN[i] = LAGI(FQN);
-    oNN[i] = LAGI(FNN);
+    if constexpr (NF == 4) {
+      oQN[i] = LAGI(FQN);
+      oNN[i] = LAGI(FNN);
+    }
 #undef LAGI
   }
 }
@@ -1185,17 +1199,25 @@ static int op_interpolag32(les_ctx* c) {
   cudaMemsetAsync(c->f[LES_W_LAG], 0, g.nfield * sizeof(double), c->stream);
   return 0;
 }
-int op_interpolag(les_ctx* c) {
+int op_interpolag(les_ctx* c) { return op_interpolag_n(c, 4); }
+// nf = 4: interpolag_Sdep.f90:2-380; nf = 2: interpolag_Ssim.f90:2-212
+int op_interpolag_n(les_ctx* c, int nf) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   double* Fn[4];
   for (int q = 0; q < 4; ++q) Fn[q] = c->spare + (size_t)q * g.nfield;
-  k_interpolag<<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
-      c->f[LES_U_LAG], c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN],
-      c->f[LES_F_NN], Fn[0], Fn[1], Fn[2], Fn[3], g.ld, g.nx, g.ny, g.nz, (double)k.cs_count, k.dt, g.dx, g.dy,
-      g.dz); LES_COUNT_LAUNCH();
+  if (nf == 4)
+    k_interpolag<4, true><<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
+        c->f[LES_U_LAG], c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN],
+        c->f[LES_F_NN], Fn[0], Fn[1], Fn[2], Fn[3], g.ld, g.nx, g.ny, g.nz, (double)k.cs_count, k.dt, g.dx, g.dy,
+        g.dz);
+  else
+    k_interpolag<2, false><<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
+        c->f[LES_U_LAG], c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_F_LM], c->f[LES_F_MM], nullptr, nullptr,
+        Fn[0], Fn[1], nullptr, nullptr, g.ld, g.nx, g.ny, g.nz, (double)k.cs_count, k.dt, g.dx, g.dy, g.dz);
+  LES_COUNT_LAUNCH();
   // interior values changed; padding columns are never read
-  for (int q = 0; q < 4; ++q)
+  for (int q = 0; q < nf; ++q)
     cudaMemcpyAsync(c->f[LES_F_LM + q], Fn[q], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemsetAsync(c->f[LES_U_LAG], 0, g.nfield * sizeof(double), c->stream);
   cudaMemsetAsync(c->f[LES_V_LAG], 0, g.nfield * sizeof(double), c->stream);
@@ -1511,6 +1533,86 @@ __global__ void __launch_bounds__(256) k_sd_final(const double* __restrict__ flt
   }
   if (threadIdx.x == 0) cs_z[jz - 1] = fmax(0.0, sn[0] / sd[0]);
 }
+// lagrange_Ssim.f90:247-302 (model 4) on one chunk of levels: L_ij and M_ij
+// (fourbeta = 4 Beta = 4) from the 21 G_test-filtered planes, LM and MM per
+// point, the Lagrangian relaxation of F_LM, F_MM and Cs^2 = F_LM / F_MM.
+// Every column of (ld,ny) is relaxed as the reference does; LM = MM = 0 on
+// the padding columns, where Cs^2 ends at eps.
+__global__ void k_ssim_final(const double* __restrict__ flt, double* F_LM, double* F_MM, double* Cs,
+                             int ld, int nx, int ny, int nlev, size_t np, int jz0, double cst, double opftdelta,
+                             double lagran_dt) {
+  const double eps = 1e-32;  // lagrange_Ssim.f90:20
+  const size_t st = np * nlev;
+  GSTRIDE(t, st) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jx = (int)(r % ld);
+    const size_t i = (size_t)(jz0 - 1 + lc) * np + r;
+    double LM = 0.0, MM = 0.0;
+    if (jx < nx) {
+      const double* G = flt + t;
+      const double ub = G[0], vb = G[st], wb = G[2 * st];
+      const double L[6] = {G[3 * st] - ub * ub, G[4 * st] - ub * vb, G[5 * st] - ub * wb,
+                           G[6 * st] - vb * vb, G[7 * st] - vb * wb, G[8 * st] - wb * wb};
+      double b[6], sb[6], M[6];
+      for (int q = 0; q < 6; ++q) { b[q] = G[(9 + q) * st]; sb[q] = G[(15 + q) * st]; }
+      const double Sb = smag(b[0], b[3], b[5], b[1], b[2], b[4]);
+      for (int q = 0; q < 6; ++q) M[q] = cst * (sb[q] - 4.0 * Sb * b[q]);
+      LM = L[0] * M[0] + L[3] * M[3] + L[5] * M[5] + 2.0 * (L[1] * M[1] + L[2] * M[2] + L[4] * M[4]);
+      MM = M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + 2.0 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+    }
+    double flm = F_LM[i], fmm = F_MM[i];
+    double Tn = fmax(flm * fmm, eps);
+    Tn = opftdelta * pow_m18(Tn);
+    const double dumfac = lagran_dt / Tn;
+    const double epsi = dumfac / (1.0 + dumfac);
+    flm = epsi * LM + (1.0 - epsi) * flm;
+    fmm = epsi * MM + (1.0 - epsi) * fmm;
+    flm = fmax(eps, flm);
+    F_LM[i] = flm;
+    F_MM[i] = fmm;
+    Cs[i] = fmax(eps, jx < nx ? flm / fmm : 0.0);
+  }
+}
+// lagrange_Ssim.f90:1-335 (model 4): Beta = 1, interpolag_Ssim, then per
+// chunk of levels the 21 planes of k_sd_prep G_test-filtered and the
+// relaxation of k_ssim_final
+int op_lagrange_ssim(les_ctx* c, const double* const* S) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  fill(c, c->f[LES_BETA], g.nfield, 1.0);
+  op_interpolag_n(c, 2);
+  Ptr6 Sp;
+  for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
+  const double cst = 2.0 * (g.delta * g.delta), opftdelta = 1.5 * g.delta;
+  const double lagran_dt = k.dt * (double)k.cs_count;
+  const int nch = c->lag_chunk;
+  for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
+    const int nl = std::min(nch, g.nz - jz0 + 1);
+    double* prep = c->tmp;
+    double* flt = c->tmp + (size_t)21 * nch * g.nplane;
+    k_sd_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W],
+                                                          Sp, prep, g.ld, g.nx, g.ny,
+                                                          jz0, nl, g.nplane); LES_COUNT_LAUNCH();
+    const double* in[21];
+    for (int q = 0; q < 21; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
+    r2c(c, 21, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nl);
+    J.nin = 1; J.nout = 1; J.nf = 21;
+    J.in[0] = c->wsA; J.fs_in = (long)nl * g.C;
+    J.out[0] = c->wsB; J.fs_out = (long)nl * g.C;
+    J.coef[0][0] = CC_G;
+    cols(c, J);
+    double* out[21];
+    for (int q = 0; q < 21; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
+    c2r(c, 21, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    k_ssim_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(flt, c->f[LES_F_LM], c->f[LES_F_MM],
+                                                             c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, nl, g.nplane,
+                                                             jz0, cst, opftdelta, lagran_dt); LES_COUNT_LAUNCH();
+  }
+  return 0;
+}
+
 // std_dynamic.f90:1-136 (model 2) -> cs_z (device, nz): the 21 planes of
 // k_sd_prep G_test-filtered, then k_sd_final with beta = 1 and
 // delta = (dx dy dz)^(1/3) (std_dynamic.f90:28)
@@ -3153,6 +3255,8 @@ static int sgs_stagT(les_ctx* c) {
       if (k.model == 2) op_stddyn(c, csz, S);
       else op_scaledep(c, csz, S);
       k_bcast_levels<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_CS_OPT2], csz, g.nplane, g.nfield); LES_COUNT_LAUNCH();
+    } else if (k.model == 4) {
+      op_lagrange_ssim(c, S);
     } else if (k.model == 5) {
       lagrangeT<MX>(c);
     }

@@ -475,6 +475,8 @@ struct Oracle {
           scaledep_dynamic(ziko.data(), S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
         for (int jz = 1; jz <= nz; ++jz)
           for (size_t i = 0; i < nplane; ++i) Cs_opt2[(size_t)(jz - 1) * nplane + i] = ziko[jz - 1];
+      } else if (model == 4) {  // sgs_stag.f90:136-137
+        lagrange_Ssim(S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
       } else if (model == 5) {
         lagrange_Sdep(S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
       }
@@ -530,13 +532,18 @@ struct Oracle {
   }
 
   // interpolag_Sdep.f90:2-380 (non-MPI, read_inflow_file = .false.)
-  void interpolag_Sdep() {
+  void interpolag_Sdep() { interpolag(4, true); }
+  // interpolag_Ssim.f90:2-212: the same back-trajectory interpolation of
+  // F_LM and F_MM only, without the near-wall clip of interpolag_Sdep.f90:
+  // 285-293 (its w_lag(1) keeps 0.25 w_lag(2), doubled when positive)
+  void interpolag_Ssim() { interpolag(2, false); }
+  void interpolag(const int nf, const bool sdep_clip) {
     const int NX = nx + 2, NY = ny + 2, NZ = nz + 2;
     std::vector<double> FLM((size_t)NX * NY * NZ), FMM(FLM.size()), FQN(FLM.size()), FNN(FLM.size());
     auto FI = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)NX * ((size_t)(j - 1) + (size_t)NY * (k - 1)); };
     std::vector<double>* FF[4] = {&FLM, &FMM, &FQN, &FNN};
     Field* Fs[4] = {&F_LM, &F_MM, &F_QN, &F_NN};
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < nf; ++q) {
       std::vector<double>& A = *FF[q];
       const Field& Fq = *Fs[q];
       for (int jz = 1; jz <= nz; ++jz)
@@ -573,14 +580,15 @@ struct Oracle {
         w2 = w2 + std::min(w2, 0.0);
         w1 = w1 + std::max(w1, 0.0);
       }
-    for (size_t i = 0; i < nplane; ++i) {
-      double& w2 = w_lag[nplane + i];
-      double& w1 = w_lag[i];
-      w2 = std::min(1.0, w2);
-      w1 = std::min(1.0, w2);
-      w2 = std::max(-1.0, w2);
-      w1 = std::max(-1.0, w2);
-    }
+    if (sdep_clip)
+      for (size_t i = 0; i < nplane; ++i) {
+        double& w2 = w_lag[nplane + i];
+        double& w1 = w_lag[i];
+        w2 = std::min(1.0, w2);
+        w1 = std::min(1.0, w2);
+        w2 = std::max(-1.0, w2);
+        w1 = std::max(-1.0, w2);
+      }
     for (int jz = 1; jz <= nz; ++jz) {
       const int jjz = jz + 1;
       for (int jy = 1; jy <= ny; ++jy) {
@@ -594,7 +602,7 @@ struct Oracle {
           const int jxa = jjx + addx, jya = jjy + addy, jza = jjz + addz;
           const double comp_x = std::fabs(u_lag[i]), comp_y = std::fabs(v_lag[i]), comp_z = std::fabs(w_lag[i]);
           const double frac_x = 1.0 - comp_x, frac_y = 1.0 - comp_y, frac_z = 1.0 - comp_z;
-          for (int q = 0; q < 4; ++q) {
+          for (int q = 0; q < nf; ++q) {
             const std::vector<double>& A = *FF[q];
             (*Fs[q])[i] = frac_x * frac_y * (A[FI(jjx, jjy, jjz)] * frac_z + A[FI(jjx, jjy, jza)] * comp_z) +
                           frac_x * comp_y * (A[FI(jjx, jya, jjz)] * frac_z + A[FI(jjx, jya, jza)] * comp_z) +
@@ -610,6 +618,81 @@ struct Oracle {
   }
 
   static inline double pow_m18(double x) { return 1.0 / std::sqrt(std::sqrt(std::sqrt(x))); }
+
+  // lagrange_Ssim.f90:1-335 (model 4; inilag = .false., inflow = .false., no
+  // buildings, no level set): Beta = 1 (:126), interpolag_Ssim (:130); per
+  // level the G_test filters of std_dynamic with fourbeta = 4 Beta
+  // (:141-245), LM and MM per point (:247-248), the Lagrangian relaxation
+  // with T = 1.5 delta (F_LM F_MM)^(-1/8) over lagran_dt = cs_count dt
+  // (:286-293, x^(-1/8) as 1/sqrt(sqrt(sqrt(x)))), F_LM >= eps, Cs^2 =
+  // F_LM / F_MM, 0 on the padding columns, >= eps (:295-302); eps = 1e-32.
+  // The relaxation covers the padding columns too, where LM = MM = 0 (the
+  // test-filtered planes are zero there).
+  void lagrange_Ssim(const double* s11, const double* s12, const double* s13, const double* s22,
+                     const double* s23, const double* s33) {
+    const double eps = 1e-32;
+    const double delta = 1.0 * std::pow(dx * dy, 1.0 / 2.0);
+    const double opftdelta = 1.5 * delta;
+    std::fill(Beta.begin(), Beta.end(), 1.0);
+    interpolag_Ssim();
+    const double lagran_dt = dt * (double)cs_count;
+    const double cst = 2.0 * (delta * delta);
+#pragma omp parallel for schedule(static)
+    for (int jz = 1; jz <= nz; ++jz) {
+      const size_t NP = nplane, o = (size_t)(jz - 1) * NP;
+      std::vector<double> buf(NP * 21);
+      auto pl = [&](int q) { return buf.data() + (size_t)q * NP; };
+      for (size_t i = 0; i < NP; ++i) {
+        double ub, vb, wb;
+        if (jz == 1) {
+          ub = u[i]; vb = v[i]; wb = 0.25 * w[NP + i];
+        } else {
+          ub = 0.5 * (u[o + i] + u[o - NP + i]); vb = 0.5 * (v[o + i] + v[o - NP + i]); wb = w[o + i];
+        }
+        pl(0)[i] = ub; pl(1)[i] = vb; pl(2)[i] = wb;
+        pl(3)[i] = ub * ub; pl(4)[i] = ub * vb; pl(5)[i] = ub * wb;  // :147-152
+        pl(6)[i] = vb * vb; pl(7)[i] = vb * wb; pl(8)[i] = wb * wb;
+      }
+      const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+      for (int q = 0; q < 3; ++q) test_filter(pl(q), G_test);
+      for (int q = 0; q < 6; ++q) {
+        test_filter(pl(3 + q), G_test);
+        for (size_t i = 0; i < NP; ++i) pl(3 + q)[i] = pl(3 + q)[i] - pl(ia[q])[i] * pl(ib[q])[i];
+      }
+      const double* Sp[6] = {s11 + o, s12 + o, s13 + o, s22 + o, s23 + o, s33 + o};
+      for (size_t i = 0; i < NP; ++i) {
+        const double S = smag(Sp[0][i], Sp[3][i], Sp[5][i], Sp[1][i], Sp[2][i], Sp[4][i]);
+        for (int q = 0; q < 6; ++q) { pl(9 + q)[i] = Sp[q][i]; pl(15 + q)[i] = S * Sp[q][i]; }
+      }
+      for (int q = 0; q < 12; ++q) test_filter(pl(9 + q), G_test);
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= ld; ++jx) {
+          const size_t i = (size_t)(jx - 1) + (size_t)ld * (jy - 1);
+          double LM = 0.0, MM = 0.0;
+          if (jx <= nx) {
+            double b[6], sb[6], Lq[6], M[6];
+            for (int q = 0; q < 6; ++q) { b[q] = pl(9 + q)[i]; sb[q] = pl(15 + q)[i]; Lq[q] = pl(3 + q)[i]; }
+            const double Sb = smag(b[0], b[3], b[5], b[1], b[2], b[4]);
+            const double fourbeta = 4.0 * Beta[o + i];
+            for (int q = 0; q < 6; ++q) M[q] = cst * (sb[q] - fourbeta * Sb * b[q]);
+            LM = Lq[0] * M[0] + Lq[3] * M[3] + Lq[5] * M[5] + 2.0 * (Lq[1] * M[1] + Lq[2] * M[2] + Lq[4] * M[4]);
+            MM = M[0] * M[0] + M[3] * M[3] + M[5] * M[5] + 2.0 * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+          }
+          double& flm = F_LM[o + i];
+          double& fmm = F_MM[o + i];
+          double Tn = std::max(flm * fmm, eps);
+          Tn = opftdelta * pow_m18(Tn);
+          const double dumfac = lagran_dt / Tn;
+          const double epsi = dumfac / (1.0 + dumfac);
+          flm = epsi * LM + (1.0 - epsi) * flm;
+          fmm = epsi * MM + (1.0 - epsi) * fmm;
+          flm = std::max(eps, flm);
+          double cs = flm / fmm;
+          if (jx > nx) cs = 0.0;
+          Cs_opt2[o + i] = std::max(eps, cs);
+        }
+    }
+  }
 
   // lagrange_Sdep.f90:4-478 (inilag = .false., inflow = .false.)
   void lagrange_Sdep(const double* s11, const double* s12, const double* s13, const double* s22,
@@ -1609,6 +1692,11 @@ void lo_lagrange_sdep(void* h) {
   o->lagrange_Sdep(o->S11.data(), o->S12.data(), o->S13.data(), o->S22.data(), o->S23.data(), o->S33.data());
 }
 void lo_interpolag_sdep(void* h) { ((Oracle*)h)->interpolag_Sdep(); }
+void lo_interpolag_ssim(void* h) { ((Oracle*)h)->interpolag_Ssim(); }
+void lo_lagrange_ssim(void* h, const double* s11, const double* s12, const double* s13, const double* s22,
+                      const double* s23, const double* s33) {
+  ((Oracle*)h)->lagrange_Ssim(s11, s12, s13, s22, s23, s33);
+}
 void lo_scaledep_dynamic(void* h, double* cs_z) {
   Oracle* o = (Oracle*)h;
   o->scaledep_dynamic(cs_z, o->S11.data(), o->S12.data(), o->S13.data(), o->S22.data(), o->S23.data(), o->S33.data());

@@ -211,6 +211,49 @@ def test_step_parity_32_std_dynamic(libs):
     assert np.any(co > 0) and rel(cg, co) < 1e-9, rel(cg, co)
 
 
+def test_interpolag_ssim_routine(libs):
+    """interpolag_Ssim.f90:2-212 on the same F_LM, F_MM and lag velocities,
+    with near-wall vertical displacements beyond one cell (interpolag_Sdep
+    would clip them; interpolag_Ssim does not)."""
+    cfg = lg.make_config(32, 32, 12, model=4)
+    surf = lg.uniform_surface(cfg)
+    g, o = pair(cfg, surf, seed=8)
+    rng = np.random.default_rng(8)
+    shp = lg.field_shape(cfg, "u")
+    f = {"F_LM": rng.uniform(0.1, 1.0, shp), "F_MM": rng.uniform(0.1, 1.0, shp),
+         "u_lag": rng.uniform(-2.0, 2.0, shp), "v_lag": rng.uniform(-2.0, 2.0, shp),
+         "w_lag": rng.uniform(-2.0, 2.0, shp)}
+    f["w_lag"][1] *= 4000.0  # level 2: |displacement| above 1 near the wall
+    for k, v in f.items():
+        g.set(k, v)
+        o.set(k, v)
+    g.call("interpolag_ssim")
+    o.call("interpolag_ssim")
+    for k in ("F_LM", "F_MM"):
+        e = rel(interior(cfg, g.get(k), slice(None)), interior(cfg, o.get(k), slice(None)))
+        assert e < 1e-14, (k, e)
+
+
+def test_step_parity_32_lagrange_ssim(libs):
+    """model = 4 (Lagrangian scale-invariant, lagrange_Ssim.f90): 10 steps
+    with active theta; F_LM, F_MM are relaxed along trajectories at steps 5
+    and 10 and Cs^2 = F_LM / F_MM feeds back."""
+    cfg = lg.make_config(32, s_flag=1, jt_total0=500, model=4, rmsdiv_every=1)
+    surf = lg.striped_surface(cfg)
+    g, o = pair(cfg, surf)
+    g.step(10)
+    assert o.step(10) == 0
+    for nm in ["u", "v", "theta"]:
+        e = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
+        assert e < TOL, (nm, e)
+    e = rel(interior(cfg, g.get("w"), slice(None)), interior(cfg, o.get("w"), slice(None)))
+    assert e < TOL, ("w", e)
+    for nm in ["Cs_opt2", "F_LM", "F_MM"]:
+        a, b = interior(cfg, g.get(nm), slice(None)), interior(cfg, o.get(nm), slice(None))
+        assert np.any(b > 1e-20) and rel(a, b) < 1e-10, (nm, rel(a, b))
+    assert np.all(g.get("Beta") == 1.0)
+
+
 def test_step_parity_128_theta(libs):
     """128^3, active theta, striped z0 and heat flux; 20 steps."""
     from oracle.oracle import Oracle

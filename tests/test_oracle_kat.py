@@ -314,3 +314,28 @@ def test_std_dynamic_galilean_invariance(O):
     v2[:, :, :16] -= 0.3
     b = _std_dynamic(O, u2, v2, w, S, nz)
     assert rel(b, a) < 1e-10, (a, b)
+
+
+@pytest.mark.parametrize("shift", [0, 1])
+def test_interpolag_ssim_shifts_by_whole_cells(O, shift):
+    """interpolag_Ssim.f90: a uniform accumulated u_lag of shift * cs_count *
+    dx / (cs_count dt) moves F_LM, F_MM back by `shift` cells in x
+    (periodic), exactly; the lag arrays are reset afterwards."""
+    cfg = C.make_config(16, 16, 8, model=4)
+    d = C.dims(cfg)
+    o = O(cfg)
+    rng = np.random.default_rng(2)
+    shp = (cfg.nz, cfg.ny, d["ld"])
+    flm, fmm = rng.uniform(0.1, 1.0, shp), rng.uniform(0.1, 1.0, shp)
+    o.set("F_LM", flm); o.set("F_MM", fmm)
+    dx = 2 * np.pi / cfg.nx
+    ul = np.zeros(shp)
+    ul[:, :, :cfg.nx] = shift * dx / cfg.dt  # sum over cs_count steps of u: displacement -u dt / dx
+    o.set("u_lag", ul); o.set("v_lag", np.zeros(shp)); o.set("w_lag", np.zeros(shp))
+    o.call("interpolag_ssim")
+    n = cfg.nx
+    want_lm = np.roll(flm[:, :, :n], shift, axis=2)
+    want_mm = np.roll(fmm[:, :, :n], shift, axis=2)
+    assert np.allclose(o.get("F_LM")[:, :, :n], want_lm, rtol=0, atol=1e-15)
+    assert np.allclose(o.get("F_MM")[:, :, :n], want_mm, rtol=0, atol=1e-15)
+    assert not o.get("u_lag").any()
