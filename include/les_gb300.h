@@ -295,8 +295,8 @@ int les_lagrange_sdep(les_ctx* ctx, const double* S11, const double* S12, const 
                       const double* S22, const double* S23, const double* S33);
 /* interpolag_Sdep.f90:2-380 on the context's F_* and u/v/w_lag. */
 int les_interpolag_sdep(les_ctx* ctx);
-/* lagrange_Ssim.f90:1-335 (model 4, calls interpolag_Ssim) with S_ij
- * (ld,ny,nz); interpolag_Ssim.f90:2-212 on the context's F_LM, F_MM and
+/* lagrange_Ssim.f90:5-335 (model 4, calls interpolag_Ssim) with S_ij
+ * (ld,ny,nz); interpolag_Ssim.f90:3-316 on the context's F_LM, F_MM and
  * u/v/w_lag. */
 int les_lagrange_ssim(les_ctx* ctx, const double* S11, const double* S12, const double* S13,
                       const double* S22, const double* S23, const double* S33);

@@ -1050,7 +1050,7 @@ __device__ __forceinline__ double lag_disp_u(const double* ul, size_t i, size_t 
   return -ua * dt * cs / dxx;
 }
 // NF: F_* fields carried (4: interpolag_Sdep, 2: interpolag_Ssim, which
-// also lacks the near-wall clip of :285-293, so its level 1 keeps
+// also lacks the near-wall clip of interpolag_Sdep.f90:290-293, so its level 1 keeps
 // 0.25 w_lag(2), doubled when positive).
 template <int NF, bool SDEP>
 __global__ void k_interpolag(const double* __restrict__ ul, const double* __restrict__ vl,
@@ -1200,7 +1200,7 @@ static int op_interpolag32(les_ctx* c) {
   return 0;
 }
 int op_interpolag(les_ctx* c) { return op_interpolag_n(c, 4); }
-// nf = 4: interpolag_Sdep.f90:2-380; nf = 2: interpolag_Ssim.f90:2-212
+// nf = 4: interpolag_Sdep.f90:2-380; nf = 2: interpolag_Ssim.f90:3-316
 int op_interpolag_n(les_ctx* c, int nf) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
@@ -1533,7 +1533,7 @@ __global__ void __launch_bounds__(256) k_sd_final(const double* __restrict__ flt
   }
   if (threadIdx.x == 0) cs_z[jz - 1] = fmax(0.0, sn[0] / sd[0]);
 }
-// lagrange_Ssim.f90:247-302 (model 4) on one chunk of levels: L_ij and M_ij
+// lagrange_Ssim.f90:140-269 (model 4) on one chunk of levels: L_ij and M_ij
 // (fourbeta = 4 Beta = 4) from the 21 G_test-filtered planes, LM and MM per
 // point, the Lagrangian relaxation of F_LM, F_MM and Cs^2 = F_LM / F_MM.
 // Every column of (ld,ny) is relaxed as the reference does; LM = MM = 0 on
@@ -1541,7 +1541,7 @@ __global__ void __launch_bounds__(256) k_sd_final(const double* __restrict__ flt
 __global__ void k_ssim_final(const double* __restrict__ flt, double* F_LM, double* F_MM, double* Cs,
                              int ld, int nx, int ny, int nlev, size_t np, int jz0, double cst, double opftdelta,
                              double lagran_dt) {
-  const double eps = 1e-32;  // lagrange_Ssim.f90:20
+  const double eps = 1e-32;  // lagrange_Ssim.f90:25
   const size_t st = np * nlev;
   GSTRIDE(t, st) {
     const int lc = (int)(t / np);
@@ -1574,7 +1574,7 @@ __global__ void k_ssim_final(const double* __restrict__ flt, double* F_LM, doubl
     Cs[i] = fmax(eps, jx < nx ? flm / fmm : 0.0);
   }
 }
-// lagrange_Ssim.f90:1-335 (model 4): Beta = 1, interpolag_Ssim, then per
+// lagrange_Ssim.f90:5-335 (model 4): Beta = 1, interpolag_Ssim, then per
 // chunk of levels the 21 planes of k_sd_prep G_test-filtered and the
 // relaxation of k_ssim_final
 int op_lagrange_ssim(les_ctx* c, const double* const* S) {

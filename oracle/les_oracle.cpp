@@ -20,13 +20,15 @@
 //
 // Deliberate, documented deviations (all at the rounding level or in values
 // nothing reads):
-//  * x**(-1/8) in lagrange_Sdep.f90:324,365 is evaluated as
-//    1/sqrt(sqrt(sqrt(x))) (correctly rounded operations only), so that CPU
-//    and GPU see identical bits before the FP32 truncation that follows.
+//  * x**(-1/8) in lagrange_Sdep.f90:324,365 and lagrange_Ssim.f90:259 is
+//    evaluated as 1/sqrt(sqrt(sqrt(x))) (correctly rounded operations only),
+//    so that CPU and GPU see identical bits before the FP32 truncation that
+//    follows in lagrange_Sdep.
 //  * the padding columns ld-1:ld hold zeros after a complex-to-real transform
-//    (FFTW leaves unspecified values there); nothing on the path reads them
-//    except scaledep_dynamic's plane sums (scaledep_dynamic.f90:187-243),
-//    which are taken over 1:nx here.
+//    (FFTW leaves unspecified values there); what reads them: the plane sums
+//    of scaledep_dynamic (scaledep_dynamic.f90:187-243) and std_dynamic
+//    (std_dynamic.f90:130-132), taken over 1:nx here, and lagrange_Ssim's
+//    relaxation of the padding columns (LM = MM = 0 there).
 //  * scaledep_dynamic is called with its own 7-argument interface; the
 //    reference's call site (sgs_stag.f90:132) passes 10 arguments.
 //  * surface inputs are given nondimensional (zo) and kinematic (wt_s [K m/s])
@@ -533,9 +535,9 @@ struct Oracle {
 
   // interpolag_Sdep.f90:2-380 (non-MPI, read_inflow_file = .false.)
   void interpolag_Sdep() { interpolag(4, true); }
-  // interpolag_Ssim.f90:2-212: the same back-trajectory interpolation of
+  // interpolag_Ssim.f90:3-316: the same back-trajectory interpolation of
   // F_LM and F_MM only, without the near-wall clip of interpolag_Sdep.f90:
-  // 285-293 (its w_lag(1) keeps 0.25 w_lag(2), doubled when positive)
+  // 290-293 (its w_lag(1) keeps 0.25 w_lag(2), doubled when positive)
   void interpolag_Ssim() { interpolag(2, false); }
   void interpolag(const int nf, const bool sdep_clip) {
     const int NX = nx + 2, NY = ny + 2, NZ = nz + 2;
@@ -619,13 +621,14 @@ struct Oracle {
 
   static inline double pow_m18(double x) { return 1.0 / std::sqrt(std::sqrt(std::sqrt(x))); }
 
-  // lagrange_Ssim.f90:1-335 (model 4; inilag = .false., inflow = .false., no
-  // buildings, no level set): Beta = 1 (:126), interpolag_Ssim (:130); per
+  // lagrange_Ssim.f90:5-335 (model 4; inilag = .false., inflow = .false., no
+  // buildings, no level set): Beta = 1 (:122), interpolag_Ssim (:126); per
   // level the G_test filters of std_dynamic with fourbeta = 4 Beta
-  // (:141-245), LM and MM per point (:247-248), the Lagrangian relaxation
+  // (:140-219), LM and MM per point (:221-222), the Lagrangian relaxation
   // with T = 1.5 delta (F_LM F_MM)^(-1/8) over lagran_dt = cs_count dt
-  // (:286-293, x^(-1/8) as 1/sqrt(sqrt(sqrt(x)))), F_LM >= eps, Cs^2 =
-  // F_LM / F_MM, 0 on the padding columns, >= eps (:295-302); eps = 1e-32.
+  // (:258-264, x^(-1/8) as 1/sqrt(sqrt(sqrt(x)))), F_LM >= eps (:265),
+  // Cs^2 = F_LM / F_MM, 0 on the padding columns, >= eps (:267-269);
+  // eps = 1e-32 (:25).
   // The relaxation covers the padding columns too, where LM = MM = 0 (the
   // test-filtered planes are zero there).
   void lagrange_Ssim(const double* s11, const double* s12, const double* s13, const double* s22,
@@ -650,7 +653,7 @@ struct Oracle {
           ub = 0.5 * (u[o + i] + u[o - NP + i]); vb = 0.5 * (v[o + i] + v[o - NP + i]); wb = w[o + i];
         }
         pl(0)[i] = ub; pl(1)[i] = vb; pl(2)[i] = wb;
-        pl(3)[i] = ub * ub; pl(4)[i] = ub * vb; pl(5)[i] = ub * wb;  // :147-152
+        pl(3)[i] = ub * ub; pl(4)[i] = ub * vb; pl(5)[i] = ub * wb;  // :154-159
         pl(6)[i] = vb * vb; pl(7)[i] = vb * wb; pl(8)[i] = wb * wb;
       }
       const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};

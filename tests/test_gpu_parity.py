@@ -212,7 +212,7 @@ def test_step_parity_32_std_dynamic(libs):
 
 
 def test_interpolag_ssim_routine(libs):
-    """interpolag_Ssim.f90:2-212 on the same F_LM, F_MM and lag velocities,
+    """interpolag_Ssim.f90:3-316 on the same F_LM, F_MM and lag velocities,
     with near-wall vertical displacements beyond one cell (interpolag_Sdep
     would clip them; interpolag_Ssim does not)."""
     cfg = lg.make_config(32, 32, 12, model=4)
