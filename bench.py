@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--steps", type=int, default=10)  # multiple of cs_count (5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
+    p.add_argument("--model", type=int, default=5, choices=[5, 4, 3, 2],
+                   help="SGS model of the FP64 step (5 Lagrangian scale-dependent, 4 scale-invariant, "
+                        "3 plane-averaged scale-dependent, 2 standard dynamic)")
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--grid", type=int, default=256)
     p.add_argument("--levels", type=int, default=None,
@@ -135,17 +138,19 @@ class ClockSampler:
 
 
 LEVELS = None  # --levels: uvp levels when not the grid size (small profiling captures)
+MODEL = 5  # --model: SGS model of the FP64 step (the mixed form runs model 5)
+MODEL_NAME = {5: "lagrangian-sdep", 4: "lagrangian-ssim", 3: "plane-sdep", 2: "std-dynamic"}
 
 
 def workload_config(lg, grid, form):
     cfg = lg.make_config(grid, nz_levels=LEVELS, s_flag=1, precision=1 if form == "mixed" else 0,
-                         rmsdiv_every=0)
+                         rmsdiv_every=0, model=5 if form == "mixed" else MODEL)
     surf = lg.striped_surface(cfg)
     return cfg, surf
 
 
 def workload_name(cfg):
-    return "les %dx%dx%d theta striped-surface lagrangian-sdep" % (cfg.nx, cfg.ny, cfg.nz - 1)
+    return "les %dx%dx%d theta striped-surface %s" % (cfg.nx, cfg.ny, cfg.nz - 1, MODEL_NAME[cfg.model])
 
 
 def oracle_build():
@@ -238,9 +243,12 @@ def timed_steps(torch, lg, ctx, steps, prof_family=None):
 
 
 def main():
-    global LEVELS
+    global LEVELS, MODEL
     args = parse()
     LEVELS = args.levels
+    MODEL = args.model
+    if args.form == "mixed" and MODEL != 5:
+        raise SystemExit("--model: the FP32-mixed form runs model 5; use --form fp64")
     if args.impl == "reference":
         run_reference(args)
         return
