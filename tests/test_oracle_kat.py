@@ -316,26 +316,32 @@ def test_std_dynamic_galilean_invariance(O):
     assert rel(b, a) < 1e-10, (a, b)
 
 
-@pytest.mark.parametrize("shift", [0, 1])
-def test_interpolag_ssim_shifts_by_whole_cells(O, shift):
-    """interpolag_Ssim.f90: a uniform accumulated u_lag of shift * cs_count *
-    dx / (cs_count dt) moves F_LM, F_MM back by `shift` cells in x
-    (periodic), exactly; the lag arrays are reset afterwards."""
-    cfg = C.make_config(16, 16, 8, model=4)
+@pytest.mark.parametrize("routine,fields", [("interpolag_ssim", ("F_LM", "F_MM")),
+                                            ("interpolag_sdep", ("F_LM", "F_MM", "F_QN", "F_NN"))])
+@pytest.mark.parametrize("axis,shift", [(2, 0), (2, 1), (2, -1), (1, 1), (1, -1)])
+def test_interpolag_shifts_by_whole_cells(O, routine, fields, axis, shift):
+    """interpolag_Ssim.f90 / interpolag_Sdep.f90: a uniform accumulated lag
+    velocity of shift * dx / dt (x) or shift * dy / dt (y) gives a
+    displacement of exactly -shift cells, so every F_* comes back shifted by
+    `shift` cells (periodic) with frac = 0, comp = 1; the lag arrays are
+    reset afterwards."""
+    cfg = C.make_config(16, 16, 8, model=4 if routine == "interpolag_ssim" else 5)
     d = C.dims(cfg)
     o = O(cfg)
     rng = np.random.default_rng(2)
     shp = (cfg.nz, cfg.ny, d["ld"])
-    flm, fmm = rng.uniform(0.1, 1.0, shp), rng.uniform(0.1, 1.0, shp)
-    o.set("F_LM", flm); o.set("F_MM", fmm)
-    dx = 2 * np.pi / cfg.nx
-    ul = np.zeros(shp)
-    ul[:, :, :cfg.nx] = shift * dx / cfg.dt  # sum over cs_count steps of u: displacement -u dt / dx
-    o.set("u_lag", ul); o.set("v_lag", np.zeros(shp)); o.set("w_lag", np.zeros(shp))
-    o.call("interpolag_ssim")
+    F = {f: rng.uniform(0.1, 1.0, shp) for f in fields}
+    for f, v in F.items():
+        o.set(f, v)
+    h = 2 * np.pi / cfg.nx  # dx = dy on the 2pi x 2pi box with nx = ny
+    lag = np.zeros(shp)
+    lag[:, :, :cfg.nx] = shift * h / cfg.dt  # sum over cs_count steps: displacement -lag dt / dx
+    o.set("u_lag", lag if axis == 2 else np.zeros(shp))
+    o.set("v_lag", lag if axis == 1 else np.zeros(shp))
+    o.set("w_lag", np.zeros(shp))
+    o.call(routine)
     n = cfg.nx
-    want_lm = np.roll(flm[:, :, :n], shift, axis=2)
-    want_mm = np.roll(fmm[:, :, :n], shift, axis=2)
-    assert np.allclose(o.get("F_LM")[:, :, :n], want_lm, rtol=0, atol=1e-15)
-    assert np.allclose(o.get("F_MM")[:, :, :n], want_mm, rtol=0, atol=1e-15)
-    assert not o.get("u_lag").any()
+    for f, v in F.items():
+        want = np.roll(v[:, :, :n], shift, axis=axis)
+        assert np.allclose(o.get(f)[:, :, :n], want, rtol=0, atol=1e-15), f
+    assert not o.get("u_lag").any() and not o.get("v_lag").any()
