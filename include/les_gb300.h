@@ -158,7 +158,9 @@ int les_get_counters(les_ctx* ctx, int* jt, int* jt_total);
  * without scalars u, v, w, RHSx, RHSy, RHSz, Cs_opt2, F_LM, F_MM, F_QN, F_NN.
  * Arrays this build does not carry are written as a model-5 run of the
  * reference holds them (qmix, RHS_q, sgs_q3 and G_* zero, Pr_t = Pr) and
- * skipped on reading.  The record keeps no step counters (the reference keeps
+ * skipped on reading.  les_checkpoint_read takes only a record of exactly
+ * its configuration's list (returning LES_ERR_IO, with no field changed,
+ * for any other length).  The record keeps no step counters (the reference keeps
  * jt_total in total_time.dat): a restart creates its context with
  * jt_total0 = the steps taken, initu = 1 and initsc = 1, then reads the file.
  * Record format: gfortran / Intel Fortran unformatted sequential, 4-byte

@@ -259,6 +259,17 @@ int les_checkpoint_read(les_ctx* c, const char* path) {
   if (!little_endian()) { les_set_error("record files are little-endian; this host is not"); return LES_ERR_UNSUPPORTED; }
   const les::Grid& g = c->g;
   const std::vector<Item> items = record_items(c);
+  // the record must hold exactly this configuration's list (a record written
+  // with scalars does not read into a context without them, nor the other
+  // way round); checked before any field changes
+  long long total = 0, rec = 0;
+  for (const Item& it : items) total += (long long)item_elems(c, it) * 8;
+  if (int st0 = les_fortran_record_read(path, 0, nullptr, nullptr, 0, &rec, nullptr)) return st0;
+  if (rec != total) {
+    les_set_error("%s: the record holds %lld bytes, the checkpoint list of this configuration %lld", path, rec,
+                  total);
+    return LES_ERR_IO;
+  }
   std::vector<double> buf((size_t)g.ld * g.ny * g.nz), sfc((size_t)g.nx * g.ny);
   FILE* fp = fopen(path, "rb");
   if (!fp) { les_set_error("cannot open %s for reading", path); return LES_ERR_IO; }

@@ -52,6 +52,17 @@ def test_prefix_read_skips_the_rest(gpu_lib, tmp_path):
     assert bytes(bufs[0]) == b"tail"
 
 
+def test_length_only_read(gpu_lib, tmp_path):
+    # no buffers: the record's length and the next offset (how the checkpoint
+    # reader checks a file before changing any field)
+    p = str(tmp_path / "l.bin")
+    open(p, "wb").write(fr.write_record(b"x" * 700, 256) + fr.write_record(b"yz", 256))
+    bufs, ln, nxt = gpu_lib.fortran_record_read(p, [])
+    assert bufs == [] and ln == 700 and nxt == 700 + 3 * 8
+    _, ln2, nxt2 = gpu_lib.fortran_record_read(p, [], offset=nxt)
+    assert ln2 == 2 and nxt2 == 700 + 3 * 8 + 2 + 8
+
+
 def test_appending_writer(gpu_lib, tmp_path):
     p = str(tmp_path / "a.bin")
     a, b = _data(100, 1), _data(50, 2)

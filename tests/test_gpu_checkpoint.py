@@ -87,3 +87,18 @@ def test_checkpoint_read_rejects_a_short_record(gpu_lib, tmp_path):
         a.checkpoint_read(p)
     assert e.value.code == -10
     a.close()
+
+
+def test_checkpoint_read_refuses_the_other_layout(gpu_lib, tmp_path):
+    """A record written without scalars does not read into a context with
+    them (the lists differ in length); nothing in the context changes."""
+    _, a = member(32, 0)
+    p = str(tmp_path / "vel.out")
+    a.checkpoint_write(p)
+    _, b = member(32, 1)
+    u0, th0 = b.get("u"), b.get("theta")
+    with pytest.raises(lg.LesError) as e:
+        b.checkpoint_read(p)
+    assert e.value.code == -10
+    assert np.array_equal(b.get("u"), u0) and np.array_equal(b.get("theta"), th0)
+    a.close(); b.close()
