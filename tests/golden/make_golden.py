@@ -1,8 +1,9 @@
 """Generates tests/golden/*.npz: oracle (CPU restatement of the reference
-step) outputs on small seeded cases, used as regression pins by
-tests/test_golden.py and as fixed inputs/outputs for the GPU parity tests.
+step) outputs on small seeded cases (SGS models 5, 2 and 4), used as
+regression pins of the oracle by tests/test_golden.py.
 
-  python tests/golden/make_golden.py
+  python tests/golden/make_golden.py            # every case
+  python tests/golden/make_golden.py NAME ...   # the named cases
 """
 import os
 import sys
@@ -21,6 +22,8 @@ CASES = {
     "neutral_16_jt0": (16, 8, 0, 0, 5, 10, "uniform"),
     "theta_16_dyn": (16, 8, 1, 500, 5, 10, "striped"),
     "theta_24_dyn": (24, 12, 1, 500, 5, 6, "striped"),
+    "theta_16_std": (16, 8, 1, 500, 2, 10, "striped"),   # std_dynamic
+    "theta_16_ssim": (16, 8, 1, 500, 4, 10, "striped"),  # lagrange_Ssim
 }
 FIELDS = ["u", "v", "w", "theta", "Cs_opt2", "F_LM", "F_MM", "p", "RHSx", "Nu_t"]
 
@@ -41,7 +44,7 @@ def run(name):
 
 if __name__ == "__main__":
     build()
-    for name in CASES:
+    for name in (sys.argv[1:] or CASES):
         cfg, out = run(name)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, {k: v.shape for k, v in out.items()})

@@ -10,7 +10,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 
 
-@pytest.mark.parametrize("name", ["neutral_16_jt0", "theta_16_dyn", "theta_24_dyn"])
+@pytest.mark.parametrize("name", ["neutral_16_jt0", "theta_16_dyn", "theta_24_dyn", "theta_16_std",
+                                  "theta_16_ssim"])
 def test_oracle_reproduces_golden(oracle_lib, name):
     import make_golden as mg
     ref = np.load(os.path.join(HERE, "golden", name + ".npz"))
