@@ -110,15 +110,20 @@ extern "C" int les_tridag_array_noalloc(const double* a, const double* b, const 
   double* gam = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kFlagBytes);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
+  // Row 1 is checked before the solve is launched, as tridag_array.f90:32-39
+  // stops before writing u: on that error u is left as the caller passed it.
   LES_CUDA_CHECK(cudaMemsetAsync(flag, 0, sizeof(int), s));
   const int nk = lh * ny;
   k_first_pivot<<<(nk + 127) / 128, 128, 0, s>>>(b, lh, ny, flag); LES_COUNT_LAUNCH();
-  les::launch_tridag_generic(a, b, c, r, u, gam, lh, ny, n, flag, s);
   int fl = 0;
   LES_CUDA_CHECK(cudaMemcpyAsync(&fl, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
   LES_CUDA_CHECK(cudaStreamSynchronize(s));
   LES_CUDA_CHECK(cudaGetLastError());
   if (fl & 2) { les_set_error("tridag_array_noalloc: rewrite eqs, zero b in row 1"); return LES_ERR_PIVOT; }
+  les::launch_tridag_generic(a, b, c, r, u, gam, lh, ny, n, flag, s);
+  LES_CUDA_CHECK(cudaMemcpyAsync(&fl, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LES_CUDA_CHECK(cudaStreamSynchronize(s));
+  LES_CUDA_CHECK(cudaGetLastError());
   if (fl) { les_set_error("tridag_array_noalloc failed: zero pivot"); return LES_ERR_PIVOT; }
   return LES_OK;
 }
