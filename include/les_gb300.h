@@ -146,6 +146,21 @@ int les_sync_to_host(les_ctx* ctx);
 /* Step counters (param.f90:147-148). */
 int les_get_counters(les_ctx* ctx, int* jt, int* jt_total);
 
+/* Whole-member state image, for a server that evicts a member from the
+ * device and resumes it later: every module array in its device storage
+ * (the FP32-held fields of a precision-1 context as they are) plus the step
+ * counters, behind a header naming the configuration.  A context created
+ * with the same configuration and surface and restored from the image
+ * continues bit for bit as the saved one would have.  les_state_save fills a
+ * host buffer of at least les_state_bytes bytes (pinned memory copies
+ * fastest) and waits for the copies; les_state_restore refuses an image of
+ * another configuration (LES_ERR_ARG).  No counterpart in the reference (its
+ * restart record, les_checkpoint_write, keeps the arrays of io.f90:1314-1338
+ * only, and a restart from it starts the Lagrangian sums and counters anew). */
+size_t les_state_bytes(const les_ctx* ctx);
+int les_state_save(les_ctx* ctx, void* host, size_t bytes);
+int les_state_restore(les_ctx* ctx, const void* host, size_t bytes);
+
 /* ---- checkpoint record ----------------------------------------------------- */
 /* io.f90:1314-1338 `checkpoint` (written by output_final, io.f90:1347-1383,
  * and into output/vel_scNNNNNN.out, io.f90:223-233) and its reader
@@ -270,11 +285,16 @@ int les_tridag_array(les_ctx* ctx, const double* a, const double* b, const doubl
  * a fixed scratch array compiled into the library, held on every GPU that
  * loads it until the process exits: lh*ny*n <= LES_NOALLOC_TRIDAG_MAX_ELEMS
  * (2^21, 16 MiB of doubles), larger sizes return LES_ERR_ARG.  The first call
- * on each device looks up that array's address; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other
- * streams or host threads on the same device) race; serialise them.  Runs
- * on `stream` (a cudaStream_t, 0 for the default stream) and waits for it
- * to finish, to report a zero pivot as LES_ERR_PIVOT. */
+ * on each device looks up that array's address.  All calls share the array:
+ * calls that overlap on the GPU (other streams or host threads on the same
+ * device) race; serialise them.  Runs on `stream` (a cudaStream_t, 0 for the
+ * default stream) and synchronises that stream on every call (twice: after
+ * the row-1 pivot check and after the solve) to report a zero pivot as
+ * LES_ERR_PIVOT, so it cannot be called inside stream capture or a CUDA
+ * graph.  A zero b in row 1 returns LES_ERR_PIVOT before the solve runs and
+ * leaves u as passed; modes the solve skips (kx = lh-1, ky = ny/2, and the
+ * (0,0) mode beyond row 1) keep the caller's values beyond row 1, as
+ * tridag_array.f90 leaves them. */
 #define LES_NOALLOC_TRIDAG_MAX_ELEMS (1u << 21)
 int les_tridag_array_noalloc(const double* a, const double* b, const double* c, const double* r,
                              double* u, int lh, int ny, int n, void* stream);

@@ -182,6 +182,27 @@ class Context:
     def set_pointer_mode(self, device):
         check(self.L.les_ctx_set_pointer_mode(self.h, 1 if device else 0))
 
+    # --- whole-state image (serving: spill and resume) ------------------------
+    def state_bytes(self):
+        f = self.L.les_state_bytes
+        f.restype = ctypes.c_size_t
+        f.argtypes = [ctypes.c_void_p]
+        return int(f(self.h))
+
+    def state_save(self, buf):
+        """Whole member state into `buf` (a uint8 numpy array of at least
+        state_bytes() bytes, pinned memory copies fastest)."""
+        f = self.L.les_state_save
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        check(f(self.h, ctypes.c_void_p(buf.ctypes.data), ctypes.c_size_t(buf.nbytes)))
+
+    def state_restore(self, buf):
+        f = self.L.les_state_restore
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        check(f(self.h, ctypes.c_void_p(buf.ctypes.data), ctypes.c_size_t(buf.nbytes)))
+
     # --- checkpoint record (io.f90:1314-1338, initial.f90:54-160) ------------
     def checkpoint_write(self, path):
         check(self.L.les_checkpoint_write(self.h, os.fsencode(path)))

@@ -424,7 +424,8 @@ enum ColCoef {
   CC_IKY = 5,     // x i ky         (ddy.f90:183)
   CC_KILL = 6,    // copy with the Nyquist row/column zeroed (filt_da.f90:114-115)
   CC_MASK = 7,    // G_test / (1/(nx*ny)): pass where G_test != 0 (input already scaled)
-  CC_MASK4 = 8    // G_test_test / (1/(nx*ny))
+  CC_MASK4 = 8,   // G_test_test / (1/(nx*ny))
+  CC_MIKY = 9     // x (-i ky): with CC_IKX on a second input, the vertical vorticity dv/dx - du/dy
 };
 enum ColMap { MAP_SAME = 0, MAP_PAD = 1, MAP_UNPAD = 2 };
 enum ColDir { DIR_FWD = 1, DIR_INV = 2, DIR_BOTH = 3 };

@@ -38,6 +38,16 @@ template <> struct Tab<float> {
   static __device__ __forceinline__ float GG(const ColJob& J, size_t i) { return J.GGf[i]; }
 };
 
+// x f - off(plane) rounded to the transform precision: an FP64 input is
+// shifted in FP64 before rounding (the mean leaves FP32 transforms of u, v,
+// w, theta with the fluctuation's precision); an FP32 input is shifted by the
+// plane constant rounded to FP32 (the derivatives of a plane constant are
+// zero, so any constant near the mean serves), with no FP64 arithmetic.
+template <typename T, typename TIn> __device__ __forceinline__ T sub_off(TIn x, double off) {
+  if constexpr (std::is_same<TIn, float>::value) return cvt<T, float>(x - cvt_d2f(off));
+  else return cvt<T, double>(cvt<double, TIn>(x) - off);
+}
+
 // ---------------------------------------------------------------------------
 // rows_r2c: x-transform of `rpc` rows per CTA.  grid = (ceil(ny/rpc), nlev, nfield)
 // NF > 0: the half length m = nx/2 is NF at compile time (fixed-length
@@ -69,9 +79,9 @@ __global__ void __launch_bounds__(256) k_rows_r2c(RowJob J, RealPlanDev P, int r
     // the pair (2k, 2k+1) in one access: rows start on even offsets
     const typename CT<TIn>::type pr = reinterpret_cast<const typename CT<TIn>::type*>(row)[k];
     T a, b;
-    if (J.off[f]) {  // subtract in double before rounding to T
-      a = cvt<T, double>(cvt<double, TIn>(pr.x) - off);
-      b = cvt<T, double>(cvt<double, TIn>(pr.y) - off);
+    if (J.off[f]) {
+      a = sub_off<T, TIn>(pr.x, off);
+      b = sub_off<T, TIn>(pr.y, off);
     } else {
       a = cvt<T, TIn>(pr.x);
       b = cvt<T, TIn>(pr.y);
@@ -208,9 +218,9 @@ __global__ void __launch_bounds__(NT) k_r2c_reg(RowJob J, RealPlanDev P) {
       if (rowok) {
         const CI pr = src[N1 * i];
         T a, b;
-        if (hasoff) {  // subtract in double before rounding to T
-          a = cvt<T, double>(cvt<double, TIn>(pr.x) - off);
-          b = cvt<T, double>(cvt<double, TIn>(pr.y) - off);
+        if (hasoff) {
+          a = sub_off<T, TIn>(pr.x, off);
+          b = sub_off<T, TIn>(pr.y, off);
         } else {
           a = cvt<T, TIn>(pr.x);
           b = cvt<T, TIn>(pr.y);
@@ -375,9 +385,9 @@ __global__ void __launch_bounds__(NT) k_r2c_reg2(RowJob J, RealPlanDev P) {
       if (rowok) {
         const CI pr = src[q + TT * j + N1 * i];
         T a, b;
-        if (hasoff) {  // subtract in double before rounding to T
-          a = cvt<T, double>(cvt<double, TIn>(pr.x) - off);
-          b = cvt<T, double>(cvt<double, TIn>(pr.y) - off);
+        if (hasoff) {
+          a = sub_off<T, TIn>(pr.x, off);
+          b = sub_off<T, TIn>(pr.y, off);
         } else {
           a = cvt<T, TIn>(pr.x);
           b = cvt<T, TIn>(pr.y);
@@ -530,6 +540,7 @@ __device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT
     case CC_GG: return cscale(v, Tab<T>::GG(J, ki));
     case CC_IKX: return ik(v, Tab<T>::kx(J, ki));
     case CC_IKY: return ik(v, Tab<T>::ky(J, ki));
+    case CC_MIKY: return ik(v, -Tab<T>::ky(J, ki));
     case CC_KILL: {
       const int lhm1 = J.lh - 1;
       if (jx == lhm1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
@@ -635,6 +646,7 @@ __device__ __forceinline__ typename CT<T>::type apply_coef_ct(typename CT<T>::ty
   else if constexpr (CODE == CC_GG) return cscale(v, Tab<T>::GG(J, ki));
   else if constexpr (CODE == CC_IKX) return ik(v, Tab<T>::kx(J, ki));
   else if constexpr (CODE == CC_IKY) return ik(v, Tab<T>::ky(J, ki));
+  else if constexpr (CODE == CC_MIKY) return ik(v, -Tab<T>::ky(J, ki));
   else if constexpr (CODE == CC_KILL) {
     if (jx == J.lh - 1 || js == J.ny_small / 2) return mk<T>((T)0, (T)0);
     return v;

@@ -202,7 +202,7 @@ static Sizes sizes_of(const Grid& g) {
   // saved spectra, wall-plane spectra, Thomas tables, reductions, wavenumber
   // and filter tables (FP64 + FP32)
   s.aux = 4 * nz * C * sizeof(double2) + 4 * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double) +
-          (28 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float) +
+          (36 * (nz + 8) + 64) * sizeof(double) + 5 * C * sizeof(double) + 4 * C * sizeof(float) +
           2 * C * sizeof(float2);
   return s;
 }
@@ -259,7 +259,9 @@ size_t les_estimate_device_bytes(const les_config* cfg) {
   Grid g;
   grid_of(*cfg, g);
   Sizes s = sizes_of(g);
-  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + (1u << 20);
+  size_t mixed = 0;  // float-float Thomas tables of the FP32-mixed form
+  if (cfg->precision == 1) mixed = 2 * (size_t)(g.nz + 1) * g.C * sizeof(float2) + 64 * sizeof(int);
+  return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + mixed + (1u << 20);
 }
 
 int les_ctx_create(const les_config* cfg, les_ctx** out) {
@@ -360,12 +362,19 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   if ((st = dalloc(c, &c->wsA, s.wsA)) || (st = dalloc(c, &c->wsB, s.wsB)) || (st = dalloc(c, &c->wsP, s.wsP)) ||
       (st = dalloc(c, (void**)&c->big, s.big)) || (st = dalloc(c, (void**)&c->tmp, s.tmp)) ||
       (st = dalloc(c, (void**)&c->spare, s.spare)) || (st = dalloc(c, (void**)&c->dscal, 64 * sizeof(double))) ||
-      (st = dalloc(c, (void**)&c->dred, 28 * (size_t)(g.nz + 8) * sizeof(double))) ||
+      (st = dalloc(c, (void**)&c->dred, 36 * (size_t)(g.nz + 8) * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->spec, 4 * (size_t)g.nz * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->wspec, 4 * g.C * sizeof(double2))) ||
       (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->gamt, (size_t)(g.nz + 1) * g.C * sizeof(double))))
     return fail(st);
+  if (k.precision == 1) {
+    c->nlow_cap = 64;
+    if ((st = dalloc(c, (void**)&c->ibet_ff, (size_t)(g.nz + 1) * g.C * sizeof(float2))) ||
+        (st = dalloc(c, (void**)&c->gamt_ff, (size_t)(g.nz + 1) * g.C * sizeof(float2))) ||
+        (st = dalloc(c, (void**)&c->lowmodes, (size_t)c->nlow_cap * sizeof(int))))
+      return fail(st);
+  }
   if ((st = thomas_tables(c))) return fail(st);
   c->wsA_bytes = s.wsA; c->wsB_bytes = s.wsB; c->wsP_bytes = s.wsP;
   if (cudaMallocHost(&c->host_scal, 64 * sizeof(double)) != cudaSuccess) { les_set_error("pinned alloc failed"); return fail(LES_ERR_OOM); }
@@ -490,6 +499,68 @@ int les_get_counters(les_ctx* c, int* jt, int* jt_total) {
   if (!c) return LES_ERR_ARG;
   if (jt) *jt = c->jt;
   if (jt_total) *jt_total = c->jt_total;
+  return LES_OK;
+}
+
+// ---- whole-member state image (serving: spill an evicted member to host
+// memory and resume it later exactly where it stopped) ----------------------
+namespace {
+struct StateHeader {
+  char magic[8];            // "LESSTAT1"
+  int nx, ny, nz, precision, model, s_flag;
+  int jt, jt_total;
+  unsigned long long bytes;  // total image size
+};
+}  // namespace
+size_t les_state_bytes(const les_ctx* c) {
+  if (!c) return 0;
+  size_t n = sizeof(StateHeader);
+  for (int f = 0; f < LES_NUM_FIELDS; ++f) n += c->fsize[f] * sizeof(double);
+  return n;
+}
+int les_state_save(les_ctx* c, void* host, size_t bytes) {
+  if (!c || !host) return LES_ERR_ARG;
+  const size_t need = les_state_bytes(c);
+  if (bytes < need) { les_set_error("state image needs %zu bytes, buffer has %zu", need, bytes); return LES_ERR_ARG; }
+  StateHeader h{};
+  std::memcpy(h.magic, "LESSTAT1", 8);
+  h.nx = c->cfg.nx; h.ny = c->cfg.ny; h.nz = c->cfg.nz;
+  h.precision = c->cfg.precision; h.model = c->cfg.model; h.s_flag = c->cfg.s_flag;
+  h.jt = c->jt; h.jt_total = c->jt_total;
+  h.bytes = need;
+  unsigned char* p = static_cast<unsigned char*>(host);
+  std::memcpy(p, &h, sizeof(h));
+  size_t off = sizeof(h);
+  for (int f = 0; f < LES_NUM_FIELDS; ++f) {  // device storage as it is (FP32-held fields included)
+    const size_t nb = c->fsize[f] * sizeof(double);
+    LES_CUDA_CHECK(cudaMemcpyAsync(p + off, c->f[f], nb, cudaMemcpyDeviceToHost, c->stream));
+    off += nb;
+  }
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  return LES_OK;
+}
+int les_state_restore(les_ctx* c, const void* host, size_t bytes) {
+  if (!c || !host) return LES_ERR_ARG;
+  const size_t need = les_state_bytes(c);
+  StateHeader h{};
+  if (bytes < sizeof(h)) { les_set_error("state image too short"); return LES_ERR_ARG; }
+  std::memcpy(&h, host, sizeof(h));
+  if (std::memcmp(h.magic, "LESSTAT1", 8) != 0 || h.bytes != need || bytes < need || h.nx != c->cfg.nx ||
+      h.ny != c->cfg.ny || h.nz != c->cfg.nz || h.precision != c->cfg.precision || h.model != c->cfg.model ||
+      h.s_flag != c->cfg.s_flag) {
+    les_set_error("state image does not match this context's configuration");
+    return LES_ERR_ARG;
+  }
+  const unsigned char* p = static_cast<const unsigned char*>(host);
+  size_t off = sizeof(h);
+  for (int f = 0; f < LES_NUM_FIELDS; ++f) {
+    const size_t nb = c->fsize[f] * sizeof(double);
+    LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], p + off, nb, cudaMemcpyHostToDevice, c->stream));
+    off += nb;
+  }
+  LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+  c->jt = h.jt;
+  c->jt_total = h.jt_total;
   return LES_OK;
 }
 

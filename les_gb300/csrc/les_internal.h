@@ -79,12 +79,18 @@ struct les_ctx {
   double2* wspec = nullptr;                    // wall-plane spectra: dudz(1), dvdz(1), dTdz(1), dTdz(nz)
   double* ibet = nullptr;                      // Thomas 1/bet per (row, mode), FP64
   double* gamt = nullptr;                      // Thomas gam per (row, mode), FP64
+  float2* ibet_ff = nullptr;                   // the same two tables as float-float pairs (mixed form)
+  float2* gamt_ff = nullptr;
+  int* lowmodes = nullptr;                     // modes the mixed form solves in FP64 (kx^2 + ky^2 <= 4)
+  int nlow = 0, nlow_cap = 0;
   int lag_chunk = 32;
   double* dscal = nullptr;                     // device scalars / reductions
-  // per-level reduction results, 24 slots of nz+8 doubles: 0 plane sums /
+  // per-level reduction results, 36 slots of nz+8 doubles: 0 plane sums /
   // rmsdiv partials / model-3 Cs(z); 2..11 scaledep sums; 14 theta plane
   // mean (mixed); 16..18 u, v, w plane means (mixed filt_da); 20..21 theta
-  // level mean and its reciprocal (calcbeta)
+  // level mean and its reciprocal (calcbeta); 24..27 partial plane sums;
+  // 28..33 the mixed form's per-level mean-wind factors (float-float);
+  // 34..35 the mixed form's txz, tyz plane means
   double* dred = nullptr;
   double* host_scal = nullptr;                 // pinned host mirror
   size_t bytes = 0;

@@ -159,16 +159,18 @@ static int cols(les_ctx* c, const ColJob& J) { return colsT<double, double2>(c, 
 // rows r0+w, r0+w+16, ..; lane l the columns l, l+32, ..; four independent
 // partial sums per thread, then a fixed-order tree, so the result is
 // deterministic.
-__device__ __forceinline__ double plane_sum_block(const double* p, int ld, int nx, int r0, int r1, double* sh) {
+template <typename TI>
+__device__ __forceinline__ double plane_sum_block(const TI* p, int ld, int nx, int r0, int r1, double* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
   for (int jy = r0 + wid; jy < r1; jy += 16) {
-    const double* row = p + (size_t)jy * ld;
+    const TI* row = p + (size_t)jy * ld;
     int jx = lane;
     for (; jx + 96 < nx; jx += 128) {
-      a0 += row[jx]; a1 += row[jx + 32]; a2 += row[jx + 64]; a3 += row[jx + 96];
+      a0 += cvt<double>(row[jx]); a1 += cvt<double>(row[jx + 32]);
+      a2 += cvt<double>(row[jx + 64]); a3 += cvt<double>(row[jx + 96]);
     }
-    for (; jx < nx; jx += 32) a0 += row[jx];
+    for (; jx < nx; jx += 32) a0 += cvt<double>(row[jx]);
   }
   sh[threadIdx.x] = (a0 + a1) + (a2 + a3);
   __syncthreads();
@@ -183,7 +185,8 @@ __device__ __forceinline__ double plane_sum_block(const double* p, int ld, int n
 // plane in order and divides by div (1: sums; nx*ny: means).  Several blocks
 // per plane keep more loads in flight than one block per plane; the order
 // stays fixed, so the result is deterministic.
-__global__ void __launch_bounds__(512) k_plane_part(const double* f, long pstride, int ld, int nx, int ny, int rows,
+template <typename TI>
+__global__ void __launch_bounds__(512) k_plane_part(const TI* f, long pstride, int ld, int nx, int ny, int rows,
                                                     double* part) {
   __shared__ double sh[512];
   const int r0 = blockIdx.x * rows, r1 = min(r0 + rows, ny);
@@ -200,11 +203,12 @@ __global__ void k_plane_fin(const double* __restrict__ part, int nsplit, int npl
 }
 // sums (div 1) or means (div nx*ny) of f(1:nx,1:ny) over nplanes planes;
 // nsplit * nplanes <= 4 (nz + 8)
-static void plane_sums(les_ctx* c, const double* f, long pstride, int nplanes, int nsplit, double div, double* out) {
+template <typename TI>
+static void plane_sums(les_ctx* c, const TI* f, long pstride, int nplanes, int nsplit, double div, double* out) {
   const Grid& g = c->g;
   double* part = c->dred + 24 * (size_t)(g.nz + 8);
   const int rows = (g.ny + nsplit - 1) / nsplit;
-  k_plane_part<<<dim3(nsplit, nplanes), 512, 0, c->stream>>>(f, pstride, g.ld, g.nx, g.ny, rows, part); LES_COUNT_LAUNCH();
+  k_plane_part<TI><<<dim3(nsplit, nplanes), 512, 0, c->stream>>>(f, pstride, g.ld, g.nx, g.ny, rows, part); LES_COUNT_LAUNCH();
   k_plane_fin<<<(nplanes + 127) / 128, 128, 0, c->stream>>>(part, nsplit, nplanes, div, out); LES_COUNT_LAUNCH();
 }
 
@@ -1873,40 +1877,134 @@ __global__ void k_rhs_ab2(double* u, double* v, double* w, double* Rx, double* R
   }
 }
 
-// Mixed form: the horizontal right-hand sides come from FP32 transforms, so
-// they and their AB2 increments are formed in FP32 (conversions on the
-// integer pipe) and only u + increment is an FP64 addition.  The vertical
-// component keeps the FP64 arithmetic of k_rhs_ab2: the pressure solve takes
-// its wall and lid conditions from the same vertical stress divergence, and
-// an FP32-rounded w right-hand side leaves a divergence the projection cannot
-// remove (rmsdiv 1e-10 instead of 1e-13 at 32^3).
-__global__ void k_rhs_ab2_32(double* u, double* v, double* w, double* Rx, double* Ry, double* Rz, double* Rxf,
-                             double* Ryf, double* Rzf, const double* __restrict__ dx_,
-                             const double* __restrict__ dy_, const double* __restrict__ dz_,
-                             const double* __restrict__ bs, size_t nv, size_t np, double dt, int sflag, int euler) {
-  const float dtf = (float)dt;
-  GSTRIDE(i, nv + np) {
-    if (i >= nv) { u[i] = LES_BOGUS; v[i] = LES_BOGUS; w[i] = LES_BOGUS; continue; }
-    double rz = -Rz[i] - dz_[i];
-    if (sflag) rz = rz + bs[i];
-    Rz[i] = rz;
-    double fz = Rzf[i];
-    if (euler) { fz = rz; Rzf[i] = rz; }
-    w[i] = w[i] + dt * (1.5 * rz + (1.0 - 1.5) * fz);
-    const float rx = -cvt_d2f(Rx[i]) - cvt_d2f(dx_[i]);
-    const float ry = -cvt_d2f(Ry[i]) - cvt_d2f(dy_[i]);
-    const double drx = cvt_f2d(rx), dry = cvt_f2d(ry);
-    Rx[i] = drx; Ry[i] = dry;
-    float fx, fy;
-    if (euler) {
-      fx = rx; fy = ry;
-      Rxf[i] = drx; Ryf[i] = dry;
-    } else {
-      fx = cvt_d2f(Rxf[i]); fy = cvt_d2f(Ryf[i]);
-    }
-    u[i] = u[i] + cvt_f2d(dtf * (1.5f * rx - 0.5f * fx));
-    v[i] = v[i] + cvt_f2d(dtf * (1.5f * ry - 0.5f * fy));
+// ---------------------------------------------------------------------------
+// Mixed form: the convective term split about the plane-mean wind.
+// With u = U(z) + u', v = V(z) + v' (U, V the plane means of the uvp levels)
+// and the w-level vorticity w_x = Ox(z) + w_x', w_y = Oy(z) + w_y' (Oy = dU/dz,
+// Ox = -dV/dz; w_z has no plane mean), the products of convec.f90:117-217
+//   cx = -v w_z + (w w_y)~      cy = u w_z - (w w_x)~
+//   cz = ((u + u_m)(-w_y) + (v + v_m) w_x) / 2       (~: the two-level average)
+// are the FP32 products of the fluctuations (k_convec_prod on u', v', w and
+// w_x', w_y', w_z, 3/2-dealiased as before) plus terms linear in one
+// fluctuating field with a plane-constant factor, plus a plane constant:
+//   cx_lin = -V w_z + (Oy w)~          cy_lin = U w_z - (Ox w)~
+//   cz_lin = (-(U + U_m) w_y' - Oy (u' + u'_m) + (V + V_m) w_x' + Ox (v' + v'_m)) / 2
+//            + (-(U + U_m) Oy + (V + V_m) Ox) / 2
+// A plane constant times a band-limited field is band-limited, so the 3/2
+// dealiasing leaves the linear terms unchanged: they are formed on the
+// small grid.  U w_z is of order U k |v'| (about 260 at 256^3), so w_z and
+// dw/dx come from float-float transforms (k_rhs_ab2_mx reads them) and the
+// linear terms and the right-hand-side sums run in float-float arithmetic.
+// In FP32 they left a relative error of about 5e-8 per step in v and w.
+// Per-level factors in float-float (entry jz, 1-based):
+//   U, V at uvp level jz; Oy, Ox at w-level jz (zero at jz = 1 and nz:
+//   level 1 vorticity is not read by the products, level nz is w = 0);
+//   Cz = the plane constant of cz at w-level jz; UVf = (U, V) in FP32.
+struct MeanTab {
+  float2 *U, *V, *Oy, *Ox, *Cz, *UVf;
+};
+static MeanTab mean_tab(les_ctx* c) {
+  const size_t ms = (size_t)c->g.nz + 8;
+  float2* b = reinterpret_cast<float2*>(c->dred + 28 * ms);  // slots 28..33
+  return MeanTab{b, b + ms, b + 2 * ms, b + 3 * ms, b + 4 * ms, b + 5 * ms};
+}
+__device__ __forceinline__ float2 df2(double x) {
+  const dfloat d = cvt<dfloat>(x);
+  return make_float2(d.hi, d.lo);
+}
+__global__ void k_mean_tab(const double* __restrict__ mean, int ms, int nz, double dz, MeanTab T) {
+  const int jz = blockIdx.x * blockDim.x + threadIdx.x + 1;  // 1..nz
+  if (jz > nz) return;
+  const double U = mean[jz - 1], V = mean[ms + jz - 1];
+  double oy = 0.0, ox = 0.0, cz = 0.0;
+  if (jz >= 2 && jz <= nz - 1) {
+    const double Um = mean[jz - 2], Vm = mean[ms + jz - 2];
+    oy = (U - Um) / dz;
+    ox = -(V - Vm) / dz;
+    cz = 0.5 * (-(U + Um) * oy + (V + Vm) * ox);
   }
+  T.U[jz] = df2(U);
+  T.V[jz] = df2(V);
+  T.Oy[jz] = df2(oy);
+  T.Ox[jz] = df2(ox);
+  T.Cz[jz] = df2(cz);
+  T.UVf[jz] = make_float2(cvt_d2f(U), cvt_d2f(V));
+  if (jz == nz) {  // w-level nz + 1 is never a neighbour with a nonzero factor
+    T.Oy[nz + 1] = make_float2(0.f, 0.f);
+    T.Ox[nz + 1] = make_float2(0.f, 0.f);
+  }
+}
+__device__ __forceinline__ dfloat ldt(const float2* p, int j) {
+  const float2 v = p[j];
+  return dfloat(v.x, v.y);
+}
+__device__ __forceinline__ dfloat dfs(float a) { return dfloat(a, 0.f); }
+
+// main.f90:309-390 for the mixed form: RHS = -(c_nl + c_lin) - divt
+// (+ buoyancy on z), the AB2 predictor u* = u + dt (1.5 RHS - 0.5 RHS_f)
+// (Euler on the first step), u*(nz) = BOGUS.  The linear terms read u and w
+// at the neighbouring levels, so u*, v*, w* go to separate fields (us, vs,
+// ws) and the state keeps its start-of-step values until the projection
+// writes u = u* - 1.5 dt grad p.  c_nl (RHSx..z on entry: the
+// dealiased FP32 products of the fluctuations) and divt are FP32-accurate;
+// the linear terms, the sums and the AB2 increments are float-float, the
+// state and RHS stay FP64 (a float-float value is joined with one FP64
+// addition).  wz = w_z, wx = dw/dx on the uvp / w levels (float-float
+// transforms), dwdy the FP32-held dw/dy.  grid (ceil(np/256), nz).
+__global__ void __launch_bounds__(256) k_rhs_ab2_mx(
+    double* u, double* v, double* w, double* Rx, double* Ry, double* Rz, double* Rxf, double* Ryf, double* Rzf,
+    const double* __restrict__ dx_, const double* __restrict__ dy_, const double* __restrict__ dz_,
+    const double* __restrict__ bs, const dfloat* __restrict__ wz, const dfloat* __restrict__ wx,
+    const float* __restrict__ dwdy, MeanTab T, double* __restrict__ us, double* __restrict__ vs,
+    double* __restrict__ ws, int ld, int ny, int nz, float2 idz2, float2 dt2, int sflag, int euler) {
+  const unsigned np = (unsigned)ld * ny;
+  const unsigned p = blockIdx.x * 256u + threadIdx.x;
+  if (p >= np) return;
+  const int jz = blockIdx.y + 1;
+  const size_t i = (size_t)(jz - 1) * np + p;
+  if (jz == nz) { us[i] = LES_BOGUS; vs[i] = LES_BOGUS; ws[i] = LES_BOGUS; return; }
+  const dfloat h(0.5f, 0.f);
+  const dfloat idz(idz2.x, idz2.y);  // 1/dz and dt as float-float pairs formed on the host
+  const dfloat U = ldt(T.U, jz), V = ldt(T.V, jz);
+  const dfloat wi = cvt<dfloat>(w[i]), wp = cvt<dfloat>(w[i + np]);
+  const dfloat s1 = wz[i];
+  const dfloat oyp = ldt(T.Oy, jz + 1), oxp = ldt(T.Ox, jz + 1), oy = ldt(T.Oy, jz), ox = ldt(T.Ox, jz);
+  const dfloat cxl = (-V) * s1 + h * (oyp * wp + oy * wi);
+  const dfloat cyl = U * s1 - h * (oxp * wp + ox * wi);
+  dfloat czl(0.f, 0.f);
+  const double ui = u[i];
+  if (jz >= 2) {
+    const size_t im = i - np;
+    const dfloat Um = ldt(T.U, jz - 1);
+    const dfloat up = cvt<dfloat>(ui) - U, upm = cvt<dfloat>(u[im]) - Um;
+    const float vp = cvt_d2f(v[i]) - T.UVf[jz].y, vpm = cvt_d2f(v[im]) - T.UVf[jz - 1].y;
+    const dfloat wyp = (up - upm) * idz - wx[i];                          // w_y' at w-level jz
+    const float wxp = dwdy[i] - (vp - vpm) * idz2.x;                    // w_x' (FP32: its factor V is small)
+    const dfloat Us = U + Um;
+    const float Vs = T.UVf[jz].y + T.UVf[jz - 1].y;
+    czl = h * ((-Us) * wyp - oy * (up + upm)) + dfs(0.5f * (Vs * wxp) + 0.5f * (ox.hi * (vp + vpm))) +
+          ldt(T.Cz, jz);
+  }
+  const dfloat rx = -(dfs(cvt_d2f(Rx[i])) + cxl) - dfs(cvt_d2f(dx_[i]));
+  const dfloat ry = -(dfs(cvt_d2f(Ry[i])) + cyl) - dfs(cvt_d2f(dy_[i]));
+  dfloat rz = -(dfs(cvt_d2f(Rz[i])) + czl) - dfs(cvt_d2f(dz_[i]));
+  if (sflag) rz = rz + cvt<dfloat>(bs[i]);
+  const double rxd = cvt<double>(rx), ryd = cvt<double>(ry), rzd = cvt<double>(rz);
+  Rx[i] = rxd;
+  Ry[i] = ryd;
+  Rz[i] = rzd;
+  dfloat fx, fy, fz;
+  if (euler) {
+    fx = rx; fy = ry; fz = rz;
+    Rxf[i] = rxd; Ryf[i] = ryd; Rzf[i] = rzd;
+  } else {
+    fx = cvt<dfloat>(Rxf[i]); fy = cvt<dfloat>(Ryf[i]); fz = cvt<dfloat>(Rzf[i]);
+  }
+  const dfloat dtf(dt2.x, dt2.y);
+  const dfloat a15(1.5f, 0.f), a05(0.5f, 0.f);
+  us[i] = ui + cvt<double>(dtf * (a15 * rx - a05 * fx));
+  vs[i] = v[i] + cvt<double>(dtf * (a15 * ry - a05 * fy));
+  ws[i] = w[i] + cvt<double>(dtf * (a15 * rz - a05 * fz));
 }
 
 // main.f90:403-410 + forcing.f90:128-219 project, one thread per point of
@@ -1952,9 +2050,13 @@ __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, doub
 }
 // Mixed form: dpdz and the projection in FP64 with the fused factor
 // -1.5 dt (the pressure comes from float-float transforms and the projection
-// sets the divergence); the horizontal RHS bookkeeping R -= grad p in FP32,
-// the vertical one in FP64 (see k_rhs_ab2_32).  grid (ceil(np/256), nz-1).
-__global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, double* w, double* Rx, double* Ry,
+// sets the divergence), and the RHS bookkeeping R -= grad p in FP64: the
+// stored RHS is next step's RHS_f, and the horizontal RHS are of order
+// U k |v'|, whose FP32 rounding is 1e-5 of v's own scale.
+// grid (ceil(np/256), nz-1).
+__global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, double* w, const double* __restrict__ us,
+                                                        const double* __restrict__ vs,
+                                                        const double* __restrict__ ws, double* Rx, double* Ry,
                                                         double* Rz, const double* __restrict__ p,
                                                         const double* __restrict__ dpdx,
                                                         const double* __restrict__ dpdy, double* dpdz, int ld,
@@ -1974,16 +2076,16 @@ __global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, do
     pz = dpdz[i];
   }
   const double gx = dpdx[i], gy = dpdy[i];
-  Rx[i] = cvt_f2d(cvt_d2f(Rx[i]) - cvt_d2f(gx));
-  Ry[i] = cvt_f2d(cvt_d2f(Ry[i]) - cvt_d2f(gy));
+  Rx[i] = Rx[i] - gx;
+  Ry[i] = Ry[i] - gy;
   Rz[i] = Rz[i] - pz;
-  double uu = u[i], vv = v[i], ww = w[i];
+  double uu = us[i], vv = vs[i], ww = ws[i];
   if (inx) {
     uu = fma(c, gx, uu);
     vv = fma(c, gy, vv);
-    u[i] = uu; v[i] = vv;
-    if (jz >= 2) { ww = fma(c, pz, ww); w[i] = ww; }
+    if (jz >= 2) ww = fma(c, pz, ww);
   }
+  u[i] = uu; v[i] = vv; w[i] = ww;
   if (jz == nz - 1) {
     const size_t top = i + np;
     dpdz[top] = LES_BOGUS;
@@ -2137,11 +2239,18 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
                                                   const C2* __restrict__ top, PC* P, const double* __restrict__ ibet,
                                                   const double* __restrict__ gam, const double* __restrict__ kx,
                                                   const double* __restrict__ ky, const float2* __restrict__ kxd,
-                                                  const float2* __restrict__ kyd, int lh, int ny, int nz, double dz) {
+                                                  const float2* __restrict__ kyd, int lh, int ny, int nz, double dz,
+                                                  const int* __restrict__ modes, int nmodes) {
   const int nk = lh * ny;
   const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
-  const int t = g2 >> 1, part = g2 & 1;
-  if (t >= nk) return;
+  int t = g2 >> 1;
+  const int part = g2 & 1;
+  if (modes) {  // a list of modes (the mixed form's lowest |k|)
+    if (t >= nmodes) return;
+    t = modes[t];
+  } else if (t >= nk) {
+    return;
+  }
   const int jx = t % lh, jy = t / lh;
   if (t == 0 || jy == ny / 2 || jx == lh - 1) {
     if (part == 0) tridiag_mode<HC, PC>(t, Hx, Hy, Hz, bot, top, P, ibet, gam, kx, ky, lh, ny, nz, dz);
@@ -2291,6 +2400,158 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
   }
 }
 
+// Mixed form: press_stag_array.f90:192-264 + tridag_array.f90:41-101 as a
+// chunked Thomas solve in float-float arithmetic, the batched hybrid for
+// many short-latency systems: the z-recurrences of 16 modes (32 systems:
+// real and imaginary parts; a, b, c are real) run per CTA, each of the
+// eight warps on one chunk of about n/8 rows, lane = system.
+//   forward   d_j = al_j d_{j-1} + ib_j r_j  (al_j = -a_j ib_j): each warp
+//             runs its chunk from d = 0 and keeps the chunk product
+//             A_j = al_s .. al_j; the true d_j = d~_j + A_j D_(chunk-1), with
+//             the chunk-end values D passed up the 8 chunks by one warp
+//             (the reduced system of the chunk boundaries);
+//   backward  x_j = d_j - g_(j+1) x_(j+1): the same from the top chunk down.
+// Rows stay in shared memory (66 KB of d / x and 33 KB of chunk products per
+// CTA); global memory sees each right-hand-side input, table entry and
+// p-hat value once, in 256-byte warp accesses.  The recurrence coefficients
+// are the FP64 Thomas tables rounded to float-float; modes with
+// kx^2 + ky^2 <= 4 (near-singular, nearly Neumann systems) and the (0,0)
+// mode are left to the FP64 solve (k_tridiag2 on a mode list); the Nyquist
+// modes are zeroed (press_stag_array.f90:263-264).
+constexpr int TRI_M = 16, TRI_W = 8;
+constexpr int TRI_K2LOW = 4;  // modes with kx^2 + ky^2 <= 4 (integer indices) stay FP64
+__device__ __forceinline__ dfloat ldff(const float2* p, size_t i) {
+  const float2 v = p[i];
+  return dfloat(v.x, v.y);
+}
+__global__ void __launch_bounds__(TRI_W * 32) k_tridiag_ffc(const dcomplex* __restrict__ Hx,
+                                                            const dcomplex* __restrict__ Hy,
+                                                            const dcomplex* __restrict__ Hz,
+                                                            const C2* __restrict__ bot, const C2* __restrict__ top,
+                                                            dcomplex* P, const float2* __restrict__ ibd,
+                                                            const float2* __restrict__ gad,
+                                                            const float2* __restrict__ kxd,
+                                                            const float2* __restrict__ kyd,
+                                                            int lh, int ny, int nz, float2 idz2, float2 a2,
+                                                            float2 dz2, int k2low) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n = nz + 1;
+  dfloat* D = reinterpret_cast<dfloat*>(smraw);            // (n + 1) x 32: d~, d, then x~, x
+  dfloat* A = D + (size_t)(n + 1) * 32;                     // (n + 1) x 16: chunk products
+  dfloat* ce = A + (size_t)(n + 1) * TRI_M;                 // TRI_W x 32: chunk-end d~ / chunk-start x~
+  dfloat* cp = ce + TRI_W * 32;                             // TRI_W x 32: their chunk products
+  dfloat* cc = cp + TRI_W * 32;                             // TRI_W x 32: carries into each chunk
+  const int nk = lh * ny;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * TRI_M + (lane >> 1), comp = lane & 1;
+  const int jx = t % lh, jy = t / lh;
+  const bool inb = t < nk;
+  const bool nyq = inb && (jy == ny / 2 || jx == lh - 1);
+  const int my = jy <= ny / 2 ? jy : jy - ny;  // wrapped ky index
+  const bool low = inb && !nyq && jx * jx + my * my <= k2low;  // includes (0,0): solved in FP64
+  const bool act = inb && !nyq && !low;
+  const size_t NK = (size_t)nk;
+  const int L = (n + TRI_W - 1) / TRI_W;
+  const int s0 = 1 + warp * L, e0 = min(n, (warp + 1) * L);  // rows of this warp's chunk (may be empty)
+  const dfloat idz(idz2.x, idz2.y), a(a2.x, a2.y), dz(dz2.x, dz2.y);
+  const dfloat zero(0.f, 0.f), one(1.f, 0.f);
+  const int ch = comp == 0 ? 1 : 0;  // component of Hx, Hy feeding this system
+  const float* Hxf = reinterpret_cast<const float*>(Hx);
+  const float* Hyf = reinterpret_cast<const float*>(Hy);
+  const float* Hzf = reinterpret_cast<const float*>(Hz);
+  auto ldh = [&](const float* H, size_t e, int cmp) -> dfloat {  // component cmp of element e
+    const float2 v = *reinterpret_cast<const float2*>(H + 4 * e + 2 * cmp);
+    return dfloat(v.x, v.y);
+  };
+  // ---- forward, local to the chunk
+  dfloat d = zero, Ap = one;
+  if (act && s0 <= e0) {
+    const dfloat k_x = ldff(kxd, t), k_y = ldff(kyd, t);
+    dfloat hz0 = zero;
+    if (s0 >= 2 && s0 <= nz) hz0 = ldh(Hzf, (size_t)(s0 - 2) * NK + t, comp);  // Hz of row s0 - 1 (levels 1..nz-1)
+    for (int j = s0; j <= e0; ++j) {
+      const dfloat ib = ldff(ibd, (size_t)(j - 1) * NK + t);
+      dfloat r, al;
+      if (j == 1) {
+        const C2 b1 = bot[t];
+        r = -(dz * cvt<dfloat>(comp == 0 ? b1.x : b1.y));
+        al = zero;
+        hz0 = ldh(Hzf, t, comp);
+      } else if (j <= nz) {
+        const dfloat hx = ldh(Hxf, (size_t)(j - 2) * NK + t, ch);
+        const dfloat hy = ldh(Hyf, (size_t)(j - 2) * NK + t, ch);
+        const dfloat hz1 = (j <= nz - 1) ? ldh(Hzf, (size_t)(j - 1) * NK + t, comp) : zero;
+        const dfloat sxy = k_x * hx + k_y * hy;
+        const dfloat dh = (hz1 - hz0) * idz;
+        r = comp == 0 ? dh - sxy : sxy + dh;
+        hz0 = hz1;
+        al = -(a * ib);
+      } else {  // row n: a = -1, r = -dz top
+        const C2 tp = top[t];
+        r = -(dz * cvt<dfloat>(comp == 0 ? tp.x : tp.y));
+        al = ib;
+      }
+      d = al * d + ib * r;
+      Ap = al * Ap;
+      D[(size_t)j * 32 + lane] = d;
+      if (comp == 0) A[(size_t)j * TRI_M + (lane >> 1)] = Ap;
+    }
+  }
+  ce[warp * 32 + lane] = d;
+  cp[warp * 32 + lane] = Ap;
+  __syncthreads();
+  if (warp == 0) {  // chunk boundaries: D_w = d~_end(w) + A_end(w) D_(w-1)
+    dfloat Dw = ce[lane];
+    cc[lane] = zero;
+    for (int w = 1; w < TRI_W; ++w) {
+      cc[w * 32 + lane] = Dw;
+      Dw = ce[w * 32 + lane] + cp[w * 32 + lane] * Dw;
+    }
+  }
+  __syncthreads();
+  // ---- fix-up of d, then backward, local to the chunk
+  dfloat x = zero, Bp = one;
+  const bool run = act && s0 <= e0;
+  if (run && warp > 0) {
+    const dfloat Din = cc[warp * 32 + lane];
+    for (int j = s0; j <= e0; ++j) {
+      const size_t q = (size_t)j * 32 + lane;
+      D[q] = D[q] + A[(size_t)j * TRI_M + (lane >> 1)] * Din;
+    }
+  }
+  __syncwarp();  // (every lane) the fix-up has read A before the backward products replace it
+  if (run) {
+    for (int j = e0; j >= s0; --j) {
+      const size_t q = (size_t)j * 32 + lane;
+      dfloat gm = zero;
+      if (j < n) gm = ldff(gad, (size_t)j * NK + t);  // g_(j+1)
+      x = D[q] - gm * x;
+      Bp = (j < n) ? -(gm * Bp) : zero;  // B_j; the top row has no carry from above
+      D[q] = x;
+      if (comp == 0) A[(size_t)j * TRI_M + (lane >> 1)] = Bp;
+    }
+  }
+  ce[warp * 32 + lane] = x;
+  cp[warp * 32 + lane] = Bp;
+  __syncthreads();
+  if (warp == 0) {  // from the top chunk down: X_w = x~_start(w) + B_start(w) X_(w+1)
+    dfloat Xw = zero;
+    for (int w = TRI_W - 1; w >= 0; --w) {
+      cc[w * 32 + lane] = Xw;
+      Xw = ce[w * 32 + lane] + cp[w * 32 + lane] * Xw;
+    }
+  }
+  __syncthreads();
+  if (!inb || low || s0 > e0) return;
+  float* Pf = reinterpret_cast<float*>(P);
+  const dfloat Xin = cc[warp * 32 + lane];
+  for (int j = s0; j <= e0; ++j) {
+    dfloat v = zero;
+    if (act) v = D[(size_t)j * 32 + lane] + A[(size_t)j * TRI_M + (lane >> 1)] * Xin;
+    *reinterpret_cast<float2*>(Pf + 4 * ((size_t)(j - 1) * NK + t) + 2 * comp) = make_float2(v.hi, v.lo);
+  }
+}
+
 // Thomas coefficients of press_stag_array.f90:144-210 for every (kx,ky):
 // they depend on k^2 and dz only, so they are formed once per context
 // (tridag_array.f90:41-69 recurrences, reciprocal of bet stored).
@@ -2326,6 +2587,25 @@ int thomas_tables(les_ctx* c) {
   }
   LES_CUDA_CHECK(cudaMemcpy(c->ibet, ib.data(), ib.size() * sizeof(double), cudaMemcpyHostToDevice));
   LES_CUDA_CHECK(cudaMemcpy(c->gamt, gm.data(), gm.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (c->ibet_ff) {  // the mixed form's chunked solve: the same tables as float-float pairs, and the
+                     // list of the modes it leaves to the FP64 solve
+    std::vector<float2> f2(ib.size());
+    auto ff = [](double v) { const float h = (float)v; return make_float2(h, (float)(v - (double)h)); };
+    for (size_t i = 0; i < ib.size(); ++i) f2[i] = ff(ib[i]);
+    LES_CUDA_CHECK(cudaMemcpy(c->ibet_ff, f2.data(), f2.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    for (size_t i = 0; i < gm.size(); ++i) f2[i] = ff(gm[i]);
+    LES_CUDA_CHECK(cudaMemcpy(c->gamt_ff, f2.data(), f2.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    std::vector<int> low;
+    for (size_t t = 0; t < NK; ++t) {
+      const int jx = (int)(t % lh), jy = (int)(t / lh);
+      if (jy == ny / 2 || jx == lh - 1) continue;
+      const int my = jy <= ny / 2 ? jy : jy - ny;
+      if (jx * jx + my * my <= TRI_K2LOW) low.push_back((int)t);
+    }
+    if ((int)low.size() > c->nlow_cap) { les_set_error("low-mode list overflow"); return LES_ERR_STATE; }
+    LES_CUDA_CHECK(cudaMemcpy(c->lowmodes, low.data(), low.size() * sizeof(int), cudaMemcpyHostToDevice));
+    c->nlow = (int)low.size();
+  }
   return 0;
 }
 
@@ -2333,22 +2613,24 @@ int thomas_tables(les_ctx* c) {
 // p-hat (double: FP64 form and the per-routine entry; dfloat: mixed form).
 // The wall planes' spectra and the tridiagonal solve are FP64 in both.
 template <typename T>
-static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
+static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const double* const* ustar = nullptr) {
   typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const int nz = g.nz;
   const double cst = 1.0 / (double)(g.nx * g.ny);
-  // spectra of u*, v*, w* (levels 1..nz-1), (const/tadv1)*(u/dt)
+  // spectra of u*, v*, w* (levels 1..nz-1), (const/tadv1)*(u/dt); u* is the
+  // state itself, or (mixed form) the separate predictor fields
   const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  if (ustar)
+    for (int q = 0; q < 3; ++q) in[q] = ustar[q];
   const double sc3[3] = {cst / 1.5, cst / 1.5, cst / 1.5};
   const double dv3[3] = {k.dt, k.dt, k.dt};
   r2cT<T, double>(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
   CX* H = (CX*)c->wsP;                                       // 3*(nz-1)*C
   C2* BT = reinterpret_cast<C2*>(H + (size_t)3 * (nz - 1) * g.C);  // bottom, top
-  // p-hat: FP64 in the mixed form (the inverse float-float y pass widens it
-  // on load, so the solve stores its FP64 values as they are)
-  typedef typename std::conditional<std::is_same<T, dfloat>::value, double2, CX>::type PCX;
+  // p-hat in the transform precision (float-float in the mixed form)
+  typedef CX PCX;
   PCX* P = reinterpret_cast<PCX*>(BT + 2 * g.C);            // (nz+1)*C
   ColJob J = coljob(c, MAP_SAME, DIR_FWD, nz - 1);
   J.nin = 1; J.nout = 1; J.nf = 3;
@@ -2368,9 +2650,30 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy) {
     K.coef[0][0] = CC_KILL;
     cols(c, K);
   }
-  k_tridiag2<CX, PCX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
-      H, H + (size_t)(nz - 1) * g.C, H + (size_t)2 * (nz - 1) * g.C, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky,
-      c->kxd, c->kyd, g.lh, g.ny, nz, g.dz); LES_COUNT_LAUNCH();
+  const CX* Hx = H;
+  const CX* Hy = H + (size_t)(nz - 1) * g.C;
+  const CX* Hz = H + (size_t)2 * (nz - 1) * g.C;
+  if constexpr (std::is_same<T, dfloat>::value) {
+    // chunked float-float Thomas for |k|^2 > TRI_K2LOW, FP64 Thomas for the rest
+    const size_t sm = ((size_t)(nz + 2) * (32 + TRI_M) + 3 * TRI_W * 32) * sizeof(dfloat);
+    static size_t sm_set = 48 * 1024;
+    if (sm > sm_set) {
+      cudaFuncSetAttribute(k_tridiag_ffc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      sm_set = sm;
+    }
+    const dfloat idz(1.0 / g.dz), a2(1.0 / (g.dz * g.dz)), dz2(g.dz);
+    k_tridiag_ffc<<<(g.lh * g.ny + TRI_M - 1) / TRI_M, TRI_W * 32, sm, c->stream>>>(
+        Hx, Hy, Hz, BT, BT + g.C, P, c->ibet_ff, c->gamt_ff, c->kxd, c->kyd, g.lh, g.ny, nz,
+        make_float2(idz.hi, idz.lo), make_float2(a2.hi, a2.lo), make_float2(dz2.hi, dz2.lo), TRI_K2LOW);
+    LES_COUNT_LAUNCH();
+    k_tridiag2<CX, PCX><<<(2 * c->nlow + 127) / 128, 128, 0, c->stream>>>(
+        Hx, Hy, Hz, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz,
+        c->lowmodes, c->nlow); LES_COUNT_LAUNCH();
+  } else {
+    k_tridiag2<CX, PCX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
+        Hx, Hy, Hz, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz,
+        nullptr, 0); LES_COUNT_LAUNCH();
+  }
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
   {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
@@ -2454,19 +2757,27 @@ __global__ void k_sflux(const double* __restrict__ theta, const double* __restri
   }
 }
 // scalars_module.f90:321-346 advection product on the 3/2 grid
+// uvm: per-level plane-mean wind (U, V) added back to um, vm (the mixed form
+// pads the fluctuations u', v'), or null
 template <typename S>
 __global__ void k_scalar_prod(const S* __restrict__ um, const S* __restrict__ vm,
                               const S* __restrict__ wm, const S* __restrict__ sx,
                               const S* __restrict__ sy, const S* __restrict__ sz, S* R, int ldb,
-                              int nx2, int ny2, int nz) {
+                              int nx2, int ny2, int nz, const float2* __restrict__ uvm) {
   const size_t np = (size_t)ldb * ny2;
   GSTRIDE(i, np * nz) {
     const int jz = (int)(i / np) + 1;
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ldb);
     if (jx >= nx2) continue;
-    if (jz == 1) R[i] = um[i] * sx[i] + vm[i] * sy[i] + ((S)0.5 * wm[i + np]) * sz[i + np];
-    else if (jz == nz) R[i] = um[i] * sx[i] + vm[i] * sy[i];
-    else R[i] = um[i] * sx[i] + vm[i] * sy[i] + (wm[i] * sz[i] + wm[i + np] * sz[i + np]) / (S)2;
+    S uu = um[i], vv = vm[i];
+    if (uvm) {
+      const float2 m = uvm[jz];
+      uu += (S)m.x;
+      vv += (S)m.y;
+    }
+    if (jz == 1) R[i] = uu * sx[i] + vv * sy[i] + ((S)0.5 * wm[i + np]) * sz[i + np];
+    else if (jz == nz) R[i] = uu * sx[i] + vv * sy[i];
+    else R[i] = uu * sx[i] + vv * sy[i] + (wm[i] * sz[i] + wm[i + np] * sz[i + np]) / (S)2;
   }
 }
 // scalars_module.f90:364-407 horizontal SGS fluxes
@@ -2659,7 +2970,7 @@ int op_theta(les_ctx* c) {
   const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DTDX], c->f[LES_DTDY], c->f[LES_DTDZ]};
   op_dealias1(c, in, bigf, 6, nz);
   k_scalar_prod<double><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
-                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
+                                                           bigf[6], g.ld_big, g.nx2, g.ny2, nz, nullptr); LES_COUNT_LAUNCH();
   double* rt = c->f[LES_RHS_T];
   const double* b6 = bigf[6];
   op_dealias2(c, &rt, &b6, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
@@ -3377,7 +3688,20 @@ static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
   const int tid[5] = {LES_TXX, LES_TXY, LES_TYY, LES_TXZ, LES_TYZ};
   for (int q = 0; q < 5; ++q) in[q] = reinterpret_cast<const TS*>(c->f[tid[q]]);
   double scs[5] = {sc, sc, sc, sc, sc};
-  r2cT<T, TS>(c, 5, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh);
+  // Mixed form: txz, tyz carry the plane-mean shear stress (large near the
+  // wall); their FP32 transforms see tau - plane mean, which the horizontal
+  // derivatives do not see, so the derivatives keep the fluctuation's precision
+  const double* offs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (MX) {
+    const size_t ms = (size_t)g.nz + 8;
+    double* m13 = c->dred + 34 * ms;
+    double* m23 = c->dred + 35 * ms;
+    plane_sums(c, in[3], (long)g.nplane, g.nz, 4, (double)(g.nx * g.ny), m13);
+    plane_sums(c, in[4], (long)g.nplane, g.nz, 4, (double)(g.nx * g.ny), m23);
+    offs[3] = m13;
+    offs[4] = m23;
+  }
+  r2cT<T, TS>(c, 5, g.nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh, offs);
   const long FS = (long)g.nz * g.C;
   ColJob J = coljob(c, MAP_SAME, DIR_BOTH, g.nz);
   J.nin = 3; J.nout = 2;
@@ -3473,7 +3797,8 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     padT<MX, CX>(c, ds, 3, o3);
   }
   k_scalar_prod<S><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
-                                                              bigf[6], g.ld_big, g.nx2, g.ny2, nz); LES_COUNT_LAUNCH();
+                                                              bigf[6], g.ld_big, g.nx2, g.ny2, nz,
+                                                              MX ? mean_tab(c).UVf : nullptr); LES_COUNT_LAUNCH();
   if constexpr (MX) {
     // FP32 scalar flux: the advection term, tx, ty and their divergence in
     // FP32 scratch (tmp), the theta RHS itself FP64
@@ -3559,6 +3884,52 @@ static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, doub
   return 0;
 }
 
+// Mixed form, the linear part of the convective term split about the plane
+// mean wind (see k_rhs_ab2_mx): the per-level factors, then w_z = dv/dx -
+// du/dy and dw/dx of the Nyquist-filtered u', v', w from float-float
+// transforms of the fluctuations, into the free half of the 3/2-grid pool
+// (the mixed form keeps its nine 3/2-grid fields in FP32 in the first half).
+static dfloat* mlin_fields(les_ctx* c) {
+  const size_t half = ((size_t)9 * c->g.nfield_big + 1) / 2;
+  const size_t off = (half + 63) / 64 * 64;  // 512-byte aligned
+  return reinterpret_cast<dfloat*>(c->big + off);
+}
+// the mixed form's predictor fields u*, v*, w* (after the two fields above)
+static double* ustar_fields(les_ctx* c) {
+  return reinterpret_cast<double*>(mlin_fields(c) + 2 * c->g.nfield);
+}
+static void meanflow_lin(les_ctx* c) {
+  const Grid& g = c->g;
+  const int nz = g.nz;
+  const int ms = nz + 8;
+  const double* mean = c->dred + 16 * (size_t)ms;  // u, v, w plane means (filt_da_uvw_mixed)
+  k_mean_tab<<<(nz + 127) / 128, 128, 0, c->stream>>>(mean, ms, nz, g.dz, mean_tab(c)); LES_COUNT_LAUNCH();
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  const double scs[3] = {sc, sc, sc};
+  const double* offs[3] = {mean, mean + ms, mean + 2 * ms};
+  r2cT<dfloat, double>(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh, offs);
+  const long FS = (long)nz * g.C;
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+  J.nin = 3; J.nout = 2; J.nf = 1;
+  J.in[0] = c->wsA; J.in[1] = (dcomplex*)c->wsA + FS; J.in[2] = (dcomplex*)c->wsA + 2 * FS;
+  J.out[0] = c->wsB; J.out[1] = (dcomplex*)c->wsB + FS;
+  J.coef[0][0] = CC_MIKY; J.coef[0][1] = CC_IKX;  // w_z = i kx v - i ky u
+  J.coef[1][2] = CC_IKX;                           // dw/dx
+  colsT<dfloat, dcomplex>(c, J);
+  dfloat* ml = mlin_fields(c);
+  dfloat* out[2] = {ml, ml + g.nfield};
+  c2rT<dfloat, dfloat>(c, 2, nz, c->wsB, out, (long)g.nplane, false, g.lh);
+}
+// the (0,0) modes of the saved u, v spectra (the plane means) set to zero:
+// the 3/2-grid u', v' and the vorticity fluctuations are padded from them
+__global__ void k_zero_mean_modes(C2* spec, size_t fs, size_t nk, int nz) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * nz) return;
+  const int f = t / nz, lev = t - f * nz;
+  spec[(size_t)f * fs + (size_t)lev * nk] = make_double2(0.0, 0.0);
+}
+
 // main.f90:202-478, one iteration on the device-resident state
 void rhs_swap(les_ctx* c) {
   std::swap(c->f[LES_RHSX], c->f[LES_RHSX_F]);
@@ -3590,6 +3961,7 @@ static int stepT(les_ctx* c) {
     filt_da_multi_spec(c, f3, x3, y3, 3, g.nz, c->spec);
   } else {
     filt_da_uvw_mixed(c);
+    meanflow_lin(c);
   }
   op_ddz(c, c->f[LES_DUDZ], c->f[LES_U], 1);
   op_ddz(c, c->f[LES_DVDZ], c->f[LES_V], 1);
@@ -3606,6 +3978,10 @@ static int stepT(les_ctx* c) {
   sgs_stagT<MX>(c);
   S* bigf[9];
   for (int q = 0; q < 9; ++q) bigf[q] = reinterpret_cast<S*>(c->big) + (size_t)q * g.nfield_big;
+  if (MX) {  // the mixed form pads u', v' (its linear terms use the plane means)
+    k_zero_mean_modes<<<(2 * g.nz + 127) / 128, 128, 0, c->stream>>>(c->spec, (size_t)g.nz * g.C, g.C, g.nz);
+    LES_COUNT_LAUNCH();
+  }
   padT<MX, C2>(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
   if (k.s_flag) thetaT<MX>(c, bigf);
   else fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
@@ -3613,23 +3989,33 @@ static int stepT(les_ctx* c) {
   convecT<MX>(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
   const size_t nv = g.nplane * (g.nz - 1);
   const int euler = (c->jt == 1 && !k.initu) ? 1 : 0;
-  if (MX)
-    k_rhs_ab2_32<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
+  if (MX) {
+    const dfloat* ml = mlin_fields(c);
+    const dfloat idz(1.0 / g.dz), dtd(k.dt);
+    k_rhs_ab2_mx<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)g.nz), 256, 0, c->stream>>>(
         c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
         c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL],
-        nv, g.nplane, k.dt, k.s_flag, euler);
-  else
+        ml, ml + g.nfield, f32(c, LES_DWDY), mean_tab(c), ustar_fields(c), ustar_fields(c) + g.nfield,
+        ustar_fields(c) + 2 * g.nfield, g.ld, g.ny, g.nz, make_float2(idz.hi, idz.lo),
+        make_float2(dtd.hi, dtd.lo), k.s_flag, euler);
+  } else
     k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
         c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
         c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL],
         nv, g.nplane, k.dt, k.s_flag, euler);
   LES_COUNT_LAUNCH();
-  pressT<typename std::conditional<MX, dfloat, double>::type>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
-  if (MX)
+  if (MX) {
+    const double* ust = ustar_fields(c);
+    const double* u3[3] = {ust, ust + g.nfield, ust + 2 * g.nfield};
+    pressT<dfloat>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY], u3);
     k_dpdz_project32<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)(g.nz - 1)), 256, 0, c->stream>>>(
-        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P],
-        c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, 1.0 / g.dz, k.dt);
-  else
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], u3[0], u3[1], u3[2], c->f[LES_RHSX], c->f[LES_RHSY],
+        c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz,
+        1.0 / g.dz, k.dt);
+  } else {
+    pressT<double>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
+  }
+  if (!MX)
     k_dpdz_project<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(
         c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_P],
         c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz, g.dz, k.dt);

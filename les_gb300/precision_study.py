@@ -1,10 +1,18 @@
 """Precision study: the FP32-mixed step against the FP64 step on the same
-seeded 256^3 member (active theta, x-striped z0 1e-4/1e-2 and heat flux
-0.05/0.15 K m/s), both on the GPU; every `--every` steps it reports the
-per-field relative L2 error and max-abs error relative to max|field|, and
-both forms' rmsdiv.
+seeded member (active theta, x-striped z0 1e-4/1e-2 and heat flux
+0.05/0.15 K m/s), both on the GPU.  Every `--every` steps it reports, per
+field, the relative L2 error and the share of the squared error in the
+lowest four levels, both forms' rmsdiv, and the largest first-level explicit
+SGS diffusion number Nu_t dt / dz^2 of the FP64 member.
+
+With --pert X a third member runs the FP64 step from the same state with
+every interior u, v, w value multiplied by (1 + X r), r uniform in [-1, 1]
+(X = 1e-15: a perturbation at the size of FP64 rounding), and its difference
+from the FP64 member is reported beside the mixed form's: it shows how the
+configuration itself amplifies a difference of rounding size.
 
   python -m les_gb300.precision_study [--grid 256] [--steps 500] [--every 50]
+                                      [--jt0 0] [--dt 2e-4] [--pert 1e-15]
 """
 import argparse
 import json
@@ -22,39 +30,52 @@ def main():
     # build up; a cold-started dynamic Cs^2 on the white-noise initial state
     # is unstable at 256^3 (Cs^2 up to 4, explicit SGS diffusion number > 0.2)
     ap.add_argument("--jt0", type=int, default=0)
+    ap.add_argument("--dt", type=float, default=2e-4)
+    ap.add_argument("--pert", type=float, default=0.0)
     args = ap.parse_args()
     import les_gb300 as lg
+    from les_gb300.config import splitmix64_uniform
+    n = args.grid
+    forms = [("mixed", 1, 0.0), ("fp64", 0, 0.0)]
+    if args.pert > 0:
+        forms.append(("fp64_pert", 0, args.pert))
     ctxs = {}
-    for prec in (0, 1):
+    for name, prec, pert in forms:
         # rmsdiv is read directly (les_rmsdiv) so the reference's CFL stop
         # (main.f90:455-458, CFLu > 0.1) does not end the study
-        cfg = lg.make_config(args.grid, s_flag=1, precision=prec, jt_total0=args.jt0, rmsdiv_every=0)
+        cfg = lg.make_config(n, s_flag=1, precision=prec, jt_total0=args.jt0, rmsdiv_every=0, dt=args.dt)
         surf = lg.striped_surface(cfg)
         c = lg.Context(cfg, surf)
-        for k, v in lg.initial_state(cfg, surf, seed=2024).items():
+        st = lg.initial_state(cfg, surf, seed=2024)
+        if pert > 0:
+            r = splitmix64_uniform(77, 3 * st["u"].size).reshape((3,) + st["u"].shape)
+            for q, k in enumerate("uvw"):
+                a = st[k]
+                a[:-1, :, :n] *= 1.0 + pert * (2.0 * r[q][:-1, :, :n] - 1.0)
+        for k, v in st.items():
             c.set(k, v)
-        ctxs[prec] = c
-    n = args.grid
-    rows = []
+        ctxs[name] = c
+    dz = 1.0 / n
     done = 0
     while done < args.steps:
         for c in ctxs.values():
             c.step_graph(args.every)
         done += args.every
         rec = {"step": done}
-        for nm in ("u", "v", "w", "theta", "Cs_opt2", "F_LM", "F_MM"):
-            a = ctxs[1].get(nm)[:-1, :, :n]
-            b = ctxs[0].get(nm)[:-1, :, :n]
-            d = a - b
-            rec[nm] = {"rel_l2": float(np.linalg.norm(d) / np.linalg.norm(b)),
-                       "rel_max": float(np.abs(d).max() / np.abs(b).max())}
-        vel_a = np.concatenate([ctxs[1].get(k)[:-1, :, :n].ravel() for k in "uvw"])
-        vel_b = np.concatenate([ctxs[0].get(k)[:-1, :, :n].ravel() for k in "uvw"])
-        rec["velocity_rel_l2"] = float(np.linalg.norm(vel_a - vel_b) / np.linalg.norm(vel_b))
-        rec["rmsdiv_mixed"] = ctxs[1].rmsdiv()
-        rec["rmsdiv_fp64"] = ctxs[0].rmsdiv()
-        rec["cflu"], rec["visc_stab"] = ctxs[0].timestep_conditions()
-        rows.append(rec)
+        ref = {nm: ctxs["fp64"].get(nm)[:-1, :, :n] for nm in ("u", "v", "w", "theta", "F_LM")}
+        for other in [k for k in ctxs if k != "fp64"]:
+            out = {}
+            for nm, b in ref.items():
+                d = ctxs[other].get(nm)[:-1, :, :n] - b
+                lev = (d ** 2).sum(axis=(1, 2))
+                out[nm] = {"rel_l2": float(np.linalg.norm(d) / np.linalg.norm(b)),
+                           "wall4": float(lev[:4].sum() / max(lev.sum(), 1e-300))}
+            out["rmsdiv"] = ctxs[other].rmsdiv()
+            rec[other] = out
+        rec["rmsdiv_fp64"] = ctxs["fp64"].rmsdiv()
+        rec["cflu"], rec["visc_stab"] = ctxs["fp64"].timestep_conditions()
+        nut1 = ctxs["fp64"].get("Nu_t")[0, :, :n]
+        rec["nut_dt_dz2_level1_max"] = float(nut1.max() * args.dt / dz ** 2)
         print(json.dumps(rec), flush=True)
     for c in ctxs.values():
         c.close()

@@ -7,8 +7,13 @@ members that are idle are evicted least-recently-used when room is needed.
 Every tick the scheduler launches one step of every active request, each on
 its member's own stream, so steps of different members overlap on the GPU;
 requests that arrive while others run join at the next tick (continuous
-batching, not a queue).  Step latency is measured from launch to completion
-of each step (CUDA events), request latency from arrival to completion.
+batching, not a queue).  Step latency is the device time of each step:
+CUDA events recorded on the member's stream just before and just after the
+step (it includes the time the step waits on the device behind other
+members' work); request latency runs from arrival to completion on the host
+clock.  An evicted member is spilled to host memory with its whole state
+(les_state_save) and resumed from it when it is admitted again
+(les_state_restore), so it continues exactly where it stopped.
 
 The scheduler is pure host logic and runs against an executor: GpuExecutor
 (les_gb300 contexts, graph-replayed steps) or FakeExecutor (deterministic
@@ -176,12 +181,11 @@ class Scheduler:
                 req.inflight += 1
 
     def poll(self):
-        for req, t_launch, t_done, pts in self.ex.completed():
+        for req, t_launch, t_done, pts, lat in self.ex.completed():
             req.inflight -= 1
             req.done_steps += 1
             if req.status == "cancelled":
                 continue
-            lat = t_done - t_launch
             self.metrics.step_lat.append(lat)
             self.metrics.step_lat_by_size[req.size].append(lat)
             self.metrics.pt_steps += pts
@@ -267,7 +271,7 @@ class FakeExecutor:
         self.steps[req.member] += 1
 
     def completed(self):
-        out = [(r, a, b, p) for (r, a, b, p, f) in self.inflight]
+        out = [(r, a, b, p, b - a) for (r, a, b, p, f) in self.inflight]
         self.inflight = []
         return out
 
@@ -276,10 +280,11 @@ class FakeExecutor:
 
 
 class GpuExecutor:
-    """les_gb300 contexts on the GPU; one CUDA event per launched step."""
+    """les_gb300 contexts on the GPU; two CUDA events per launched step (its
+    device time); evicted members spilled to pinned host memory."""
 
     def __init__(self, precision=1, seed0=1000, use_graphs=True, autotune=True):
-        import torch  # events on the members' streams
+        import torch  # events on the members' streams, pinned host buffers
         import les_gb300 as lg
         self.torch = torch
         self.lg = lg
@@ -290,7 +295,9 @@ class GpuExecutor:
         self.ctx = {}
         self.streams = {}
         self.inflight = collections.deque()
-        self.tuned = set()
+        self.spilled = {}      # member -> pinned host image of its whole state
+        self.spills = 0
+        self.restores = 0
 
     def config(self, size):
         nx, ny, nz = size
@@ -311,8 +318,13 @@ class GpuExecutor:
             if e.code == -3:
                 raise MemoryError(str(e))
             raise
-        for k, v in lg.initial_state(cfg, surf, seed=self.seed0 + member).items():
-            ctx.set(k, v)
+        img = self.spilled.pop(member, None)
+        if img is not None:  # resume where the member stopped
+            ctx.state_restore(img)
+            self.restores += 1
+        else:
+            for k, v in lg.initial_state(cfg, surf, seed=self.seed0 + member).items():
+                ctx.set(k, v)
         if self.autotune:
             ctx.autotune()
         self.ctx[member] = ctx
@@ -322,29 +334,37 @@ class GpuExecutor:
         ctx = self.ctx.pop(member, None)
         self.streams.pop(member, None)
         if ctx is not None:
+            nb = ctx.state_bytes()
+            buf = self.torch.empty(nb, dtype=self.torch.uint8, pin_memory=True).numpy()
+            ctx.state_save(buf)
+            self.spilled[member] = buf
+            self.spills += 1
             ctx.close()
 
     def launch(self, req, t):
         ctx = self.ctx[req.member]
+        st = self.streams[req.member]
+        e0 = self.torch.cuda.Event(enable_timing=True)
+        e1 = self.torch.cuda.Event(enable_timing=True)
+        e0.record(st)
         if self.use_graphs:
             ctx.step_graph(1)
         else:
             ctx.step(1)
-        ev = self.torch.cuda.Event()
-        ev.record(self.streams[req.member])
+        e1.record(st)
         nx, ny, nz = req.size
-        self.inflight.append((req, t, ev, nx * ny * nz))
+        self.inflight.append((req, t, e0, e1, nx * ny * nz))
 
     def completed(self):
         out = []
         now = time.perf_counter()
         keep = collections.deque()
         while self.inflight:
-            req, t, ev, pts = self.inflight.popleft()
-            if ev.query():
-                out.append((req, t, now, pts))
+            req, t, e0, e1, pts = self.inflight.popleft()
+            if e1.query():
+                out.append((req, t, now, pts, e0.elapsed_time(e1) / 1e3))
             else:
-                keep.append((req, t, ev, pts))
+                keep.append((req, t, e0, e1, pts))
         self.inflight = keep
         return out
 

@@ -146,22 +146,38 @@ def test_step_parity_32(libs, s_flag, jt0):
     assert rg < 1e-12 and ro < 1e-12 and abs(rg - ro) < 1e-13, (rg, ro)
 
 
+# The oracle's own rounding sensitivity for model 3 (32^3, theta, striped
+# surface, jt_total0 = 500, 10 steps): the oracle built with FMA contraction
+# (-ffp-contract=fast) against the oracle without it (-ffp-contract=off)
+# differs by u 1.7e-9, v 1.7e-7, w 9.8e-8 (relative L2), Cs^2 5.1e-2 and
+# rmsdiv 1.6 %.  The GPU is held to three times that measured spread.
+M3_SPREAD = {"u": 1.7e-9, "v": 1.7e-7, "w": 9.8e-8, "theta": 4.2e-16, "Cs_opt2": 5.1e-2, "rmsdiv": 1.6e-2}
+
+
 def test_step_parity_32_plane_scaledep(libs):
-    """model = 3 (scaledep_dynamic): the plane-averaged quintic for beta is
-    ill-conditioned in the reference algorithm itself; the oracle built with
-    and without FMA contraction differs by about 2e-9 in u after 10 steps, so
-    the GPU is held to that rounding sensitivity (1e-8), not 1e-12."""
+    """model = 3 (scaledep_dynamic): the plane-averaged quintic for beta
+    (sgsmodule.f90:37-59 rtnewt) is ill-conditioned in the reference
+    algorithm itself, so the GPU (plane sums in a fixed tree order, FMA
+    contraction) is held to three times the oracle's own FMA / no-FMA spread
+    (M3_SPREAD) per field, Cs^2 and rmsdiv included."""
     cfg = lg.make_config(32, s_flag=1, jt_total0=500, model=3, rmsdiv_every=1)
     surf = lg.striped_surface(cfg)
     g, o = pair(cfg, surf)
     g.step(10)
     assert o.step(10) == 0
-    for nm in ["u", "theta"]:
-        e = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
-        assert e < 1e-8, (nm, e)
-    for nm in ["v", "w"]:
-        e = rel(interior(cfg, g.get(nm), slice(None)), interior(cfg, o.get(nm), slice(None)))
-        assert e < 1e-5, (nm, e)
+    errs = {}
+    for nm in ["u", "v", "theta"]:
+        errs[nm] = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
+    errs["w"] = rel(interior(cfg, g.get("w"), slice(None)), interior(cfg, o.get("w"), slice(None)))
+    errs["Cs_opt2"] = rel(interior(cfg, g.get("Cs_opt2"), slice(None)), interior(cfg, o.get("Cs_opt2"), slice(None)))
+    rg, ro = g.rmsdiv(), o.rmsdiv()
+    errs["rmsdiv"] = abs(rg - ro) / ro
+    print("model 3 GPU vs oracle", errs)
+    for nm, e in errs.items():
+        bound = 3.0 * M3_SPREAD[nm]
+        if nm == "theta":
+            bound = TOL
+        assert e < bound, (nm, e, bound)
 
 
 def test_std_dynamic_routine(libs):
@@ -254,17 +270,71 @@ def test_step_parity_32_lagrange_ssim(libs):
     assert np.all(g.get("Beta") == 1.0)
 
 
-def test_step_parity_128_theta(libs):
-    """128^3, active theta, striped z0 and heat flux; 20 steps."""
+C2_SEED = 21
+# The oracle's own rounding sensitivity on the 128^3 workload (theta, striped
+# surface, jt_total from 0), from `python -m oracle.rounding_spread c2`: the
+# oracle built with FMA contraction against the oracle without it.  The
+# builds agree to 5e-13 up to step 50; from about step 55 the first level's
+# explicit SGS diffusion (Nu_t dt / dz^2 above the AB2 limit there) grows
+# every rounding difference until it saturates, and at step 200 they differ
+# by these relative L2 amounts (and the plane-mean u, theta profiles by
+# 5.4e-7, 2.1e-9 of max |mean|).
+C2_SPREAD_200 = {"u": 3.5e-5, "v": 4.5e-3, "w": 6.0e-3, "theta": 8.2e-8}
+C2_MEAN_SPREAD_200 = {"u": 5.4e-7, "theta": 2.1e-9}
+
+
+def _c2_pair():
     from oracle.oracle import Oracle
     cfg = lg.make_config(128, s_flag=1, rmsdiv_every=10)
     surf = lg.striped_surface(cfg)
-    g, o = pair(cfg, surf, seed=21)
+    g, o = pair(cfg, surf, seed=C2_SEED)
     Oracle.set_threads(max(1, Oracle.max_threads()))
-    g.step(20)
-    assert o.step(20) == 0
+    return cfg, g, o
+
+
+def test_step_parity_128_theta(libs):
+    """128^3 FP64, active theta, x-striped z0 (1e-4 / 1e-2) and surface heat
+    flux (0.05 / 0.15 K m/s), dt = 2e-4, from the reference's spin-up
+    (jt_total from 0: Cs^2 = 0.16^2 while the Lagrangian averages F_LM..F_NN
+    build up every cs_count steps), rmsdiv and the CFL check every 10 steps
+    (main.f90:451-458).  First 50 steps, before the first-level
+    amplification of rounding differences sets in (see C2_SPREAD_200):
+    u, v, w, theta to 1e-12; the Lagrangian averages F_LM..F_NN, which the
+    reference rounds through FP32 (lagrange_Sdep.f90:321-421), to 1e-6;
+    rmsdiv at FP64 roundoff in both.  Then on to 200 steps: every field
+    within twice the oracle's own FMA / no-FMA spread at step 200."""
+    cfg, g, o = _c2_pair()
+    g.step(50)
+    assert o.step(50) == 0
+    assert g.counters() == o.counters() == (50, 50)
     for nm in ["u", "v", "theta"]:
         e = rel(interior(cfg, g.get(nm)), interior(cfg, o.get(nm)))
         assert e < TOL, (nm, e)
     e = rel(interior(cfg, g.get("w"), slice(None)), interior(cfg, o.get("w"), slice(None)))
     assert e < TOL, ("w", e)
+    cg, co = interior(cfg, g.get("Cs_opt2"), slice(None)), interior(cfg, o.get("Cs_opt2"), slice(None))
+    assert np.array_equal(cg, co)  # the spin-up value 0.16**2 (in FP32) everywhere
+    # F_LM and F_QN are rounded through FP32 at every update; a 1-ulp FP64
+    # difference upstream flips a rounding, and the flip is then carried along
+    # the trajectories by ten interpolated updates, so these are held to a
+    # few FP32 roundings of their norm
+    for nm in ["F_LM", "F_QN", "F_MM", "F_NN"]:
+        a, b = interior(cfg, g.get(nm), slice(None)), interior(cfg, o.get(nm), slice(None))
+        assert rel(a, b) < 1e-6, (nm, rel(a, b))
+    rg, ro = g.rmsdiv(), o.rmsdiv()
+    assert rg < 1e-12 and ro < 1e-12 and abs(rg - ro) < 1e-13, (rg, ro)
+    # steps 51..200
+    g.step(150)
+    assert o.step(150) == 0
+    for nm in ["u", "v", "w", "theta"]:
+        lev = slice(None) if nm == "w" else slice(0, -1)
+        a, b = interior(cfg, g.get(nm), lev), interior(cfg, o.get(nm), lev)
+        e = rel(a, b)
+        assert e < 2.0 * C2_SPREAD_200[nm], (nm, e)
+        if nm in C2_MEAN_SPREAD_200:
+            ma, mb = a.mean(axis=(1, 2)), b.mean(axis=(1, 2))
+            em = np.abs(ma - mb).max() / np.abs(mb).max()
+            # one realisation of the amplified difference: an order of magnitude
+            assert em < 10.0 * C2_MEAN_SPREAD_200[nm], (nm, "mean profile", em)
+    rg, ro = g.rmsdiv(), o.rmsdiv()
+    assert rg < 1e-12 and ro < 1e-12 and abs(rg - ro) < 1e-13, (rg, ro)
