@@ -2,6 +2,7 @@
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|fp64]
                   [--impl ours|reference] [--grid 256] [--no-fp64] [--no-e2e] [--no-cpu]
+                  [--no-serve]
 
 Workload: 256^3 LES member (box 2pi x 2pi x 1, active theta, x-striped
 z0 = 1e-4/1e-2 and surface heat flux 0.05/0.15 K m/s in stripes of width
@@ -9,7 +10,10 @@ Nx/8, Lagrangian scale-dependent SGS, dt = 2e-4), seeded synthetic initial
 state.  A step is one call of the fused time step (main.f90:202-478) on the
 device-resident member; the headline is the FP32-mixed step, with the FP64
 step of the same member timed beside it (and the velocity error and rmsdiv
-of the mixed state after the same steps).  With N > 1 (torchrun) every rank
+of the mixed state after the same steps).  The line also carries the
+served ensemble's p50/p99 step latency (Poisson arrivals over 64 members of
+uneven sizes, les_gb300.serve_bench), each transform family's share of the
+step and HBM fraction, and the whole-step ledger.  With N > 1 (torchrun) every rank
 advances its own independent member: replicas only, no collective.
 
 `--impl reference` times the CPU restatement of the reference step (the
@@ -33,17 +37,18 @@ sys.path.insert(0, ROOT)
 METRIC = "pt-steps/s at 256³: FP32-mixed vs FP64 (≤1e-5 err); p99 ensemble step latency"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
-# Dominant kernel of each form's step (largest share of the ncu launch list
-# of the 256^3 step): the FP32 y-pass transforms (k_colsr, k_colsr_sum,
-# k_colsr_pad, k_colsf<float,...>) in the mixed form, the FP64 y-pass transforms
-# (k_cols<double,...>) in the FP64 form; les_profile_begin family ids.
-DOMINANT = {"mixed": (2, "k_colsr/k_colsr_sum/k_colsr_pad/k_colsf<float> (FP32 y-pass transforms)"),
-            "fp64": (1, "k_cols<double> (FP64 y-pass transforms)")}
+# Transform families the profiling hook (les_profile_begin) can bracket; the
+# roofline object reports the one with the largest share of the step, found
+# by a short untimed pre-pass over all four.
+FAMILIES = {1: "k_cols/k_colsf<double|dfloat> (FP64 / float-float y pass)",
+            2: "k_colsr/k_colsr_sum/k_colsr_pad/k_colsf<float> (FP32 y pass)",
+            3: "k_rows_r2c/k_rows_c2r<double|dfloat> (FP64 / float-float x pass)",
+            4: "k_r2c_reg*/k_c2r_reg*/k_rows_*<float> (FP32 x pass)"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# byte of the dominant family, from one ncu capture (1 pass) of the same
-# 256^3 run's timed launches; scales the live algorithmic bytes per launch
-# to the traffic per launch.  Only valid at 256^3.
-TRAFFIC_RATIO = {"mixed": 0.8774, "fp64": 0.9209}
+# byte of a family, from one ncu capture of that family's launches on a small
+# grid (profiles/); scales the live algorithmic bytes per launch to the
+# traffic per launch.  Only where a capture exists.
+TRAFFIC_RATIO = {("mixed", 2): 0.8774, ("fp64", 1): 0.9209}
 
 
 def parse():
@@ -62,9 +67,11 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 step timed beside the mixed one")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-serve", action="store_true", help="skip the served-ensemble latency run")
+    p.add_argument("--serve-requests", type=int, default=200)
     p.add_argument("--prof-family", type=int, default=0,
                    help="transform family for the roofline object: 1 FP64/float-float y pass, 2 FP32 y pass, "
-                        "3 FP64/float-float x pass, 4 FP32 x pass (default: the form's dominant kernel)")
+                        "3 FP64/float-float x pass, 4 FP32 x pass (default: the largest share of the step)")
     return p.parse_args()
 
 
@@ -242,6 +249,31 @@ def timed_steps(torch, lg, ctx, steps, prof_family=None):
     return ev[0].elapsed_time(ev[-1]), per, prof
 
 
+def e2e_run(torch, lg, ctx, cfg, world, ke=5):
+    """End to end through the public API: H2D of the prognostic fields from
+    pinned host buffers, one step, D2H of the prognostic fields, ke times."""
+    L = lg.lib()
+    names = ["u", "v", "w", "theta"]
+    host = {}
+    for nm in names:
+        a = torch.empty(lg.field_shape(cfg, nm), dtype=torch.float64, pin_memory=True).numpy()
+        a[...] = ctx.get(nm)
+        host[nm] = a
+    nbytes = sum(a.nbytes for a in host.values())
+    pts = cfg.nx * cfg.ny * (cfg.nz - 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        for nm in names:
+            lg.check(L.les_set_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
+        ctx.step(1)
+        for nm in names:
+            lg.check(L.les_get_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
+    dt = time.perf_counter() - t0
+    return {"value": pts * ke * world / dt, "unit": "pt-steps/s", "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes}
+
+
 def main():
     global LEVELS, MODEL
     args = parse()
@@ -275,11 +307,16 @@ def main():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
-    fam, fam_name = DOMINANT[args.form]
-    if args.prof_family:
-        fam = args.prof_family
-        fam_name = {1: "k_cols (FP64 / float-float y pass)", 2: "k_cols (FP32 y pass)",
-                    3: "k_rows (FP64 / float-float x pass)", 4: "k_rows (FP32 x pass)"}[fam]
+    cflu, visc = ctx.timestep_conditions()
+    # share of the step of each transform family (short untimed pre-pass)
+    fam_share = {}
+    for f in FAMILIES:
+        ms_f, _, pr = timed_steps(torch, lg, ctx, 5, prof_family=f)
+        if pr[0]:
+            fam_share[f] = (pr[1] / ms_f, pr[0] / 5.0, pr[2] / pr[1] / 1e6)
+    fam = args.prof_family or max(fam_share, key=lambda f: fam_share[f][0])
+    fam_name = FAMILIES[fam]
+    torch.cuda.synchronize()
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
@@ -295,37 +332,26 @@ def main():
     hbm, src = measured_peaks()
     n_l, ms_l, bytes_l = prof
     achieved = (bytes_l / n_l) / (ms_l / n_l / 1e3) / 1e9 if n_l else None
-    ratio = TRAFFIC_RATIO[args.form] if not args.prof_family else None
+    ratio = TRAFFIC_RATIO.get((args.form, fam))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm if achieved else None,
-                "traffic": (ratio * bytes_l / n_l) if (ratio and n_l and args.grid == 256 and LEVELS is None) else None,
+                "traffic": (ratio * bytes_l / n_l) if (ratio and n_l) else None,
                 "peak_source": src, "kernel": fam_name, "launches_timed": n_l,
                 "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
-                "algorithmic_bytes_per_launch": bytes_l / n_l if n_l else None}
+                "algorithmic_bytes_per_launch": bytes_l / n_l if n_l else None,
+                "share_of_step": ms_l / ms if ms else None}
+    families = {FAMILIES[f]: {"share_of_step": v[0], "launches_per_step": v[1], "achieved_gbs": v[2],
+                              "frac": v[2] / hbm} for f, v in sorted(fam_share.items())}
+    from les_gb300.ledger import bytes_per_point
+    bpp = bytes_per_point(args.form)
+    ledger = {"bytes_per_point": bpp, "gb_per_step": bpp * pts / 1e9,
+              "achieved_gbs": bpp * pts / (ms / args.steps / 1e3) / 1e9,
+              "frac": bpp * pts / (ms / args.steps / 1e3) / 1e9 / hbm,
+              "definition": "routine-interface ledger (les_gb300/ledger.py) at the form's element sizes"}
 
     e2e = None
     if not args.no_e2e:
-        # end to end through the public API: H2D of the prognostic fields from
-        # pinned host buffers, one step, D2H of the prognostic fields
-        names = ["u", "v", "w", "theta"]
-        host = {}
-        for nm in names:
-            a = torch.empty(lg.field_shape(cfg, nm), dtype=torch.float64, pin_memory=True).numpy()
-            a[...] = ctx.get(nm)
-            host[nm] = a
-        nbytes = sum(a.nbytes for a in host.values())
-        ke = 5
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            for nm in names:
-                lg.check(L.les_set_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
-            ctx.step(1)
-            for nm in names:
-                lg.check(L.les_get_field(ctx.h, lg.FIELD_ID[nm], lg._ptr(host[nm])))
-        dt = time.perf_counter() - t0
-        e2e = {"value": pts * ke * world / dt, "unit": "pt-steps/s", "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes}
+        e2e = e2e_run(torch, lg, ctx, cfg, world)
 
     compare = None
     if rank == 0 and args.form == "mixed" and not args.no_fp64:
@@ -341,17 +367,27 @@ def main():
         ms_d, per_d, _ = timed_steps(torch, lg, ctx_d, args.steps)
         ctx_m.step(args.steps)
         err = {}
-        for nm in ("u", "v", "w"):
+        for nm in ("u", "v", "w", "theta"):
             a = ctx_m.get(nm)[:-1, :, :cfg.nx]
             d = ctx_d.get(nm)[:-1, :, :cfg.nx]
-            err[nm] = (float(np.linalg.norm(a - d)), float(np.linalg.norm(d)))
-        vel = float(np.sqrt(sum(e[0] ** 2 for e in err.values())) / np.sqrt(sum(e[1] ** 2 for e in err.values())))
+            err[nm] = float(np.linalg.norm(a - d) / np.linalg.norm(d))
+        bpp_d = bytes_per_point("fp64")
         compare = {"fp64_ms_per_step": ms_d / args.steps, "fp64_value": pts * args.steps / (ms_d / 1e3),
                    "mixed_over_fp64": (pts * args.steps / (ms / 1e3)) / (pts * args.steps / (ms_d / 1e3)),
-                   "steps_compared": warm + args.steps, "velocity_rel_err": vel,
-                   "rmsdiv_mixed": ctx_m.rmsdiv()}
+                   "steps_compared": warm + args.steps, "rel_err": err,
+                   "rmsdiv_mixed": ctx_m.rmsdiv(), "rmsdiv_fp64": ctx_d.rmsdiv(),
+                   "fp64_step_ledger_frac": bpp_d * pts / (ms_d / args.steps / 1e3) / 1e9 / hbm}
         ctx_m.close()
+        if not args.no_e2e:
+            compare["fp64_e2e"] = e2e_run(torch, lg, ctx_d, cfg_d, world)
         ctx_d.close()
+    served = None
+    if rank == 0 and world == 1 and not args.no_serve:
+        try:
+            from les_gb300.serve_bench import serve
+            served = serve(requests=args.serve_requests, rate=200.0, seed=11, baseline_requests=0)
+        except Exception as ex:  # reported, never fatal
+            served = {"error": str(ex)[:200]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
@@ -365,14 +401,19 @@ def main():
                 "dtype": "f64" if args.form == "fp64" else "f32/f64-mixed",
                 "data": "synthetic (seeded SplitMix64 initial state, x-striped surface)",
                 "config": {"workload": workload_name(cfg), "grid": [cfg.nx, cfg.ny, cfg.nz - 1],
-                           "form": args.form, "dt": cfg.dt,
+                           "form": args.form, "dt": cfg.dt, "cflu": cflu, "visc_stab": visc,
+                           "cflu_note": "CFLu of the seeded state; the reference stops above 0.1 in its "
+                                        "every-500-steps check (main.f90:451-458); the in-step check is off "
+                                        "(rmsdiv_every = 0)",
                            "l2": "inputs larger than L2 (member state %.1f GB resident)"
                                  % (lg.estimate_device_bytes(cfg) / 1e9),
                            "parallelism": "replicas x%d" % world},
                 "step_latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                                     "max": float(max(per))},
+                "served_ensemble": served,
                 "fp64_comparison": compare,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": ck,
+                "roofline": roofline, "roofline_families": families, "step_ledger": ledger,
+                "cpu_baseline": cpu, "e2e": e2e, "clocks": ck,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if ctx is not None:

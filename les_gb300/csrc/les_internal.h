@@ -86,7 +86,8 @@ struct les_ctx {
   int lag_chunk = 32;
   double* dscal = nullptr;                     // device scalars / reductions
   // per-level reduction results, 36 slots of nz+8 doubles: 0 plane sums /
-  // rmsdiv partials / model-3 Cs(z); 2..11 scaledep sums; 14 theta plane
+  // rmsdiv partials / model-3 Cs(z); 2..11 scaledep sums; 12..13 timestep_conditions
+  // partial maxima; 14 theta plane
   // mean (mixed); 16..18 u, v, w plane means (mixed filt_da); 20..21 theta
   // level mean and its reciprocal (calcbeta); 24..27 partial plane sums;
   // 28..33 the mixed form's per-level mean-wind factors (float-float);

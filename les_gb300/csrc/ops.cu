@@ -2401,10 +2401,10 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
 }
 
 // Mixed form: press_stag_array.f90:192-264 + tridag_array.f90:41-101 as a
-// chunked Thomas solve in float-float arithmetic, the batched hybrid for
-// many short-latency systems: the z-recurrences of 16 modes (32 systems:
-// real and imaginary parts; a, b, c are real) run per CTA, each of the
-// eight warps on one chunk of about n/8 rows, lane = system.
+// chunked Thomas solve, the batched hybrid for many short-latency systems:
+// the z-recurrences of 16 modes (32 systems: real and imaginary parts; a, b,
+// c are real) run per CTA, each of the eight warps on one chunk of about n/8
+// rows, lane = system.
 //   forward   d_j = al_j d_{j-1} + ib_j r_j  (al_j = -a_j ib_j): each warp
 //             runs its chunk from d = 0 and keeps the chunk product
 //             A_j = al_s .. al_j; the true d_j = d~_j + A_j D_(chunk-1), with
@@ -2413,95 +2413,132 @@ __global__ void __launch_bounds__(128) k_tridiag2(const HC* __restrict__ Hx, con
 //   backward  x_j = d_j - g_(j+1) x_(j+1): the same from the top chunk down.
 // Rows stay in shared memory (66 KB of d / x and 33 KB of chunk products per
 // CTA); global memory sees each right-hand-side input, table entry and
-// p-hat value once, in 256-byte warp accesses.  The recurrence coefficients
-// are the FP64 Thomas tables rounded to float-float; modes with
-// kx^2 + ky^2 <= 4 (near-singular, nearly Neumann systems) and the (0,0)
-// mode are left to the FP64 solve (k_tridiag2 on a mode list); the Nyquist
-// modes are zeroed (press_stag_array.f90:263-264).
-constexpr int TRI_M = 16, TRI_W = 8;
+// p-hat value once, in 256-byte warp accesses, each warp keeping the loads
+// of its next four rows in flight.  The recurrences of the general modes
+// run in float-float with the FP64 Thomas tables rounded to float-float.
+// Modes with kx^2 + ky^2 <= 4 (near-singular, nearly Neumann systems) run
+// the same chunked solve in FP64 in the grid's first CTA, which also
+// integrates the kx = ky = 0 mode directly (press_stag_array.f90:238-247,
+// a prefix sum over the levels, by one warp); the Nyquist modes are zeroed
+// (press_stag_array.f90:263-264).
+constexpr int TRI_M = 16, TRI_W = 8, TRI_D = 4;
 constexpr int TRI_K2LOW = 4;  // modes with kx^2 + ky^2 <= 4 (integer indices) stay FP64
 __device__ __forceinline__ dfloat ldff(const float2* p, size_t i) {
   const float2 v = p[i];
   return dfloat(v.x, v.y);
 }
-__global__ void __launch_bounds__(TRI_W * 32) k_tridiag_ffc(const dcomplex* __restrict__ Hx,
-                                                            const dcomplex* __restrict__ Hy,
-                                                            const dcomplex* __restrict__ Hz,
-                                                            const C2* __restrict__ bot, const C2* __restrict__ top,
-                                                            dcomplex* P, const float2* __restrict__ ibd,
-                                                            const float2* __restrict__ gad,
-                                                            const float2* __restrict__ kxd,
-                                                            const float2* __restrict__ kyd,
-                                                            int lh, int ny, int nz, float2 idz2, float2 a2,
-                                                            float2 dz2, int k2low) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int n = nz + 1;
-  dfloat* D = reinterpret_cast<dfloat*>(smraw);            // (n + 1) x 32: d~, d, then x~, x
-  dfloat* A = D + (size_t)(n + 1) * 32;                     // (n + 1) x 16: chunk products
-  dfloat* ce = A + (size_t)(n + 1) * TRI_M;                 // TRI_W x 32: chunk-end d~ / chunk-start x~
-  dfloat* cp = ce + TRI_W * 32;                             // TRI_W x 32: their chunk products
-  dfloat* cc = cp + TRI_W * 32;                             // TRI_W x 32: carries into each chunk
-  const int nk = lh * ny;
+struct TriArgs {
+  const float *Hx, *Hy, *Hz;         // float-float complex spectra (4 floats per mode)
+  const C2 *bot, *top;               // wall and lid planes (FP64)
+  float* P;                          // p-hat, float-float complex
+  const float2 *ibd, *gad, *kxd, *kyd;  // float-float tables
+  const double *ib, *gm, *kx, *ky;   // FP64 tables
+  const int* low;                    // the FP64 modes
+  int nlow, nk, lh, ny, nz;
+  float2 idz2, a2, dz2;
+  double dz;
+};
+template <typename R> __device__ __forceinline__ R tri_h(const float* H, size_t e, int cmp) {
+  const float2 v = *reinterpret_cast<const float2*>(H + 4 * e + 2 * cmp);
+  if constexpr (std::is_same<R, dfloat>::value) return dfloat(v.x, v.y);
+  else return cvt<double>(dfloat(v.x, v.y));
+}
+template <typename R> __device__ __forceinline__ R tri_tab(const float2* f, const double* d, size_t i) {
+  if constexpr (std::is_same<R, dfloat>::value) return ldff(f, i);
+  else return d[i];
+}
+template <typename R> __device__ __forceinline__ R tri_cst(float2 f, double d) {
+  if constexpr (std::is_same<R, dfloat>::value) return dfloat(f.x, f.y);
+  else return d;
+}
+template <typename R> __device__ __forceinline__ R tri_of(double x) {
+  if constexpr (std::is_same<R, dfloat>::value) return cvt<dfloat>(x);
+  else return x;
+}
+__device__ __forceinline__ float2 tri_ff(dfloat v) { return make_float2(v.hi, v.lo); }
+__device__ __forceinline__ float2 tri_ff(double v) {
+  const dfloat d = cvt<dfloat>(v);
+  return make_float2(d.hi, d.lo);
+}
+// One CTA's 32 systems: lane = 2 * (mode slot) + component; mode t, `act`
+// false for lanes without a system; `wr` lanes store their p-hat rows
+// (zero where not act).  Called by every thread of the CTA.
+template <typename R>
+__device__ __forceinline__ void tri_chunk(const TriArgs& A, int t, bool act, bool wr, unsigned char* smraw) {
+  const int nz = A.nz, n = nz + 1;
+  R* D = reinterpret_cast<R*>(smraw);            // (n + 1) x 32: d~, d, then x~, x
+  R* Pr = D + (size_t)(n + 1) * 32;              // (n + 1) x 16: chunk products
+  R* ce = Pr + (size_t)(n + 1) * TRI_M;          // TRI_W x 32: chunk-end d~ / chunk-start x~
+  R* cp = ce + TRI_W * 32;                       // TRI_W x 32: their chunk products
+  R* cc = cp + TRI_W * 32;                       // TRI_W x 32: carries into each chunk
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = blockIdx.x * TRI_M + (lane >> 1), comp = lane & 1;
-  const int jx = t % lh, jy = t / lh;
-  const bool inb = t < nk;
-  const bool nyq = inb && (jy == ny / 2 || jx == lh - 1);
-  const int my = jy <= ny / 2 ? jy : jy - ny;  // wrapped ky index
-  const bool low = inb && !nyq && jx * jx + my * my <= k2low;  // includes (0,0): solved in FP64
-  const bool act = inb && !nyq && !low;
-  const size_t NK = (size_t)nk;
+  const int m = lane >> 1, comp = lane & 1;
+  const size_t NK = (size_t)A.nk;
   const int L = (n + TRI_W - 1) / TRI_W;
   const int s0 = 1 + warp * L, e0 = min(n, (warp + 1) * L);  // rows of this warp's chunk (may be empty)
-  const dfloat idz(idz2.x, idz2.y), a(a2.x, a2.y), dz(dz2.x, dz2.y);
-  const dfloat zero(0.f, 0.f), one(1.f, 0.f);
+  const R zero = tri_cst<R>(make_float2(0.f, 0.f), 0.0), one = tri_cst<R>(make_float2(1.f, 0.f), 1.0);
+  const R idz = tri_cst<R>(A.idz2, 1.0 / A.dz), a = tri_cst<R>(A.a2, 1.0 / (A.dz * A.dz));
+  const R dz = tri_cst<R>(A.dz2, A.dz);
   const int ch = comp == 0 ? 1 : 0;  // component of Hx, Hy feeding this system
-  const float* Hxf = reinterpret_cast<const float*>(Hx);
-  const float* Hyf = reinterpret_cast<const float*>(Hy);
-  const float* Hzf = reinterpret_cast<const float*>(Hz);
-  auto ldh = [&](const float* H, size_t e, int cmp) -> dfloat {  // component cmp of element e
-    const float2 v = *reinterpret_cast<const float2*>(H + 4 * e + 2 * cmp);
-    return dfloat(v.x, v.y);
-  };
-  // ---- forward, local to the chunk
-  dfloat d = zero, Ap = one;
-  if (act && s0 <= e0) {
-    const dfloat k_x = ldff(kxd, t), k_y = ldff(kyd, t);
-    dfloat hz0 = zero;
-    if (s0 >= 2 && s0 <= nz) hz0 = ldh(Hzf, (size_t)(s0 - 2) * NK + t, comp);  // Hz of row s0 - 1 (levels 1..nz-1)
-    for (int j = s0; j <= e0; ++j) {
-      const dfloat ib = ldff(ibd, (size_t)(j - 1) * NK + t);
-      dfloat r, al;
-      if (j == 1) {
-        const C2 b1 = bot[t];
-        r = -(dz * cvt<dfloat>(comp == 0 ? b1.x : b1.y));
-        al = zero;
-        hz0 = ldh(Hzf, t, comp);
-      } else if (j <= nz) {
-        const dfloat hx = ldh(Hxf, (size_t)(j - 2) * NK + t, ch);
-        const dfloat hy = ldh(Hyf, (size_t)(j - 2) * NK + t, ch);
-        const dfloat hz1 = (j <= nz - 1) ? ldh(Hzf, (size_t)(j - 1) * NK + t, comp) : zero;
-        const dfloat sxy = k_x * hx + k_y * hy;
-        const dfloat dh = (hz1 - hz0) * idz;
-        r = comp == 0 ? dh - sxy : sxy + dh;
-        hz0 = hz1;
-        al = -(a * ib);
-      } else {  // row n: a = -1, r = -dz top
-        const C2 tp = top[t];
-        r = -(dz * cvt<dfloat>(comp == 0 ? tp.x : tp.y));
-        al = ib;
+  const bool run = act && s0 <= e0;
+  // ---- forward, local to the chunk; row j's inputs in ring slot (j - s0) % TRI_D
+  R d = zero, Ap = one;
+  if (run) {
+    const R k_x = tri_tab<R>(A.kxd, A.kx, t), k_y = tri_tab<R>(A.kyd, A.ky, t);
+    R hz0 = zero;
+    if (s0 >= 2 && s0 <= nz) hz0 = tri_h<R>(A.Hz, (size_t)(s0 - 2) * NK + t, comp);  // Hz of row s0 - 1
+    R bx[TRI_D], by[TRI_D], bz[TRI_D], bi[TRI_D];
+    auto load = [&](int j, R& x, R& y, R& z, R& ib) {
+      if (j > e0) return;
+      ib = tri_tab<R>(A.ibd, A.ib, (size_t)(j - 1) * NK + t);
+      if (j >= 2 && j <= nz) {
+        x = tri_h<R>(A.Hx, (size_t)(j - 2) * NK + t, ch);
+        y = tri_h<R>(A.Hy, (size_t)(j - 2) * NK + t, ch);
+        z = (j <= nz - 1) ? tri_h<R>(A.Hz, (size_t)(j - 1) * NK + t, comp) : zero;
       }
-      d = al * d + ib * r;
-      Ap = al * Ap;
-      D[(size_t)j * 32 + lane] = d;
-      if (comp == 0) A[(size_t)j * TRI_M + (lane >> 1)] = Ap;
+    };
+#pragma unroll
+    for (int q = 0; q < TRI_D; ++q) {
+      bx[q] = zero; by[q] = zero; bz[q] = zero; bi[q] = zero;
+      load(s0 + q, bx[q], by[q], bz[q], bi[q]);
+    }
+    for (int jb = s0; jb <= e0; jb += TRI_D) {
+#pragma unroll
+      for (int q = 0; q < TRI_D; ++q) {
+        const int j = jb + q;
+        if (j <= e0) {
+          const R hx = bx[q], hy = by[q], hz1 = bz[q], ib = bi[q];
+          load(j + TRI_D, bx[q], by[q], bz[q], bi[q]);
+          R r, al;
+          if (j == 1) {
+            const C2 b1 = A.bot[t];
+            r = -(dz * tri_of<R>(comp == 0 ? b1.x : b1.y));
+            al = zero;
+            hz0 = tri_h<R>(A.Hz, t, comp);
+          } else if (j <= nz) {
+            const R sxy = k_x * hx + k_y * hy;
+            const R dh = (hz1 - hz0) * idz;
+            r = comp == 0 ? dh - sxy : sxy + dh;
+            hz0 = hz1;
+            al = -(a * ib);
+          } else {  // row n: a = -1, r = -dz top
+            const C2 tp = A.top[t];
+            r = -(dz * tri_of<R>(comp == 0 ? tp.x : tp.y));
+            al = ib;
+          }
+          d = al * d + ib * r;
+          Ap = al * Ap;
+          D[(size_t)j * 32 + lane] = d;
+          if (comp == 0) Pr[(size_t)j * TRI_M + m] = Ap;
+        }
+      }
     }
   }
   ce[warp * 32 + lane] = d;
   cp[warp * 32 + lane] = Ap;
   __syncthreads();
   if (warp == 0) {  // chunk boundaries: D_w = d~_end(w) + A_end(w) D_(w-1)
-    dfloat Dw = ce[lane];
+    R Dw = ce[lane];
     cc[lane] = zero;
     for (int w = 1; w < TRI_W; ++w) {
       cc[w * 32 + lane] = Dw;
@@ -2510,46 +2547,114 @@ __global__ void __launch_bounds__(TRI_W * 32) k_tridiag_ffc(const dcomplex* __re
   }
   __syncthreads();
   // ---- fix-up of d, then backward, local to the chunk
-  dfloat x = zero, Bp = one;
-  const bool run = act && s0 <= e0;
+  R x = zero, Bp = one;
   if (run && warp > 0) {
-    const dfloat Din = cc[warp * 32 + lane];
+    const R Din = cc[warp * 32 + lane];
     for (int j = s0; j <= e0; ++j) {
       const size_t q = (size_t)j * 32 + lane;
-      D[q] = D[q] + A[(size_t)j * TRI_M + (lane >> 1)] * Din;
+      D[q] = D[q] + Pr[(size_t)j * TRI_M + m] * Din;
     }
   }
-  __syncwarp();  // (every lane) the fix-up has read A before the backward products replace it
+  __syncwarp();  // (every lane) the fix-up has read Pr before the backward products replace it
   if (run) {
-    for (int j = e0; j >= s0; --j) {
-      const size_t q = (size_t)j * 32 + lane;
-      dfloat gm = zero;
-      if (j < n) gm = ldff(gad, (size_t)j * NK + t);  // g_(j+1)
-      x = D[q] - gm * x;
-      Bp = (j < n) ? -(gm * Bp) : zero;  // B_j; the top row has no carry from above
-      D[q] = x;
-      if (comp == 0) A[(size_t)j * TRI_M + (lane >> 1)] = Bp;
+    R bg[TRI_D];
+    auto loadg = [&](int j, R& g) {
+      if (j >= s0 && j < n) g = tri_tab<R>(A.gad, A.gm, (size_t)j * NK + t);  // g_(j+1)
+    };
+#pragma unroll
+    for (int q = 0; q < TRI_D; ++q) {
+      bg[q] = zero;
+      loadg(e0 - q, bg[q]);
+    }
+    for (int jb = e0; jb >= s0; jb -= TRI_D) {
+#pragma unroll
+      for (int q = 0; q < TRI_D; ++q) {
+        const int j = jb - q;
+        if (j >= s0) {
+          const R gm = (j < n) ? bg[q] : zero;
+          loadg(j - TRI_D, bg[q]);
+          const size_t qq = (size_t)j * 32 + lane;
+          x = D[qq] - gm * x;
+          Bp = (j < n) ? -(gm * Bp) : zero;  // B_j; the top row has no carry from above
+          D[qq] = x;
+          if (comp == 0) Pr[(size_t)j * TRI_M + m] = Bp;
+        }
+      }
     }
   }
   ce[warp * 32 + lane] = x;
   cp[warp * 32 + lane] = Bp;
   __syncthreads();
   if (warp == 0) {  // from the top chunk down: X_w = x~_start(w) + B_start(w) X_(w+1)
-    dfloat Xw = zero;
+    R Xw = zero;
     for (int w = TRI_W - 1; w >= 0; --w) {
       cc[w * 32 + lane] = Xw;
       Xw = ce[w * 32 + lane] + cp[w * 32 + lane] * Xw;
     }
   }
   __syncthreads();
-  if (!inb || low || s0 > e0) return;
-  float* Pf = reinterpret_cast<float*>(P);
-  const dfloat Xin = cc[warp * 32 + lane];
+  if (!wr || s0 > e0) return;
+  const R Xin = cc[warp * 32 + lane];
   for (int j = s0; j <= e0; ++j) {
-    dfloat v = zero;
-    if (act) v = D[(size_t)j * 32 + lane] + A[(size_t)j * TRI_M + (lane >> 1)] * Xin;
-    *reinterpret_cast<float2*>(Pf + 4 * ((size_t)(j - 1) * NK + t) + 2 * comp) = make_float2(v.hi, v.lo);
+    R v = zero;
+    if (act) v = D[(size_t)j * 32 + lane] + Pr[(size_t)j * TRI_M + m] * Xin;
+    *reinterpret_cast<float2*>(A.P + 4 * ((size_t)(j - 1) * NK + t) + 2 * comp) = tri_ff(v);
   }
+}
+// grid 1 + ceil(nk / 16): CTA 0 the FP64 modes, CTA b > 0 the modes
+// 16 (b - 1) .. 16 b - 1 in float-float (skipping the FP64 ones)
+__global__ void __launch_bounds__(TRI_W * 32) k_tridiag_chunk(TriArgs A, int k2low) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31;
+  if (blockIdx.x == 0) {
+    const int s = lane >> 1;
+    const int t = s < A.nlow ? A.low[s] : 0;
+    const bool act = s < A.nlow && t != 0;
+    tri_chunk<double>(A, t, act, act, smraw);
+    if (threadIdx.x >= 32) return;
+    // kx = ky = 0: p(0) = 0, p(1) = -dz bottom, p(jz) = p(jz-1) + dz Hz(jz) for
+    // jz = 2..nz (Hz = 0 at jz = nz); each lane sums a run of levels, then a
+    // warp scan of the run sums
+    const int nz = A.nz, cnt = nz - 1;
+    const int per = (cnt + 31) / 32;
+    const int j0 = 2 + lane * per, j1 = min(nz, j0 + per - 1);
+    const C2 b = A.bot[0];
+    const double p1x = -A.dz * b.x, p1y = -A.dz * b.y;
+    double sx = 0.0, sy = 0.0;
+    for (int jz = j0; jz <= j1; ++jz) {
+      if (jz <= nz - 1) {
+        sx += tri_h<double>(A.Hz, (size_t)(jz - 1) * A.nk, 0) * A.dz;
+        sy += tri_h<double>(A.Hz, (size_t)(jz - 1) * A.nk, 1) * A.dz;
+      }
+    }
+    double ix = sx, iy = sy;  // inclusive scan over lanes
+    for (int o = 1; o < 32; o <<= 1) {
+      const double ux = __shfl_up_sync(0xffffffffu, ix, o), uy = __shfl_up_sync(0xffffffffu, iy, o);
+      if (lane >= o) { ix += ux; iy += uy; }
+    }
+    double px = p1x + (ix - sx), py = p1y + (iy - sy);
+    float2* P2 = reinterpret_cast<float2*>(A.P);
+    if (lane == 0) {
+      P2[0] = make_float2(0.f, 0.f); P2[1] = make_float2(0.f, 0.f);
+      P2[2 * (size_t)A.nk] = tri_ff(p1x); P2[2 * (size_t)A.nk + 1] = tri_ff(p1y);
+    }
+    for (int jz = j0; jz <= j1; ++jz) {
+      if (jz <= nz - 1) {
+        px += tri_h<double>(A.Hz, (size_t)(jz - 1) * A.nk, 0) * A.dz;
+        py += tri_h<double>(A.Hz, (size_t)(jz - 1) * A.nk, 1) * A.dz;
+      }
+      P2[2 * (size_t)jz * A.nk] = tri_ff(px);
+      P2[2 * (size_t)jz * A.nk + 1] = tri_ff(py);
+    }
+    return;
+  }
+  const int t = (blockIdx.x - 1) * TRI_M + (lane >> 1);
+  const int jx = t % A.lh, jy = t / A.lh;
+  const bool inb = t < A.nk;
+  const bool nyq = inb && (jy == A.ny / 2 || jx == A.lh - 1);
+  const int my = jy <= A.ny / 2 ? jy : jy - A.ny;  // wrapped ky index
+  const bool low = inb && !nyq && jx * jx + my * my <= k2low;  // includes (0,0): CTA 0 solves them
+  tri_chunk<dfloat>(A, inb ? t : 0, inb && !nyq && !low, inb && !low, smraw);
 }
 
 // Thomas coefficients of press_stag_array.f90:144-210 for every (kx,ky):
@@ -2654,21 +2759,33 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const doubl
   const CX* Hy = H + (size_t)(nz - 1) * g.C;
   const CX* Hz = H + (size_t)2 * (nz - 1) * g.C;
   if constexpr (std::is_same<T, dfloat>::value) {
-    // chunked float-float Thomas for |k|^2 > TRI_K2LOW, FP64 Thomas for the rest
+    // chunked float-float Thomas for |k|^2 > TRI_K2LOW, chunked FP64 Thomas for the rest
     const size_t sm = ((size_t)(nz + 2) * (32 + TRI_M) + 3 * TRI_W * 32) * sizeof(dfloat);
+    if (sm > 227 * 1024) {
+      les_set_error("pressure solve: %d levels exceed the shared-memory row buffer", nz);
+      return LES_ERR_UNSUPPORTED;
+    }
     static size_t sm_set = 48 * 1024;
     if (sm > sm_set) {
-      cudaFuncSetAttribute(k_tridiag_ffc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      LES_CUDA_CHECK(cudaFuncSetAttribute(k_tridiag_chunk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       sm_set = sm;
     }
+    if (c->nlow > TRI_M) { les_set_error("too many FP64 pressure modes (%d)", c->nlow); return LES_ERR_STATE; }
     const dfloat idz(1.0 / g.dz), a2(1.0 / (g.dz * g.dz)), dz2(g.dz);
-    k_tridiag_ffc<<<(g.lh * g.ny + TRI_M - 1) / TRI_M, TRI_W * 32, sm, c->stream>>>(
-        Hx, Hy, Hz, BT, BT + g.C, P, c->ibet_ff, c->gamt_ff, c->kxd, c->kyd, g.lh, g.ny, nz,
-        make_float2(idz.hi, idz.lo), make_float2(a2.hi, a2.lo), make_float2(dz2.hi, dz2.lo), TRI_K2LOW);
+    TriArgs A;
+    A.Hx = reinterpret_cast<const float*>(Hx);
+    A.Hy = reinterpret_cast<const float*>(Hy);
+    A.Hz = reinterpret_cast<const float*>(Hz);
+    A.bot = BT; A.top = BT + g.C;
+    A.P = reinterpret_cast<float*>(P);
+    A.ibd = c->ibet_ff; A.gad = c->gamt_ff; A.kxd = c->kxd; A.kyd = c->kyd;
+    A.ib = c->ibet; A.gm = c->gamt; A.kx = c->kx; A.ky = c->ky;
+    A.low = c->lowmodes; A.nlow = c->nlow;
+    A.nk = g.lh * g.ny; A.lh = g.lh; A.ny = g.ny; A.nz = nz;
+    A.idz2 = make_float2(idz.hi, idz.lo); A.a2 = make_float2(a2.hi, a2.lo); A.dz2 = make_float2(dz2.hi, dz2.lo);
+    A.dz = g.dz;
+    k_tridiag_chunk<<<1 + (g.lh * g.ny + TRI_M - 1) / TRI_M, TRI_W * 32, sm, c->stream>>>(A, TRI_K2LOW);
     LES_COUNT_LAUNCH();
-    k_tridiag2<CX, PCX><<<(2 * c->nlow + 127) / 128, 128, 0, c->stream>>>(
-        Hx, Hy, Hz, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz,
-        c->lowmodes, c->nlow); LES_COUNT_LAUNCH();
   } else {
     k_tridiag2<CX, PCX><<<(2 * g.lh * g.ny + 127) / 128, 128, 0, c->stream>>>(
         Hx, Hy, Hz, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz,
@@ -3042,39 +3159,54 @@ int op_rmsdiv(les_ctx* c, double* out_dev) {
   k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev); LES_COUNT_LAUNCH();
   return 0;
 }
+// timestep_conditions maxima: one block per level reduces max |u|^2 and
+// max Nu_t over its plane, then one warp reduces the per-level partials
 template <typename NT>
-__global__ void __launch_bounds__(512) k_tsc(const double* __restrict__ u, const double* __restrict__ v,
-                                             const double* __restrict__ w, const NT* __restrict__ nut,
-                                             double* out, int ld, int nx, int ny, int nz) {
-  __shared__ double s1[512], s2[512];
+__global__ void __launch_bounds__(512) k_tsc_part(const double* __restrict__ u, const double* __restrict__ v,
+                                                  const double* __restrict__ w, const NT* __restrict__ nut,
+                                                  double* part1, double* part2, int ld, int nx, int ny) {
+  __shared__ double s1[16], s2[16];
   double m1 = -1e300, m2 = -1e300;
-  const size_t n = (size_t)nx * ny * (nz - 1);
-  for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
-    const size_t jx = e % nx, r = e / nx;
-    const size_t i = jx + (size_t)ld * r;
+  const size_t base = (size_t)ld * ny * blockIdx.x;
+  const int n = nx * ny;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const size_t i = base + (size_t)(e % nx) + (size_t)ld * (e / nx);
     m1 = fmax(m1, u[i] * u[i] + v[i] * v[i] + w[i] * w[i]);
     m2 = fmax(m2, cvt<double, NT>(nut[i]));
   }
-  s1[threadIdx.x] = m1; s2[threadIdx.x] = m2;
-  __syncthreads();
-  for (int k = 256; k > 0; k >>= 1) {
-    if (threadIdx.x < k) {
-      s1[threadIdx.x] = fmax(s1[threadIdx.x], s1[threadIdx.x + k]);
-      s2[threadIdx.x] = fmax(s2[threadIdx.x], s2[threadIdx.x + k]);
-    }
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
   }
-  if (threadIdx.x == 0) { out[0] = s1[0]; out[1] = s2[0]; }
+  if ((threadIdx.x & 31) == 0) { s1[threadIdx.x >> 5] = m1; s2[threadIdx.x >> 5] = m2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { m1 = fmax(m1, s1[k]); m2 = fmax(m2, s2[k]); }
+    part1[blockIdx.x] = m1;
+    part2[blockIdx.x] = m2;
+  }
+}
+__global__ void k_tsc_fin(const double* part1, const double* part2, int n, double* out) {
+  double m1 = -1e300, m2 = -1e300;
+  for (int k = threadIdx.x; k < n; k += 32) { m1 = fmax(m1, part1[k]); m2 = fmax(m2, part2[k]); }
+  for (int o = 16; o > 0; o >>= 1) {
+    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+  }
+  if (threadIdx.x == 0) { out[0] = m1; out[1] = m2; }
 }
 int op_tsc(les_ctx* c, double* cflu, double* visc) {
   const Grid& g = c->g;
+  double* p1 = c->dred + 12 * (size_t)(g.nz + 8);  // slots 12, 13
+  double* p2 = c->dred + 13 * (size_t)(g.nz + 8);
   if (c->cfg.precision == 1)
-    k_tsc<float><<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], f32(c, LES_NU_T), c->dscal + 2,
-                                           g.ld, g.nx, g.ny, g.nz);
+    k_tsc_part<float><<<g.nz - 1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], f32(c, LES_NU_T),
+                                                       p1, p2, g.ld, g.nx, g.ny);
   else
-    k_tsc<double><<<1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_NU_T], c->dscal + 2,
-                                            g.ld, g.nx, g.ny, g.nz);
+    k_tsc_part<double><<<g.nz - 1, 512, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_NU_T],
+                                                        p1, p2, g.ld, g.nx, g.ny);
   LES_COUNT_LAUNCH();
+  k_tsc_fin<<<1, 32, 0, c->stream>>>(p1, p2, g.nz - 1, c->dscal + 2); LES_COUNT_LAUNCH();
   LES_CUDA_CHECK(cudaMemcpyAsync(c->host_scal + 2, c->dscal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
   const double delta = std::min(g.dx, g.dy);

@@ -13,19 +13,14 @@ import json
 import time
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--requests", type=int, default=200)
-    ap.add_argument("--rate", type=float, default=200.0)
-    ap.add_argument("--seed", type=int, default=11)
-    ap.add_argument("--budget-gb", type=float, default=0.0, help="0: 90%% of free device memory")
-    ap.add_argument("--baseline-requests", type=int, default=60)
-    args = ap.parse_args()
+def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60):
+    """Serve one Poisson trace; returns the summary (and, when
+    baseline_requests > 0, the unbatched FP64 baseline on its prefix)."""
     import torch
     from les_gb300.serve import GpuExecutor, Scheduler, poisson_trace
     free, total = torch.cuda.mem_get_info()
-    budget = int(args.budget_gb * 2 ** 30) if args.budget_gb > 0 else int(0.9 * free)
-    trace = poisson_trace(args.requests, args.rate, args.seed)
+    budget = int(budget_gb * 2 ** 30) if budget_gb > 0 else int(0.9 * free)
+    trace = poisson_trace(requests, rate, seed)
     ex = GpuExecutor(precision=1, autotune=True)
     sched = Scheduler(ex, budget_bytes=budget)
     summary, wall = sched.run(trace)
@@ -34,25 +29,42 @@ def main():
         status[r.status] = status.get(r.status, 0) + 1
     for m in list(ex.ctx):
         ex.evict(m)
-    # unbatched FP64 baseline on a prefix of the same trace
-    base = GpuExecutor(precision=0, autotune=False, use_graphs=False)
-    nb = min(args.baseline_requests, len(trace))
-    pts = 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for r in trace[:nb]:
-        if r.member not in base.ctx:
-            base.load(r.member, r.size)
-        base.ctx[r.member].step(r.nsteps)
-        base.ctx[r.member].synchronize()
-        nx, ny, nz = r.size
-        pts += nx * ny * nz * r.nsteps
-    tb = time.perf_counter() - t0
-    out = {"requests": len(trace), "rate_per_s": args.rate, "wall_s": wall, "status": status,
-           "budget_gb": budget / 2 ** 30, "serving": summary,
-           "fp64_unbatched_pt_steps_per_s": pts / tb, "fp64_unbatched_requests": nb}
-    out["speedup_vs_fp64_unbatched"] = summary["pt_steps_per_s"] / out["fp64_unbatched_pt_steps_per_s"]
-    print(json.dumps(out))
+    out = {"requests": len(trace), "rate_per_s": rate, "wall_s": wall, "status": status,
+           "budget_gb": budget / 2 ** 30, "serving": summary}
+    if summary.get("step_p50_ms"):
+        out["step_p99_over_p50"] = summary["step_p99_ms"] / summary["step_p50_ms"]
+    if baseline_requests > 0:
+        # unbatched FP64 baseline on a prefix of the same trace
+        base = GpuExecutor(precision=0, autotune=False, use_graphs=False)
+        nb = min(baseline_requests, len(trace))
+        pts = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for r in trace[:nb]:
+            if r.member not in base.ctx:
+                base.load(r.member, r.size)
+            base.ctx[r.member].step(r.nsteps)
+            base.ctx[r.member].synchronize()
+            nx, ny, nz = r.size
+            pts += nx * ny * nz * r.nsteps
+        tb = time.perf_counter() - t0
+        for m in list(base.ctx):
+            base.evict(m)
+        out["fp64_unbatched_pt_steps_per_s"] = pts / tb
+        out["fp64_unbatched_requests"] = nb
+        out["speedup_vs_fp64_unbatched"] = summary["pt_steps_per_s"] / out["fp64_unbatched_pt_steps_per_s"]
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--budget-gb", type=float, default=0.0, help="0: 90%% of free device memory")
+    ap.add_argument("--baseline-requests", type=int, default=60)
+    args = ap.parse_args()
+    print(json.dumps(serve(args.requests, args.rate, args.seed, args.budget_gb, args.baseline_requests)))
 
 
 if __name__ == "__main__":
