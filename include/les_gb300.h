@@ -63,7 +63,9 @@ typedef struct les_config {
   int jt_total0;        /* total_time.dat (param.f90:203-214) step offset        */
   int precision;        /* 0 = FP64 throughout, 1 = FP32-mixed form             */
   int rmsdiv_every;     /* main.f90:451   rmsdiv/CFL diagnostic period (500)    */
-  int reserved0;
+  int q_flag;           /* main.f90:274   1 = humidity qmix (scalars_module_q.f90)
+                                          advanced after theta; needs s_flag.
+                                          0 = qmix identically zero (not stored) */
   double l_x, l_y;      /* param.f90:62   horizontal box (nondimensional)       */
   double lz_over_zi;    /* param.f90:63   L_z / z_i                             */
   double z_i;           /* param.f90:63   [m]                                   */
@@ -74,6 +76,8 @@ typedef struct les_config {
   double dtdz_top;      /* param.f90:81   [K/m]                                 */
   double pr;            /* param.f90:53   SGS Prandtl number                    */
   double g;             /* param.f90:177  [m/s^2]                               */
+  double q_scale;       /* param.f90:85   humidity scale [g/kg]                 */
+  double dqdz_top;      /* param.f90:83   humidity gradient at the lid [g/kg/m] */
 } les_config;
 
 /* State arrays that mirror the reference's module arrays (sim_param.f90:18-38,
@@ -91,9 +95,13 @@ typedef enum les_field {
   LES_U_LAG, LES_V_LAG, LES_W_LAG,
   LES_RHS_T, LES_RHS_TF, LES_BETA_SCAL, LES_DTDX, LES_DTDY, LES_DTDZ,
   LES_S11, LES_S12, LES_S13, LES_S22, LES_S23, LES_S33,   /* calc_Sij output */
+  /* humidity (scalars_module_q.f90:17-27; stored only when q_flag = 1) */
+  LES_Q, LES_RHS_Q, LES_RHS_QF, LES_DQDX, LES_DQDY, LES_DQDZ,
   /* surface planes (nx,ny) */
   LES_ZO, LES_WT_S, LES_USTAR_AVG, LES_PHI_M, LES_PSI_M, LES_PSI_M0,
   LES_PHI_H, LES_PSI_H, LES_PSI_H0, LES_SGS_T3_SFC,
+  LES_WQ_S,              /* bottombc.f90:15 surface moisture flux [g/kg m/s] (q_flag) */
+  LES_SGS_Q3_SFC,        /* scalars_module_q.f90:23 sgs_q3(:,:,1) (q_flag)          */
   LES_NUM_FIELDS
 } les_field;
 
@@ -172,8 +180,8 @@ int les_state_restore(les_ctx* ctx, const void* host, size_t bytes);
  *   Cs_opt2, F_LM, F_MM, F_QN, F_NN, G_LM, G_MM, G_QN, G_NN, Pr_t (ld,ny,nz);
  * without scalars u, v, w, RHSx, RHSy, RHSz, Cs_opt2, F_LM, F_MM, F_QN, F_NN.
  * Arrays this build does not carry are written as a model-5 run of the
- * reference holds them (qmix, RHS_q, sgs_q3 and G_* zero, Pr_t = Pr) and
- * skipped on reading.  les_checkpoint_read takes only a record of exactly
+ * reference holds them (G_* zero, Pr_t = Pr; qmix, RHS_q and sgs_q3 zero when
+ * q_flag = 0, the context's arrays when q_flag = 1) and skipped on reading.  les_checkpoint_read takes only a record of exactly
  * its configuration's list (returning LES_ERR_IO, with no field changed,
  * for any other length).  The record keeps no step counters (the reference keeps
  * jt_total in total_time.dat): a restart creates its context with
@@ -337,6 +345,26 @@ int les_wallstress(les_ctx* ctx);
 int les_obukhov(les_ctx* ctx);
 int les_project(les_ctx* ctx);
 int les_theta_all_in_one(les_ctx* ctx);
+/* scalars_module_q.f90:31-141 q_all_in_one (filt_da and ddz_uv of qmix, the
+ * lid gradient dqdz_top, scalar_q_RHS_calc :145-367, step_scalar_q :370-397)
+ * on the context's module state; needs q_flag = 1 (else LES_ERR_STATE) and a
+ * precision-0 context.  In les_step it runs after theta_all_in_one
+ * (main.f90:273-274); qmix also enters calcbeta's virtual temperature
+ * (scalars_module.f90:200-223) and obukhov's buoyancy flux
+ * (scalars_module.f90:547-550). */
+int les_q_all_in_one(les_ctx* ctx);
+/* atm_thermodynamics.f90:25-60 thermo(): the diagnostic arrays of the module
+ * from the context's theta and qmix, levels 1..nz-1, columns 1..nx (each
+ * array (ld,ny,nz); padding columns and level nz are zero): actual and
+ * virtual temperature [nondimensional, T_scale], saturation vapour pressure
+ * [Pa], pressure [Pa], vapour pressure [Pa], saturation mixing ratio,
+ * relative humidity from pressures and from mixing ratios, and the lifting
+ * condensation level [m].  Nothing in the step reads them (main.f90:275);
+ * the reference's periodic zlcl_parcel output files are not written.
+ * Needs q_flag = 1 and s_flag = 1. */
+int les_atm_thermodynamics(les_ctx* ctx, double* actual_T, double* actual_Tv, double* sat_vapor_pr,
+                           double* pr_atm, double* vapor_pr, double* sat_qmix, double* rel_hum,
+                           double* rel_hum_q, double* zlcl_all);
 
 #ifdef __cplusplus
 }

@@ -26,13 +26,14 @@ class LesConfig(ctypes.Structure):
         ("initu", ctypes.c_int), ("initsc", ctypes.c_int),
         ("cs_count", ctypes.c_int), ("jt_total0", ctypes.c_int),
         ("precision", ctypes.c_int), ("rmsdiv_every", ctypes.c_int),
-        ("reserved0", ctypes.c_int),
+        ("q_flag", ctypes.c_int),
         ("l_x", ctypes.c_double), ("l_y", ctypes.c_double),
         ("lz_over_zi", ctypes.c_double), ("z_i", ctypes.c_double),
         ("u_star", ctypes.c_double), ("dt", ctypes.c_double),
         ("vonk", ctypes.c_double), ("t_scale", ctypes.c_double),
         ("dtdz_top", ctypes.c_double), ("pr", ctypes.c_double),
         ("g", ctypes.c_double),
+        ("q_scale", ctypes.c_double), ("dqdz_top", ctypes.c_double),
     ]
 
 
@@ -49,16 +50,20 @@ FIELDS = [
     "u_lag", "v_lag", "w_lag",
     "RHS_T", "RHS_Tf", "beta_scal", "dTdx", "dTdy", "dTdz",
     "S11", "S12", "S13", "S22", "S23", "S33",
+    "q", "RHS_q", "RHS_qf", "dqdx", "dqdy", "dqdz",
     "zo", "wt_s", "ustar_avg", "phi_m", "psi_m", "psi_m0",
-    "phi_h", "psi_h", "psi_h0", "sgs_t3",
+    "phi_h", "psi_h", "psi_h0", "sgs_t3", "wq_s", "sgs_q3",
 ]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 SURFACE_FIELDS = set(FIELDS[FIELDS.index("zo"):])
+# humidity arrays, stored only with q_flag = 1
+Q_FIELDS = {"q", "RHS_q", "RHS_qf", "dqdx", "dqdy", "dqdz", "wq_s", "sgs_q3"}
 
 
 def make_config(nx, ny=None, nz_levels=None, *, model=5, s_flag=0, jt_total0=0,
                 precision=0, dt=2e-4, vonk=0.4, cs_count=5, rmsdiv_every=500,
-                t_scale=400.0, dtdz_top=0.005, initu=0, initsc=0):
+                t_scale=400.0, dtdz_top=0.005, initu=0, initsc=0, q_flag=0, q_scale=100.0,
+                dqdz_top=-0.004):
     """Config for an nx x ny x nz_levels grid on the 2pi x 2pi x 1 box.
 
     ``nz_levels`` is the number of uvp levels; the Fortran extent is +1."""
@@ -75,6 +80,7 @@ def make_config(nx, ny=None, nz_levels=None, *, model=5, s_flag=0, jt_total0=0,
     c.lz_over_zi, c.z_i = 1.0, 1000.0
     c.u_star, c.dt, c.vonk = 1.0, dt, vonk
     c.t_scale, c.dtdz_top, c.pr, c.g = t_scale, dtdz_top, 0.55, 9.81
+    c.q_flag, c.q_scale, c.dqdz_top = q_flag, q_scale, dqdz_top
     return c
 
 
@@ -169,7 +175,26 @@ def initial_state(cfg, surface, seed=1234, noise=0.1, theta_k=300.0, theta_noise
         k = min(theta_levels, nz - 1)
         th[:k, :, :nx] += theta_noise * (2.0 * r[3, :k] - 1.0) / cfg.t_scale
         th[nz - 1] = th[nz - 2]
-    return {"u": u, "v": v, "w": w, "theta": th}
+    out = {"u": u, "v": v, "w": w, "theta": th}
+    if getattr(cfg, "q_flag", 0):
+        # humidity: 10 g/kg with a seeded +-0.2 g/kg perturbation in the lowest
+        # levels (nondimensional qmix = q / q_scale)
+        q = np.zeros((nz, ny, ld))
+        rq = splitmix64_uniform(seed + 7, n).reshape(nz, ny, nx)
+        q[:, :, :nx] = 10.0 / cfg.q_scale
+        k = min(theta_levels, nz - 1)
+        q[:k, :, :nx] += 0.2 * (2.0 * rq[:k] - 1.0) / cfg.q_scale
+        q[nz - 1] = q[nz - 2]
+        out["q"] = q
+    return out
+
+
+def moisture_flux(cfg, wq=(0.02, 0.06), width=None):
+    """x-striped kinematic surface moisture flux [g/kg m/s] on the stripes of
+    striped_surface (width nx/8), for the wq_s plane of q_flag = 1."""
+    width = cfg.nx // 8 if width is None else width
+    sel = (np.arange(cfg.nx) // width) % 2
+    return np.ascontiguousarray(np.where(sel == 0, wq[0], wq[1])[None, :].repeat(cfg.ny, 0).astype(np.float64))
 
 
 # Named workloads (one per configuration of the benchmark definition).

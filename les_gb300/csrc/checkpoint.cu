@@ -154,11 +154,17 @@ struct Item {
   ItemKind kind;
   int field;  // LES_* for VOL, SFC_LD, PLANE
 };
+// Without humidity (q_flag = 0) qmix, RHS_q and sgs_q3 are written as the
+// zeros a run of the reference holds for them and skipped on reading.
 std::vector<Item> record_items(const les_ctx* c) {
+  const bool q = c->cfg.q_flag != 0;
+  const Item qv = q ? Item{VOL, LES_Q} : Item{VOL_ZERO, -1};
+  const Item qr = q ? Item{VOL, LES_RHS_Q} : Item{VOL_ZERO, -1};
+  const Item q3 = q ? Item{SFC_LD, LES_SGS_Q3_SFC} : Item{SFC_LD_ZERO, -1};
   if (c->cfg.s_flag)
-    return {{VOL, LES_U},       {VOL, LES_V},       {VOL, LES_W},       {VOL, LES_THETA},   {VOL_ZERO, -1},  // qmix
-            {VOL, LES_RHSX},    {VOL, LES_RHSY},    {VOL, LES_RHSZ},    {VOL, LES_RHS_T},   {VOL_ZERO, -1},  // RHS_q
-            {SFC_LD, LES_SGS_T3_SFC}, {SFC_LD_ZERO, -1},                                                     // sgs_t3, sgs_q3
+    return {{VOL, LES_U},       {VOL, LES_V},       {VOL, LES_W},       {VOL, LES_THETA},   qv,  // qmix
+            {VOL, LES_RHSX},    {VOL, LES_RHSY},    {VOL, LES_RHSZ},    {VOL, LES_RHS_T},   qr,  // RHS_q
+            {SFC_LD, LES_SGS_T3_SFC}, q3,                                                        // sgs_t3, sgs_q3
             {PLANE, LES_PSI_M}, {PLANE, LES_PSI_M0}, {PLANE, LES_PSI_H}, {PLANE, LES_PSI_H0},
             {VOL, LES_CS_OPT2}, {VOL, LES_F_LM},    {VOL, LES_F_MM},    {VOL, LES_F_QN},    {VOL, LES_F_NN},
             {VOL_ZERO, -1},     {VOL_ZERO, -1},     {VOL_ZERO, -1},     {VOL_ZERO, -1},                      // G_*

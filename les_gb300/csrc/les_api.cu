@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
+#include <memory>
 #include <vector>
 #include <algorithm>
 #include <map>
@@ -185,7 +186,7 @@ struct Sizes {
   size_t wsA, wsB, wsP, big, tmp, fields, surf, spare, aux;
   int lag_chunk, ntmp;
 };
-static Sizes sizes_of(const Grid& g) {
+static Sizes sizes_of(const Grid& g, bool q) {
   Sizes s{};
   s.lag_chunk = std::min(32, g.nz);
   const size_t nz = g.nz, C = g.C, CB = g.CB, ch = s.lag_chunk;
@@ -196,8 +197,9 @@ static Sizes sizes_of(const Grid& g) {
   s.ntmp = (int)std::max<size_t>(63 * ch, 3 * nz + 2);
   s.tmp = (size_t)s.ntmp * g.nplane * sizeof(double);
   s.fields = 0;
-  for (int f = 0; f < LES_ZO; ++f) s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
-  s.surf = (size_t)(LES_NUM_FIELDS - LES_ZO + 1) * g.nx * g.ny * sizeof(double);
+  for (int f = 0; f < LES_ZO; ++f)
+    if (q || !is_q_field(f)) s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
+  s.surf = (size_t)(LES_NUM_FIELDS - LES_ZO + 1 - (q ? 0 : 2)) * g.nx * g.ny * sizeof(double);
   s.spare = 4 * g.nfield * sizeof(double) + (4 * nz + 4) * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double);
   // saved spectra, wall-plane spectra, Thomas tables, reductions, wavenumber
   // and filter tables (FP64 + FP32)
@@ -240,6 +242,7 @@ static void filter_G(const Grid& g, const std::vector<double>& k2, double alpha,
 }
 
 static size_t felems(const les_ctx* c, int f) {
+  if (is_q_field(f) && !c->cfg.q_flag) return 0;  // humidity arrays exist only with q_flag
   if (f >= LES_ZO) return (size_t)c->g.nx * c->g.ny;
   if (f == LES_P) return c->g.nplane * (c->g.nz + 1);
   return c->g.nfield;
@@ -258,7 +261,7 @@ size_t les_estimate_device_bytes(const les_config* cfg) {
   if (!cfg) return 0;
   Grid g;
   grid_of(*cfg, g);
-  Sizes s = sizes_of(g);
+  Sizes s = sizes_of(g, cfg->q_flag != 0);
   size_t mixed = 0;  // float-float Thomas tables of the FP32-mixed form
   if (cfg->precision == 1) mixed = 2 * (size_t)(g.nz + 1) * g.C * sizeof(float2) + 64 * sizeof(int);
   return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + mixed + (1u << 20);
@@ -277,6 +280,10 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     return LES_ERR_ARG;
   }
   if (k.precision != 0 && k.precision != 1) { les_set_error("precision must be 0 or 1"); return LES_ERR_ARG; }
+  if (k.q_flag != 0 && (k.q_flag != 1 || !k.s_flag || !(k.q_scale > 0.0))) {
+    les_set_error("q_flag = 1 needs s_flag = 1 and q_scale > 0");
+    return LES_ERR_ARG;
+  }
   if (k.model != 5 && k.model != 4 && k.model != 3 && k.model != 2) {
     les_set_error("model must be 5, 4, 3 or 2");
     return LES_ERR_UNSUPPORTED;
@@ -299,6 +306,7 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   c->own_stream = true;
   for (int f = 0; f < LES_NUM_FIELDS; ++f) {
     c->fsize[f] = felems(c, f);
+    if (c->fsize[f] == 0) continue;  // not stored in this configuration (null pointer)
     if ((st = dalloc(c, (void**)&c->f[f], c->fsize[f] * sizeof(double)))) return fail(st);
   }
   if ((st = dalloc(c, (void**)&c->z_os, (size_t)g.nx * g.ny * sizeof(double)))) return fail(st);
@@ -355,7 +363,7 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   if ((st = make_real_plan(c, g.nx, c->rx)) || (st = make_real_plan(c, g.nx2, c->rxb)) ||
       (st = make_plan(c, g.ny, c->cy)) || (st = make_plan(c, g.ny2, c->cyb)))
     return fail(st);
-  Sizes s = sizes_of(g);
+  Sizes s = sizes_of(g, k.q_flag != 0);
   c->lag_chunk = s.lag_chunk;
   c->ntmp = s.ntmp;
   c->nbig = 9;
@@ -448,8 +456,14 @@ static int field_out(les_ctx* c, int f, double* host) {
   LES_CUDA_CHECK(cudaMemcpyAsync(host, c->f[f], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   return LES_OK;
 }
+static int absent(const les_ctx* c, int f) {
+  if (c->fsize[f]) return LES_OK;
+  les_set_error("field %d is not stored in this context (humidity arrays need q_flag = 1)", f);
+  return LES_ERR_STATE;
+}
 int les_set_field(les_ctx* c, les_field f, const double* host) {
   if (!c || !host || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
+  if (int a = absent(c, f)) return a;
   int st = field_in(c, f, host);
   if (st) return st;
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
@@ -457,6 +471,7 @@ int les_set_field(les_ctx* c, les_field f, const double* host) {
 }
 int les_get_field(les_ctx* c, les_field f, double* host) {
   if (!c || !host || f < 0 || f >= LES_NUM_FIELDS) return LES_ERR_ARG;
+  if (int a = absent(c, f)) return a;
   int st = field_out(c, f, host);
   if (st) return st;
   LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
@@ -912,6 +927,8 @@ struct Arg {
   size_t n;
   bool owned = false;
   Arg(les_ctx* c_, const void* u, size_t n_) : c(c_), user(u), n(n_) {}
+  Arg(const Arg&) = delete;
+  Arg& operator=(const Arg&) = delete;
   // caller device arrays are read and written as pairs of doubles (16 bytes)
   int take_user() {
     if (reinterpret_cast<uintptr_t>(user) & 15u) {
@@ -932,7 +949,10 @@ struct Arg {
     if (c->ptr_mode) return take_user();
     if (cudaMalloc(&dev, n * sizeof(double)) != cudaSuccess) { les_set_error("staging alloc failed"); return LES_ERR_OOM; }
     owned = true;
-    cudaMemsetAsync(dev, 0, n * sizeof(double), c->stream);
+    if (cudaMemsetAsync(dev, 0, n * sizeof(double), c->stream) != cudaSuccess) {
+      les_set_error("staging clear failed");
+      return LES_ERR_CUDA;
+    }
     return 0;
   }
   int out() {
@@ -1195,6 +1215,35 @@ int les_theta_all_in_one(les_ctx* c) {
   if (!c) return LES_ERR_ARG;
   if (int st = need_fp64(c, "les_theta_all_in_one")) return st;
   op_theta(c);
+  return finish(c);
+}
+int les_q_all_in_one(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  if (!c->cfg.q_flag) { les_set_error("les_q_all_in_one: the context has no humidity (q_flag = 0)"); return LES_ERR_STATE; }
+  if (int st = need_fp64(c, "les_q_all_in_one")) return st;
+  op_q(c);
+  return finish(c);
+}
+int les_atm_thermodynamics(les_ctx* c, double* actual_T, double* actual_Tv, double* sat_vapor_pr, double* pr_atm,
+                           double* vapor_pr, double* sat_qmix, double* rel_hum, double* rel_hum_q, double* zlcl_all) {
+  double* o[9] = {actual_T, actual_Tv, sat_vapor_pr, pr_atm, vapor_pr, sat_qmix, rel_hum, rel_hum_q, zlcl_all};
+  if (!c) return LES_ERR_ARG;
+  for (double* p : o)
+    if (!p) return LES_ERR_ARG;
+  if (!c->cfg.q_flag) {
+    les_set_error("les_atm_thermodynamics: the context has no humidity (q_flag = 0)");
+    return LES_ERR_STATE;
+  }
+  const size_t n = c->g.nfield;
+  std::unique_ptr<Arg> a[9];
+  double* dev[9];
+  for (int i = 0; i < 9; ++i) {
+    a[i].reset(new Arg(c, o[i], n));
+    CHK(a[i]->alloc());
+    dev[i] = a[i]->dev;
+  }
+  op_thermo(c, dev);
+  for (int i = 0; i < 9; ++i) CHK(a[i]->out());
   return finish(c);
 }
 

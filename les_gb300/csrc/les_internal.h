@@ -86,10 +86,10 @@ struct les_ctx {
   int lag_chunk = 32;
   double* dscal = nullptr;                     // device scalars / reductions
   // per-level reduction results, 36 slots of nz+8 doubles: 0 plane sums /
-  // rmsdiv partials / model-3 Cs(z); 2..11 scaledep sums; 12..13 timestep_conditions
-  // partial maxima; 14 theta plane
-  // mean (mixed); 16..18 u, v, w plane means (mixed filt_da); 20..21 theta
-  // level mean and its reciprocal (calcbeta); 24..27 partial plane sums;
+  // rmsdiv partials / model-3 Cs(z); 2..11 scaledep sums; 12..13
+  // timestep_conditions partial maxima; 14 theta, 15 qmix plane means
+  // (mixed); 16..18 u, v, w plane means (mixed filt_da); 20..21 the (virtual)
+  // theta level mean and its reciprocal (calcbeta); 24..27 partial plane sums;
   // 28..33 the mixed form's per-level mean-wind factors (float-float);
   // 34..35 the mixed form's txz, tyz plane means
   double* dred = nullptr;
@@ -121,14 +121,18 @@ inline bool mixed_f32_field(int f) {
     case LES_S11: case LES_S12: case LES_S13: case LES_S22: case LES_S23: case LES_S33:
     case LES_NU_T:
     case LES_TXX: case LES_TXY: case LES_TYY: case LES_TXZ: case LES_TYZ: case LES_TZZ:
-    case LES_DTDX: case LES_DTDY:
+    case LES_DTDX: case LES_DTDY: case LES_DQDX: case LES_DQDY:
       return true;
     default:
       return false;
   }
 }
+// humidity arrays: stored only when q_flag = 1
+inline bool is_q_field(int f) {
+  return (f >= LES_Q && f <= LES_DQDZ) || f == LES_WQ_S || f == LES_SGS_Q3_SFC;
+}
 inline float* f32(les_ctx* c, int f) { return reinterpret_cast<float*>(c->f[f]); }
-void rhs_swap(les_ctx* c);  // exchange RHSx/RHSx_f, RHSy/.., RHSz/.., RHS_T/RHS_Tf buffers
+void rhs_swap(les_ctx* c);  // exchange RHSx/RHSx_f, RHSy/.., RHSz/.., RHS_T/RHS_Tf (RHS_q/RHS_qf) buffers
 int step_fp64(les_ctx* c);
 int step_mixed(les_ctx* c);
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev);
@@ -152,6 +156,8 @@ int op_lagrange_ssim(les_ctx* c, const double* const* S);
 int op_scaledep(les_ctx* c, double* cs_z_dev, const double* const* S);
 int op_stddyn(les_ctx* c, double* cs_z_dev, const double* const* S);
 int op_theta(les_ctx* c);
+int op_q(les_ctx* c);
+int op_thermo(les_ctx* c, double* const* out);  // 9 (ld,ny,nz) arrays, atm_thermodynamics.f90 order
 int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz);
 int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz, int w_variant);
 int op_convec(les_ctx* c, double* cx, double* cy, double* cz);

@@ -667,13 +667,15 @@ int op_dealias2(les_ctx* c, double* const* out, const double* const* in, int nf,
 }
 
 // ---------------------------------------------------------------------------
-// scalars_module.f90:508-690 obukhov (q = 0, patch_flag = 1); u1, v1 are the
-// 4-delta filtered first-level velocities, theta_sum the plane sum of theta(1).
+// scalars_module.f90:508-690 obukhov (patch_flag = 1); u1, v1 are the
+// 4-delta filtered first-level velocities, theta_sum the plane sum of theta(1);
+// sgs_q3 the surface moisture flux (null without humidity: qmix = 0)
 __global__ void k_obukhov(const double* __restrict__ u1, const double* __restrict__ v1,
                           const double* __restrict__ theta, const double* __restrict__ zo,
                           const double* __restrict__ z_os, double* __restrict__ sgs_t3,
                           double* ustar_avg, double* psi_m, double* psi_m0, double* psi_h,
                           double* psi_h0, double* phi_m, double* phi_h, const double* theta_sum,
+                          const double* __restrict__ sgs_q3, double q_scale,
                           int nx, int ny, int ld, double dz, double vonk, double g_, double nxny_f) {
   GSTRIDE(s, (size_t)nx * ny) {
     const int jy = (int)(s / nx), jx = (int)(s - (size_t)jy * nx);
@@ -683,7 +685,9 @@ __global__ void k_obukhov(const double* __restrict__ u1, const double* __restric
     const double us = u_avg * vonk / (log(0.5 * dz / zo[s]) - psi_m[s] + psi_m0[s]);
     ustar_avg[s] = us;
     const double wt_avg = sgs_t3[s];
-    const double wtv_avg = sgs_t3[s] + 0.61 * theta[i] * (0.001 * 100.0 * 0.0);
+    // virtual buoyancy flux (scalars_module.f90:549-550)
+    const double wtv_avg = sgs_q3 ? sgs_t3[s] + 0.61 * theta[i] * (0.001 * q_scale * sgs_q3[s])
+                                  : sgs_t3[s] + 0.61 * theta[i] * (0.001 * 100.0 * 0.0);
     const double L = -(us * us * us) / (vonk * (g_ / theta_) * wtv_avg);
     double zeta = 0.5 * dz / L, zeta0 = zo[s] / L, zeta0s = z_os[s] / L;
     if (zeta < -30.0) zeta = -30.0;
@@ -716,10 +720,14 @@ __global__ void k_obukhov(const double* __restrict__ u1, const double* __restric
   }
 }
 __global__ void k_obukhov_init(double* psi_m, double* psi_m0, double* psi_h, double* psi_h0,
-                               double* sgs_t3, const double* wt_s, size_t n, int initsc, double div) {
+                               double* sgs_t3, const double* wt_s, double* sgs_q3, const double* wq_s,
+                               size_t n, int initsc, double div, double divq) {
   GSTRIDE(s, n) {
     psi_m[s] = 0.0; psi_m0[s] = 0.0; psi_h[s] = 0.0; psi_h0[s] = 0.0;
-    if (!initsc) sgs_t3[s] = wt_s[s] / div;
+    if (!initsc) {
+      sgs_t3[s] = wt_s[s] / div;
+      if (sgs_q3) sgs_q3[s] = wq_s[s] / divq;
+    }
   }
 }
 // G_test_test-filtered surface u, v (test_filtermodule.f90:13-30 on the
@@ -747,7 +755,8 @@ int op_obukhov(les_ctx* c, const double* uv1) {
   if (c->jt == 1) {  // SCAL_init = 1 (scalars_module.f90:525-542)
     k_obukhov_init<<<grid1(ns), 256, 0, c->stream>>>(c->f[LES_PSI_M], c->f[LES_PSI_M0], c->f[LES_PSI_H],
                                                      c->f[LES_PSI_H0], c->f[LES_SGS_T3_SFC], c->f[LES_WT_S],
-                                                     ns, k.initsc, k.u_star * k.t_scale); LES_COUNT_LAUNCH();
+                                                     c->f[LES_SGS_Q3_SFC], c->f[LES_WQ_S], ns, k.initsc,
+                                                     k.u_star * k.t_scale, k.u_star * k.q_scale); LES_COUNT_LAUNCH();
   }
   plane_sums(c, c->f[LES_THETA], 0, 1, 16, 1.0, c->dscal + 0);
   if (!uv1) {
@@ -760,7 +769,8 @@ int op_obukhov(les_ctx* c, const double* uv1) {
   k_obukhov<<<grid1(ns), 256, 0, c->stream>>>(u1, v1, c->f[LES_THETA], c->f[LES_ZO], c->z_os,
                                               c->f[LES_SGS_T3_SFC], c->f[LES_USTAR_AVG], c->f[LES_PSI_M],
                                               c->f[LES_PSI_M0], c->f[LES_PSI_H], c->f[LES_PSI_H0],
-                                              c->f[LES_PHI_M], c->f[LES_PHI_H], c->dscal + 0, g.nx, g.ny,
+                                              c->f[LES_PHI_M], c->f[LES_PHI_H], c->dscal + 0,
+                                              c->f[LES_SGS_Q3_SFC], k.q_scale, g.nx, g.ny,
                                               g.ld, g.dz, k.vonk, g_, (double)(float)(g.nx * g.ny)); LES_COUNT_LAUNCH();
   return 0;
 }
@@ -3038,16 +3048,54 @@ __global__ void k_calcbeta(const double* __restrict__ theta, const double* __res
     }
   }
 }
+// virtual potential temperature theta (1 + 0.61 * 0.001 qmix q_scale)
+// (scalars_module.f90:203,221-222), padding columns zero
+__global__ void k_thetav(const double* __restrict__ theta, const double* __restrict__ q, double* __restrict__ tv,
+                         size_t n, int ld, int nx, double q_scale) {
+  GSTRIDE(i, n) {
+    tv[i] = ((int)(i % ld) < nx) ? theta[i] * (1.0 + 0.61 * 0.001 * q[i] * q_scale) : 0.0;
+  }
+}
+// with humidity, calcbeta reads the virtual temperature of the start-of-step
+// theta and qmix (q_all_in_one runs after theta_all_in_one, main.f90:273-274),
+// formed in c->tmp (free at this point of the scalar step)
 static void calcbeta(les_ctx* c) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   double* sbr = c->dred + 20 * (size_t)(g.nz + 8);  // 2 * nz values
-  plane_sums(c, c->f[LES_THETA], (long)g.nplane, g.nz, 4, 1.0, c->dred);
+  const double* th = c->f[LES_THETA];
+  if (k.q_flag) {
+    k_thetav<<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_Q], c->tmp, g.nfield, g.ld, g.nx,
+                                                     k.q_scale); LES_COUNT_LAUNCH();
+    th = c->tmp;
+  }
+  plane_sums(c, th, (long)g.nplane, g.nz, 4, 1.0, c->dred);
   const double g_hat = k.g * (k.z_i / (k.u_star * k.u_star));
   k_calcbeta_levels<<<1, 256, 0, c->stream>>>(c->dred, sbr, g.nz, (double)(g.nx * g.ny), 0.5 * g_hat); LES_COUNT_LAUNCH();
   k_calcbeta<8><<<dim3((unsigned)((g.nplane + 255) / 256), (g.nz + 7) / 8), 256, 0, c->stream>>>(
-      c->f[LES_THETA], sbr, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny, g.nz);
+      th, sbr, c->f[LES_BETA_SCAL], g.ld, g.nx, g.ny, g.nz);
   LES_COUNT_LAUNCH();
+}
+// One active scalar of the step: theta (scalars_module.f90:57-504) or the
+// humidity qmix (scalars_module_q.f90:31-397), which share the algorithm and
+// differ in their arrays, surface flux scale, lid gradient and in theta
+// alone feeding the buoyancy.
+struct ScalarDesc {
+  int s, rhs, rhsf, dsdx, dsdy, dsdz, flux, sgs3;
+  double flux_scale;  // surf_flux = flux / flux_scale  (T_scale u_star or q_scale u_star)
+  double top_grad;    // dsdz(nz) (dTdz_top / T_scale z_i or dqdz_top / q_scale z_i)
+  int mean_slot;      // dred slot of the mixed form's plane means
+  bool buoyancy;
+};
+static ScalarDesc theta_desc(const les_ctx* c) {
+  const les_config& k = c->cfg;
+  return ScalarDesc{LES_THETA, LES_RHS_T, LES_RHS_TF, LES_DTDX, LES_DTDY, LES_DTDZ, LES_WT_S, LES_SGS_T3_SFC,
+                    k.t_scale * k.u_star, k.dtdz_top / k.t_scale * k.z_i, 14, true};
+}
+static ScalarDesc q_desc(const les_ctx* c) {
+  const les_config& k = c->cfg;
+  return ScalarDesc{LES_Q, LES_RHS_Q, LES_RHS_QF, LES_DQDX, LES_DQDY, LES_DQDZ, LES_WQ_S, LES_SGS_Q3_SFC,
+                    k.q_scale * k.u_star, k.dqdz_top / k.q_scale * k.z_i, 15, false};
 }
 // scalars_module.f90:457-504 step_scalar
 // grid (ceil(np/256), nz-1): one element per thread (a column walk per
@@ -3068,34 +3116,35 @@ __global__ void k_step_scalar(double* __restrict__ theta, const double* __restri
   }
   if (jz == nz - 1) theta[i + np] = top_grad ? t + inc : t;
 }
-// scalars_module.f90:57-171 theta_all_in_one (S_FLAG, lbc = 1, model 5 Pr)
-int op_theta(les_ctx* c) {
+// scalars_module.f90:57-171 theta_all_in_one / scalars_module_q.f90:31-141
+// q_all_in_one (S_FLAG, lbc = 1, model 5 Pr)
+static int op_scalar(les_ctx* c, const ScalarDesc& d) {
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const int nz = g.nz;
-  op_filt_da(c, c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY], nz);
-  op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
-  fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
-  // RHS_Tf = RHS_T (pointer swap; RHS_T is fully rewritten below)
-  cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
-                                                            c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
-                                                            c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
-                                                            k.t_scale * k.u_star, k.vonk, g.dz); LES_COUNT_LAUNCH();
+  op_filt_da(c, c->f[d.s], c->f[d.dsdx], c->f[d.dsdy], nz);
+  op_ddz(c, c->f[d.dsdz], c->f[d.s], 1);
+  fill(c, c->f[d.dsdz] + (size_t)(nz - 1) * g.nplane, g.nplane, d.top_grad);
+  // RHS_Tf = RHS_T (RHS_T is fully rewritten below)
+  cudaMemcpyAsync(c->f[d.rhsf], c->f[d.rhs], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[d.s], c->f[d.flux], c->f[LES_PHI_H],
+                                                            c->f[LES_USTAR_AVG], c->f[d.dsdz],
+                                                            c->f[d.sgs3], g.nx, g.ny, g.ld,
+                                                            d.flux_scale, k.vonk, g.dz); LES_COUNT_LAUNCH();
   double* bigf[7];
   for (int q = 0; q < 7; ++q) bigf[q] = c->big + (size_t)q * g.nfield_big;
-  const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_DTDX], c->f[LES_DTDY], c->f[LES_DTDZ]};
+  const double* in[6] = {c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[d.dsdx], c->f[d.dsdy], c->f[d.dsdz]};
   op_dealias1(c, in, bigf, 6, nz);
   k_scalar_prod<double><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
                                                            bigf[6], g.ld_big, g.nx2, g.ny2, nz, nullptr); LES_COUNT_LAUNCH();
-  double* rt = c->f[LES_RHS_T];
+  double* rt = c->f[d.rhs];
   const double* b6 = bigf[6];
   op_dealias2(c, &rt, &b6, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
   // horizontal SGS flux divergence (ddx + ddy summed in spectral space)
   double* tx = c->tmp;
   double* ty = c->tmp + g.nfield;
   double* dxy = c->tmp + 2 * g.nfield;
-  k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX], c->f[LES_DTDY], tx, ty,
+  k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[d.dsdx], c->f[d.dsdy], tx, ty,
                                                           g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
   {
     const double sc = 1.0 / (double)(g.nx * g.ny);
@@ -3108,18 +3157,57 @@ int op_theta(les_ctx* c) {
     cols(c, J);
     c2r(c, 1, nz, c->wsB, &dxy, (long)g.nplane, false, g.lh);
   }
-  k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[LES_DTDZ],
-                                                                 c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny, nz, k.pr,
+  k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[d.dsdz],
+                                                                 c->f[d.sgs3], g.ld, g.nx, g.ny, nz, k.pr,
                                                                  1.0 / g.dz); LES_COUNT_LAUNCH();
   // calcbeta on theta before the update
-  calcbeta(c);
+  if (d.buoyancy) calcbeta(c);
   if (c->jt == 1 && !k.initsc)
-    cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
+    cudaMemcpyAsync(c->f[d.rhsf], c->f[d.rhs], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
   const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
   k_step_scalar<<<dim3((unsigned)((g.nplane + 255) / 256), nz - 1), 256, 0, c->stream>>>(
-      c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx, g.ny, nz, k.dt, topg,
-      k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
+      c->f[d.s], c->f[d.rhs], c->f[d.rhsf], g.ld, g.nx, g.ny, nz, k.dt, topg,
+      d.top_grad * g.dz); LES_COUNT_LAUNCH();
+  return 0;
+}
+
+int op_theta(les_ctx* c) { return op_scalar(c, theta_desc(c)); }
+int op_q(les_ctx* c) { return op_scalar(c, q_desc(c)); }
+
+// atm_thermodynamics.f90:37-52 for levels 1..nz-1, columns 1..nx
+__global__ void k_thermo(const double* __restrict__ theta, const double* __restrict__ q, double* aT, double* aTv,
+                         double* svp, double* pa, double* vp, double* sq, double* rh, double* rhq, double* zl,
+                         int ld, int nx, int ny, int nz, double dz, double z_i, double T_scale, double q_scale,
+                         double g, double cp, double Rd, double pr_surf) {
+  const size_t np = (size_t)ld * ny;
+  GSTRIDE(i, np * (nz - 1)) {
+    if ((int)(i % ld) >= nx) continue;
+    const int jz = (int)(i / np) + 1;  // k_global = jz (one domain)
+    const double zg = jz * dz * z_i;
+    const double T = theta[i] - (g / cp) * zg / T_scale;
+    const double Tv = T * (1 + 0.61 * 0.001 * q[i] * q_scale);
+    const double Tc = T * T_scale - 273.2;
+    const double es = 611.2 * exp(17.62 * Tc / (243.12 + Tc));
+    const double p = pr_surf * exp(-zg / (Rd * Tv * T_scale / g));
+    const double qq = 0.001 * q_scale * q[i];
+    const double e = (qq / (qq + 0.622)) * p;
+    const double qs = 0.622 * es / (p - es);
+    const double rq = qq / qs;
+    aT[i] = T; aTv[i] = Tv; svp[i] = es; pa[i] = p; vp[i] = e; sq[i] = qs;
+    rh[i] = e / es;
+    rhq[i] = rq;
+    zl[i] = zg + (cp / g) * (T * T_scale - 55 - 1.0 / (1 / (T * T_scale - 55) - log(rq) / 2840));
+  }
+}
+int op_thermo(les_ctx* c, double* const* o) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  // param.f90:90-96
+  const double cp = 1005.0, Rd = 287.04, pr_surf = 100000.0;
+  k_thermo<<<grid1(g.nplane * (g.nz - 1)), 256, 0, c->stream>>>(
+      c->f[LES_THETA], c->f[LES_Q], o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], g.ld, g.nx, g.ny, g.nz,
+      g.dz, k.z_i, k.t_scale, k.q_scale, k.g, cp, Rd, pr_surf); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -3864,7 +3952,7 @@ static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
 }
 
 template <bool MX>
-static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
+static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc& d) {
   typedef typename PX<MX>::T T;
   typedef typename PX<MX>::CX CX;
   typedef typename PX<MX>::S S;
@@ -3872,16 +3960,18 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
   const les_config& k = c->cfg;
   const int nz = g.nz;
   const size_t FS = (size_t)nz * g.C;
-  CX* specT = reinterpret_cast<CX*>(c->spec + 3 * FS);  // theta spectrum (precision of the transform)
+  // the scalar's spectrum (precision of the transform) in the fourth saved
+  // spectrum slot: theta's, then (qmix after theta) the humidity's
+  CX* specT = reinterpret_cast<CX*>(c->spec + 3 * FS);
   // FP32 transforms see theta - th0(level) (th0 = plane mean): the filter and
   // the horizontal derivatives are unchanged by a per-level constant, and the
   // perturbation keeps its precision; th0 is added back in FP64
-  double* th0 = MX ? c->dred + 14 * (size_t)(nz + 8) : nullptr;
+  double* th0 = MX ? c->dred + d.mean_slot * (size_t)(nz + 8) : nullptr;
   if (MX) {
-    plane_sums(c, c->f[LES_THETA], (long)g.nplane, nz, 4, (double)(g.nx * g.ny), th0);
+    plane_sums(c, c->f[d.s], (long)g.nplane, nz, 4, (double)(g.nx * g.ny), th0);
   }
   {  // filt_da(theta) with the spectrum saved
-    const double* in[1] = {c->f[LES_THETA]};
+    const double* in[1] = {c->f[d.s]};
     const double sc[1] = {1.0 / (double)(g.nx * g.ny)};
     const double* offs[1] = {th0};
     r2cT<T, double>(c, 1, nz, in, (long)g.nplane, sc, nullptr, c->wsA, false, g.lh, offs);
@@ -3892,27 +3982,27 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY; J.coef[3][0] = CC_KILL;
     colsT<T, CX>(c, J);
     if constexpr (MX) {  // theta in FP64 (plane mean added back), the gradients FP32-held
-      double* o1[1] = {c->f[LES_THETA]};
+      double* o1[1] = {c->f[d.s]};
       const double* offo[1] = {th0};
       c2rT<T, double>(c, 1, nz, c->wsB, o1, (long)g.nplane, false, g.lh, offo);
-      float* o2[2] = {f32(c, LES_DTDX), f32(c, LES_DTDY)};
+      float* o2[2] = {f32(c, d.dsdx), f32(c, d.dsdy)};
       c2rT<T, float>(c, 2, nz, (CX*)c->wsB + FS, o2, (long)g.nplane, false, g.lh);
     } else {
-      double* out[3] = {c->f[LES_THETA], c->f[LES_DTDX], c->f[LES_DTDY]};
+      double* out[3] = {c->f[d.s], c->f[d.dsdx], c->f[d.dsdy]};
       const double* offo[3] = {th0, nullptr, nullptr};
       c2rT<T, double>(c, 3, nz, c->wsB, out, (long)g.nplane, false, g.lh, offo);
     }
   }
-  op_ddz(c, c->f[LES_DTDZ], c->f[LES_THETA], 1);
-  fill(c, c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);
+  op_ddz(c, c->f[d.dsdz], c->f[d.s], 1);
+  fill(c, c->f[d.dsdz] + (size_t)(nz - 1) * g.nplane, g.nplane, d.top_grad);
   // RHS_Tf = RHS_T: exchanged with the momentum RHS at the start of the step
-  k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[LES_THETA], c->f[LES_WT_S], c->f[LES_PHI_H],
-                                                            c->f[LES_USTAR_AVG], c->f[LES_DTDZ],
-                                                            c->f[LES_SGS_T3_SFC], g.nx, g.ny, g.ld,
-                                                            k.t_scale * k.u_star, k.vonk, g.dz); LES_COUNT_LAUNCH();
+  k_sflux<<<grid1((size_t)g.nx * g.ny), 256, 0, c->stream>>>(c->f[d.s], c->f[d.flux], c->f[LES_PHI_H],
+                                                            c->f[LES_USTAR_AVG], c->f[d.dsdz],
+                                                            c->f[d.sgs3], g.nx, g.ny, g.ld,
+                                                            d.flux_scale, k.vonk, g.dz); LES_COUNT_LAUNCH();
   {
     const double cs = 1.0 / (double)(g.nx * g.ny);
-    const double* pl[2] = {c->f[LES_DTDZ], c->f[LES_DTDZ] + (size_t)(nz - 1) * g.nplane};
+    const double* pl[2] = {c->f[d.dsdz], c->f[d.dsdz] + (size_t)(nz - 1) * g.nplane};
     const double sc[2] = {cs, cs};
     plane_spectra(c, 2, pl, sc, c->wspec + 2 * g.C);
   }
@@ -3945,14 +4035,14 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
       unpadT<MX, float>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
     }
     const dim3 gpl((unsigned)((g.nplane + 255) / 256), (unsigned)nz);
-    k_scalar_temp_xy32<<<gpl, 256, 0, c->stream>>>(f32(c, LES_NU_T), f32(c, LES_DTDX), f32(c, LES_DTDY), tx, ty,
+    k_scalar_temp_xy32<<<gpl, 256, 0, c->stream>>>(f32(c, LES_NU_T), f32(c, d.dsdx), f32(c, d.dsdy), tx, ty,
                                                    g.ld, g.nx, g.ny, nz, (float)(1.0 / k.pr)); LES_COUNT_LAUNCH();
     div_xyT<MX, float>(c, tx, ty, dxy, nz);
     k_scalar_rhs32<<<dim3(gpl.x, (unsigned)(nz - 1)), 256, 0, c->stream>>>(
-        c->f[LES_RHS_T], rtf, dxy, f32(c, LES_NU_T), c->f[LES_DTDZ], c->f[LES_SGS_T3_SFC], g.ld, g.nx, g.ny,
+        c->f[d.rhs], rtf, dxy, f32(c, LES_NU_T), c->f[d.dsdz], c->f[d.sgs3], g.ld, g.nx, g.ny,
         (float)(1.0 / k.pr), (float)(1.0 / g.dz)); LES_COUNT_LAUNCH();
   } else {
-    double* rt = c->f[LES_RHS_T];
+    double* rt = c->f[d.rhs];
     {
       S* b6[1] = {bigf[6]};
       double* o[1] = {rt};
@@ -3961,23 +4051,23 @@ static int thetaT(les_ctx* c, typename PX<MX>::S* const* bigf) {
     double* tx = c->tmp;
     double* ty = c->tmp + g.nfield;
     double* dxy = c->tmp + 2 * g.nfield;
-    k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[LES_DTDX],
-                                                                    c->f[LES_DTDY], tx, ty, g.ld, g.nx, g.ny, nz,
+    k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[d.dsdx],
+                                                                    c->f[d.dsdy], tx, ty, g.ld, g.nx, g.ny, nz,
                                                                     k.pr); LES_COUNT_LAUNCH();
     div_xyT<MX>(c, tx, ty, dxy, nz);
     k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T],
-                                                                           c->f[LES_DTDZ], c->f[LES_SGS_T3_SFC],
+                                                                           c->f[d.dsdz], c->f[d.sgs3],
                                                                            g.ld, g.nx, g.ny, nz, k.pr, 1.0 / g.dz);
     LES_COUNT_LAUNCH();
   }
-  calcbeta(c);
+  if (d.buoyancy) calcbeta(c);
   if (c->jt == 1 && !k.initsc)
-    cudaMemcpyAsync(c->f[LES_RHS_TF], c->f[LES_RHS_T], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
+    cudaMemcpyAsync(c->f[d.rhsf], c->f[d.rhs], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice,
                     c->stream);
   const int topg = k.lz_over_zi > 1.0 ? 1 : 0;
   k_step_scalar<<<dim3((unsigned)((g.nplane + 255) / 256), nz - 1), 256, 0, c->stream>>>(
-      c->f[LES_THETA], c->f[LES_RHS_T], c->f[LES_RHS_TF], g.ld, g.nx, g.ny, nz, k.dt, topg,
-      k.dtdz_top / k.t_scale * k.z_i * g.dz); LES_COUNT_LAUNCH();
+      c->f[d.s], c->f[d.rhs], c->f[d.rhsf], g.ld, g.nx, g.ny, nz, k.dt, topg,
+      d.top_grad * g.dz); LES_COUNT_LAUNCH();
   return 0;
 }
 
@@ -4068,6 +4158,7 @@ void rhs_swap(les_ctx* c) {
   std::swap(c->f[LES_RHSY], c->f[LES_RHSY_F]);
   std::swap(c->f[LES_RHSZ], c->f[LES_RHSZ_F]);
   std::swap(c->f[LES_RHS_T], c->f[LES_RHS_TF]);
+  std::swap(c->f[LES_RHS_Q], c->f[LES_RHS_QF]);  // null without humidity
   c->rhs_par ^= 1;
 }
 
@@ -4115,8 +4206,12 @@ static int stepT(les_ctx* c) {
     LES_COUNT_LAUNCH();
   }
   padT<MX, C2>(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
-  if (k.s_flag) thetaT<MX>(c, bigf);
-  else fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
+  if (k.s_flag) {
+    scalarT<MX>(c, bigf, theta_desc(c));
+    if (k.q_flag) scalarT<MX>(c, bigf, q_desc(c));  // main.f90:273-274
+  } else {
+    fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
+  }
   divstressT<MX>(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
   convecT<MX>(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
   const size_t nv = g.nplane * (g.nz - 1);

@@ -8,7 +8,9 @@
 // layout: real fields (ld,ny,nz) column-major, complex planes (lh,ny) over the
 // same storage, pressure (ld,ny,0:nz).  Non-MPI build (nproc = 1, lbz = 1),
 // lbc_mom = 'wall', lbc = 1, ifilter = 1 (spectral cutoff), filter_size = 1,
-// molec = dns_bc = use_bldg = inflow = .false., ubc = 0, no Coriolis, q = 0.
+// molec = dns_bc = use_bldg = inflow = .false., ubc = 0, no Coriolis; the
+// humidity qmix (scalars_module_q.f90) is advanced when q_flag = 1 and is
+// identically zero otherwise.
 //
 // Parity status: the reference cannot be compiled here (no Fortran compiler,
 // no FFTW 2) and ships no tests or golden vectors, so this restatement is
@@ -31,8 +33,12 @@
 //    relaxation of the padding columns (LM = MM = 0 there).
 //  * scaledep_dynamic is called with its own 7-argument interface; the
 //    reference's call site (sgs_stag.f90:132) passes 10 arguments.
-//  * surface inputs are given nondimensional (zo) and kinematic (wt_s [K m/s])
-//    instead of being read from zom.dat / wts.dat [W/m^2] (bottombc.f90:31-59).
+//  * surface inputs are given nondimensional (zo) and kinematic (wt_s [K m/s],
+//    wq_s [g/kg m/s]) instead of being read from zom.dat / wts.dat / wqs.dat
+//    [W/m^2] (bottombc.f90:31-59).
+//  * thermo (atm_thermodynamics.f90:37-52) fills columns 1..nx and leaves the
+//    padding columns zero (the reference evaluates its formulas on whatever
+//    the padding holds; nothing reads those values).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -59,9 +65,9 @@ using Field = std::vector<double>;
 struct Oracle {
   les_config cfg;
   int nx, ny, nz, ld, lh, nx2, ny2, ld_big, lh_big;
-  double dx, dy, dz, L_x, L_y, z_i, u_star, dt, vonk, T_scale, dTdz_top, Pr, g;
+  double dx, dy, dz, L_x, L_y, z_i, u_star, dt, vonk, T_scale, dTdz_top, Pr, g, q_scale, dqdz_top;
   int cs_count, model;
-  bool s_flag, initu, initsc;
+  bool s_flag, initu, initsc, q_flag;
   int jt = 0, jt_total = 0;
   double tt = 0.0;
   std::unique_ptr<FFT2> fs, fb;
@@ -80,8 +86,11 @@ struct Oracle {
   Field S11, S12, S13, S22, S23, S33;
   // scalars_module.f90:31-36
   Field beta_scal, dTdx, dTdy, dTdz, RHS_T, RHS_Tf;
+  // scalars_module_q.f90:17-27
+  Field qmix, dqdx, dqdy, dqdz, RHS_q, RHS_qf;
   // bottombc.f90:9-16 (nx,ny)
   Field zo, z_os, wt_s, ustar_avg, phi_m, psi_m, psi_m0, phi_h, psi_h, psi_h0, sgs_t3;
+  Field wq_s, sgs_q3;  // bottombc.f90:15, scalars_module_q.f90:23 (level 1)
   // fft.f90:19, test_filtermodule.f90:9
   Field kx, ky, k2, G_test, G_test_test;
   double rmsdiv_last = 0.0;
@@ -107,6 +116,7 @@ struct Oracle {
     dx = L_x / nx; dy = L_y / ny;                      // param.f90:65
     u_star = c.u_star; dt = c.dt; vonk = c.vonk; T_scale = c.t_scale;
     dTdz_top = c.dtdz_top; Pr = c.pr; g = c.g;
+    q_flag = c.q_flag != 0; q_scale = c.q_scale; dqdz_top = c.dqdz_top;
     cs_count = c.cs_count; model = c.model;
     s_flag = c.s_flag != 0; initu = c.initu != 0; initsc = c.initsc != 0;
     jt_total = c.jt_total0;
@@ -117,11 +127,12 @@ struct Oracle {
                    &dwdz, &RHSx, &RHSy, &RHSz, &RHSx_f, &RHSy_f, &RHSz_f, &dpdx, &dpdy, &dpdz,
                    &txx, &txy, &tyy, &txz, &tyz, &tzz, &divtx, &divty, &divtz, &F_LM, &F_MM,
                    &F_QN, &F_NN, &Beta, &Cs_opt2, &Nu_t, &u_lag, &v_lag, &w_lag, &S11, &S12,
-                   &S13, &S22, &S23, &S33, &beta_scal, &dTdx, &dTdy, &dTdz, &RHS_T, &RHS_Tf};
+                   &S13, &S22, &S23, &S33, &beta_scal, &dTdx, &dTdy, &dTdz, &RHS_T, &RHS_Tf,
+                   &qmix, &dqdx, &dqdy, &dqdz, &RHS_q, &RHS_qf};
     for (Field* f : fl) f->assign(nfield, 0.0);
     p.assign(nplane * (nz + 1), 0.0);
     Field* sf[] = {&zo, &z_os, &wt_s, &ustar_avg, &phi_m, &psi_m, &psi_m0, &phi_h, &psi_h,
-                   &psi_h0, &sgs_t3};
+                   &psi_h0, &sgs_t3, &wq_s, &sgs_q3};
     for (Field* f : sf) f->assign((size_t)nx * ny, 0.0);
     for (double& x : phi_m) x = 1.0;
     for (double& x : phi_h) x = 1.0;
@@ -1038,15 +1049,18 @@ struct Oracle {
       }
   }
 
-  // scalars_module.f90:508-690 (q = 0, patch_flag = 1)
+  // scalars_module.f90:508-690 (patch_flag = 1)
   void obukhov() {
     if (jt == 1) {  // SCAL_init = 1
       std::fill(psi_m.begin(), psi_m.end(), 0.0);
       std::fill(psi_m0.begin(), psi_m0.end(), 0.0);
       std::fill(psi_h.begin(), psi_h.end(), 0.0);
       std::fill(psi_h0.begin(), psi_h0.end(), 0.0);
-      if (!initsc)
+      if (!initsc) {
         for (size_t s = 0; s < sgs_t3.size(); ++s) sgs_t3[s] = wt_s[s] / (u_star * T_scale);
+        if (q_flag)
+          for (size_t s = 0; s < sgs_q3.size(); ++s) sgs_q3[s] = wq_s[s] / (u_star * q_scale);
+      }
     }
     const double g_ = (g * z_i) / (u_star * u_star);
     double th = 0.0;
@@ -1067,7 +1081,8 @@ struct Oracle {
       for (int jy = 1; jy <= ny; ++jy) {
         const size_t s = S2(jx, jy);
         const double wt_avg = sgs_t3[s];
-        const double wtv_avg = sgs_t3[s] + 0.61 * theta[I(jx, jy, 1)] * (0.001 * 100.0 * 0.0);
+        const double wtv_avg = q_flag ? sgs_t3[s] + 0.61 * theta[I(jx, jy, 1)] * (0.001 * q_scale * sgs_q3[s])
+                                      : sgs_t3[s] + 0.61 * theta[I(jx, jy, 1)] * (0.001 * 100.0 * 0.0);
         const double us = ustar_avg[s];
         const double L = -(us * us * us) / (vonk * (g_ / theta_) * wtv_avg);
         double zeta = 0.5 * dz / L, zeta0 = zo[s] / L, zeta0s = z_os[s] / L;
@@ -1325,31 +1340,35 @@ struct Oracle {
     }
   }
 
-  // scalars_module.f90:232-454
-  void scalar_RHS_calc() {
-    // dsdx = dTdx, dsdy = dTdy, dsdz = dTdz, RHS = RHS_T
+  // scalars_module.f90:232-454 scalar_RHS_calc (theta) and
+  // scalars_module_q.f90:145-367 scalar_q_RHS_calc (qmix): the same
+  // algorithm on the scalar's arrays; the surface flux is wt_s/(T_scale u_star)
+  // for theta and wq_s/q_scale/u_star for qmix (lbc = 1)
+  void scalar_RHS_calc(const Field& scalar, Field& dsdx, Field& dsdy, Field& dsdz, Field& RHS, const Field& flux,
+                       Field& sgs_vert, bool humidity) {
     std::vector<double> ustar_local = ustar_avg;
     std::vector<double> sn1(nplane);
-    for (size_t i = 0; i < nplane; ++i) sn1[i] = theta[i];
+    for (size_t i = 0; i < nplane; ++i) sn1[i] = scalar[i];
     test_filter(sn1.data(), G_test);
     std::vector<double> surf_flux((size_t)nx * ny, 0.0);
-    if (theta[0] < 2.0) {  // lbc == 1
+    if (scalar[0] < 2.0) {  // lbc == 1
       for (int i = 1; i <= nx; ++i)
-        for (int j = 1; j <= ny; ++j) surf_flux[S2(i, j)] = wt_s[S2(i, j)] / (T_scale * u_star);
+        for (int j = 1; j <= ny; ++j)
+          surf_flux[S2(i, j)] = humidity ? flux[S2(i, j)] / q_scale / u_star : flux[S2(i, j)] / (T_scale * u_star);
     }
     for (int i = 1; i <= nx; ++i)
       for (int j = 1; j <= ny; ++j) {
         const size_t s = S2(i, j);
-        dTdz[I(i, j, 1)] = -phi_h[s] * surf_flux[s] / (ustar_local[s] * vonk * dz / 2.0);
+        dsdz[I(i, j, 1)] = -phi_h[s] * surf_flux[s] / (ustar_local[s] * vonk * dz / 2.0);
       }
     const size_t NB = nplane_big * nz;
     std::vector<double> u_m(NB), v_m(NB), w_m(NB), dsdx_m(NB), dsdy_m(NB), dsdz_m(NB), RHS_m(NB, 0.0);
     dealias1(u.data(), u_m.data(), nz);
     dealias1(v.data(), v_m.data(), nz);
     dealias1(w.data(), w_m.data(), nz);
-    dealias1(dTdx.data(), dsdx_m.data(), nz);
-    dealias1(dTdy.data(), dsdy_m.data(), nz);
-    dealias1(dTdz.data(), dsdz_m.data(), nz);
+    dealias1(dsdx.data(), dsdx_m.data(), nz);
+    dealias1(dsdy.data(), dsdy_m.data(), nz);
+    dealias1(dsdz.data(), dsdz_m.data(), nz);
     auto Bi = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)ld_big * ((size_t)(j - 1) + (size_t)ny2 * (k - 1)); };
     for (int k = 2; k <= nz - 1; ++k)
       for (int j = 1; j <= ny2; ++j)
@@ -1367,48 +1386,48 @@ struct Oracle {
         const size_t a = Bi(i, j, nz);
         RHS_m[a] = u_m[a] * dsdx_m[a] + v_m[a] * dsdy_m[a];
       }
-    dealias2(RHS_T.data(), RHS_m.data(), nz);
+    dealias2(RHS.data(), RHS_m.data(), nz);
     std::vector<double> temp(nfield, 0.0), dtemp(nfield, 0.0);
     const double Pr_ = Pr;
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         const size_t a = I(i, j, 1);
-        temp[a] = (1.0 / Pr_) * Nu_t[a] * dTdx[a];
+        temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdx[a];
       }
     for (int k = 2; k <= nz - 1; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k), b = I(i, j, k + 1);
-          temp[a] = (1.0 / (0.5 * (Pr_ + Pr_))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dTdx[a];
+          temp[a] = (1.0 / (0.5 * (Pr_ + Pr_))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dsdx[a];
         }
     ddx(dtemp.data(), temp.data(), nz);
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         const size_t a = I(i, j, 1);
-        RHS_T[a] = (-1.0 * RHS_T[a] + dtemp[a]);
-        temp[a] = (1.0 / Pr_) * Nu_t[a] * dTdy[a];
+        RHS[a] = (-1.0 * RHS[a] + dtemp[a]);
+        temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdy[a];
       }
     for (int k = 2; k <= nz - 1; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k), b = I(i, j, k + 1);
-          RHS_T[a] = (-1.0 * RHS_T[a] + dtemp[a]);
-          temp[a] = (1.0 / (0.5 * (Pr_ + Pr_))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dTdy[a];
+          RHS[a] = (-1.0 * RHS[a] + dtemp[a]);
+          temp[a] = (1.0 / (0.5 * (Pr_ + Pr_))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dsdy[a];
         }
     ddy(dtemp.data(), temp.data(), nz);
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         const size_t a = I(i, j, 1);
-        RHS_T[a] = RHS_T[a] + dtemp[a];
+        RHS[a] = RHS[a] + dtemp[a];
         temp[a] = -1.0 * surf_flux[S2(i, j)];
-        sgs_t3[S2(i, j)] = surf_flux[S2(i, j)];
+        sgs_vert[S2(i, j)] = surf_flux[S2(i, j)];
       }
     for (int k = 2; k <= nz; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k);
-          RHS_T[a] = RHS_T[a] + dtemp[a];
-          temp[a] = (1.0 / Pr_) * Nu_t[a] * dTdz[a];
+          RHS[a] = RHS[a] + dtemp[a];
+          temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdz[a];
         }
     std::fill(dtemp.begin(), dtemp.end(), 0.0);
     ddz_w(dtemp.data(), temp.data());
@@ -1416,44 +1435,51 @@ struct Oracle {
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k);
-          RHS_T[a] = RHS_T[a] + dtemp[a];
+          RHS[a] = RHS[a] + dtemp[a];
         }
   }
 
-  // scalars_module.f90:175-228 (q = 0)
+  // scalars_module.f90:175-228 calcbeta(theta, qmix): the virtual
+  // temperature theta (1 + 0.61 * 0.001 qmix q_scale) (qmix = 0 without humidity)
   void calcbeta() {
     const double g_hat = g * (z_i / (u_star * u_star));
     std::fill(beta_scal.begin(), beta_scal.end(), 0.0);
+    auto tv = [&](size_t a) {
+      return q_flag ? theta[a] * (1 + 0.61 * 0.001 * qmix[a] * q_scale) : theta[a] * 1.0;
+    };
     std::vector<double> sb(nz + 1, 0.0);
     for (int k = 1; k <= nz; ++k) {
       double s = 0.0;
       for (int j = 1; j <= ny; ++j)
-        for (int i = 1; i <= nx; ++i) s = s + theta[I(i, j, k)] * (1.0 + 0.61 * 0.001 * 0.0 * 100.0);
+        for (int i = 1; i <= nx; ++i)
+          s = s + (q_flag ? tv(I(i, j, k)) : theta[I(i, j, k)] * (1.0 + 0.61 * 0.001 * 0.0 * 100.0));
       sb[k] = s / (double)(nx * ny);
     }
     for (int k = 2; k <= nz - 1; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
-          const double above = (theta[I(i, j, k)] * 1.0 - sb[k]) / sb[k];
-          const double below = (theta[I(i, j, k - 1)] * 1.0 - sb[k - 1]) / sb[k - 1];
+          const double above = (tv(I(i, j, k)) - sb[k]) / sb[k];
+          const double below = (tv(I(i, j, k - 1)) - sb[k - 1]) / sb[k - 1];
           beta_scal[I(i, j, k)] = g_hat * (above + below) / 2.0;
         }
   }
 
-  // scalars_module.f90:457-504
-  void step_scalar() {
+  // scalars_module.f90:457-504 step_scalar / scalars_module_q.f90:370-397
+  // step_scalar_q; the lid value follows the gradient when L_z > z_i
+  // (a one-process domain: L_z nproc = L_z), else it copies level nz-1
+  void step_scalar(Field& scalar, const Field& RHS, const Field& RHSf, double top_grad) {
     for (int k = 1; k <= nz - 1; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k);
-          theta[a] = theta[a] + dt * (1.5 * RHS_T[a] - 0.5 * RHS_Tf[a]);
+          scalar[a] = scalar[a] + dt * (1.5 * RHS[a] - 0.5 * RHSf[a]);
         }
     const size_t ot = (size_t)(nz - 1) * nplane, ob = (size_t)(nz - 2) * nplane;
     if (cfg.lz_over_zi > 1.0) {
-      const double inc = dTdz_top / T_scale * z_i * dz;
-      for (size_t i = 0; i < nplane; ++i) theta[ot + i] = theta[ob + i] + inc;
+      const double inc = top_grad * dz;
+      for (size_t i = 0; i < nplane; ++i) scalar[ot + i] = scalar[ob + i] + inc;
     } else {
-      for (size_t i = 0; i < nplane; ++i) theta[ot + i] = theta[ob + i];
+      for (size_t i = 0; i < nplane; ++i) scalar[ot + i] = scalar[ob + i];
     }
   }
 
@@ -1466,10 +1492,48 @@ struct Oracle {
       for (size_t i = 0; i < nplane; ++i) dTdz[(size_t)(nz - 1) * nplane + i] = top;
     }
     RHS_Tf = RHS_T;
-    scalar_RHS_calc();
+    scalar_RHS_calc(theta, dTdx, dTdy, dTdz, RHS_T, wt_s, sgs_t3, false);
     calcbeta();
     if (jt == 1 && !initsc) RHS_Tf = RHS_T;
-    step_scalar();
+    step_scalar(theta, RHS_T, RHS_Tf, dTdz_top / T_scale * z_i);
+  }
+
+  // scalars_module_q.f90:31-141 (Pr_ = Pr for models 1-5)
+  void q_all_in_one() {
+    filt_da(qmix.data(), dqdx.data(), dqdy.data(), nz);
+    ddz_uv(dqdz.data(), qmix.data());
+    {
+      const double top = dqdz_top / q_scale * z_i;
+      for (size_t i = 0; i < nplane; ++i) dqdz[(size_t)(nz - 1) * nplane + i] = top;
+    }
+    RHS_qf = RHS_q;
+    scalar_RHS_calc(qmix, dqdx, dqdy, dqdz, RHS_q, wq_s, sgs_q3, true);
+    if (jt == 1 && !initsc) RHS_qf = RHS_q;
+    step_scalar(qmix, RHS_q, RHS_qf, dqdz_top / q_scale * z_i);
+  }
+
+  // atm_thermodynamics.f90:37-52 (k_global = jz), columns 1..nx; out: actual_T,
+  // actual_Tv, sat_vapor_pr, pr_atm, vapor_pr, sat_qmix, rel_hum, rel_hum_q, zlcl_all
+  void thermo(double* const* out) {
+    const double cp = 1005.0, Rd = 287.04, pr_surf = 100000.0;  // param.f90:90-96
+    for (int k = 0; k < 9; ++k) std::fill(out[k], out[k] + nfield, 0.0);
+    for (int jz = 1; jz <= nz - 1; ++jz)
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= nx; ++jx) {
+          const size_t a = I(jx, jy, jz);
+          const double zg = jz * dz * z_i;
+          const double aT = theta[a] - (g / cp) * (zg) / T_scale;
+          const double aTv = aT * (1 + 0.61 * 0.001 * qmix[a] * q_scale);
+          const double svp = 611.2 * std::exp(17.62 * (aT * T_scale - 273.2) / (243.12 + (aT * T_scale - 273.2)));
+          const double pa = pr_surf * std::exp(-(zg) / (Rd * aTv * T_scale / g));
+          const double vp = (0.001 * q_scale * qmix[a] / (0.001 * q_scale * qmix[a] + 0.622)) * pa;
+          const double sq = 0.622 * svp / (pa - svp);
+          const double rh = vp / svp;
+          const double rhq = 0.001 * q_scale * qmix[a] / sq;
+          const double zl = zg + (cp / g) * (aT * T_scale - 55 - std::pow(1 / (aT * T_scale - 55) - std::log(rhq) / 2840, -1.0));
+          out[0][a] = aT; out[1][a] = aTv; out[2][a] = svp; out[3][a] = pa; out[4][a] = vp;
+          out[5][a] = sq; out[6][a] = rh; out[7][a] = rhq; out[8][a] = zl;
+        }
   }
 
   // rmsdiv.f90:1-113
@@ -1514,8 +1578,12 @@ struct Oracle {
     ddz_w(dwdz.data(), w.data());
     wallstress();
     sgs_stag();
-    if (s_flag) theta_all_in_one();
-    else std::fill(beta_scal.begin(), beta_scal.end(), 0.0);
+    if (s_flag) {  // main.f90:272-275 (thermo writes diagnostics only)
+      theta_all_in_one();
+      if (q_flag) q_all_in_one();
+    } else {
+      std::fill(beta_scal.begin(), beta_scal.end(), 0.0);
+    }
     divstress_uv(divtx.data(), txx.data(), txy.data(), txz.data());
     divstress_uv(divty.data(), txy.data(), tyy.data(), tyz.data());
     divstress_w(divtz.data(), txz.data(), tyz.data(), tzz.data());
@@ -1583,6 +1651,9 @@ struct Oracle {
       case LES_PHI_M: return &phi_m; case LES_PSI_M: return &psi_m; case LES_PSI_M0: return &psi_m0;
       case LES_PHI_H: return &phi_h; case LES_PSI_H: return &psi_h; case LES_PSI_H0: return &psi_h0;
       case LES_SGS_T3_SFC: return &sgs_t3;
+      case LES_Q: return &qmix; case LES_RHS_Q: return &RHS_q; case LES_RHS_QF: return &RHS_qf;
+      case LES_DQDX: return &dqdx; case LES_DQDY: return &dqdy; case LES_DQDZ: return &dqdz;
+      case LES_WQ_S: return &wq_s; case LES_SGS_Q3_SFC: return &sgs_q3;
       default: return nullptr;
     }
   }
@@ -1712,5 +1783,11 @@ void lo_wallstress(void* h) { ((Oracle*)h)->wallstress(); }
 void lo_obukhov(void* h) { ((Oracle*)h)->obukhov(); }
 void lo_project(void* h) { ((Oracle*)h)->project(); }
 void lo_theta_all_in_one(void* h) { ((Oracle*)h)->theta_all_in_one(); }
+void lo_q_all_in_one(void* h) { ((Oracle*)h)->q_all_in_one(); }
+void lo_atm_thermodynamics(void* h, double* o0, double* o1, double* o2, double* o3, double* o4, double* o5,
+                           double* o6, double* o7, double* o8) {
+  double* o[9] = {o0, o1, o2, o3, o4, o5, o6, o7, o8};
+  ((Oracle*)h)->thermo(o);
+}
 
 }  // extern "C"

@@ -32,5 +32,16 @@ def test_estimate_bytes_without_gpu(gpu_lib):
 
 
 def test_config_struct_layout():
-    from les_gb300.config import LesConfig
-    assert ctypes.sizeof(LesConfig) == 12 * 4 + 11 * 8
+    """les_config in include/les_gb300.h: 12 ints, then 13 doubles; the
+    ctypes mirror and the field enumeration follow the header."""
+    from les_gb300.config import LesConfig, FIELDS
+    assert ctypes.sizeof(LesConfig) == 12 * 4 + 13 * 8
+    assert LesConfig.q_flag.offset == 11 * 4 and LesConfig.dqdz_top.offset == 12 * 4 + 12 * 8
+    txt = open(os.path.join(ROOT, "include", "les_gb300.h")).read()
+    enum = re.search(r"typedef enum les_field \{(.*?)\} les_field;", txt, flags=re.S).group(1)
+    enum = re.sub(r"/\*.*?\*/", "", enum, flags=re.S)
+    names = [n.strip().split("=")[0].strip() for n in enum.split(",") if n.strip()]
+    assert names[-1] == "LES_NUM_FIELDS" and len(names) - 1 == len(FIELDS)
+    assert names.index("LES_Q") == FIELDS.index("q")
+    assert names.index("LES_ZO") == FIELDS.index("zo")
+    assert names.index("LES_SGS_Q3_SFC") == FIELDS.index("sgs_q3")

@@ -1,0 +1,137 @@
+"""The humidity scalar qmix (scalars_module_q.f90:31-400: q_all_in_one,
+scalar_q_RHS_calc, step_scalar_q), its coupling into the buoyancy through
+the virtual temperature (scalars_module.f90:200-223 calcbeta) and into the
+Obukhov length through the moisture flux (scalars_module.f90:547-550), and
+the thermodynamic diagnostics (atm_thermodynamics.f90:25-60), on the GPU
+against the CPU oracle, through the C ABI.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import les_gb300 as lg
+from les_gb300.config import moisture_flux
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def libs(gpu_lib, oracle_lib):
+    return gpu_lib, oracle_lib
+
+
+def q_pair(n=32, jt0=0, seed=41, levels=None, precision=0):
+    from oracle.oracle import Oracle
+    cfg = lg.make_config(n, nz_levels=levels, s_flag=1, q_flag=1, jt_total0=jt0, rmsdiv_every=1,
+                         precision=precision)
+    surf = lg.striped_surface(cfg)
+    g = lg.Context(cfg, surf)
+    o = Oracle(cfg, surf) if precision == 0 else None
+    wq = moisture_flux(cfg)
+    g.set("wq_s", wq)
+    if o is not None:
+        o.set("wq_s", wq)
+    for k, v in lg.initial_state(cfg, surf, seed=seed).items():
+        g.set(k, v)
+        if o is not None:
+            o.set(k, v)
+    return cfg, g, o
+
+
+@pytest.mark.parametrize("jt0", [0, 500])
+def test_step_parity_32_humidity(libs, jt0):
+    """32^3 FP64 with theta and qmix, striped z0, heat and moisture fluxes,
+    10 steps (jt_total0 = 500: the dynamic Cs^2 feeds back from step 5)."""
+    cfg, g, o = q_pair(jt0=jt0)
+    g.step(10)
+    assert o.step(10) == 0
+    n = cfg.nx
+    for nm in ("u", "v", "theta", "q"):
+        e = rel(g.get(nm)[:-1, :, :n], o.get(nm)[:-1, :, :n])
+        assert e < TOL, (nm, e)
+    e = rel(g.get("w")[:, :, :n], o.get("w")[:, :, :n])
+    assert e < TOL, ("w", e)
+    assert rel(g.get("sgs_q3"), o.get("sgs_q3")) < TOL
+    assert rel(g.get("beta_scal"), o.get("beta_scal")) < 1e-10
+    # the moisture flux moistened the first level
+    q = g.get("q")[:-1, :, :n]
+    assert q[0].mean() > 10.0 / cfg.q_scale
+
+
+def test_q_all_in_one_and_thermodynamics_routines(libs):
+    """les_q_all_in_one and les_atm_thermodynamics on identical module state."""
+    cfg, g, o = q_pair(n=32, seed=43)
+    g.step(3)
+    assert o.step(3) == 0
+    names = ["u", "v", "w", "theta", "q", "RHS_q", "RHS_qf", "Nu_t", "ustar_avg", "phi_h", "psi_h",
+             "sgs_q3", "wq_s"]
+    for nm in names:
+        o.set(nm, g.get(nm))
+    g.call("q_all_in_one")
+    o.call("q_all_in_one")
+    n = cfg.nx
+    lev = slice(0, cfg.nz - 1)
+    for nm in ("q", "RHS_q", "dqdx", "dqdy", "dqdz"):
+        e = rel(g.get(nm)[lev, :, :n], o.get(nm)[lev, :, :n])
+        assert e < TOL, (nm, e)
+    shp = lg.config.field_shape(cfg, "u")
+    og = [np.zeros(shp) for _ in range(9)]
+    oo = [np.zeros(shp) for _ in range(9)]
+    o.set("theta", g.get("theta"))
+    o.set("q", g.get("q"))
+    g.call("atm_thermodynamics", *og)
+    o.call("atm_thermodynamics", *oo)
+    for k in range(9):
+        assert rel(og[k][:cfg.nz - 1, :, :n], oo[k][:cfg.nz - 1, :, :n]) < 1e-13, k
+
+
+def test_humidity_entry_points_refuse_without_q(gpu_lib):
+    cfg = lg.make_config(32, s_flag=1)
+    g = lg.Context(cfg, lg.striped_surface(cfg))
+    f = lg.lib().les_q_all_in_one
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p]
+    assert f(g.h) == -8  # LES_ERR_STATE
+    with pytest.raises(lg.LesError):
+        g.get("q")
+
+
+def test_mixed_form_with_humidity(gpu_lib):
+    """The FP32-mixed form carries qmix like theta (FP32 transforms of
+    q - plane mean, FP32-held horizontal gradients, FP64 state): per field
+    within 1e-5 of the FP64 form after 20 steps at 64^3."""
+    out = {}
+    for prec in (1, 0):
+        cfg, g, _ = q_pair(n=64, precision=prec, seed=44)
+        g.step(20)
+        out[prec] = {nm: g.get(nm)[:-1, :, :64] for nm in ("u", "v", "w", "theta", "q")}
+        out[prec]["rmsdiv"] = g.rmsdiv()
+        g.close()
+    for nm in ("u", "v", "w", "theta", "q"):
+        e = rel(out[1][nm], out[0][nm])
+        assert e <= 1e-5, (nm, e)
+    assert out[1]["rmsdiv"] <= 1e-10
+
+
+def test_checkpoint_carries_humidity(gpu_lib, tmp_path):
+    """With q_flag = 1 the restart record holds qmix, RHS_q and sgs_q3
+    (io.f90:1325-1330) instead of zeros, and reads them back bit for bit."""
+    cfg, g, _ = q_pair(n=32, seed=45, precision=0)
+    g.step(4)
+    path = os.fspath(tmp_path / "vel_sc.out")
+    g.checkpoint_write(path)
+    cfg2 = lg.make_config(32, s_flag=1, q_flag=1, jt_total0=4, initu=1, initsc=1, rmsdiv_every=1)
+    h = lg.Context(cfg2, lg.striped_surface(cfg2))
+    h.checkpoint_read(path)
+    for nm in ("q", "RHS_q"):
+        assert np.array_equal(h.get(nm), g.get(nm)), nm
+    assert np.array_equal(h.get("sgs_q3"), g.get("sgs_q3"))

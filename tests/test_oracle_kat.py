@@ -345,3 +345,101 @@ def test_interpolag_shifts_by_whole_cells(O, routine, fields, axis, shift):
         want = np.roll(v[:, :, :n], shift, axis=axis)
         assert np.allclose(o.get(f)[:, :, :n], want, rtol=0, atol=1e-15), f
     assert not o.get("u_lag").any() and not o.get("v_lag").any()
+
+
+# ---- humidity (scalars_module_q.f90, atm_thermodynamics.f90) ----------------
+
+def _q_pair(O, n=16, levels=8, **kw):
+    cfg = C.make_config(n, n, levels, s_flag=1, **kw)
+    surf = C.striped_surface(cfg)
+    o = O(cfg, surf)
+    for k, v in C.initial_state(cfg, surf, seed=5).items():
+        o.set(k, v)
+    return cfg, o
+
+
+def test_zero_humidity_leaves_the_step_unchanged(O):
+    """qmix = 0, wq_s = 0 and dqdz_top = 0: theta (1 + 0.61 0.001 qmix q_scale)
+    is theta and the moisture buoyancy flux is zero, so a q_flag = 1 run
+    gives the q_flag = 0 run's state bit for bit and qmix stays zero."""
+    cfg0, a = _q_pair(O)
+    cfg1, b = _q_pair(O, q_flag=1, dqdz_top=0.0)
+    b.set("q", np.zeros(C.field_shape(cfg1, "q")))
+    b.set("wq_s", np.zeros((cfg1.ny, cfg1.nx)))
+    assert a.step(4) == 0 and b.step(4) == 0
+    for nm in ("u", "v", "w", "theta", "p", "Cs_opt2"):
+        assert np.array_equal(a.get(nm), b.get(nm)), nm
+    assert not b.get("q").any()
+
+
+def test_surface_moisture_flux_first_step(O):
+    """Uniform wind, uniform qmix = 0.1, uniform surface moisture flux wq_s:
+    nothing advects or diffuses qmix in the first (Euler) step, whose
+    right-hand side is the surface flux divergence surf_flux / dz at level 1
+    (scalars_module_q.f90:174-178, 298-347, surf_flux = wq_s / q_scale / u_star)
+    and zero above (dqdz_top = 0)."""
+    n, lev = 16, 8
+    cfg = C.make_config(n, n, lev, s_flag=1, q_flag=1, dqdz_top=0.0)
+    surf = C.uniform_surface(cfg, 1e-4, 0.0)
+    o = O(cfg, surf)
+    shp = C.field_shape(cfg, "u")
+    u = np.zeros(shp)
+    u[:, :, :n] = 5.0
+    th = np.zeros(shp)
+    th[:, :, :n] = 300.0 / cfg.t_scale
+    q = np.zeros(shp)
+    q[:, :, :n] = 0.1
+    for nm, v in (("u", u), ("theta", th), ("q", q)):
+        o.set(nm, v)
+    wq = 0.05
+    o.set("wq_s", np.full((n, n), wq))
+    assert o.step(1) == 0
+    dz = cfg.lz_over_zi / (cfg.nz - 1)
+    inc = cfg.dt * (wq / cfg.q_scale / cfg.u_star) / dz
+    got = o.get("q")
+    assert np.allclose(got[0, :, :n], 0.1 + inc, rtol=0, atol=1e-13)
+    assert np.allclose(got[1:cfg.nz - 1, :, :n], 0.1, rtol=0, atol=1e-13)
+    assert np.allclose(o.get("sgs_q3"), wq / cfg.q_scale / cfg.u_star, rtol=1e-15)
+
+
+def test_humid_step_moistens_and_stays_finite(O):
+    """Striped surface with a striped moisture flux: 6 steps of the coupled
+    theta / qmix step stay finite, the first level moistens, and qmix enters
+    the buoyancy (beta_scal differs from the dry run's)."""
+    cfg, o = _q_pair(O, q_flag=1)
+    o.set("wq_s", C.moisture_flux(cfg))
+    q0 = o.get("q")[0, :, :cfg.nx].mean()
+    _, dry = _q_pair(O)
+    assert o.step(6) == 0 and dry.step(6) == 0
+    q = o.get("q")
+    assert np.isfinite(q).all()
+    assert q[0, :, :cfg.nx].mean() > q0
+    assert not np.array_equal(o.get("beta_scal"), dry.get("beta_scal"))
+
+
+def test_thermo_restatement(O):
+    """The oracle's thermo against a numpy writing of
+    atm_thermodynamics.f90:37-52 on a seeded theta / qmix state."""
+    cfg, o = _q_pair(O, q_flag=1)
+    shp = C.field_shape(cfg, "u")
+    out = [np.zeros(shp) for _ in range(9)]
+    o.call("atm_thermodynamics", *out)
+    th, q = o.get("theta"), o.get("q")
+    n, nz = cfg.nx, cfg.nz
+    dz = cfg.lz_over_zi / (nz - 1)
+    cp, Rd, prs, g = 1005.0, 287.04, 100000.0, cfg.g
+    k = np.arange(1, nz)[:, None, None]
+    zg = k * dz * cfg.z_i
+    T = th[:nz - 1, :, :n] - (g / cp) * zg / cfg.t_scale
+    qq = 0.001 * cfg.q_scale * q[:nz - 1, :, :n]
+    Tv = T * (1 + 0.61 * qq)
+    es = 611.2 * np.exp(17.62 * (T * cfg.t_scale - 273.2) / (243.12 + (T * cfg.t_scale - 273.2)))
+    p = prs * np.exp(-zg / (Rd * Tv * cfg.t_scale / g))
+    e = qq / (qq + 0.622) * p
+    qs = 0.622 * es / (p - es)
+    rq = qq / qs
+    zl = zg + (cp / g) * (T * cfg.t_scale - 55 - 1.0 / (1 / (T * cfg.t_scale - 55) - np.log(rq) / 2840))
+    for a, b in zip(out, (T, Tv, es, p, e, qs, e / es, rq, zl)):
+        assert rel(a[:nz - 1, :, :n], b) < 1e-13
+        assert not a[nz - 1].any() and not a[:, :, n:].any()
+    assert 0.0 < rq.min() and rq.max() < 1.5
