@@ -68,7 +68,13 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-serve", action="store_true", help="skip the served-ensemble latency run")
+    p.add_argument("--threads", type=int, default=0,
+                   help="--impl reference: host threads of the CPU step (0: all)")
     p.add_argument("--serve-requests", type=int, default=200)
+    p.add_argument("--capture-step", action="store_true",
+                   help="after the warm-up, run one step of --prof-family's transforms bracketed by "
+                        "cudaProfilerStart/Stop (for ncu --profile-from-start off) and print its "
+                        "launches and algorithmic bytes, then exit")
     p.add_argument("--prof-family", type=int, default=0,
                    help="transform family for the roofline object: 1 FP64/float-float y pass, 2 FP32 y pass, "
                         "3 FP64/float-float x pass, 4 FP32 x pass (default: the largest share of the step)")
@@ -194,7 +200,8 @@ def run_reference(args):
     oracle_build()
     cfg, surf = workload_config(lg, args.grid, "fp64")
     o = Oracle(cfg, surf)
-    cores = Oracle.max_threads()
+    cores = args.threads if args.threads > 0 else Oracle.max_threads()
+    Oracle.set_threads(cores)
     for k, v in lg.initial_state(cfg, surf, seed=1234).items():
         o.set(k, v)
     for _ in range(max(args.warmup, 0)):
@@ -307,6 +314,16 @@ def main():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
+    if args.capture_step:
+        fam = args.prof_family or 4
+        torch.cuda.profiler.start()
+        ms_c, _, pr = timed_steps(torch, lg, ctx, 1, prof_family=fam)
+        torch.cuda.profiler.stop()
+        print(json.dumps({"capture_step": FAMILIES[fam], "family": fam, "launches": pr[0],
+                          "algorithmic_bytes": pr[2], "family_ms": pr[1], "step_ms": ms_c,
+                          "grid": [cfg.nx, cfg.ny, cfg.nz - 1], "form": args.form}), flush=True)
+        ctx.close()
+        return
     cflu, visc = ctx.timestep_conditions()
     # share of the step of each transform family (short untimed pre-pass)
     fam_share = {}
