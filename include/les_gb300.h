@@ -154,6 +154,34 @@ int les_sync_to_host(les_ctx* ctx);
 /* Step counters (param.f90:147-148). */
 int les_get_counters(les_ctx* ctx, int* jt, int* jt_total);
 
+/* Running statistics, io.f90:403-1218 (MM_XYZ_Out): time averages of 133
+ * quantities on the (nx,ny,nz-1) grid (first to third moments of the
+ * velocity, pressure, theta and qmix interpolated to the w nodes, fluxes,
+ * gradients, SGS stresses and their products with strains and velocities,
+ * pressure transport, the thermodynamic diagnostics), held on the device in
+ * FP64.  les_stats_enable allocates them (133 nx ny (nz-1) doubles) and
+ * zeroes them; with auto_accumulate = 1, les_step and les_step_graph
+ * accumulate after every step whose jt is a multiple of c_count, as
+ * output_loop does (io.f90:211-213; needs s_flag).  les_stats_accumulate is
+ * one call of MM_XYZ_Out's accumulation on the current module state
+ * (weight c_count / p_count; every statistic zeroed first when jt_total <=
+ * c_count, io.f90:457-502).  The reference writes and zeroes two groups of
+ * statistics every p_count and 2 p_count steps (io.f90:966-1217): the
+ * caller reads them with les_stats_get and zeroes them with les_stats_reset
+ * (group 1 or 2); les_stats_group tells each statistic's group (0: the
+ * reference never zeroes it, atxy).  Statistic i (0 <= i < les_stats_count())
+ * is named by les_stats_name(i) after the reference's array (au, u2, awt,
+ * at11s11, azlcl_all, ...).  The output files themselves stay with the
+ * caller.  Thermodynamic statistics use qmix = 0 without humidity, as the
+ * reference does. */
+int les_stats_enable(les_ctx* ctx, int c_count, int p_count, int auto_accumulate);
+int les_stats_accumulate(les_ctx* ctx);
+int les_stats_count(void);
+const char* les_stats_name(int i);
+int les_stats_group(int i);
+int les_stats_get(les_ctx* ctx, int i, double* host);  /* (nx,ny,nz-1) */
+int les_stats_reset(les_ctx* ctx, int group);
+
 /* Whole-member state image, for a server that evicts a member from the
  * device and resumes it later: every module array in its device storage
  * (the FP32-held fields of a precision-1 context as they are) plus the step

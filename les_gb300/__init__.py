@@ -203,6 +203,23 @@ class Context:
         f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         check(f(self.h, ctypes.c_void_p(buf.ctypes.data), ctypes.c_size_t(buf.nbytes)))
 
+    # --- running statistics (io.f90:403-1218 MM_XYZ_Out) ---------------------
+    def stats_enable(self, c_count, p_count, auto=False):
+        check(self.L.les_stats_enable(self.h, int(c_count), int(p_count), 1 if auto else 0))
+
+    def stats_accumulate(self):
+        check(self.L.les_stats_accumulate(self.h))
+
+    def stats_reset(self, group):
+        check(self.L.les_stats_reset(self.h, int(group)))
+
+    def stats_get(self, name):
+        """One statistic by the reference's array name, (nz-1, ny, nx)."""
+        i = stats_names().index(name)
+        out = np.empty((self.cfg.nz - 1, self.cfg.ny, self.cfg.nx))
+        check(self.L.les_stats_get(self.h, int(i), _ptr(out)))
+        return out
+
     # --- checkpoint record (io.f90:1314-1338, initial.f90:54-160) ------------
     def checkpoint_write(self, path):
         check(self.L.les_checkpoint_write(self.h, os.fsencode(path)))
@@ -265,6 +282,19 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+def stats_names():
+    """Names of the running statistics in the library's order."""
+    L = lib()
+    L.les_stats_name.restype = ctypes.c_char_p
+    L.les_stats_name.argtypes = [ctypes.c_int]
+    return [L.les_stats_name(i).decode() for i in range(L.les_stats_count())]
+
+
+def stats_groups():
+    L = lib()
+    return {n: L.les_stats_group(i) for i, n in enumerate(stats_names())}
 
 
 def estimate_device_bytes(cfg):

@@ -13,7 +13,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liblesgb300.so")
-UNITS = ["fft_kernels.cu", "fft_fixed.cu", "ops.cu", "les_api.cu", "noalloc.cu", "checkpoint.cu"]
+UNITS = ["fft_kernels.cu", "fft_fixed.cu", "ops.cu", "les_api.cu", "noalloc.cu", "checkpoint.cu", "stats.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr"]

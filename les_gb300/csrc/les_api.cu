@@ -579,12 +579,19 @@ int les_state_restore(les_ctx* c, const void* host, size_t bytes) {
   return LES_OK;
 }
 
+// output_loop's running statistics (io.f90:211-213) after a step, when
+// les_stats_enable asked for them
+static void stats_after_step(les_ctx* c) {
+  if (c->stats && c->stats_auto && c->cfg.s_flag && c->jt % c->stats_c == 0) op_stats(c);
+}
+
 int les_step(les_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return LES_ERR_ARG;
   if (!c->surface_set) { les_set_error("les_set_surface must be called before les_step"); return LES_ERR_STATE; }
   for (int i = 0; i < nsteps; ++i) {
     int st = c->cfg.precision == 1 ? step_mixed(c) : step_fp64(c);
     if (st) return st;
+    stats_after_step(c);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { les_set_error("%s", cudaGetErrorString(e)); return LES_ERR_CUDA; }
@@ -626,6 +633,7 @@ int les_step_graph(les_ctx* c, int nsteps) {
     if (special_step(c, nj)) {
       int st = run_step(c);
       if (st) return st;
+      stats_after_step(c);
       continue;
     }
     int lag, ov;
@@ -643,6 +651,7 @@ int les_step_graph(les_ctx* c, int nsteps) {
     rhs_swap(c);  // what the replayed step did
     c->jt = nj;
     c->jt_total = nt;
+    stats_after_step(c);
   }
   return LES_OK;
 }

@@ -93,6 +93,9 @@ struct les_ctx {
   // 28..33 the mixed form's per-level mean-wind factors (float-float);
   // 34..35 the mixed form's txz, tyz plane means
   double* dred = nullptr;
+  // running statistics (MM_XYZ_Out): 133 accumulators of nx ny (nz-1)
+  double* stats = nullptr;
+  int stats_c = 0, stats_p = 0, stats_auto = 0;
   double* host_scal = nullptr;                 // pinned host mirror
   size_t bytes = 0;
   std::vector<void*> allocs;
@@ -158,6 +161,7 @@ int op_stddyn(les_ctx* c, double* cs_z_dev, const double* const* S);
 int op_theta(les_ctx* c);
 int op_q(les_ctx* c);
 int op_thermo(les_ctx* c, double* const* out);  // 9 (ld,ny,nz) arrays, atm_thermodynamics.f90 order
+int op_stats(les_ctx* c);                        // one MM_XYZ_Out accumulation (io.f90:403-866)
 int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz);
 int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz, int w_variant);
 int op_convec(les_ctx* c, double* cx, double* cy, double* cz);

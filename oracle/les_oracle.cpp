@@ -47,6 +47,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <map>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -91,6 +92,13 @@ struct Oracle {
   // bottombc.f90:9-16 (nx,ny)
   Field zo, z_os, wt_s, ustar_avg, phi_m, psi_m, psi_m0, phi_h, psi_h, psi_h0, sgs_t3;
   Field wq_s, sgs_q3;  // bottombc.f90:15, scalars_module_q.f90:23 (level 1)
+  // the whole vertical SGS flux arrays sgs_t3, sgs_q3 (ld,ny,nz) of
+  // scalar_RHS_calc (level 1 the surface flux), read by MM_XYZ_Out
+  Field sgs_t3_vol, sgs_q3_vol;
+  // io.f90:403-1218 MM_XYZ_Out running statistics, (nx,ny,nz-1) each
+  std::vector<Field> stats;
+  std::vector<std::string> stat_names;
+  int stats_c = 0, stats_p = 0;
   // fft.f90:19, test_filtermodule.f90:9
   Field kx, ky, k2, G_test, G_test_test;
   double rmsdiv_last = 0.0;
@@ -128,7 +136,7 @@ struct Oracle {
                    &txx, &txy, &tyy, &txz, &tyz, &tzz, &divtx, &divty, &divtz, &F_LM, &F_MM,
                    &F_QN, &F_NN, &Beta, &Cs_opt2, &Nu_t, &u_lag, &v_lag, &w_lag, &S11, &S12,
                    &S13, &S22, &S23, &S33, &beta_scal, &dTdx, &dTdy, &dTdz, &RHS_T, &RHS_Tf,
-                   &qmix, &dqdx, &dqdy, &dqdz, &RHS_q, &RHS_qf};
+                   &qmix, &dqdx, &dqdy, &dqdz, &RHS_q, &RHS_qf, &sgs_t3_vol, &sgs_q3_vol};
     for (Field* f : fl) f->assign(nfield, 0.0);
     p.assign(nplane * (nz + 1), 0.0);
     Field* sf[] = {&zo, &z_os, &wt_s, &ustar_avg, &phi_m, &psi_m, &psi_m0, &phi_h, &psi_h,
@@ -1345,7 +1353,7 @@ struct Oracle {
   // algorithm on the scalar's arrays; the surface flux is wt_s/(T_scale u_star)
   // for theta and wq_s/q_scale/u_star for qmix (lbc = 1)
   void scalar_RHS_calc(const Field& scalar, Field& dsdx, Field& dsdy, Field& dsdz, Field& RHS, const Field& flux,
-                       Field& sgs_vert, bool humidity) {
+                       Field& sgs_vert, Field& sgs_vol, bool humidity) {
     std::vector<double> ustar_local = ustar_avg;
     std::vector<double> sn1(nplane);
     for (size_t i = 0; i < nplane; ++i) sn1[i] = scalar[i];
@@ -1421,6 +1429,7 @@ struct Oracle {
         RHS[a] = RHS[a] + dtemp[a];
         temp[a] = -1.0 * surf_flux[S2(i, j)];
         sgs_vert[S2(i, j)] = surf_flux[S2(i, j)];
+        sgs_vol[a] = surf_flux[S2(i, j)];
       }
     for (int k = 2; k <= nz; ++k)
       for (int j = 1; j <= ny; ++j)
@@ -1428,6 +1437,7 @@ struct Oracle {
           const size_t a = I(i, j, k);
           RHS[a] = RHS[a] + dtemp[a];
           temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdz[a];
+          sgs_vol[a] = -1.0 * temp[a];
         }
     std::fill(dtemp.begin(), dtemp.end(), 0.0);
     ddz_w(dtemp.data(), temp.data());
@@ -1492,7 +1502,7 @@ struct Oracle {
       for (size_t i = 0; i < nplane; ++i) dTdz[(size_t)(nz - 1) * nplane + i] = top;
     }
     RHS_Tf = RHS_T;
-    scalar_RHS_calc(theta, dTdx, dTdy, dTdz, RHS_T, wt_s, sgs_t3, false);
+    scalar_RHS_calc(theta, dTdx, dTdy, dTdz, RHS_T, wt_s, sgs_t3, sgs_t3_vol, false);
     calcbeta();
     if (jt == 1 && !initsc) RHS_Tf = RHS_T;
     step_scalar(theta, RHS_T, RHS_Tf, dTdz_top / T_scale * z_i);
@@ -1507,7 +1517,7 @@ struct Oracle {
       for (size_t i = 0; i < nplane; ++i) dqdz[(size_t)(nz - 1) * nplane + i] = top;
     }
     RHS_qf = RHS_q;
-    scalar_RHS_calc(qmix, dqdx, dqdy, dqdz, RHS_q, wq_s, sgs_q3, true);
+    scalar_RHS_calc(qmix, dqdx, dqdy, dqdz, RHS_q, wq_s, sgs_q3, sgs_q3_vol, true);
     if (jt == 1 && !initsc) RHS_qf = RHS_q;
     step_scalar(qmix, RHS_q, RHS_qf, dqdz_top / q_scale * z_i);
   }
@@ -1534,6 +1544,181 @@ struct Oracle {
           out[0][a] = aT; out[1][a] = aTv; out[2][a] = svp; out[3][a] = pa; out[4][a] = vp;
           out[5][a] = sq; out[6][a] = rh; out[7][a] = rhq; out[8][a] = zl;
         }
+  }
+
+  // io.f90:403-1218 MM_XYZ_Out, the accumulation (the output files are the
+  // caller's): statistics by the reference's array names
+  Field& st(const char* name) {
+    for (size_t i = 0; i < stat_names.size(); ++i)
+      if (stat_names[i] == name) return stats[i];
+    stat_names.push_back(name);
+    stats.emplace_back((size_t)nx * ny * (nz - 1), 0.0);
+    return stats.back();
+  }
+  void stats_enable(int c_count, int p_count) {
+    stats_c = c_count;
+    stats_p = p_count;
+    for (Field& f : stats) std::fill(f.begin(), f.end(), 0.0);
+  }
+  void stats_accumulate() {
+    const size_t SN = (size_t)nx * ny * (nz - 1);
+    static const char* const all[] = {
+        "au", "av", "aw", "ap", "atheta", "aq", "p2", "u2", "v2", "w2", "theta2", "q2", "u3", "v3", "w3", "q3",
+        "T3", "adudx", "adudy", "adudz", "advdx", "advdy", "advdz", "adwdx", "adwdy", "adwdz", "adTdx", "adTdy",
+        "adTdz", "adqdx", "adqdy", "adqdz", "adpdx", "adpdy", "adpdz", "tke", "awe", "aue", "ave", "auw", "avw",
+        "awt", "awq", "aut", "avt", "auq", "avq", "auv", "awuu", "awvv", "awqq", "awtt", "awwu", "awwv", "awwt",
+        "awwq", "atxx", "atxz", "atyy", "atyz", "atzz", "aup", "avp", "awp", "atp", "aqp", "atq", "aupx", "aupy",
+        "aupz", "avpx", "avpy", "avpz", "awpx", "awpy", "awpz", "at11ux", "at12uy", "at13uz", "at21vx", "at22vy",
+        "at23vz", "at31wx", "at32wy", "at33wz", "apux", "apuy", "apuz", "apvx", "apvy", "apvz", "apwx", "apwy",
+        "apwz", "aptx", "apty", "aptz", "apqx", "apqy", "apqz", "at11s11", "at12s12", "at13s13", "at22s22",
+        "at23s23", "at33s33", "as11", "as12", "as13", "as22", "as23", "as33", "aut11", "aut12", "aut13", "avt21",
+        "avt22", "avt23", "awt31", "awt32", "awt33", "asgst3", "asgsq3", "aactual_T", "aactual_Tv", "apr_atm",
+        "arel_hum", "arel_hum_q", "avapor_pr", "asat_vapor_pr", "asat_qmix", "azlcl_all"};
+    for (const char* nm : all) st(nm);
+    st("atxy");  // never zeroed (io.f90:457-502 and the output blocks leave it out)
+    if (jt_total <= stats_c)  // io.f90:457
+      for (const char* nm : all) std::fill(st(nm).begin(), st(nm).end(), 0.0);
+    // atm_thermodynamics.f90:37-52 of the current theta, qmix (thermo() ran
+    // on them at the end of the step)
+    std::vector<Field> th(9, Field(nfield, 0.0));
+    {
+      const double cp = 1005.0, Rd = 287.04, pr_surf = 100000.0;
+      for (int jz = 1; jz <= nz - 1; ++jz)
+        for (int jy = 1; jy <= ny; ++jy)
+          for (int jx = 1; jx <= nx; ++jx) {
+            const size_t a = I(jx, jy, jz);
+            const double qa = q_flag ? qmix[a] : 0.0;
+            const double zg = jz * dz * z_i;
+            const double aT = theta[a] - (g / cp) * (zg) / T_scale;
+            const double aTv = aT * (1 + 0.61 * 0.001 * qa * q_scale);
+            const double svp = 611.2 * std::exp(17.62 * (aT * T_scale - 273.2) / (243.12 + (aT * T_scale - 273.2)));
+            const double pa = pr_surf * std::exp(-(zg) / (Rd * aTv * T_scale / g));
+            const double vp = (0.001 * q_scale * qa / (0.001 * q_scale * qa + 0.622)) * pa;
+            const double sq = 0.622 * svp / (pa - svp);
+            const double rhq = 0.001 * q_scale * qa / sq;
+            th[0][a] = aT; th[1][a] = aTv; th[2][a] = svp; th[3][a] = pa; th[4][a] = vp; th[5][a] = sq;
+            th[6][a] = vp / svp; th[7][a] = rhq;
+            th[8][a] = zg + (cp / g) * (aT * T_scale - 55 - std::pow(1 / (aT * T_scale - 55) - std::log(rhq) / 2840, -1.0));
+          }
+    }
+    const double fr = (1.0 / (double)stats_p) * (double)stats_c;  // io.f90:504
+    auto Q = [&](const Field& f, size_t a) { return q_flag ? f[a] : 0.0; };
+    std::map<std::string, double*> ptr;
+    for (size_t i = 0; i < stat_names.size(); ++i) ptr[stat_names[i]] = stats[i].data();
+    for (int k = 1; k <= nz - 1; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          const size_t a = I(i, j, k), o = (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (k - 1));
+          double arg1, arg2, arg3, arg4, arg7, arg8, ux, uy, uz, vx, vy, vz, wx, wy, wz, px, py, pz, tx, ty, tz, qx,
+              qy, qz;
+          if (k == 1) {  // io.f90:531-581
+            const size_t b = I(i, j, k + 1);
+            arg1 = u[a]; arg2 = v[a]; arg3 = 0.25 * w[b];
+            arg4 = p[P(i, j, k)] - 0.5 * (arg1 * arg1 + arg2 * arg2 + arg3 * arg3);
+            arg7 = theta[a]; arg8 = Q(qmix, a);
+            ux = dudx[a]; uy = dudy[a]; uz = dudz[a];
+            vx = dvdx[a]; vy = dvdy[a]; vz = dvdz[a];
+            wx = ((dwdx[b]) / 2.0); wy = ((dwdy[b]) / 2.0); wz = dwdz[a];
+            px = dpdx[a] - arg1 * ux - arg2 * vx - arg3 * wx;
+            py = dpdy[a] - arg1 * uy - arg2 * vy - arg3 * wy;
+            pz = dpdz[a] - arg1 * uz - arg2 * vz - arg3 * wz;
+            tx = dTdx[a]; ty = dTdy[a]; tz = dTdz[a];
+            qx = Q(dqdx, a); qy = Q(dqdy, a); qz = Q(dqdz, a);
+          } else {  // io.f90:583-622
+            const size_t m = I(i, j, k - 1);
+            arg1 = (u[a] + u[m]) / 2.0; arg2 = (v[a] + v[m]) / 2.0; arg3 = w[a];
+            arg4 = ((p[P(i, j, k)] + p[P(i, j, k - 1)]) / 2.0 - 0.5 * (arg1 * arg1 + arg2 * arg2 + arg3 * arg3));
+            arg7 = (theta[a] + theta[m]) / 2.0; arg8 = (Q(qmix, a) + Q(qmix, m)) / 2.0;
+            ux = ((dudx[a] + dudx[m]) / 2.0); uy = ((dudy[a] + dudy[m]) / 2.0); uz = dudz[a];
+            vx = ((dvdx[a] + dvdx[m]) / 2.0); vy = ((dvdy[a] + dvdy[m]) / 2.0); vz = dvdz[a];
+            wx = dwdx[a]; wy = dwdy[a]; wz = ((dwdz[a] + dwdz[m]) / 2.0);
+            px = ((dpdx[a] + dpdx[m]) / 2.0) - arg1 * ux - arg2 * vx - arg3 * wx;
+            py = ((dpdy[a] + dpdy[m]) / 2.0) - arg1 * uy - arg2 * vy - arg3 * wy;
+            pz = dpdz[a] - arg1 * uz - arg2 * vz - arg3 * wz;
+            tx = ((dTdx[a] + dTdx[m]) / 2.0); ty = ((dTdy[a] + dTdy[m]) / 2.0); tz = dTdz[a];
+            qx = ((Q(dqdx, a) + Q(dqdx, m)) / 2.0); qy = ((Q(dqdy, a) + Q(dqdy, m)) / 2.0); qz = Q(dqdz, a);
+          }
+          auto A = [&](const char* nm, double val) { double* f = ptr.at(nm); f[o] = f[o] + val; };
+          // io.f90:628-639
+          A("aactual_T", fr * th[0][a] * T_scale); A("aactual_Tv", fr * th[1][a] * T_scale);
+          A("apr_atm", fr * th[3][a]); A("arel_hum", fr * th[6][a]); A("arel_hum_q", fr * th[7][a]);
+          A("avapor_pr", fr * th[4][a]); A("asat_vapor_pr", fr * th[2][a]); A("asat_qmix", fr * th[5][a]);
+          A("azlcl_all", fr * th[8][a]);
+          // io.f90:642-717
+          A("au", fr * arg1); A("av", fr * arg2); A("aw", fr * arg3); A("ap", fr * arg4);
+          A("atheta", fr * arg7); A("aq", fr * arg8);
+          A("u2", fr * arg1 * arg1); A("v2", fr * arg2 * arg2); A("w2", fr * arg3 * arg3);
+          A("p2", fr * arg4 * arg4); A("theta2", fr * arg7 * arg7); A("q2", fr * arg8 * arg8);
+          A("tke", fr * (0.5 * (arg1 * arg1 + arg2 * arg2 + arg3 * arg3)));
+          A("u3", fr * arg1 * arg1 * arg1); A("v3", fr * arg2 * arg2 * arg2); A("w3", fr * arg3 * arg3 * arg3);
+          A("T3", fr * arg7 * arg7 * arg7); A("q3", fr * arg8 * arg8 * arg8);
+          A("awe", fr * arg3 * (0.5 * (arg1 * arg1 + arg2 * arg2 + arg3 * arg3)));
+          A("ave", fr * arg2 * (0.5 * (arg1 * arg1 + arg2 * arg2 + arg3 * arg3)));
+          A("aue", fr * arg1 * (0.5 * (arg1 * arg1 + arg2 * arg2 + arg3 * arg3)));
+          A("auw", fr * arg1 * arg3); A("avw", fr * arg2 * arg3); A("awt", fr * arg3 * arg7);
+          A("awq", fr * arg3 * arg8); A("auv", fr * arg1 * arg2); A("aut", fr * arg1 * arg7);
+          A("avt", fr * arg2 * arg7); A("auq", fr * arg1 * arg8); A("avq", fr * arg2 * arg8);
+          A("awuu", fr * arg3 * arg1 * arg1); A("awvv", fr * arg3 * arg2 * arg2); A("awtt", fr * arg3 * arg7 * arg7);
+          A("awqq", fr * arg3 * arg8 * arg8); A("awwu", fr * arg3 * arg3 * arg1); A("awwv", fr * arg3 * arg3 * arg2);
+          A("awwt", fr * arg3 * arg3 * arg7); A("awwq", fr * arg3 * arg3 * arg8);
+          A("asgst3", fr * (sgs_t3_vol[a]));
+          A("asgsq3", fr * (q_flag ? sgs_q3_vol[a] : 0.0));
+          // io.f90:751-773
+          A("adudx", fr * ux); A("adudy", fr * uy); A("adudz", fr * uz);
+          A("advdx", fr * vx); A("advdy", fr * vy); A("advdz", fr * vz);
+          A("adwdx", fr * wx); A("adwdy", fr * wy); A("adwdz", fr * wz);
+          A("adTdx", fr * tx); A("adTdy", fr * ty); A("adTdz", fr * tz);
+          A("adqdx", fr * qx); A("adqdy", fr * qy); A("adqdz", fr * qz);
+          A("adpdx", fr * px); A("adpdy", fr * py); A("adpdz", fr * pz);
+          // io.f90:778-846
+          A("atxx", fr * txx[a]); A("atxy", fr * txy[a]); A("atxz", fr * txz[a]);
+          A("atyz", fr * tyz[a]); A("atyy", fr * tyy[a]); A("atzz", fr * tzz[a]);
+          A("aup", fr * arg1 * arg4); A("avp", fr * arg2 * arg4); A("awp", fr * arg3 * arg4);
+          A("atp", fr * arg7 * arg4); A("aqp", fr * arg8 * arg4); A("atq", fr * arg7 * arg8);
+          A("aupx", fr * arg1 * px); A("aupy", fr * arg1 * py); A("aupz", fr * arg1 * pz);
+          A("avpx", fr * arg2 * px); A("avpy", fr * arg2 * py); A("avpz", fr * arg2 * pz);
+          A("awpx", fr * arg3 * px); A("awpy", fr * arg3 * py); A("awpz", fr * arg3 * pz);
+          A("at11ux", fr * txx[a] * dudx[a]); A("at12uy", fr * txy[a] * dudy[a]); A("at13uz", fr * txz[a] * dudz[a]);
+          A("at21vx", fr * txy[a] * dvdx[a]); A("at22vy", fr * tyy[a] * dvdy[a]); A("at23vz", fr * tyz[a] * dvdz[a]);
+          A("at31wx", fr * txz[a] * dwdx[a]); A("at32wy", fr * tyz[a] * dwdy[a]); A("at33wz", fr * tzz[a] * dwdz[a]);
+          A("apux", fr * arg4 * ux); A("apuy", fr * arg4 * uy); A("apuz", fr * arg4 * uz);
+          A("apvx", fr * arg4 * vx); A("apvy", fr * arg4 * vy); A("apvz", fr * arg4 * vz);
+          A("apwx", fr * arg4 * wx); A("apwy", fr * arg4 * wy); A("apwz", fr * arg4 * wz);
+          A("aptx", fr * arg4 * tx); A("apty", fr * arg4 * ty); A("aptz", fr * arg4 * tz);
+          A("apqx", fr * arg4 * qx); A("apqy", fr * arg4 * qy); A("apqz", fr * arg4 * qz);
+          // io.f90:851-876
+          const double S11_ = ux, S12_ = 0.5 * (uy + vx), S13_ = 0.5 * (uz + wx);
+          const double S22_ = vy, S23_ = 0.5 * (vz + wy), S33_ = wz;
+          A("as11", fr * S11_); A("as12", fr * S12_); A("as13", fr * S13_);
+          A("as22", fr * S22_); A("as23", fr * S23_); A("as33", fr * S33_);
+          A("at11s11", fr * txx[a] * S11_); A("at12s12", fr * txy[a] * S12_); A("at13s13", fr * txz[a] * S13_);
+          A("at22s22", fr * tyy[a] * S22_); A("at23s23", fr * tyz[a] * S23_); A("at33s33", fr * tzz[a] * S33_);
+          A("aut11", fr * txx[a] * arg1); A("aut12", fr * txy[a] * arg1); A("aut13", fr * txz[a] * arg1);
+          A("avt21", fr * txy[a] * arg2); A("avt22", fr * tyy[a] * arg2); A("avt23", fr * tyz[a] * arg2);
+          A("awt31", fr * txz[a] * arg3); A("awt32", fr * tyz[a] * arg3); A("awt33", fr * tzz[a] * arg3);
+        }
+    (void)SN;
+  }
+  // the zeroing after output, io.f90:997-1006 (group 1, every p_count steps)
+  // and io.f90:1189-1216 (group 2, every 2 p_count steps)
+  void stats_reset(int group) {
+    static const char* const g1[] = {"au", "av", "aw", "atheta", "aq", "u2", "v2", "w2", "theta2", "q2", "auw",
+                                     "avw", "awt", "awq", "atxz", "atyz", "asgst3", "asgsq3", "azlcl_all"};
+    static const char* const g2[] = {
+        "ap", "p2", "u3", "v3", "w3", "q3", "T3", "adudx", "adudy", "adudz", "advdx", "advdy", "advdz", "adwdx",
+        "adwdy", "adwdz", "adTdx", "adTdy", "adTdz", "adqdx", "adqdy", "adqdz", "adpdx", "adpdy", "adpdz", "tke",
+        "awe", "aue", "ave", "aut", "avt", "auq", "avq", "auv", "awuu", "awvv", "awqq", "awtt", "awwu", "awwv",
+        "awwt", "awwq", "atxx", "atyy", "atzz", "aup", "avp", "awp", "atp", "aqp", "atq", "aupx", "aupy", "aupz",
+        "avpx", "avpy", "avpz", "awpx", "awpy", "awpz", "at11ux", "at12uy", "at13uz", "at21vx", "at22vy", "at23vz",
+        "at31wx", "at32wy", "at33wz", "apux", "apuy", "apuz", "apvx", "apvy", "apvz", "apwx", "apwy", "apwz",
+        "aptx", "apty", "aptz", "apqx", "apqy", "apqz", "at11s11", "at12s12", "at13s13", "at22s22", "at23s23",
+        "at33s33", "as11", "as12", "as13", "as22", "as23", "as33", "aut11", "aut12", "aut13", "avt21", "avt22",
+        "avt23", "awt31", "awt32", "awt33", "aactual_T", "aactual_Tv", "apr_atm", "arel_hum", "arel_hum_q",
+        "avapor_pr", "asat_vapor_pr", "asat_qmix"};
+    if (group == 1)
+      for (const char* nm : g1) std::fill(st(nm).begin(), st(nm).end(), 0.0);
+    if (group == 2)
+      for (const char* nm : g2) std::fill(st(nm).begin(), st(nm).end(), 0.0);
   }
 
   // rmsdiv.f90:1-113
@@ -1784,6 +1969,19 @@ void lo_obukhov(void* h) { ((Oracle*)h)->obukhov(); }
 void lo_project(void* h) { ((Oracle*)h)->project(); }
 void lo_theta_all_in_one(void* h) { ((Oracle*)h)->theta_all_in_one(); }
 void lo_q_all_in_one(void* h) { ((Oracle*)h)->q_all_in_one(); }
+void lo_stats_enable(void* h, int c_count, int p_count) { ((Oracle*)h)->stats_enable(c_count, p_count); }
+void lo_stats_accumulate(void* h) { ((Oracle*)h)->stats_accumulate(); }
+void lo_stats_reset(void* h, int group) { ((Oracle*)h)->stats_reset(group); }
+// statistic by name into out (nx,ny,nz-1); 0 if it exists
+int lo_stats_get(void* h, const char* name, double* out) {
+  Oracle* o = (Oracle*)h;
+  for (size_t i = 0; i < o->stat_names.size(); ++i)
+    if (o->stat_names[i] == name) {
+      std::copy(o->stats[i].begin(), o->stats[i].end(), out);
+      return 0;
+    }
+  return -1;
+}
 void lo_atm_thermodynamics(void* h, double* o0, double* o1, double* o2, double* o3, double* o4, double* o5,
                            double* o6, double* o7, double* o8) {
   double* o[9] = {o0, o1, o2, o3, o4, o5, o6, o7, o8};

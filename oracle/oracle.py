@@ -109,3 +109,21 @@ class Oracle:
     def call(self, name, *arrays, ints=()):
         args = [ctypes.c_void_p(self.h)] + [_p(a) for a in arrays] + [ctypes.c_int(i) for i in ints]
         return getattr(self.L, "lo_" + name)(*args)
+
+    # running statistics (io.f90:403-1218), by the reference's array names
+    def stats_enable(self, c_count, p_count):
+        self.L.lo_stats_enable(ctypes.c_void_p(self.h), int(c_count), int(p_count))
+
+    def stats_accumulate(self):
+        self.L.lo_stats_accumulate(ctypes.c_void_p(self.h))
+
+    def stats_reset(self, group):
+        self.L.lo_stats_reset(ctypes.c_void_p(self.h), int(group))
+
+    def stats_get(self, name):
+        out = np.zeros((self.cfg.nz - 1, self.cfg.ny, self.cfg.nx))
+        f = self.L.lo_stats_get
+        f.restype = ctypes.c_int
+        if f(ctypes.c_void_p(self.h), name.encode(), _p(out)) != 0:
+            raise KeyError(name)
+        return out

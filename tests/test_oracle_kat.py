@@ -443,3 +443,43 @@ def test_thermo_restatement(O):
         assert rel(a[:nz - 1, :, :n], b) < 1e-13
         assert not a[nz - 1].any() and not a[:, :, n:].any()
     assert 0.0 < rq.min() and rq.max() < 1.5
+
+
+# ---- running statistics (io.f90:403-1218 MM_XYZ_Out) ------------------------
+
+def test_running_statistics_bookkeeping(O):
+    """A fixed state accumulated three times gives 3 fr x (the w-node value):
+    u at level 1, (u(k) + u(k-1))/2 above, 0.25 w(2) at level 1; groups 1 and 2
+    are zeroed separately and atxy by neither (io.f90:457-502, 997-1006,
+    1189-1216); with jt_total <= c_count every accumulation starts from zero."""
+    cfg, o = _q_pair(O, q_flag=1, jt_total0=100)
+    assert o.step(1) == 0  # nonzero stresses and gradients
+    o.stats_enable(2, 10)
+    fr = 2 / 10
+    for _ in range(3):
+        o.stats_accumulate()
+    n = cfg.nx
+    u, w, txy = o.get("u")[:, :, :n], o.get("w")[:, :, :n], o.get("txy")[:, :, :n]
+    au = o.stats_get("au")
+    assert np.allclose(au[0], 3 * fr * u[0], rtol=1e-14, atol=0)
+    assert np.allclose(au[1:], 3 * fr * (u[1:cfg.nz - 1] + u[:cfg.nz - 2]) / 2, rtol=1e-14, atol=0)
+    assert np.allclose(o.stats_get("aw")[0], 3 * fr * 0.25 * w[1], rtol=1e-14, atol=1e-300)
+    assert np.allclose(o.stats_get("u2")[0], 3 * fr * u[0] ** 2, rtol=1e-14, atol=0)
+    assert np.allclose(o.stats_get("atxy"), 3 * fr * txy[:cfg.nz - 1], rtol=1e-14, atol=1e-300)
+    o.stats_reset(1)
+    assert not o.stats_get("au").any() and o.stats_get("ap").any() and o.stats_get("atxy").any()
+    o.stats_reset(2)
+    assert not o.stats_get("ap").any() and not o.stats_get("aactual_T").any() and o.stats_get("atxy").any()
+    # a run whose jt_total <= c_count starts every accumulation from zero
+    cfg2, o2 = _q_pair(O, q_flag=1)
+    o2.stats_enable(2, 10)
+    o2.stats_accumulate()
+    o2.stats_accumulate()
+    assert np.allclose(o2.stats_get("au")[0], fr * o2.get("u")[0, :, :n], rtol=1e-14, atol=0)
+    # thermodynamic statistics follow thermo (T_scale-scaled temperatures)
+    out = [np.zeros(C.field_shape(cfg, "u")) for _ in range(9)]
+    o.call("atm_thermodynamics", *out)
+    o.stats_enable(2, 10)
+    o.stats_accumulate()
+    assert np.allclose(o.stats_get("aactual_T"), fr * out[0][:cfg.nz - 1, :, :n] * cfg.t_scale, rtol=1e-14)
+    assert np.allclose(o.stats_get("azlcl_all"), fr * out[8][:cfg.nz - 1, :, :n], rtol=1e-14)
