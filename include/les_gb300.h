@@ -120,6 +120,12 @@ int les_ctx_destroy(les_ctx* ctx);
 int les_ctx_set_pointer_mode(les_ctx* ctx, int device_pointers);
 /* Stream the context launches on (a cudaStream_t, passed as void*). */
 void* les_ctx_stream(les_ctx* ctx);
+/* Replace the context's stream by one of the given CUDA priority (lower is
+ * more urgent; clamped to the device's range), after waiting for the work
+ * queued on the old one.  A server gives members whose steps take longest
+ * the most urgent streams so their steps are not starved by many small
+ * ones.  No counterpart in the reference. */
+int les_ctx_set_priority(les_ctx* ctx, int priority);
 /* Bytes of device memory this context holds. */
 size_t les_ctx_device_bytes(const les_ctx* ctx);
 /* Estimated device bytes for a configuration (admission control). */

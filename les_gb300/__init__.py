@@ -137,6 +137,10 @@ class Context:
     def stream(self):
         return self.L.les_ctx_stream(self.h)
 
+    def set_priority(self, priority):
+        """Move the context to a stream of this CUDA priority (lower is more urgent)."""
+        check(self.L.les_ctx_set_priority(self.h, int(priority)))
+
     def device_bytes(self):
         return self.L.les_ctx_device_bytes(self.h)
 

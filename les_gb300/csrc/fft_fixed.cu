@@ -260,6 +260,7 @@ template bool launch_rows_c2r_fixed<double, double>(const RowJob&, const RealPla
 template bool launch_rows_c2r_fixed<float, float>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 template bool launch_rows_c2r_fixed<float, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 template bool launch_rows_r2c_fixed<dfloat, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
+template bool launch_rows_r2c_fixed<dfloat, dfloat>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 template bool launch_rows_c2r_fixed<dfloat, double>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 template bool launch_rows_c2r_fixed<dfloat, dfloat>(const RowJob&, const RealPlanDev&, int, size_t, cudaStream_t);
 #define LES_INST_COLS(T, TX, CIn)                                                                   \

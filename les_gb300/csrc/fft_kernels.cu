@@ -105,6 +105,7 @@ template int launch_rows_c2r<float, double>(const RowJob&, const RealPlanDev&, c
 template int launch_cols<float, float2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 template int launch_cols<float, double2>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);
 template int launch_rows_r2c<dfloat, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
+template int launch_rows_r2c<dfloat, dfloat>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_c2r<dfloat, double>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_rows_c2r<dfloat, dfloat>(const RowJob&, const RealPlanDev&, cudaStream_t);
 template int launch_cols<dfloat, dcomplex>(const ColJob&, const FftPlanDev&, const FftPlanDev&, cudaStream_t);

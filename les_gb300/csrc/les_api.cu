@@ -411,6 +411,23 @@ int les_ctx_set_pointer_mode(les_ctx* c, int device_pointers) {
   return LES_OK;
 }
 void* les_ctx_stream(les_ctx* c) { return c ? (void*)c->stream : nullptr; }
+int les_ctx_set_priority(les_ctx* c, int priority) {
+  if (!c) return LES_ERR_ARG;
+  if (!c->own_stream) { les_set_error("the context does not own its stream"); return LES_ERR_STATE; }
+  int lo = 0, hi = 0;
+  LES_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));  // lo least urgent, hi most urgent
+  const int p = std::max(hi, std::min(lo, priority));
+  cudaStream_t s = nullptr;
+  LES_CUDA_CHECK(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, p));
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    cudaStreamDestroy(s);
+    les_set_error("%s", cudaGetErrorString(cudaGetLastError()));
+    return LES_ERR_CUDA;
+  }
+  cudaStreamDestroy(c->stream);
+  c->stream = s;
+  return LES_OK;
+}
 size_t les_ctx_device_bytes(const les_ctx* c) { return c ? c->bytes : 0; }
 
 int les_set_surface(les_ctx* c, const double* zo, const double* wt_s) {
@@ -432,8 +449,20 @@ int les_set_surface(les_ctx* c, const double* zo, const double* wt_s) {
 // host <-> device copy of one field; the FP32-held fields of a mixed
 // context are narrowed / widened on the host
 static bool f32_held(const les_ctx* c, int f) { return c->cfg.precision == 1 && mixed_f32_field(f); }
+static bool ff_held(const les_ctx* c, int f) { return c->cfg.precision == 1 && mixed_ff_field(f); }
 static int field_in(les_ctx* c, int f, const double* host) {
   const size_t n = c->fsize[f];
+  if (ff_held(c, f)) {  // hi = the value rounded to FP32, lo = the rest rounded to FP32
+    std::vector<float> t(2 * n);
+    for (size_t i = 0; i < n; ++i) {
+      const float h = (float)host[i];
+      t[2 * i] = h;
+      t[2 * i + 1] = (float)(host[i] - (double)h);
+    }
+    LES_CUDA_CHECK(cudaMemcpyAsync(c->f[f], t.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    return LES_OK;
+  }
   if (f32_held(c, f)) {
     std::vector<float> t(n);
     for (size_t i = 0; i < n; ++i) t[i] = (float)host[i];
@@ -446,6 +475,13 @@ static int field_in(les_ctx* c, int f, const double* host) {
 }
 static int field_out(les_ctx* c, int f, double* host) {
   const size_t n = c->fsize[f];
+  if (ff_held(c, f)) {
+    std::vector<float> t(2 * n);
+    LES_CUDA_CHECK(cudaMemcpyAsync(t.data(), c->f[f], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    LES_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) host[i] = (double)t[2 * i] + (double)t[2 * i + 1];
+    return LES_OK;
+  }
   if (f32_held(c, f)) {
     std::vector<float> t(n);
     LES_CUDA_CHECK(cudaMemcpyAsync(t.data(), c->f[f], n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));

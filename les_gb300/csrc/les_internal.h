@@ -134,6 +134,13 @@ inline bool mixed_f32_field(int f) {
 inline bool is_q_field(int f) {
   return (f >= LES_Q && f <= LES_DQDZ) || f == LES_WQ_S || f == LES_SGS_Q3_SFC;
 }
+// An FP32-mixed context keeps the momentum right-hand sides (this step's
+// and the previous step's) as float-float pairs: hi and lo floats in each
+// 8-byte slot of the FP64 layout.  les_get_field / les_set_field convert.
+inline bool mixed_ff_field(int f) {
+  return f == LES_RHSX || f == LES_RHSY || f == LES_RHSZ || f == LES_RHSX_F || f == LES_RHSY_F || f == LES_RHSZ_F;
+}
+inline float2* ff2(les_ctx* c, int f) { return reinterpret_cast<float2*>(c->f[f]); }
 inline float* f32(les_ctx* c, int f) { return reinterpret_cast<float*>(c->f[f]); }
 void rhs_swap(les_ctx* c);  // exchange RHSx/RHSx_f, RHSy/.., RHSz/.., RHS_T/RHS_Tf (RHS_q/RHS_qf) buffers
 int step_fp64(les_ctx* c);

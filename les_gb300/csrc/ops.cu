@@ -1949,30 +1949,43 @@ __device__ __forceinline__ dfloat ldt(const float2* p, int j) {
   return dfloat(v.x, v.y);
 }
 __device__ __forceinline__ dfloat dfs(float a) { return dfloat(a, 0.f); }
+__device__ __forceinline__ dfloat ldf2(const float2* p, size_t i) {
+  const float2 v = p[i];
+  return dfloat(v.x, v.y);
+}
 
 // main.f90:309-390 for the mixed form: RHS = -(c_nl + c_lin) - divt
 // (+ buoyancy on z), the AB2 predictor u* = u + dt (1.5 RHS - 0.5 RHS_f)
 // (Euler on the first step), u*(nz) = BOGUS.  The linear terms read u and w
 // at the neighbouring levels, so u*, v*, w* go to separate fields (us, vs,
 // ws) and the state keeps its start-of-step values until the projection
-// writes u = u* - 1.5 dt grad p.  c_nl (RHSx..z on entry: the
+// writes u = u* - 1.5 dt grad p.  c_nl (RHSx..z on entry: the FP64-stored
 // dealiased FP32 products of the fluctuations) and divt are FP32-accurate;
-// the linear terms, the sums and the AB2 increments are float-float, the
-// state and RHS stay FP64 (a float-float value is joined with one FP64
-// addition).  wz = w_z, wx = dw/dx on the uvp / w levels (float-float
-// transforms), dwdy the FP32-held dw/dy.  grid (ceil(np/256), nz).
+// the linear terms, the sums and the AB2 increments are float-float.  The
+// RHS (this step's, then next step's RHS_f) and u*, v*, w* are stored as
+// float-float pairs (hi, lo floats in each 8-byte slot, about 48 bits): no
+// FP64 operation joins them, which leaves this kernel five FP64 operations
+// per point (splitting u and w into float-float) instead of seventeen; the
+// projection forms the FP64 state from u* (k_dpdz_project32).  wz = w_z,
+// wx = dw/dx on the uvp / w levels (float-float transforms), dwdy the
+// FP32-held dw/dy.  grid (ceil(np/256), nz).
 __global__ void __launch_bounds__(256) k_rhs_ab2_mx(
-    double* u, double* v, double* w, double* Rx, double* Ry, double* Rz, double* Rxf, double* Ryf, double* Rzf,
+    const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ w, double* Rx,
+    double* Ry, double* Rz, float2* Rxf, float2* Ryf, float2* Rzf,
     const double* __restrict__ dx_, const double* __restrict__ dy_, const double* __restrict__ dz_,
     const double* __restrict__ bs, const dfloat* __restrict__ wz, const dfloat* __restrict__ wx,
-    const float* __restrict__ dwdy, MeanTab T, double* __restrict__ us, double* __restrict__ vs,
-    double* __restrict__ ws, int ld, int ny, int nz, float2 idz2, float2 dt2, int sflag, int euler) {
+    const float* __restrict__ dwdy, MeanTab T, float2* __restrict__ us, float2* __restrict__ vs,
+    float2* __restrict__ ws, int ld, int ny, int nz, float2 idz2, float2 dt2, int sflag, int euler) {
   const unsigned np = (unsigned)ld * ny;
   const unsigned p = blockIdx.x * 256u + threadIdx.x;
   if (p >= np) return;
   const int jz = blockIdx.y + 1;
   const size_t i = (size_t)(jz - 1) * np + p;
-  if (jz == nz) { us[i] = LES_BOGUS; vs[i] = LES_BOGUS; ws[i] = LES_BOGUS; return; }
+  if (jz == nz) {
+    const float2 bog = make_float2((float)LES_BOGUS, 0.f);
+    us[i] = bog; vs[i] = bog; ws[i] = bog;
+    return;
+  }
   const dfloat h(0.5f, 0.f);
   const dfloat idz(idz2.x, idz2.y);  // 1/dz and dt as float-float pairs formed on the host
   const dfloat U = ldt(T.U, jz), V = ldt(T.V, jz);
@@ -1982,11 +1995,11 @@ __global__ void __launch_bounds__(256) k_rhs_ab2_mx(
   const dfloat cxl = (-V) * s1 + h * (oyp * wp + oy * wi);
   const dfloat cyl = U * s1 - h * (oxp * wp + ox * wi);
   dfloat czl(0.f, 0.f);
-  const double ui = u[i];
+  const dfloat uf = cvt<dfloat>(u[i]);
   if (jz >= 2) {
     const size_t im = i - np;
     const dfloat Um = ldt(T.U, jz - 1);
-    const dfloat up = cvt<dfloat>(ui) - U, upm = cvt<dfloat>(u[im]) - Um;
+    const dfloat up = uf - U, upm = cvt<dfloat>(u[im]) - Um;
     const float vp = cvt_d2f(v[i]) - T.UVf[jz].y, vpm = cvt_d2f(v[im]) - T.UVf[jz - 1].y;
     const dfloat wyp = (up - upm) * idz - wx[i];                          // w_y' at w-level jz
     const float wxp = dwdy[i] - (vp - vpm) * idz2.x;                    // w_x' (FP32: its factor V is small)
@@ -1999,22 +2012,25 @@ __global__ void __launch_bounds__(256) k_rhs_ab2_mx(
   const dfloat ry = -(dfs(cvt_d2f(Ry[i])) + cyl) - dfs(cvt_d2f(dy_[i]));
   dfloat rz = -(dfs(cvt_d2f(Rz[i])) + czl) - dfs(cvt_d2f(dz_[i]));
   if (sflag) rz = rz + cvt<dfloat>(bs[i]);
-  const double rxd = cvt<double>(rx), ryd = cvt<double>(ry), rzd = cvt<double>(rz);
-  Rx[i] = rxd;
-  Ry[i] = ryd;
-  Rz[i] = rzd;
+  const float2 rx2 = make_float2(rx.hi, rx.lo), ry2 = make_float2(ry.hi, ry.lo), rz2 = make_float2(rz.hi, rz.lo);
+  reinterpret_cast<float2*>(Rx)[i] = rx2;  // the slot held c_nl in FP64 until now
+  reinterpret_cast<float2*>(Ry)[i] = ry2;
+  reinterpret_cast<float2*>(Rz)[i] = rz2;
   dfloat fx, fy, fz;
   if (euler) {
     fx = rx; fy = ry; fz = rz;
-    Rxf[i] = rxd; Ryf[i] = ryd; Rzf[i] = rzd;
+    Rxf[i] = rx2; Ryf[i] = ry2; Rzf[i] = rz2;
   } else {
-    fx = cvt<dfloat>(Rxf[i]); fy = cvt<dfloat>(Ryf[i]); fz = cvt<dfloat>(Rzf[i]);
+    fx = ldf2(Rxf, i); fy = ldf2(Ryf, i); fz = ldf2(Rzf, i);
   }
   const dfloat dtf(dt2.x, dt2.y);
   const dfloat a15(1.5f, 0.f), a05(0.5f, 0.f);
-  us[i] = ui + cvt<double>(dtf * (a15 * rx - a05 * fx));
-  vs[i] = v[i] + cvt<double>(dtf * (a15 * ry - a05 * fy));
-  ws[i] = w[i] + cvt<double>(dtf * (a15 * rz - a05 * fz));
+  const dfloat ux = uf + dtf * (a15 * rx - a05 * fx);
+  const dfloat vx = cvt<dfloat>(v[i]) + dtf * (a15 * ry - a05 * fy);
+  const dfloat wx2 = wi + dtf * (a15 * rz - a05 * fz);
+  us[i] = make_float2(ux.hi, ux.lo);
+  vs[i] = make_float2(vx.hi, vx.lo);
+  ws[i] = make_float2(wx2.hi, wx2.lo);
 }
 
 // main.f90:403-410 + forcing.f90:128-219 project, one thread per point of
@@ -2060,14 +2076,15 @@ __global__ void k_dpdz_project(double* u, double* v, double* w, double* Rx, doub
 }
 // Mixed form: dpdz and the projection in FP64 with the fused factor
 // -1.5 dt (the pressure comes from float-float transforms and the projection
-// sets the divergence), and the RHS bookkeeping R -= grad p in FP64: the
-// stored RHS is next step's RHS_f, and the horizontal RHS are of order
-// U k |v'|, whose FP32 rounding is 1e-5 of v's own scale.
-// grid (ceil(np/256), nz-1).
-__global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, double* w, const double* __restrict__ us,
-                                                        const double* __restrict__ vs,
-                                                        const double* __restrict__ ws, double* Rx, double* Ry,
-                                                        double* Rz, const double* __restrict__ p,
+// sets the divergence): u = u* - 1.5 dt grad p from the float-float
+// predictor u*, v*, w* (one FP64 addition joins each), and the RHS
+// bookkeeping R -= grad p in float-float on the float-float RHS (it is next
+// step's RHS_f; the horizontal RHS are of order U k |v'|, whose FP32
+// rounding is 1e-5 of v's own scale).  grid (ceil(np/256), nz-1).
+__global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, double* w, const float2* __restrict__ us,
+                                                        const float2* __restrict__ vs,
+                                                        const float2* __restrict__ ws, float2* Rx, float2* Ry,
+                                                        float2* Rz, const double* __restrict__ p,
                                                         const double* __restrict__ dpdx,
                                                         const double* __restrict__ dpdy, double* dpdz, int ld,
                                                         int nx, int ny, int nz, double idz, double dt) {
@@ -2086,10 +2103,12 @@ __global__ void __launch_bounds__(256) k_dpdz_project32(double* u, double* v, do
     pz = dpdz[i];
   }
   const double gx = dpdx[i], gy = dpdy[i];
-  Rx[i] = Rx[i] - gx;
-  Ry[i] = Ry[i] - gy;
-  Rz[i] = Rz[i] - pz;
-  double uu = us[i], vv = vs[i], ww = ws[i];
+  const dfloat rx = ldf2(Rx, i) - cvt<dfloat>(gx), ry = ldf2(Ry, i) - cvt<dfloat>(gy);
+  const dfloat rz = ldf2(Rz, i) - cvt<dfloat>(pz);
+  Rx[i] = make_float2(rx.hi, rx.lo);
+  Ry[i] = make_float2(ry.hi, ry.lo);
+  Rz[i] = make_float2(rz.hi, rz.lo);
+  double uu = cvt<double>(ldf2(us, i)), vv = cvt<double>(ldf2(vs, i)), ww = cvt<double>(ldf2(ws, i));
   if (inx) {
     uu = fma(c, gx, uu);
     vv = fma(c, gy, vv);
@@ -2728,20 +2747,29 @@ int thomas_tables(les_ctx* c) {
 // p-hat (double: FP64 form and the per-routine entry; dfloat: mixed form).
 // The wall planes' spectra and the tridiagonal solve are FP64 in both.
 template <typename T>
-static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const double* const* ustar = nullptr) {
+static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const float2* const* ustar = nullptr) {
   typedef typename CT<T>::type CX;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const int nz = g.nz;
   const double cst = 1.0 / (double)(g.nx * g.ny);
   // spectra of u*, v*, w* (levels 1..nz-1), (const/tadv1)*(u/dt); u* is the
-  // state itself, or (mixed form) the separate predictor fields
-  const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
-  if (ustar)
-    for (int q = 0; q < 3; ++q) in[q] = ustar[q];
+  // state itself, or (mixed form) the separate float-float predictor fields
   const double sc3[3] = {cst / 1.5, cst / 1.5, cst / 1.5};
   const double dv3[3] = {k.dt, k.dt, k.dt};
-  r2cT<T, double>(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
+  if (ustar) {
+    if constexpr (std::is_same<T, dfloat>::value) {
+      const dfloat* in[3] = {reinterpret_cast<const dfloat*>(ustar[0]), reinterpret_cast<const dfloat*>(ustar[1]),
+                             reinterpret_cast<const dfloat*>(ustar[2])};
+      r2cT<T, dfloat>(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
+    } else {
+      les_set_error("float-float predictor fields need float-float transforms");
+      return LES_ERR_STATE;
+    }
+  } else {
+    const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+    r2cT<T, double>(c, 3, nz - 1, in, (long)g.nplane, sc3, dv3, c->wsA, false, g.lh);
+  }
   CX* H = (CX*)c->wsP;                                       // 3*(nz-1)*C
   C2* BT = reinterpret_cast<C2*>(H + (size_t)3 * (nz - 1) * g.C);  // bottom, top
   // p-hat in the transform precision (float-float in the mixed form)
@@ -4117,8 +4145,9 @@ static dfloat* mlin_fields(les_ctx* c) {
   return reinterpret_cast<dfloat*>(c->big + off);
 }
 // the mixed form's predictor fields u*, v*, w* (after the two fields above)
-static double* ustar_fields(les_ctx* c) {
-  return reinterpret_cast<double*>(mlin_fields(c) + 2 * c->g.nfield);
+// the float-float predictor u*, v*, w* (three fields after the linear terms)
+static float2* ustar_fields(les_ctx* c) {
+  return reinterpret_cast<float2*>(mlin_fields(c) + 2 * c->g.nfield);
 }
 static void meanflow_lin(les_ctx* c) {
   const Grid& g = c->g;
@@ -4220,10 +4249,10 @@ static int stepT(les_ctx* c) {
     const dfloat* ml = mlin_fields(c);
     const dfloat idz(1.0 / g.dz), dtd(k.dt);
     k_rhs_ab2_mx<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)g.nz), 256, 0, c->stream>>>(
-        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], c->f[LES_RHSX_F],
-        c->f[LES_RHSY_F], c->f[LES_RHSZ_F], c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ], c->f[LES_BETA_SCAL],
-        ml, ml + g.nfield, f32(c, LES_DWDY), mean_tab(c), ustar_fields(c), ustar_fields(c) + g.nfield,
-        ustar_fields(c) + 2 * g.nfield, g.ld, g.ny, g.nz, make_float2(idz.hi, idz.lo),
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ], ff2(c, LES_RHSX_F),
+        ff2(c, LES_RHSY_F), ff2(c, LES_RHSZ_F), c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ],
+        c->f[LES_BETA_SCAL], ml, ml + g.nfield, f32(c, LES_DWDY), mean_tab(c), ustar_fields(c),
+        ustar_fields(c) + g.nfield, ustar_fields(c) + 2 * g.nfield, g.ld, g.ny, g.nz, make_float2(idz.hi, idz.lo),
         make_float2(dtd.hi, dtd.lo), k.s_flag, euler);
   } else
     k_rhs_ab2<<<grid1(nv + g.nplane), 256, 0, c->stream>>>(
@@ -4232,12 +4261,12 @@ static int stepT(les_ctx* c) {
         nv, g.nplane, k.dt, k.s_flag, euler);
   LES_COUNT_LAUNCH();
   if (MX) {
-    const double* ust = ustar_fields(c);
-    const double* u3[3] = {ust, ust + g.nfield, ust + 2 * g.nfield};
+    const float2* ust = ustar_fields(c);
+    const float2* u3[3] = {ust, ust + g.nfield, ust + 2 * g.nfield};
     pressT<dfloat>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY], u3);
     k_dpdz_project32<<<dim3((unsigned)((g.nplane + 255) / 256), (unsigned)(g.nz - 1)), 256, 0, c->stream>>>(
-        c->f[LES_U], c->f[LES_V], c->f[LES_W], u3[0], u3[1], u3[2], c->f[LES_RHSX], c->f[LES_RHSY],
-        c->f[LES_RHSZ], c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz,
+        c->f[LES_U], c->f[LES_V], c->f[LES_W], u3[0], u3[1], u3[2], ff2(c, LES_RHSX), ff2(c, LES_RHSY),
+        ff2(c, LES_RHSZ), c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz,
         1.0 / g.dz, k.dt);
   } else {
     pressT<double>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);

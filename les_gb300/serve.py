@@ -234,6 +234,14 @@ class Scheduler:
         return self.metrics.summary(wall), wall
 
 
+def priority_of(size, lo=32 ** 3, hi=192 * 192 * 128, levels=5):
+    """CUDA stream priority of a member: 0 (least urgent) for the smallest
+    size, -levels for the largest, by log of the grid points."""
+    nx, ny, nz = size
+    f = (math.log(nx * ny * nz) - math.log(lo)) / (math.log(hi) - math.log(lo))
+    return -int(round(levels * min(1.0, max(0.0, f))))
+
+
 class FakeExecutor:
     """Deterministic executor for host-side tests: a step of an nx*ny*nz
     member takes `ns_per_pt` ns per grid point; allocation can be made to
@@ -283,7 +291,7 @@ class GpuExecutor:
     """les_gb300 contexts on the GPU; two CUDA events per launched step (its
     device time); evicted members spilled to pinned host memory."""
 
-    def __init__(self, precision=1, seed0=1000, use_graphs=True, autotune=True):
+    def __init__(self, precision=1, seed0=1000, use_graphs=True, autotune=True, priorities=True):
         import torch  # events on the members' streams, pinned host buffers
         import les_gb300 as lg
         self.torch = torch
@@ -292,6 +300,9 @@ class GpuExecutor:
         self.seed0 = seed0
         self.use_graphs = use_graphs
         self.autotune = autotune
+        # larger members get more urgent streams, so their steps are not
+        # starved behind many small members' short kernels
+        self.priorities = priorities
         self.ctx = {}
         self.streams = {}
         self.inflight = collections.deque()
@@ -327,6 +338,8 @@ class GpuExecutor:
                 ctx.set(k, v)
         if self.autotune:
             ctx.autotune()
+        if self.priorities:
+            ctx.set_priority(priority_of(size))
         self.ctx[member] = ctx
         self.streams[member] = self.torch.cuda.ExternalStream(ctx.stream())
 

@@ -13,7 +13,7 @@ import json
 import time
 
 
-def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60):
+def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60, priorities=True):
     """Serve one Poisson trace; returns the summary (and, when
     baseline_requests > 0, the unbatched FP64 baseline on its prefix)."""
     import torch
@@ -21,7 +21,7 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
     free, total = torch.cuda.mem_get_info()
     budget = int(budget_gb * 2 ** 30) if budget_gb > 0 else int(0.9 * free)
     trace = poisson_trace(requests, rate, seed)
-    ex = GpuExecutor(precision=1, autotune=True)
+    ex = GpuExecutor(precision=1, autotune=True, priorities=priorities)
     sched = Scheduler(ex, budget_bytes=budget)
     summary, wall = sched.run(trace)
     status = {}
@@ -29,7 +29,7 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
         status[r.status] = status.get(r.status, 0) + 1
     for m in list(ex.ctx):
         ex.evict(m)
-    out = {"requests": len(trace), "rate_per_s": rate, "wall_s": wall, "status": status,
+    out = {"requests": len(trace), "rate_per_s": rate, "priorities": priorities, "wall_s": wall, "status": status,
            "budget_gb": budget / 2 ** 30, "serving": summary}
     if summary.get("step_p50_ms"):
         out["step_p99_over_p50"] = summary["step_p99_ms"] / summary["step_p50_ms"]
@@ -63,8 +63,10 @@ def main():
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--budget-gb", type=float, default=0.0, help="0: 90%% of free device memory")
     ap.add_argument("--baseline-requests", type=int, default=60)
+    ap.add_argument("--no-priorities", action="store_true", help="every member on a default-priority stream")
     args = ap.parse_args()
-    print(json.dumps(serve(args.requests, args.rate, args.seed, args.budget_gb, args.baseline_requests)))
+    print(json.dumps(serve(args.requests, args.rate, args.seed, args.budget_gb, args.baseline_requests,
+                           priorities=not args.no_priorities)))
 
 
 if __name__ == "__main__":
