@@ -10,12 +10,15 @@ each field is printed.  Two cases:
   model3   32^3, theta, striped surface, jt_total0 = 500, model 3, 10 steps:
            the plane-averaged quintic of scaledep_dynamic (sgsmodule.f90:37-59)
            is ill-conditioned.
+  humid0, humid500
+           32^3, theta and qmix with the striped moisture flux, jt_total0 = 0
+           or 500 (the dynamic Cs^2 feeds back from step 5), 10 steps.
   c2       128^3, theta, striped surface, jt_total from 0, model 5, 200 steps
            (every 10 steps): the first level's explicit SGS diffusion number
            Nu_t dt / dz^2 is above the AB2 stability limit, so from about
            step 55 rounding differences at level 1 grow until they saturate.
 
-  python -m oracle.rounding_spread model3|c2
+  python -m oracle.rounding_spread model3|humid0|humid500|c2
 """
 import json
 import os
@@ -51,11 +54,16 @@ def run_case(case, lib_path, out_path):
     if case == "model3":
         cfg = lc.make_config(32, s_flag=1, jt_total0=500, model=3, rmsdiv_every=1)
         seed, blocks, every = 11, 1, 10
+    elif case in ("humid0", "humid500"):
+        cfg = lc.make_config(32, s_flag=1, q_flag=1, jt_total0=0 if case == "humid0" else 500, rmsdiv_every=1)
+        seed, blocks, every = 41, 1, 10
     else:
         cfg = lc.make_config(128, s_flag=1, rmsdiv_every=10)
         seed, blocks, every = 21, 20, 10
     surf = lc.striped_surface(cfg)
     o = oo.Oracle(cfg, surf)
+    if getattr(cfg, "q_flag", 0):
+        o.set("wq_s", lc.moisture_flux(cfg))
     for k, v in lc.initial_state(cfg, surf, seed=seed).items():
         o.set(k, v)
     n = cfg.nx
@@ -63,7 +71,7 @@ def run_case(case, lib_path, out_path):
     for b in range(blocks):
         o.step(every)
         step = (b + 1) * every
-        for nm in ("u", "v", "w", "theta", "Cs_opt2"):
+        for nm in ("u", "v", "w", "theta", "Cs_opt2") + (("q",) if getattr(cfg, "q_flag", 0) else ()):
             out["%s_%d" % (nm, step)] = o.get(nm)[:-1, :, :n]
         out["rmsdiv_%d" % step] = np.array(o.rmsdiv())
     np.savez(out_path, **out)
@@ -87,7 +95,7 @@ def main():
     steps = sorted({int(k.split("_")[-1]) for k in a.files})
     for s in steps:
         rec = {"step": s}
-        for nm in ("u", "v", "w", "theta", "Cs_opt2"):
+        for nm in [f.rsplit("_", 1)[0] for f in a.files if f.endswith("_%d" % s) and not f.startswith("rmsdiv")]:
             x, y = a["%s_%d" % (nm, s)], b["%s_%d" % (nm, s)]
             rec[nm] = float(np.linalg.norm(x - y) / max(np.linalg.norm(x), 1e-300))
         x, y = float(a["rmsdiv_%d" % s]), float(b["rmsdiv_%d" % s])

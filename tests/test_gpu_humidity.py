@@ -17,6 +17,12 @@ from les_gb300.config import moisture_flux
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+# The oracle's own rounding sensitivity for the jt_total0 = 500 case (the
+# dynamic Cs^2 and its FP32 truncations feed back from step 5): built with
+# FMA contraction against without it (`python -m oracle.rounding_spread
+# humid500`), the two oracles differ after 10 steps by these relative L2
+# amounts; the GPU is held to 1e-12 or three times that spread.
+HUMID500_SPREAD = {"u": 3.1e-15, "v": 8.6e-13, "w": 1.2e-12, "theta": 6.9e-15, "q": 1.6e-13}
 
 
 def rel(a, b):
@@ -55,11 +61,14 @@ def test_step_parity_32_humidity(libs, jt0):
     g.step(10)
     assert o.step(10) == 0
     n = cfg.nx
+
+    def bound(nm):
+        return TOL if jt0 == 0 else max(TOL, 3.0 * HUMID500_SPREAD[nm])
     for nm in ("u", "v", "theta", "q"):
         e = rel(g.get(nm)[:-1, :, :n], o.get(nm)[:-1, :, :n])
-        assert e < TOL, (nm, e)
+        assert e < bound(nm), (nm, e)
     e = rel(g.get("w")[:, :, :n], o.get("w")[:, :, :n])
-    assert e < TOL, ("w", e)
+    assert e < bound("w"), ("w", e)
     assert rel(g.get("sgs_q3"), o.get("sgs_q3")) < TOL
     # beta_scal = g_hat (theta_v - mean) / mean is a difference about the
     # plane mean, so it is held in absolute terms: a buoyancy difference of
