@@ -7,11 +7,13 @@ members that are idle are evicted least-recently-used when room is needed.
 Every tick the scheduler launches one step of every active request, each on
 its member's own stream, so steps of different members overlap on the GPU;
 requests that arrive while others run join at the next tick (continuous
-batching, not a queue).  Step latency is the device time of each step:
-CUDA events recorded on the member's stream just before and just after the
-step (it includes the time the step waits on the device behind other
-members' work); request latency runs from arrival to completion on the host
-clock.  An evicted member is spilled to host memory with its whole state
+batching, not a queue).  A request's step latency runs from the completion
+of its previous step to the completion of this one (its first step: from
+the step's start), on the device's clock: CUDA events recorded on the
+member's stream, so it includes host scheduling, any wait for an in-flight
+work budget and the time the step shares the device with other members;
+the device time of each step alone is reported beside it.  Request latency
+runs from arrival to completion on the host clock.  An evicted member is spilled to host memory with its whole state
 (les_state_save) and resumed from it when it is admitted again
 (les_state_restore), so it continues exactly where it stopped.
 
@@ -45,12 +47,15 @@ class Request:
     finished: float = None
     status: str = "pending"   # pending | active | done | cancelled | rejected | failed
     error: str = None
+    last_tick: int = 0
+    prev_done: object = None  # executor's completion marker of the previous step
 
 
 @dataclass
 class Metrics:
-    step_lat: list = field(default_factory=list)            # seconds
+    step_lat: list = field(default_factory=list)            # seconds, inter-step (see Scheduler)
     step_lat_by_size: dict = field(default_factory=lambda: collections.defaultdict(list))
+    step_dev: list = field(default_factory=list)            # seconds, device time of the step alone
     req_lat: list = field(default_factory=list)
     pt_steps: float = 0.0
     admitted: int = 0
@@ -63,6 +68,8 @@ class Metrics:
         out = {"steps": len(self.step_lat),
                "step_p50_ms": None if not self.step_lat else 1e3 * pct(self.step_lat, 50),
                "step_p99_ms": None if not self.step_lat else 1e3 * pct(self.step_lat, 99),
+               "step_device_p50_ms": None if not self.step_dev else 1e3 * pct(self.step_dev, 50),
+               "step_device_p99_ms": None if not self.step_dev else 1e3 * pct(self.step_dev, 99),
                "req_p50_ms": None if not self.req_lat else 1e3 * pct(self.req_lat, 50),
                "req_p99_ms": None if not self.req_lat else 1e3 * pct(self.req_lat, 99),
                "pt_steps_per_s": self.pt_steps / wall if wall > 0 else None,
@@ -89,7 +96,21 @@ def poisson_trace(n_requests, rate, seed, n_members=64, sizes=SIZES, weights=WEI
 
 
 class Scheduler:
-    def __init__(self, executor, budget_bytes, max_inflight_per_member=1, clock=time.perf_counter):
+    """Admission by footprint, one step per active request per tick.
+
+    A request's step latency is the time from the completion of its previous
+    step (or, for its first step, from the step's start on the device) to
+    the completion of this one, on the device's clock (CUDA events on the
+    member's stream): what the request waits per step, host scheduling and
+    queueing included.  The device time of the step alone is kept beside it.
+    With max_inflight_points set, a tick launches steps only while the grid
+    points of all steps in flight stay within it (at least one step always
+    runs), oldest-served request first: every step then shares the device
+    with a bounded amount of other work, which bounds the spread of its
+    latency at some cost in overlap."""
+
+    def __init__(self, executor, budget_bytes, max_inflight_per_member=1, clock=time.perf_counter,
+                 max_inflight_points=None):
         self.ex = executor
         self.budget = budget_bytes
         self.used = 0
@@ -100,6 +121,9 @@ class Scheduler:
         self.metrics = Metrics()
         self.clock = clock
         self.max_inflight = max_inflight_per_member
+        self.max_points = max_inflight_points
+        self.inflight_points = 0
+        self.tick_no = 0
         self.done = []
 
     # ---- admission ----------------------------------------------------------
@@ -169,25 +193,39 @@ class Scheduler:
         self.pending = waiting
         # one step per active request per tick; requests on one member run in
         # arrival order (the oldest owns the member until it completes)
+        self.tick_no += 1
         owned = set()
+        ready = []
         for req in self.active:
             if req.status != "active" or req.member in owned:
                 continue
             owned.add(req.member)
             if req.done_steps + req.inflight >= req.nsteps or req.inflight >= self.max_inflight:
                 continue
+            ready.append(req)
+        if self.max_points is not None:  # least recently served first
+            ready.sort(key=lambda q: q.last_tick)
+        for req in ready:
+            pts = req.size[0] * req.size[1] * req.size[2]
+            if (self.max_points is not None and self.inflight_points > 0 and
+                    self.inflight_points + pts > self.max_points):
+                continue
             self.ex.launch(req, self.clock())
             if req.status == "active":
                 req.inflight += 1
+                req.last_tick = self.tick_no
+                self.inflight_points += pts
 
     def poll(self):
-        for req, t_launch, t_done, pts, lat in self.ex.completed():
+        for req, t_launch, t_done, pts, lat, dev in self.ex.completed():
             req.inflight -= 1
             req.done_steps += 1
+            self.inflight_points -= pts
             if req.status == "cancelled":
                 continue
             self.metrics.step_lat.append(lat)
             self.metrics.step_lat_by_size[req.size].append(lat)
+            self.metrics.step_dev.append(dev)
             self.metrics.pt_steps += pts
         still = []
         for req in self.active:
@@ -275,11 +313,16 @@ class FakeExecutor:
             req.error = "non-finite state detected"
             return
         dur = self.ns * 1e-9 * nx * ny * nz
-        self.inflight.append((req, t, t + dur, nx * ny * nz, False))
+        start = t if req.prev_done is None else max(t, req.prev_done)  # after the request's previous step
+        self.inflight.append((req, start, start + dur, nx * ny * nz, False))
         self.steps[req.member] += 1
 
     def completed(self):
-        out = [(r, a, b, p, b - a) for (r, a, b, p, f) in self.inflight]
+        out = []
+        for (r, a, b, p, f) in self.inflight:
+            gap = b - r.prev_done if r.prev_done is not None else b - a
+            r.prev_done = b
+            out.append((r, a, b, p, gap, b - a))
         self.inflight = []
         return out
 
@@ -291,7 +334,7 @@ class GpuExecutor:
     """les_gb300 contexts on the GPU; two CUDA events per launched step (its
     device time); evicted members spilled to pinned host memory."""
 
-    def __init__(self, precision=1, seed0=1000, use_graphs=True, autotune=True, priorities=True):
+    def __init__(self, precision=1, seed0=1000, use_graphs=True, autotune=True, priorities=False):
         import torch  # events on the members' streams, pinned host buffers
         import les_gb300 as lg
         self.torch = torch
@@ -375,7 +418,10 @@ class GpuExecutor:
         while self.inflight:
             req, t, e0, e1, pts = self.inflight.popleft()
             if e1.query():
-                out.append((req, t, now, pts, e0.elapsed_time(e1) / 1e3))
+                dev = e0.elapsed_time(e1) / 1e3
+                gap = req.prev_done.elapsed_time(e1) / 1e3 if req.prev_done is not None else dev
+                req.prev_done = e1
+                out.append((req, t, now, pts, gap, dev))
             else:
                 keep.append((req, t, e0, e1, pts))
         self.inflight = keep

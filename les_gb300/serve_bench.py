@@ -13,7 +13,8 @@ import json
 import time
 
 
-def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60, priorities=True):
+def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60, priorities=False,
+          max_inflight_points=None):
     """Serve one Poisson trace; returns the summary (and, when
     baseline_requests > 0, the unbatched FP64 baseline on its prefix)."""
     import torch
@@ -22,14 +23,15 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
     budget = int(budget_gb * 2 ** 30) if budget_gb > 0 else int(0.9 * free)
     trace = poisson_trace(requests, rate, seed)
     ex = GpuExecutor(precision=1, autotune=True, priorities=priorities)
-    sched = Scheduler(ex, budget_bytes=budget)
+    sched = Scheduler(ex, budget_bytes=budget, max_inflight_points=max_inflight_points)
     summary, wall = sched.run(trace)
     status = {}
     for r in sched.done:
         status[r.status] = status.get(r.status, 0) + 1
     for m in list(ex.ctx):
         ex.evict(m)
-    out = {"requests": len(trace), "rate_per_s": rate, "priorities": priorities, "wall_s": wall, "status": status,
+    out = {"requests": len(trace), "rate_per_s": rate, "priorities": priorities,
+           "max_inflight_points": max_inflight_points, "wall_s": wall, "status": status,
            "budget_gb": budget / 2 ** 30, "serving": summary}
     if summary.get("step_p50_ms"):
         out["step_p99_over_p50"] = summary["step_p99_ms"] / summary["step_p50_ms"]
@@ -63,10 +65,13 @@ def main():
     ap.add_argument("--seed", type=int, default=11)
     ap.add_argument("--budget-gb", type=float, default=0.0, help="0: 90%% of free device memory")
     ap.add_argument("--baseline-requests", type=int, default=60)
-    ap.add_argument("--no-priorities", action="store_true", help="every member on a default-priority stream")
+    ap.add_argument("--priorities", action="store_true", help="more urgent streams for larger members")
+    ap.add_argument("--max-inflight-points", type=float, default=0.0,
+                    help="grid points of all steps in flight at once (0: no limit)")
     args = ap.parse_args()
+    mip = int(args.max_inflight_points) if args.max_inflight_points > 0 else None
     print(json.dumps(serve(args.requests, args.rate, args.seed, args.budget_gb, args.baseline_requests,
-                           priorities=not args.no_priorities)))
+                           priorities=args.priorities, max_inflight_points=mip)))
 
 
 if __name__ == "__main__":

@@ -105,3 +105,39 @@ def test_poisson_trace_shape():
     assert len(tr) == 200 and all(1 <= r.nsteps <= 50 for r in tr)
     gaps = [b.arrival - a.arrival for a, b in zip(tr, tr[1:])]
     assert 0.002 < sum(gaps) / len(gaps) < 0.01
+
+
+def test_inflight_work_budget_bounds_concurrency():
+    """With max_inflight_points the scheduler launches steps only while the
+    points of the steps in flight fit the budget (one step always runs), the
+    least recently served request first, and still completes every request."""
+    ex = FakeExecutor()
+    pts = 32 * 32 * 32
+    s = Scheduler(ex, budget_bytes=10 ** 12, max_inflight_points=2 * pts)
+    for i in range(5):
+        s.submit(R(i, member=i, n=3))
+    seen = []
+    for _ in range(200):
+        if s.idle():
+            break
+        s.tick(0.0)
+        seen.append(sum(r.inflight for r in s.active))
+        s.poll()
+    assert s.idle() and max(seen) == 2
+    assert all(r.status == "done" for r in s.done) and all(ex.steps[m] == 3 for m in range(5))
+    # a member larger than the budget still runs, alone
+    s2 = Scheduler(FakeExecutor(), budget_bytes=10 ** 12, max_inflight_points=pts)
+    s2.submit(R(0, 0, size=(64, 64, 64)))
+    drain(s2)
+    assert s2.done[0].status == "done"
+
+
+def test_step_latency_counts_the_wait_between_steps():
+    """The step latency of a request's later steps runs from its previous
+    step's completion; the device time of the step alone is kept beside it."""
+    ex = FakeExecutor(ns_per_pt=1.0)
+    s = Scheduler(ex, budget_bytes=10 ** 12)
+    s.submit(R(0, 0, n=3))
+    drain(s)
+    assert len(s.metrics.step_lat) == 3 and len(s.metrics.step_dev) == 3
+    assert all(g >= d - 1e-15 for g, d in zip(s.metrics.step_lat, s.metrics.step_dev))
