@@ -45,10 +45,11 @@ FAMILIES = {1: "k_cols/k_colsf<double|dfloat> (FP64 / float-float y pass)",
             3: "k_rows_r2c/k_rows_c2r<double|dfloat> (FP64 / float-float x pass)",
             4: "k_r2c_reg*/k_c2r_reg*/k_rows_*<float> (FP32 x pass)"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# byte of a family, from one ncu capture of that family's launches on a small
-# grid (profiles/); scales the live algorithmic bytes per launch to the
-# traffic per launch.  Only where a capture exists.
-TRAFFIC_RATIO = {("mixed", 2): 0.8774, ("fp64", 1): 0.9209}
+# byte of a family, from one ncu capture of one step's launches of that
+# family on a 256 x 256 x 96 member (bench.py --capture-step;
+# profiles/transforms_fp32_traffic.md); scales the live algorithmic bytes
+# per launch to the traffic per launch.  Only where a capture exists.
+TRAFFIC_RATIO = {("mixed", 4): 0.742, ("mixed", 2): 0.760}
 
 
 def parse():
