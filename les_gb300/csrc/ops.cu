@@ -1913,6 +1913,29 @@ __global__ void k_rhs_ab2(double* u, double* v, double* w, double* Rx, double* R
 struct MeanTab {
   float2 *U, *V, *Oy, *Ox, *Cz, *UVf;
 };
+// d/dx of x-spectra with y still physical (rows [plane][ny][lh], float-float):
+// out = i kx in (acc: out += i kx in), kx of the column (the kx = nx/2 column
+// zeroed, as ddx.f90 zeroes it).  The fields this is used on carry no
+// ky = ny/2 content (Nyquist-filtered state, or p-hat with its Nyquist modes
+// zeroed), so skipping the y round trip that ddx would make loses nothing.
+__global__ void k_ikx_rows(const dcomplex* __restrict__ in, dcomplex* out, const float2* __restrict__ kxd, int lh,
+                           size_t n, int acc) {
+  GSTRIDE(e, n) {
+    const int jx = (int)(e % lh);
+    const float2 kv = kxd[jx];  // row 0 of the (lh, ny) table: the column's kx
+    const dfloat k(kv.x, kv.y);
+    const dcomplex v = in[e];
+    dcomplex r;
+    r.x = -(k * v.y);
+    r.y = k * v.x;
+    if (acc) {
+      const dcomplex o = out[e];
+      r.x = r.x + o.x;
+      r.y = r.y + o.y;
+    }
+    out[e] = r;
+  }
+}
 static MeanTab mean_tab(les_ctx* c) {
   const size_t ms = (size_t)c->g.nz + 8;
   float2* b = reinterpret_cast<float2*>(c->dred + 28 * ms);  // slots 28..33
@@ -2830,7 +2853,25 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const float
         nullptr, 0); LES_COUNT_LAUNCH();
   }
   // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
-  {
+  if constexpr (std::is_same<T, dfloat>::value) {
+    // float-float: p-hat's y round trip for levels 0..nz-1 and for i ky on
+    // 1..nz-1; dp/dx by the x wavenumber alone (p-hat's Nyquist modes are zero)
+    ColJob K = coljob(c, MAP_SAME, DIR_INV, nz);
+    K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
+    colsT<T, PCX>(c, K);
+    const size_t L1 = (size_t)(nz - 1) * g.C;
+    CX* Y = (CX*)c->wsB;
+    CX* Yx = Y + (size_t)nz * g.C;
+    CX* Yy = Yx + L1;
+    ColJob L = coljob(c, MAP_SAME, DIR_INV, nz - 1);
+    L.nin = 1; L.nout = 1; L.in[0] = P + g.C; L.out[0] = Yy; L.coef[0][0] = CC_IKY;
+    colsT<T, PCX>(c, L);
+    k_ikx_rows<<<grid1(L1), 256, 0, c->stream>>>(Y + g.C, Yx, c->kxd, g.lh, L1, 0); LES_COUNT_LAUNCH();
+    double* o0 = p;
+    c2rT<T, double>(c, 1, nz, Y, &o0, (long)g.nplane, false, g.lh);
+    double* o1[2] = {dpdx, dpdy};
+    c2rT<T, double>(c, 2, nz - 1, Yx, o1, (long)g.nplane, false, g.lh);
+  } else {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
     K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
     colsT<T, PCX>(c, K);
@@ -4161,13 +4202,20 @@ static void meanflow_lin(les_ctx* c) {
   const double* offs[3] = {mean, mean + ms, mean + 2 * ms};
   r2cT<dfloat, double>(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh, offs);
   const long FS = (long)nz * g.C;
+  // w_z = i kx v - i ky u: -du/dy needs the y round trip, dv/dx and dw/dx do
+  // not (x wavenumber alone, k_ikx_rows)
   ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
-  J.nin = 3; J.nout = 2; J.nf = 1;
-  J.in[0] = c->wsA; J.in[1] = (dcomplex*)c->wsA + FS; J.in[2] = (dcomplex*)c->wsA + 2 * FS;
-  J.out[0] = c->wsB; J.out[1] = (dcomplex*)c->wsB + FS;
-  J.coef[0][0] = CC_MIKY; J.coef[0][1] = CC_IKX;  // w_z = i kx v - i ky u
-  J.coef[1][2] = CC_IKX;                           // dw/dx
+  J.nin = 1; J.nout = 1; J.nf = 1;
+  J.in[0] = c->wsA;
+  J.out[0] = c->wsB;
+  J.coef[0][0] = CC_MIKY;
   colsT<dfloat, dcomplex>(c, J);
+  const dcomplex* sa = (const dcomplex*)c->wsA;
+  dcomplex* sb = (dcomplex*)c->wsB;
+  k_ikx_rows<<<grid1((size_t)FS), 256, 0, c->stream>>>(sa + FS, sb, c->kxd, g.lh, (size_t)FS, 1);
+  LES_COUNT_LAUNCH();
+  k_ikx_rows<<<grid1((size_t)FS), 256, 0, c->stream>>>(sa + 2 * FS, sb + FS, c->kxd, g.lh, (size_t)FS, 0);
+  LES_COUNT_LAUNCH();
   dfloat* ml = mlin_fields(c);
   dfloat* out[2] = {ml, ml + g.nfield};
   c2rT<dfloat, dfloat>(c, 2, nz, c->wsB, out, (long)g.nplane, false, g.lh);
