@@ -727,19 +727,25 @@ __global__ void __launch_bounds__(256) k_colsf(ColJob J, FftPlanDev Pin, FftPlan
     }
   }
   for (int o = 0; o < J.nout; ++o) {
+    // single-input jobs: the coefficient dispatched once per output; any code
+    // not listed (and every multi-input job) takes the per-element dispatch
+    bool done = J.nin == 1;
     if (J.nin == 1) {
       switch (J.coef[o][0]) {
+        case CC_NONE: coef_rows<T, TX, NIN, NOUT, CC_NONE>(IN, A, b, r0, jx, colok, J); break;
         case CC_ONE: coef_rows<T, TX, NIN, NOUT, CC_ONE>(IN, A, b, r0, jx, colok, J); break;
         case CC_G: coef_rows<T, TX, NIN, NOUT, CC_G>(IN, A, b, r0, jx, colok, J); break;
         case CC_GG: coef_rows<T, TX, NIN, NOUT, CC_GG>(IN, A, b, r0, jx, colok, J); break;
         case CC_IKX: coef_rows<T, TX, NIN, NOUT, CC_IKX>(IN, A, b, r0, jx, colok, J); break;
         case CC_IKY: coef_rows<T, TX, NIN, NOUT, CC_IKY>(IN, A, b, r0, jx, colok, J); break;
+        case CC_MIKY: coef_rows<T, TX, NIN, NOUT, CC_MIKY>(IN, A, b, r0, jx, colok, J); break;
         case CC_KILL: coef_rows<T, TX, NIN, NOUT, CC_KILL>(IN, A, b, r0, jx, colok, J); break;
         case CC_MASK: coef_rows<T, TX, NIN, NOUT, CC_MASK>(IN, A, b, r0, jx, colok, J); break;
         case CC_MASK4: coef_rows<T, TX, NIN, NOUT, CC_MASK4>(IN, A, b, r0, jx, colok, J); break;
-        default: coef_rows<T, TX, NIN, NOUT, CC_NONE>(IN, A, b, r0, jx, colok, J); break;
+        default: done = false; break;
       }
-    } else {
+    }
+    if (!done) {
       for (int row = r0; row < NOUT; row += RS) {
         int rin, js;
         row_map<NIN, NOUT>(row, J.ny_small, rin, js);
