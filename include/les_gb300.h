@@ -55,7 +55,10 @@ typedef struct les_config {
   int model;            /* param.f90:115  5 = Lagrangian scale-dependent,
                                           4 = Lagrangian scale-invariant,
                                           3 = plane-averaged scale-dependent,
-                                          2 = standard dynamic (plane-averaged) */
+                                          2 = standard dynamic (plane-averaged),
+                                          7 = model 5 plus the Lagrangian
+                                              scale-dependent SGS Prandtl number
+                                              of the scalars (s_flag, precision 0) */
   int s_flag;           /* param.f90:158  1 = active potential temperature      */
   int initu;            /* param.f90:79   0 = Euler first momentum step         */
   int initsc;           /* param.f90:79   0 = Euler first scalar step           */
@@ -97,6 +100,11 @@ typedef enum les_field {
   LES_S11, LES_S12, LES_S13, LES_S22, LES_S23, LES_S33,   /* calc_Sij output */
   /* humidity (scalars_module_q.f90:17-27; stored only when q_flag = 1) */
   LES_Q, LES_RHS_Q, LES_RHS_QF, LES_DQDX, LES_DQDY, LES_DQDZ,
+  /* model 7 (sgsmodule.f90:8-34; stored only when model = 7): the scalar
+   * Lagrangian averages, the turbulent Prandtl number, the scalar path's
+   * Lagrangian velocity sums and the time scales lagrange_Sdep leaves */
+  LES_G_LM, LES_G_MM, LES_G_QN, LES_G_NN, LES_PR_T,
+  LES_U_LAG_S, LES_V_LAG_S, LES_W_LAG_S, LES_TN_LMMM, LES_TN_QNNN,
   /* surface planes (nx,ny) */
   LES_ZO, LES_WT_S, LES_USTAR_AVG, LES_PHI_M, LES_PSI_M, LES_PSI_M0,
   LES_PHI_H, LES_PSI_H, LES_PSI_H0, LES_SGS_T3_SFC,
@@ -373,6 +381,18 @@ int les_scaledep_dynamic(les_ctx* ctx, double* cs_opt2, const double* S11, const
  * the context's u, v, w. */
 int les_std_dynamic(les_ctx* ctx, double* cs_opt2, const double* S11, const double* S12, const double* S13,
                     const double* S22, const double* S23, const double* S33);
+/* Model 7 (sgs_stag.f90:147-152): lagrange_scalar_Sdep.f90:1-467 computes
+ * Cs2_Pr = Cs^2/Pr_t with Lagrangian averaging of the scalar's
+ * L.M and Q.N along the pathlines (G_LM, G_MM, G_QN, G_NN, relaxed with the
+ * time scales of lagrange_Sdep), re-filters theta (filt_da) and sets
+ * Pr_t = Cs_opt2 / Cs2_Pr, Beta to the scalar's scale-dependence factor;
+ * interpolag_scalar_Sdep.f90 moves G_* along the back-trajectories of
+ * u_lag_s, v_lag_s, w_lag_s and resets them.  The scalars' SGS fluxes then
+ * use Pr_t instead of Pr (scalars_module.f90:77-82).  Both act on the
+ * module state of a model-7 context; cs2_pr is (ld,ny,nz). */
+int les_lagrange_scalar_sdep(les_ctx* ctx, double* cs2_pr, const double* S11, const double* S12,
+                             const double* S13, const double* S22, const double* S23, const double* S33);
+int les_interpolag_scalar_sdep(les_ctx* ctx);
 /* wallstress.f90:5-69, scalars_module.f90:508-690 (obukhov),
  * forcing.f90:128-219 (project), scalars_module.f90:57-171 (theta_all_in_one). */
 int les_wallstress(les_ctx* ctx);

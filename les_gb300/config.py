@@ -51,6 +51,7 @@ FIELDS = [
     "RHS_T", "RHS_Tf", "beta_scal", "dTdx", "dTdy", "dTdz",
     "S11", "S12", "S13", "S22", "S23", "S33",
     "q", "RHS_q", "RHS_qf", "dqdx", "dqdy", "dqdz",
+    "G_LM", "G_MM", "G_QN", "G_NN", "Pr_t", "u_lag_s", "v_lag_s", "w_lag_s", "TnLMMM", "TnQNNN",
     "zo", "wt_s", "ustar_avg", "phi_m", "psi_m", "psi_m0",
     "phi_h", "psi_h", "psi_h0", "sgs_t3", "wq_s", "sgs_q3",
 ]
@@ -58,6 +59,8 @@ FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 SURFACE_FIELDS = set(FIELDS[FIELDS.index("zo"):])
 # humidity arrays, stored only with q_flag = 1
 Q_FIELDS = {"q", "RHS_q", "RHS_qf", "dqdx", "dqdy", "dqdz", "wq_s", "sgs_q3"}
+# model 7 arrays, stored only with model = 7
+M7_FIELDS = {"G_LM", "G_MM", "G_QN", "G_NN", "Pr_t", "u_lag_s", "v_lag_s", "w_lag_s", "TnLMMM", "TnQNNN"}
 
 
 def make_config(nx, ny=None, nz_levels=None, *, model=5, s_flag=0, jt_total0=0,

@@ -155,20 +155,23 @@ struct Item {
   int field;  // LES_* for VOL, SFC_LD, PLANE
 };
 // Without humidity (q_flag = 0) qmix, RHS_q and sgs_q3 are written as the
-// zeros a run of the reference holds for them and skipped on reading.
+// zeros a run of the reference holds for them and skipped on reading; outside
+// model 7 G_LM..G_NN likewise, and Pr_t as the constant Pr.
 std::vector<Item> record_items(const les_ctx* c) {
   const bool q = c->cfg.q_flag != 0;
+  const bool m7 = c->cfg.model == 7;
   const Item qv = q ? Item{VOL, LES_Q} : Item{VOL_ZERO, -1};
   const Item qr = q ? Item{VOL, LES_RHS_Q} : Item{VOL_ZERO, -1};
   const Item q3 = q ? Item{SFC_LD, LES_SGS_Q3_SFC} : Item{SFC_LD_ZERO, -1};
+  auto g7 = [&](int f) { return m7 ? Item{VOL, f} : Item{VOL_ZERO, -1}; };
   if (c->cfg.s_flag)
     return {{VOL, LES_U},       {VOL, LES_V},       {VOL, LES_W},       {VOL, LES_THETA},   qv,  // qmix
             {VOL, LES_RHSX},    {VOL, LES_RHSY},    {VOL, LES_RHSZ},    {VOL, LES_RHS_T},   qr,  // RHS_q
             {SFC_LD, LES_SGS_T3_SFC}, q3,                                                        // sgs_t3, sgs_q3
             {PLANE, LES_PSI_M}, {PLANE, LES_PSI_M0}, {PLANE, LES_PSI_H}, {PLANE, LES_PSI_H0},
             {VOL, LES_CS_OPT2}, {VOL, LES_F_LM},    {VOL, LES_F_MM},    {VOL, LES_F_QN},    {VOL, LES_F_NN},
-            {VOL_ZERO, -1},     {VOL_ZERO, -1},     {VOL_ZERO, -1},     {VOL_ZERO, -1},                      // G_*
-            {VOL_PR, -1}};                                                                                   // Pr_t
+            g7(LES_G_LM),       g7(LES_G_MM),       g7(LES_G_QN),       g7(LES_G_NN),
+            m7 ? Item{VOL, LES_PR_T} : Item{VOL_PR, -1}};
   return {{VOL, LES_U},    {VOL, LES_V},       {VOL, LES_W},    {VOL, LES_RHSX},
           {VOL, LES_RHSY}, {VOL, LES_RHSZ},    {VOL, LES_CS_OPT2}, {VOL, LES_F_LM},
           {VOL, LES_F_MM}, {VOL, LES_F_QN},    {VOL, LES_F_NN}};
@@ -291,7 +294,7 @@ int les_checkpoint_read(les_ctx* c, const char* path) {
           std::memcpy(&sfc[(size_t)jy * g.nx], &buf[(size_t)jy * g.ld], (size_t)g.nx * sizeof(double));
         st = les_set_field(c, (les_field)it.field, sfc.data());
         break;
-      default: break;  // qmix, RHS_q, sgs_q3, G_*, Pr_t: not carried by this build
+      default: break;  // the zero and constant items of this configuration
     }
     if (st != LES_OK) break;
   }

@@ -186,7 +186,7 @@ struct Sizes {
   size_t wsA, wsB, wsP, big, tmp, fields, surf, spare, aux;
   int lag_chunk, ntmp;
 };
-static Sizes sizes_of(const Grid& g, bool q) {
+static Sizes sizes_of(const Grid& g, bool q, bool m7) {
   Sizes s{};
   s.lag_chunk = std::min(32, g.nz);
   const size_t nz = g.nz, C = g.C, CB = g.CB, ch = s.lag_chunk;
@@ -198,7 +198,8 @@ static Sizes sizes_of(const Grid& g, bool q) {
   s.tmp = (size_t)s.ntmp * g.nplane * sizeof(double);
   s.fields = 0;
   for (int f = 0; f < LES_ZO; ++f)
-    if (q || !is_q_field(f)) s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
+    if ((q || !is_q_field(f)) && (m7 || !is_m7_field(f)))
+      s.fields += (f == LES_P ? g.nplane * (nz + 1) : g.nfield) * sizeof(double);
   s.surf = (size_t)(LES_NUM_FIELDS - LES_ZO + 1 - (q ? 0 : 2)) * g.nx * g.ny * sizeof(double);
   s.spare = 4 * g.nfield * sizeof(double) + (4 * nz + 4) * C * sizeof(double2) + 2 * (nz + 1) * C * sizeof(double);
   // saved spectra, wall-plane spectra, Thomas tables, reductions, wavenumber
@@ -243,6 +244,7 @@ static void filter_G(const Grid& g, const std::vector<double>& k2, double alpha,
 
 static size_t felems(const les_ctx* c, int f) {
   if (is_q_field(f) && !c->cfg.q_flag) return 0;  // humidity arrays exist only with q_flag
+  if (is_m7_field(f) && c->cfg.model != 7) return 0;  // model-7 arrays exist only with model 7
   if (f >= LES_ZO) return (size_t)c->g.nx * c->g.ny;
   if (f == LES_P) return c->g.nplane * (c->g.nz + 1);
   return c->g.nfield;
@@ -261,7 +263,7 @@ size_t les_estimate_device_bytes(const les_config* cfg) {
   if (!cfg) return 0;
   Grid g;
   grid_of(*cfg, g);
-  Sizes s = sizes_of(g, cfg->q_flag != 0);
+  Sizes s = sizes_of(g, cfg->q_flag != 0, cfg->model == 7);
   size_t mixed = 0;  // float-float Thomas tables of the FP32-mixed form
   if (cfg->precision == 1) mixed = 2 * (size_t)(g.nz + 1) * g.C * sizeof(float2) + 64 * sizeof(int);
   return s.wsA + s.wsB + s.wsP + s.big + s.tmp + s.fields + s.surf + s.spare + s.aux + mixed + (1u << 20);
@@ -284,8 +286,12 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     les_set_error("q_flag = 1 needs s_flag = 1 and q_scale > 0");
     return LES_ERR_ARG;
   }
-  if (k.model != 5 && k.model != 4 && k.model != 3 && k.model != 2) {
-    les_set_error("model must be 5, 4, 3 or 2");
+  if (k.model == 7 && (k.precision != 0 || !k.s_flag)) {
+    les_set_error("model 7 needs s_flag = 1 and precision 0");
+    return LES_ERR_UNSUPPORTED;
+  }
+  if (k.model != 5 && k.model != 4 && k.model != 3 && k.model != 2 && k.model != 7) {
+    les_set_error("model must be 7, 5, 4, 3 or 2");
     return LES_ERR_UNSUPPORTED;
   }
   if (k.precision == 1 && k.model != 5) {  // the plane-averaged models read S_ij in FP64
@@ -310,6 +316,10 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     if ((st = dalloc(c, (void**)&c->f[f], c->fsize[f] * sizeof(double)))) return fail(st);
   }
   if ((st = dalloc(c, (void**)&c->z_os, (size_t)g.nx * g.ny * sizeof(double)))) return fail(st);
+  if (k.model == 7) {  // Pr_t starts at Pr (the reference reads it from the restart record)
+    std::vector<double> pr(g.nfield, k.pr);
+    cudaMemcpy(c->f[LES_PR_T], pr.data(), pr.size() * sizeof(double), cudaMemcpyHostToDevice);
+  }
   {  // phi_m = phi_h = 1 (set by obukhov before first use in any case)
     std::vector<double> one((size_t)g.nx * g.ny, 1.0);
     cudaMemcpy(c->f[LES_PHI_M], one.data(), one.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -363,7 +373,7 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
   if ((st = make_real_plan(c, g.nx, c->rx)) || (st = make_real_plan(c, g.nx2, c->rxb)) ||
       (st = make_plan(c, g.ny, c->cy)) || (st = make_plan(c, g.ny2, c->cyb)))
     return fail(st);
-  Sizes s = sizes_of(g, k.q_flag != 0);
+  Sizes s = sizes_of(g, k.q_flag != 0, k.model == 7);
   c->lag_chunk = s.lag_chunk;
   c->ntmp = s.ntmp;
   c->nbig = 9;
@@ -1216,6 +1226,24 @@ int les_interpolag_ssim(les_ctx* c) {
 int les_interpolag_sdep(les_ctx* c) {
   if (!c) return LES_ERR_ARG;
   op_interpolag(c);
+  return finish(c);
+}
+int les_lagrange_scalar_sdep(les_ctx* c, double* cs2_pr, const double* S11, const double* S12, const double* S13,
+                             const double* S22, const double* S23, const double* S33) {
+  if (!c || !cs2_pr || !S11 || !S12 || !S13 || !S22 || !S23 || !S33) return LES_ERR_ARG;
+  if (!c->f[LES_G_LM]) { les_set_error("les_lagrange_scalar_sdep needs a model-7 context"); return LES_ERR_STATE; }
+  const size_t n = c->g.nfield;
+  Arg a(c, S11, n), b(c, S12, n), d(c, S13, n), e(c, S22, n), f(c, S23, n), h(c, S33, n), o(c, cs2_pr, n);
+  CHK(a.in()); CHK(b.in()); CHK(d.in()); CHK(e.in()); CHK(f.in()); CHK(h.in()); CHK(o.alloc());
+  const double* S[6] = {a.dev, b.dev, d.dev, e.dev, f.dev, h.dev};
+  op_lagrange_scalar(c, S, o.dev);
+  CHK(o.out());
+  return finish(c);
+}
+int les_interpolag_scalar_sdep(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  if (!c->f[LES_G_LM]) { les_set_error("les_interpolag_scalar_sdep needs a model-7 context"); return LES_ERR_STATE; }
+  op_interpolag_scalar(c);
   return finish(c);
 }
 int les_scaledep_dynamic(les_ctx* c, double* cs_opt2, const double* S11, const double* S12, const double* S13,

@@ -134,6 +134,8 @@ inline bool mixed_f32_field(int f) {
 inline bool is_q_field(int f) {
   return (f >= LES_Q && f <= LES_DQDZ) || f == LES_WQ_S || f == LES_SGS_Q3_SFC;
 }
+// model 7 arrays: stored only when model = 7
+inline bool is_m7_field(int f) { return f >= LES_G_LM && f <= LES_TN_QNNN; }
 // An FP32-mixed context keeps the momentum right-hand sides (this step's
 // and the previous step's) as float-float pairs: hi and lo floats in each
 // 8-byte slot of the FP64 layout.  les_get_field / les_set_field convert.
@@ -169,6 +171,8 @@ int op_theta(les_ctx* c);
 int op_q(les_ctx* c);
 int op_thermo(les_ctx* c, double* const* out);  // 9 (ld,ny,nz) arrays, atm_thermodynamics.f90 order
 int op_stats(les_ctx* c);                        // one MM_XYZ_Out accumulation (io.f90:403-866)
+int op_lagrange_scalar(les_ctx* c, const double* const* S, double* cs2_pr);  // model 7 (cs2_pr may be null)
+int op_interpolag_scalar(les_ctx* c);
 int op_divstress(les_ctx* c, double* divtx, double* divty, double* divtz);
 int op_divstress_one(les_ctx* c, double* divt, const double* tx, const double* ty, const double* tz, int w_variant);
 int op_convec(les_ctx* c, double* cx, double* cy, double* cz);

@@ -823,7 +823,8 @@ int op_wallstress(les_ctx* c, const double* uv1) {
 
 // ---------------------------------------------------------------------------
 // sgs_stag.f90:371-498 calc_Sij ('wall') fused with the Lagrangian velocity
-// accumulation of sgs_stag.f90:59-69
+// accumulation of sgs_stag.f90:59-69 (uls, vls, wls: the scalar model's
+// second sum, u_lag_s, when it is carried, else null)
 __global__ void k_calc_sij(const double* __restrict__ dudx, const double* __restrict__ dudy,
                            const double* __restrict__ dudz, const double* __restrict__ dvdx,
                            const double* __restrict__ dvdy, const double* __restrict__ dvdz,
@@ -831,12 +832,14 @@ __global__ void k_calc_sij(const double* __restrict__ dudx, const double* __rest
                            const double* __restrict__ dwdz, double* S11, double* S12, double* S13,
                            double* S22, double* S23, double* S33, const double* __restrict__ u,
                            const double* __restrict__ v, const double* __restrict__ w, double* ul,
-                           double* vl, double* wl, int ld, int nx, int ny, int nz, int lag) {
+                           double* vl, double* wl, double* uls, double* vls, double* wls, int ld, int nx,
+                           int ny, int nz, int lag) {
   const size_t np = (size_t)ld * ny;
   GSTRIDE(i, np * nz) {
     const int jz = (int)(i / np) + 1;
     const int jx = (int)((i - (size_t)(jz - 1) * np) % ld);
     if (lag) { ul[i] += u[i]; vl[i] += v[i]; wl[i] += w[i]; }
+    if (uls) { uls[i] += u[i]; vls[i] += v[i]; wls[i] += w[i]; }
     if (jx >= nx) continue;
     double ux, uy, uz, vx, vy, vz, wx, wy, wz;
     if (jz == 1) {
@@ -1023,7 +1026,8 @@ int op_sgs_stag(les_ctx* c) {
       c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
       c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
       c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
-      c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0); LES_COUNT_LAUNCH();
+      c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_U_LAG_S], c->f[LES_V_LAG_S], c->f[LES_W_LAG_S], g.ld, g.nx, g.ny,
+      g.nz, lag ? 1 : 0); LES_COUNT_LAUNCH();
   const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
   if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {  // sgs_stag.f90:120-160
     if (k.model == 2 || k.model == 3) {
@@ -1036,6 +1040,9 @@ int op_sgs_stag(les_ctx* c) {
       op_lagrange_ssim(c, S);
     } else if (k.model == 5) {
       op_lagrange(c, S);
+    } else if (k.model == 7) {  // sgs_stag.f90:150-152
+      op_lagrange(c, S);
+      op_lagrange_scalar(c, S, nullptr);
     }
   }
   int ov = 0;
@@ -1044,6 +1051,7 @@ int op_sgs_stag(les_ctx* c) {
     ov = 1;
     const float c016 = 0.16f;
     csov = (double)(c016 * c016);
+    if (k.model == 7) fill(c, c->f[LES_PR_T], g.nfield, k.pr);  // Pr_t = Pr (:171)
   }
   const double delta = g.delta;
   k_nut<<<grid1(g.nfield), 256, 0, c->stream>>>(S[0], S[1], S[2], S[3], S[4], S[5], c->f[LES_CS_OPT2],
@@ -1283,8 +1291,9 @@ __device__ __forceinline__ R smagR(R a11, R a22, R a33, R a12, R a13, R a23) {
 // arrays stay FP64.
 template <typename S, typename R>
 __global__ void k_lag_final(const S* __restrict__ flt, double* F_LM, double* F_MM, double* F_QN,
-                            double* F_NN, double* Beta, double* Cs, int ld, int nx, int ny, int nz, int jz0,
-                            int nlev, size_t np, R cst, R opftdelta, R lagran_dt, int bexp_one, R bexp) {
+                            double* F_NN, double* Beta, double* Cs, double* TnLM, double* TnQN, int ld, int nx,
+                            int ny, int nz, int jz0, int nlev, size_t np, R cst, R opftdelta, R lagran_dt,
+                            int bexp_one, R bexp) {
   const size_t tot = np * nlev;
   GSTRIDE(t, tot) {
     const int lc = (int)(t / np);
@@ -1323,6 +1332,7 @@ __global__ void k_lag_final(const S* __restrict__ flt, double* F_LM, double* F_M
     const R e24 = (R)1e-24f;
     R flm = (R)F_LM[gi], fmm = (R)F_MM[gi];
     R Tn = fmax32r(flm * fmm, e24);
+    if (TnLM) TnLM[gi] = (double)Tn;  // lagrange_Sdep.f90:322, read by lagrange_scalar_Sdep
     Tn = opftdelta * pow_m18(Tn);
     Tn = fmax32r(e24, Tn);
     R dumfac = lagran_dt / Tn;
@@ -1334,6 +1344,7 @@ __global__ void k_lag_final(const S* __restrict__ flt, double* F_LM, double* F_M
     F_LM[gi] = flm; F_MM[gi] = fmm;
     R fqn = (R)F_QN[gi], fnn = (R)F_NN[gi];
     Tn = fmax32r(fqn * fnn, e24);
+    if (TnQN) TnQN[gi] = (double)Tn;  // :363
     Tn = opftdelta * pow_m18(Tn);
     Tn = fmax32r(e24, Tn);
     dumfac = lagran_dt / Tn;
@@ -1386,9 +1397,245 @@ int op_lagrange(les_ctx* c, const double* const* S) {
     c2r(c, 42, nl, c->wsB, out, (long)g.nplane, false, g.lh);
     k_lag_final<double, double><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
-        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst, opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
+        c->f[LES_CS_OPT2], c->f[LES_TN_LMMM], c->f[LES_TN_QNNN], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, cst,
+        opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
   }
   // the level loop's pointer table must outlive the launches
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Model 7: the scalar's Lagrangian scale-dependent SGS Prandtl number.
+// interpolag_scalar_Sdep.f90:1-227: interpolag_Sdep's back-trajectory
+// interpolation applied to G_LM, G_MM, G_QN, G_NN along u_lag_s, v_lag_s,
+// w_lag_s, which it then resets.
+int op_interpolag_scalar(les_ctx* c) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  if (!c->f[LES_G_LM]) return LES_ERR_STATE;
+  double* Fn[4];
+  for (int q = 0; q < 4; ++q) Fn[q] = c->spare + (size_t)q * g.nfield;
+  k_interpolag<4, true><<<grid1((size_t)g.nx * g.ny * g.nz), 256, 0, c->stream>>>(
+      c->f[LES_U_LAG_S], c->f[LES_V_LAG_S], c->f[LES_W_LAG_S], c->f[LES_G_LM], c->f[LES_G_MM], c->f[LES_G_QN],
+      c->f[LES_G_NN], Fn[0], Fn[1], Fn[2], Fn[3], g.ld, g.nx, g.ny, g.nz, (double)k.cs_count, k.dt, g.dx, g.dy,
+      g.dz); LES_COUNT_LAUNCH();
+  for (int q = 0; q < 4; ++q)
+    cudaMemcpyAsync(c->f[LES_G_LM + q], Fn[q], g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemsetAsync(c->f[LES_U_LAG_S], 0, g.nfield * sizeof(double), c->stream);
+  cudaMemsetAsync(c->f[LES_V_LAG_S], 0, g.nfield * sizeof(double), c->stream);
+  cudaMemsetAsync(c->f[LES_W_LAG_S], 0, g.nfield * sizeof(double), c->stream);
+  return 0;
+}
+
+// lagrange_scalar_Sdep.f90:96-131 (lbc = 1): the homogeneous surface flux
+// and the plane-mean u* of the log law give dTdz at z = dz/2.  One CTA: the
+// four plane sums, then the first level.
+__global__ void __launch_bounds__(1024) k_lag_s_surface(const double* __restrict__ u, const double* __restrict__ v,
+                                                        const double* __restrict__ zo,
+                                                        const double* __restrict__ wt_s,
+                                                        const double* __restrict__ psi_m,
+                                                        const double* __restrict__ phi_h, double* dTdz, int nx,
+                                                        int ny, int ld, double dz, double vonk, double t_scale,
+                                                        double u_star) {
+  __shared__ double red[4][32];
+  const int ns = nx * ny;
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+    const int jy = s / nx, jx = s - jy * nx;
+    const size_t i = (size_t)jy * ld + jx;
+    a[0] += log(zo[s]);
+    a[1] += wt_s[s];
+    a[2] += sqrt(u[i] * u[i] + v[i] * v[i]);
+    a[3] += psi_m[s];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
+    if (lane == 0) red[q][wid] = a[q];
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      a[q] = lane < nw ? red[q][lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
+    }
+    if (lane == 0) {
+      red[0][0] = a[0]; red[1][0] = a[1]; red[2][0] = a[2]; red[3][0] = a[3];
+    }
+  }
+  __syncthreads();
+  const double nf = (double)(float)ns;  // float(nx*ny)
+  const double zo_avg = exp(red[0][0] / nf);
+  const double ustar_ = red[2][0] / nf * vonk / (log(0.5 * dz / zo_avg) - red[3][0] / nf);
+  const double sflux = (red[1][0] / (double)ns) / t_scale / u_star;
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+    const int jy = s / nx, jx = s - jy * nx;
+    dTdz[(size_t)jy * ld + jx] = -phi_h[s] * sflux / (ustar_ * vonk * dz / 2.0);
+  }
+}
+
+// lagrange_scalar_Sdep.f90:140-262 inputs: 19 planes per level of the chunk
+// (u, v, w, theta on the w-node; their products with theta; S_ij; |S| dT/dx_i
+// and dT/dx_i on the w-node), each filtered at 2 delta and at 4 delta
+__global__ void k_lag_s_prep(const double* __restrict__ u, const double* __restrict__ v,
+                             const double* __restrict__ w, const double* __restrict__ th, Ptr6 Sp,
+                             const double* __restrict__ dTx, const double* __restrict__ dTy,
+                             const double* __restrict__ dTz, double* out, int jz0, int nlev, size_t np) {
+  const size_t tot = np * nlev;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jz = jz0 + lc;
+    const size_t i = (size_t)(jz - 1) * np + r;
+    const double s11 = Sp.p[0][i], s12 = Sp.p[1][i], s13 = Sp.p[2][i], s22 = Sp.p[3][i], s23 = Sp.p[4][i],
+                 s33 = Sp.p[5][i];
+    const double S = smag(s11, s22, s33, s12, s13, s23);
+    double ub, vb, wb, tb, gx, gy, gz, sx, sy, sz;
+    if (jz == 1) {  // :140-145, :227-235, :253-262
+      ub = u[i]; vb = v[i]; wb = 0.25 * w[i + np]; tb = th[i];
+      sx = S * dTx[i];
+      sy = S * dTy[i];
+      sz = S * (dTz[i] + dTz[i + np]) / 2.0;
+      gx = dTx[i]; gy = dTy[i]; gz = (dTz[i] + dTz[i + np]) / 2.0;
+    } else {
+      ub = 0.5 * (u[i] + u[i - np]); vb = 0.5 * (v[i] + v[i - np]); wb = w[i];
+      tb = 0.5 * (th[i] + th[i - np]);
+      sx = S * (dTx[i] + dTx[i - np]) / 2.0;
+      sy = S * (dTy[i] + dTy[i - np]) / 2.0;
+      sz = S * dTz[i];
+      gx = (dTx[i] + dTx[i - np]) / 2.0; gy = (dTy[i] + dTy[i - np]) / 2.0; gz = dTz[i];
+    }
+    double* o = out + t;
+    const size_t st = np * nlev;
+    o[0] = ub; o[st] = vb; o[2 * st] = wb; o[3 * st] = tb;
+    o[4 * st] = ub * tb; o[5 * st] = vb * tb; o[6 * st] = wb * tb;
+    o[7 * st] = s11; o[8 * st] = s12; o[9 * st] = s13; o[10 * st] = s22; o[11 * st] = s23; o[12 * st] = s33;
+    o[13 * st] = sx; o[14 * st] = sy; o[15 * st] = sz;
+    o[16 * st] = gx; o[17 * st] = gy; o[18 * st] = gz;
+  }
+}
+
+// lagrange_scalar_Sdep.f90:166-390 from the 38 filtered planes (G_test: q,
+// G_test_test: 19 + q): L_i = bar(u_i T) - bar u_i bar T, Q_i at 4 delta,
+// M_i, N_i, the relaxed G_*, Cs2_Pr at 2 and 4 delta, Beta, Cs2_Pr, Pr_t
+__global__ void k_lag_s_final(const double* __restrict__ flt, double* G_LM, double* G_MM, double* G_QN, double* G_NN,
+                              const double* __restrict__ TnLM, const double* __restrict__ TnQN,
+                              const double* __restrict__ Cs, double* Beta, double* Pr_t, double* cs2_pr, int ld,
+                              int nx, int nz, int jz0, int nlev, size_t np, double cst, double opftdelta,
+                              double lagran_dt, int bexp_one, double bexp) {
+  const size_t tot = np * nlev;
+  const double e24 = (double)1e-24f;
+  GSTRIDE(t, tot) {
+    const int lc = (int)(t / np);
+    const size_t r = t - (size_t)lc * np;
+    const int jx = (int)(r % ld);
+    const int jz = jz0 + lc;
+    const size_t gi = (size_t)(jz - 1) * np + r;
+    if (jx >= nx) {  // padding: Cs2_Pr = Cs_opt2 = 1e-24 (:334-336, :384-386)
+      Pr_t[gi] = 1.0;
+      if (cs2_pr) cs2_pr[gi] = e24;
+      continue;
+    }
+    const size_t st = np * nlev;
+    const double* G = flt + t;
+    const double* H = flt + t + 19 * st;
+    double L[3], Q[3], M[3], N[3];
+    const double Sb = smag(G[7 * st], G[10 * st], G[12 * st], G[8 * st], G[9 * st], G[11 * st]);
+    const double Sh = smag(H[7 * st], H[10 * st], H[12 * st], H[8 * st], H[9 * st], H[11 * st]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      L[q] = G[(4 + q) * st] - G[q * st] * G[3 * st];
+      Q[q] = H[(4 + q) * st] - H[q * st] * H[3 * st];
+      M[q] = cst * (G[(13 + q) * st] - 4.0 * Sb * G[(16 + q) * st]);
+      N[q] = cst * (H[(13 + q) * st] - 16.0 * Sh * H[(16 + q) * st]);
+    }
+    const double LM = L[0] * M[0] + L[1] * M[1] + L[2] * M[2];
+    const double MM = M[0] * M[0] + M[1] * M[1] + M[2] * M[2];
+    const double QN = Q[0] * N[0] + Q[1] * N[1] + Q[2] * N[2];
+    const double NN = N[0] * N[0] + N[1] * N[1] + N[2] * N[2];
+    double Tn = opftdelta * pow_m18(TnLM[gi]);
+    Tn = fmax32(e24, Tn);
+    double dumfac = lagran_dt / Tn;
+    double epsi = dumfac / (1.0 + dumfac);
+    double glm = (epsi * LM + (1.0 - epsi) * G_LM[gi]);
+    const double gmm = (epsi * MM + (1.0 - epsi) * G_MM[gi]);
+    glm = fmax32(e24, glm);
+    const double c2 = fmax32(e24, glm / gmm);
+    G_LM[gi] = glm; G_MM[gi] = gmm;
+    Tn = opftdelta * pow_m18(TnQN[gi]);
+    Tn = fmax32(e24, Tn);
+    dumfac = lagran_dt / Tn;
+    epsi = dumfac / (1.0 + dumfac);
+    double gqn = (epsi * QN + (1.0 - epsi) * G_QN[gi]);
+    const double gnn = (epsi * NN + (1.0 - epsi) * G_NN[gi]);
+    gqn = fmax32(e24, gqn);
+    const double c4 = fmax32(e24, gqn / gnn);
+    G_QN[gi] = gqn; G_NN[gi] = gnn;
+    double beta = bexp_one ? c4 / c2 : pow(c4 / c2, bexp);
+    if (jz == nz) beta = 1.0;
+    Beta[gi] = beta;
+    const double betaclip = fmax32(beta, 1.0 / (2.0 * 4.0));
+    const double cp = fmax32(e24, c2 / betaclip);
+    if (cs2_pr) cs2_pr[gi] = cp;
+    Pr_t[gi] = Cs[gi] / cp;  // :390
+  }
+}
+
+// lagrange_scalar_Sdep.f90:1-467 (inilag = .false., inflow = .false.,
+// lbc = 1); S = S11..S33 (device).  theta is Nyquist-filtered in place
+// (filt_da, :83) as in the reference; cs2_pr may be null.
+int op_lagrange_scalar(les_ctx* c, const double* const* S, double* cs2_pr) {
+  const Grid& g = c->g;
+  const les_config& k = c->cfg;
+  if (!c->f[LES_G_LM]) return LES_ERR_STATE;
+  op_interpolag_scalar(c);  // :76 (reads nothing the copies below change)
+  double* th0 = c->spare;  // theta_temp (:74): theta before the filter
+  double* dTx = c->spare + g.nfield;
+  double* dTy = c->spare + 2 * g.nfield;
+  double* dTz = c->spare + 3 * g.nfield;
+  double* theta = c->f[LES_THETA];
+  cudaMemcpyAsync(th0, theta, g.nfield * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  op_filt_da(c, theta, dTx, dTy, g.nz);  // :83-84
+  op_ddz(c, dTz, theta, 1);
+  fill(c, dTz + (size_t)(g.nz - 1) * g.nplane, g.nplane, k.dtdz_top / k.t_scale * k.z_i);  // :86
+  k_lag_s_surface<<<1, 1024, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_ZO], c->f[LES_WT_S],
+                                             c->f[LES_PSI_M], c->f[LES_PHI_H], dTz, g.nx, g.ny, g.ld, g.dz, k.vonk,
+                                             k.t_scale, k.u_star); LES_COUNT_LAUNCH();
+  const double delta = g.delta;
+  const double cst = delta * delta;  // :81
+  const double opftdelta = 1.5 * delta;
+  const double lagran_dt = k.dt * (double)k.cs_count;
+  const double bexp = std::log(2.0) / (std::log(4.0) - std::log(2.0));
+  const int bone = (bexp == 1.0) ? 1 : 0;
+  Ptr6 Sp;
+  for (int q = 0; q < 6; ++q) Sp.p[q] = S[q];
+  const int nch = c->lag_chunk;
+  for (int jz0 = 1; jz0 <= g.nz; jz0 += nch) {
+    const int nl = std::min(nch, g.nz - jz0 + 1);
+    double* prep = c->tmp;                               // 19 * nl planes
+    double* flt = c->tmp + (size_t)19 * nch * g.nplane;  // 38 * nl planes
+    k_lag_s_prep<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], th0, Sp, dTx,
+                                                             dTy, dTz, prep, jz0, nl, g.nplane); LES_COUNT_LAUNCH();
+    const double* in[19];
+    for (int q = 0; q < 19; ++q) in[q] = prep + (size_t)q * nl * g.nplane;
+    r2c(c, 19, nl, in, (long)g.nplane, nullptr, nullptr, c->wsA, false, g.lh);
+    ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nl);
+    J.nin = 1; J.nout = 2; J.nf = 19;
+    J.in[0] = c->wsA; J.fs_in = (long)nl * g.C;
+    J.out[0] = c->wsB; J.out[1] = (C2*)c->wsB + (size_t)19 * nl * g.C; J.fs_out = (long)nl * g.C;
+    J.coef[0][0] = CC_G; J.coef[1][0] = CC_GG;
+    cols(c, J);
+    double* out[38];
+    for (int q = 0; q < 38; ++q) out[q] = flt + (size_t)q * nl * g.nplane;
+    c2r(c, 38, nl, c->wsB, out, (long)g.nplane, false, g.lh);
+    k_lag_s_final<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
+        flt, c->f[LES_G_LM], c->f[LES_G_MM], c->f[LES_G_QN], c->f[LES_G_NN], c->f[LES_TN_LMMM], c->f[LES_TN_QNNN],
+        c->f[LES_CS_OPT2], c->f[LES_BETA], c->f[LES_PR_T], cs2_pr, g.ld, g.nx, g.nz, jz0, nl, g.nplane, cst,
+        opftdelta, lagran_dt, bone, bexp); LES_COUNT_LAUNCH();
+  }
   return 0;
 }
 
@@ -1917,7 +2164,9 @@ struct MeanTab {
 // out = i kx in (acc: out += i kx in), kx of the column (the kx = nx/2 column
 // zeroed, as ddx.f90 zeroes it).  The fields this is used on carry no
 // ky = ny/2 content (Nyquist-filtered state, or p-hat with its Nyquist modes
-// zeroed), so skipping the y round trip that ddx would make loses nothing.
+// zeroed), so skipping the y round trip that ddx would make loses nothing;
+// the forward x pass that made `in` is scaled for an x round trip alone
+// (1/nx, not 1/(nx ny)), or `in` is already the inverse y transform.
 __global__ void k_ikx_rows(const dcomplex* __restrict__ in, dcomplex* out, const float2* __restrict__ kxd, int lh,
                            size_t n, int acc) {
   GSTRIDE(e, n) {
@@ -2976,11 +3225,16 @@ __global__ void k_scalar_prod(const S* __restrict__ um, const S* __restrict__ vm
     else R[i] = uu * sx[i] + vv * sy[i] + (wm[i] * sz[i] + wm[i + np] * sz[i + np]) / (S)2;
   }
 }
+// scalars_module.f90:77-82 Pr_: the constant Pr, or the field Pr_t of
+// model 7 when prt is not null
+__device__ __forceinline__ double pr_at(const double* __restrict__ prt, double pr, size_t i) {
+  return prt ? prt[i] : pr;
+}
 // scalars_module.f90:364-407 horizontal SGS fluxes
 template <typename NT>
 __global__ void k_scalar_temp_xy(const NT* __restrict__ nut, const double* __restrict__ dsx,
                                  const double* __restrict__ dsy, double* tx, double* ty, int ld, int nx, int ny,
-                                 int nz, double pr) {
+                                 int nz, double pr, const double* __restrict__ prt) {
   const size_t np = (size_t)ld * ny;
   GSTRIDE(i, np * nz) {
     const int jz = (int)(i / np) + 1;
@@ -2989,10 +3243,12 @@ __global__ void k_scalar_temp_xy(const NT* __restrict__ nut, const double* __res
     if (jz == nz) { tx[i] = 0.0; ty[i] = 0.0; continue; }
     const double nu = cvt<double, NT>(nut[i]);
     if (jz == 1) {
-      tx[i] = (1.0 / pr) * nu * dsx[i];
-      ty[i] = (1.0 / pr) * nu * dsy[i];
+      const double p1 = pr_at(prt, pr, i);
+      tx[i] = (1.0 / p1) * nu * dsx[i];
+      ty[i] = (1.0 / p1) * nu * dsy[i];
     } else {
-      const double f = (1.0 / (0.5 * (pr + pr))) * 0.5 * (nu + cvt<double, NT>(nut[i + np]));
+      const double f = (1.0 / (0.5 * (pr_at(prt, pr, i) + pr_at(prt, pr, i + np)))) * 0.5 *
+                       (nu + cvt<double, NT>(nut[i + np]));
       tx[i] = f * dsx[i];
       ty[i] = f * dsy[i];
     }
@@ -3002,7 +3258,7 @@ __global__ void k_scalar_temp_xy(const NT* __restrict__ nut, const double* __res
 template <typename NT>
 __global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const NT* __restrict__ nut,
                              const double* __restrict__ dsz, const double* __restrict__ sgs_t3, int ld, int nx,
-                             int ny, int nz, double pr, double cdz) {
+                             int ny, int nz, double pr, const double* __restrict__ prt, double cdz) {
   const size_t np = (size_t)ld * ny;
   GSTRIDE(i, np * (nz - 1)) {
     const int jz = (int)(i / np) + 1;
@@ -3011,9 +3267,9 @@ __global__ void k_scalar_rhs(double* R, const double* __restrict__ dxy, const NT
     if (jx >= nx) continue;
     const int jy = (int)(r / ld);
     // temp(k) = Nu_t dsdz / Pr on w-nodes, temp(1) = -surf_flux
-    const double t0 =
-        (jz == 1) ? -1.0 * sgs_t3[(size_t)jy * nx + jx] : (1.0 / pr) * cvt<double, NT>(nut[i]) * dsz[i];
-    const double t1 = (1.0 / pr) * cvt<double, NT>(nut[i + np]) * dsz[i + np];
+    const double t0 = (jz == 1) ? -1.0 * sgs_t3[(size_t)jy * nx + jx]
+                                : (1.0 / pr_at(prt, pr, i)) * cvt<double, NT>(nut[i]) * dsz[i];
+    const double t1 = (1.0 / pr_at(prt, pr, i + np)) * cvt<double, NT>(nut[i + np]) * dsz[i + np];
     R[i] = (-1.0 * R[i] + dxy[i]) + cdz * (t1 - t0);
   }
 }
@@ -3214,7 +3470,8 @@ static int op_scalar(les_ctx* c, const ScalarDesc& d) {
   double* ty = c->tmp + g.nfield;
   double* dxy = c->tmp + 2 * g.nfield;
   k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[d.dsdx], c->f[d.dsdy], tx, ty,
-                                                          g.ld, g.nx, g.ny, nz, k.pr); LES_COUNT_LAUNCH();
+                                                          g.ld, g.nx, g.ny, nz, k.pr, c->f[LES_PR_T]);
+  LES_COUNT_LAUNCH();
   {
     const double sc = 1.0 / (double)(g.nx * g.ny);
     const double* ii[2] = {tx, ty};
@@ -3228,7 +3485,7 @@ static int op_scalar(les_ctx* c, const ScalarDesc& d) {
   }
   k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T], c->f[d.dsdz],
                                                                  c->f[d.sgs3], g.ld, g.nx, g.ny, nz, k.pr,
-                                                                 1.0 / g.dz); LES_COUNT_LAUNCH();
+                                                                 c->f[LES_PR_T], 1.0 / g.dz); LES_COUNT_LAUNCH();
   // calcbeta on theta before the update
   if (d.buoyancy) calcbeta(c);
   if (c->jt == 1 && !k.initsc)
@@ -3823,8 +4080,8 @@ static int lagrangeT(les_ctx* c) {
     c2rT<T, S>(c, 21, nl, ob + (size_t)21 * FS, out + 21, (long)g.nplane, false, nGG);  // G_test_test
     k_lag_final<S, S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(
         flt, c->f[LES_F_LM], c->f[LES_F_MM], c->f[LES_F_QN], c->f[LES_F_NN], c->f[LES_BETA],
-        c->f[LES_CS_OPT2], g.ld, g.nx, g.ny, g.nz, jz0, nl, g.nplane, (S)cst, (S)opftdelta, (S)lagran_dt, bone,
-        (S)bexp); LES_COUNT_LAUNCH();
+        c->f[LES_CS_OPT2], MX ? nullptr : c->f[LES_TN_LMMM], MX ? nullptr : c->f[LES_TN_QNNN], g.ld, g.nx, g.ny,
+        g.nz, jz0, nl, g.nplane, (S)cst, (S)opftdelta, (S)lagran_dt, bone, (S)bexp); LES_COUNT_LAUNCH();
   }
   return 0;
 }
@@ -3846,7 +4103,8 @@ static int sgs_stagT(les_ctx* c) {
         c->f[LES_DUDX], c->f[LES_DUDY], c->f[LES_DUDZ], c->f[LES_DVDX], c->f[LES_DVDY], c->f[LES_DVDZ],
         c->f[LES_DWDX], c->f[LES_DWDY], c->f[LES_DWDZ], c->f[LES_S11], c->f[LES_S12], c->f[LES_S13],
         c->f[LES_S22], c->f[LES_S23], c->f[LES_S33], c->f[LES_U], c->f[LES_V], c->f[LES_W], c->f[LES_U_LAG],
-        c->f[LES_V_LAG], c->f[LES_W_LAG], g.ld, g.nx, g.ny, g.nz, lag ? 1 : 0);
+        c->f[LES_V_LAG], c->f[LES_W_LAG], c->f[LES_U_LAG_S], c->f[LES_V_LAG_S], c->f[LES_W_LAG_S], g.ld, g.nx,
+        g.ny, g.nz, lag ? 1 : 0);
   LES_COUNT_LAUNCH();
   const double* S[6] = {c->f[LES_S11], c->f[LES_S12], c->f[LES_S13], c->f[LES_S22], c->f[LES_S23], c->f[LES_S33]};
   if ((c->jt >= 1 || k.initu) && (c->jt % k.cs_count == 0)) {
@@ -3859,6 +4117,9 @@ static int sgs_stagT(les_ctx* c) {
       op_lagrange_ssim(c, S);
     } else if (k.model == 5) {
       lagrangeT<MX>(c);
+    } else if (k.model == 7) {  // sgs_stag.f90:150-152 (FP64 form only)
+      lagrangeT<MX>(c);
+      op_lagrange_scalar(c, S, nullptr);
     }
   }
   int ov = 0;
@@ -3867,6 +4128,7 @@ static int sgs_stagT(les_ctx* c) {
     ov = 1;
     const float c016 = 0.16f;
     csov = (double)(c016 * c016);
+    if (k.model == 7) fill(c, c->f[LES_PR_T], g.nfield, k.pr);  // Pr_t = Pr (:171)
   }
   if (MX) {
     Ptr6f Sp;
@@ -4122,11 +4384,12 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
     double* dxy = c->tmp + 2 * g.nfield;
     k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[d.dsdx],
                                                                     c->f[d.dsdy], tx, ty, g.ld, g.nx, g.ny, nz,
-                                                                    k.pr); LES_COUNT_LAUNCH();
+                                                                    k.pr, c->f[LES_PR_T]); LES_COUNT_LAUNCH();
     div_xyT<MX>(c, tx, ty, dxy, nz);
     k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T],
                                                                            c->f[d.dsdz], c->f[d.sgs3],
-                                                                           g.ld, g.nx, g.ny, nz, k.pr, 1.0 / g.dz);
+                                                                           g.ld, g.nx, g.ny, nz, k.pr, c->f[LES_PR_T],
+                                                                           1.0 / g.dz);
     LES_COUNT_LAUNCH();
   }
   if (d.buoyancy) calcbeta(c);
@@ -4196,9 +4459,11 @@ static void meanflow_lin(les_ctx* c) {
   const int ms = nz + 8;
   const double* mean = c->dred + 16 * (size_t)ms;  // u, v, w plane means (filt_da_uvw_mixed)
   k_mean_tab<<<(nz + 127) / 128, 128, 0, c->stream>>>(mean, ms, nz, g.dz, mean_tab(c)); LES_COUNT_LAUNCH();
-  const double sc = 1.0 / (double)(g.nx * g.ny);
+  // the transforms are unnormalised: u's x and y round trips gain nx ny,
+  // v's and w's x round trip alone gains nx
+  const double sc = 1.0 / (double)(g.nx * g.ny), scx = 1.0 / (double)g.nx;
   const double* in[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
-  const double scs[3] = {sc, sc, sc};
+  const double scs[3] = {sc, scx, scx};
   const double* offs[3] = {mean, mean + ms, mean + 2 * ms};
   r2cT<dfloat, double>(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh, offs);
   const long FS = (long)nz * g.C;

@@ -84,6 +84,8 @@ struct Oracle {
   Field divtx, divty, divtz;
   // sgsmodule.f90:8-34
   Field F_LM, F_MM, F_QN, F_NN, Beta, Cs_opt2, Nu_t, u_lag, v_lag, w_lag;
+  // model 7: G_LM..G_NN, Pr_t, u_lag_s.. (sgsmodule.f90:8-34), TnLMMM, TnQNNN
+  Field G_LM, G_MM, G_QN, G_NN, Pr_t, u_lag_s, v_lag_s, w_lag_s, TnLMMM, TnQNNN;
   Field S11, S12, S13, S22, S23, S33;
   // scalars_module.f90:31-36
   Field beta_scal, dTdx, dTdy, dTdz, RHS_T, RHS_Tf;
@@ -136,13 +138,15 @@ struct Oracle {
                    &txx, &txy, &tyy, &txz, &tyz, &tzz, &divtx, &divty, &divtz, &F_LM, &F_MM,
                    &F_QN, &F_NN, &Beta, &Cs_opt2, &Nu_t, &u_lag, &v_lag, &w_lag, &S11, &S12,
                    &S13, &S22, &S23, &S33, &beta_scal, &dTdx, &dTdy, &dTdz, &RHS_T, &RHS_Tf,
-                   &qmix, &dqdx, &dqdy, &dqdz, &RHS_q, &RHS_qf, &sgs_t3_vol, &sgs_q3_vol};
+                   &qmix, &dqdx, &dqdy, &dqdz, &RHS_q, &RHS_qf, &sgs_t3_vol, &sgs_q3_vol,
+                   &G_LM, &G_MM, &G_QN, &G_NN, &Pr_t, &u_lag_s, &v_lag_s, &w_lag_s, &TnLMMM, &TnQNNN};
     for (Field* f : fl) f->assign(nfield, 0.0);
     p.assign(nplane * (nz + 1), 0.0);
     Field* sf[] = {&zo, &z_os, &wt_s, &ustar_avg, &phi_m, &psi_m, &psi_m0, &phi_h, &psi_h,
                    &psi_h0, &sgs_t3, &wq_s, &sgs_q3};
     for (Field* f : sf) f->assign((size_t)nx * ny, 0.0);
     for (double& x : phi_m) x = 1.0;
+    for (double& x : Pr_t) x = Pr;  // the reference reads Pr_t from the restart record
     for (double& x : phi_h) x = 1.0;
     Beta_avg.assign(nz, 0.0); Betaclip_avg.assign(nz, 0.0);
     init_wavenumber();
@@ -485,6 +489,7 @@ struct Oracle {
       for (int jx = 1; jx <= nx; ++jx) { txzp[S2(jx, jy)] = txz[I(jx, jy, 1)]; tyzp[S2(jx, jy)] = tyz[I(jx, jy, 1)]; }
     if (model == 4 || model == 5 || model == 7) {  // :59-69
       for (size_t i = 0; i < nfield; ++i) { u_lag[i] += u[i]; v_lag[i] += v[i]; w_lag[i] += w[i]; }
+      for (size_t i = 0; i < nfield; ++i) { u_lag_s[i] += u[i]; v_lag_s[i] += v[i]; w_lag_s[i] += w[i]; }
     }
     const double l = delta;  // :109
     if ((jt >= 1 || initu) && (jt % cs_count == 0)) {  // :120-121, DYN_init = 1
@@ -500,6 +505,11 @@ struct Oracle {
         lagrange_Ssim(S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
       } else if (model == 5) {
         lagrange_Sdep(S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
+      } else if (model == 7) {  // :147-149
+        lagrange_Sdep(S11.data(), S12.data(), S13.data(), S22.data(), S23.data(), S33.data());
+        Field cs2pr(nfield, 0.0);
+        lagrange_scalar_Sdep(cs2pr.data(), S11.data(), S12.data(), S13.data(), S22.data(), S23.data(),
+                             S33.data());
       }
     }
     if (model == 5 || model == 6 || model == 7) {  // :166-173
@@ -507,6 +517,7 @@ struct Oracle {
         const float c016 = 0.16f;
         const double cs = (double)(c016 * c016);
         for (double& x : Cs_opt2) x = cs;
+        for (double& x : Pr_t) x = Pr;
       }
     }
     for (int jz = 1; jz <= nz; ++jz)  // :179-211
@@ -553,17 +564,28 @@ struct Oracle {
   }
 
   // interpolag_Sdep.f90:2-380 (non-MPI, read_inflow_file = .false.)
-  void interpolag_Sdep() { interpolag(4, true); }
+  void interpolag_Sdep() {
+    Field* F[4] = {&F_LM, &F_MM, &F_QN, &F_NN};
+    interpolag(4, true, F, u_lag, v_lag, w_lag);
+  }
+  // interpolag_scalar_Sdep.f90:1-227: the same algorithm on G_* along the
+  // scalar path's Lagrangian velocity sums
+  void interpolag_scalar_Sdep() {
+    Field* G[4] = {&G_LM, &G_MM, &G_QN, &G_NN};
+    interpolag(4, true, G, u_lag_s, v_lag_s, w_lag_s);
+  }
   // interpolag_Ssim.f90:3-316: the same back-trajectory interpolation of
   // F_LM and F_MM only, without the near-wall clip of interpolag_Sdep.f90:
   // 290-293 (its w_lag(1) keeps 0.25 w_lag(2), doubled when positive)
-  void interpolag_Ssim() { interpolag(2, false); }
-  void interpolag(const int nf, const bool sdep_clip) {
+  void interpolag_Ssim() {
+    Field* F[4] = {&F_LM, &F_MM, &F_QN, &F_NN};
+    interpolag(2, false, F, u_lag, v_lag, w_lag);
+  }
+  void interpolag(const int nf, const bool sdep_clip, Field* const* Fs, Field& u_lag, Field& v_lag, Field& w_lag) {
     const int NX = nx + 2, NY = ny + 2, NZ = nz + 2;
     std::vector<double> FLM((size_t)NX * NY * NZ), FMM(FLM.size()), FQN(FLM.size()), FNN(FLM.size());
     auto FI = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)NX * ((size_t)(j - 1) + (size_t)NY * (k - 1)); };
     std::vector<double>* FF[4] = {&FLM, &FMM, &FQN, &FNN};
-    Field* Fs[4] = {&F_LM, &F_MM, &F_QN, &F_NN};
     for (int q = 0; q < nf; ++q) {
       std::vector<double>& A = *FF[q];
       const Field& Fq = *Fs[q];
@@ -799,6 +821,7 @@ struct Oracle {
           double NN = N[0] * N[0] + N[3] * N[3] + N[5] * N[5] + 2.0 * (N[1] * N[1] + N[2] * N[2] + N[4] * N[4]);
           // :321-331
           double Tn = fmax32(F_LM[gi] * F_MM[gi], (double)f1em24);
+          TnLMMM[gi] = Tn;  // :322
           Tn = opftdelta * pow_m18(Tn);
           Tn = fmax32((double)f1em24, Tn);
           double dumfac = lagran_dt / Tn;
@@ -810,6 +833,7 @@ struct Oracle {
           cs2d = fmax32((double)f1em24, cs2d);
           // :362-385
           Tn = fmax32(F_QN[gi] * F_NN[gi], (double)f1em24);
+          TnQNNN[gi] = Tn;  // :363
           Tn = opftdelta * pow_m18(Tn);
           Tn = fmax32((double)f1em24, Tn);
           dumfac = lagran_dt / Tn;
@@ -832,6 +856,162 @@ struct Oracle {
         for (int jx = nx + 1; jx <= ld; ++jx) Cs_opt2[o + (size_t)(jx - 1) + (size_t)ld * (jy - 1)] = (double)f1em24;
       Beta_avg[jz - 1] = sum2d / sumcs;
       Betaclip_avg[jz - 1] = sum4d / sum2d;
+    }
+  }
+
+  // lagrange_scalar_Sdep.f90:1-467 (model 7; inilag = .false., inflow =
+  // .false., lbc = 1): Cs2_Pr = Cs^2 / Pr_t from Lagrangian averages of the
+  // scalar's L.M and Q.N along the pathlines, relaxed with the time scales
+  // lagrange_Sdep left in TnLMMM, TnQNNN; Pr_t = Cs_opt2 / Cs2_Pr; Beta is
+  // overwritten with the scalar's scale-dependence factor.
+  void lagrange_scalar_Sdep(double* cs2_pr, const double* s11, const double* s12, const double* s13,
+                            const double* s22, const double* s23, const double* s33) {
+    const double delta = 1.0 * std::pow(dx * dy, 1.0 / 2.0);  // :61
+    const double tf1 = 2.0, tf2 = 4.0;
+    const double opftdelta = 1.5 * delta;  // opftime = 1.5
+    const Field u_temp = u, v_temp = v, theta_temp = theta;  // :72-74
+    interpolag_scalar_Sdep();  // :76
+    const double lagran_dt = dt * (double)cs_count;  // :79
+    const double cst = delta * delta;  // const = delta**2 (:81)
+    // :83-87: theta is Nyquist-filtered in place; the derivatives are local
+    Field ldTdx(nfield, 0.0), ldTdy(nfield, 0.0), ldTdz(nfield, 0.0);
+    filt_da(theta.data(), ldTdx.data(), ldTdy.data(), nz);
+    ddz_uv(ldTdz.data(), theta.data());
+    for (size_t i = 0; i < nplane; ++i) ldTdz[(size_t)(nz - 1) * nplane + i] = dTdz_top / T_scale * z_i;
+    {  // :96-131, lbc = 1: the mean surface flux and the mean u*
+      double slz = 0.0, sws = 0.0, sus = 0.0, spm = 0.0;
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= nx; ++jx) slz += std::log(zo[S2(jx, jy)]);
+      const double zo_avg = std::exp(slz / (double)(float)(nx * ny));
+      for (size_t q = 0; q < wt_s.size(); ++q) sws += wt_s[q];
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= nx; ++jx) {
+          const size_t i = I(jx, jy, 1);
+          sus += std::sqrt(u[i] * u[i] + v[i] * v[i]);
+          spm += psi_m[S2(jx, jy)];
+        }
+      const double ustar_ = sus / (double)(float)(nx * ny) * vonk /
+                            (std::log(0.5 * dz / zo_avg) - spm / (double)(float)(nx * ny));
+      const double sflux = (sws / (double)(nx * ny)) / T_scale / u_star;
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= nx; ++jx)
+          ldTdz[I(jx, jy, 1)] = -phi_h[S2(jx, jy)] * sflux / (ustar_ * vonk * dz / 2.0);
+    }
+    const float f1em24 = 1e-24f;
+    const double bexp = std::log(tf1) / (std::log(tf2) - std::log(tf1));
+#pragma omp parallel for schedule(static)
+    for (int jz = 1; jz <= nz; ++jz) {
+      const size_t NP = nplane, o = (size_t)(jz - 1) * NP;
+      // planes: 0..3 u,v,w,theta bar ; 4..7 hat ; 8..10 L ; 11..13 Q ; 14..19 S bar ;
+      // 20..25 S hat ; 26..28 S dT bar ; 29..31 S dT hat ; 32..34 dT bar ; 35..37 dT hat
+      std::vector<double> buf(NP * 38);
+      auto pl = [&](int q) { return buf.data() + (size_t)q * NP; };
+      for (size_t i = 0; i < NP; ++i) {
+        double ub, vb, wb, tb;
+        if (jz == 1) {  // :140-145
+          ub = u_temp[i]; vb = v_temp[i]; wb = 0.25 * w[NP + i]; tb = theta_temp[i];
+        } else {
+          ub = 0.5 * (u_temp[o + i] + u_temp[o - NP + i]);
+          vb = 0.5 * (v_temp[o + i] + v_temp[o - NP + i]);
+          wb = w[o + i];
+          tb = 0.5 * (theta_temp[o + i] + theta_temp[o - NP + i]);
+        }
+        pl(0)[i] = ub; pl(1)[i] = vb; pl(2)[i] = wb; pl(3)[i] = tb;
+        pl(4)[i] = ub; pl(5)[i] = vb; pl(6)[i] = wb; pl(7)[i] = tb;
+        pl(8)[i] = ub * tb; pl(9)[i] = vb * tb; pl(10)[i] = wb * tb;
+        pl(11)[i] = ub * tb; pl(12)[i] = vb * tb; pl(13)[i] = wb * tb;
+      }
+      for (int q = 0; q < 4; ++q) test_filter(pl(q), G_test);  // :166-169
+      for (int q = 0; q < 3; ++q) {  // :171-176
+        test_filter(pl(8 + q), G_test);
+        for (size_t i = 0; i < NP; ++i) pl(8 + q)[i] = pl(8 + q)[i] - pl(q)[i] * pl(3)[i];
+      }
+      for (int q = 0; q < 4; ++q) test_filter(pl(4 + q), G_test_test);  // :178-181
+      for (int q = 0; q < 3; ++q) {  // :183-188
+        test_filter(pl(11 + q), G_test_test);
+        for (size_t i = 0; i < NP; ++i) pl(11 + q)[i] = pl(11 + q)[i] - pl(4 + q)[i] * pl(7)[i];
+      }
+      const double* Sp[6] = {s11 + o, s12 + o, s13 + o, s22 + o, s23 + o, s33 + o};
+      std::vector<double> S(NP);
+      for (size_t i = 0; i < NP; ++i) {
+        S[i] = smag(Sp[0][i], Sp[3][i], Sp[5][i], Sp[1][i], Sp[2][i], Sp[4][i]);  // :190-191
+        for (int q = 0; q < 6; ++q) { pl(14 + q)[i] = Sp[q][i]; pl(20 + q)[i] = Sp[q][i]; }
+        double dx_, dy_, dz_;
+        if (jz == 1) {  // :227-235
+          dx_ = ldTdx[o + i]; dy_ = ldTdy[o + i]; dz_ = (ldTdz[o + i] + ldTdz[o + NP + i]) / 2.0;
+          pl(26)[i] = S[i] * ldTdx[o + i];
+          pl(27)[i] = S[i] * ldTdy[o + i];
+          pl(28)[i] = S[i] * (ldTdz[o + i] + ldTdz[o + NP + i]) / 2.0;
+        } else {
+          dx_ = (ldTdx[o + i] + ldTdx[o - NP + i]) / 2.0;
+          dy_ = (ldTdy[o + i] + ldTdy[o - NP + i]) / 2.0;
+          dz_ = ldTdz[o + i];
+          pl(26)[i] = S[i] * (ldTdx[o + i] + ldTdx[o - NP + i]) / 2.0;
+          pl(27)[i] = S[i] * (ldTdy[o + i] + ldTdy[o - NP + i]) / 2.0;
+          pl(28)[i] = S[i] * ldTdz[o + i];
+        }
+        pl(29)[i] = pl(26)[i]; pl(30)[i] = pl(27)[i]; pl(31)[i] = pl(28)[i];
+        pl(32)[i] = dx_; pl(33)[i] = dy_; pl(34)[i] = dz_;  // :253-262
+        pl(35)[i] = dx_; pl(36)[i] = dy_; pl(37)[i] = dz_;
+      }
+      for (int q = 0; q < 6; ++q) test_filter(pl(14 + q), G_test);  // :208-220
+      for (int q = 0; q < 6; ++q) test_filter(pl(20 + q), G_test_test);
+      for (int q = 0; q < 3; ++q) test_filter(pl(26 + q), G_test);  // :241-247
+      for (int q = 0; q < 3; ++q) test_filter(pl(29 + q), G_test_test);
+      for (int q = 0; q < 3; ++q) test_filter(pl(32 + q), G_test);  // :268-274
+      for (int q = 0; q < 3; ++q) test_filter(pl(35 + q), G_test_test);
+      // columns 1:nx; the padding columns (Cs2_Pr = Cs_opt2 = 1e-24 there,
+      // :334-336, :384-386) carry Pr_t = 1 and feed nothing back
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = nx + 1; jx <= ld; ++jx) {
+          Pr_t[o + (size_t)(jx - 1) + (size_t)ld * (jy - 1)] = 1.0;
+          cs2_pr[o + (size_t)(jx - 1) + (size_t)ld * (jy - 1)] = (double)f1em24;
+        }
+      for (int jy = 1; jy <= ny; ++jy)
+        for (int jx = 1; jx <= nx; ++jx) {
+          const size_t i = (size_t)(jx - 1) + (size_t)ld * (jy - 1);
+          const size_t gi = o + i;
+          const double Sb = smag(pl(14)[i], pl(17)[i], pl(19)[i], pl(15)[i], pl(16)[i], pl(18)[i]);
+          const double Sh = smag(pl(20)[i], pl(23)[i], pl(25)[i], pl(21)[i], pl(22)[i], pl(24)[i]);
+          double M[3], N[3];
+          for (int q = 0; q < 3; ++q) {  // :276-282
+            M[q] = cst * (pl(26 + q)[i] - 4.0 * Sb * pl(32 + q)[i]);
+            N[q] = cst * (pl(29 + q)[i] - 16.0 * Sh * pl(35 + q)[i]);
+          }
+          const double LM = pl(8)[i] * M[0] + pl(9)[i] * M[1] + pl(10)[i] * M[2];  // :286-289
+          const double MM = M[0] * M[0] + M[1] * M[1] + M[2] * M[2];
+          const double QN = pl(11)[i] * N[0] + pl(12)[i] * N[1] + pl(13)[i] * N[2];
+          const double NN = N[0] * N[0] + N[1] * N[1] + N[2] * N[2];
+          // :322-332
+          double Tn = opftdelta * pow_m18(TnLMMM[gi]);
+          Tn = fmax32((double)f1em24, Tn);
+          double dumfac = lagran_dt / Tn;
+          double epsi = dumfac / (1.0 + dumfac);
+          G_LM[gi] = (epsi * LM + (1.0 - epsi) * G_LM[gi]);
+          G_MM[gi] = (epsi * MM + (1.0 - epsi) * G_MM[gi]);
+          G_LM[gi] = fmax32((double)f1em24, G_LM[gi]);
+          double c2 = G_LM[gi] / G_MM[gi];  // :334-337
+          c2 = fmax32((double)f1em24, c2);
+          // :350-365
+          Tn = opftdelta * pow_m18(TnQNNN[gi]);
+          Tn = fmax32((double)f1em24, Tn);
+          dumfac = lagran_dt / Tn;
+          epsi = dumfac / (1.0 + dumfac);
+          G_QN[gi] = (epsi * QN + (1.0 - epsi) * G_QN[gi]);
+          G_NN[gi] = (epsi * NN + (1.0 - epsi) * G_NN[gi]);
+          G_QN[gi] = fmax32((double)f1em24, G_QN[gi]);
+          double c4 = G_QN[gi] / G_NN[gi];
+          c4 = fmax32((double)f1em24, c4);
+          // :367-388
+          double beta = (bexp == 1.0) ? c4 / c2 : std::pow(c4 / c2, bexp);
+          if (jz == nz) beta = 1.0;
+          Beta[gi] = beta;
+          const double betaclip = fmax32(beta, 1.0 / (tf1 * tf2));
+          double cp = c2 / betaclip;
+          cp = fmax32((double)f1em24, cp);
+          cs2_pr[gi] = cp;
+          Pr_t[gi] = Cs_opt2[gi] / cp;  // :390
+        }
     }
   }
 
@@ -1396,31 +1576,32 @@ struct Oracle {
       }
     dealias2(RHS.data(), RHS_m.data(), nz);
     std::vector<double> temp(nfield, 0.0), dtemp(nfield, 0.0);
-    const double Pr_ = Pr;
+    // Pr_ (scalars_module.f90:77-82): Pr for models 1-5, the field Pr_t otherwise
+    auto Pr_ = [&](size_t a) { return model == 7 ? Pr_t[a] : Pr; };
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         const size_t a = I(i, j, 1);
-        temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdx[a];
+        temp[a] = (1.0 / Pr_(a)) * Nu_t[a] * dsdx[a];
       }
     for (int k = 2; k <= nz - 1; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k), b = I(i, j, k + 1);
-          temp[a] = (1.0 / (0.5 * (Pr_ + Pr_))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dsdx[a];
+          temp[a] = (1.0 / (0.5 * (Pr_(a) + Pr_(b)))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dsdx[a];
         }
     ddx(dtemp.data(), temp.data(), nz);
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         const size_t a = I(i, j, 1);
         RHS[a] = (-1.0 * RHS[a] + dtemp[a]);
-        temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdy[a];
+        temp[a] = (1.0 / Pr_(a)) * Nu_t[a] * dsdy[a];
       }
     for (int k = 2; k <= nz - 1; ++k)
       for (int j = 1; j <= ny; ++j)
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k), b = I(i, j, k + 1);
           RHS[a] = (-1.0 * RHS[a] + dtemp[a]);
-          temp[a] = (1.0 / (0.5 * (Pr_ + Pr_))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dsdy[a];
+          temp[a] = (1.0 / (0.5 * (Pr_(a) + Pr_(b)))) * 0.5 * (Nu_t[a] + Nu_t[b]) * dsdy[a];
         }
     ddy(dtemp.data(), temp.data(), nz);
     for (int j = 1; j <= ny; ++j)
@@ -1436,7 +1617,7 @@ struct Oracle {
         for (int i = 1; i <= nx; ++i) {
           const size_t a = I(i, j, k);
           RHS[a] = RHS[a] + dtemp[a];
-          temp[a] = (1.0 / Pr_) * Nu_t[a] * dsdz[a];
+          temp[a] = (1.0 / Pr_(a)) * Nu_t[a] * dsdz[a];
           sgs_vol[a] = -1.0 * temp[a];
         }
     std::fill(dtemp.begin(), dtemp.end(), 0.0);
@@ -1839,6 +2020,10 @@ struct Oracle {
       case LES_Q: return &qmix; case LES_RHS_Q: return &RHS_q; case LES_RHS_QF: return &RHS_qf;
       case LES_DQDX: return &dqdx; case LES_DQDY: return &dqdy; case LES_DQDZ: return &dqdz;
       case LES_WQ_S: return &wq_s; case LES_SGS_Q3_SFC: return &sgs_q3;
+      case LES_G_LM: return &G_LM; case LES_G_MM: return &G_MM; case LES_G_QN: return &G_QN;
+      case LES_G_NN: return &G_NN; case LES_PR_T: return &Pr_t; case LES_U_LAG_S: return &u_lag_s;
+      case LES_V_LAG_S: return &v_lag_s; case LES_W_LAG_S: return &w_lag_s; case LES_TN_LMMM: return &TnLMMM;
+      case LES_TN_QNNN: return &TnQNNN;
       default: return nullptr;
     }
   }
@@ -1969,6 +2154,12 @@ void lo_obukhov(void* h) { ((Oracle*)h)->obukhov(); }
 void lo_project(void* h) { ((Oracle*)h)->project(); }
 void lo_theta_all_in_one(void* h) { ((Oracle*)h)->theta_all_in_one(); }
 void lo_q_all_in_one(void* h) { ((Oracle*)h)->q_all_in_one(); }
+void lo_lagrange_scalar_sdep(void* h, double* cs2_pr) {
+  Oracle* o = (Oracle*)h;
+  o->lagrange_scalar_Sdep(cs2_pr, o->S11.data(), o->S12.data(), o->S13.data(), o->S22.data(), o->S23.data(),
+                          o->S33.data());
+}
+void lo_interpolag_scalar_sdep(void* h) { ((Oracle*)h)->interpolag_scalar_Sdep(); }
 void lo_stats_enable(void* h, int c_count, int p_count) { ((Oracle*)h)->stats_enable(c_count, p_count); }
 void lo_stats_accumulate(void* h) { ((Oracle*)h)->stats_accumulate(); }
 void lo_stats_reset(void* h, int group) { ((Oracle*)h)->stats_reset(group); }

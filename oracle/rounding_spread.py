@@ -13,12 +13,15 @@ each field is printed.  Two cases:
   humid0, humid500
            32^3, theta and qmix with the striped moisture flux, jt_total0 = 0
            or 500 (the dynamic Cs^2 feeds back from step 5), 10 steps.
+  model7   the humid500 case with SGS model 7 (the scalars' Lagrangian
+           dynamic Prandtl number Pr_t = Cs_opt2 / Cs2_Pr, both rounded
+           through FP32 by the reference) and theta perturbed on every level.
   c2       128^3, theta, striped surface, jt_total from 0, model 5, 200 steps
            (every 10 steps): the first level's explicit SGS diffusion number
            Nu_t dt / dz^2 is above the AB2 stability limit, so from about
            step 55 rounding differences at level 1 grow until they saturate.
 
-  python -m oracle.rounding_spread model3|humid0|humid500|c2
+  python -m oracle.rounding_spread model3|humid0|humid500|model7|c2
 """
 import json
 import os
@@ -57,6 +60,9 @@ def run_case(case, lib_path, out_path):
     elif case in ("humid0", "humid500"):
         cfg = lc.make_config(32, s_flag=1, q_flag=1, jt_total0=0 if case == "humid0" else 500, rmsdiv_every=1)
         seed, blocks, every = 41, 1, 10
+    elif case == "model7":
+        cfg = lc.make_config(32, s_flag=1, q_flag=1, jt_total0=500, model=7, rmsdiv_every=1)
+        seed, blocks, every = 41, 1, 10
     else:
         cfg = lc.make_config(128, s_flag=1, rmsdiv_every=10)
         seed, blocks, every = 21, 20, 10
@@ -64,14 +70,16 @@ def run_case(case, lib_path, out_path):
     o = oo.Oracle(cfg, surf)
     if getattr(cfg, "q_flag", 0):
         o.set("wq_s", lc.moisture_flux(cfg))
-    for k, v in lc.initial_state(cfg, surf, seed=seed).items():
+    levels = {"theta_levels": cfg.nz} if case == "model7" else {}
+    for k, v in lc.initial_state(cfg, surf, seed=seed, **levels).items():
         o.set(k, v)
     n = cfg.nx
     out = {}
     for b in range(blocks):
         o.step(every)
         step = (b + 1) * every
-        for nm in ("u", "v", "w", "theta", "Cs_opt2") + (("q",) if getattr(cfg, "q_flag", 0) else ()):
+        for nm in ("u", "v", "w", "theta", "Cs_opt2") + (("q",) if getattr(cfg, "q_flag", 0) else ()) + \
+                (("Pr_t", "G_LM", "G_QN") if cfg.model == 7 else ()):
             out["%s_%d" % (nm, step)] = o.get(nm)[:-1, :, :n]
         out["rmsdiv_%d" % step] = np.array(o.rmsdiv())
     np.savez(out_path, **out)

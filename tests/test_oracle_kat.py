@@ -317,15 +317,19 @@ def test_std_dynamic_galilean_invariance(O):
 
 
 @pytest.mark.parametrize("routine,fields", [("interpolag_ssim", ("F_LM", "F_MM")),
-                                            ("interpolag_sdep", ("F_LM", "F_MM", "F_QN", "F_NN"))])
+                                            ("interpolag_sdep", ("F_LM", "F_MM", "F_QN", "F_NN")),
+                                            ("interpolag_scalar_sdep", ("G_LM", "G_MM", "G_QN", "G_NN"))])
 @pytest.mark.parametrize("axis,shift", [(2, 0), (2, 1), (2, -1), (1, 1), (1, -1)])
 def test_interpolag_shifts_by_whole_cells(O, routine, fields, axis, shift):
     """interpolag_Ssim.f90 / interpolag_Sdep.f90: a uniform accumulated lag
     velocity of shift * dx / dt (x) or shift * dy / dt (y) gives a
     displacement of exactly -shift cells, so every F_* comes back shifted by
     `shift` cells (periodic) with frac = 0, comp = 1; the lag arrays are
-    reset afterwards."""
-    cfg = C.make_config(16, 16, 8, model=4 if routine == "interpolag_ssim" else 5)
+    reset afterwards.  interpolag_scalar_Sdep.f90 moves G_* along u_lag_s,
+    v_lag_s, w_lag_s the same way."""
+    model = {"interpolag_ssim": 4, "interpolag_sdep": 5, "interpolag_scalar_sdep": 7}[routine]
+    sfx = "_s" if model == 7 else ""
+    cfg = C.make_config(16, 16, 8, model=model, s_flag=1 if model == 7 else 0)
     d = C.dims(cfg)
     o = O(cfg)
     rng = np.random.default_rng(2)
@@ -336,15 +340,91 @@ def test_interpolag_shifts_by_whole_cells(O, routine, fields, axis, shift):
     h = 2 * np.pi / cfg.nx  # dx = dy on the 2pi x 2pi box with nx = ny
     lag = np.zeros(shp)
     lag[:, :, :cfg.nx] = shift * h / cfg.dt  # sum over cs_count steps: displacement -lag dt / dx
-    o.set("u_lag", lag if axis == 2 else np.zeros(shp))
-    o.set("v_lag", lag if axis == 1 else np.zeros(shp))
-    o.set("w_lag", np.zeros(shp))
+    o.set("u_lag" + sfx, lag if axis == 2 else np.zeros(shp))
+    o.set("v_lag" + sfx, lag if axis == 1 else np.zeros(shp))
+    o.set("w_lag" + sfx, np.zeros(shp))
     o.call(routine)
     n = cfg.nx
     for f, v in F.items():
         want = np.roll(v[:, :, :n], shift, axis=axis)
         assert np.allclose(o.get(f)[:, :, :n], want, rtol=0, atol=1e-15), f
-    assert not o.get("u_lag").any() and not o.get("v_lag").any()
+    assert not o.get("u_lag" + sfx).any() and not o.get("v_lag" + sfx).any()
+
+
+# ---- SGS model 7: the scalars' Lagrangian dynamic Prandtl number -----------
+
+def _m7(O, jt0=500, model=7, seed=9, **kw):
+    cfg = C.make_config(16, 16, 8, s_flag=1, model=model, jt_total0=jt0, **kw)
+    surf = C.striped_surface(cfg)
+    o = O(cfg, surf)
+    for k, v in C.initial_state(cfg, surf, seed=seed, theta_levels=cfg.nz).items():
+        o.set(k, v)
+    return cfg, surf, o
+
+
+def test_model7_below_500_is_model5(O):
+    """sgs_stag.f90:166-173: while jt_total < 500 model 7 holds Cs_opt2 at
+    0.16^2 and Pr_t at Pr, so its run is model 5's; the only trace of
+    lagrange_scalar_Sdep is its in-place Nyquist filter of theta (filt_da,
+    lagrange_scalar_Sdep.f90:83), which changes theta by rounding only."""
+    _, _, a = _m7(O, jt0=0, model=5)
+    cfg, _, b = _m7(O, jt0=0)
+    assert a.step(10) == 0 and b.step(10) == 0
+    n = cfg.nx
+    for nm in ("u", "v", "w", "theta"):
+        assert rel(b.get(nm)[:-1, :, :n], a.get(nm)[:-1, :, :n]) < 1e-13, nm
+    assert np.all(b.get("Pr_t") == cfg.pr)
+    # the scalar averages were updated at jt = 5 and 10 all the same
+    assert np.abs(b.get("G_MM")[:-1, :, :n]).min() > 0.0
+
+
+def test_lagrange_scalar_scale_covariance(O):
+    """theta -> 2 theta with the surface heat flux and the lid gradient
+    doubled: every filtered product and gradient doubles exactly (powers of
+    two scale IEEE arithmetic exactly), L_i and M_i double, L.M and M.M
+    quadruple, so with G_* quadrupled the relaxed G_* quadruple bit for bit
+    and Cs2_Pr and Pr_t are unchanged wherever the 1e-24 floor on G_LM,
+    G_QN (lagrange_scalar_Sdep.f90:331, :359) does not bind."""
+    cfg, surf, a = _m7(O, dtdz_top=0.003)
+    assert a.step(7) == 0  # past the update at jt = 5; lag sums of two steps
+    cfg2 = C.make_config(16, 16, 8, s_flag=1, model=7, jt_total0=500, dtdz_top=0.006)
+    b = O(cfg2, surf)
+    names = ["u", "v", "w", "theta", "G_LM", "G_MM", "G_QN", "G_NN", "u_lag_s", "v_lag_s", "w_lag_s",
+             "TnLMMM", "TnQNNN", "Cs_opt2", "psi_m", "phi_h", "wt_s", "S11", "S12", "S13", "S22", "S23", "S33"]
+    scale = {"theta": 2.0, "wt_s": 2.0, "G_LM": 4.0, "G_MM": 4.0, "G_QN": 4.0, "G_NN": 4.0}
+    for nm in names:
+        b.set(nm, scale.get(nm, 1.0) * a.get(nm))
+    shp = C.field_shape(cfg, "u")
+    ca, cb = np.zeros(shp), np.zeros(shp)
+    a.call("lagrange_scalar_sdep", ca)
+    b.call("lagrange_scalar_sdep", cb)
+    n = cfg.nx
+    free = (a.get("G_LM") > 1e-23) & (a.get("G_QN") > 1e-23)
+    free[:, :, n:] = False
+    assert free.sum() > 0.2 * free[:, :, :n].size
+    for nm in ("G_LM", "G_MM", "G_QN", "G_NN"):
+        assert np.array_equal(b.get(nm)[free], 4.0 * a.get(nm)[free]), nm
+    assert np.array_equal(cb[free], ca[free])
+    assert np.array_equal(b.get("Pr_t")[free], a.get("Pr_t")[free])
+    assert np.array_equal(b.get("theta")[:, :, :n], 2.0 * a.get("theta")[:, :, :n])
+    # Pr_t = Cs_opt2 / Cs2_Pr everywhere, the padding columns at 1
+    pr = a.get("Pr_t")
+    assert np.array_equal(pr[:, :, :n], a.get("Cs_opt2")[:, :, :n] / ca[:, :, :n])
+    assert np.all(pr[:, :, n:] == 1.0)
+
+
+def test_model7_step_is_finite_and_diffuses_with_pr_t(O):
+    """From jt_total = 500 model 7 runs its scalar SGS fluxes with the
+    dynamic Pr_t (scalars_module.f90:77-82): the state stays finite and the
+    scalar differs from model 5's, the velocities only through buoyancy."""
+    _, _, a = _m7(O, model=5)
+    cfg, _, b = _m7(O)
+    assert a.step(10) == 0 and b.step(10) == 0
+    n = cfg.nx
+    for nm in ("u", "v", "w", "theta", "Pr_t", "G_LM", "G_MM"):
+        assert np.all(np.isfinite(b.get(nm)[:-1, :, :n])), nm
+    assert rel(b.get("theta")[:-1, :, :n], a.get("theta")[:-1, :, :n]) > 1e-9
+    assert not np.all(b.get("Pr_t") == cfg.pr)
 
 
 # ---- humidity (scalars_module_q.f90, atm_thermodynamics.f90) ----------------
