@@ -1,6 +1,6 @@
 """Benchmark of the per-timestep spectral core (pt-steps/s = Nx*Ny*Nz*steps / s).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|fp64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|fp64|ff]
                   [--impl ours|reference] [--grid 256] [--no-fp64] [--no-e2e] [--no-cpu]
                   [--no-serve]
 
@@ -57,7 +57,8 @@ def parse():
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)  # multiple of cs_count (5)
     p.add_argument("--warmup", type=int, default=3)
-    p.add_argument("--form", default="mixed", choices=["fp64", "mixed"])
+    p.add_argument("--form", default="mixed", choices=["fp64", "mixed", "ff"],
+                   help="mixed: FP32-mixed step; fp64: FP64 step; ff: FP64 state with float-float transforms")
     p.add_argument("--model", type=int, default=5, choices=[5, 4, 3, 2],
                    help="SGS model of the FP64 step (5 Lagrangian scale-dependent, 4 scale-invariant, "
                         "3 plane-averaged scale-dependent, 2 standard dynamic)")
@@ -156,8 +157,11 @@ MODEL = 5  # --model: SGS model of the FP64 step (the mixed form runs model 5)
 MODEL_NAME = {5: "lagrangian-sdep", 4: "lagrangian-ssim", 3: "plane-sdep", 2: "std-dynamic"}
 
 
+PRECISION = {"fp64": 0, "mixed": 1, "ff": 2}
+
+
 def workload_config(lg, grid, form):
-    cfg = lg.make_config(grid, nz_levels=LEVELS, s_flag=1, precision=1 if form == "mixed" else 0,
+    cfg = lg.make_config(grid, nz_levels=LEVELS, s_flag=1, precision=PRECISION[form],
                          rmsdiv_every=0, model=5 if form == "mixed" else MODEL)
     surf = lg.striped_surface(cfg)
     return cfg, surf
@@ -396,6 +400,22 @@ def main():
                    "rmsdiv_mixed": ctx_m.rmsdiv(), "rmsdiv_fp64": ctx_d.rmsdiv(),
                    "fp64_step_ledger_frac": bpp_d * pts / (ms_d / args.steps / 1e3) / 1e9 / hbm}
         ctx_m.close()
+        # the FP64 state with float-float transforms (precision 2), same steps
+        cfg_f, ctx_f = new_member(lg, args.grid, "ff", 1234)
+        for _ in range(warm):
+            ctx_f.step(1)
+        torch.cuda.synchronize()
+        ms_f, _, _ = timed_steps(torch, lg, ctx_f, args.steps)
+        err_f = {}
+        for nm in ("u", "v", "w", "theta"):
+            a = ctx_f.get(nm)[:-1, :, :cfg.nx]
+            d = ctx_d.get(nm)[:-1, :, :cfg.nx]
+            err_f[nm] = float(np.linalg.norm(a - d) / np.linalg.norm(d))
+        compare["ff"] = {"ms_per_step": ms_f / args.steps, "value": pts * args.steps / (ms_f / 1e3),
+                         "over_fp64": ms_d / ms_f, "rel_err_vs_fp64": err_f, "rmsdiv": ctx_f.rmsdiv()}
+        if not args.no_e2e:
+            compare["ff"]["e2e"] = e2e_run(torch, lg, ctx_f, cfg_f, world)
+        ctx_f.close()
         if not args.no_e2e:
             compare["fp64_e2e"] = e2e_run(torch, lg, ctx_d, cfg_d, world)
         ctx_d.close()
@@ -416,7 +436,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "pt-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": warm, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64" if args.form == "fp64" else "f32/f64-mixed",
+                "dtype": {"fp64": "f64", "ff": "f64 (float-float transforms)"}.get(args.form, "f32/f64-mixed"),
                 "data": "synthetic (seeded SplitMix64 initial state, x-striped surface)",
                 "config": {"workload": workload_name(cfg), "grid": [cfg.nx, cfg.ny, cfg.nz - 1],
                            "form": args.form, "dt": cfg.dt, "cflu": cflu, "visc_stab": visc,

@@ -58,13 +58,15 @@ typedef struct les_config {
                                           2 = standard dynamic (plane-averaged),
                                           7 = model 5 plus the Lagrangian
                                               scale-dependent SGS Prandtl number
-                                              of the scalars (s_flag, precision 0) */
+                                              of the scalars (s_flag, precision 0 or 2) */
   int s_flag;           /* param.f90:158  1 = active potential temperature      */
   int initu;            /* param.f90:79   0 = Euler first momentum step         */
   int initsc;           /* param.f90:79   0 = Euler first scalar step           */
   int cs_count;         /* param.f90:100  steps between dynamic Cs updates (5)  */
   int jt_total0;        /* total_time.dat (param.f90:203-214) step offset        */
-  int precision;        /* 0 = FP64 throughout, 1 = FP32-mixed form             */
+  int precision;        /* 0 = FP64 throughout, 1 = FP32-mixed form,
+                                          2 = FP64 state and arithmetic with
+                                              float-float (about 48-bit) transforms */
   int rmsdiv_every;     /* main.f90:451   rmsdiv/CFL diagnostic period (500)    */
   int q_flag;           /* main.f90:274   1 = humidity qmix (scalars_module_q.f90)
                                           advanced after theta; needs s_flag.
@@ -153,7 +155,7 @@ int les_set_surface(les_ctx* ctx, const double* zo, const double* wt_s);
  * array); these copies and les_sync_* narrow / widen them, and
  * les_field_device_ptr returns that FP32 storage.  The per-routine entries
  * les_convec, les_sgs_stag, les_wallstress and les_theta_all_in_one need a
- * precision-0 context.  Precision 1 runs model 5. */
+ * precision-0 or precision-2 context.  Precision 1 runs model 5. */
 int les_set_field(les_ctx* ctx, les_field f, const double* host);
 int les_get_field(les_ctx* ctx, les_field f, double* host);
 /* Device address of a module array (for zero-copy use by the caller).  The
@@ -402,7 +404,7 @@ int les_theta_all_in_one(les_ctx* ctx);
 /* scalars_module_q.f90:31-141 q_all_in_one (filt_da and ddz_uv of qmix, the
  * lid gradient dqdz_top, scalar_q_RHS_calc :145-367, step_scalar_q :370-397)
  * on the context's module state; needs q_flag = 1 (else LES_ERR_STATE) and a
- * precision-0 context.  In les_step it runs after theta_all_in_one
+ * precision-0 or precision-2 context.  In les_step it runs after theta_all_in_one
  * (main.f90:273-274); qmix also enters calcbeta's virtual temperature
  * (scalars_module.f90:200-223) and obukhov's buoyancy flux
  * (scalars_module.f90:547-550). */

@@ -281,13 +281,13 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
     les_set_error("invalid physical parameters");
     return LES_ERR_ARG;
   }
-  if (k.precision != 0 && k.precision != 1) { les_set_error("precision must be 0 or 1"); return LES_ERR_ARG; }
+  if (k.precision < 0 || k.precision > 2) { les_set_error("precision must be 0, 1 or 2"); return LES_ERR_ARG; }
   if (k.q_flag != 0 && (k.q_flag != 1 || !k.s_flag || !(k.q_scale > 0.0))) {
     les_set_error("q_flag = 1 needs s_flag = 1 and q_scale > 0");
     return LES_ERR_ARG;
   }
-  if (k.model == 7 && (k.precision != 0 || !k.s_flag)) {
-    les_set_error("model 7 needs s_flag = 1 and precision 0");
+  if (k.model == 7 && (k.precision == 1 || !k.s_flag)) {
+    les_set_error("model 7 needs s_flag = 1 and precision 0 or 2");
     return LES_ERR_UNSUPPORTED;
   }
   if (k.model != 5 && k.model != 4 && k.model != 3 && k.model != 2 && k.model != 7) {
@@ -386,7 +386,7 @@ int les_ctx_create(const les_config* cfg, les_ctx** out) {
       (st = dalloc(c, (void**)&c->ibet, (size_t)(g.nz + 1) * g.C * sizeof(double))) ||
       (st = dalloc(c, (void**)&c->gamt, (size_t)(g.nz + 1) * g.C * sizeof(double))))
     return fail(st);
-  if (k.precision == 1) {
+  if (k.precision == 1) {  // the mixed form's float-float pressure solve
     c->nlow_cap = 64;
     if ((st = dalloc(c, (void**)&c->ibet_ff, (size_t)(g.nz + 1) * g.C * sizeof(float2))) ||
         (st = dalloc(c, (void**)&c->gamt_ff, (size_t)(g.nz + 1) * g.C * sizeof(float2))) ||
@@ -627,6 +627,13 @@ int les_state_restore(les_ctx* c, const void* host, size_t bytes) {
 
 // output_loop's running statistics (io.f90:211-213) after a step, when
 // les_stats_enable asked for them
+static int run_step(les_ctx* c) {
+  switch (c->cfg.precision) {
+    case 1: return step_mixed(c);
+    case 2: return step_ff(c);
+    default: return step_fp64(c);
+  }
+}
 static void stats_after_step(les_ctx* c) {
   if (c->stats && c->stats_auto && c->cfg.s_flag && c->jt % c->stats_c == 0) op_stats(c);
 }
@@ -635,7 +642,7 @@ int les_step(les_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return LES_ERR_ARG;
   if (!c->surface_set) { les_set_error("les_set_surface must be called before les_step"); return LES_ERR_STATE; }
   for (int i = 0; i < nsteps; ++i) {
-    int st = c->cfg.precision == 1 ? step_mixed(c) : step_fp64(c);
+    int st = run_step(c);
     if (st) return st;
     stats_after_step(c);
   }
@@ -654,7 +661,7 @@ static inline void step_key(const les_ctx* c, int next_jt, int next_total, int* 
   *lag = (next_jt % k.cs_count == 0) ? 1 : 0;
   *ov = ((k.model == 5 || k.model == 6 || k.model == 7) && next_total < 500) ? 1 : 0;
 }
-static int run_step(les_ctx* c) { return c->cfg.precision == 1 ? step_mixed(c) : step_fp64(c); }
+
 
 // capture one step of c on stream `s` (c->stream must be s or joined to it);
 // the host state (counters, RHS buffer exchange) is left as before the step
@@ -1270,10 +1277,10 @@ int les_std_dynamic(les_ctx* c, double* cs_opt2, const double* S11, const double
 }
 // The per-routine module operations below read or write S_ij, Nu_t, tau_ij or
 // the velocity gradients in FP64; on an FP32-mixed context those are held in
-// FP32, so these entries need a precision-0 context.
+// FP32, so these entries need a precision-0 or precision-2 context.
 static int need_fp64(const les_ctx* c, const char* name) {
-  if (c->cfg.precision == 0) return LES_OK;
-  les_set_error("%s: needs a precision-0 context (the mixed form holds S_ij, Nu_t, tau_ij in FP32)", name);
+  if (c->cfg.precision != 1) return LES_OK;
+  les_set_error("%s: needs a precision-0 or -2 context (the mixed form holds S_ij, Nu_t, tau_ij in FP32)", name);
   return LES_ERR_ARG;
 }
 int les_wallstress(les_ctx* c) {

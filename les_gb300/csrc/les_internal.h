@@ -147,6 +147,7 @@ inline float* f32(les_ctx* c, int f) { return reinterpret_cast<float*>(c->f[f]);
 void rhs_swap(les_ctx* c);  // exchange RHSx/RHSx_f, RHSy/.., RHSz/.., RHS_T/RHS_Tf (RHS_q/RHS_qf) buffers
 int step_fp64(les_ctx* c);
 int step_mixed(les_ctx* c);
+int step_ff(les_ctx* c);  // precision 2: FP64 state and arithmetic, float-float transforms
 int op_filt_da(les_ctx* c, double* f, double* dfdx, double* dfdy, int nlev);
 int op_ddxy(les_ctx* c, double* dfdx, double* dfdy, const double* f, int nlev);
 int op_test_filter(les_ctx* c, double* out, const double* in, int nplanes, int which, long pstride);

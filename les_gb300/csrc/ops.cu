@@ -3763,14 +3763,14 @@ __global__ void k_dtheta_spec(const CI* __restrict__ T, const C2* __restrict__ Z
   GSTRIDE(t, (size_t)nk * nz) {
     const int jz = (int)(t / nk) + 1;
     const size_t m = t - (size_t)(jz - 1) * nk;
-    const C2 th = make_double2(T[t].x, T[t].y);
+    const C2 th = to_d2(T[t]);
     const C2 a = ik(th, kx[m]);
     const C2 b = ik(th, ky[m]);
     C2 z;
     if (jz == 1) z = Z1[m];
     else if (jz == nz) z = ZN[m];
     else {
-      z = cscale(csub(th, make_double2(T[t - nk].x, T[t - nk].y)), idz);
+      z = cscale(csub(th, to_d2(T[t - nk])), idz);
       // the spectra are of theta - th0(level): restore the mean gradient
       if (th0 && m == 0) z.x += (th0[jz - 1] - th0[jz - 2]) * idz;
     }
@@ -3997,17 +3997,19 @@ __global__ void k_lag_prod(const double* __restrict__ u, const double* __restric
 // scalar, convective, stress-divergence and SGS terms (the projection path,
 // the Nyquist filtering of u, v, w, rmsdiv and the plane/wall quantities
 // stay FP64).
-template <bool MX> struct PX {
-  typedef typename std::conditional<MX, float, double>::type T;     // transform precision
-  typedef typename CT<T>::type CX;                                   // its complex type
-  typedef T S;                                                       // temporary storage
+template <int M> struct PX {
+  typedef typename std::conditional<M == 1, float,
+                                    typename std::conditional<M == 2, dfloat, double>::type>::type T;  // transforms
+  typedef typename CT<T>::type CX;                                              // their complex type
+  typedef typename std::conditional<M == 1, float, double>::type S;             // temporary storage
 };
 
-template <bool MX>
+template <int M>
 static int lagrangeT(les_ctx* c) {
-  typedef typename PX<MX>::T T;
-  typedef typename PX<MX>::CX CX;
-  typedef typename PX<MX>::S S;
+  constexpr bool MX = M == 1;  // the FP32-mixed form
+  typedef typename PX<M>::T T;
+  typedef typename PX<M>::CX CX;
+  typedef typename PX<M>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   if (MX) op_interpolag32(c);
@@ -4041,14 +4043,14 @@ static int lagrangeT(les_ctx* c) {
     else
       k_lag_spec<CX><<<grid1((size_t)g.C * nl), 256, 0, c->stream>>>(U, V, W, c->wspec, c->wspec + g.C, sp, c->kx,
                                                                   c->ky, (int)g.C, g.nz, jz0, nl, 1.0 / g.dz,
-                                                                  MX ? 1 : 0); LES_COUNT_LAUNCH();
+                                                                  M != 0 ? 1 : 0); LES_COUNT_LAUNCH();
     if constexpr (MX)
       k_lag_prod32<<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sf, prod,
                                                                 g.ld, jz0, nl, g.nplane, U, V, g.C);
     else
       k_lag_prod<S><<<grid1(g.nplane * nl), 256, 0, c->stream>>>(c->f[LES_U], c->f[LES_V], c->f[LES_W], Sp, prod, g.ld,
-                                                              jz0, nl, g.nplane, MX ? U : nullptr, MX ? V : nullptr,
-                                                              g.C); LES_COUNT_LAUNCH();
+                                                              jz0, nl, g.nplane, M != 0 ? U : nullptr,
+                                                              M != 0 ? V : nullptr, g.C); LES_COUNT_LAUNCH();
     const S* in[12];
     for (int q = 0; q < 12; ++q) in[q] = prod + (size_t)q * nl * g.nplane;
     // G_test and G_test_test are cutoffs: only the first ncG (ncGG) kx columns of
@@ -4086,8 +4088,9 @@ static int lagrangeT(les_ctx* c) {
   return 0;
 }
 
-template <bool MX>
+template <int M>
 static int sgs_stagT(les_ctx* c) {
+  constexpr bool MX = M == 1;  // the FP32-mixed form
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const bool lag = (k.model == 4 || k.model == 5 || k.model == 7);
@@ -4116,9 +4119,9 @@ static int sgs_stagT(les_ctx* c) {
     } else if (k.model == 4) {
       op_lagrange_ssim(c, S);
     } else if (k.model == 5) {
-      lagrangeT<MX>(c);
+      lagrangeT<M>(c);
     } else if (k.model == 7) {  // sgs_stag.f90:150-152 (FP64 form only)
-      lagrangeT<MX>(c);
+      lagrangeT<M>(c);
       op_lagrange_scalar(c, S, nullptr);
     }
   }
@@ -4150,9 +4153,9 @@ static int sgs_stagT(les_ctx* c) {
 }
 
 // inverse-only 3/2 padding of full spectra (field stride nz*C) -> big physical
-template <bool MX, typename CIn>
-static void padT(les_ctx* c, const CIn* spec, int nf, typename PX<MX>::S* const* out) {
-  typedef typename PX<MX>::T T;
+template <int M, typename CIn>
+static void padT(les_ctx* c, const CIn* spec, int nf, typename PX<M>::S* const* out) {
+  typedef typename PX<M>::T T;
   const Grid& g = c->g;
   ColJob J = coljob(c, MAP_PAD, DIR_INV, g.nz);
   J.nin = 1; J.nout = 1; J.nf = nf;
@@ -4160,15 +4163,14 @@ static void padT(les_ctx* c, const CIn* spec, int nf, typename PX<MX>::S* const*
   J.out[0] = c->wsB; J.fs_out = (long)g.nz * g.CB;
   J.coef[0][0] = CC_ONE;
   colsT<T, CIn>(c, J);
-  c2rT<T, typename PX<MX>::S>(c, nf, g.nz, c->wsB, out, (long)g.nplane_big, true, g.nx / 2);
+  c2rT<T, typename PX<M>::S>(c, nf, g.nz, c->wsB, out, (long)g.nplane_big, true, g.nx / 2);
 }
-
 // dealias2 of nf big fields (already scaled) into FP64 small fields
-template <bool MX, typename TO = double>
-static void unpadT(les_ctx* c, typename PX<MX>::S* const* in, TO* const* out, int nf, int nlev, double scale) {
-  typedef typename PX<MX>::T T;
-  typedef typename PX<MX>::CX CX;
-  typedef typename PX<MX>::S S;
+template <int M, typename TO = double>
+static void unpadT(les_ctx* c, typename PX<M>::S* const* in, TO* const* out, int nf, int nlev, double scale) {
+  typedef typename PX<M>::T T;
+  typedef typename PX<M>::CX CX;
+  typedef typename PX<M>::S S;
   const Grid& g = c->g;
   double sc[JOB_MAXF];
   for (int i = 0; i < nf; ++i) sc[i] = scale;
@@ -4186,10 +4188,10 @@ static void unpadT(les_ctx* c, typename PX<MX>::S* const* in, TO* const* out, in
 
 // ddx + ddy of two fields summed in spectral space (one inverse); TS: their
 // storage (FP64, or FP32 in the mixed form's scalar flux)
-template <bool MX, typename TS = double>
+template <int M, typename TS = double>
 static void div_xyT(les_ctx* c, const TS* tx, const TS* ty, TS* out, int nlev) {
-  typedef typename PX<MX>::T T;
-  typedef typename PX<MX>::CX CX;
+  typedef typename PX<M>::T T;
+  typedef typename PX<M>::CX CX;
   const Grid& g = c->g;
   const double sc = 1.0 / (double)(g.nx * g.ny);
   const TS* ii[2] = {tx, ty};
@@ -4207,7 +4209,7 @@ static void div_xyT(les_ctx* c, const TS* tx, const TS* ty, TS* out, int nlev) {
 // inverse) into dh (one field) from the filtered u, v.
 static void rmsdiv_mixed(les_ctx* c, double* dh, const double* dwdz, double* out_dev) {
   const Grid& g = c->g;
-  div_xyT<false>(c, c->f[LES_U], c->f[LES_V], dh, g.nz);
+  div_xyT<0>(c, c->f[LES_U], c->f[LES_V], dh, g.nz);
   double* part = c->dred;
   k_rmsdiv_part<<<g.nz - 1, 512, 0, c->stream>>>(dh, nullptr, dwdz, part, g.ld, g.nx, g.ny); LES_COUNT_LAUNCH();
   k_rmsdiv_fin<<<1, 32, 0, c->stream>>>(part, g.nz - 1, (double)(g.nx * g.ny * (g.nz - 1)), out_dev); LES_COUNT_LAUNCH();
@@ -4228,10 +4230,11 @@ int op_rmsdiv_state(les_ctx* c, double* out_dev) {
   return 0;
 }
 
-template <bool MX>
+template <int M>
 static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
-  typedef typename PX<MX>::T T;
-  typedef typename PX<MX>::CX CX;
+  constexpr bool MX = M == 1;  // the FP32-mixed form
+  typedef typename PX<M>::T T;
+  typedef typename PX<M>::CX CX;
   typedef typename std::conditional<MX, float, double>::type TS;  // tau and h storage
   const Grid& g = c->g;
   const double sc = 1.0 / (double)(g.nx * g.ny);
@@ -4239,11 +4242,12 @@ static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
   const int tid[5] = {LES_TXX, LES_TXY, LES_TYY, LES_TXZ, LES_TYZ};
   for (int q = 0; q < 5; ++q) in[q] = reinterpret_cast<const TS*>(c->f[tid[q]]);
   double scs[5] = {sc, sc, sc, sc, sc};
-  // Mixed form: txz, tyz carry the plane-mean shear stress (large near the
-  // wall); their FP32 transforms see tau - plane mean, which the horizontal
-  // derivatives do not see, so the derivatives keep the fluctuation's precision
+  // FP32 and float-float transforms: txz, tyz carry the plane-mean shear
+  // stress (large near the wall); the transforms see tau - plane mean, which
+  // the horizontal derivatives do not see, so the derivatives keep the
+  // fluctuation's precision
   const double* offs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  if (MX) {
+  if (M != 0) {
     const size_t ms = (size_t)g.nz + 8;
     double* m13 = c->dred + 34 * ms;
     double* m23 = c->dred + 35 * ms;
@@ -4282,11 +4286,12 @@ static int divstressT(les_ctx* c, double* divtx, double* divty, double* divtz) {
   return 0;
 }
 
-template <bool MX>
-static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc& d) {
-  typedef typename PX<MX>::T T;
-  typedef typename PX<MX>::CX CX;
-  typedef typename PX<MX>::S S;
+template <int M>
+static int scalarT(les_ctx* c, typename PX<M>::S* const* bigf, const ScalarDesc& d) {
+  constexpr bool MX = M == 1;  // the FP32-mixed form
+  typedef typename PX<M>::T T;
+  typedef typename PX<M>::CX CX;
+  typedef typename PX<M>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   const int nz = g.nz;
@@ -4294,11 +4299,12 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
   // the scalar's spectrum (precision of the transform) in the fourth saved
   // spectrum slot: theta's, then (qmix after theta) the humidity's
   CX* specT = reinterpret_cast<CX*>(c->spec + 3 * FS);
-  // FP32 transforms see theta - th0(level) (th0 = plane mean): the filter and
-  // the horizontal derivatives are unchanged by a per-level constant, and the
-  // perturbation keeps its precision; th0 is added back in FP64
-  double* th0 = MX ? c->dred + d.mean_slot * (size_t)(nz + 8) : nullptr;
-  if (MX) {
+  // FP32 and float-float transforms see theta - th0(level) (th0 = plane
+  // mean): the filter and the horizontal derivatives are unchanged by a
+  // per-level constant, and the perturbation keeps its precision; th0 is added
+  // back in FP64
+  double* th0 = M != 0 ? c->dred + d.mean_slot * (size_t)(nz + 8) : nullptr;
+  if (M != 0) {
     plane_sums(c, c->f[d.s], (long)g.nplane, nz, 4, (double)(g.nx * g.ny), th0);
   }
   {  // filt_da(theta) with the spectrum saved
@@ -4347,7 +4353,7 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
                                                          th0); LES_COUNT_LAUNCH();
   {
     S* o3[3] = {bigf[3], bigf[4], bigf[5]};
-    padT<MX, CX>(c, ds, 3, o3);
+    padT<M, CX>(c, ds, 3, o3);
   }
   k_scalar_prod<S><<<grid1(g.nfield_big), 256, 0, c->stream>>>(bigf[0], bigf[1], bigf[2], bigf[3], bigf[4], bigf[5],
                                                               bigf[6], g.ld_big, g.nx2, g.ny2, nz,
@@ -4363,12 +4369,12 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
     {
       S* b6[1] = {bigf[6]};
       float* o[1] = {rtf};
-      unpadT<MX, float>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+      unpadT<M, float>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
     }
     const dim3 gpl((unsigned)((g.nplane + 255) / 256), (unsigned)nz);
     k_scalar_temp_xy32<<<gpl, 256, 0, c->stream>>>(f32(c, LES_NU_T), f32(c, d.dsdx), f32(c, d.dsdy), tx, ty,
                                                    g.ld, g.nx, g.ny, nz, (float)(1.0 / k.pr)); LES_COUNT_LAUNCH();
-    div_xyT<MX, float>(c, tx, ty, dxy, nz);
+    div_xyT<M, float>(c, tx, ty, dxy, nz);
     k_scalar_rhs32<<<dim3(gpl.x, (unsigned)(nz - 1)), 256, 0, c->stream>>>(
         c->f[d.rhs], rtf, dxy, f32(c, LES_NU_T), c->f[d.dsdz], c->f[d.sgs3], g.ld, g.nx, g.ny,
         (float)(1.0 / k.pr), (float)(1.0 / g.dz)); LES_COUNT_LAUNCH();
@@ -4377,7 +4383,7 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
     {
       S* b6[1] = {bigf[6]};
       double* o[1] = {rt};
-      unpadT<MX>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
+      unpadT<M>(c, b6, o, 1, nz, 1.0 / (double)(g.nx2 * g.ny2));
     }
     double* tx = c->tmp;
     double* ty = c->tmp + g.nfield;
@@ -4385,7 +4391,7 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
     k_scalar_temp_xy<double><<<grid1(g.nfield), 256, 0, c->stream>>>(c->f[LES_NU_T], c->f[d.dsdx],
                                                                     c->f[d.dsdy], tx, ty, g.ld, g.nx, g.ny, nz,
                                                                     k.pr, c->f[LES_PR_T]); LES_COUNT_LAUNCH();
-    div_xyT<MX>(c, tx, ty, dxy, nz);
+    div_xyT<M>(c, tx, ty, dxy, nz);
     k_scalar_rhs<double><<<grid1(g.nplane * (nz - 1)), 256, 0, c->stream>>>(rt, dxy, c->f[LES_NU_T],
                                                                            c->f[d.dsdz], c->f[d.sgs3],
                                                                            g.ld, g.nx, g.ny, nz, k.pr, c->f[LES_PR_T],
@@ -4403,10 +4409,11 @@ static int scalarT(les_ctx* c, typename PX<MX>::S* const* bigf, const ScalarDesc
   return 0;
 }
 
-template <bool MX>
-static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, double* cy, double* cz) {
-  typedef typename PX<MX>::CX CX;
-  typedef typename PX<MX>::S S;
+template <int M>
+static int convecT(les_ctx* c, typename PX<M>::S* const* bigf, double* cx, double* cy, double* cz) {
+  constexpr bool MX = M == 1;  // the FP32-mixed form
+  typedef typename PX<M>::CX CX;
+  typedef typename PX<M>::S S;
   const Grid& g = c->g;
   const size_t FS = (size_t)g.nz * g.C;
   CX* vs = (CX*)c->wsA;
@@ -4420,7 +4427,7 @@ static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, doub
                                                    1.0 / g.dz); LES_COUNT_LAUNCH();
   {
     S* o3[3] = {bigf[3], bigf[4], bigf[5]};
-    padT<MX, CX>(c, vs, 3, o3);
+    padT<M, CX>(c, vs, 3, o3);
   }
   const S cst2 = (S)(1.0 / (double)(g.nx2 * g.ny2));
   k_convec_prod<S><<<grid1(g.nplane_big * (g.nz - 1)), 256, 0, c->stream>>>(
@@ -4429,7 +4436,7 @@ static int convecT(les_ctx* c, typename PX<MX>::S* const* bigf, double* cx, doub
   {
     S* bins[3] = {bigf[6], bigf[7], bigf[8]};
     double* outs[3] = {cx, cy, cz};
-    unpadT<MX>(c, bins, outs, 3, g.nz - 1, 1.0);
+    unpadT<M>(c, bins, outs, 3, g.nz - 1, 1.0);
   }
   const size_t top = (size_t)(g.nz - 1) * g.nplane;
   fill(c, cx + top, g.nplane, LES_BOGUS);
@@ -4494,6 +4501,57 @@ __global__ void k_zero_mean_modes(C2* spec, size_t fs, size_t nk, int nz) {
   spec[(size_t)f * fs + (size_t)lev * nk] = make_double2(0.0, 0.0);
 }
 
+// float-float spectra of f - plane mean widened to FP64 in place (hi + lo,
+// exact), the plane mean put back into each level's (0,0) mode
+__global__ void k_widen_dc(C2* p, size_t n, size_t nk, int nz, const double* __restrict__ mean, int ms) {
+  GSTRIDE(i, n) {
+    const dcomplex v = reinterpret_cast<const dcomplex*>(p)[i];
+    double2 w = to_d2(v);
+    const size_t pl = i / nk;
+    if (i - pl * nk == 0) {
+      const int f = (int)(pl / (size_t)nz), lev = (int)(pl - (size_t)f * nz);
+      w.x += mean[(size_t)f * ms + lev];
+    }
+    p[i] = w;
+  }
+}
+// filt_da of u, v, w in float-float transforms (FP64 state in and out), the
+// Nyquist-filtered spectra F(f/(nx ny)) saved in FP64 like filt_da_multi_spec.
+// The transforms see f - plane mean: a float-float rounding is relative to
+// the values transformed, and u's mean is a hundred times v's and w's
+// fluctuations; the mean is added back in FP64.
+static int filt_da_uvw_ff(les_ctx* c) {
+  const Grid& g = c->g;
+  const int nz = g.nz;
+  const int ms = nz + 8;
+  const long FS = (long)nz * g.C;
+  double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
+  double* mean = c->dred + 16 * (size_t)ms;  // slots 16..18
+  for (int q = 0; q < 3; ++q) plane_sums(c, f3[q], (long)g.nplane, nz, 4, (double)(g.nx * g.ny), mean + q * ms);
+  const double sc = 1.0 / (double)(g.nx * g.ny);
+  const double* in[3] = {f3[0], f3[1], f3[2]};
+  const double scs[3] = {sc, sc, sc};
+  const double* offs[3] = {mean, mean + ms, mean + 2 * ms};
+  r2cT<dfloat, double>(c, 3, nz, in, (long)g.nplane, scs, nullptr, c->wsA, false, g.lh, offs);
+  ColJob J = coljob(c, MAP_SAME, DIR_BOTH, nz);
+  J.nin = 1; J.nout = 4; J.nf = 3; J.inv_mask = 7u;  // output 3 (the spectrum) stays spectral
+  J.in[0] = c->wsA; J.fs_in = FS;
+  J.out[0] = c->wsB;
+  J.out[1] = (dcomplex*)c->wsB + 3 * FS;
+  J.out[2] = (dcomplex*)c->wsB + 6 * FS;
+  J.out[3] = reinterpret_cast<dcomplex*>(c->spec);
+  J.fs_out = FS;
+  J.coef[0][0] = CC_KILL; J.coef[1][0] = CC_IKX; J.coef[2][0] = CC_IKY; J.coef[3][0] = CC_KILL;
+  colsT<dfloat, dcomplex>(c, J);
+  k_widen_dc<<<grid1(3 * (size_t)FS), 256, 0, c->stream>>>(c->spec, 3 * (size_t)FS, g.C, nz, mean, ms);
+  LES_COUNT_LAUNCH();
+  double* o9[9] = {f3[0], f3[1], f3[2], c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX],
+                   c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
+  const double* offo[9] = {mean, mean + ms, mean + 2 * ms, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  c2rT<dfloat, double>(c, 9, nz, c->wsB, o9, (long)g.nplane, false, g.lh, offo);
+  return 0;
+}
+
 // main.f90:202-478, one iteration on the device-resident state
 void rhs_swap(les_ctx* c) {
   std::swap(c->f[LES_RHSX], c->f[LES_RHSX_F]);
@@ -4504,9 +4562,10 @@ void rhs_swap(les_ctx* c) {
   c->rhs_par ^= 1;
 }
 
-template <bool MX>
+template <int M>
 static int stepT(les_ctx* c) {
-  typedef typename PX<MX>::S S;
+  constexpr bool MX = M == 1;  // the FP32-mixed form
+  typedef typename PX<M>::S S;
   const Grid& g = c->g;
   const les_config& k = c->cfg;
   c->jt += 1;
@@ -4519,7 +4578,9 @@ static int stepT(les_ctx* c) {
   const double* uv1 = c->tmp + (size_t)(c->ntmp - 2) * g.nplane;
   surface_uv_filtered(c, const_cast<double*>(uv1));
   op_obukhov(c, uv1);
-  if (!MX) {
+  if (M == 2) {
+    filt_da_uvw_ff(c);
+  } else if (!MX) {
     double* f3[3] = {c->f[LES_U], c->f[LES_V], c->f[LES_W]};
     double* x3[3] = {c->f[LES_DUDX], c->f[LES_DVDX], c->f[LES_DWDX]};
     double* y3[3] = {c->f[LES_DUDY], c->f[LES_DVDY], c->f[LES_DWDY]};
@@ -4540,22 +4601,22 @@ static int stepT(les_ctx* c) {
     const double sc[2] = {cs, cs};
     plane_spectra(c, 2, pl, sc, c->wspec);
   }
-  sgs_stagT<MX>(c);
+  sgs_stagT<M>(c);
   S* bigf[9];
   for (int q = 0; q < 9; ++q) bigf[q] = reinterpret_cast<S*>(c->big) + (size_t)q * g.nfield_big;
   if (MX) {  // the mixed form pads u', v' (its linear terms use the plane means)
     k_zero_mean_modes<<<(2 * g.nz + 127) / 128, 128, 0, c->stream>>>(c->spec, (size_t)g.nz * g.C, g.C, g.nz);
     LES_COUNT_LAUNCH();
   }
-  padT<MX, C2>(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
+  padT<M, C2>(c, c->spec, 3, bigf);  // padded u, v, w (convec.f90:45-65)
   if (k.s_flag) {
-    scalarT<MX>(c, bigf, theta_desc(c));
-    if (k.q_flag) scalarT<MX>(c, bigf, q_desc(c));  // main.f90:273-274
+    scalarT<M>(c, bigf, theta_desc(c));
+    if (k.q_flag) scalarT<M>(c, bigf, q_desc(c));  // main.f90:273-274
   } else {
     fill(c, c->f[LES_BETA_SCAL], g.nfield, 0.0);
   }
-  divstressT<MX>(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
-  convecT<MX>(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
+  divstressT<M>(c, c->f[LES_DIVTX], c->f[LES_DIVTY], c->f[LES_DIVTZ]);
+  convecT<M>(c, bigf, c->f[LES_RHSX], c->f[LES_RHSY], c->f[LES_RHSZ]);
   const size_t nv = g.nplane * (g.nz - 1);
   const int euler = (c->jt == 1 && !k.initu) ? 1 : 0;
   if (MX) {
@@ -4582,6 +4643,9 @@ static int stepT(les_ctx* c) {
         ff2(c, LES_RHSZ), c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY], c->f[LES_DPDZ], g.ld, g.nx, g.ny, g.nz,
         1.0 / g.dz, k.dt);
   } else {
+    // FP64 projection in the FP64 form and in the float-float transform form:
+    // float-float transforms of the predictor would leave its rounding times
+    // the wavenumber in the divergence (rmsdiv 4e-12 instead of 1e-13 at 128^3)
     pressT<double>(c, c->f[LES_P], c->f[LES_DPDX], c->f[LES_DPDY]);
   }
   if (!MX)
@@ -4634,7 +4698,8 @@ void autotune_probe(les_ctx* c, int fp32) {
   else tune_probe<double>(c);
 }
 
-int step_fp64(les_ctx* c) { return stepT<false>(c); }
-int step_mixed(les_ctx* c) { return stepT<true>(c); }
+int step_fp64(les_ctx* c) { return stepT<0>(c); }
+int step_mixed(les_ctx* c) { return stepT<1>(c); }
+int step_ff(les_ctx* c) { return stepT<2>(c); }
 
 }  // namespace les

@@ -39,9 +39,10 @@ MIXED_FP32_UNITS = sum(r[2] for r in ROUTINES) * _SCALE
 
 
 def bytes_per_point(form, theta=True):
-    """Algorithmic bytes per grid point per step ("fp64" or "mixed")."""
+    """Algorithmic bytes per grid point per step ("fp64", "ff" or "mixed";
+    the float-float transform form stores every array in 8 bytes like FP64)."""
     units = VELOCITY_UNITS + (THETA_UNITS if theta else 0.0)
-    if form == "fp64":
+    if form in ("fp64", "ff"):
         return 8.0 * units
     f32 = MIXED_FP32_UNITS + (THETA_FP32_UNITS if theta else 0.0)
     return 8.0 * (units - f32) + 4.0 * f32
