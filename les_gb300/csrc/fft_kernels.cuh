@@ -280,17 +280,15 @@ __global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
   constexpr int M = N1 * N2, TT = N1 > N2 ? N1 : N2, RPB = NT / TT, MS = N2 * (N1 + 1);
   extern __shared__ __align__(16) unsigned char smraw[];
   C* S = reinterpret_cast<C*>(smraw);  // RPB rows x MS
-  C* tw = S + RPB * MS;                // exp(-2 pi i j / M), j < M
-  C* wr = tw + M;                      // exp(-2 pi i k / nx), k <= M
-  for (int t = threadIdx.x; t < M; t += NT) tw[t] = UnitSel<T>::get(P.c, t);
-  for (int t = threadIdx.x; t <= M; t += NT) wr[t] = rw<T>(P, t);
+  // twiddles exp(-2 pi i j / M) and exp(-2 pi i k / nx) straight from their
+  // (cached) global tables: a block issues its row loads without first
+  // waiting for a table fill and a barrier
   const int q = threadIdx.x % TT, r = threadIdx.x / TT;
   const int f = blockIdx.z, lev = blockIdx.y;
   const int row = blockIdx.x * RPB + r;
   const bool rowok = r < RPB && row < J.ny;
   C* Sr = S + (r < RPB ? r : 0) * MS;
   C v[TT];
-  __syncthreads();  // tables
   if (q < N1) {
     const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work +
                   (size_t)(rowok ? row : 0) * J.wc;
@@ -306,12 +304,12 @@ __global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
       if (k == 0) { a.y = (T)0; bb.y = (T)0; }  // the halfcomplex pass ignores Im of X[0], X[M]
       const C b = cconj(bb);
       const C e = cadd(a, b);
-      const C d = cmul(csub(a, b), cconj(wr[k]));  // x exp(+2 pi i k / nx)
+      const C d = cmul(csub(a, b), cconj(rw<T>(P, k)));  // x exp(+2 pi i k / nx)
       v[i] = cadd(e, cmuli(d));
     }
     dft_n<T, N2>(v, +1);  // over k2: v[i] = y[k1 = q][n2 = i]
 #pragma unroll
-    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(tw[q * i]));
+    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(UnitSel<T>::get(P.c, q * i)));
     if (r < RPB) {
 #pragma unroll
       for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + q] = v[i];
@@ -445,17 +443,15 @@ __global__ void __launch_bounds__(NT) k_r2c_reg2(RowJob J, RealPlanDev P) {
 }
 
 template <typename T, typename TOut, int N1, int N2, int TT, int NT>
-__global__ void __launch_bounds__(NT) k_c2r_reg2(RowJob J, RealPlanDev P) {
+__global__ void __launch_bounds__(NT, 5) k_c2r_reg2(RowJob J, RealPlanDev P) {
   typedef typename CT<T>::type C;
   typedef typename CT<TOut>::type CO;
   static_assert(N1 % TT == 0 && N2 % TT == 0 && NT % TT == 0, "thread split");
   constexpr int M = N1 * N2, RPB = NT / TT, MS = N2 * (N1 + 1), J1 = N1 / TT, J2 = N2 / TT;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* S = reinterpret_cast<C*>(smraw);  // RPB rows x MS
-  C* tw = S + RPB * MS;                // exp(-2 pi i j / M), j < M
-  C* wr = tw + M;                      // exp(-2 pi i k / nx), k <= M
-  for (int t = threadIdx.x; t < M; t += NT) tw[t] = UnitSel<T>::get(P.c, t);
-  for (int t = threadIdx.x; t <= M; t += NT) wr[t] = rw<T>(P, t);
+  // twiddles from their cached global tables (no table fill and barrier
+  // ahead of the row loads)
   const int q = threadIdx.x % TT, r = threadIdx.x / TT;
   const int f = blockIdx.z, lev = blockIdx.y;
   const int row = blockIdx.x * RPB + r;
@@ -464,7 +460,6 @@ __global__ void __launch_bounds__(NT) k_c2r_reg2(RowJob J, RealPlanDev P) {
   const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work +
                 (size_t)(rowok ? row : 0) * J.wc;
   const int nc = J.ncols;
-  __syncthreads();  // tables
 #pragma unroll
   for (int j = 0; j < J1; ++j) {
     const int k1 = q + TT * j;
@@ -480,12 +475,12 @@ __global__ void __launch_bounds__(NT) k_c2r_reg2(RowJob J, RealPlanDev P) {
       if (k == 0) { a.y = (T)0; bb.y = (T)0; }  // the halfcomplex pass ignores Im of X[0], X[M]
       const C b = cconj(bb);
       const C e = cadd(a, b);
-      const C d = cmul(csub(a, b), cconj(wr[k]));  // x exp(+2 pi i k / nx)
+      const C d = cmul(csub(a, b), cconj(rw<T>(P, k)));  // x exp(+2 pi i k / nx)
       v[i] = cadd(e, cmuli(d));
     }
     dft_n<T, N2>(v, +1);  // over k2: v[i] = y[k1][n2 = i]
 #pragma unroll
-    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(tw[k1 * i]));
+    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(UnitSel<T>::get(P.c, k1 * i)));
 #pragma unroll
     for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + k1] = v[i];
   }
