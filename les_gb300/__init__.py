@@ -54,8 +54,12 @@ def lib():
         L.les_field_elems.restype = ctypes.c_size_t
         L.les_field_elems.argtypes = [vp, ip]
         for name in ["les_ctx_destroy", "les_step", "les_set_field", "les_get_field",
-                     "les_set_surface", "les_rmsdiv", "les_ctx_set_pointer_mode"]:
+                     "les_set_surface", "les_rmsdiv", "les_ctx_set_pointer_mode", "les_register_field",
+                     "les_sync_from_host", "les_sync_to_host"]:
             getattr(L, name).restype = ip
+        L.les_register_field.argtypes = [vp, ip, dp]
+        L.les_sync_from_host.argtypes = [vp]
+        L.les_sync_to_host.argtypes = [vp]
         L.les_ctx_destroy.argtypes = [vp]
         L.les_step.argtypes = [vp, ip]
         L.les_set_field.argtypes = [vp, ip, dp]

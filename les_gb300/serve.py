@@ -107,10 +107,17 @@ class Scheduler:
     points of all steps in flight stay within it (at least one step always
     runs), oldest-served request first: every step then shares the device
     with a bounded amount of other work, which bounds the spread of its
-    latency at some cost in overlap."""
+    latency at some cost in overlap.
+
+    With max_active_points set, a pending request becomes active (a slot)
+    only while the grid points of the active requests stay within it (one is
+    always admitted when none is active), in arrival order: under overload
+    the requests queue before they start instead of all stretching each
+    other's steps, so the work of one round of steps, and with it the step
+    latency, stays near the cap."""
 
     def __init__(self, executor, budget_bytes, max_inflight_per_member=1, clock=time.perf_counter,
-                 max_inflight_points=None):
+                 max_inflight_points=None, max_active_points=None):
         self.ex = executor
         self.budget = budget_bytes
         self.used = 0
@@ -123,6 +130,8 @@ class Scheduler:
         self.max_inflight = max_inflight_per_member
         self.max_points = max_inflight_points
         self.inflight_points = 0
+        self.max_active = max_active_points
+        self.active_points = 0
         self.tick_no = 0
         self.done = []
 
@@ -181,7 +190,13 @@ class Scheduler:
             req = self.pending.popleft()
             if req.status == "rejected":
                 continue
+            pts = req.size[0] * req.size[1] * req.size[2]
+            if (self.max_active is not None and self.active and
+                    (waiting or self.active_points + pts > self.max_active)):
+                waiting.append(req)  # no slot: wait, in arrival order
+                continue
             if self._admit_member(req):
+                self.active_points += pts
                 req.status = "active"
                 req.started = now
                 self.busy[req.member] += 1
@@ -231,6 +246,7 @@ class Scheduler:
         for req in self.active:
             if req.status == "failed":
                 self.busy[req.member] -= 1
+                self.active_points -= req.size[0] * req.size[1] * req.size[2]
                 self.done.append(req)
             elif req.inflight == 0 and (req.done_steps >= req.nsteps or req.status == "cancelled"):
                 req.finished = self.clock()
@@ -239,6 +255,7 @@ class Scheduler:
                     t_arr = req.arrival_wall if req.arrival_wall is not None else req.started
                     self.metrics.req_lat.append(req.finished - t_arr)
                 self.busy[req.member] -= 1
+                self.active_points -= req.size[0] * req.size[1] * req.size[2]
                 self.done.append(req)
             else:
                 still.append(req)
@@ -293,6 +310,7 @@ class FakeExecutor:
         self.inflight = []
         self.loaded = {}
         self.steps = collections.Counter()
+        self.stream_end = {}  # member -> end time of its last queued step (one stream per member)
 
     def footprint(self, size):
         nx, ny, nz = size
@@ -313,7 +331,8 @@ class FakeExecutor:
             req.error = "non-finite state detected"
             return
         dur = self.ns * 1e-9 * nx * ny * nz
-        start = t if req.prev_done is None else max(t, req.prev_done)  # after the request's previous step
+        start = max(t, self.stream_end.get(req.member, t))  # behind the member's queued steps
+        self.stream_end[req.member] = start + dur
         self.inflight.append((req, start, start + dur, nx * ny * nz, False))
         self.steps[req.member] += 1
 
@@ -352,6 +371,28 @@ class GpuExecutor:
         self.spilled = {}      # member -> pinned host image of its whole state
         self.spills = 0
         self.restores = 0
+        self.prepared = {}     # member -> (surface, initial state), made before serving
+
+    def prepare(self, trace):
+        """Work that is not the server's, done before the trace starts: each
+        member's seeded surface and initial state (what a client would send
+        with its first request), and one tuning of the launch shapes per grid
+        size (the server's start-up; every later context of that size reuses
+        the process-wide table)."""
+        lg = self.lg
+        for req in trace:
+            if req.member in self.prepared:
+                continue
+            cfg = self.config(req.size)
+            surf = lg.patch_surface(cfg, self.seed0 + req.member)
+            surf.wt_s[:] = 0.05
+            self.prepared[req.member] = (surf, lg.initial_state(cfg, surf, seed=self.seed0 + req.member))
+        if self.autotune:
+            for size in sorted({r.size for r in trace}):
+                cfg = self.config(size)
+                ctx = lg.Context(cfg, lg.patch_surface(cfg, 0))
+                ctx.autotune()
+                ctx.close()
 
     def config(self, size):
         nx, ny, nz = size
@@ -364,8 +405,13 @@ class GpuExecutor:
     def load(self, member, size):
         lg = self.lg
         cfg = self.config(size)
-        surf = lg.patch_surface(cfg, self.seed0 + member)
-        surf.wt_s[:] = 0.05
+        prep = self.prepared.get(member)
+        if prep is None:
+            surf = lg.patch_surface(cfg, self.seed0 + member)
+            surf.wt_s[:] = 0.05
+            state = None
+        else:
+            surf, state = prep
         try:
             ctx = lg.Context(cfg, surf)
         except lg.LesError as e:
@@ -377,7 +423,9 @@ class GpuExecutor:
             ctx.state_restore(img)
             self.restores += 1
         else:
-            for k, v in lg.initial_state(cfg, surf, seed=self.seed0 + member).items():
+            if state is None:
+                state = lg.initial_state(cfg, surf, seed=self.seed0 + member)
+            for k, v in state.items():
                 ctx.set(k, v)
         if self.autotune:
             ctx.autotune()

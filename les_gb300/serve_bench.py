@@ -2,7 +2,10 @@
 requests (N ~ U{1..50}) over a pool of 64 members with sizes drawn from
 {32^3, 64^3, 96^2x64, 128^3, 192^2x128} (weights 0.3/0.3/0.2/0.15/0.05),
 FP32-mixed steps replayed from CUDA graphs, admission by estimated footprint
-against free device memory.  Reports p50/p99 step and request latency and
+against free device memory.  Before the trace starts the members' seeded
+surfaces and initial states are generated (the client's side of a request)
+and the launch shapes are tuned once per grid size (the server's start-up);
+admitting a member is then its allocation, upload and graph capture.  Reports p50/p99 step and request latency and
 aggregate pt-steps/s, beside an unbatched FP64 baseline (the same requests
 served one at a time, eager FP64 steps).
 
@@ -14,7 +17,7 @@ import time
 
 
 def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60, priorities=False,
-          max_inflight_points=None):
+          max_inflight_points=None, steps_in_flight=1, max_active_points=None):
     """Serve one Poisson trace; returns the summary (and, when
     baseline_requests > 0, the unbatched FP64 baseline on its prefix)."""
     import torch
@@ -23,7 +26,9 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
     budget = int(budget_gb * 2 ** 30) if budget_gb > 0 else int(0.9 * free)
     trace = poisson_trace(requests, rate, seed)
     ex = GpuExecutor(precision=1, autotune=True, priorities=priorities)
-    sched = Scheduler(ex, budget_bytes=budget, max_inflight_points=max_inflight_points)
+    ex.prepare(trace)  # members' seeded states and the per-size tuning, before the clock starts
+    sched = Scheduler(ex, budget_bytes=budget, max_inflight_per_member=steps_in_flight,
+                      max_inflight_points=max_inflight_points, max_active_points=max_active_points)
     summary, wall = sched.run(trace)
     status = {}
     for r in sched.done:
@@ -31,7 +36,9 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
     for m in list(ex.ctx):
         ex.evict(m)
     out = {"requests": len(trace), "rate_per_s": rate, "priorities": priorities,
-           "max_inflight_points": max_inflight_points, "wall_s": wall, "status": status,
+           "max_inflight_points": max_inflight_points, "steps_in_flight": steps_in_flight,
+           "max_active_points": max_active_points,
+           "wall_s": wall, "status": status,
            "budget_gb": budget / 2 ** 30, "serving": summary}
     if summary.get("step_p50_ms"):
         out["step_p99_over_p50"] = summary["step_p99_ms"] / summary["step_p50_ms"]
@@ -68,10 +75,16 @@ def main():
     ap.add_argument("--priorities", action="store_true", help="more urgent streams for larger members")
     ap.add_argument("--max-inflight-points", type=float, default=0.0,
                     help="grid points of all steps in flight at once (0: no limit)")
+    ap.add_argument("--steps-in-flight", type=int, default=1,
+                    help="steps of one request queued on its member's stream at once")
+    ap.add_argument("--max-active-points", type=float, default=0.0,
+                    help="grid points of the active requests (slots; 0: no limit)")
     args = ap.parse_args()
     mip = int(args.max_inflight_points) if args.max_inflight_points > 0 else None
+    map_ = int(args.max_active_points) if args.max_active_points > 0 else None
     print(json.dumps(serve(args.requests, args.rate, args.seed, args.budget_gb, args.baseline_requests,
-                           priorities=args.priorities, max_inflight_points=mip)))
+                           priorities=args.priorities, max_inflight_points=mip,
+                           steps_in_flight=args.steps_in_flight, max_active_points=map_)))
 
 
 if __name__ == "__main__":

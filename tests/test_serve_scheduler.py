@@ -141,3 +141,45 @@ def test_step_latency_counts_the_wait_between_steps():
     drain(s)
     assert len(s.metrics.step_lat) == 3 and len(s.metrics.step_dev) == 3
     assert all(g >= d - 1e-15 for g, d in zip(s.metrics.step_lat, s.metrics.step_dev))
+
+
+def test_two_steps_in_flight_per_request():
+    """With two steps of a request queued on its member's stream at once the
+    host's poll-and-relaunch no longer sits between them; the steps still
+    run in order, one stream per member, and every step is counted once."""
+    ex = FakeExecutor(ns_per_pt=1.0)
+    s = Scheduler(ex, budget_bytes=10 ** 12, max_inflight_per_member=2)
+    s.submit(R(0, 0, n=5))
+    s.submit(R(1, 1, n=1))
+    s.tick(0.0)
+    s.tick(0.0)
+    reqs = {r.rid: r for r in s.active}
+    assert reqs[0].inflight == 2 and reqs[1].inflight == 1
+    ends = [b for (r, a, b, p, f) in ex.inflight if r.rid == 0]
+    starts = [a for (r, a, b, p, f) in ex.inflight if r.rid == 0]
+    assert starts[1] >= ends[0]                     # queued behind the first on the stream
+    drain(s)
+    assert ex.steps[0] == 5 and ex.steps[1] == 1
+    assert len(s.metrics.step_lat) == 6
+    assert all(r.status == "done" for r in s.done)
+
+
+def test_active_slots_queue_requests_in_arrival_order():
+    """With an active-points cap, pending requests start only as slots free
+    up, in arrival order; the first one always starts; all complete."""
+    ex = FakeExecutor()
+    pts = 32 * 32 * 32
+    s = Scheduler(ex, budget_bytes=10 ** 12, max_active_points=2 * pts)
+    for i in range(5):
+        s.submit(R(i, member=i, n=2))
+    s.tick(0.0)
+    assert sorted(r.rid for r in s.active) == [0, 1]
+    assert [r.rid for r in s.pending] == [2, 3, 4]
+    assert s.active_points == 2 * pts
+    drain(s)
+    assert all(r.status == "done" for r in s.done) and len(s.done) == 5
+    assert s.active_points == 0
+    big = Scheduler(FakeExecutor(), budget_bytes=10 ** 12, max_active_points=1)
+    big.submit(R(0, 0, n=1, size=(64, 64, 64)))   # larger than the cap: starts when nothing runs
+    big.tick(0.0)
+    assert len(big.active) == 1
