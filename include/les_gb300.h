@@ -259,6 +259,12 @@ int les_step(les_ctx* ctx, int nsteps);
  * (dynamic-model step or not, Cs^2 override on or off).  No counterpart in the
  * reference (its time loop is main.f90:202-509). */
 int les_step_graph(les_ctx* ctx, int nsteps);
+/* Captures and instantiates the graphs les_step_graph will replay for the
+ * next steps of both kinds (with and without the dynamic-model update) and
+ * both RHS buffer parities, without running a step (counters and state are
+ * unchanged), so a serving loop does not capture on its own path.  No
+ * counterpart in the reference. */
+int les_step_graph_prepare(les_ctx* ctx);
 /* Times candidate launch shapes of the plane-transform kernels for this grid
  * size (kx columns per CTA of the y pass, rows per CTA of the x pass) and
  * keeps the fastest; results are cached per grid size for the process.

@@ -161,6 +161,14 @@ class Context:
         """Advance n steps replaying captured CUDA graphs (les_step_graph)."""
         check(self.L.les_step_graph(self.h, int(n)))
 
+    def graph_prepare(self):
+        """Capture the step graphs step_graph will replay, without stepping
+        (les_step_graph_prepare)."""
+        f = self.L.les_step_graph_prepare
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p]
+        check(f(self.h))
+
     def autotune(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(self.L.les_autotune(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))

@@ -709,6 +709,45 @@ int les_step_graph(les_ctx* c, int nsteps) {
   return LES_OK;
 }
 
+// Capture and instantiate the step graphs that les_step_graph replays for the
+// next non-special steps of both kinds (with and without the Lagrangian
+// update) and both RHS buffer parities, without running a step: a serving
+// loop moves the capture cost off its path.  Counters and buffers are left as
+// they were.
+int les_step_graph_prepare(les_ctx* c) {
+  if (!c) return LES_ERR_ARG;
+  if (!c->surface_set) { les_set_error("les_set_surface must be called before les_step_graph_prepare"); return LES_ERR_STATE; }
+  const int jt0 = c->jt, jtt0 = c->jt_total, par0 = c->rhs_par;
+  int st = LES_OK;
+  for (int want = 0; want < 2 && st == LES_OK; ++want) {
+    int nj = jt0 + 1, found = 0;
+    for (int k = 0; k < 4 * c->cfg.cs_count + 8; ++k, ++nj) {
+      int lag, ov;
+      step_key(c, nj, jtt0 + (nj - jt0), &lag, &ov);
+      if (lag == want && !special_step(c, nj)) { found = 1; break; }
+    }
+    if (!found) continue;  // every step of this kind runs eagerly
+    for (int par = 0; par < 2 && st == LES_OK; ++par) {
+      c->jt = nj - 1;
+      c->jt_total = jtt0 + (nj - jt0) - 1;
+      if (c->rhs_par != par) rhs_swap(c);
+      int lag, ov;
+      step_key(c, nj, c->jt_total + 1, &lag, &ov);
+      if (c->gexec[lag][ov][par]) continue;
+      cudaGraph_t gr;
+      st = capture_step(c, &gr);
+      if (st) break;
+      cudaError_t e = cudaGraphInstantiate(&c->gexec[lag][ov][par], gr, 0);
+      cudaGraphDestroy(gr);
+      if (e != cudaSuccess) { les_set_error("instantiate: %s", cudaGetErrorString(e)); st = LES_ERR_CUDA; }
+    }
+  }
+  c->jt = jt0;
+  c->jt_total = jtt0;
+  if (c->rhs_par != par0) rhs_swap(c);
+  return st;
+}
+
 // process-wide cache of tuned launch shapes per (grid, precision)
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> g_tune;

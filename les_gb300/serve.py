@@ -114,10 +114,18 @@ class Scheduler:
     always admitted when none is active), in arrival order: under overload
     the requests queue before they start instead of all stretching each
     other's steps, so the work of one round of steps, and with it the step
-    latency, stays near the cap."""
+    latency, stays near the cap.  max_active_ms caps instead the sum of the
+    active requests' step times as the executor estimates them
+    (executor.step_ms(size)); small members' steps are launch-bound, so
+    equal points are not equal time.
+
+    With rounds set, the active requests step in lock-step rounds: a tick
+    launches only when every step of the previous round has completed, so
+    every request of a round sees the same latency whatever its member's
+    size (small members do not run ahead of large ones)."""
 
     def __init__(self, executor, budget_bytes, max_inflight_per_member=1, clock=time.perf_counter,
-                 max_inflight_points=None, max_active_points=None):
+                 max_inflight_points=None, max_active_points=None, max_active_ms=None, rounds=False):
         self.ex = executor
         self.budget = budget_bytes
         self.used = 0
@@ -132,6 +140,9 @@ class Scheduler:
         self.inflight_points = 0
         self.max_active = max_active_points
         self.active_points = 0
+        self.max_active_ms = max_active_ms
+        self.active_ms = 0.0
+        self.rounds = rounds
         self.tick_no = 0
         self.done = []
 
@@ -191,12 +202,16 @@ class Scheduler:
             if req.status == "rejected":
                 continue
             pts = req.size[0] * req.size[1] * req.size[2]
-            if (self.max_active is not None and self.active and
-                    (waiting or self.active_points + pts > self.max_active)):
+            cost = self.ex.step_ms(req.size) if self.max_active_ms is not None else 0.0
+            if self.active and ((self.max_active is not None and
+                                 (waiting or self.active_points + pts > self.max_active)) or
+                                (self.max_active_ms is not None and
+                                 (waiting or self.active_ms + cost > self.max_active_ms))):
                 waiting.append(req)  # no slot: wait, in arrival order
                 continue
             if self._admit_member(req):
                 self.active_points += pts
+                self.active_ms += cost
                 req.status = "active"
                 req.started = now
                 self.busy[req.member] += 1
@@ -209,6 +224,8 @@ class Scheduler:
         # one step per active request per tick; requests on one member run in
         # arrival order (the oldest owns the member until it completes)
         self.tick_no += 1
+        if self.rounds and any(r.inflight for r in self.active):
+            return  # the previous round is still on the device
         owned = set()
         ready = []
         for req in self.active:
@@ -246,7 +263,7 @@ class Scheduler:
         for req in self.active:
             if req.status == "failed":
                 self.busy[req.member] -= 1
-                self.active_points -= req.size[0] * req.size[1] * req.size[2]
+                self._release(req)
                 self.done.append(req)
             elif req.inflight == 0 and (req.done_steps >= req.nsteps or req.status == "cancelled"):
                 req.finished = self.clock()
@@ -255,11 +272,16 @@ class Scheduler:
                     t_arr = req.arrival_wall if req.arrival_wall is not None else req.started
                     self.metrics.req_lat.append(req.finished - t_arr)
                 self.busy[req.member] -= 1
-                self.active_points -= req.size[0] * req.size[1] * req.size[2]
+                self._release(req)
                 self.done.append(req)
             else:
                 still.append(req)
         self.active = still
+
+    def _release(self, req):
+        self.active_points -= req.size[0] * req.size[1] * req.size[2]
+        if self.max_active_ms is not None:
+            self.active_ms = max(0.0, self.active_ms - self.ex.step_ms(req.size))
 
     def idle(self):
         return not self.pending and not self.active
@@ -315,6 +337,10 @@ class FakeExecutor:
     def footprint(self, size):
         nx, ny, nz = size
         return int(1200 * nx * ny * (nz + 1))
+
+    def step_ms(self, size):
+        nx, ny, nz = size
+        return self.ns * 1e-6 * nx * ny * nz
 
     def load(self, member, size):
         if member in self.fail_alloc:
@@ -372,13 +398,18 @@ class GpuExecutor:
         self.spills = 0
         self.restores = 0
         self.prepared = {}     # member -> (surface, initial state), made before serving
+        self.ms = {}           # grid size -> device time of one step (ms), measured at start-up
 
-    def prepare(self, trace):
+    def prepare(self, trace, preload_bytes=0):
         """Work that is not the server's, done before the trace starts: each
         member's seeded surface and initial state (what a client would send
         with its first request), and one tuning of the launch shapes per grid
         size (the server's start-up; every later context of that size reuses
-        the process-wide table)."""
+        the process-wide table), with one step time measured per size.  With
+        preload_bytes > 0 the pool's members are made resident up front, in
+        order of first request while their footprints fit, with their step
+        graphs captured (les_step_graph_prepare): admitting them later costs
+        no allocation or capture on the serving path."""
         lg = self.lg
         for req in trace:
             if req.member in self.prepared:
@@ -387,12 +418,45 @@ class GpuExecutor:
             surf = lg.patch_surface(cfg, self.seed0 + req.member)
             surf.wt_s[:] = 0.05
             self.prepared[req.member] = (surf, lg.initial_state(cfg, surf, seed=self.seed0 + req.member))
-        if self.autotune:
-            for size in sorted({r.size for r in trace}):
-                cfg = self.config(size)
-                ctx = lg.Context(cfg, lg.patch_surface(cfg, 0))
+        for size in sorted({r.size for r in trace}):
+            cfg = self.config(size)
+            surf = lg.patch_surface(cfg, 0)
+            surf.wt_s[:] = 0.05
+            ctx = lg.Context(cfg, surf)
+            if self.autotune:
                 ctx.autotune()
-                ctx.close()
+            for k, v in lg.initial_state(cfg, surf, seed=1).items():
+                ctx.set(k, v)
+            st = self.torch.cuda.ExternalStream(ctx.stream())
+            step = ctx.step_graph if self.use_graphs else ctx.step
+            step(3)
+            e0 = self.torch.cuda.Event(enable_timing=True)
+            e1 = self.torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            step(5)
+            e1.record(st)
+            e1.synchronize()
+            self.ms[size] = e0.elapsed_time(e1) / 5.0
+            ctx.close()
+        used = 0
+        for req in trace:
+            if req.member in self.ctx or preload_bytes <= 0:
+                continue
+            need = self.footprint(req.size)
+            if used + need > preload_bytes:
+                continue
+            self.load(req.member, req.size)
+            if self.use_graphs:
+                self.ctx[req.member].graph_prepare()
+            used += need
+
+    def step_ms(self, size):
+        """Device time of one step of a member of this size (measured by
+        prepare(); a points-proportional guess before it)."""
+        if size in self.ms:
+            return self.ms[size]
+        nx, ny, nz = size
+        return 0.5 + 1e-6 * nx * ny * nz
 
     def config(self, size):
         nx, ny, nz = size
@@ -403,6 +467,8 @@ class GpuExecutor:
         return int(self.lg.estimate_device_bytes(self.config(size)))
 
     def load(self, member, size):
+        if member in self.ctx:  # made resident by prepare()
+            return
         lg = self.lg
         cfg = self.config(size)
         prep = self.prepared.get(member)

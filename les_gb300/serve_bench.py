@@ -17,7 +17,8 @@ import time
 
 
 def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60, priorities=False,
-          max_inflight_points=None, steps_in_flight=1, max_active_points=None):
+          max_inflight_points=None, steps_in_flight=1, max_active_points=None, max_active_ms=None,
+          preload=True, rounds=False):
     """Serve one Poisson trace; returns the summary (and, when
     baseline_requests > 0, the unbatched FP64 baseline on its prefix)."""
     import torch
@@ -26,9 +27,12 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
     budget = int(budget_gb * 2 ** 30) if budget_gb > 0 else int(0.9 * free)
     trace = poisson_trace(requests, rate, seed)
     ex = GpuExecutor(precision=1, autotune=True, priorities=priorities)
-    ex.prepare(trace)  # members' seeded states and the per-size tuning, before the clock starts
+    # members' seeded states, the per-size tuning and, within the budget, the
+    # resident pool with its captured step graphs: before the clock starts
+    ex.prepare(trace, preload_bytes=budget if preload else 0)
     sched = Scheduler(ex, budget_bytes=budget, max_inflight_per_member=steps_in_flight,
-                      max_inflight_points=max_inflight_points, max_active_points=max_active_points)
+                      max_inflight_points=max_inflight_points, max_active_points=max_active_points,
+                      max_active_ms=max_active_ms, rounds=rounds)
     summary, wall = sched.run(trace)
     status = {}
     for r in sched.done:
@@ -37,7 +41,8 @@ def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60
         ex.evict(m)
     out = {"requests": len(trace), "rate_per_s": rate, "priorities": priorities,
            "max_inflight_points": max_inflight_points, "steps_in_flight": steps_in_flight,
-           "max_active_points": max_active_points,
+           "max_active_points": max_active_points, "max_active_ms": max_active_ms, "preload": preload, "rounds": rounds,
+           "step_ms_by_size": {"%dx%dx%d" % k: v for k, v in sorted(ex.ms.items())},
            "wall_s": wall, "status": status,
            "budget_gb": budget / 2 ** 30, "serving": summary}
     if summary.get("step_p50_ms"):
@@ -79,12 +84,19 @@ def main():
                     help="steps of one request queued on its member's stream at once")
     ap.add_argument("--max-active-points", type=float, default=0.0,
                     help="grid points of the active requests (slots; 0: no limit)")
+    ap.add_argument("--max-active-ms", type=float, default=0.0,
+                    help="summed step times of the active requests, ms (slots; 0: no limit)")
+    ap.add_argument("--rounds", action="store_true", help="lock-step rounds of steps")
+    ap.add_argument("--no-preload", action="store_true",
+                    help="admit members on their first request (allocation and graph capture on the path)")
     args = ap.parse_args()
     mip = int(args.max_inflight_points) if args.max_inflight_points > 0 else None
     map_ = int(args.max_active_points) if args.max_active_points > 0 else None
     print(json.dumps(serve(args.requests, args.rate, args.seed, args.budget_gb, args.baseline_requests,
                            priorities=args.priorities, max_inflight_points=mip,
-                           steps_in_flight=args.steps_in_flight, max_active_points=map_)))
+                           steps_in_flight=args.steps_in_flight, max_active_points=map_,
+                           max_active_ms=args.max_active_ms if args.max_active_ms > 0 else None,
+                           preload=not args.no_preload, rounds=args.rounds)))
 
 
 if __name__ == "__main__":

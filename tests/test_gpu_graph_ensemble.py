@@ -35,6 +35,33 @@ def test_graph_replay_is_bit_identical(gpu_lib, precision):
         assert np.array_equal(sa[k], sb[k]), k
 
 
+@pytest.mark.parametrize("precision", [1, 2])
+def test_graph_prepare_changes_nothing(gpu_lib, precision):
+    """les_step_graph_prepare captures the replayed step graphs ahead of time
+    without stepping: counters and state are unchanged, and the prepared
+    member then replays bit-identically to one capturing on first use and to
+    eager steps."""
+    a = member(32, 32, 7, precision)
+    b = member(32, 32, 7, precision)
+    c = member(32, 32, 7, precision)
+    a.step(1)
+    b.step(1)
+    c.step(1)
+    before = state(b)
+    b.graph_prepare()
+    assert b.counters() == a.counters()
+    after = state(b)
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    a.step_graph(11)
+    b.step_graph(11)
+    c.step(11)
+    sa, sb, sc = state(a), state(b), state(c)
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+        assert np.array_equal(sa[k], sc[k]), k
+
+
 def test_autotune_keeps_results(gpu_lib):
     a = member(32, 32, 6)
     b = member(32, 32, 6)

@@ -183,3 +183,34 @@ def test_active_slots_queue_requests_in_arrival_order():
     big.submit(R(0, 0, n=1, size=(64, 64, 64)))   # larger than the cap: starts when nothing runs
     big.tick(0.0)
     assert len(big.active) == 1
+
+
+def test_active_slots_by_step_time():
+    """max_active_ms caps the summed step-time estimates of the active
+    requests (FakeExecutor: ns_per_pt per grid point)."""
+    ex = FakeExecutor(ns_per_pt=1.0)              # a 32^3 step: 0.0328 ms
+    s = Scheduler(ex, budget_bytes=10 ** 12, max_active_ms=0.07)
+    for i in range(4):
+        s.submit(R(i, member=i, n=2))
+    s.tick(0.0)
+    assert len(s.active) == 2 and len(s.pending) == 2
+    drain(s)
+    assert len(s.done) == 4 and abs(s.active_ms) < 1e-12
+
+
+def test_lock_step_rounds():
+    """With rounds, no step launches while any step of the previous round is
+    in flight; every request still completes."""
+    ex = FakeExecutor()
+    s = Scheduler(ex, budget_bytes=10 ** 12, rounds=True)
+    s.submit(R(0, 0, n=3))
+    s.submit(R(1, 1, n=3, size=(64, 64, 64)))
+    s.tick(0.0)
+    assert len(ex.inflight) == 2
+    s.tick(0.0)                       # round 1 still in flight: nothing new
+    assert len(ex.inflight) == 2
+    s.poll()
+    s.tick(0.0)
+    assert len(ex.inflight) == 2
+    drain(s)
+    assert ex.steps[0] == 3 and ex.steps[1] == 3
