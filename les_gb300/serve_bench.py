@@ -2,7 +2,8 @@
 requests (N ~ U{1..50}) over a pool of 64 members with sizes drawn from
 {32^3, 64^3, 96^2x64, 128^3, 192^2x128} (weights 0.3/0.3/0.2/0.15/0.05),
 FP32-mixed steps replayed from CUDA graphs, admission by estimated footprint
-against free device memory.  Before the trace starts the members' seeded
+against free device memory, then to a slot while the active requests' summed
+step times stay within 24 ms; the active requests step in lock-step rounds.  Before the trace starts the members' seeded
 surfaces and initial states are generated (the client's side of a request)
 and the launch shapes are tuned once per grid size (the server's start-up);
 admitting a member is then its allocation, upload and graph capture.  Reports p50/p99 step and request latency and
@@ -17,8 +18,8 @@ import time
 
 
 def serve(requests=200, rate=200.0, seed=11, budget_gb=0.0, baseline_requests=60, priorities=False,
-          max_inflight_points=None, steps_in_flight=1, max_active_points=None, max_active_ms=None,
-          preload=True, rounds=False):
+          max_inflight_points=None, steps_in_flight=1, max_active_points=None, max_active_ms=24.0,
+          preload=True, rounds=True):
     """Serve one Poisson trace; returns the summary (and, when
     baseline_requests > 0, the unbatched FP64 baseline on its prefix)."""
     import torch
@@ -84,9 +85,10 @@ def main():
                     help="steps of one request queued on its member's stream at once")
     ap.add_argument("--max-active-points", type=float, default=0.0,
                     help="grid points of the active requests (slots; 0: no limit)")
-    ap.add_argument("--max-active-ms", type=float, default=0.0,
+    ap.add_argument("--max-active-ms", type=float, default=24.0,
                     help="summed step times of the active requests, ms (slots; 0: no limit)")
-    ap.add_argument("--rounds", action="store_true", help="lock-step rounds of steps")
+    ap.add_argument("--no-rounds", action="store_true",
+                    help="relaunch each request as its step completes instead of lock-step rounds")
     ap.add_argument("--no-preload", action="store_true",
                     help="admit members on their first request (allocation and graph capture on the path)")
     args = ap.parse_args()
@@ -96,7 +98,7 @@ def main():
                            priorities=args.priorities, max_inflight_points=mip,
                            steps_in_flight=args.steps_in_flight, max_active_points=map_,
                            max_active_ms=args.max_active_ms if args.max_active_ms > 0 else None,
-                           preload=not args.no_preload, rounds=args.rounds)))
+                           preload=not args.no_preload, rounds=not args.no_rounds)))
 
 
 if __name__ == "__main__":
