@@ -4693,8 +4693,12 @@ static void tune_probe(les_ctx* c) {
   double* bo[3] = {c->big + 3 * g.nfield_big, c->big + 4 * g.nfield_big, c->big + 5 * g.nfield_big};
   c2rT<T, double>(c, 3, nz, c->wsA, bo, (long)g.nplane_big, true, g.nx / 2);
 }
+// fp32: the FP32 transforms' knobs; else the 8-byte-real knobs, probed with
+// the kernels the form runs them with (FP64 in the FP64 form, float-float in
+// the mixed and float-float transform forms)
 void autotune_probe(les_ctx* c, int fp32) {
   if (fp32) tune_probe<float>(c);
+  else if (c->cfg.precision != 0) tune_probe<dfloat>(c);
   else tune_probe<double>(c);
 }
 
