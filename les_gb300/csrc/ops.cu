@@ -2167,18 +2167,31 @@ struct MeanTab {
 // zeroed), so skipping the y round trip that ddx would make loses nothing;
 // the forward x pass that made `in` is scaled for an x round trip alone
 // (1/nx, not 1/(nx ny)), or `in` is already the inverse y transform.
-__global__ void k_ikx_rows(const dcomplex* __restrict__ in, dcomplex* out, const float2* __restrict__ kxd, int lh,
-                           size_t n, int acc) {
+// The column's kx: row 0 of the (lh, ny) table, as a float-float pair or FP64.
+template <typename CX> struct KxCol;
+template <> struct KxCol<dcomplex> {
+  static __device__ __forceinline__ dfloat get(const float2* __restrict__ kxd, const double*, int jx) {
+    const float2 kv = kxd[jx];
+    return dfloat(kv.x, kv.y);
+  }
+};
+template <> struct KxCol<double2> {
+  static __device__ __forceinline__ double get(const float2*, const double* __restrict__ kx, int jx) {
+    return kx[jx];
+  }
+};
+template <typename CX>
+__global__ void k_ikx_rows(const CX* __restrict__ in, CX* out, const float2* __restrict__ kxd,
+                           const double* __restrict__ kx, int lh, size_t n, int acc) {
   GSTRIDE(e, n) {
     const int jx = (int)(e % lh);
-    const float2 kv = kxd[jx];  // row 0 of the (lh, ny) table: the column's kx
-    const dfloat k(kv.x, kv.y);
-    const dcomplex v = in[e];
-    dcomplex r;
+    const auto k = KxCol<CX>::get(kxd, kx, jx);
+    const CX v = in[e];
+    CX r;
     r.x = -(k * v.y);
     r.y = k * v.x;
     if (acc) {
-      const dcomplex o = out[e];
+      const CX o = out[e];
       r.x = r.x + o.x;
       r.y = r.y + o.y;
     }
@@ -3101,10 +3114,12 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const float
         Hx, Hy, Hz, BT, BT + g.C, P, c->ibet, c->gamt, c->kx, c->ky, c->kxd, c->kyd, g.lh, g.ny, nz, g.dz,
         nullptr, 0); LES_COUNT_LAUNCH();
   }
-  // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy
-  if constexpr (std::is_same<T, dfloat>::value) {
-    // float-float: p-hat's y round trip for levels 0..nz-1 and for i ky on
-    // 1..nz-1; dp/dx by the x wavenumber alone (p-hat's Nyquist modes are zero)
+  // p level 0 ; levels 1..nz-1 : p, dpdx, dpdy.  p-hat's y round trip for
+  // levels 0..nz-1 and i ky's for 1..nz-1; dp/dx by the x wavenumber alone
+  // on the inverse y transform (p-hat's Nyquist modes are zero,
+  // press_stag_array.f90:263-264, so the y round trip that ddx makes adds
+  // nothing)
+  {
     ColJob K = coljob(c, MAP_SAME, DIR_INV, nz);
     K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
     colsT<T, PCX>(c, K);
@@ -3115,26 +3130,11 @@ static int pressT(les_ctx* c, double* p, double* dpdx, double* dpdy, const float
     ColJob L = coljob(c, MAP_SAME, DIR_INV, nz - 1);
     L.nin = 1; L.nout = 1; L.in[0] = P + g.C; L.out[0] = Yy; L.coef[0][0] = CC_IKY;
     colsT<T, PCX>(c, L);
-    k_ikx_rows<<<grid1(L1), 256, 0, c->stream>>>(Y + g.C, Yx, c->kxd, g.lh, L1, 0); LES_COUNT_LAUNCH();
+    k_ikx_rows<CX><<<grid1(L1), 256, 0, c->stream>>>(Y + g.C, Yx, c->kxd, c->kx, g.lh, L1, 0); LES_COUNT_LAUNCH();
     double* o0 = p;
     c2rT<T, double>(c, 1, nz, Y, &o0, (long)g.nplane, false, g.lh);
     double* o1[2] = {dpdx, dpdy};
     c2rT<T, double>(c, 2, nz - 1, Yx, o1, (long)g.nplane, false, g.lh);
-  } else {
-    ColJob K = coljob(c, MAP_SAME, DIR_INV, 1);
-    K.nin = 1; K.nout = 1; K.in[0] = P; K.out[0] = c->wsB; K.coef[0][0] = CC_ONE;
-    colsT<T, PCX>(c, K);
-    ColJob L = coljob(c, MAP_SAME, DIR_INV, nz - 1);
-    L.nin = 1; L.nout = 3; L.in[0] = P + g.C;
-    L.out[0] = (CX*)c->wsB + g.C;
-    L.out[1] = (CX*)c->wsB + g.C + (size_t)(nz - 1) * g.C;
-    L.out[2] = (CX*)c->wsB + g.C + (size_t)2 * (nz - 1) * g.C;
-    L.coef[0][0] = CC_ONE; L.coef[1][0] = CC_IKX; L.coef[2][0] = CC_IKY;
-    colsT<T, PCX>(c, L);
-    double* o0 = p;
-    c2rT<T, double>(c, 1, 1, c->wsB, &o0, (long)g.nplane, false, g.lh);
-    double* o1[3] = {p + g.nplane, dpdx, dpdy};
-    c2rT<T, double>(c, 3, nz - 1, (CX*)c->wsB + g.C, o1, (long)g.nplane, false, g.lh);
   }
   fill(c, dpdx + (size_t)(nz - 1) * g.nplane, g.nplane, LES_BOGUS);
   fill(c, dpdy + (size_t)(nz - 1) * g.nplane, g.nplane, LES_BOGUS);
@@ -4484,9 +4484,10 @@ static void meanflow_lin(les_ctx* c) {
   colsT<dfloat, dcomplex>(c, J);
   const dcomplex* sa = (const dcomplex*)c->wsA;
   dcomplex* sb = (dcomplex*)c->wsB;
-  k_ikx_rows<<<grid1((size_t)FS), 256, 0, c->stream>>>(sa + FS, sb, c->kxd, g.lh, (size_t)FS, 1);
+  k_ikx_rows<dcomplex><<<grid1((size_t)FS), 256, 0, c->stream>>>(sa + FS, sb, c->kxd, c->kx, g.lh, (size_t)FS, 1);
   LES_COUNT_LAUNCH();
-  k_ikx_rows<<<grid1((size_t)FS), 256, 0, c->stream>>>(sa + 2 * FS, sb + FS, c->kxd, g.lh, (size_t)FS, 0);
+  k_ikx_rows<dcomplex><<<grid1((size_t)FS), 256, 0, c->stream>>>(sa + 2 * FS, sb + FS, c->kxd, c->kx, g.lh,
+                                                                 (size_t)FS, 0);
   LES_COUNT_LAUNCH();
   dfloat* ml = mlin_fields(c);
   dfloat* out[2] = {ml, ml + g.nfield};
