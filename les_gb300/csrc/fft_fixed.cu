@@ -218,6 +218,10 @@ bool launch_rows_c2r_fixed(const RowJob& J, const RealPlanDev& P, int rpc, size_
 
 // float-float y pass (the projection path): same-length pairs, kx tile 4
 #define LES_COL_SAME(X) X(32, 32) X(64, 64) X(96, 96) X(128, 128) X(192, 192) X(256, 256)
+// float-float 3/2 padding and truncation (the float-float transform form's
+// convective and scalar terms), kx tile 4
+#define LES_COL_FF_PAD(X) X(32, 48) X(64, 96) X(96, 144) X(128, 192) X(192, 288) X(256, 384)
+#define LES_COL_FF_UNPAD(X) X(48, 32) X(96, 64) X(144, 96) X(192, 128) X(288, 192) X(384, 256)
 
 template <typename T, int TX, typename CIn>
 bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev& Pout, size_t sm, dim3 grid,
@@ -239,12 +243,22 @@ bool launch_cols_fixed(const ColJob& J, const FftPlanDev& Pin, const FftPlanDev&
 #undef LES_CASE
       default: return false;
     }
-  } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 &&
-                       (std::is_same<CIn, dcomplex>::value || std::is_same<CIn, double2>::value)) {
+  } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 && std::is_same<CIn, dcomplex>::value) {
     switch (key) {
 #define LES_CASE(a, b) \
   case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, grid, s); return true;
       LES_COL_SAME(LES_CASE)
+      LES_COL_FF_PAD(LES_CASE)
+      LES_COL_FF_UNPAD(LES_CASE)
+#undef LES_CASE
+      default: return false;
+    }
+  } else if constexpr (std::is_same<T, dfloat>::value && TX == 4 && std::is_same<CIn, double2>::value) {
+    switch (key) {  // float-float transforms of the saved FP64 spectra (same length, and padding)
+#define LES_CASE(a, b) \
+  case a * 10000 + b: cols_fixed<T, TX, CIn, a, b>(J, Pin, Pout, grid, s); return true;
+      LES_COL_SAME(LES_CASE)
+      LES_COL_FF_PAD(LES_CASE)
 #undef LES_CASE
       default: return false;
     }

@@ -9,10 +9,11 @@ With --pert X a third member runs the FP64 step from the same state with
 every interior u, v, w value multiplied by (1 + X r), r uniform in [-1, 1]
 (X = 1e-15: a perturbation at the size of FP64 rounding), and its difference
 from the FP64 member is reported beside the mixed form's: it shows how the
-configuration itself amplifies a difference of rounding size.
+configuration itself amplifies a difference of rounding size.  With --ff the
+FP64 state with float-float transforms (precision 2) runs beside them too.
 
   python -m les_gb300.precision_study [--grid 256] [--steps 500] [--every 50]
-                                      [--jt0 0] [--dt 2e-4] [--pert 1e-15]
+                                      [--jt0 0] [--dt 2e-4] [--pert 1e-15] [--ff]
 """
 import argparse
 import json
@@ -32,6 +33,7 @@ def main():
     ap.add_argument("--jt0", type=int, default=0)
     ap.add_argument("--dt", type=float, default=2e-4)
     ap.add_argument("--pert", type=float, default=0.0)
+    ap.add_argument("--ff", action="store_true", help="also the float-float transform form (precision 2)")
     args = ap.parse_args()
     import les_gb300 as lg
     from les_gb300.config import splitmix64_uniform
@@ -39,6 +41,8 @@ def main():
     forms = [("mixed", 1, 0.0), ("fp64", 0, 0.0)]
     if args.pert > 0:
         forms.append(("fp64_pert", 0, args.pert))
+    if args.ff:
+        forms.append(("ff", 2, 0.0))
     ctxs = {}
     for name, prec, pert in forms:
         # rmsdiv is read directly (les_rmsdiv) so the reference's CFL stop
