@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
 // and in the Hermitian pre/post-processing (half length 128 = 16 x 8 with
 // eight threads per row).
 template <typename T, typename TIn, int N1, int N2, int TT, int NT>
-__global__ void __launch_bounds__(NT) k_r2c_reg2(RowJob J, RealPlanDev P) {
+__global__ void __launch_bounds__(NT, 5) k_r2c_reg2(RowJob J, RealPlanDev P) {
   typedef typename CT<T>::type C;
   typedef typename CT<TIn>::type CI;
   static_assert(N1 % TT == 0 && N2 % TT == 0 && NT % TT == 0, "thread split");
