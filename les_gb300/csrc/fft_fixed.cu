@@ -30,7 +30,10 @@ struct RegRows {
 };
 
 // FP32 x pass, half length 128 = 16 x 8 with eight threads per row (every
-// lane busy in both steps)
+// lane busy in both steps).  The float-float x pass keeps the shared-memory
+// kernels: this form in float-float takes 128 registers (two CTAs per SM)
+// and made the 256^3 steps slower (FP32-mixed 13.10 -> 13.23 ms, float-float
+// transform form 36.9 -> 37.5 ms).
 template <typename T, int NF> struct RowSplit2 { static constexpr int n1 = 0, n2 = 0, tt = 0; };
 template <> struct RowSplit2<float, 128> { static constexpr int n1 = 16, n2 = 8, tt = 8; };
 template <typename T, int N1, int N2, int TT>
@@ -111,6 +114,10 @@ void cols_reg(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (nsm <= 0) nsm = 1;
   }
+  // lh = nx/2 + 1 columns leave one column in the last tile of each
+  // (level, field) set.  Packing those columns of sixteen sets into one item
+  // made the FP32 y pass slower in the 256^3 step (2.21 -> 2.33 ms), so the
+  // last tile stays one item per set.
   const int ntile = (J.ncols + TX - 1) / TX;
   const int nitems = ntile * J.nlev * (J.nf > 0 ? J.nf : 1);
   const int nblk = std::min(nitems, 3 * nsm);  // three resident CTAs per SM (registers, shared memory)
