@@ -178,6 +178,44 @@ __global__ void __launch_bounds__(256) k_rows_c2r(RowJob J, RealPlanDev P, int r
   }
 }
 
+// Asynchronous 8-byte global -> shared copies (zero-filled when src_bytes is 0).
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Warp-local staging of the inverse x pass's rows: the TT threads of a row
+// are lanes of one warp, so warp w copies its 32/TT rows (nc <= M + 1
+// complex each, M + 1 <= MS) into those rows' slots of the exchange buffer
+// with coalesced 8-byte cp.async copies: every element is read from global
+// memory once (the Hermitian pre-processing reads X[k] and X[M - k]) and all
+// of a thread's copies are in flight together.  __syncwarp makes them
+// visible to the row's lanes.
+template <typename C, int TT, int RPB, int MS, int M>
+__device__ __forceinline__ void stage_rows_warp(C* S, const C* base, size_t wc, int row0, int ny, int nc) {
+  static_assert(sizeof(C) == 8 && 32 % TT == 0 && MS >= M + 1, "8-byte elements, rows within one warp");
+  constexpr int RPW = 32 / TT, KMAX = (M + 1 + 31) / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n = nc < M + 1 ? nc : M + 1;
+#pragma unroll
+  for (int rr = 0; rr < RPW; ++rr) {
+    const int rl = w * RPW + rr, row = row0 + rl;
+    if (rl < RPB && row < ny) {
+      const C* src = base + (size_t)row * wc;
+#pragma unroll
+      for (int kk = 0; kk < KMAX; ++kk) {
+        const int k = lane + 32 * kk;
+        if (k < n) cp_async8(&S[rl * MS + k], src + k, 8);
+      }
+    }
+  }
+  cp_async_commit();
+  cp_async_wait_all();
+  __syncwarp();
+}
+
 // ---------------------------------------------------------------------------
 // Register-resident x pass, half length M = N1 * N2.  A row is served by
 // TT = max(N1, N2) threads.  Forward (r2c): n = n1 + N1 n2, k = k2 + N2 k1;
@@ -289,17 +327,17 @@ __global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
   const bool rowok = r < RPB && row < J.ny;
   C* Sr = S + (r < RPB ? r : 0) * MS;
   C v[TT];
+  const int nc = J.ncols;
+  stage_rows_warp<C, TT, RPB, MS, M>(S, reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work, J.wc,
+                                     blockIdx.x * RPB, J.ny, nc);
   if (q < N1) {
-    const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work +
-                  (size_t)(rowok ? row : 0) * J.wc;
-    const int nc = J.ncols;
 #pragma unroll
     for (int i = 0; i < N2; ++i) {
       const int k = q + N1 * i, km = M - k;
       C a = mk<T>((T)0, (T)0), bb = mk<T>((T)0, (T)0);
       if (rowok) {
-        if (k < nc) a = in[k];
-        if (km < nc) bb = in[km];
+        if (k < nc) a = Sr[k];
+        if (km < nc) bb = Sr[km];
       }
       if (k == 0) { a.y = (T)0; bb.y = (T)0; }  // the halfcomplex pass ignores Im of X[0], X[M]
       const C b = cconj(bb);
@@ -307,6 +345,9 @@ __global__ void __launch_bounds__(NT) k_c2r_reg(RowJob J, RealPlanDev P) {
       const C d = cmul(csub(a, b), cconj(rw<T>(P, k)));  // x exp(+2 pi i k / nx)
       v[i] = cadd(e, cmuli(d));
     }
+  }
+  __syncwarp();  // the row's staged input is read before its exchange slots are written
+  if (q < N1) {
     dft_n<T, N2>(v, +1);  // over k2: v[i] = y[k1 = q][n2 = i]
 #pragma unroll
     for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(UnitSel<T>::get(P.c, q * i)));
@@ -457,32 +498,37 @@ __global__ void __launch_bounds__(NT, 5) k_c2r_reg2(RowJob J, RealPlanDev P) {
   const int row = blockIdx.x * RPB + r;
   const bool rowok = row < J.ny;
   C* Sr = S + r * MS;
-  const C* in = reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work +
-                (size_t)(rowok ? row : 0) * J.wc;
   const int nc = J.ncols;
+  stage_rows_warp<C, TT, RPB, MS, M>(S, reinterpret_cast<const C*>(J.work[f]) + (size_t)lev * J.pstride_work, J.wc,
+                                     blockIdx.x * RPB, J.ny, nc);
+  C v[J1][N2];
 #pragma unroll
   for (int j = 0; j < J1; ++j) {
     const int k1 = q + TT * j;
-    C v[N2];
 #pragma unroll
     for (int i = 0; i < N2; ++i) {
       const int k = k1 + N1 * i, km = M - k;
       C a = mk<T>((T)0, (T)0), bb = mk<T>((T)0, (T)0);
       if (rowok) {
-        if (k < nc) a = in[k];
-        if (km < nc) bb = in[km];
+        if (k < nc) a = Sr[k];
+        if (km < nc) bb = Sr[km];
       }
       if (k == 0) { a.y = (T)0; bb.y = (T)0; }  // the halfcomplex pass ignores Im of X[0], X[M]
       const C b = cconj(bb);
       const C e = cadd(a, b);
       const C d = cmul(csub(a, b), cconj(rw<T>(P, k)));  // x exp(+2 pi i k / nx)
-      v[i] = cadd(e, cmuli(d));
+      v[j][i] = cadd(e, cmuli(d));
     }
-    dft_n<T, N2>(v, +1);  // over k2: v[i] = y[k1][n2 = i]
+  }
+  __syncwarp();  // the row's staged input is read before its exchange slots are written
 #pragma unroll
-    for (int i = 1; i < N2; ++i) v[i] = cmul(v[i], cconj(UnitSel<T>::get(P.c, k1 * i)));
+  for (int j = 0; j < J1; ++j) {
+    const int k1 = q + TT * j;
+    dft_n<T, N2>(v[j], +1);  // over k2: v[j][i] = y[k1][n2 = i]
 #pragma unroll
-    for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + k1] = v[i];
+    for (int i = 1; i < N2; ++i) v[j][i] = cmul(v[j][i], cconj(UnitSel<T>::get(P.c, k1 * i)));
+#pragma unroll
+    for (int i = 0; i < N2; ++i) Sr[i * (N1 + 1) + k1] = v[j][i];
   }
   __syncthreads();
   if (rowok) {
@@ -785,13 +831,6 @@ __device__ __forceinline__ void dft_r(typename CT<T>::type* v, int sign) {
   else if constexpr (R == 8) dft8<C, T>(v, sign);
   else dft4(v, sign);
 }
-// Asynchronous 8-byte global -> shared copies (zero-filled when src_bytes is 0).
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, int src_bytes) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Persistent form: a CTA walks the (kx tile, level, field set) items of the
 // job with stride gridDim.x; each thread stages its R input elements of the
