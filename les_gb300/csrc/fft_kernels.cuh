@@ -244,12 +244,19 @@ __global__ void __launch_bounds__(NT) k_r2c_reg(RowJob J, RealPlanDev P) {
   const bool rowok = r < RPB && row < J.ny;
   C* Sr = S + (r < RPB ? r : 0) * MS;
   C v[TT];
+  // FP32 input: the rows (M pairs each) are staged once through their
+  // exchange slots (stage_rows_warp); an FP64 row does not fit its slot and
+  // is read straight from global memory
+  constexpr bool STAGED = sizeof(CI) == sizeof(C);
+  const TIn* plane = reinterpret_cast<const TIn*>(J.phys[f]) + (size_t)lev * J.pstride_phys;
+  if constexpr (STAGED)
+    stage_rows_warp<C, TT, RPB, MS, M>(S, reinterpret_cast<const C*>(plane), J.ld / 2, blockIdx.x * RPB, J.ny, M);
   if (q < N1) {
     const T sd = (T)(J.div[f] != 0.0 ? J.scale[f] / J.div[f] : J.scale[f]);  // scale/div, one product
     const bool hasoff = J.off[f] != nullptr;
     const double off = hasoff ? J.off[f][lev] : 0.0;
-    const CI* src = reinterpret_cast<const CI*>(reinterpret_cast<const TIn*>(J.phys[f]) +
-                                                (size_t)lev * J.pstride_phys + (size_t)(rowok ? row : 0) * J.ld) + q;
+    const CI* src = STAGED ? reinterpret_cast<const CI*>(Sr) + q
+                           : reinterpret_cast<const CI*>(plane + (size_t)(rowok ? row : 0) * J.ld) + q;
 #pragma unroll
     for (int i = 0; i < N2; ++i) {
       v[i] = mk<T>((T)0, (T)0);
@@ -413,8 +420,13 @@ __global__ void __launch_bounds__(NT, 5) k_r2c_reg2(RowJob J, RealPlanDev P) {
   const T sd = (T)(J.div[f] != 0.0 ? J.scale[f] / J.div[f] : J.scale[f]);  // scale/div, one product
   const bool hasoff = J.off[f] != nullptr;
   const double off = hasoff ? J.off[f][lev] : 0.0;
-  const CI* src = reinterpret_cast<const CI*>(reinterpret_cast<const TIn*>(J.phys[f]) +
-                                              (size_t)lev * J.pstride_phys + (size_t)(rowok ? row : 0) * J.ld);
+  // FP32 input staged as in k_r2c_reg
+  constexpr bool STAGED = sizeof(CI) == sizeof(C);
+  const TIn* plane = reinterpret_cast<const TIn*>(J.phys[f]) + (size_t)lev * J.pstride_phys;
+  if constexpr (STAGED)
+    stage_rows_warp<C, TT, RPB, MS, M>(S, reinterpret_cast<const C*>(plane), J.ld / 2, blockIdx.x * RPB, J.ny, M);
+  const CI* src = STAGED ? reinterpret_cast<const CI*>(Sr)
+                         : reinterpret_cast<const CI*>(plane + (size_t)(rowok ? row : 0) * J.ld);
   C v[J1][N2];
 #pragma unroll
   for (int j = 0; j < J1; ++j)
