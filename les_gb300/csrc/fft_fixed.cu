@@ -104,7 +104,7 @@ template <typename T, typename CIn, int R>
 void cols_reg(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
   typedef typename CT<T>::type C;
   constexpr int TX = 16, N = R * R;
-  const size_t smf = (size_t)N * TX * (sizeof(C) + sizeof(CIn)) + (size_t)N * sizeof(C);
+  const size_t smf = (size_t)N * TX * (sizeof(C) + sizeof(CIn)) + (size_t)N * (sizeof(C) + sizeof(T));
   static size_t set = 48 * 1024;
   raise_smem(k_colsr<T, TX, CIn, R>, smf, set);
   static int nsm = 0;
@@ -129,7 +129,7 @@ template <typename T, typename CIn, int R>
 void cols_reg_sum(const ColJob& J, const FftPlanDev& P, cudaStream_t s) {
   typedef typename CT<T>::type C;
   constexpr int TX = 16, N = R * R;
-  const size_t smf = (size_t)(3 * N * TX + N) * sizeof(C);
+  const size_t smf = (size_t)(3 * N * TX + N) * sizeof(C) + (size_t)N * sizeof(T);
   static size_t set = 48 * 1024;
   raise_smem(k_colsr_sum<T, TX, CIn, R, 2>, smf, set);
   const dim3 grid((J.ncols + TX - 1) / TX, J.nlev, J.nf > 0 ? J.nf : 1);

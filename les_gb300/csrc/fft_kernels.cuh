@@ -605,6 +605,23 @@ __device__ __forceinline__ typename CT<T>::type apply_coef(int code, typename CT
   }
 }
 
+// i kx, i ky and -i ky without a (lh, ny) table load per element: the
+// tables hold kx by column and ky by row, zeroed on the column kx = nx/2 and
+// the row ky = ny/2 (fft.f90:54-81), so kx(jx, js) is row 0's entry (kxc,
+// held by the column's thread) but zero on row ny/2, and ky(jx, js) column
+// 0's entry (kys, a shared-memory copy of that column) but zero on column
+// lh - 1: the same values as the table.  Other codes read the tables.
+template <typename T>
+__device__ __forceinline__ typename CT<T>::type apply_coef_k(int code, typename CT<T>::type v, int jx, int js,
+                                                             T kxc, const T* kys, const ColJob& J) {
+  switch (code) {
+    case CC_IKX: return ik(v, js == J.ny_small / 2 ? (T)0 : kxc);
+    case CC_IKY: return ik(v, jx == J.lh - 1 ? (T)0 : kys[js]);
+    case CC_MIKY: return ik(v, -(jx == J.lh - 1 ? (T)0 : kys[js]));
+    default: return apply_coef<T>(code, v, jx, js, J);
+  }
+}
+
 // Runtime lengths (plans Pin, Pout): the fixed-length kernels below cover
 // the lengths the workloads use.
 template <typename T, int TX, typename CIn>
@@ -859,7 +876,11 @@ __global__ void __launch_bounds__(TX * R, 3) k_colsr(ColJob J, FftPlanDev P, int
   C* S = reinterpret_cast<C*>(smraw);          // exchange: element (i, q) of column b at (i * R + q) * TX + b
   CIn* G = reinterpret_cast<CIn*>(S + N * TX);  // staged input, same index
   C* tw = reinterpret_cast<C*>(G + N * TX);    // exp(-2 pi i m / N), m < N
-  for (int t = threadIdx.x; t < N; t += TX * R) tw[t] = UnitSel<T>::get(P, t);
+  T* kys = reinterpret_cast<T*>(tw + N);        // ky of row js (column 0 of the table), js < N
+  for (int t = threadIdx.x; t < N; t += TX * R) {
+    tw[t] = UnitSel<T>::get(P, t);
+    kys[t] = Tab<T>::ky(J, (size_t)J.lh * t);
+  }
   const int b = threadIdx.x % TX, q = threadIdx.x / TX;
   const int nlev = J.nlev;
   auto stage = [&](int item) {
@@ -900,11 +921,13 @@ __global__ void __launch_bounds__(TX * R, 3) k_colsr(ColJob J, FftPlanDev P, int
       for (int i = 0; i < R; ++i) v[i] = S[(q * R + i) * TX + b];  // y[n1 = i][k2 = q]
       dft_r<T, R>(v, -1);  // over n1: v[i] = X[q + R i]
     }
+    const T kxc = colok ? Tab<T>::kx(J, (size_t)jx) : (T)0;  // row 0: kx of the column
     for (int o = 0; o < J.nout; ++o) {
       C y[R];
       const int code = J.coef[o][0];
 #pragma unroll
-      for (int i = 0; i < R; ++i) y[i] = colok ? apply_coef<T>(code, v[i], jx, q + R * i, J) : mk<T>((T)0, (T)0);
+      for (int i = 0; i < R; ++i)
+        y[i] = colok ? apply_coef_k<T>(code, v[i], jx, q + R * i, kxc, kys, J) : mk<T>((T)0, (T)0);
       if ((J.inv_mask >> o) & 1u) {
         dft_r<T, R>(y, +1);  // over k1: y[i] = z[k2 = q][n1 = i]
 #pragma unroll
@@ -1081,10 +1104,15 @@ __global__ void __launch_bounds__(TX * R, 2) k_colsr_sum(ColJob J, FftPlanDev P)
   C* S = reinterpret_cast<C*>(smraw);  // exchange: element (i, q) of column b at (i * R + q) * TX + b
   C* A = S + N * TX;                   // NO accumulators, same index
   C* tw = A + NO * N * TX;             // exp(-2 pi i m / N), m < N
-  for (int t = threadIdx.x; t < N; t += TX * R) tw[t] = UnitSel<T>::get(P, t);
+  T* kys = reinterpret_cast<T*>(tw + N);  // ky of row js (column 0 of the table), js < N
+  for (int t = threadIdx.x; t < N; t += TX * R) {
+    tw[t] = UnitSel<T>::get(P, t);
+    kys[t] = Tab<T>::ky(J, (size_t)J.lh * t);
+  }
   const int b = threadIdx.x % TX, q = threadIdx.x / TX;
   const int jx = blockIdx.x * TX + b;
   const bool colok = jx < J.ncols;
+  const T kxc = colok ? Tab<T>::kx(J, (size_t)jx) : (T)0;  // row 0: kx of the column
   const int lev = blockIdx.y;
 #pragma unroll
   for (int o = 0; o < NO; ++o)
@@ -1122,7 +1150,8 @@ __global__ void __launch_bounds__(TX * R, 2) k_colsr_sum(ColJob J, FftPlanDev P)
         if (code != CC_NONE) {
           C* a = A + o * N * TX + q * TX + b;
 #pragma unroll
-          for (int i = 0; i < R; ++i) a[i * R * TX] = cadd(a[i * R * TX], apply_coef<T>(code, v[i], jx, q + R * i, J));
+          for (int i = 0; i < R; ++i)
+            a[i * R * TX] = cadd(a[i * R * TX], apply_coef_k<T>(code, v[i], jx, q + R * i, kxc, kys, J));
         }
       }
     }
