@@ -49,7 +49,7 @@ FAMILIES = {1: "k_cols/k_colsf<double|dfloat> (FP64 / float-float y pass)",
 # family on a 256 x 256 x 96 member (bench.py --capture-step;
 # profiles/transforms_fp32_traffic.md); scales the live algorithmic bytes
 # per launch to the traffic per launch.  Only where a capture exists.
-TRAFFIC_RATIO = {("mixed", 4): 0.742, ("mixed", 2): 0.760}
+TRAFFIC_RATIO = {("mixed", 4): 0.741, ("mixed", 2): 0.797}
 
 
 def parse():
